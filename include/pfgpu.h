@@ -1,0 +1,249 @@
+/*
+ * pfgpu.h -- C ABI of the GB300 (sm_103a) per-cell geochemistry engine.
+ *
+ * The engine replaces PFLOTRAN's per-cell reaction loops:
+ *   - the operator-split cell loop that calls RStep/RReact once per cell
+ *     (src/pflotran/pmc_subsurface_osrt.F90:346-378,
+ *      src/pflotran/reaction.F90:3564-4055), and
+ *   - the per-cell accumulation/reaction blocks and 7-point flux blocks that
+ *     RTResidual/RTJacobian assemble in global-implicit mode
+ *     (src/pflotran/reactive_transport.F90:1964-3349).
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, int32 status codes.  No library
+ *     ever aborts or prints; every entry point returns a PfStatus.
+ *   - Species/component ids are 0-based (Fortran ids minus one).
+ *   - Per-cell arrays are structure-of-arrays, component-major:
+ *       value(k, cell) = array[k * ncells + cell]
+ *     so that a warp reading component k of 32 consecutive cells issues one
+ *     coalesced 256-byte transaction.  The Fortran shim packs the AoS
+ *     rt_auxvar/global_auxvar/material_auxvar types into this layout.
+ *   - Device entry points take device pointers and a cudaStream_t passed as
+ *     void*; host entry points (suffix _host) take host pointers and do the
+ *     copies themselves.
+ *   - All arithmetic is IEEE FP64.
+ */
+#ifndef PFGPU_H_
+#define PFGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef enum PfStatus {
+  PF_OK = 0,
+  PF_CELL_FAILURES = 1,      /* call succeeded; some cells report status != 0 */
+  PF_ERR_INVALID = -1,       /* bad argument (null pointer, size, id range)   */
+  PF_ERR_UNSUPPORTED = -2,   /* network feature this engine does not handle  */
+  PF_ERR_CUDA = -3,          /* a CUDA runtime call failed                    */
+  PF_ERR_TOO_LARGE = -4,     /* ncomp/nsec/nmnrl above the compiled maxima     */
+  PF_ERR_TIMEOUT = -5        /* a bounded device wait ran out                  */
+} PfStatus;
+
+/* per-cell status codes written to PfCellState.status */
+enum {
+  PF_CELL_OK = 0,
+  PF_CELL_TOO_MANY_CUTS = 1, /* RStep: num_cuts > maximum_reaction_cuts      */
+  PF_CELL_NAN = 2            /* non-finite residual or activity coefficient  */
+};
+
+/* reaction%act_coef_update_frequency, src/pflotran/reaction_aux.F90:392 */
+enum { PF_ACT_COEF_OFF = 0, PF_ACT_COEF_TIMESTEP = 1, PF_ACT_COEF_NEWTON_ITER = 2 };
+/* reaction%act_coef_update_algorithm, src/pflotran/reaction_aux.F90:393 */
+enum { PF_ACT_COEF_ALGO_LAG = 0, PF_ACT_COEF_ALGO_NEWTON = 1 };
+
+/* Kernel forms for pf_rstep. */
+enum {
+  PF_KERNEL_PLAIN = 0,   /* one thread per cell, direct form, no queue       */
+  PF_KERNEL_BATCHED = 1  /* persistent, lane-refilling work queue, ncomp-
+                            specialised, tables staged in shared memory      */
+};
+
+/* Compiled maxima (per network). */
+#define PF_MAX_NCOMP 24
+#define PF_MAX_NSEC 96
+#define PF_MAX_NMNRL 16
+#define PF_MAX_SPEC_PER_RXN 24
+
+/*
+ * Solver options: the CHEMISTRY-block fields of reaction_rt_type with the
+ * defaults of ReactionCreate (src/pflotran/reaction_aux.F90:371-556).
+ */
+typedef struct PfOptions {
+  int32_t use_log_formulation;          /* reaction_base.F90:33 (deck: LOG_FORMULATION) */
+  int32_t act_coef_update_frequency;    /* PF_ACT_COEF_*                       */
+  int32_t act_coef_update_algorithm;    /* PF_ACT_COEF_ALGO_*                  */
+  int32_t maximum_reaction_cuts;        /* 10                                  */
+  int32_t maximum_reaction_iterations;  /* 20                                  */
+  int32_t use_total_as_guess;           /* 0                                   */
+  int32_t isothermal;                   /* 1: logK fixed; 0: logK(T) per cell  */
+  int32_t fork_literal_rsolve;          /* 1: RSolve skips back-substitution as
+                                           reaction.F90:5501-5504 does when
+                                           solve_error is passed (update = 0).
+                                           Documentation aid; default 0.      */
+  double max_dlnC_rreact;               /* 5                                   */
+  double max_relative_change_tolerance; /* 1e-6                                */
+  double max_residual_tolerance;        /* 1e-12                               */
+  double max_rel_residual_tolerance;    /* 1e-8                                */
+} PfOptions;
+
+/*
+ * Flattened reaction network (reaction_rt_type, reaction_aux.F90:123-311,
+ * and mineral_type, reaction_mineral_aux.F90:82-138).
+ *
+ * Secondary (aqueous complex) i:
+ *   sec_nspec[i]                     = eqcplxspecid(0,i)
+ *   sec_spec[i*sec_stride + s]       = eqcplxspecid(s+1,i) - 1
+ *   sec_stoich[i*sec_stride + s]     = eqcplxstoich(s+1,i)
+ * Kinetic mineral m: same scheme with mnrl_* and mnrl_stride
+ *   (kinmnrlspecid / kinmnrlstoich).
+ * logK coefficient fits: 5 per reaction (ReactionInterpolateLogK,
+ * reaction_aux.F90:1285-1312); may be NULL when isothermal.
+ * Optional TST arrays (min_scale_factor, Temkin_const, affinity_power) are
+ * NULL when the reference leaves them unassociated
+ * (reaction_database.F90:2039-2092); the rate formulas differ by branch.
+ */
+typedef struct PfNetworkDesc {
+  int32_t ncomp;   /* naqcomp (no immobile species)          */
+  int32_t nsec;    /* neqcplx                                 */
+  int32_t nmnrl;   /* mineral%nkinmnrl                        */
+  int32_t sec_stride;
+  int32_t mnrl_stride;
+  int32_t h_ion_id;                   /* 0-based id of H+, -1 if none (pH output) */
+  const int32_t* sec_nspec;           /* [nsec]                */
+  const int32_t* sec_spec;            /* [nsec*sec_stride]     */
+  const double* sec_stoich;           /* [nsec*sec_stride]     */
+  const double* sec_logK;             /* [nsec] at the reference temperature */
+  const double* sec_logKcoef;         /* [nsec*5] or NULL      */
+  const double* pri_Z;                /* [ncomp] primary_spec_Z  */
+  const double* pri_a0;               /* [ncomp] primary_spec_a0 */
+  const double* sec_Z;                /* [nsec]  eqcplx_Z        */
+  const double* sec_a0;               /* [nsec]  eqcplx_a0       */
+  const int32_t* mnrl_nspec;          /* [nmnrl]               */
+  const int32_t* mnrl_spec;           /* [nmnrl*mnrl_stride]   */
+  const double* mnrl_stoich;          /* [nmnrl*mnrl_stride]   */
+  const double* mnrl_logK;            /* [nmnrl]               */
+  const double* mnrl_logKcoef;        /* [nmnrl*5] or NULL     */
+  const double* mnrl_rate_constant;   /* [nmnrl] mol/m^2/s     */
+  const double* mnrl_activation_energy; /* [nmnrl] J/mol (0 = none) */
+  const double* mnrl_molar_vol;       /* [nmnrl] m^3/mol       */
+  const double* mnrl_affinity_threshold; /* [nmnrl]            */
+  const double* mnrl_rate_limiter;    /* [nmnrl]               */
+  const int32_t* mnrl_irreversible;   /* [nmnrl]               */
+  const double* mnrl_min_scale_factor; /* [nmnrl] or NULL      */
+  const double* mnrl_Temkin_const;    /* [nmnrl] or NULL       */
+  const double* mnrl_affinity_power;  /* [nmnrl] or NULL       */
+  double debyeA, debyeB, debyeBdot;   /* reaction_database.F90:931-1022 */
+  PfOptions opts;
+} PfNetworkDesc;
+
+/*
+ * Per-cell state, structure-of-arrays (value(k,cell) = a[k*ncells+cell]).
+ * Mirrors rt_auxvar (reactive_transport_aux.F90:21-74), global_auxvar
+ * (global_aux.F90:11-35) and material_auxvar (material_aux.F90:53-77).
+ */
+typedef struct PfCellState {
+  int64_t ncells;
+  double* total;          /* [ncomp]  total(:,1), mol/L; in: transported total */
+  double* pri_molal;      /* [ncomp]  in: guess (free ion); out: solution     */
+  double* pri_act_coef;   /* [ncomp]                                           */
+  double* sec_act_coef;   /* [nsec]                                            */
+  double* sec_molal;      /* [nsec]                                            */
+  double* mnrl_volfrac;   /* [nmnrl]                                           */
+  double* mnrl_area;      /* [nmnrl]  m^2/m^3 bulk                             */
+  double* mnrl_rate;      /* [nmnrl]  out: mol/m^3/s                           */
+  const double* porosity; /* [1]                                               */
+  const double* saturation;
+  const double* den_kg;   /* kg/m^3                                            */
+  const double* volume;   /* m^3                                               */
+  const double* temperature; /* C (used when !isothermal)                      */
+  const double* dt_cell;  /* [1] per-cell operator-split dt, or NULL = uniform  */
+  int32_t* status;        /* [1] out: PF_CELL_*                                */
+  int32_t* newton_its;    /* [1] out: Newton iterations summed over substeps   */
+  int32_t* num_substeps;  /* [1] out                                           */
+} PfCellState;
+
+typedef struct PfStepStats {
+  int64_t cells;
+  int64_t failed_cells;
+  int64_t newton_iterations;   /* sum over cells */
+  int32_t max_newton_iterations;
+  int32_t max_substeps;
+} PfStepStats;
+
+typedef struct PfNetwork PfNetwork;   /* opaque: device-resident tables */
+
+/* ---------------------------------------------------------------- network */
+/* Validates and uploads the network tables to the current CUDA device.
+ * Replaces the setup-time flattening in BasisInit
+ * (reaction_database.F90:812-2367) as seen by the cell loop. */
+int32_t pf_network_create(const PfNetworkDesc* desc, PfNetwork** out);
+int32_t pf_network_destroy(PfNetwork* net);
+/* Copy of the descriptor's options; lets a caller change tolerances without
+ * re-uploading tables (e.g. the tight mode of the parity tests). */
+int32_t pf_network_set_options(PfNetwork* net, const PfOptions* opts);
+
+/* ------------------------------------------------------------ operator split */
+/*
+ * pf_rstep -- one operator-split reaction step for every cell.
+ * Replaces the loop body at src/pflotran/pmc_subsurface_osrt.F90:349-378,
+ * i.e. for each cell: guess = pri_molal; RStep(guess, rt_auxvar, ...)
+ * (src/pflotran/reaction.F90:3564-3738, RReact :3742-4055).
+ * dt: option%tran_dt [s] (ignored for cells when state->dt_cell != NULL).
+ * kernel: PF_KERNEL_PLAIN or PF_KERNEL_BATCHED.
+ * stats: optional (NULL); when given the call synchronises the stream and
+ * reduces the per-cell counters (the MPI_Allreduce of rstep_error at
+ * pmc_subsurface_osrt.F90:381 becomes this device reduction).
+ * Returns PF_OK, PF_CELL_FAILURES (stats->failed_cells > 0) or PF_ERR_*.
+ */
+int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt,
+                 int32_t kernel, void* stream, PfStepStats* stats);
+
+/*
+ * pf_update_auxvars -- RTUpdateAuxVars for cells
+ * (src/pflotran/reactive_transport.F90:3525-3660): optionally
+ * RActivityCoefficients (reaction.F90:4368-4614), then RTotal
+ * (reaction.F90:4618-4759) from pri_molal; writes total and sec_molal.
+ */
+int32_t pf_update_auxvars(PfNetwork* net, const PfCellState* state,
+                          int32_t update_activity_coefs, void* stream);
+
+/*
+ * pf_update_activity_coefs -- RTUpdateActivityCoefficients for cells
+ * (src/pflotran/reactive_transport.F90:3441-3521): activity coefficients
+ * only, totals untouched (the TIMESTEP update of pm_osrt.F90:145-151).
+ */
+int32_t pf_update_activity_coefs(PfNetwork* net, const PfCellState* state,
+                                 void* stream);
+
+/*
+ * pf_rstep_host -- the same step through host buffers: copies the state to
+ * the device, runs pf_rstep (kernel form as given), copies results back.
+ * Host arrays use the same SoA layout.  This is the entry point a Fortran
+ * caller binds through iso_c_binding (contiguous temporaries via c_loc).
+ */
+int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
+                      double dt, int32_t kernel, PfStepStats* stats);
+
+/* ------------------------------------------------------------ capabilities */
+/* Kernel launch configuration for the batched form; chosen by the
+ * autotuner (pfgpu.autotune) and settable per network. */
+typedef struct PfLaunchConfig {
+  int32_t threads_per_block;  /* multiple of 32                        */
+  int32_t blocks_per_sm;      /* persistent grid = SMs * blocks_per_sm */
+  int32_t jac_in_shared;      /* 1: Jacobian in shared memory, 0: local */
+  int32_t reserved;
+} PfLaunchConfig;
+int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg);
+int32_t pf_network_get_launch(const PfNetwork* net, PfLaunchConfig* cfg);
+
+/* Library version / build info string (static storage). */
+const char* pf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFGPU_H_ */

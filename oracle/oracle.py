@@ -1,0 +1,100 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module; the product path never imports it.  The C++ restatement it
+wraps is oracle/rxn_oracle.hpp (see the file header for the reference
+routines it follows).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+_REPO = os.path.dirname(HERE)
+_PKG = os.path.join(_REPO, "pflotran-elm-interface_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+
+from pfgpu import abi  # noqa: E402  (struct layouts shared with the product)
+
+CON_TOTAL, CON_FREE, CON_PH, CON_CHARGE_BAL, CON_LOG = 1, 2, 3, 4, 5
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "rxn_oracle.hpp")]
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+class Oracle:
+    def __init__(self):
+        build()
+        lib = C.CDLL(LIB)
+        S, D = C.POINTER(abi.PfCellState), C.POINTER(abi.PfNetworkDesc)
+        lib.oracle_rstep.argtypes = [D, S, C.c_double, C.c_int]
+        lib.oracle_rreact.argtypes = [D, S, C.c_double, C.c_int]
+        lib.oracle_update_kinetic_state.argtypes = [D, S, C.c_double]
+        lib.oracle_implicit_step.argtypes = [D, S, C.c_double, C.c_double, C.c_int]
+        lib.oracle_update_auxvars.argtypes = [D, S, C.c_int, C.c_int]
+        lib.oracle_update_activity_coefs.argtypes = [D, S, C.c_int]
+        lib.oracle_equilibrate.argtypes = [D, S, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                           C.c_int, C.POINTER(C.c_int32), C.c_int]
+        lib.oracle_ifc67_density.argtypes = [C.c_double, C.c_double]
+        lib.oracle_ifc67_density.restype = C.c_double
+        for f in ("oracle_rstep", "oracle_rreact", "oracle_implicit_step", "oracle_update_kinetic_state",
+                  "oracle_update_auxvars", "oracle_update_activity_coefs", "oracle_equilibrate"):
+            getattr(lib, f).restype = C.c_int
+        self.lib = lib
+
+    @staticmethod
+    def _args(net, state):
+        d = net.desc()
+        s = state.struct()
+        return d, s
+
+    def rstep(self, net, state, dt, nthreads=1):
+        d, s = self._args(net, state)
+        return self.lib.oracle_rstep(C.byref(d), C.byref(s), dt, nthreads)
+
+    def rreact(self, net, state, dt, nthreads=1):
+        d, s = self._args(net, state)
+        return self.lib.oracle_rreact(C.byref(d), C.byref(s), dt, nthreads)
+
+    def implicit_step(self, net, state, dt, rel_tol=1e-10, max_its=100):
+        d, s = self._args(net, state)
+        return self.lib.oracle_implicit_step(C.byref(d), C.byref(s), dt, rel_tol, max_its)
+
+    def update_kinetic_state(self, net, state, dt):
+        d, s = self._args(net, state)
+        return self.lib.oracle_update_kinetic_state(C.byref(d), C.byref(s), dt)
+
+    def update_auxvars(self, net, state, update_act=False, nthreads=1):
+        d, s = self._args(net, state)
+        return self.lib.oracle_update_auxvars(C.byref(d), C.byref(s), int(update_act), nthreads)
+
+    def update_activity_coefs(self, net, state, nthreads=1):
+        d, s = self._args(net, state)
+        return self.lib.oracle_update_activity_coefs(C.byref(d), C.byref(s), nthreads)
+
+    def equilibrate(self, net, state, ctype, cconc, use_prev=False, nthreads=1):
+        d, s = self._args(net, state)
+        ct = np.ascontiguousarray(ctype, np.int32)
+        cc = np.ascontiguousarray(cconc, np.float64)
+        its = np.zeros(state.ncells, np.int32)
+        rc = self.lib.oracle_equilibrate(C.byref(d), C.byref(s),
+                                         ct.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         cc.ctypes.data_as(C.POINTER(C.c_double)),
+                                         int(use_prev), its.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         nthreads)
+        return rc, its
+
+    def density(self, t, p):
+        return self.lib.oracle_ifc67_density(t, p)

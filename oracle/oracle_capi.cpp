@@ -1,0 +1,234 @@
+// oracle_capi.cpp -- C entry points of the CPU oracle (TEST INFRASTRUCTURE).
+//
+// Wraps the restatement in rxn_oracle.hpp for ctypes: each entry point takes
+// the same PfNetworkDesc / PfCellState (host pointers, SoA layout
+// value(k,cell) = a[k*ncells+cell]) as the GPU library, loops over cells
+// (OpenMP when nthreads > 1) and writes results back in place.
+#include "rxn_oracle.hpp"
+
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace oracle;
+
+namespace {
+
+inline void gather(const Net& net, const PfCellState* s, int64_t i, Cell& c) {
+  const int64_t N = s->ncells;
+  for (int k = 0; k < net.n; ++k) {
+    c.total[k] = s->total[k * N + i];
+    c.pri_molal[k] = s->pri_molal[k * N + i];
+    c.pri_act_coef[k] = s->pri_act_coef[k * N + i];
+  }
+  for (int k = 0; k < net.ns; ++k) {
+    c.sec_act_coef[k] = s->sec_act_coef[k * N + i];
+    c.sec_molal[k] = s->sec_molal[k * N + i];
+  }
+  for (int k = 0; k < net.nm; ++k) {
+    c.mnrl_volfrac[k] = s->mnrl_volfrac[k * N + i];
+    c.mnrl_area[k] = s->mnrl_area[k * N + i];
+    c.mnrl_rate[k] = s->mnrl_rate[k * N + i];
+  }
+  c.porosity = s->porosity[i];
+  c.sat = s->saturation[i];
+  c.den_kg = s->den_kg[i];
+  c.volume = s->volume[i];
+  c.temp = s->temperature ? s->temperature[i] : 25.0;
+  c.ln_act_h2o = 0.0;
+  c.ierror = 0;
+  set_logK(net, c);
+}
+
+inline void scatter(const Net& net, const PfCellState* s, int64_t i, const Cell& c) {
+  const int64_t N = s->ncells;
+  for (int k = 0; k < net.n; ++k) {
+    s->total[k * N + i] = c.total[k];
+    s->pri_molal[k * N + i] = c.pri_molal[k];
+    s->pri_act_coef[k * N + i] = c.pri_act_coef[k];
+  }
+  for (int k = 0; k < net.ns; ++k) {
+    s->sec_act_coef[k * N + i] = c.sec_act_coef[k];
+    s->sec_molal[k * N + i] = c.sec_molal[k];
+  }
+  for (int k = 0; k < net.nm; ++k) {
+    s->mnrl_volfrac[k * N + i] = c.mnrl_volfrac[k];
+    s->mnrl_area[k * N + i] = c.mnrl_area[k];
+    s->mnrl_rate[k * N + i] = c.mnrl_rate[k];
+  }
+}
+
+int check(const PfNetworkDesc* d, const PfCellState* s) {
+  if (!d || !s) return PF_ERR_INVALID;
+  if (d->ncomp < 1 || d->ncomp > MAXN || d->nsec < 0 || d->nsec > MAXS || d->nmnrl < 0 ||
+      d->nmnrl > MAXM)
+    return PF_ERR_TOO_LARGE;
+  return PF_OK;
+}
+
+template <class F>
+void for_cells(int64_t n, int nthreads, F&& f) {
+#ifdef _OPENMP
+  if (nthreads > 1) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+#endif
+  (void)nthreads;
+  for (int64_t i = 0; i < n; ++i) f(i);
+}
+
+}  // namespace
+
+extern "C" {
+
+// RStep for every cell (the pmc_subsurface_osrt.F90:349-378 loop body).
+int oracle_rstep(const PfNetworkDesc* d, const PfCellState* s, double dt, int nthreads) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  int64_t failed = 0;
+  for_cells(s->ncells, nthreads, [&](int64_t i) {
+    Cell c;
+    gather(net, s, i, c);
+    double guess[MAXN];
+    for (int k = 0; k < net.n; ++k) guess[k] = c.pri_molal[k];
+    double dti = s->dt_cell ? s->dt_cell[i] : dt;
+    StepResult r = rstep(net, c, guess, dti);
+    scatter(net, s, i, c);
+    if (s->status) s->status[i] = r.ierror ? PF_CELL_TOO_MANY_CUTS : PF_CELL_OK;
+    if (s->newton_its) s->newton_its[i] = r.num_iterations;
+    if (s->num_substeps) s->num_substeps[i] = r.num_sub_steps;
+    if (r.ierror) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+      failed++;
+    }
+  });
+  return failed ? PF_CELL_FAILURES : PF_OK;
+}
+
+// RReact alone (no flooring, no sub-stepping): one implicit step solved from
+// guess = pri_molal.  Used to emulate a converged single-cell implicit step.
+int oracle_rreact(const PfNetworkDesc* d, const PfCellState* s, double dt, int nthreads) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  int64_t failed = 0;
+  for_cells(s->ncells, nthreads, [&](int64_t i) {
+    Cell c;
+    gather(net, s, i, c);
+    double guess[MAXN];
+    for (int k = 0; k < net.n; ++k) guess[k] = c.pri_molal[k];
+    int its = 0;
+    int ierr = rreact(net, c, guess, dt, &its);
+    scatter(net, s, i, c);
+    if (s->status) s->status[i] = ierr;
+    if (s->newton_its) s->newton_its[i] = its;
+    if (ierr) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+      failed++;
+    }
+  });
+  return failed ? PF_CELL_FAILURES : PF_OK;
+}
+
+// implicit_step for every cell (the converged single-cell GIRT step).
+int oracle_implicit_step(const PfNetworkDesc* d, const PfCellState* s, double dt, double rel_tol,
+                         int max_its) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  int failed = 0;
+  for (int64_t i = 0; i < s->ncells; ++i) {
+    Cell c;
+    gather(net, s, i, c);
+    int its = 0;
+    int ierr = implicit_step(net, c, dt, rel_tol, max_its, &its);
+    scatter(net, s, i, c);
+    if (s->status) s->status[i] = ierr;
+    if (s->newton_its) s->newton_its[i] = its;
+    failed += ierr;
+  }
+  return failed ? PF_CELL_FAILURES : PF_OK;
+}
+
+int oracle_update_kinetic_state(const PfNetworkDesc* d, const PfCellState* s, double dt) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  for (int64_t i = 0; i < s->ncells; ++i) {
+    Cell c;
+    gather(net, s, i, c);
+    update_kinetic_state(net, c, dt);
+    scatter(net, s, i, c);
+  }
+  return PF_OK;
+}
+
+// RTUpdateAuxVars for cells (reactive_transport.F90:3625-3660).
+int oracle_update_auxvars(const PfNetworkDesc* d, const PfCellState* s, int update_act, int nthreads) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  for_cells(s->ncells, nthreads, [&](int64_t i) {
+    Cell c;
+    gather(net, s, i, c);
+    if (update_act) activity_coefficients(net, c);
+    total_aqueous(net, c);
+    scatter(net, s, i, c);
+  });
+  return PF_OK;
+}
+
+// RTUpdateActivityCoefficients for cells (reactive_transport.F90:3441-3521).
+int oracle_update_activity_coefs(const PfNetworkDesc* d, const PfCellState* s, int nthreads) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  for_cells(s->ncells, nthreads, [&](int64_t i) {
+    Cell c;
+    gather(net, s, i, c);
+    activity_coefficients(net, c);
+    scatter(net, s, i, c);
+  });
+  return PF_OK;
+}
+
+// ReactionEquilibrateConstraint subset for every cell; ctype[ncomp] shared,
+// cconc[k*ncells+i] per cell.  iterations[i] = count or -1 on failure.
+int oracle_equilibrate(const PfNetworkDesc* d, const PfCellState* s, const int32_t* ctype,
+                       const double* cconc, int use_prev_soln_as_guess, int32_t* iterations,
+                       int nthreads) {
+  int rc = check(d, s);
+  if (rc) return rc;
+  Net net(d);
+  int64_t failed = 0;
+  const int64_t N = s->ncells;
+  for_cells(N, nthreads, [&](int64_t i) {
+    Cell c;
+    gather(net, s, i, c);
+    int ct[MAXN];
+    double cc[MAXN];
+    for (int k = 0; k < net.n; ++k) { ct[k] = ctype[k]; cc[k] = cconc[k * N + i]; }
+    int its = equilibrate_constraint(net, c, ct, cc, use_prev_soln_as_guess != 0);
+    scatter(net, s, i, c);
+    if (iterations) iterations[i] = its;
+    if (its < 0) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+      failed++;
+    }
+  });
+  return failed ? PF_CELL_FAILURES : PF_OK;
+}
+
+double oracle_ifc67_density(double t, double p) { return ifc67_density(t, p); }
+
+}  // extern "C"

@@ -1,0 +1,844 @@
+// rxn_oracle.hpp -- CPU restatement of PFLOTRAN's per-cell geochemistry.
+//
+// TEST INFRASTRUCTURE ONLY.  This is the oracle the GPU engine is checked
+// against; nothing in the product links or calls it.  Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+//
+// Every routine restates one reference subroutine, in the same loop order and
+// with the same left-to-right evaluation of each Fortran expression, so that
+// rounding follows the reference as closely as a C++ compiler allows
+// (built with -ffp-contract=off: no FMA contraction on either host).
+// File:line citations are to src/pflotran/ of fmyuan/pflotran-elm-interface.
+//
+// Pinning: the restatement is checked against the reference's own regression
+// gold files (regression_tests/ascem/batch/*.regression.gold, tolerances from
+// batch.cfg:20-27) and the pFUnit pin of the water density
+// (src/pflotran/unittests/test_eos_water.pf:146-157); see tests/test_oracle_kat.py.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <algorithm>
+
+#include "../include/pfgpu.h"
+
+namespace oracle {
+
+// pflotran_constants.F90:84 (truncated, not ln 10) and :89
+constexpr double LOG_TO_LN = 2.30258509299;
+constexpr double IDEAL_GAS_CONSTANT = 8.31446;
+// reactive_transport_aux.F90:19
+constexpr double rt_min_saturation = 1.0e-40;
+// pflotran_constants.F90:76,80
+constexpr double H2O_CRITICAL_TEMPERATURE = 647.3;
+constexpr double H2O_CRITICAL_PRESSURE = 22.064e6;
+
+constexpr int MAXN = PF_MAX_NCOMP;
+constexpr int MAXS = PF_MAX_NSEC;
+constexpr int MAXM = PF_MAX_NMNRL;
+
+// Fortran SIGN(1.d0, x): +1 for x >= +0, -1 for x < 0 (and for -0.0).
+inline double fsign1(double x) { return std::signbit(x) ? -1.0 : 1.0; }
+
+// Per-cell working copy of rt_auxvar + global_auxvar + material_auxvar
+// (reactive_transport_aux.F90:21-74, global_aux.F90:11-35,
+//  material_aux.F90:53-77), plus the per-cell logK the reference keeps in the
+// shared reaction object (reaction.F90:5976-6069 mutates it per cell).
+struct Cell {
+  double pri_molal[MAXN];
+  double total[MAXN];
+  double dtotal[MAXN * MAXN];  // dtotal(i,j) = dtotal[i*MAXN + j]
+  double pri_act_coef[MAXN];
+  double sec_act_coef[MAXS];
+  double sec_molal[MAXS];
+  double mnrl_volfrac[MAXM];
+  double mnrl_area[MAXM];
+  double mnrl_rate[MAXM];
+  double porosity, sat, den_kg, volume, temp;
+  double ln_act_h2o;
+  double sec_logK[MAXS];
+  double mnrl_logK[MAXM];
+  int ierror;  // option%ierror side channel (activity-coefficient failure)
+};
+
+struct Net {
+  const PfNetworkDesc* d;
+  PfOptions o;
+  int n, ns, nm;
+  int sid(int i, int s) const { return d->sec_spec[i * d->sec_stride + s]; }
+  double sst(int i, int s) const { return d->sec_stoich[i * d->sec_stride + s]; }
+  int mid(int m, int s) const { return d->mnrl_spec[m * d->mnrl_stride + s]; }
+  double mst(int m, int s) const { return d->mnrl_stoich[m * d->mnrl_stride + s]; }
+  explicit Net(const PfNetworkDesc* desc) : d(desc), o(desc->opts), n(desc->ncomp),
+      ns(desc->nsec), nm(desc->nmnrl) {}
+};
+
+// ReactionInterpolateLogK, reaction_aux.F90:1285-1312
+inline void interpolate_logK(const double* coefs, double* logKs, double temp, int n) {
+  double temp_kelvin = temp + 273.15;
+  for (int i = 0; i < n; ++i) {
+    const double* c = coefs + 5 * i;
+    logKs[i] = c[0] * std::log(temp_kelvin) + c[1] + c[2] * temp_kelvin +
+               c[3] / temp_kelvin + c[4] / (temp_kelvin * temp_kelvin);
+  }
+}
+
+// Per-cell logK: isothermal -> the network's reference-temperature values;
+// otherwise RUpdateTempDependentCoefs (reaction.F90:5976-6069) and
+// MineralUpdateTempDepCoefs (reaction_mineral.F90:1306-1357).
+inline void set_logK(const Net& net, Cell& c) {
+  if (net.o.isothermal || !net.d->sec_logKcoef) {
+    for (int i = 0; i < net.ns; ++i) c.sec_logK[i] = net.d->sec_logK[i];
+  } else {
+    interpolate_logK(net.d->sec_logKcoef, c.sec_logK, c.temp, net.ns);
+  }
+  if (net.o.isothermal || !net.d->mnrl_logKcoef) {
+    for (int m = 0; m < net.nm; ++m) c.mnrl_logK[m] = net.d->mnrl_logK[m];
+  } else {
+    interpolate_logK(net.d->mnrl_logKcoef, c.mnrl_logK, c.temp, net.nm);
+  }
+}
+
+// RActivityCoefficients, reaction.F90:4368-4614 (use_activity_h2o = false)
+inline void activity_coefficients(const Net& net, Cell& c) {
+  const PfNetworkDesc* d = net.d;
+  const double A = d->debyeA, B = d->debyeB, Bdot = d->debyeBdot;
+  if (net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON) {
+    // reaction.F90:4403-4551
+    double ln_conc[MAXN], ln_act[MAXN];
+    for (int j = 0; j < net.n; ++j) {
+      ln_conc[j] = std::log(c.pri_molal[j]);
+      ln_act[j] = ln_conc[j] + std::log(c.pri_act_coef[j]);
+    }
+    double fpri = 0.0;
+    for (int j = 0; j < net.n; ++j)
+      fpri = fpri + c.pri_molal[j] * d->pri_Z[j] * d->pri_Z[j];
+    int it = 0;
+    double II = 0.0, I, f, sqrt_I, den = 0.0;
+    for (;;) {
+      it = it + 1;
+      if (it > 50) {
+        for (int j = 0; j < net.n; ++j) { c.pri_molal[j] = NAN; c.pri_act_coef[j] = NAN; }
+        for (int i = 0; i < net.ns; ++i) c.sec_act_coef[i] = NAN;
+        c.ierror = 1;
+        return;  // the reference keeps looping on NaN until |I-II| test fails; bounded here
+      }
+      I = fpri;
+      for (int i = 0; i < net.ns; ++i)
+        I = I + c.sec_molal[i] * d->sec_Z[i] * d->sec_Z[i];
+      I = 0.5 * I;
+      f = I;
+      if (std::fabs(I - II) < 1.0e-6 * I) break;
+      if (net.ns > 0) {
+        double didi = 0.0;
+        sqrt_I = std::sqrt(I);
+        for (int i = 0; i < net.ns; ++i) {
+          if (std::fabs(d->sec_Z[i]) > 0.0) {
+            double t = 1.0 + B * d->sec_a0[i] * sqrt_I;
+            double sum = 0.5 * A * d->sec_Z[i] * d->sec_Z[i] / (sqrt_I * (t * t)) - Bdot;
+            int nsp = d->sec_nspec[i];
+            for (int s = 0; s < nsp; ++s) {
+              int j = net.sid(i, s);
+              if (std::fabs(d->pri_Z[j]) > 0.0) {
+                double tj = 1.0 + B * d->pri_a0[j] * sqrt_I;
+                double dgamdi = -0.5 * A * (d->pri_Z[j] * d->pri_Z[j]) / (sqrt_I * (tj * tj)) + Bdot;
+                sum = sum + net.sst(i, s) * dgamdi;
+              }
+            }
+            double dcdi = c.sec_molal[i] * LOG_TO_LN * sum;
+            didi = didi + 0.5 * d->sec_Z[i] * d->sec_Z[i] * dcdi;
+          }
+        }
+        den = 1.0 - didi;
+        if (std::fabs(den) > 0.0) II = (f - I * didi) / den;
+        else II = f;
+      } else {
+        II = f;
+      }
+      if (II < 0.0) {
+        for (int j = 0; j < net.n; ++j) { c.pri_molal[j] = NAN; c.pri_act_coef[j] = NAN; }
+        for (int i = 0; i < net.ns; ++i) c.sec_act_coef[i] = NAN;
+        c.ierror = 1;
+        return;
+      }
+      I = II;
+      sqrt_I = std::sqrt(I);
+      for (int j = 0; j < net.n; ++j) {
+        if (std::fabs(d->pri_Z[j]) > 0.0) {
+          c.pri_act_coef[j] = std::exp((-d->pri_Z[j] * d->pri_Z[j] * sqrt_I * A /
+                                        (1.0 + d->pri_a0[j] * B * sqrt_I) + Bdot * I) * LOG_TO_LN);
+        } else {
+          c.pri_act_coef[j] = 1.0;
+        }
+      }
+      for (int i = 0; i < net.ns; ++i) {
+        if (std::fabs(d->sec_Z[i]) > 0.0) {
+          c.sec_act_coef[i] = std::exp((-d->sec_Z[i] * d->sec_Z[i] * sqrt_I * A /
+                                        (1.0 + d->sec_a0[i] * B * sqrt_I) + Bdot * I) * LOG_TO_LN);
+        } else {
+          c.sec_act_coef[i] = 1.0;
+        }
+        double lnQK = -c.sec_logK[i] * LOG_TO_LN;
+        int nsp = d->sec_nspec[i];
+        for (int s = 0; s < nsp; ++s) lnQK = lnQK + net.sst(i, s) * ln_act[net.sid(i, s)];
+        c.sec_molal[i] = std::exp(lnQK) / c.sec_act_coef[i];
+      }
+    }
+    return;
+  }
+  // LAG algorithm, reaction.F90:4553-4612
+  double I = 0.0;
+  for (int j = 0; j < net.n; ++j) I = I + c.pri_molal[j] * d->pri_Z[j] * d->pri_Z[j];
+  for (int i = 0; i < net.ns; ++i) I = I + c.sec_molal[i] * d->sec_Z[i] * d->sec_Z[i];
+  I = 0.5 * I;
+  double sqrt_I = std::sqrt(I);
+  for (int j = 0; j < net.n; ++j) {
+    if (std::fabs(d->pri_Z[j]) > 1.0e-10) {
+      c.pri_act_coef[j] = std::exp((-d->pri_Z[j] * d->pri_Z[j] * sqrt_I * A /
+                                    (1.0 + d->pri_a0[j] * B * sqrt_I) + Bdot * I) * LOG_TO_LN);
+    } else {
+      c.pri_act_coef[j] = 1.0;
+    }
+  }
+  for (int i = 0; i < net.ns; ++i) {
+    if (std::fabs(d->sec_Z[i]) > 1.0e-10) {
+      c.sec_act_coef[i] = std::exp((-d->sec_Z[i] * d->sec_Z[i] * sqrt_I * A /
+                                    (1.0 + d->sec_a0[i] * B * sqrt_I) + Bdot * I) * LOG_TO_LN);
+    } else {
+      c.sec_act_coef[i] = 1.0;
+    }
+  }
+}
+
+// RTotalAqueous, reaction.F90:4665-4759 (RTotal :4618 -> aqueous only).
+inline void total_aqueous(const Net& net, Cell& c) {
+  const PfNetworkDesc* d = net.d;
+  const int n = net.n;
+  double xmass = 1.0;
+  double den_kg_per_L = c.den_kg * xmass * 1.0e-3;
+  double ln_conc[MAXN], ln_act[MAXN];
+  for (int j = 0; j < n; ++j) {
+    ln_conc[j] = std::log(c.pri_molal[j]);
+    ln_act[j] = ln_conc[j] + std::log(c.pri_act_coef[j]);
+    c.total[j] = c.pri_molal[j];
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) c.dtotal[i * MAXN + j] = (i == j) ? 1.0 : 0.0;
+  for (int i = 0; i < net.ns; ++i) {
+    double lnQK = -c.sec_logK[i] * LOG_TO_LN;
+    int nsp = d->sec_nspec[i];
+    for (int s = 0; s < nsp; ++s) lnQK = lnQK + net.sst(i, s) * ln_act[net.sid(i, s)];
+    c.sec_molal[i] = std::exp(lnQK) / c.sec_act_coef[i];
+    for (int s = 0; s < nsp; ++s) {
+      int k = net.sid(i, s);
+      c.total[k] = c.total[k] + net.sst(i, s) * c.sec_molal[i];
+    }
+    for (int sj = 0; sj < nsp; ++sj) {
+      int jc = net.sid(i, sj);
+      double tempreal = net.sst(i, sj) * std::exp(lnQK - ln_conc[jc]) / c.sec_act_coef[i];
+      for (int si = 0; si < nsp; ++si) {
+        int ic = net.sid(i, si);
+        c.dtotal[ic * MAXN + jc] = c.dtotal[ic * MAXN + jc] + net.sst(i, si) * tempreal;
+      }
+    }
+  }
+  for (int j = 0; j < n; ++j) c.total[j] = c.total[j] * den_kg_per_L;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) c.dtotal[i * MAXN + j] = c.dtotal[i * MAXN + j] * den_kg_per_L;
+}
+
+// RTAccumulation, reaction.F90:5710-5771 (aqueous, single phase)
+inline void accumulation(const Net& net, const Cell& c, double* res) {
+  for (int j = 0; j < net.n; ++j) res[j] = 0.0;
+  if (c.sat < rt_min_saturation) return;
+  double psv_t = c.porosity * c.sat * 1000.0 * c.volume;
+  for (int j = 0; j < net.n; ++j) res[j] = psv_t * c.total[j];
+}
+
+// RTAccumulationDerivative, reaction.F90:5775-5848. J(i,j) = J[i*MAXN+j]
+inline void accumulation_derivative(const Net& net, const Cell& c, double dt, double* J) {
+  const int n = net.n;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) J[i * MAXN + j] = 0.0;
+  if (c.sat < rt_min_saturation) {
+    for (int i = 0; i < n; ++i) J[i * MAXN + i] = 1.0;
+    return;
+  }
+  double psvd_t = c.porosity * c.sat * 1000.0 * c.volume / dt;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) J[i * MAXN + j] = c.dtotal[i * MAXN + j] * psvd_t;
+}
+
+// RKineticMineral, reaction_mineral.F90:647-1078 (no prefactors, no solid
+// solution, no water activity).  J may be null when !compute_derivative.
+inline void kinetic_mineral(const Net& net, Cell& c, double* Res, double* J,
+                            bool compute_derivative) {
+  const PfNetworkDesc* d = net.d;
+  double ln_conc[MAXN], ln_act[MAXN];
+  for (int j = 0; j < net.n; ++j) {
+    ln_conc[j] = std::log(c.pri_molal[j]);
+    ln_act[j] = ln_conc[j] + std::log(c.pri_act_coef[j]);
+  }
+  for (int m = 0; m < net.nm; ++m) c.mnrl_rate[m] = 0.0;
+  for (int m = 0; m < net.nm; ++m) {
+    double lnQK = -c.mnrl_logK[m] * LOG_TO_LN;
+    int nsp = d->mnrl_nspec[m];
+    for (int s = 0; s < nsp; ++s) lnQK = lnQK + net.mst(m, s) * ln_act[net.mid(m, s)];
+    double QK = std::exp(lnQK);
+    double affinity_factor;
+    if (d->mnrl_Temkin_const) {
+      if (d->mnrl_min_scale_factor)
+        affinity_factor = 1.0 - std::pow(QK, 1.0 / (d->mnrl_min_scale_factor[m] * d->mnrl_Temkin_const[m]));
+      else
+        affinity_factor = 1.0 - std::pow(QK, 1.0 / d->mnrl_Temkin_const[m]);
+    } else if (d->mnrl_min_scale_factor) {
+      affinity_factor = 1.0 - std::pow(QK, 1.0 / d->mnrl_min_scale_factor[m]);
+    } else {
+      affinity_factor = 1.0 - QK;
+    }
+    double sign_ = fsign1(affinity_factor);
+    double Im, Im_const, sum_prefactor_rate;
+    if (c.mnrl_volfrac[m] > 0 || sign_ < 0.0) {
+      if (d->mnrl_irreversible[m] == 1 && sign_ < 0.0) continue;
+      if (d->mnrl_affinity_threshold[m] > 0.0) {
+        if (sign_ < 0.0 && QK < d->mnrl_affinity_threshold[m]) continue;
+      }
+      if (d->mnrl_rate_limiter[m] > 0.0) {
+        affinity_factor = affinity_factor / (1.0 + (1.0 - affinity_factor) / d->mnrl_rate_limiter[m]);
+      }
+      double arrhenius_factor = 1.0;
+      if (d->mnrl_activation_energy[m] > 0.0) {
+        arrhenius_factor = std::exp(d->mnrl_activation_energy[m] / IDEAL_GAS_CONSTANT *
+                                    (1.0 / (25.0 + 273.15) - 1.0 / (c.temp + 273.15)));
+      }
+      sum_prefactor_rate = d->mnrl_rate_constant[m] * arrhenius_factor;
+      Im_const = -c.mnrl_area[m];
+      if (d->mnrl_min_scale_factor) Im_const = Im_const / d->mnrl_min_scale_factor[m];
+      if (d->mnrl_affinity_power) {
+        Im = Im_const * sign_ * std::pow(std::fabs(affinity_factor), d->mnrl_affinity_power[m]) *
+             sum_prefactor_rate;
+      } else {
+        Im = Im_const * sign_ * std::fabs(affinity_factor) * sum_prefactor_rate;
+      }
+      c.mnrl_rate[m] = Im;
+    } else {
+      continue;
+    }
+    Im_const = Im_const * c.volume;
+    Im = Im * c.volume;
+    for (int s = 0; s < nsp; ++s) {
+      int k = net.mid(m, s);
+      Res[k] = Res[k] + net.mst(m, s) * Im;
+    }
+    if (!compute_derivative) continue;
+    double dIm_dQK;
+    if (d->mnrl_affinity_power)
+      dIm_dQK = -Im * d->mnrl_affinity_power[m] / std::fabs(affinity_factor);
+    else
+      dIm_dQK = -Im_const * sum_prefactor_rate;
+    if (d->mnrl_Temkin_const) {
+      if (d->mnrl_min_scale_factor)
+        dIm_dQK = dIm_dQK * (1.0 / (d->mnrl_min_scale_factor[m] * d->mnrl_Temkin_const[m])) / QK *
+                  (1.0 - affinity_factor);
+      else
+        dIm_dQK = dIm_dQK * (1.0 / d->mnrl_Temkin_const[m]) / QK * (1.0 - affinity_factor);
+    } else if (d->mnrl_min_scale_factor) {
+      dIm_dQK = dIm_dQK * (1.0 / d->mnrl_min_scale_factor[m]) / QK * (1.0 - affinity_factor);
+    }
+    if (d->mnrl_rate_limiter[m] <= 0.0) {
+      for (int sj = 0; sj < nsp; ++sj) {
+        int jc = net.mid(m, sj);
+        double dQK_dCj = net.mst(m, sj) * QK * std::exp(-ln_conc[jc]);
+        double dQK_dmj = dQK_dCj * c.den_kg * 1.0e-3;
+        for (int si = 0; si < nsp; ++si) {
+          int ic = net.mid(m, si);
+          J[ic * MAXN + jc] = J[ic * MAXN + jc] + net.mst(m, si) * dIm_dQK * dQK_dmj;
+        }
+      }
+    } else {
+      double rl = d->mnrl_rate_limiter[m];
+      double den = 1.0 + (1.0 - affinity_factor) / rl;
+      for (int sj = 0; sj < nsp; ++sj) {
+        int jc = net.mid(m, sj);
+        double dQK_dCj = net.mst(m, sj) * QK * std::exp(-ln_conc[jc]);
+        double dQK_dmj = dQK_dCj * c.den_kg * 1.0e-3;
+        for (int si = 0; si < nsp; ++si) {
+          int ic = net.mid(m, si);
+          J[ic * MAXN + jc] = J[ic * MAXN + jc] +
+                              net.mst(m, si) * dIm_dQK * (1.0 + QK / rl / den) * dQK_dmj / den;
+        }
+      }
+    }
+  }
+}
+
+// RReaction, reaction.F90:4059-4130 (kinetic minerals are the only kind in scope)
+inline void reaction(const Net& net, Cell& c, double* Res, double* J, bool derivative) {
+  if (c.sat < rt_min_saturation) return;
+  if (net.nm > 0) kinetic_mineral(net, c, Res, J, derivative);
+}
+
+// RReactionDerivative, reaction.F90:4134-4240 (analytical branch)
+inline void reaction_derivative(const Net& net, Cell& c, double* Res, double* J) {
+  if (c.sat < rt_min_saturation) return;
+  for (int i = 0; i < net.n; ++i) {
+    Res[i] = 0.0;
+    for (int j = 0; j < net.n; ++j) J[i * MAXN + j] = 0.0;
+  }
+  reaction(net, c, Res, J, true);
+  for (int i = 0; i < net.n; ++i)
+    for (int j = 0; j < net.n; ++j)
+      if (std::fabs(J[i * MAXN + j]) < 1.0e-40) J[i * MAXN + j] = 0.0;
+}
+
+// LUDecomposition1, utility.F90:597-688 (stop_on_error = false). A(i,j) = A[i*MAXN+j]
+inline int lu_decomposition(double* A, int N, int* INDX) {
+  const double tiny = 1.0e-20;
+  double VV[MAXN];
+  for (int i = 0; i < N; ++i) {
+    double aamax = 0.0;
+    for (int j = 0; j < N; ++j)
+      if (std::fabs(A[i * MAXN + j]) > aamax) aamax = std::fabs(A[i * MAXN + j]);
+    if (aamax <= 0.0) return 1;
+    VV[i] = 1.0 / aamax;
+  }
+  for (int j = 0; j < N; ++j) {
+    for (int i = 0; i < j; ++i) {
+      double sum = A[i * MAXN + j];
+      for (int k = 0; k < i; ++k) sum = sum - A[i * MAXN + k] * A[k * MAXN + j];
+      A[i * MAXN + j] = sum;
+    }
+    double aamax = 0.0;
+    int imax = j;  // the reference leaves imax unset if every dum is NaN
+    for (int i = j; i < N; ++i) {
+      double sum = A[i * MAXN + j];
+      for (int k = 0; k < j; ++k) sum = sum - A[i * MAXN + k] * A[k * MAXN + j];
+      A[i * MAXN + j] = sum;
+      double dum = VV[i] * std::fabs(sum);
+      if (dum >= aamax) { imax = i; aamax = dum; }
+    }
+    if (j != imax) {
+      for (int k = 0; k < N; ++k) {
+        double dum = A[imax * MAXN + k];
+        A[imax * MAXN + k] = A[j * MAXN + k];
+        A[j * MAXN + k] = dum;
+      }
+      VV[imax] = VV[j];
+    }
+    INDX[j] = imax;
+    if (A[j * MAXN + j] == 0.0) A[j * MAXN + j] = tiny;
+    if (j != N - 1) {
+      double dum = 1.0 / A[j * MAXN + j];
+      for (int i = j + 1; i < N; ++i) A[i * MAXN + j] = A[i * MAXN + j] * dum;
+    }
+  }
+  return 0;
+}
+
+// LUBackSubstitution, utility.F90:692-735
+inline void lu_back_substitution(const double* A, int N, const int* INDX, double* B) {
+  int ii = -1;
+  for (int i = 0; i < N; ++i) {
+    int ll = INDX[i];
+    double sum = B[ll];
+    B[ll] = B[i];
+    if (ii >= 0) {
+      for (int j = ii; j < i; ++j) sum = sum - A[i * MAXN + j] * B[j];
+    } else if (sum != 0.0) {
+      ii = i;
+    }
+    B[i] = sum;
+  }
+  for (int i = N - 1; i >= 0; --i) {
+    double sum = B[i];
+    if (i < N - 1)
+      for (int j = i + 1; j < N; ++j) sum = sum - A[i * MAXN + j] * B[j];
+    B[i] = sum / A[i * MAXN + i];
+  }
+}
+
+// RSolve, reaction.F90:5457-5516.  Back-substitutes (the branch at
+// :5506-5512); with fork_literal the update is left untouched (the
+// solve_error branch at :5501-5504 returns after the decomposition).
+inline int rsolve(const double* Res, double* J, const double* conc, double* update, int n,
+                  bool use_log_formulation, bool fork_literal) {
+  double rhs[MAXN];
+  int indices[MAXN];
+  for (int i = 0; i < n; ++i) {
+    double mx = 0.0;
+    for (int j = 0; j < n; ++j) mx = std::max(mx, std::fabs(J[i * MAXN + j]));
+    double norm = std::max(1.0, mx);
+    norm = 1.0 / norm;
+    rhs[i] = Res[i] * norm;
+    for (int j = 0; j < n; ++j) J[i * MAXN + j] = J[i * MAXN + j] * norm;
+  }
+  if (use_log_formulation) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) J[i * MAXN + j] = J[i * MAXN + j] * conc[j];
+  }
+  int ierror = lu_decomposition(J, n, indices);
+  if (ierror != 0) return ierror;
+  if (fork_literal) return 0;
+  lu_back_substitution(J, n, indices, rhs);
+  for (int i = 0; i < n; ++i) update[i] = rhs[i];
+  return 0;
+}
+
+// RUpdateKineticState -> MineralUpdateKineticState,
+// reaction.F90:5935-5972, reaction_mineral.F90:1456-1525
+inline void update_kinetic_state(const Net& net, Cell& c, double dt) {
+  if (net.nm == 0) return;
+  double res[MAXN];
+  for (int j = 0; j < net.n; ++j) res[j] = 0.0;
+  kinetic_mineral(net, c, res, nullptr, false);
+  for (int m = 0; m < net.nm; ++m) {
+    double delta_volfrac = c.mnrl_rate[m] * net.d->mnrl_molar_vol[m] * dt;
+    c.mnrl_volfrac[m] = c.mnrl_volfrac[m] + delta_volfrac;
+    if (c.mnrl_volfrac[m] < 0.0) c.mnrl_volfrac[m] = 0.0;
+  }
+}
+
+// RReact, reaction.F90:3742-4055.  Returns ierror; *num_iterations as the
+// reference counts them (the failing evaluation included).
+inline int rreact(const Net& net, Cell& c, const double* guess, double dt, int* num_iterations) {
+  const int n = net.n;
+  const PfOptions& o = net.o;
+  int ierror = 0;
+  double fixed_accum[MAXN], initial_total[MAXN], residual[MAXN], update[MAXN];
+  double J[MAXN * MAXN];
+  double prev_solution[MAXN], latest_solution[MAXN], conc[MAXN];
+  double two_norm_r0 = 0.0;
+  *num_iterations = 0;
+  c.ierror = 0;
+  set_logK(net, c);
+  accumulation(net, c, fixed_accum);
+  for (int j = 0; j < n; ++j) initial_total[j] = c.total[j];
+  for (int j = 0; j < n; ++j) c.pri_molal[j] = guess[j];
+  for (int j = 0; j < n; ++j) update[j] = 0.0;
+  for (;;) {
+    *num_iterations = *num_iterations + 1;
+    if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) activity_coefficients(net, c);
+    total_aqueous(net, c);
+    if (*num_iterations > o.maximum_reaction_iterations) {
+      ierror = 1;
+      for (int j = 0; j < n; ++j) c.total[j] = initial_total[j];
+      return ierror;
+    }
+    accumulation(net, c, residual);
+    accumulation_derivative(net, c, dt, J);
+    for (int j = 0; j < n; ++j) residual[j] = (residual[j] - fixed_accum[j]) / dt;
+    reaction(net, c, residual, J, true);
+    if (c.ierror != 0) return c.ierror;
+    double dot = 0.0;
+    for (int j = 0; j < n; ++j) dot = dot + residual[j] * residual[j];
+    double two_norm_r = std::sqrt(dot);
+    if (*num_iterations == 1) two_norm_r0 = two_norm_r;
+    double rel_residual = two_norm_r / two_norm_r0;
+    double maxabs = 0.0;
+    for (int j = 0; j < n; ++j) maxabs = std::max(maxabs, std::fabs(residual[j]));
+    if (maxabs < o.max_residual_tolerance) break;
+    if (rel_residual < o.max_rel_residual_tolerance) break;
+    for (int j = 0; j < n; ++j) conc[j] = c.pri_molal[j];
+    int solve_error = rsolve(residual, J, conc, update, n, o.use_log_formulation != 0,
+                             o.fork_literal_rsolve != 0);
+    if (solve_error != 0) { ierror = 1; return ierror; }
+    for (int j = 0; j < n; ++j) prev_solution[j] = c.pri_molal[j];
+    if (o.use_log_formulation) {
+      for (int j = 0; j < n; ++j) {
+        update[j] = fsign1(update[j]) * std::min(std::fabs(update[j]), o.max_dlnC_rreact);
+        latest_solution[j] = prev_solution[j] * std::exp(-update[j]);
+      }
+    } else {
+      double min_ratio = 1.7976931348623157e308;
+      for (int j = 0; j < n; ++j) {
+        if (prev_solution[j] <= update[j]) {
+          double ratio = std::fabs(prev_solution[j] / update[j]);
+          if (ratio < min_ratio) min_ratio = ratio;
+        }
+      }
+      if (min_ratio < 1.0)
+        for (int j = 0; j < n; ++j) update[j] = update[j] * min_ratio * 0.99;
+      for (int j = 0; j < n; ++j) latest_solution[j] = prev_solution[j] - update[j];
+    }
+    double max_rel = 0.0;
+    for (int j = 0; j < n; ++j)
+      max_rel = std::max(max_rel, std::fabs((latest_solution[j] - prev_solution[j]) / prev_solution[j]));
+    if (max_rel < o.max_relative_change_tolerance) break;
+    for (int j = 0; j < n; ++j) c.pri_molal[j] = latest_solution[j];
+  }
+  total_aqueous(net, c);  // "one last update", reaction.F90:4052
+  return ierror;
+}
+
+// Single-cell implicit step as a converged Newton solve: the residual and
+// Jacobian of RReact (reaction.F90:3899-3916), the global-implicit log update
+// with the dlnC clip of PMRTCheckUpdatePre (pm_rt.F90:857-963), and every
+// update applied before the convergence test (the SNES order), iterating until
+// the applied relative change is below rel_tol.  Emulates one GIRT step of a
+// one-cell problem without transport (the batch regression decks).
+inline int implicit_step(const Net& net, Cell& c, double dt, double rel_tol, int max_its,
+                         int* num_iterations) {
+  const int n = net.n;
+  double fixed_accum[MAXN], residual[MAXN], update[MAXN], J[MAXN * MAXN], conc[MAXN];
+  set_logK(net, c);
+  accumulation(net, c, fixed_accum);
+  *num_iterations = 0;
+  for (;;) {
+    *num_iterations += 1;
+    if (net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) activity_coefficients(net, c);
+    total_aqueous(net, c);
+    accumulation(net, c, residual);
+    accumulation_derivative(net, c, dt, J);
+    for (int j = 0; j < n; ++j) residual[j] = (residual[j] - fixed_accum[j]) / dt;
+    reaction(net, c, residual, J, true);
+    for (int j = 0; j < n; ++j) conc[j] = c.pri_molal[j];
+    if (rsolve(residual, J, conc, update, n, true, false) != 0) return 1;
+    double max_rel = 0.0;
+    for (int j = 0; j < n; ++j) {
+      update[j] = fsign1(update[j]) * std::min(std::fabs(update[j]), 5.0);
+      double nv = c.pri_molal[j] * std::exp(-update[j]);
+      max_rel = std::max(max_rel, std::fabs((nv - c.pri_molal[j]) / c.pri_molal[j]));
+      c.pri_molal[j] = nv;
+    }
+    if (max_rel < rel_tol) break;
+    if (*num_iterations >= max_its) return 1;
+  }
+  total_aqueous(net, c);
+  return 0;
+}
+
+struct StepResult {
+  int ierror;
+  int num_iterations;
+  int num_sub_steps;
+  int num_kinetic_state_updates;
+};
+
+// RStep, reaction.F90:3564-3738 (use_full_geochemistry, no immobile species).
+inline StepResult rstep(const Net& net, Cell& c, double* guess, double tran_dt) {
+  const int n = net.n;
+  StepResult r{0, 0, 0, 0};
+  bool small[MAXN];
+  double small_val[MAXN];
+  for (int i = 0; i < n; ++i) {
+    small[i] = false;
+    if (c.total[i] <= 1.0e-40) {
+      small[i] = true;
+      small_val[i] = c.total[i];
+      c.total[i] = 1.0e-40;
+    }
+  }
+  if (net.o.use_total_as_guess)
+    for (int i = 0; i < n; ++i) guess[i] = c.total[i];
+  double target_time = tran_dt;
+  double cumulative_time = 0.0;
+  double dt = tran_dt;
+  int num_constant_timesteps_after_cut = 0;
+  int num_cuts = 0;
+  for (;;) {
+    if (cumulative_time >= target_time) break;
+    int inner = 0;
+    int ierror = rreact(net, c, guess, dt, &inner);
+    r.num_iterations += inner;
+    if (ierror != 0) {
+      num_cuts = num_cuts + 1;
+      if (num_cuts > net.o.maximum_reaction_cuts) {
+        r.ierror = 1;
+        return r;
+      }
+      dt = 0.5 * dt;
+      num_constant_timesteps_after_cut = 0;
+    } else {
+      update_kinetic_state(net, c, dt);
+      if (net.nm > 0) r.num_kinetic_state_updates += 1;
+      cumulative_time = cumulative_time + dt;
+      r.num_sub_steps += 1;
+      num_constant_timesteps_after_cut += 1;
+      for (int i = 0; i < n; ++i) guess[i] = c.pri_molal[i];
+      if (num_constant_timesteps_after_cut >= 4) {
+        num_cuts = num_cuts - 1;
+        dt = std::min(2.0 * dt, target_time - cumulative_time);
+      }
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    if (small[i]) c.total[i] = small_val[i];
+  return r;
+}
+
+// EOSWaterDensityIFC67 (density only), eos_water.F90:1583-1748.  The 1967
+// IFC industrial formulation; its published coefficients are a table that has
+// to be the same as the reference's.
+inline double ifc67_density(double t, double p) {
+  static const double aa[23] = {
+      6.824687741e03, -5.422063673e02, -2.096666205e04, 3.941286787e04,
+      -6.733277739e04, 9.902381028e04, -1.093911774e05, 8.590841667e04,
+      -4.511168742e04, 1.418138926e04, -2.017271113e03, 7.982692717e00,
+      -2.616571843e-2, 1.522411790e-3, 2.284279054e-2, 2.421647003e02,
+      1.269716088e-10, 2.074838328e-7, 2.174020350e-8, 1.105710498e-9,
+      1.293441934e01, 1.308119072e-5, 6.047626338e-14};
+  const double a1 = 8.438375405e-1, a2 = 5.362162162e-4, a3 = 1.720000000e00,
+               a4 = 7.342278489e-2, a5 = 4.975858870e-2, a6 = 6.537154300e-1,
+               a7 = 1.150000000e-6, a8 = 1.510800000e-5, a9 = 1.418800000e-1,
+               a10 = 7.002753165e00, a11 = 2.995284926e-4, a12 = 2.040000000e-1;
+  const double tc1 = H2O_CRITICAL_TEMPERATURE, pc1 = H2O_CRITICAL_PRESSURE;
+  const double vc1 = 0.00317;
+  const double utc1 = 1.0 / tc1, upc1 = 1.0 / pc1;
+  double theta = (t + 273.15) * utc1;
+  double theta2x = theta * theta;
+  double theta18 = std::pow(theta, 18.0);
+  double theta20 = theta18 * theta2x;
+  double beta = p * upc1;
+  double beta2x = beta * beta;
+  double yy = 1.0 - a1 * theta2x - a2 * std::pow(theta, -6.0);
+  double xx = a3 * yy * yy - 2.0 * (a4 * theta - a5 * beta);
+  if (xx > 0.0) xx = std::sqrt(xx);
+  else xx = 1.0e-6;
+  double zz = yy + xx;
+  double u0 = -5.0 / 17.0;
+  double u1 = aa[11] * a5 * std::pow(zz, u0);
+  double u2 = 1.0 / (a8 + std::pow(theta, 11.0));
+  double u3 = aa[17] + (2.0 * aa[18] + 3.0 * aa[19] * beta) * beta;
+  double u4 = 1.0 / (a7 + theta18 * theta);
+  double u5 = std::pow(a10 + beta, -4.0);
+  double u6 = a11 - 3.0 * u5;
+  double u7 = aa[20] * theta18 * (a9 + theta2x);
+  double u8 = aa[15] * std::pow(a6 - theta, 9.0);
+  double vr = u1 + aa[12] + theta * (aa[13] + aa[14] * theta) + u8 * (a6 - theta) +
+              aa[16] * u4 - u2 * u3 - u6 * u7 +
+              (3.0 * aa[21] * (a12 - theta) + 4.0 * aa[22] * beta / theta20) * beta2x;
+  return 1.0 / (vr * vc1);
+}
+
+// Constraint types (transport_constraint_rt.F90:22-34 subset)
+enum { CON_TOTAL = 1, CON_FREE = 2, CON_PH = 3, CON_CHARGE_BAL = 4, CON_LOG = 5 };
+
+// ReactionEquilibrateConstraint, reaction.F90:1328-2115, for the
+// TOTAL/FREE/LOG/PH/CHARGE_BAL subset with no minerals, sorption or gases
+// (initialize_with_molality = false, use_prev_soln_as_guess as given).
+// Returns the iteration count, or -1 when the iteration limit is reached /
+// a concentration goes non-positive / the decomposition is singular.
+inline int equilibrate_constraint(const Net& net, Cell& c, const int* ctype,
+                                  const double* cconc, bool use_prev_soln_as_guess,
+                                  int max_iterations = 10000) {
+  const PfNetworkDesc* d = net.d;
+  const int n = net.n;
+  double xmass = 1.0;
+  double convert_molal_to_molar = 1.0;
+  double convert_molar_to_molal = 1000.0 / c.den_kg / xmass;
+  set_logK(net, c);
+  double free_conc[MAXN], total_conc[MAXN];
+  for (int i = 0; i < n; ++i) free_conc[i] = use_prev_soln_as_guess ? c.pri_molal[i] : 1.0e-9;
+  for (int i = 0; i < n; ++i) {
+    total_conc[i] = 0.0;
+    switch (ctype[i]) {
+      case CON_TOTAL: total_conc[i] = cconc[i] * convert_molal_to_molar; break;
+      case CON_FREE: free_conc[i] = cconc[i] * convert_molar_to_molal; break;
+      case CON_LOG: free_conc[i] = std::pow(10.0, cconc[i]) * convert_molar_to_molal; break;
+      case CON_CHARGE_BAL:
+        if (!use_prev_soln_as_guess) free_conc[i] = cconc[i] * convert_molar_to_molal;
+        break;
+      case CON_PH: free_conc[i] = std::pow(10.0, -cconc[i]); break;
+      default: return -1;
+    }
+  }
+  for (int i = 0; i < n; ++i) c.pri_molal[i] = free_conc[i];
+  int num_iterations = 0, num_it_act_coef_turned_on = 0;
+  bool compute_activity_coefs = use_prev_soln_as_guess;
+  bool charge_balance_warning_flag = false;
+  double Res[MAXN], J[MAXN * MAXN], update[MAXN], prev_molal[MAXN];
+  for (;;) {
+    for (int i = 0; i < n; ++i)
+      if (ctype[i] == CON_FREE || ctype[i] == CON_LOG) c.pri_molal[i] = free_conc[i];
+    if (net.o.act_coef_update_frequency != PF_ACT_COEF_OFF && compute_activity_coefs)
+      activity_coefficients(net, c);
+    total_aqueous(net, c);
+    for (int i = 0; i < n * MAXN; ++i) J[i] = 0.0;
+    for (int i = 0; i < n; ++i) {
+      switch (ctype[i]) {
+        case CON_TOTAL:
+          Res[i] = c.total[i] - total_conc[i];
+          for (int j = 0; j < n; ++j) J[i * MAXN + j] = c.dtotal[i * MAXN + j];
+          break;
+        case CON_FREE:
+        case CON_LOG:
+          Res[i] = 0.0;
+          for (int j = 0; j < n; ++j) J[i * MAXN + j] = 0.0;
+          J[i * MAXN + i] = 1.0;
+          break;
+        case CON_CHARGE_BAL:
+          Res[i] = 0.0;
+          for (int j = 0; j < n; ++j) J[i * MAXN + j] = 0.0;
+          for (int j = 0; j < n; ++j) {
+            Res[i] = Res[i] + d->pri_Z[j] * c.total[j];
+            for (int k = 0; k < n; ++k)
+              J[i * MAXN + j] = J[i * MAXN + j] + d->pri_Z[k] * c.dtotal[k * MAXN + j];
+          }
+          if (c.pri_molal[i] < 1.0e-20 && !charge_balance_warning_flag) {
+            if ((Res[i] > 0.0 && d->pri_Z[i] > 0.0) || (Res[i] < 0.0 && d->pri_Z[i] < 0.0)) {
+              charge_balance_warning_flag = true;
+              c.pri_molal[i] = (double)1.e-3f;  // the reference writes the single-precision literal 1.e-3
+            }
+          }
+          break;
+        case CON_PH:
+          Res[i] = 0.0;
+          for (int j = 0; j < n; ++j) J[i * MAXN + j] = 0.0;
+          c.pri_molal[i] = std::pow(10.0, -cconc[i]) / c.pri_act_coef[i];
+          J[i * MAXN + i] = 1.0;
+          break;
+      }
+    }
+    double maximum_residual = 0.0;
+    for (int i = 0; i < n; ++i) maximum_residual = std::max(maximum_residual, std::fabs(Res[i]));
+    bool use_log_formulation;
+    if (net.o.use_log_formulation) {
+      if (num_iterations > 3 && num_iterations < 9)
+        use_log_formulation = (num_iterations % 2 == 0);
+      else
+        use_log_formulation = true;
+    } else {
+      use_log_formulation = false;
+    }
+    double conc[MAXN];
+    for (int i = 0; i < n; ++i) conc[i] = c.pri_molal[i];
+    if (rsolve(Res, J, conc, update, n, use_log_formulation, false) != 0) return -1;
+    for (int i = 0; i < n; ++i) prev_molal[i] = c.pri_molal[i];
+    if (use_log_formulation) {
+      for (int i = 0; i < n; ++i) {
+        update[i] = fsign1(update[i]) * std::min(std::fabs(update[i]), 5.0);  // reaction%max_dlnC
+        c.pri_molal[i] = c.pri_molal[i] * std::exp(-update[i]);
+      }
+    } else {
+      double min_ratio = 1.7976931348623157e308;
+      for (int i = 0; i < n; ++i) {
+        if (prev_molal[i] <= update[i]) {
+          double ratio = std::fabs(prev_molal[i] / update[i]);
+          if (ratio < min_ratio) min_ratio = ratio;
+        }
+      }
+      if (min_ratio <= 1.0)
+        for (int i = 0; i < n; ++i) update[i] = update[i] * min_ratio * 0.99;
+      for (int i = 0; i < n; ++i) c.pri_molal[i] = prev_molal[i] - update[i];
+    }
+    double mn = c.pri_molal[0];
+    for (int i = 1; i < n; ++i) mn = std::min(mn, c.pri_molal[i]);
+    if (!(mn > 0.0)) return -1;
+    double maximum_relative_change = 0.0;
+    for (int i = 0; i < n; ++i)
+      maximum_relative_change =
+          std::max(maximum_relative_change, std::fabs((c.pri_molal[i] - prev_molal[i]) / prev_molal[i]));
+    num_iterations = num_iterations + 1;
+    if (num_iterations >= max_iterations) return -1;
+    if (maximum_residual < net.o.max_residual_tolerance &&
+        maximum_relative_change < net.o.max_relative_change_tolerance) {
+      if (compute_activity_coefs && num_iterations - num_it_act_coef_turned_on > 1) break;
+      if (!compute_activity_coefs) num_it_act_coef_turned_on = num_iterations;
+      compute_activity_coefs = true;
+    }
+  }
+  return num_iterations;
+}
+
+}  // namespace oracle

@@ -1,0 +1,160 @@
+"""ctypes mirror of include/pfgpu.h and the loader of the CUDA library.
+
+The structs here are byte-for-byte the C structs of the public header; both
+the GPU library (libpfgpu.so, built from ../csrc) and the CPU oracle take
+them, so one host-side description drives both.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PF_OK = 0
+PF_CELL_FAILURES = 1
+PF_ERR_INVALID = -1
+PF_ERR_UNSUPPORTED = -2
+PF_ERR_CUDA = -3
+PF_ERR_TOO_LARGE = -4
+PF_ERR_TIMEOUT = -5
+
+PF_CELL_OK = 0
+PF_CELL_TOO_MANY_CUTS = 1
+PF_CELL_NAN = 2
+
+PF_ACT_COEF_OFF = 0
+PF_ACT_COEF_TIMESTEP = 1
+PF_ACT_COEF_NEWTON_ITER = 2
+PF_ACT_COEF_ALGO_LAG = 0
+PF_ACT_COEF_ALGO_NEWTON = 1
+
+PF_KERNEL_PLAIN = 0
+PF_KERNEL_BATCHED = 1
+
+PF_MAX_NCOMP = 24
+PF_MAX_NSEC = 96
+PF_MAX_NMNRL = 16
+PF_MAX_SPEC_PER_RXN = 24
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class PfOptions(C.Structure):
+    _fields_ = [
+        ("use_log_formulation", C.c_int32),
+        ("act_coef_update_frequency", C.c_int32),
+        ("act_coef_update_algorithm", C.c_int32),
+        ("maximum_reaction_cuts", C.c_int32),
+        ("maximum_reaction_iterations", C.c_int32),
+        ("use_total_as_guess", C.c_int32),
+        ("isothermal", C.c_int32),
+        ("fork_literal_rsolve", C.c_int32),
+        ("max_dlnC_rreact", C.c_double),
+        ("max_relative_change_tolerance", C.c_double),
+        ("max_residual_tolerance", C.c_double),
+        ("max_rel_residual_tolerance", C.c_double),
+    ]
+
+
+class PfNetworkDesc(C.Structure):
+    _fields_ = [
+        ("ncomp", C.c_int32), ("nsec", C.c_int32), ("nmnrl", C.c_int32),
+        ("sec_stride", C.c_int32), ("mnrl_stride", C.c_int32), ("h_ion_id", C.c_int32),
+        ("sec_nspec", _ip), ("sec_spec", _ip), ("sec_stoich", _dp),
+        ("sec_logK", _dp), ("sec_logKcoef", _dp),
+        ("pri_Z", _dp), ("pri_a0", _dp), ("sec_Z", _dp), ("sec_a0", _dp),
+        ("mnrl_nspec", _ip), ("mnrl_spec", _ip), ("mnrl_stoich", _dp),
+        ("mnrl_logK", _dp), ("mnrl_logKcoef", _dp),
+        ("mnrl_rate_constant", _dp), ("mnrl_activation_energy", _dp),
+        ("mnrl_molar_vol", _dp), ("mnrl_affinity_threshold", _dp),
+        ("mnrl_rate_limiter", _dp), ("mnrl_irreversible", _ip),
+        ("mnrl_min_scale_factor", _dp), ("mnrl_Temkin_const", _dp),
+        ("mnrl_affinity_power", _dp),
+        ("debyeA", C.c_double), ("debyeB", C.c_double), ("debyeBdot", C.c_double),
+        ("opts", PfOptions),
+    ]
+
+
+class PfCellState(C.Structure):
+    _fields_ = [
+        ("ncells", C.c_int64),
+        ("total", _dp), ("pri_molal", _dp), ("pri_act_coef", _dp),
+        ("sec_act_coef", _dp), ("sec_molal", _dp),
+        ("mnrl_volfrac", _dp), ("mnrl_area", _dp), ("mnrl_rate", _dp),
+        ("porosity", _dp), ("saturation", _dp), ("den_kg", _dp),
+        ("volume", _dp), ("temperature", _dp), ("dt_cell", _dp),
+        ("status", _ip), ("newton_its", _ip), ("num_substeps", _ip),
+    ]
+
+
+class PfStepStats(C.Structure):
+    _fields_ = [
+        ("cells", C.c_int64), ("failed_cells", C.c_int64),
+        ("newton_iterations", C.c_int64),
+        ("max_newton_iterations", C.c_int32), ("max_substeps", C.c_int32),
+    ]
+
+
+class PfLaunchConfig(C.Structure):
+    _fields_ = [
+        ("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
+        ("jac_in_shared", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_NAME = "libpfgpu.so"
+LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
+
+# Every exported symbol with its ctypes signature (restype, argtypes).
+_P = C.c_void_p
+SIGNATURES = {
+    "pf_network_create": (C.c_int32, [C.POINTER(PfNetworkDesc), C.POINTER(_P)]),
+    "pf_network_destroy": (C.c_int32, [_P]),
+    "pf_network_set_options": (C.c_int32, [_P, C.POINTER(PfOptions)]),
+    "pf_rstep": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32, _P,
+                             C.POINTER(PfStepStats)]),
+    "pf_update_auxvars": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_int32, _P]),
+    "pf_update_activity_coefs": (C.c_int32, [_P, C.POINTER(PfCellState), _P]),
+    "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
+                                  C.POINTER(PfStepStats)]),
+    "pf_network_set_launch": (C.c_int32, [_P, C.POINTER(PfLaunchConfig)]),
+    "pf_network_get_launch": (C.c_int32, [_P, C.POINTER(PfLaunchConfig)]),
+    "pf_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+class PfError(RuntimeError):
+    def __init__(self, fn, code):
+        super().__init__(f"{fn} returned {code}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load libpfgpu.so (built in-tree by __graft_entry__.build()).
+
+    Raises if the library is missing: there is no fallback path.
+    """
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"{p} not found: build the CUDA library first (python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(fn: str, code: int, allow_cell_failures: bool = True) -> int:
+    if code == PF_OK or (allow_cell_failures and code == PF_CELL_FAILURES):
+        return code
+    raise PfError(fn, code)

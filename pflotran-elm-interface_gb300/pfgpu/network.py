@@ -1,0 +1,321 @@
+"""Host-side reaction network and per-cell state.
+
+`ReactionNetwork` is the flattened counterpart of PFLOTRAN's reaction_rt_type
+(src/pflotran/reaction_aux.F90:123-311) restricted to what the per-cell hot
+path reads: aqueous complexes (eqcplxspecid/eqcplxstoich/eqcplx_logK, Z, a0),
+kinetic minerals (kinmnrlspecid/kinmnrlstoich/kinmnrl_logK, TST constants,
+reaction_mineral_aux.F90:82-138), the Debye-Hueckel constants and the
+CHEMISTRY-block options.  `CellState` is the structure-of-arrays form of
+rt_auxvar/global_auxvar/material_auxvar.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+def default_options(**kw) -> dict:
+    """ReactionCreate defaults (src/pflotran/reaction_aux.F90:391-393, 427-432,
+    533-537) with LOG_FORMULATION and ACTIVITY_COEFFICIENTS TIMESTEP on, the
+    settings of the operator-split decks."""
+    o = dict(
+        use_log_formulation=1,
+        act_coef_update_frequency=abi.PF_ACT_COEF_TIMESTEP,
+        act_coef_update_algorithm=abi.PF_ACT_COEF_ALGO_LAG,
+        maximum_reaction_cuts=10,
+        maximum_reaction_iterations=20,
+        use_total_as_guess=0,
+        isothermal=1,
+        fork_literal_rsolve=0,
+        max_dlnC_rreact=5.0,
+        max_relative_change_tolerance=1e-6,
+        max_residual_tolerance=1e-12,
+        max_rel_residual_tolerance=1e-8,
+    )
+    o.update(kw)
+    return o
+
+
+def tight_options(**kw) -> dict:
+    """Tolerances tight enough that every Newton solve converges to rounding
+    level; separates arithmetic error from stopping-rule noise."""
+    return default_options(max_relative_change_tolerance=1e-15,
+                           max_residual_tolerance=1e-300,
+                           max_rel_residual_tolerance=1e-300,
+                           maximum_reaction_iterations=60, **kw)
+
+
+def _ptr(a, ctype):
+    if a is None:
+        return C.cast(None, C.POINTER(ctype))
+    return C.cast(a.ctypes.data, C.POINTER(ctype))
+
+
+@dataclass
+class ReactionNetwork:
+    primary: list
+    secondary: list = field(default_factory=list)
+    minerals: list = field(default_factory=list)
+    pri_Z: np.ndarray = None
+    pri_a0: np.ndarray = None
+    # secondary complexes
+    sec_nspec: np.ndarray = None
+    sec_spec: np.ndarray = None
+    sec_stoich: np.ndarray = None
+    sec_logK: np.ndarray = None
+    sec_logKcoef: np.ndarray = None
+    sec_Z: np.ndarray = None
+    sec_a0: np.ndarray = None
+    # kinetic minerals
+    mnrl_nspec: np.ndarray = None
+    mnrl_spec: np.ndarray = None
+    mnrl_stoich: np.ndarray = None
+    mnrl_logK: np.ndarray = None
+    mnrl_logKcoef: np.ndarray = None
+    mnrl_rate_constant: np.ndarray = None
+    mnrl_activation_energy: np.ndarray = None
+    mnrl_molar_vol: np.ndarray = None
+    mnrl_affinity_threshold: np.ndarray = None
+    mnrl_rate_limiter: np.ndarray = None
+    mnrl_irreversible: np.ndarray = None
+    mnrl_min_scale_factor: np.ndarray = None
+    mnrl_Temkin_const: np.ndarray = None
+    mnrl_affinity_power: np.ndarray = None
+    debyeA: float = 0.5114
+    debyeB: float = 0.3288
+    debyeBdot: float = 0.0410
+    options: dict = field(default_factory=default_options)
+
+    @property
+    def ncomp(self):
+        return len(self.primary)
+
+    @property
+    def nsec(self):
+        return len(self.secondary)
+
+    @property
+    def nmnrl(self):
+        return len(self.minerals)
+
+    @property
+    def h_ion_id(self):
+        return self.primary.index("H+") if "H+" in self.primary else -1
+
+    @staticmethod
+    def build(primary, pri_Z, pri_a0, secondaries, minerals=(), debye=(0.5114, 0.3288, 0.0410),
+              options=None):
+        """primary: names; secondaries: list of dicts {name, stoich:{species:nu}, logK, Z, a0,
+        [logKcoef]}; minerals: list of dicts {name, stoich, logK, rate (mol/m^2/s), molar_vol
+        (m^3/mol), [logKcoef, activation_energy, affinity_threshold, rate_limiter, irreversible]}.
+        """
+        n = len(primary)
+        idx = {s: i for i, s in enumerate(primary)}
+
+        def flatten(rxns):
+            m = len(rxns)
+            stride = max([len(r["stoich"]) for r in rxns] + [1])
+            nspec = np.zeros(m, np.int32)
+            spec = np.zeros((m, stride), np.int32)
+            sto = np.zeros((m, stride), np.float64)
+            for i, r in enumerate(rxns):
+                items = list(r["stoich"].items())
+                nspec[i] = len(items)
+                for s, (name, nu) in enumerate(items):
+                    spec[i, s] = idx[name] if isinstance(name, str) else int(name)
+                    sto[i, s] = nu
+            return nspec, spec, sto
+
+        net = ReactionNetwork(primary=list(primary))
+        net.pri_Z = np.asarray(pri_Z, np.float64)
+        net.pri_a0 = np.asarray(pri_a0, np.float64)
+        net.secondary = [r["name"] for r in secondaries]
+        net.sec_nspec, net.sec_spec, net.sec_stoich = flatten(secondaries)
+        net.sec_logK = np.array([r["logK"] for r in secondaries], np.float64)
+        net.sec_Z = np.array([r["Z"] for r in secondaries], np.float64)
+        net.sec_a0 = np.array([r["a0"] for r in secondaries], np.float64)
+        if secondaries and all("logKcoef" in r for r in secondaries):
+            net.sec_logKcoef = np.array([r["logKcoef"] for r in secondaries], np.float64)
+        mins = list(minerals)
+        net.minerals = [r["name"] for r in mins]
+        net.mnrl_nspec, net.mnrl_spec, net.mnrl_stoich = flatten(mins)
+        nm = len(mins)
+        net.mnrl_logK = np.array([r["logK"] for r in mins], np.float64)
+        net.mnrl_rate_constant = np.array([r["rate"] for r in mins], np.float64)
+        net.mnrl_molar_vol = np.array([r["molar_vol"] for r in mins], np.float64)
+        net.mnrl_activation_energy = np.array([r.get("activation_energy", 0.0) for r in mins],
+                                              np.float64)
+        net.mnrl_affinity_threshold = np.array([r.get("affinity_threshold", 0.0) for r in mins],
+                                               np.float64)
+        net.mnrl_rate_limiter = np.array([r.get("rate_limiter", 0.0) for r in mins], np.float64)
+        net.mnrl_irreversible = np.array([r.get("irreversible", 0) for r in mins], np.int32)
+        if mins and all("logKcoef" in r for r in mins):
+            net.mnrl_logKcoef = np.array([r["logKcoef"] for r in mins], np.float64)
+        for key in ("min_scale_factor", "Temkin_const", "affinity_power"):
+            if any(key in r for r in mins):
+                setattr(net, "mnrl_" + key,
+                        np.array([r.get(key, 1.0) for r in mins], np.float64))
+        if nm == 0:
+            for k in ("mnrl_logK", "mnrl_rate_constant", "mnrl_molar_vol",
+                      "mnrl_activation_energy", "mnrl_affinity_threshold", "mnrl_rate_limiter"):
+                setattr(net, k, np.zeros(0, np.float64))
+            net.mnrl_irreversible = np.zeros(0, np.int32)
+        net.debyeA, net.debyeB, net.debyeBdot = debye
+        net.options = options if options is not None else default_options()
+        assert net.pri_Z.shape == (n,)
+        return net
+
+    def with_options(self, **kw):
+        import copy
+        other = copy.copy(self)
+        other.options = dict(self.options)
+        other.options.update(kw)
+        return other
+
+    def desc(self) -> abi.PfNetworkDesc:
+        """PfNetworkDesc pointing into this object's arrays (keep self alive)."""
+        self._keep = []
+
+        def arr(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(a)
+            return a
+
+        d = abi.PfNetworkDesc()
+        d.ncomp, d.nsec, d.nmnrl = self.ncomp, self.nsec, self.nmnrl
+        d.sec_stride = int(self.sec_spec.shape[1]) if self.nsec else 1
+        d.mnrl_stride = int(self.mnrl_spec.shape[1]) if self.nmnrl else 1
+        d.h_ion_id = self.h_ion_id
+        i32, f64 = np.int32, np.float64
+        d.sec_nspec = _ptr(arr(self.sec_nspec, i32), C.c_int32)
+        d.sec_spec = _ptr(arr(self.sec_spec, i32), C.c_int32)
+        d.sec_stoich = _ptr(arr(self.sec_stoich, f64), C.c_double)
+        d.sec_logK = _ptr(arr(self.sec_logK, f64), C.c_double)
+        d.sec_logKcoef = _ptr(arr(self.sec_logKcoef, f64), C.c_double)
+        d.pri_Z = _ptr(arr(self.pri_Z, f64), C.c_double)
+        d.pri_a0 = _ptr(arr(self.pri_a0, f64), C.c_double)
+        d.sec_Z = _ptr(arr(self.sec_Z, f64), C.c_double)
+        d.sec_a0 = _ptr(arr(self.sec_a0, f64), C.c_double)
+        d.mnrl_nspec = _ptr(arr(self.mnrl_nspec, i32), C.c_int32)
+        d.mnrl_spec = _ptr(arr(self.mnrl_spec, i32), C.c_int32)
+        d.mnrl_stoich = _ptr(arr(self.mnrl_stoich, f64), C.c_double)
+        d.mnrl_logK = _ptr(arr(self.mnrl_logK, f64), C.c_double)
+        d.mnrl_logKcoef = _ptr(arr(self.mnrl_logKcoef, f64), C.c_double)
+        d.mnrl_rate_constant = _ptr(arr(self.mnrl_rate_constant, f64), C.c_double)
+        d.mnrl_activation_energy = _ptr(arr(self.mnrl_activation_energy, f64), C.c_double)
+        d.mnrl_molar_vol = _ptr(arr(self.mnrl_molar_vol, f64), C.c_double)
+        d.mnrl_affinity_threshold = _ptr(arr(self.mnrl_affinity_threshold, f64), C.c_double)
+        d.mnrl_rate_limiter = _ptr(arr(self.mnrl_rate_limiter, f64), C.c_double)
+        d.mnrl_irreversible = _ptr(arr(self.mnrl_irreversible, i32), C.c_int32)
+        d.mnrl_min_scale_factor = _ptr(arr(self.mnrl_min_scale_factor, f64), C.c_double)
+        d.mnrl_Temkin_const = _ptr(arr(self.mnrl_Temkin_const, f64), C.c_double)
+        d.mnrl_affinity_power = _ptr(arr(self.mnrl_affinity_power, f64), C.c_double)
+        d.debyeA, d.debyeB, d.debyeBdot = self.debyeA, self.debyeB, self.debyeBdot
+        d.opts = self.options_struct()
+        return d
+
+    def options_struct(self) -> abi.PfOptions:
+        o = abi.PfOptions()
+        for k, _ in abi.PfOptions._fields_:
+            setattr(o, k, self.options[k])
+        return o
+
+
+# ---------------------------------------------------------------- cell state
+STATE_FIELDS = {
+    # name: (rows, dtype)  rows: 'n' ncomp, 's' nsec, 'm' nmnrl, 1 scalar
+    "total": ("n", np.float64), "pri_molal": ("n", np.float64),
+    "pri_act_coef": ("n", np.float64), "sec_act_coef": ("s", np.float64),
+    "sec_molal": ("s", np.float64), "mnrl_volfrac": ("m", np.float64),
+    "mnrl_area": ("m", np.float64), "mnrl_rate": ("m", np.float64),
+    "porosity": (1, np.float64), "saturation": (1, np.float64),
+    "den_kg": (1, np.float64), "volume": (1, np.float64),
+    "temperature": (1, np.float64), "dt_cell": (1, np.float64),
+    "status": (1, np.int32), "newton_its": (1, np.int32), "num_substeps": (1, np.int32),
+}
+OPTIONAL_FIELDS = ("dt_cell",)
+
+
+def _rows(net, r):
+    return {"n": net.ncomp, "s": net.nsec, "m": net.nmnrl}.get(r, r)
+
+
+class CellState:
+    """SoA per-cell state. Arrays are numpy (host) or torch tensors (device),
+    shaped (rows, ncells) so that value(k, cell) = a[k*ncells+cell]."""
+
+    def __init__(self, net: ReactionNetwork, arrays: dict):
+        self.net = net
+        self.a = dict(arrays)
+        self.ncells = int(self.a["porosity"].shape[-1])
+
+    @staticmethod
+    def empty(net, ncells, with_dt=False):
+        a = {}
+        for k, (r, dt) in STATE_FIELDS.items():
+            if k in OPTIONAL_FIELDS and not with_dt:
+                continue
+            rows = _rows(net, r)
+            a[k] = np.zeros((rows, ncells), dt) if r != 1 else np.zeros(ncells, dt)
+        a["pri_act_coef"][:] = 1.0
+        a["sec_act_coef"][:] = 1.0
+        a["saturation"][:] = 1.0
+        a["volume"][:] = 1.0
+        a["temperature"][:] = 25.0
+        return CellState(net, a)
+
+    def copy(self):
+        out = {}
+        for k, v in self.a.items():
+            out[k] = v.copy() if isinstance(v, np.ndarray) else v.clone()
+        return CellState(self.net, out)
+
+    def to(self, device):
+        import torch
+        out = {}
+        for k, v in self.a.items():
+            t = v if not isinstance(v, np.ndarray) else torch.from_numpy(np.ascontiguousarray(v))
+            out[k] = t.to(device).contiguous()
+        return CellState(self.net, out)
+
+    def numpy(self):
+        out = {}
+        for k, v in self.a.items():
+            out[k] = v if isinstance(v, np.ndarray) else v.detach().cpu().numpy()
+        return CellState(self.net, out)
+
+    def subset(self, idx):
+        out = {}
+        for k, v in self.a.items():
+            if isinstance(v, np.ndarray):
+                out[k] = np.ascontiguousarray(v[..., idx])
+            else:
+                out[k] = v[..., idx].contiguous()
+        return CellState(self.net, out)
+
+    def struct(self) -> abi.PfCellState:
+        s = abi.PfCellState()
+        s.ncells = self.ncells
+        for k, (r, dt) in STATE_FIELDS.items():
+            v = self.a.get(k)
+            ct = C.c_int32 if dt == np.int32 else C.c_double
+            if v is None:
+                setattr(s, k, C.cast(None, C.POINTER(ct)))
+                continue
+            if isinstance(v, np.ndarray):
+                assert v.flags.c_contiguous and v.dtype == dt, k
+                addr = v.ctypes.data
+            else:
+                assert v.is_contiguous(), k
+                addr = v.data_ptr()
+            setattr(s, k, C.cast(addr, C.POINTER(ct)))
+        return s

@@ -1,0 +1,211 @@
+"""Generate the known-answer fixtures in tests/golden/ from the reference's own
+regression decks, thermodynamic databases and gold files.
+
+Runs only where the reference tree is mounted (default /root/reference; pass
+another root as argv[1]).  The tests read the JSON this writes and never the
+reference tree itself.
+
+Sources (paths within fmyuan/pflotran-elm-interface):
+  regression_tests/ascem/batch/<deck>.in              chemistry block, constraint, times
+  regression_tests/ascem/batch/{calcite,carbonate,ca-carbonate}.dat  database
+  regression_tests/ascem/batch/<deck>.regression.gold  expected values
+  regression_tests/ascem/batch/batch.cfg:20-27         tolerances (1e-12 absolute)
+  src/pflotran/unittests/test_eos_water.pf:146-157     IFC67 density pin
+"""
+import json
+import os
+import re
+import shlex
+import sys
+
+ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+BATCH = os.path.join(ROOT, "regression_tests", "ascem", "batch")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+DECKS = ["carbonate-unit-activity", "carbonate-debye-huckel-activity",
+         "ca-carbonate-unit-activity", "ca-carbonate-debye-huckel-activity",
+         "calcite-kinetics", "calcite-kinetics-volume-fractions"]
+
+TIME_UNITS = {"s": 1.0, "sec": 1.0, "min": 60.0, "h": 3600.0, "hr": 3600.0,
+              "d": 86400.0, "day": 86400.0, "w": 7 * 86400.0,
+              "mo": 365.0 / 12.0 * 86400.0, "y": 365.0 * 86400.0, "yr": 365.0 * 86400.0}
+
+
+def fnum(s):
+    return float(s.lower().replace("d", "e"))
+
+
+def read_dat(path):
+    """Parse the PFLOTRAN .dat database format (reaction_database.F90:26)."""
+    toks = shlex.split(open(path).read())
+    i = 0
+    assert toks[i] == "temperature points"
+    ntemp = int(toks[i + 1])
+    temps = [fnum(t) for t in toks[i + 2:i + 2 + ntemp]]
+    i += 2 + ntemp
+    primary = {}
+    while toks[i] != "null":
+        primary[toks[i]] = dict(a0=fnum(toks[i + 1]), Z=fnum(toks[i + 2]))
+        i += 4
+    i += 4
+
+    def aq_record(i):  # name ns (nu sp)*ns logK*ntemp a0 Z mw
+        name = toks[i]; ns = int(fnum(toks[i + 1])); i += 2
+        st = []
+        for _ in range(ns):
+            st.append((toks[i + 1], fnum(toks[i]))); i += 2
+        logK = [fnum(t) for t in toks[i:i + ntemp]]; i += ntemp
+        rec = dict(stoich=st, logK=logK, a0=fnum(toks[i]), Z=fnum(toks[i + 1]))
+        return name, rec, i + 3
+
+    def solid_record(i):  # name molar_vol ns (nu sp)*ns logK*ntemp mw
+        name = toks[i]; mv = fnum(toks[i + 1]); ns = int(fnum(toks[i + 2])); i += 3
+        st = []
+        for _ in range(ns):
+            st.append((toks[i + 1], fnum(toks[i]))); i += 2
+        logK = [fnum(t) for t in toks[i:i + ntemp]]; i += ntemp
+        return name, dict(stoich=st, logK=logK, molar_vol_cm3=mv), i + 1
+
+    secondary = {}
+    while True:
+        name, rec, i = aq_record(i)
+        if name == "null":
+            break
+        secondary[name] = rec
+    while True:  # gases
+        name, rec, i = solid_record(i)
+        if name == "null":
+            break
+    minerals = {}
+    while True:
+        name, rec, i = solid_record(i)
+        if name == "null":
+            break
+        minerals[name] = rec
+    return temps, primary, secondary, minerals
+
+
+def block(lines, start):
+    out = []
+    for ln in lines[start + 1:]:
+        s = ln.strip()
+        if s == "/" or s.upper() == "END":
+            break
+        if s:
+            out.append(s)
+    return out
+
+
+def read_deck(path):
+    raw = [ln.split("#")[0].rstrip() for ln in open(path)]
+    lines = [ln for ln in raw]
+    up = [ln.strip().upper() for ln in lines]
+    deck = {}
+    i = up.index("PRIMARY_SPECIES")
+    deck["primary"] = block(lines, i)
+    i = up.index("SECONDARY_SPECIES")
+    deck["secondary"] = block(lines, i)
+    deck["minerals"] = block(lines, up.index("MINERALS")) if "MINERALS" in up else []
+    deck["rates"] = {}
+    if "MINERAL_KINETICS" in up:
+        j = up.index("MINERAL_KINETICS") + 1
+        while up[j] != "/":
+            name = lines[j].strip()
+            k = j + 1
+            while up[k] != "/":
+                m = re.match(r"RATE_CONSTANT\s+(\S+)\s*(\S*)", lines[k].strip(), re.I)
+                if m:
+                    v = fnum(m.group(1))
+                    unit = m.group(2)
+                    if unit == "mol/cm^2-sec":
+                        v *= 1.0e4
+                    deck["rates"][name] = v
+                k += 1
+            j = k + 1
+    chem = " ".join(up[up.index("CHEMISTRY"):])
+    deck["database"] = re.search(r"DATABASE\s+(\S+)", " ".join(lines)).group(1)
+    deck["log_formulation"] = "LOG_FORMULATION" in chem
+    m = re.search(r"ACTIVITY_COEFFICIENTS\s+(\w+)", chem)
+    deck["act_coef"] = m.group(1) if m and m.group(1) in ("TIMESTEP", "NEWTON_ITERATION", "OFF") else "OFF"
+    ci = [k for k, s in enumerate(up) if s.startswith("CONSTRAINT INITIAL")][0]
+    k = up.index("CONCENTRATIONS", ci)
+    deck["constraint"] = {}
+    for s in block(lines, k):
+        parts = s.split()
+        deck["constraint"][parts[0]] = (parts[2].upper(), fnum(parts[1]))
+    deck["mineral_init"] = {}
+    if "MINERALS" in up[ci:]:
+        k = up.index("MINERALS", ci)
+        for s in block(lines, k):
+            p = s.split()
+            area = fnum(p[2])
+            unit = p[3] if len(p) > 3 else "m^2/m^3"
+            if unit == "cm^2/cm^3":
+                area *= 100.0
+            deck["mineral_init"][p[0]] = (fnum(p[1]), area)
+    deck["porosity"] = fnum(re.search(r"POROSITY\s+(\S+)", " ".join(lines)).group(1))
+    for key in ("FINAL_TIME", "INITIAL_TIMESTEP_SIZE", "MAXIMUM_TIMESTEP_SIZE"):
+        m = re.search(key + r"\s+(\S+)\s+(\S+)", " ".join(lines))
+        deck[key.lower()] = fnum(m.group(1)) * TIME_UNITS[m.group(2)]
+    return deck
+
+
+def read_gold(path):
+    gold = {}
+    txt = open(path).read().splitlines()
+    for i, ln in enumerate(txt):
+        m = re.match(r"-- (\w+): (.+) --", ln)
+        if m and m.group(1) != "SOLUTION" and m.group(1) != "DISCRETE":
+            gold[m.group(2)] = float(txt[i + 1].split()[1])
+        if m and m.group(1) == "SOLUTION":
+            for ln2 in txt[i + 1:]:
+                mm = re.match(r"\s+(Time Steps|Newton Iterations):\s+(\d+)", ln2)
+                if mm:
+                    gold[mm.group(1)] = int(mm.group(2))
+    return gold
+
+
+def main():
+    tref_index = None
+    fixtures = {}
+    for name in DECKS:
+        deck = read_deck(os.path.join(BATCH, name + ".in"))
+        temps, pri, sec, mins = read_dat(os.path.join(BATCH, deck["database"].lstrip("./")))
+        tref_index = temps.index(25.0)
+        primary = deck["primary"]
+        fx = dict(
+            deck=name,
+            source="regression_tests/ascem/batch/%s.in" % name,
+            primary=primary,
+            pri_Z=[pri[s]["Z"] for s in primary],
+            pri_a0=[pri[s]["a0"] for s in primary],
+            secondaries=[dict(name=s, stoich={sp: nu for sp, nu in sec[s]["stoich"] if sp != "H2O"},
+                              logK=sec[s]["logK"][tref_index], Z=sec[s]["Z"], a0=sec[s]["a0"])
+                         for s in deck["secondary"]],
+            minerals=[dict(name=m, stoich={sp: nu for sp, nu in mins[m]["stoich"] if sp != "H2O"},
+                           logK=mins[m]["logK"][tref_index], rate=deck["rates"][m],
+                           molar_vol=mins[m]["molar_vol_cm3"] * 1.0e-6)
+                      for m in deck["minerals"]],
+            log_formulation=deck["log_formulation"],
+            act_coef=deck["act_coef"],
+            constraint=deck["constraint"],
+            mineral_init=deck["mineral_init"],
+            porosity=deck["porosity"],
+            final_time=deck["final_time"],
+            dt=deck["maximum_timestep_size"],
+            gold=read_gold(os.path.join(BATCH, name + ".regression.gold")),
+            tolerance_abs=1.0e-12,
+        )
+        fixtures[name] = fx
+    # IFC67 pin: src/pflotran/unittests/test_eos_water.pf
+    pf = open(os.path.join(ROOT, "src", "pflotran", "unittests", "test_eos_water.pf")).read()
+    m = re.search(r"998\.\d+", pf)
+    fixtures["_eos_water_pin"] = dict(source="src/pflotran/unittests/test_eos_water.pf",
+                                      t=20.0, p=101325.0, density=float(m.group(0)))
+    with open(os.path.join(OUT, "kat_batch.json"), "w") as f:
+        json.dump(fixtures, f, indent=1, sort_keys=True)
+    print("wrote", os.path.join(OUT, "kat_batch.json"))
+
+
+if __name__ == "__main__":
+    main()
