@@ -1,0 +1,364 @@
+"""Benchmark: operator-split cell chemistry solves per second on GB300.
+
+Workload (default, --config c2): one synthetic network with 12 primary
+species, 40 aqueous complexes and 6 kinetic minerals over 1,000,000 cells,
+FP64, dt = 1 day, T ~ U[5, 60] C (non-isothermal logK), totals log10
+U[-6, -2] with H+ by charge balance.  Inputs are generated and equilibrated on
+the device (pf_equilibrate_constraint); the state (~1.1 GB) is far larger than
+L2, and every step restarts from the same initial state (device-to-device
+reset, inside the timed step).
+
+One step = one pf_rstep over all cells (RStep for every cell: Newton, dt
+cuts, kinetic-state update).  value = cells x steps / time.
+  value        batched persistent kernel, inputs resident in HBM
+  e2e          pf_rstep_host: host buffers, H2D + step + D2H inside the call
+  plain_gpu    the plain one-thread-per-cell form on the same inputs
+  cpu_baseline the CPU restatement of the reference (oracle) on the host cores
+--impl reference times that CPU restatement alone (the reference itself is
+Fortran on PETSc and cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "pflotran-elm-interface_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "cell chemistry solves/s at 1e-10 rel. tol vs plain GPU; adjoint/forward time ratio"
+UNIT = "cell-solves/s"
+MUTABLE = ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
+           "mnrl_rate", "status", "newton_its", "num_substeps")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload(name):
+    if name == "c1":
+        return dict(workload="calcite 10x10x10 operator-split RStep (ncomp 3, 6 complexes, kinetic calcite)",
+                    cells=1000, dt=3600.0)
+    return dict(workload="synthetic network, 12 primaries / 40 complexes / 6 kinetic minerals, "
+                         "operator-split RStep, non-isothermal", cells=1_000_000, dt=86400.0)
+
+
+def build_state(cfg_name, ncells, device, seed=2026):
+    import torch
+
+    from pfgpu import abi, generate
+    from pfgpu.engine import ReactionEngine
+    from pfgpu.network import CellState, default_options
+
+    if cfg_name == "c1":
+        net = generate.calcite_network()
+        st, ct, cc = generate.calcite_cells(net, ncells + ncells // 20 + 64, seed=20261203)
+    else:
+        net = generate.random_network(12, 40, 6, seed=12, options=default_options(isothermal=0))
+        st, ct, cc = generate.random_cells(net, ncells + ncells // 20 + 64, seed=seed)
+    eng = ReactionEngine(net)
+    dev = st.to(device)
+    its = eng.equilibrate(dev, ct, torch.from_numpy(cc).to(device))
+    good = torch.nonzero(its > 0).flatten()[:ncells]
+    if good.numel() < ncells:
+        raise RuntimeError("only %d of %d cells equilibrated" % (good.numel(), ncells))
+    dev = dev.subset(good)
+    # initial auxvars (condition_control.F90:1638-1649) then the step prelude
+    # of pm_osrt.F90:115-153 (RTUpdateAuxVars, TIMESTEP activity update)
+    dev.a["pri_act_coef"].fill_(1.0)
+    dev.a["sec_act_coef"].fill_(1.0)
+    dev.a["sec_molal"].zero_()
+    eng.update_auxvars(dev, False)
+    eng.update_auxvars(dev, True)
+    eng.update_auxvars(dev, True)
+    eng.update_auxvars(dev, False)
+    eng.update_activity_coefs(dev)
+    torch.cuda.synchronize()
+    return net, eng, dev
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return None
+        rows = [r for r in rows if len(r) >= 8]
+        if not rows:
+            return None
+        sm = sorted(float(r[0]) for r in rows)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[4:8]):
+                if v.strip() == "Active":
+                    reasons.add(nm)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": float(rows[0][1]), "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def fp64_peak(lib, device_sms):
+    """Measured FP64 FMA throughput (TFLOP/s) with the library's probe."""
+    import ctypes as C
+
+    import torch
+    blocks, threads, iters = device_sms * 8, 256, 5000
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    best = 0.0
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.pf_bench_fp64_fma(C.c_void_p(out.data_ptr()), iters, blocks, threads, C.c_void_p(s.cuda_stream))
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, blocks * threads * iters * 16.0 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def time_steps(eng, dev, pristine, dt, kernel, steps, warmup):
+    import torch
+    from pfgpu import abi  # noqa: F401
+
+    def reset():
+        for k in MUTABLE:
+            if k in dev.a:
+                dev.a[k].copy_(pristine[k], non_blocking=True)
+
+    for _ in range(warmup):
+        reset()
+        eng.rstep(dev, dt, kernel=kernel, stats=False)
+    torch.cuda.synchronize()
+    ks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for a, b in ks:
+        reset()
+        a.record()
+        eng.rstep(dev, dt, kernel=kernel, stats=False)
+        b.record()
+    t1.record()
+    torch.cuda.synchronize()
+    total_ms = t0.elapsed_time(t1)
+    kern_ms = [a.elapsed_time(b) for a, b in ks]
+    return total_ms, kern_ms
+
+
+def cpu_baseline(net, host_state, dt, budget_s=15.0):
+    """The oracle (C++ restatement of the reference, OpenMP over cells) on a
+    bounded sample of the same cells, all host cores."""
+    from oracle.oracle import Oracle
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    n = min(host_state.ncells, 2000)
+    while True:
+        sub = host_state.subset(range(n))
+        t = time.perf_counter()
+        o.rstep(net, sub, dt, nthreads=cores)
+        el = time.perf_counter() - t
+        if el > budget_s / 4 or n >= host_state.ncells:
+            break
+        n = min(host_state.ncells, int(n * min(8.0, max(2.0, (budget_s / 3) / max(el, 1e-3)))))
+    return {"value": n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d cells of the same workload, one RStep each, %.2f s" % (n, el)}
+
+
+def run_reference(args):
+    import numpy as np  # noqa: F401
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+    cfg = workload(args.config)
+    # inputs: the same generator and device equilibration as our arm when a GPU
+    # is present; the CPU restatement is then timed on the host cores
+    net, eng, dev = build_state(args.config, min(cfg["cells"], 200_000), "cuda")
+    host = dev.numpy()
+    from oracle.oracle import Oracle
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    n = min(host.ncells, 20000 if args.config != "c1" else 1000)
+    vals = []
+    for k in range(args.warmup + args.steps):
+        sub = host.subset(range(n))
+        t = time.perf_counter()
+        o.rstep(net, sub, cfg["dt"], nthreads=cores)
+        el = time.perf_counter() - t
+        if k >= args.warmup:
+            vals.append(n / el)
+    v = float(np.median(vals)) if vals else 0.0
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v if v else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": cfg["workload"], "cells_per_step_sample": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d cells per step (bounded sample of the %d-cell workload)" % (
+                                 n, cfg["cells"])},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference is Fortran+PETSc (no Fortran compiler here); timed its C++ restatement"}
+    print(json.dumps(line), flush=True)
+    del torch
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--cells", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    import numpy as np
+    import torch
+
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from pfgpu import abi, flops
+    cfg = workload(args.config)
+    ncells = args.cells or cfg["cells"]
+    t_build = time.perf_counter()
+    net, eng, dev = build_state(args.config, ncells, "cuda", seed=2026 + rank)
+    log("state built: %d cells in %.1f s" % (ncells, time.perf_counter() - t_build))
+    pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}
+    dt = cfg["dt"]
+
+    # one instrumented step: iteration statistics for the flop count
+    stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
+    its_mean = stats["newton_iterations"] / ncells
+    for k in pristine:
+        dev.a[k].copy_(pristine[k])
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        total_ms, kern_ms = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, args.steps, args.warmup)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * ncells * args.steps / (total_ms * 1e-3)
+    kern_avg = float(np.mean(kern_ms))
+
+    # plain one-thread-per-cell form, same inputs
+    p_total, p_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_PLAIN, max(1, min(args.steps, 3)), 1)
+    plain_value = ncells * len(p_kern) / (p_total * 1e-3)
+
+    # roofline: FP64 pipe (algorithmic flops of the reference iteration)
+    f_it, tr_it = flops.per_iteration(net)
+    flops_per_launch = f_it * its_mean * ncells
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak = fp64_peak(abi.load(), sms)
+    achieved = flops_per_launch / (kern_avg * 1e-3) / 1e12
+    state_bytes = sum(v.numel() * v.element_size() for v in dev.a.values())
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "FP64 DFMA probe (pf_bench_fp64_fma) measured in this run",
+                "flops_per_cell_solve": f_it * its_mean, "transcendentals_per_cell_solve": tr_it * its_mean,
+                "hbm_gbs": state_bytes * 2 / (kern_avg * 1e-3) / 1e9}
+
+    e2e = None
+    if not args.no_e2e:
+        host = dev.numpy()
+        pin = {}
+        for k, v in dev.a.items():
+            pin[k] = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+        from pfgpu.network import CellState
+        hs = CellState(net, {k: pin[k].numpy() for k in pin})
+        h2d = sum(pin[k].numel() * pin[k].element_size() for k in pin if k not in ("mnrl_rate", "status",
+                                                                                  "newton_its", "num_substeps"))
+        d2h = sum(pin[k].numel() * pin[k].element_size() for k in pin
+                  if k in ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
+                           "mnrl_rate", "status", "newton_its", "num_substeps"))
+        src = {k: pristine[k].cpu().numpy() if k in pristine else host.a[k] for k in pin}
+        times = []
+        for k in range(args.warmup + args.steps):
+            for f in pin:
+                np.copyto(hs.a[f], src[f])
+            t = time.perf_counter()
+            eng.rstep_host(hs, dt)
+            el = time.perf_counter() - t
+            if k >= args.warmup:
+                times.append(el)
+        e2e = {"value": ncells * len(times) / sum(times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        host = dev.numpy()
+        for k in pristine:
+            host.a[k] = pristine[k].cpu().numpy()
+        cpu = cpu_baseline(net, host, dt)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": cfg["workload"], "cells": ncells, "dt_s": dt,
+                           "parallelism": "replicas" if world > 1 else "single-gpu",
+                           "l2": "state %.2f GB > L2; state reset D2D each step" % (state_bytes / 1e9),
+                           "kernel": "batched persistent (PF_KERNEL_BATCHED)",
+                           "launch": eng.launch_config()},
+                "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
+                "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
+                "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},
+                "speedup_vs_plain_gpu": value / plain_value,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": args.steps}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

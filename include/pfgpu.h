@@ -228,6 +228,33 @@ int32_t pf_update_activity_coefs(PfNetwork* net, const PfCellState* state,
 int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
                       double dt, int32_t kernel, PfStepStats* stats);
 
+/* ----------------------------------------------------------- constraints */
+/* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */
+enum {
+  PF_CONSTRAINT_TOTAL = 1,
+  PF_CONSTRAINT_FREE = 2,
+  PF_CONSTRAINT_PH = 3,
+  PF_CONSTRAINT_CHARGE_BAL = 4,
+  PF_CONSTRAINT_LOG = 5
+};
+
+/*
+ * pf_equilibrate_constraint -- ReactionEquilibrateConstraint
+ * (src/pflotran/reaction.F90:1328-2115) for every cell, restricted to the
+ * aqueous constraint types above (no mineral/gas/sorption constraints).
+ * ctype: host array [ncomp], one type per primary component.
+ * cconc: device array [ncomp][ncells]: total (mol/L), free (mol/L),
+ *        log10 free, pH, or the charge-balance species' initial guess.
+ * On return pri_molal, pri_act_coef, sec_act_coef, sec_molal and total hold
+ * the equilibrated state; iterations[cell] (device, optional) holds the
+ * Newton count or -1 when the cell did not converge within 10000 iterations
+ * or produced a non-positive molality (the reference stops the run there).
+ */
+int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state,
+                                  const int32_t* ctype, const double* cconc,
+                                  int32_t use_prev_soln_as_guess,
+                                  int32_t* iterations, void* stream);
+
 /* ------------------------------------------------------------ capabilities */
 /* Kernel launch configuration for the batched form; chosen by the
  * autotuner (pfgpu.autotune) and settable per network. */

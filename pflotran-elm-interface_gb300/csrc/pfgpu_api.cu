@@ -1,0 +1,379 @@
+// pfgpu_api.cu -- the C ABI (include/pfgpu.h): network upload, argument
+// checking, kernel dispatch, the status reduction and the host-buffer path.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "pfgpu_common.cuh"
+#include "pfgpu_kernels.h"
+
+using namespace pfgpu;
+
+extern "C" int32_t pf_equilibrate_constraint_impl(const DevNet* net, const PfCellState* st,
+                                                  const int32_t* ctype, const double* cconc, int use_prev,
+                                                  int32_t* iterations, int max_iterations, void* stream);
+
+struct PfNetwork {
+  DevNet dev{};
+  void* d_tables = nullptr;
+  unsigned long long* d_counters = nullptr;  // [0] queue [1] its [2] fails [3] err [4] max its [5] max substeps
+  unsigned long long* h_counters = nullptr;  // pinned mirror
+  int32_t* d_ctype = nullptr;                // constraint types [PF_MAX_NCOMP]
+  PfLaunchConfig launch{};
+  int device = 0;
+  int num_sms = 0;
+  // host-path arena (grow-only)
+  void* d_arena = nullptr;
+  size_t arena_bytes = 0;
+};
+
+namespace {
+
+inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? PF_OK : PF_ERR_CUDA; }
+
+size_t pad16(size_t bytes) { return (bytes + 15) & ~size_t(15); }
+
+int validate_desc(const PfNetworkDesc* d) {
+  if (!d) return PF_ERR_INVALID;
+  if (d->ncomp < 1 || d->nsec < 0 || d->nmnrl < 0) return PF_ERR_INVALID;
+  if (d->ncomp > PF_MAX_NCOMP || d->nsec > PF_MAX_NSEC || d->nmnrl > PF_MAX_NMNRL) return PF_ERR_TOO_LARGE;
+  if (!d->pri_Z || !d->pri_a0) return PF_ERR_INVALID;
+  if (d->nsec > 0 && (!d->sec_nspec || !d->sec_spec || !d->sec_stoich || !d->sec_logK || !d->sec_Z ||
+                      !d->sec_a0 || d->sec_stride < 1))
+    return PF_ERR_INVALID;
+  for (int i = 0; i < d->nsec; ++i) {
+    if (d->sec_nspec[i] < 0 || d->sec_nspec[i] > d->sec_stride || d->sec_nspec[i] > PF_MAX_SPEC_PER_RXN)
+      return PF_ERR_INVALID;
+    for (int s = 0; s < d->sec_nspec[i]; ++s) {
+      int k = d->sec_spec[i * d->sec_stride + s];
+      if (k < 0 || k >= d->ncomp) return PF_ERR_INVALID;
+    }
+  }
+  if (d->nmnrl > 0 && (!d->mnrl_nspec || !d->mnrl_spec || !d->mnrl_stoich || !d->mnrl_logK ||
+                       !d->mnrl_rate_constant || !d->mnrl_activation_energy || !d->mnrl_molar_vol ||
+                       !d->mnrl_affinity_threshold || !d->mnrl_rate_limiter || !d->mnrl_irreversible ||
+                       d->mnrl_stride < 1))
+    return PF_ERR_INVALID;
+  for (int m = 0; m < d->nmnrl; ++m) {
+    if (d->mnrl_nspec[m] < 0 || d->mnrl_nspec[m] > d->mnrl_stride || d->mnrl_nspec[m] > PF_MAX_SPEC_PER_RXN)
+      return PF_ERR_INVALID;
+    for (int s = 0; s < d->mnrl_nspec[m]; ++s) {
+      int k = d->mnrl_spec[m * d->mnrl_stride + s];
+      if (k < 0 || k >= d->ncomp) return PF_ERR_INVALID;
+    }
+  }
+  if (d->opts.maximum_reaction_iterations < 1 || d->opts.maximum_reaction_cuts < 0) return PF_ERR_INVALID;
+  if (d->opts.act_coef_update_frequency < 0 || d->opts.act_coef_update_frequency > 2) return PF_ERR_INVALID;
+  return PF_OK;
+}
+
+int validate_state(const PfNetwork* net, const PfCellState* s) {
+  if (!net || !s) return PF_ERR_INVALID;
+  if (s->ncells < 0) return PF_ERR_INVALID;
+  if (s->ncells == 0) return PF_OK;
+  if (!s->total || !s->pri_molal || !s->pri_act_coef || !s->porosity || !s->saturation || !s->den_kg ||
+      !s->volume)
+    return PF_ERR_INVALID;
+  if (net->dev.ns > 0 && (!s->sec_act_coef || !s->sec_molal)) return PF_ERR_INVALID;
+  if (net->dev.nm > 0 && (!s->mnrl_volfrac || !s->mnrl_area || !s->mnrl_rate)) return PF_ERR_INVALID;
+  if (!net->dev.o.isothermal && !s->temperature) return PF_ERR_INVALID;
+  return PF_OK;
+}
+
+PfLaunchConfig default_launch(const DevNet& dev) {
+  PfLaunchConfig c{};
+  c.threads_per_block = 128;
+  c.blocks_per_sm = 1;
+  c.jac_in_shared = dev.n <= 12 ? 1 : 0;
+  // shrink until one block fits the 227 KB opt-in shared memory
+  while (c.threads_per_block > 32 && batched_smem_bytes(dev, c) > 227u * 1024u) c.threads_per_block -= 32;
+  if (batched_smem_bytes(dev, c) > 227u * 1024u) c.jac_in_shared = 0;
+  return c;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pf_version(void) { return "pfgpu 0.1 (sm_103a, FP64)"; }
+
+int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
+  if (!out) return PF_ERR_INVALID;
+  *out = nullptr;
+  int rc = validate_desc(d);
+  if (rc) return rc;
+  const int n = d->ncomp, ns = d->nsec, nm = d->nmnrl;
+  // CSR rows
+  std::vector<int32_t> ints;
+  std::vector<double> dbls;
+  DevNet dev{};
+  dev.n = n;
+  dev.ns = ns;
+  dev.nm = nm;
+  dev.o_sec_ptr = (int)ints.size();
+  int nnz = 0;
+  for (int i = 0; i < ns; ++i) { ints.push_back(nnz); nnz += d->sec_nspec[i]; }
+  ints.push_back(nnz);
+  dev.nnz_s = nnz;
+  dev.o_sec_idx = (int)ints.size();
+  for (int i = 0; i < ns; ++i)
+    for (int s = 0; s < d->sec_nspec[i]; ++s) ints.push_back(d->sec_spec[i * d->sec_stride + s]);
+  dev.o_mnrl_ptr = (int)ints.size();
+  nnz = 0;
+  for (int m = 0; m < nm; ++m) { ints.push_back(nnz); nnz += d->mnrl_nspec[m]; }
+  ints.push_back(nnz);
+  dev.nnz_m = nnz;
+  dev.o_mnrl_idx = (int)ints.size();
+  for (int m = 0; m < nm; ++m)
+    for (int s = 0; s < d->mnrl_nspec[m]; ++s) ints.push_back(d->mnrl_spec[m * d->mnrl_stride + s]);
+  dev.o_irrev = (int)ints.size();
+  for (int m = 0; m < nm; ++m) ints.push_back(d->mnrl_irreversible[m]);
+  while (ints.size() % 4) ints.push_back(0);
+  auto put = [&](const double* src, int count, double dflt) {
+    int off = (int)dbls.size();
+    for (int k = 0; k < count; ++k) dbls.push_back(src ? src[k] : dflt);
+    return off;
+  };
+  dev.o_sec_nu = (int)dbls.size();
+  for (int i = 0; i < ns; ++i)
+    for (int s = 0; s < d->sec_nspec[i]; ++s) dbls.push_back(d->sec_stoich[i * d->sec_stride + s]);
+  dev.o_sec_logK = put(d->sec_logK, ns, 0.0);
+  dev.o_sec_logKcoef = put(d->sec_logKcoef, 5 * ns, 0.0);
+  dev.o_pri_Z = put(d->pri_Z, n, 0.0);
+  dev.o_pri_a0 = put(d->pri_a0, n, 0.0);
+  dev.o_sec_Z = put(d->sec_Z, ns, 0.0);
+  dev.o_sec_a0 = put(d->sec_a0, ns, 0.0);
+  dev.o_mnrl_nu = (int)dbls.size();
+  for (int m = 0; m < nm; ++m)
+    for (int s = 0; s < d->mnrl_nspec[m]; ++s) dbls.push_back(d->mnrl_stoich[m * d->mnrl_stride + s]);
+  dev.o_mnrl_logK = put(d->mnrl_logK, nm, 0.0);
+  dev.o_mnrl_logKcoef = put(d->mnrl_logKcoef, 5 * nm, 0.0);
+  dev.o_rate = put(d->mnrl_rate_constant, nm, 0.0);
+  dev.o_ea = put(d->mnrl_activation_energy, nm, 0.0);
+  dev.o_molar_vol = put(d->mnrl_molar_vol, nm, 0.0);
+  dev.o_thresh = put(d->mnrl_affinity_threshold, nm, 0.0);
+  dev.o_limiter = put(d->mnrl_rate_limiter, nm, 0.0);
+  dev.o_msf = put(d->mnrl_min_scale_factor, nm, 1.0);
+  dev.o_temkin = put(d->mnrl_Temkin_const, nm, 1.0);
+  dev.o_power = put(d->mnrl_affinity_power, nm, 1.0);
+  while (dbls.size() % 2) dbls.push_back(0.0);
+  dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
+              (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |
+              (d->mnrl_affinity_power ? NETF_POWER : 0);
+  dev.int_words = (int)ints.size();
+  dev.dbl_words = (int)dbls.size();
+  dev.A = d->debyeA;
+  dev.B = d->debyeB;
+  dev.Bdot = d->debyeBdot;
+  dev.o = d->opts;
+  if (!dev.o.isothermal && ((ns > 0 && !d->sec_logKcoef) || (nm > 0 && !d->mnrl_logKcoef)))
+    return PF_ERR_INVALID;
+
+  PfNetwork* net = new (std::nothrow) PfNetwork();
+  if (!net) return PF_ERR_INVALID;
+  const size_t ib = pad16(ints.size() * 4), db = pad16(dbls.size() * 8);
+  cudaError_t e = cudaGetDevice(&net->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&net->num_sms, cudaDevAttrMultiProcessorCount, net->device);
+  if (e == cudaSuccess) e = cudaMalloc(&net->d_tables, ib + db);
+  if (e == cudaSuccess) e = cudaMemcpy(net->d_tables, ints.data(), ints.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy((char*)net->d_tables + ib, dbls.data(), dbls.size() * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&net->d_counters, 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(&net->h_counters, 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&net->d_ctype, PF_MAX_NCOMP * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    pf_network_destroy(net);
+    return PF_ERR_CUDA;
+  }
+  dev.ints = (const int32_t*)net->d_tables;
+  dev.dbls = (const double*)((char*)net->d_tables + ib);
+  net->dev = dev;
+  net->launch = default_launch(dev);
+  *out = net;
+  return PF_OK;
+}
+
+int32_t pf_network_destroy(PfNetwork* net) {
+  if (!net) return PF_ERR_INVALID;
+  if (net->d_tables) cudaFree(net->d_tables);
+  if (net->d_counters) cudaFree(net->d_counters);
+  if (net->h_counters) cudaFreeHost(net->h_counters);
+  if (net->d_arena) cudaFree(net->d_arena);
+  if (net->d_ctype) cudaFree(net->d_ctype);
+  delete net;
+  return PF_OK;
+}
+
+int32_t pf_network_set_options(PfNetwork* net, const PfOptions* opts) {
+  if (!net || !opts) return PF_ERR_INVALID;
+  if (opts->maximum_reaction_iterations < 1 || opts->maximum_reaction_cuts < 0) return PF_ERR_INVALID;
+  if (opts->act_coef_update_frequency < 0 || opts->act_coef_update_frequency > 2) return PF_ERR_INVALID;
+  if (!opts->isothermal && ((net->dev.ns > 0 && !(net->dev.flags & NETF_SEC_LOGKCOEF)) ||
+                            (net->dev.nm > 0 && !(net->dev.flags & NETF_MNRL_LOGKCOEF))))
+    return PF_ERR_INVALID;
+  net->dev.o = *opts;
+  return PF_OK;
+}
+
+int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg) {
+  if (!net || !cfg) return PF_ERR_INVALID;
+  if (cfg->threads_per_block < 32 || cfg->threads_per_block > 256 || cfg->threads_per_block % 32 ||
+      cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 16)
+    return PF_ERR_INVALID;
+  if (batched_smem_bytes(net->dev, *cfg) > 227u * 1024u) return PF_ERR_TOO_LARGE;
+  net->launch = *cfg;
+  return PF_OK;
+}
+
+int32_t pf_network_get_launch(const PfNetwork* net, PfLaunchConfig* cfg) {
+  if (!net || !cfg) return PF_ERR_INVALID;
+  *cfg = net->launch;
+  return PF_OK;
+}
+
+int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel, void* stream,
+                 PfStepStats* stats) {
+  int rc = validate_state(net, state);
+  if (rc) return rc;
+  if (!(dt > 0.0) && !state->dt_cell) return PF_ERR_INVALID;
+  if (kernel != PF_KERNEL_PLAIN && kernel != PF_KERNEL_BATCHED) return PF_ERR_INVALID;
+  if (kernel == PF_KERNEL_BATCHED && !batched_supported(net->dev)) return PF_ERR_UNSUPPORTED;
+  if (state->ncells == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return PF_OK;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(net->d_counters, 0, 8 * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return PF_ERR_CUDA;
+  int lr;
+  if (kernel == PF_KERNEL_PLAIN)
+    lr = launch_rstep_plain(net->dev, *state, dt, net->d_counters + 1, s);
+  else
+    lr = launch_rstep_batched(net->dev, *state, dt, net->launch, net->num_sms, net->d_counters,
+                              net->d_counters + 1, s);
+  if (lr != 0) return PF_ERR_CUDA;
+  if (!stats) return PF_OK;
+  e = cudaMemcpyAsync(net->h_counters, net->d_counters, 8 * sizeof(unsigned long long),
+                      cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return PF_ERR_CUDA;
+  const unsigned long long* h = net->h_counters;
+  stats->cells = state->ncells;
+  stats->newton_iterations = (int64_t)h[1];
+  stats->failed_cells = (int64_t)h[2];
+  stats->max_newton_iterations = (int32_t)h[4];
+  stats->max_substeps = (int32_t)h[5];
+  if (h[3]) return PF_ERR_TIMEOUT;
+  return stats->failed_cells ? PF_CELL_FAILURES : PF_OK;
+}
+
+int32_t pf_update_auxvars(PfNetwork* net, const PfCellState* state, int32_t update_activity_coefs,
+                          void* stream) {
+  int rc = validate_state(net, state);
+  if (rc) return rc;
+  if (update_activity_coefs && (net->dev.ns > 0) && !state->sec_act_coef) return PF_ERR_INVALID;
+  return launch_update_auxvars(net->dev, *state, update_activity_coefs, (cudaStream_t)stream) ? PF_ERR_CUDA
+                                                                                              : PF_OK;
+}
+
+int32_t pf_update_activity_coefs(PfNetwork* net, const PfCellState* state, void* stream) {
+  int rc = validate_state(net, state);
+  if (rc) return rc;
+  return launch_update_activity_coefs(net->dev, *state, (cudaStream_t)stream) ? PF_ERR_CUDA : PF_OK;
+}
+
+int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, const int32_t* ctype,
+                                  const double* cconc, int32_t use_prev, int32_t* iterations, void* stream) {
+  int rc = validate_state(net, state);
+  if (rc) return rc;
+  if (!ctype || !cconc || (net->dev.ns > 0 && !state->sec_act_coef)) return PF_ERR_INVALID;
+  int ncb = 0;
+  for (int j = 0; j < net->dev.n; ++j) {
+    if (ctype[j] < PF_CONSTRAINT_TOTAL || ctype[j] > PF_CONSTRAINT_LOG) return PF_ERR_INVALID;
+    ncb += ctype[j] == PF_CONSTRAINT_CHARGE_BAL;
+  }
+  if (ncb > 1) return PF_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(net->d_ctype, ctype, net->dev.n * sizeof(int32_t), cudaMemcpyHostToDevice, s) !=
+      cudaSuccess)
+    return PF_ERR_CUDA;
+  return pf_equilibrate_constraint_impl(&net->dev, state, net->d_ctype, cconc, use_prev, iterations, 10000,
+                                        stream);
+}
+
+int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t kernel, PfStepStats* stats) {
+  int rc = validate_state(net, h);
+  if (rc) return rc;
+  const int64_t N = h->ncells;
+  if (N == 0) return pf_rstep(net, h, dt, kernel, nullptr, stats);
+  const int n = net->dev.n, ns = net->dev.ns, nm = net->dev.nm;
+  struct Field {
+    void* host;
+    size_t bytes;
+    bool in, out;
+  };
+  const size_t d8 = sizeof(double), i4 = sizeof(int32_t);
+  Field f[] = {
+      {h->total, n * N * d8, true, true},          {h->pri_molal, n * N * d8, true, true},
+      {h->pri_act_coef, n * N * d8, true, true},   {h->sec_act_coef, ns * N * d8, true, true},
+      {h->sec_molal, ns * N * d8, true, true},     {h->mnrl_volfrac, nm * N * d8, true, true},
+      {h->mnrl_area, nm * N * d8, true, false},    {h->mnrl_rate, nm * N * d8, false, true},
+      {(void*)h->porosity, N * d8, true, false},   {(void*)h->saturation, N * d8, true, false},
+      {(void*)h->den_kg, N * d8, true, false},     {(void*)h->volume, N * d8, true, false},
+      {(void*)h->temperature, N * d8, true, false}, {(void*)h->dt_cell, N * d8, true, false},
+      {h->status, N * i4, false, true},            {h->newton_its, N * i4, false, true},
+      {h->num_substeps, N * i4, false, true},
+  };
+  const int nf = sizeof(f) / sizeof(f[0]);
+  size_t need = 0;
+  for (int k = 0; k < nf; ++k)
+    if (f[k].host) need += pad16(f[k].bytes);
+  if (need > net->arena_bytes) {
+    if (net->d_arena) cudaFree(net->d_arena);
+    net->d_arena = nullptr;
+    net->arena_bytes = 0;
+    if (cudaMalloc(&net->d_arena, need) != cudaSuccess) return PF_ERR_CUDA;
+    net->arena_bytes = need;
+  }
+  void* dptr[32];
+  size_t off = 0;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nf; ++k) {
+    dptr[k] = nullptr;
+    if (!f[k].host) continue;
+    dptr[k] = (char*)net->d_arena + off;
+    off += pad16(f[k].bytes);
+    if (f[k].in && f[k].bytes && e == cudaSuccess)
+      e = cudaMemcpyAsync(dptr[k], f[k].host, f[k].bytes, cudaMemcpyHostToDevice, 0);
+  }
+  if (e != cudaSuccess) return PF_ERR_CUDA;
+  PfCellState d = *h;
+  d.total = (double*)dptr[0];
+  d.pri_molal = (double*)dptr[1];
+  d.pri_act_coef = (double*)dptr[2];
+  d.sec_act_coef = (double*)dptr[3];
+  d.sec_molal = (double*)dptr[4];
+  d.mnrl_volfrac = (double*)dptr[5];
+  d.mnrl_area = (double*)dptr[6];
+  d.mnrl_rate = (double*)dptr[7];
+  d.porosity = (const double*)dptr[8];
+  d.saturation = (const double*)dptr[9];
+  d.den_kg = (const double*)dptr[10];
+  d.volume = (const double*)dptr[11];
+  d.temperature = (const double*)dptr[12];
+  d.dt_cell = (const double*)dptr[13];
+  d.status = (int32_t*)dptr[14];
+  d.newton_its = (int32_t*)dptr[15];
+  d.num_substeps = (int32_t*)dptr[16];
+  PfStepStats local{};
+  rc = pf_rstep(net, &d, dt, kernel, nullptr, stats ? stats : &local);
+  if (rc < 0) return rc;
+  for (int k = 0; k < nf; ++k)
+    if (f[k].host && f[k].out && f[k].bytes && e == cudaSuccess)
+      e = cudaMemcpyAsync(f[k].host, dptr[k], f[k].bytes, cudaMemcpyDeviceToHost, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  return e == cudaSuccess ? rc : PF_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,10 @@
+// pfgpu_batched_n8.cu -- batched kernel instantiated for ncomp = 8.
+#include "pfgpu_batched.cuh"
+
+namespace pfgpu {
+int launch_batched_8(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
+                      int num_sms, unsigned long long* queue, unsigned long long* counters,
+                      cudaStream_t stream) {
+  return launch_batched_n<8>(net, st, dt, cfg, num_sms, queue, counters, stream);
+}
+}  // namespace pfgpu

@@ -1,0 +1,100 @@
+// pfgpu_common.cuh -- device-side network tables and shared helpers.
+//
+// A network lives on the device as one packed buffer (see pfgpu_api.cu):
+// reaction rows in CSR form (row pointer, species id, stoichiometry), so the
+// per-secondary species loops read a contiguous, broadcastable slice that a
+// block stages once into shared memory.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/pfgpu.h"
+
+namespace pfgpu {
+
+// pflotran_constants.F90:84 (truncated constant, kept for parity) and :89
+constexpr double LOG_TO_LN = 2.30258509299;
+constexpr double IDEAL_GAS_CONSTANT = 8.31446;
+constexpr double RT_MIN_SATURATION = 1.0e-40;  // reactive_transport_aux.F90:19
+
+enum : int32_t {
+  NETF_SEC_LOGKCOEF = 1,
+  NETF_MNRL_LOGKCOEF = 2,
+  NETF_MSF = 4,
+  NETF_TEMKIN = 8,
+  NETF_POWER = 16,
+};
+
+// Device view of a network.  All pointers index one packed allocation whose
+// layout is: [ints: sec_ptr(ns+1) sec_idx(nnz_s) mnrl_ptr(nm+1) mnrl_idx(nnz_m)
+// irreversible(nm)] [doubles: sec_nu(nnz_s) sec_logK(ns) sec_logKcoef(5ns)
+// pri_Z pri_a0 sec_Z sec_a0 mnrl_nu(nnz_m) mnrl_logK mnrl_logKcoef(5nm)
+// rate_constant activation_energy molar_vol affinity_threshold rate_limiter
+// msf temkin power]
+struct DevNet {
+  int32_t n, ns, nm;
+  int32_t nnz_s, nnz_m;
+  int32_t flags;
+  int32_t int_words;     // number of int32 words in the int block
+  int32_t dbl_words;     // number of doubles in the double block
+  const int32_t* ints;   // device: start of int block (16-byte aligned)
+  const double* dbls;    // device: start of double block (16-byte aligned)
+  // offsets (in elements) into the int block
+  int32_t o_sec_ptr, o_sec_idx, o_mnrl_ptr, o_mnrl_idx, o_irrev;
+  // offsets into the double block
+  int32_t o_sec_nu, o_sec_logK, o_sec_logKcoef, o_pri_Z, o_pri_a0, o_sec_Z, o_sec_a0;
+  int32_t o_mnrl_nu, o_mnrl_logK, o_mnrl_logKcoef, o_rate, o_ea, o_molar_vol, o_thresh,
+      o_limiter, o_msf, o_temkin, o_power;
+  double A, B, Bdot;
+  PfOptions o;
+};
+
+// Table accessor over either global or shared copies of the packed blocks.
+struct Tables {
+  const int32_t* I;
+  const double* D;
+  const DevNet* net;
+  __device__ __forceinline__ int sec_begin(int i) const { return I[net->o_sec_ptr + i]; }
+  __device__ __forceinline__ int sec_end(int i) const { return I[net->o_sec_ptr + i + 1]; }
+  __device__ __forceinline__ int sec_idx(int p) const { return I[net->o_sec_idx + p]; }
+  __device__ __forceinline__ double sec_nu(int p) const { return D[net->o_sec_nu + p]; }
+  __device__ __forceinline__ double sec_logK(int i) const { return D[net->o_sec_logK + i]; }
+  __device__ __forceinline__ const double* sec_logKcoef(int i) const { return D + net->o_sec_logKcoef + 5 * i; }
+  __device__ __forceinline__ double pri_Z(int j) const { return D[net->o_pri_Z + j]; }
+  __device__ __forceinline__ double pri_a0(int j) const { return D[net->o_pri_a0 + j]; }
+  __device__ __forceinline__ double sec_Z(int i) const { return D[net->o_sec_Z + i]; }
+  __device__ __forceinline__ double sec_a0(int i) const { return D[net->o_sec_a0 + i]; }
+  __device__ __forceinline__ int mnrl_begin(int m) const { return I[net->o_mnrl_ptr + m]; }
+  __device__ __forceinline__ int mnrl_end(int m) const { return I[net->o_mnrl_ptr + m + 1]; }
+  __device__ __forceinline__ int mnrl_idx(int p) const { return I[net->o_mnrl_idx + p]; }
+  __device__ __forceinline__ double mnrl_nu(int p) const { return D[net->o_mnrl_nu + p]; }
+  __device__ __forceinline__ double mnrl_logK(int m) const { return D[net->o_mnrl_logK + m]; }
+  __device__ __forceinline__ const double* mnrl_logKcoef(int m) const { return D + net->o_mnrl_logKcoef + 5 * m; }
+  __device__ __forceinline__ double rate(int m) const { return D[net->o_rate + m]; }
+  __device__ __forceinline__ double ea(int m) const { return D[net->o_ea + m]; }
+  __device__ __forceinline__ double molar_vol(int m) const { return D[net->o_molar_vol + m]; }
+  __device__ __forceinline__ double thresh(int m) const { return D[net->o_thresh + m]; }
+  __device__ __forceinline__ double limiter(int m) const { return D[net->o_limiter + m]; }
+  __device__ __forceinline__ int irreversible(int m) const { return I[net->o_irrev + m]; }
+  __device__ __forceinline__ double msf(int m) const { return D[net->o_msf + m]; }
+  __device__ __forceinline__ double temkin(int m) const { return D[net->o_temkin + m]; }
+  __device__ __forceinline__ double power(int m) const { return D[net->o_power + m]; }
+};
+
+// Fortran SIGN(1.d0, x)
+__device__ __forceinline__ double fsign1(double x) { return signbit(x) ? -1.0 : 1.0; }
+
+// ReactionInterpolateLogK, reaction_aux.F90:1285-1312 (one reaction)
+__device__ __forceinline__ double interp_logK(const double* c, double temp) {
+  double tk = temp + 273.15;
+  return c[0] * log(tk) + c[1] + c[2] * tk + c[3] / tk + c[4] / (tk * tk);
+}
+
+// Per-cell SoA accessor
+struct SoA {
+  int64_t N;
+  __device__ __forceinline__ int64_t at(int k, int64_t cell) const { return (int64_t)k * N + cell; }
+};
+
+}  // namespace pfgpu

@@ -1,0 +1,393 @@
+// pfgpu_plain.cu -- the plain GPU form of the operator-split reaction step.
+//
+// One thread per cell, no work queue, no table staging: each thread runs
+// RStep (src/pflotran/reaction.F90:3564-3738) exactly as written -- RReact's
+// Newton loop (:3742-4055) with RTotalAqueous (:4665-4759), RKineticMineral
+// (reaction_mineral.F90:647-1078), RSolve (:5457-5516, back-substituting) and
+// the Crout LU (utility.F90:597-735) -- on per-thread arrays sized for the
+// largest ncomp of its bucket.  It is the baseline the batched kernel is
+// measured against, and a second, independent GPU statement of the algorithm.
+#include "pfgpu_common.cuh"
+#include "pfgpu_kernels.h"
+
+namespace pfgpu {
+namespace plain {
+
+template <int NMAX>
+struct Work {
+  double c[NMAX], total[NMAX], gamma[NMAX], lnc[NMAX], lna[NMAX];
+  double dtotal[NMAX * NMAX];
+  double J[NMAX * NMAX];
+  double res[NMAX], fixed[NMAX], init_total[NMAX], update[NMAX];
+};
+
+struct CellScalars {
+  double porosity, sat, den_kg, volume, temp;
+};
+
+template <int NMAX>
+__device__ void total_aqueous(const Tables& T, int n, int ns, const double* sec_logK,
+                              const double* sec_gamma, double* sec_molal_out, int64_t cell,
+                              const SoA& soa, const CellScalars& cs, Work<NMAX>& w) {
+  const double den_kg_per_L = cs.den_kg * 1.0 * 1.0e-3;
+  for (int j = 0; j < n; ++j) {
+    w.lnc[j] = log(w.c[j]);
+    w.lna[j] = w.lnc[j] + log(w.gamma[j]);
+    w.total[j] = w.c[j];
+  }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) w.dtotal[i * NMAX + j] = (i == j) ? 1.0 : 0.0;
+  for (int i = 0; i < ns; ++i) {
+    const int b = T.sec_begin(i), e = T.sec_end(i);
+    double lnQK = -sec_logK[i] * LOG_TO_LN;
+    for (int p = b; p < e; ++p) lnQK = lnQK + T.sec_nu(p) * w.lna[T.sec_idx(p)];
+    const double g = sec_gamma[soa.at(i, cell)];
+    const double s = exp(lnQK) / g;
+    sec_molal_out[soa.at(i, cell)] = s;
+    for (int p = b; p < e; ++p) {
+      int k = T.sec_idx(p);
+      w.total[k] = w.total[k] + T.sec_nu(p) * s;
+    }
+    for (int pj = b; pj < e; ++pj) {
+      int jc = T.sec_idx(pj);
+      double tempreal = T.sec_nu(pj) * exp(lnQK - w.lnc[jc]) / g;
+      for (int pi = b; pi < e; ++pi) {
+        int ic = T.sec_idx(pi);
+        w.dtotal[ic * NMAX + jc] = w.dtotal[ic * NMAX + jc] + T.sec_nu(pi) * tempreal;
+      }
+    }
+  }
+  for (int j = 0; j < n; ++j) w.total[j] = w.total[j] * den_kg_per_L;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) w.dtotal[i * NMAX + j] = w.dtotal[i * NMAX + j] * den_kg_per_L;
+}
+
+// RKineticMineral without prefactors.  Jac may be null (derivative = false).
+template <int NMAX>
+__device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const double* mnrl_logK,
+                                int64_t cell, const SoA& soa, const PfCellState& st,
+                                const CellScalars& cs, Work<NMAX>& w, double* Res, double* Jac) {
+  const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN,
+             has_pw = net.flags & NETF_POWER;
+  for (int m = 0; m < net.nm; ++m) st.mnrl_rate[soa.at(m, cell)] = 0.0;
+  for (int m = 0; m < net.nm; ++m) {
+    const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
+    double lnQK = -mnrl_logK[m] * LOG_TO_LN;
+    for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * w.lna[T.mnrl_idx(p)];
+    double QK = exp(lnQK);
+    double aff;
+    if (has_tk) {
+      if (has_msf) aff = 1.0 - pow(QK, 1.0 / (T.msf(m) * T.temkin(m)));
+      else aff = 1.0 - pow(QK, 1.0 / T.temkin(m));
+    } else if (has_msf) {
+      aff = 1.0 - pow(QK, 1.0 / T.msf(m));
+    } else {
+      aff = 1.0 - QK;
+    }
+    double sign_ = fsign1(aff);
+    double Im, Im_const, k;
+    const double vf = st.mnrl_volfrac[soa.at(m, cell)];
+    if (vf > 0 || sign_ < 0.0) {
+      if (T.irreversible(m) == 1 && sign_ < 0.0) continue;
+      if (T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m)) continue;
+      if (T.limiter(m) > 0.0) aff = aff / (1.0 + (1.0 - aff) / T.limiter(m));
+      double arr = 1.0;
+      if (T.ea(m) > 0.0)
+        arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (cs.temp + 273.15)));
+      k = T.rate(m) * arr;
+      Im_const = -st.mnrl_area[soa.at(m, cell)];
+      if (has_msf) Im_const = Im_const / T.msf(m);
+      if (has_pw) Im = Im_const * sign_ * pow(fabs(aff), T.power(m)) * k;
+      else Im = Im_const * sign_ * fabs(aff) * k;
+      st.mnrl_rate[soa.at(m, cell)] = Im;
+    } else {
+      continue;
+    }
+    Im_const = Im_const * cs.volume;
+    Im = Im * cs.volume;
+    for (int p = b; p < e; ++p) {
+      int ic = T.mnrl_idx(p);
+      Res[ic] = Res[ic] + T.mnrl_nu(p) * Im;
+    }
+    if (!Jac) continue;
+    double dIm_dQK;
+    if (has_pw) dIm_dQK = -Im * T.power(m) / fabs(aff);
+    else dIm_dQK = -Im_const * k;
+    if (has_tk) {
+      if (has_msf) dIm_dQK = dIm_dQK * (1.0 / (T.msf(m) * T.temkin(m))) / QK * (1.0 - aff);
+      else dIm_dQK = dIm_dQK * (1.0 / T.temkin(m)) / QK * (1.0 - aff);
+    } else if (has_msf) {
+      dIm_dQK = dIm_dQK * (1.0 / T.msf(m)) / QK * (1.0 - aff);
+    }
+    const double rl = T.limiter(m);
+    const double den = 1.0 + (1.0 - aff) / rl;
+    for (int pj = b; pj < e; ++pj) {
+      int jc = T.mnrl_idx(pj);
+      double dQK_dmj = T.mnrl_nu(pj) * QK * exp(-w.lnc[jc]) * cs.den_kg * 1.0e-3;
+      for (int pi = b; pi < e; ++pi) {
+        int ic = T.mnrl_idx(pi);
+        if (rl <= 0.0)
+          Jac[ic * NMAX + jc] = Jac[ic * NMAX + jc] + T.mnrl_nu(pi) * dIm_dQK * dQK_dmj;
+        else
+          Jac[ic * NMAX + jc] = Jac[ic * NMAX + jc] +
+                                T.mnrl_nu(pi) * dIm_dQK * (1.0 + QK / rl / den) * dQK_dmj / den;
+      }
+    }
+  }
+}
+
+// RSolve + LUDecomposition1 + LUBackSubstitution (intended branch).
+template <int NMAX>
+__device__ int rsolve(int n, double* J, const double* conc, const double* Res, double* update,
+                      bool log_form, bool fork_literal) {
+  double rhs[NMAX], VV[NMAX];
+  int indx[NMAX];
+  for (int i = 0; i < n; ++i) {
+    double mx = 0.0;
+    for (int j = 0; j < n; ++j) mx = fmax(mx, fabs(J[i * NMAX + j]));
+    double norm = 1.0 / fmax(1.0, mx);
+    rhs[i] = Res[i] * norm;
+    for (int j = 0; j < n; ++j) J[i * NMAX + j] = J[i * NMAX + j] * norm;
+  }
+  if (log_form)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) J[i * NMAX + j] = J[i * NMAX + j] * conc[j];
+  for (int i = 0; i < n; ++i) {
+    double aamax = 0.0;
+    for (int j = 0; j < n; ++j)
+      if (fabs(J[i * NMAX + j]) > aamax) aamax = fabs(J[i * NMAX + j]);
+    if (aamax <= 0.0) return 1;
+    VV[i] = 1.0 / aamax;
+  }
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < j; ++i) {
+      double sum = J[i * NMAX + j];
+      for (int k = 0; k < i; ++k) sum = sum - J[i * NMAX + k] * J[k * NMAX + j];
+      J[i * NMAX + j] = sum;
+    }
+    double aamax = 0.0;
+    int imax = j;
+    for (int i = j; i < n; ++i) {
+      double sum = J[i * NMAX + j];
+      for (int k = 0; k < j; ++k) sum = sum - J[i * NMAX + k] * J[k * NMAX + j];
+      J[i * NMAX + j] = sum;
+      double dum = VV[i] * fabs(sum);
+      if (dum >= aamax) { imax = i; aamax = dum; }
+    }
+    if (j != imax) {
+      for (int k = 0; k < n; ++k) {
+        double d = J[imax * NMAX + k];
+        J[imax * NMAX + k] = J[j * NMAX + k];
+        J[j * NMAX + k] = d;
+      }
+      VV[imax] = VV[j];
+    }
+    indx[j] = imax;
+    if (J[j * NMAX + j] == 0.0) J[j * NMAX + j] = 1.0e-20;
+    if (j != n - 1) {
+      double dum = 1.0 / J[j * NMAX + j];
+      for (int i = j + 1; i < n; ++i) J[i * NMAX + j] = J[i * NMAX + j] * dum;
+    }
+  }
+  if (fork_literal) return 0;
+  int ii = -1;
+  for (int i = 0; i < n; ++i) {
+    int ll = indx[i];
+    double sum = rhs[ll];
+    rhs[ll] = rhs[i];
+    if (ii >= 0) {
+      for (int j = ii; j < i; ++j) sum = sum - J[i * NMAX + j] * rhs[j];
+    } else if (sum != 0.0) {
+      ii = i;
+    }
+    rhs[i] = sum;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double sum = rhs[i];
+    for (int j = i + 1; j < n; ++j) sum = sum - J[i * NMAX + j] * rhs[j];
+    rhs[i] = sum / J[i * NMAX + i];
+  }
+  for (int i = 0; i < n; ++i) update[i] = rhs[i];
+  return 0;
+}
+
+template <int NMAX>
+__global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellState st, double dt_uniform,
+                                                          unsigned long long* counters) {
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= st.ncells) return;
+  Tables T{net.ints, net.dbls, &net};
+  const SoA soa{st.ncells};
+  const int n = net.n, ns = net.ns, nm = net.nm;
+  const PfOptions& o = net.o;
+  Work<NMAX> w;
+  CellScalars cs{st.porosity[cell], st.saturation[cell], st.den_kg[cell], st.volume[cell],
+                 st.temperature ? st.temperature[cell] : 25.0};
+  // per-cell logK (RUpdateTempDependentCoefs mutates the shared arrays; kept per thread here)
+  double sec_logK[PF_MAX_NSEC], mnrl_logK[PF_MAX_NMNRL];
+  const bool iso = o.isothermal != 0;
+  for (int i = 0; i < ns; ++i)
+    sec_logK[i] = (!iso && (net.flags & NETF_SEC_LOGKCOEF)) ? interp_logK(T.sec_logKcoef(i), cs.temp)
+                                                            : T.sec_logK(i);
+  for (int m = 0; m < nm; ++m)
+    mnrl_logK[m] = (!iso && (net.flags & NETF_MNRL_LOGKCOEF)) ? interp_logK(T.mnrl_logKcoef(m), cs.temp)
+                                                              : T.mnrl_logK(m);
+  for (int j = 0; j < n; ++j) w.gamma[j] = st.pri_act_coef[soa.at(j, cell)];
+  double guess[NMAX], small_val[NMAX];
+  unsigned small_mask = 0;
+  double total_io[NMAX];
+  for (int j = 0; j < n; ++j) {
+    total_io[j] = st.total[soa.at(j, cell)];
+    guess[j] = st.pri_molal[soa.at(j, cell)];
+    if (total_io[j] <= 1.0e-40) {  // RStep floor, reaction.F90:3618-3624
+      small_mask |= 1u << j;
+      small_val[j] = total_io[j];
+      total_io[j] = 1.0e-40;
+    }
+  }
+  if (o.use_total_as_guess)
+    for (int j = 0; j < n; ++j) guess[j] = total_io[j];
+  const double target_time = st.dt_cell ? st.dt_cell[cell] : dt_uniform;
+  double cumulative = 0.0, dt = target_time;
+  int num_cuts = 0, n_const = 0, nsub = 0, its_total = 0, ierror_step = 0;
+  const double psv_t = cs.porosity * cs.sat * 1000.0 * cs.volume;
+  const bool dry = cs.sat < RT_MIN_SATURATION;
+  for (;;) {
+    if (cumulative >= target_time) break;
+    // ------------------------------------------------------------- RReact
+    int ierror = 0, its = 0;
+    double r0 = 0.0;
+    for (int j = 0; j < n; ++j) {
+      w.fixed[j] = dry ? 0.0 : psv_t * total_io[j];
+      w.init_total[j] = total_io[j];
+      w.c[j] = guess[j];
+    }
+    for (;;) {
+      its = its + 1;
+      total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
+      for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
+      if (its > o.maximum_reaction_iterations) {
+        ierror = 1;
+        for (int j = 0; j < n; ++j) total_io[j] = w.init_total[j];
+        break;
+      }
+      if (dry) {
+        for (int j = 0; j < n; ++j) {
+          w.res[j] = (0.0 - w.fixed[j]) / dt;
+          for (int k = 0; k < n; ++k) w.J[j * NMAX + k] = (j == k) ? 1.0 : 0.0;
+        }
+      } else {
+        const double psvd_t = cs.porosity * cs.sat * 1000.0 * cs.volume / dt;
+        for (int j = 0; j < n; ++j) {
+          w.res[j] = (psv_t * w.total[j] - w.fixed[j]) / dt;
+          for (int k = 0; k < n; ++k) w.J[j * NMAX + k] = w.dtotal[j * NMAX + k] * psvd_t;
+        }
+        if (nm > 0) kinetic_mineral<NMAX>(T, net, n, mnrl_logK, cell, soa, st, cs, w, w.res, w.J);
+      }
+      double dot = 0.0, mx = 0.0;
+      for (int j = 0; j < n; ++j) {
+        dot = dot + w.res[j] * w.res[j];
+        mx = fmax(mx, fabs(w.res[j]));
+      }
+      double two_norm = sqrt(dot);
+      if (its == 1) r0 = two_norm;
+      if (mx < o.max_residual_tolerance) break;
+      if (two_norm / r0 < o.max_rel_residual_tolerance) break;
+      if (!o.fork_literal_rsolve || its == 1)
+        for (int j = 0; j < n; ++j) w.update[j] = 0.0;
+      if (rsolve<NMAX>(n, w.J, w.c, w.res, w.update, o.use_log_formulation != 0,
+                       o.fork_literal_rsolve != 0)) {
+        ierror = 1;  // solve_error path: no total restore (reaction.F90:3963-3966)
+        break;
+      }
+      double max_rel = 0.0;
+      double latest[NMAX];
+      if (o.use_log_formulation) {
+        for (int j = 0; j < n; ++j) {
+          double u = fsign1(w.update[j]) * fmin(fabs(w.update[j]), o.max_dlnC_rreact);
+          latest[j] = w.c[j] * exp(-u);
+        }
+      } else {
+        double min_ratio = 1.7976931348623157e308;
+        for (int j = 0; j < n; ++j)
+          if (w.c[j] <= w.update[j]) min_ratio = fmin(min_ratio, fabs(w.c[j] / w.update[j]));
+        for (int j = 0; j < n; ++j) {
+          double u = (min_ratio < 1.0) ? w.update[j] * min_ratio * 0.99 : w.update[j];
+          latest[j] = w.c[j] - u;
+        }
+      }
+      for (int j = 0; j < n; ++j) max_rel = fmax(max_rel, fabs((latest[j] - w.c[j]) / w.c[j]));
+      if (max_rel < o.max_relative_change_tolerance) break;
+      for (int j = 0; j < n; ++j) w.c[j] = latest[j];
+    }
+    if (ierror == 0) {
+      // final RTAuxVarCompute (reaction.F90:4052)
+      total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
+      for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
+    }
+    its_total += its;
+    // ---------------------------------------------------------- RStep control
+    if (ierror != 0) {
+      num_cuts = num_cuts + 1;
+      if (num_cuts > o.maximum_reaction_cuts) {
+        ierror_step = 1;
+        break;
+      }
+      dt = 0.5 * dt;
+      n_const = 0;
+    } else {
+      // RUpdateKineticState -> MineralUpdateKineticState
+      if (nm > 0) {
+        double dummy[NMAX];
+        for (int j = 0; j < n; ++j) dummy[j] = 0.0;
+        kinetic_mineral<NMAX>(T, net, n, mnrl_logK, cell, soa, st, cs, w, dummy, nullptr);
+        for (int m = 0; m < nm; ++m) {
+          double vf = st.mnrl_volfrac[soa.at(m, cell)] + st.mnrl_rate[soa.at(m, cell)] * T.molar_vol(m) * dt;
+          st.mnrl_volfrac[soa.at(m, cell)] = vf < 0.0 ? 0.0 : vf;
+        }
+      }
+      cumulative = cumulative + dt;
+      nsub += 1;
+      n_const += 1;
+      for (int j = 0; j < n; ++j) guess[j] = w.c[j];
+      if (n_const >= 4) {
+        num_cuts = num_cuts - 1;
+        dt = fmin(2.0 * dt, target_time - cumulative);
+      }
+    }
+  }
+  if (!ierror_step)
+    for (int j = 0; j < n; ++j)
+      if (small_mask & (1u << j)) total_io[j] = small_val[j];
+  for (int j = 0; j < n; ++j) {
+    st.total[soa.at(j, cell)] = total_io[j];
+    st.pri_molal[soa.at(j, cell)] = w.c[j];
+  }
+  const int status = ierror_step ? PF_CELL_TOO_MANY_CUTS : PF_CELL_OK;
+  if (st.status) st.status[cell] = status;
+  if (st.newton_its) st.newton_its[cell] = its_total;
+  if (st.num_substeps) st.num_substeps[cell] = nsub;
+  if (counters) {
+    atomicAdd(&counters[0], (unsigned long long)its_total);
+    if (status) atomicAdd(&counters[1], 1ull);
+    atomicMax(&counters[3], (unsigned long long)its_total);
+    atomicMax(&counters[4], (unsigned long long)nsub);
+  }
+}
+
+}  // namespace plain
+
+int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
+                       unsigned long long* counters, cudaStream_t stream) {
+  const int tpb = 128;
+  const int64_t blocks = (st.ncells + tpb - 1) / tpb;
+  if (blocks == 0) return 0;
+  if (net.n <= 4) plain::rstep_plain_kernel<4><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else if (net.n <= 8) plain::rstep_plain_kernel<8><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else if (net.n <= 12) plain::rstep_plain_kernel<12><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else if (net.n <= 16) plain::rstep_plain_kernel<16><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else plain::rstep_plain_kernel<24><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace pfgpu

@@ -30,6 +30,12 @@ PF_ACT_COEF_ALGO_NEWTON = 1
 PF_KERNEL_PLAIN = 0
 PF_KERNEL_BATCHED = 1
 
+PF_CONSTRAINT_TOTAL = 1
+PF_CONSTRAINT_FREE = 2
+PF_CONSTRAINT_PH = 3
+PF_CONSTRAINT_CHARGE_BAL = 4
+PF_CONSTRAINT_LOG = 5
+
 PF_MAX_NCOMP = 24
 PF_MAX_NSEC = 96
 PF_MAX_NMNRL = 16
@@ -118,9 +124,12 @@ SIGNATURES = {
     "pf_update_activity_coefs": (C.c_int32, [_P, C.POINTER(PfCellState), _P]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
                                   C.POINTER(PfStepStats)]),
+    "pf_equilibrate_constraint": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(C.c_int32),
+                                              _P, C.c_int32, _P, _P]),
     "pf_network_set_launch": (C.c_int32, [_P, C.POINTER(PfLaunchConfig)]),
     "pf_network_get_launch": (C.c_int32, [_P, C.POINTER(PfLaunchConfig)]),
     "pf_version": (C.c_char_p, []),
+    "pf_bench_fp64_fma": (C.c_int32, [_P, C.c_int64, C.c_int32, C.c_int32, _P]),
 }
 
 _lib = None

@@ -1,0 +1,59 @@
+"""Algorithmic FP64 work of the reference's RReact iteration.
+
+Counts the floating-point operations the reference performs per Newton
+iteration (src/pflotran/reaction.F90 RReact :3851-4045 with RTotalAqueous
+:4665-4759, RTAccumulation[Derivative] :5710-5848, RKineticMineral
+reaction_mineral.F90:647-1078 without prefactors, RSolve :5457-5516 and the
+Crout LU utility.F90:597-735): add/sub/mul/div each 1, a fused multiply-add 2,
+sqrt 1.  exp/log/pow calls are counted separately as transcendentals.
+These are the units of the FP64 roofline ("algorithmic flops"); the counting
+build of the oracle measures the same quantity by instrumenting every
+operation (tests/test_flops.py checks that the two agree).
+"""
+from __future__ import annotations
+
+
+def per_iteration(net, mineral_active=None):
+    """(flops, transcendentals) of one RReact Newton iteration that goes on
+    to the solve and update (the common case)."""
+    n = net.ncomp
+    s = [int(net.sec_nspec[i]) for i in range(net.nsec)]
+    t = [int(net.mnrl_nspec[m]) for m in range(net.nmnrl)]
+    act = mineral_active if mineral_active is not None else [True] * len(t)
+    f = 0
+    tr = 0
+    # RTotalAqueous
+    tr += 2 * n
+    f += n
+    for si in s:
+        f += 1 + 2 * si + 1 + 2 * si + si * 3 + 2 * si * si
+        tr += 1 + si
+    f += n + n * n
+    # RTAccumulation, derivative, residual
+    f += 3 + n + 4 + n * n + 2 * n
+    # RKineticMineral
+    tr += 2 * n
+    f += n
+    for ti, a in zip(t, act):
+        f += 1 + 2 * ti + 1
+        tr += 1
+        if a:
+            f += 1 + 3 + 2 + 2 * ti + 1 + 4 * ti + 3 * ti * ti
+            tr += ti
+    # norms and tests
+    f += 2 * n + 1 + 1
+    # RSolve scaling
+    f += n + n + 2 * n * n
+    # LU
+    f += n
+    for j in range(n):
+        f += sum(2 * i for i in range(j))
+        f += sum(2 * j + 1 for _ in range(j, n))
+        f += (n - 1 - j)
+    f += n - 1
+    # back substitution
+    f += sum(2 * i for i in range(n)) + sum(2 * (n - 1 - i) + 1 for i in range(n))
+    # update + relative change
+    f += 3 * n + 2 * n
+    tr += n
+    return f, tr

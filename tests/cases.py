@@ -1,0 +1,63 @@
+"""Parity cases: seeded networks + cells equilibrated by the oracle's
+constraint restatement (reaction.F90:1328-2115 subset), with the reference's
+initial auxvar sequence (condition_control.F90:1638-1649) and one TIMESTEP
+activity refresh (pm_osrt.F90:145-151), i.e. the state the operator-split
+cell loop sees at the start of a step.
+"""
+import numpy as np
+
+from pfgpu import abi, generate
+from pfgpu.network import CellState, default_options, tight_options
+
+
+def prepare(oracle, net, st, ctype, cconc):
+    rc, its = oracle.equilibrate(net, st, ctype, cconc, nthreads=8)
+    ok = its > 0
+    st = st.subset(np.nonzero(ok)[0])
+    den = st.a["den_kg"]
+    st.a["pri_molal"][:] = st.a["pri_molal"] * den / 1000.0 / den * 1000.0
+    st.a["pri_act_coef"][:] = 1.0
+    st.a["sec_act_coef"][:] = 1.0
+    st.a["sec_molal"][:] = 0.0
+    oracle.update_auxvars(net, st, False, nthreads=8)
+    if net.options["act_coef_update_frequency"] != abi.PF_ACT_COEF_OFF:
+        oracle.update_auxvars(net, st, True, nthreads=8)
+        oracle.update_auxvars(net, st, True, nthreads=8)
+        oracle.update_auxvars(net, st, False, nthreads=8)
+        oracle.update_activity_coefs(net, st, nthreads=8)
+    return st, int((~ok).sum())
+
+
+_CACHE = {}
+
+
+def case(oracle, name, tight=False):
+    key = (name, tight)
+    if key in _CACHE:
+        net, st = _CACHE[key]
+        return net, st.copy()
+    mk = tight_options if tight else default_options
+    if name == "calcite":
+        net = generate.calcite_network(mk())
+        st, ct, cc = generate.calcite_cells(net, 1000, seed=20261203)
+        dt = 3600.0
+    elif name == "random12":
+        net = generate.random_network(12, 40, 6, seed=12, options=mk(isothermal=0))
+        st, ct, cc = generate.random_cells(net, 1500, seed=1212)
+        dt = 86400.0
+    elif name.startswith("hetero"):
+        n = int(name[6:])
+        net = generate.random_network(n, 3 * n, max(1, n // 2), seed=700 + n, options=mk(isothermal=0))
+        st, ct, cc = generate.random_cells(net, 400, seed=7000 + n, dt_range=(3600.0, 30 * 86400.0))
+        dt = 86400.0
+    else:
+        raise KeyError(name)
+    st, nfail = prepare(oracle, net, st, ct, cc)
+    assert nfail < 0.05 * len(ct and cc[0]), (name, nfail)
+    _CACHE[key] = (net, st)
+    return net, st.copy()
+
+
+CASE_DT = {"calcite": 3600.0, "random12": 86400.0}
+CASE_DT.update({"hetero%d" % n: 86400.0 for n in (4, 6, 8, 10, 12, 16, 20, 24)})
+HETERO = (4, 6, 8, 10, 12, 16, 20, 24)

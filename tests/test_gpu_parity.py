@@ -1,0 +1,188 @@
+"""GPU parity: both kernel forms against the CPU oracle on identical inputs.
+
+Quantities and tolerances (FP64 throughout):
+  pri_molal, sec_molal        1e-10 relative
+  total                       1e-10 relative to the component's gross scale
+                              den*(m_k + sum_i |nu_ik| s_i) (totals can cancel)
+  mnrl_rate                   1e-10 relative to max(|rate|, 1e-30)
+  mnrl_volfrac                1e-10 relative to max(volfrac, 1e-30)
+  status, num_substeps        exact
+Cells whose Newton iteration count differs from the oracle's ("flips": the
+last relative change sat within rounding of the 1e-6 exit test) are counted
+and reported; they may differ by up to the unapplied final update (<= 1e-6
+relative) and must stay below 2 % of the cells.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from pfgpu import abi
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+REL = 1.0e-10
+OUT = os.environ.get("PFGPU_PARITY_OUT", os.path.join(os.path.dirname(os.path.dirname(__file__)),
+                                                       "gpurun_out"))
+_report = {}
+
+
+def _engine(net):
+    from pfgpu.engine import ReactionEngine
+    return ReactionEngine(net)
+
+
+def _gross_total(net, st):
+    """den*(m_k + sum_i |nu_ik| s_i): the scale of total_k before cancellation."""
+    g = st.a["pri_molal"].copy()
+    for i in range(net.nsec):
+        for s in range(net.sec_nspec[i]):
+            g[net.sec_spec[i, s]] += abs(net.sec_stoich[i, s]) * st.a["sec_molal"][i]
+    return g * st.a["den_kg"] * 1e-3
+
+
+def compare(net, ref, got, label):
+    """Returns (max errors dict, flips, mask of cells compared)."""
+    its_r, its_g = ref.a["newton_its"], got.a["newton_its"]
+    same = (its_r == its_g) & (ref.a["status"] == 0)
+    flips = int((its_r != its_g).sum())
+    errs = {}
+
+    def rel(a, b, scale):
+        return float(np.max(np.abs(a - b)[..., same] / scale[..., same])) if same.any() else 0.0
+
+    errs["pri_molal"] = rel(got.a["pri_molal"], ref.a["pri_molal"], np.abs(ref.a["pri_molal"]))
+    if net.nsec:
+        errs["sec_molal"] = rel(got.a["sec_molal"], ref.a["sec_molal"],
+                                np.maximum(np.abs(ref.a["sec_molal"]), 1e-300))
+    errs["total"] = rel(got.a["total"], ref.a["total"], _gross_total(net, ref))
+    if net.nmnrl:
+        errs["mnrl_rate"] = rel(got.a["mnrl_rate"], ref.a["mnrl_rate"],
+                                np.maximum(np.abs(ref.a["mnrl_rate"]), 1e-30))
+        errs["mnrl_volfrac"] = rel(got.a["mnrl_volfrac"], ref.a["mnrl_volfrac"],
+                                   np.maximum(np.abs(ref.a["mnrl_volfrac"]), 1e-30))
+    _report[label] = dict(cells=int(ref.ncells), compared=int(same.sum()), flips=flips,
+                          failed_ref=int((ref.a["status"] != 0).sum()),
+                          failed_gpu=int((got.a["status"] != 0).sum()),
+                          its_mean=float(its_r.mean()), its_max=int(its_r.max()),
+                          substeps_max=int(ref.a["num_substeps"].max()), max_rel_err=errs)
+    return errs, flips, same
+
+
+def run_pair(oracle, name, kernel, tight=False):
+    net, st0 = cases.case(oracle, name, tight=tight)
+    dt = cases.CASE_DT[name]
+    ref = st0.copy()
+    oracle.rstep(net, ref, dt, nthreads=8)
+    eng = _engine(net)
+    dev = st0.to("cuda")
+    stats = eng.rstep(dev, dt, kernel=kernel)
+    torch.cuda.synchronize()
+    got = dev.numpy()
+    return net, ref, got, stats
+
+
+@pytest.mark.parametrize("kernel", [abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED], ids=["plain", "batched"])
+@pytest.mark.parametrize("name", ["calcite", "random12"] + ["hetero%d" % n for n in cases.HETERO])
+def test_rstep_parity(oracle, name, kernel):
+    net, ref, got, stats = run_pair(oracle, name, kernel)
+    label = "%s/%s" % (name, "plain" if kernel == 0 else "batched")
+    errs, flips, same = compare(net, ref, got, label)
+    n = ref.ncells
+    assert flips <= max(2, 0.02 * n), (label, flips)
+    for k, v in errs.items():
+        assert v < REL, (label, k, v, errs)
+    np.testing.assert_array_equal(got.a["status"][same], ref.a["status"][same])
+    np.testing.assert_array_equal(got.a["num_substeps"][same], ref.a["num_substeps"][same])
+    assert stats["failed_cells"] == int((got.a["status"] != 0).sum())
+    assert stats["newton_iterations"] == int(got.a["newton_its"].sum())
+    assert stats["max_newton_iterations"] == int(got.a["newton_its"].max())
+
+
+@pytest.mark.parametrize("name", ["calcite", "random12", "hetero16"])
+def test_rstep_parity_tight(oracle, name):
+    """Tight tolerances: every solve converges to rounding level, separating
+    arithmetic error from stopping-rule noise."""
+    net, ref, got, stats = run_pair(oracle, name, abi.PF_KERNEL_BATCHED, tight=True)
+    errs, flips, same = compare(net, ref, got, name + "/batched/tight")
+    ok = (ref.a["status"] == 0) & (got.a["status"] == 0)
+    m = ok
+    e = np.max(np.abs(got.a["pri_molal"] - ref.a["pri_molal"])[:, m] / ref.a["pri_molal"][:, m])
+    assert e < REL, (name, e)
+
+
+def test_rstep_host_path_matches_device(oracle):
+    net, st0 = cases.case(oracle, "calcite")
+    eng = _engine(net)
+    dev = st0.to("cuda")
+    eng.rstep(dev, 3600.0)
+    host = st0.copy()
+    eng.rstep_host(host, 3600.0)
+    d = dev.numpy()
+    for k in ("total", "pri_molal", "sec_molal", "mnrl_rate", "mnrl_volfrac", "newton_its"):
+        np.testing.assert_array_equal(host.a[k], d.a[k])
+
+
+def test_zero_cells_and_bad_args(oracle):
+    net, st0 = cases.case(oracle, "calcite")
+    eng = _engine(net)
+    empty = st0.subset(np.arange(0)).to("cuda")
+    st = eng.rstep(empty, 3600.0)
+    assert st["cells"] == 0
+    dev = st0.to("cuda")
+    with pytest.raises(abi.PfError):
+        eng.rstep(dev, -1.0)
+    with pytest.raises(abi.PfError):
+        eng.rstep(dev, 3600.0, kernel=7)
+
+
+def test_dry_and_floored_cells(oracle):
+    """Saturation below rt_min_saturation (reactive_transport_aux.F90:19) and
+    totals <= 1e-40 (RStep floor, reaction.F90:3618-3631) follow the oracle."""
+    net, st0 = cases.case(oracle, "calcite")
+    st0 = st0.subset(np.arange(64))
+    st0.a["saturation"][:8] = 0.0
+    st0.a["total"][1, 8:16] = -1.0e-3  # negative HCO3- total: floored, then restored
+    ref = st0.copy()
+    oracle.rstep(net, ref, 3600.0)
+    for kernel in (abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED):
+        eng = _engine(net)
+        dev = st0.to("cuda")
+        eng.rstep(dev, 3600.0, kernel=kernel)
+        got = dev.numpy()
+        np.testing.assert_array_equal(got.a["status"], ref.a["status"])
+        same = got.a["newton_its"] == ref.a["newton_its"]
+        np.testing.assert_allclose(got.a["total"][:, same], ref.a["total"][:, same], rtol=1e-10, atol=1e-25)
+        np.testing.assert_allclose(got.a["pri_molal"][:, same], ref.a["pri_molal"][:, same], rtol=1e-10)
+
+
+def test_failing_cells_report_status(oracle):
+    """Cells that cannot converge: RStep cuts dt maximum_reaction_cuts times
+    and reports ierror = 1 (reaction.F90:3657-3666); both forms agree with
+    the oracle on which cells fail and how many Newton iterations they spent."""
+    net, st0 = cases.case(oracle, "calcite")
+    st0 = st0.subset(np.arange(32))
+    net2 = net.with_options(maximum_reaction_iterations=2, maximum_reaction_cuts=3)
+    ref = st0.copy()
+    oracle.rstep(net2, ref, 3600.0)
+    assert (ref.a["status"] != 0).any()
+    for kernel in (abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED):
+        eng = _engine(net2)
+        dev = st0.to("cuda")
+        stats = eng.rstep(dev, 3600.0, kernel=kernel)
+        got = dev.numpy()
+        np.testing.assert_array_equal(got.a["status"], ref.a["status"])
+        np.testing.assert_array_equal(got.a["newton_its"], ref.a["newton_its"])
+        assert stats["failed_cells"] == int((ref.a["status"] != 0).sum())
+
+
+def test_write_parity_report():
+    """Writes the per-case error/flip/iteration summary collected above."""
+    if not _report:
+        pytest.skip("no parity cases ran")
+    os.makedirs(OUT, exist_ok=True)
+    with open(os.path.join(OUT, "parity_report.json"), "w") as f:
+        json.dump(_report, f, indent=1, sort_keys=True)
