@@ -245,6 +245,7 @@ def main():
     ap.add_argument("--cells", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -271,6 +272,12 @@ def main():
     log("state built: %d cells in %.1f s" % (ncells, time.perf_counter() - t_build))
     pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}
     dt = cfg["dt"]
+    tuned = None
+    if not args.no_tune:
+        from pfgpu import autotune
+        best, table = autotune.tune(eng, dev, dt, use_cache=False)
+        tuned = {"best": best, "top": table[:6]}
+        log("autotune:", json.dumps(tuned))
 
     # one instrumented step: iteration statistics for the flop count
     stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
@@ -348,7 +355,7 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single-gpu",
                            "l2": "state %.2f GB > L2; state reset D2D each step" % (state_bytes / 1e9),
                            "kernel": "batched persistent (PF_KERNEL_BATCHED)",
-                           "launch": eng.launch_config()},
+                           "launch": eng.launch_config(), "autotune": tuned},
                 "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
                 "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
                 "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},

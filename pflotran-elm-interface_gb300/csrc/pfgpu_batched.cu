@@ -14,7 +14,7 @@ namespace pfgpu {
 PF_BATCHED_NCOMPS(PF_DECL)
 #undef PF_DECL
 
-static size_t lane_doubles(int n, bool js) { return (js ? (size_t)n * n : 0) + 8 * (size_t)n; }
+static size_t lane_doubles(int n, bool js) { return (js ? (size_t)n * n : 0) + 3 * (size_t)n; }
 
 size_t batched_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg) {
   const size_t tables = (size_t)net.int_words * 4 + (size_t)net.dbl_words * 8;

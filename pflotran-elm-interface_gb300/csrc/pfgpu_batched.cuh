@@ -56,14 +56,12 @@ struct Lane {
   }
   static constexpr int OFF = JS ? N * N : 0;
   __device__ __forceinline__ double& lna(int j) { return base[(OFF + j) * stride]; }
+  // S (secondary sums, live during the evaluation) and VV (pivot scales, live
+  // during the factorisation) share one slot
   __device__ __forceinline__ double& S(int j) { return base[(OFF + N + j) * stride]; }
+  __device__ __forceinline__ double& VV(int j) { return base[(OFF + N + j) * stride]; }
   __device__ __forceinline__ double& rhs(int j) { return base[(OFF + 2 * N + j) * stride]; }
-  __device__ __forceinline__ double& VV(int j) { return base[(OFF + 3 * N + j) * stride]; }
-  __device__ __forceinline__ double& fixed(int j) { return base[(OFF + 4 * N + j) * stride]; }
-  __device__ __forceinline__ double& init_tot(int j) { return base[(OFF + 5 * N + j) * stride]; }
-  __device__ __forceinline__ double& guess(int j) { return base[(OFF + 6 * N + j) * stride]; }
-  __device__ __forceinline__ double& small_val(int j) { return base[(OFF + 7 * N + j) * stride]; }
-  static constexpr int DOUBLES = OFF + 8 * N;
+  static constexpr int DOUBLES = OFF + 3 * N;
 };
 
 // Crout LU with implicit partial pivoting (utility.F90:597-688) on the lane's
@@ -204,6 +202,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
   int phase = NEED;
   long long cell = -1;
   double c[N], lnc[N], lng[N], tot[N];
+  double fixed[N], init_tot[N], guess[N], small_val[N];
   double lnKeff[PF_MAX_NSEC];
   double lnKm[PF_MAX_NMNRL], rate[PF_MAX_NMNRL], vf[PF_MAX_NMNRL];
   double psv = 0, den_L = 0, den_k = 0, volume = 0, target = 0, cum = 0, dt = 0, inv_dt = 0, r0 = 0;
@@ -240,16 +239,16 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
             double t = st.total[soa.at(j, cell)];
             if (t <= 1.0e-40) {  // RStep floor (reaction.F90:3618-3624)
               small_mask |= 1u << j;
-              L.small_val(j) = t;
+              small_val[j] = t;
               t = 1.0e-40;
             }
             tot[j] = t;
-            L.guess(j) = st.pri_molal[soa.at(j, cell)];
+            guess[j] = st.pri_molal[soa.at(j, cell)];
             lng[j] = log(st.pri_act_coef[soa.at(j, cell)]);
           }
           if (o.use_total_as_guess) {
 #pragma unroll
-            for (int j = 0; j < N; ++j) L.guess(j) = tot[j];
+            for (int j = 0; j < N; ++j) guess[j] = tot[j];
           }
           const double tk = temp + 273.15;
           const bool tsec = !iso && (net.flags & NETF_SEC_LOGKCOEF);
@@ -275,7 +274,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           n_const = 0;
           zero_step = !(cum < target);  // nothing to integrate: write back as is
 #pragma unroll
-          for (int j = 0; j < N; ++j) c[j] = L.guess(j);
+          for (int j = 0; j < N; ++j) c[j] = guess[j];
         }
       }
     }
@@ -292,9 +291,9 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
     if (phase == START) {
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        L.fixed(j) = dry ? 0.0 : psv * tot[j];
-        L.init_tot(j) = tot[j];
-        c[j] = L.guess(j);
+        fixed[j] = dry ? 0.0 : psv * tot[j];
+        init_tot[j] = tot[j];
+        c[j] = guess[j];
         lnc[j] = log(c[j]);
       }
       its = 0;
@@ -366,7 +365,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
 #pragma unroll
       for (int j = 0; j < N; ++j) {
         tot[j] = (c[j] + L.S(j)) * den_L;
-        L.rhs(j) = dry ? -L.fixed(j) * inv_dt : (psv * tot[j] - L.fixed(j)) * inv_dt;
+        L.rhs(j) = dry ? -fixed[j] * inv_dt : (psv * tot[j] - fixed[j]) * inv_dt;
       }
       if (dry) {
 #pragma unroll
@@ -454,7 +453,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
       int react_end = -1;  // -1: continue, 0: converged, 1: failed
       if (its > o.maximum_reaction_iterations) {
 #pragma unroll
-        for (int j = 0; j < N; ++j) tot[j] = L.init_tot(j);
+        for (int j = 0; j < N; ++j) tot[j] = init_tot[j];
         react_end = 1;
       } else if (mx < o.max_residual_tolerance || two_norm < o.max_rel_residual_tolerance * r0) {
         react_end = 0;
@@ -521,7 +520,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           nsub += 1;
           n_const += 1;
 #pragma unroll
-          for (int j = 0; j < N; ++j) L.guess(j) = c[j];
+          for (int j = 0; j < N; ++j) guess[j] = c[j];
           if (n_const >= 4) {
             num_cuts = num_cuts - 1;
             dt = fmin(2.0 * dt, target - cum);
@@ -537,7 +536,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
       if (!cell_failed) {
 #pragma unroll
         for (int j = 0; j < N; ++j)
-          if (small_mask & (1u << j)) tot[j] = L.VV(j);
+          if (small_mask & (1u << j)) tot[j] = small_val[j];
       }
 #pragma unroll
       for (int j = 0; j < N; ++j) {

@@ -1,0 +1,86 @@
+"""Launch-configuration autotuner for the batched step kernel.
+
+For one network and a sample of its cells, times every configuration the
+library accepts -- threads per block (32..256), resident blocks per SM
+(1..4), Jacobian in shared or local memory -- with CUDA events on the
+launching stream, restoring the sample before each launch, and installs the
+fastest with pf_network_set_launch.  Results are cached per (GPU, network
+shape) in autotune_cache.json next to this file.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+
+from . import abi
+from .network import CellState
+
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "autotune_cache.json")
+MUTABLE = ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
+           "mnrl_rate", "status", "newton_its", "num_substeps")
+
+
+def network_key(eng) -> str:
+    import torch
+    net = eng.net
+    h = hashlib.sha1()
+    for a in (net.sec_nspec, net.sec_spec, net.mnrl_nspec, net.mnrl_spec):
+        h.update(a.tobytes())
+    return "%s|n%d|s%d|m%d|%s" % (torch.cuda.get_device_name(), net.ncomp, net.nsec, net.nmnrl,
+                                  h.hexdigest()[:12])
+
+
+def candidates():
+    for js in (1, 0):
+        for tpb in range(32, 257, 32):
+            for bps in (1, 2, 3, 4):
+                yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=js)
+
+
+def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2, use_cache: bool = True,
+         verbose: bool = False):
+    import torch
+    key = network_key(eng)
+    cache = {}
+    if use_cache and os.path.exists(CACHE):
+        try:
+            cache = json.load(open(CACHE))
+        except Exception:
+            cache = {}
+    if use_cache and key in cache:
+        cfg = cache[key]["best"]
+        if eng.set_launch_config(**cfg) == abi.PF_OK:
+            return cfg, cache[key]["table"]
+    n = min(state.ncells, max_cells)
+    sample = state.subset(torch.arange(n, device=state.a["porosity"].device))
+    pristine = {k: sample.a[k].clone() for k in MUTABLE if k in sample.a}
+    table = []
+    for cfg in candidates():
+        if eng.set_launch_config(**cfg) != abi.PF_OK:
+            continue
+        best = None
+        for _ in range(reps + 1):
+            for k, v in pristine.items():
+                sample.a[k].copy_(v)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            eng.rstep(sample, dt, stats=False)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        table.append(dict(cfg, ms=best))
+        if verbose:
+            print(cfg, "%.3f ms" % best)
+    table.sort(key=lambda r: r["ms"])
+    top = {k: table[0][k] for k in ("threads_per_block", "blocks_per_sm", "jac_in_shared")}
+    eng.set_launch_config(**top)
+    for k, v in pristine.items():
+        sample.a[k].copy_(v)
+    cache[key] = {"best": top, "table": table[:12], "cells": n}
+    try:
+        json.dump(cache, open(CACHE, "w"), indent=1)
+    except OSError:
+        pass
+    return top, table

@@ -11,7 +11,10 @@ from pfgpu.network import CellState, default_options, tight_options
 
 
 def prepare(oracle, net, st, ctype, cconc):
-    rc, its = oracle.equilibrate(net, st, ctype, cconc, nthreads=8)
+    # constraints always equilibrate with the reference's default tolerances
+    eq = net.with_options(max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12,
+                          max_rel_residual_tolerance=1e-8)
+    rc, its = oracle.equilibrate(eq, st, ctype, cconc, nthreads=8)
     ok = its > 0
     st = st.subset(np.nonzero(ok)[0])
     den = st.a["den_kg"]
