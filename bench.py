@@ -150,7 +150,7 @@ def fp64_peak(lib, device_sms):
     return best
 
 
-def time_steps(eng, dev, pristine, dt, kernel, steps, warmup):
+def time_steps(eng, dev, pristine, dt, kernel, steps, warmup, order=None):
     import torch
     from pfgpu import abi  # noqa: F401
 
@@ -161,7 +161,7 @@ def time_steps(eng, dev, pristine, dt, kernel, steps, warmup):
 
     for _ in range(warmup):
         reset()
-        eng.rstep(dev, dt, kernel=kernel, stats=False)
+        eng.rstep(dev, dt, kernel=kernel, stats=False, order=order)
     torch.cuda.synchronize()
     ks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -169,7 +169,7 @@ def time_steps(eng, dev, pristine, dt, kernel, steps, warmup):
     for a, b in ks:
         reset()
         a.record()
-        eng.rstep(dev, dt, kernel=kernel, stats=False)
+        eng.rstep(dev, dt, kernel=kernel, stats=False, order=order)
         b.record()
     t1.record()
     torch.cuda.synchronize()
@@ -282,6 +282,9 @@ def main():
     # one instrumented step: iteration statistics for the flop count
     stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
     its_mean = stats["newton_iterations"] / ncells
+    # work-queue order for the timed steps: descending Newton count of the
+    # previous step (here the instrumented one), longest cells first
+    order = torch.argsort(dev.a["newton_its"].to(torch.int64), descending=True)
     for k in pristine:
         dev.a[k].copy_(pristine[k])
 
@@ -289,7 +292,9 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        total_ms, kern_ms = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, args.steps, args.warmup)
+        total_ms, kern_ms = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, args.steps, args.warmup,
+                                       order=order)
+    nat_total, nat_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, max(1, min(args.steps, 3)), 1)
     if dist:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -355,10 +360,13 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single-gpu",
                            "l2": "state %.2f GB > L2; state reset D2D each step" % (state_bytes / 1e9),
                            "kernel": "batched persistent (PF_KERNEL_BATCHED)",
+                           "cell_order": "descending Newton count of the previous step",
                            "launch": eng.launch_config(), "autotune": tuned},
                 "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
                 "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
                 "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},
+                "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),
+                                  "kernel_ms": float(np.mean(nat_kern))},
                 "speedup_vs_plain_gpu": value / plain_value,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "gpu_launches": args.steps}

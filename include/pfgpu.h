@@ -164,6 +164,10 @@ typedef struct PfCellState {
   int32_t* status;        /* [1] out: PF_CELL_*                                */
   int32_t* newton_its;    /* [1] out: Newton iterations summed over substeps   */
   int32_t* num_substeps;  /* [1] out                                           */
+  const int64_t* cell_order; /* optional permutation of 0..ncells-1: the order in
+                              which the batched kernel's work queue hands out
+                              cells (e.g. descending previous iteration count);
+                              NULL = natural order.  Results do not depend on it. */
 } PfCellState;
 
 typedef struct PfStepStats {
@@ -185,6 +189,10 @@ int32_t pf_network_destroy(PfNetwork* net);
 /* Copy of the descriptor's options; lets a caller change tolerances without
  * re-uploading tables (e.g. the tight mode of the parity tests). */
 int32_t pf_network_set_options(PfNetwork* net, const PfOptions* opts);
+/* Pre-allocates the per-cell scratch of the batched kernel for up to ncells
+ * cells (pf_rstep grows it on demand otherwise; call this before capturing
+ * pf_rstep into a CUDA graph, since allocation cannot be captured). */
+int32_t pf_network_reserve(PfNetwork* net, int64_t ncells);
 
 /* ------------------------------------------------------------ operator split */
 /*

@@ -20,6 +20,8 @@ struct PfNetwork {
   unsigned long long* d_counters = nullptr;  // [0] queue [1] its [2] fails [3] err [4] max its [5] max substeps
   unsigned long long* h_counters = nullptr;  // pinned mirror
   int32_t* d_ctype = nullptr;                // constraint types [PF_MAX_NCOMP]
+  double* d_scratch = nullptr;               // batched kernel per-cell scratch
+  size_t scratch_cap = 0;                    // doubles
   PfLaunchConfig launch{};
   int device = 0;
   int num_sms = 0;
@@ -129,6 +131,54 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
     for (int s = 0; s < d->mnrl_nspec[m]; ++s) ints.push_back(d->mnrl_spec[m * d->mnrl_stride + s]);
   dev.o_irrev = (int)ints.size();
   for (int m = 0; m < nm; ++m) ints.push_back(d->mnrl_irreversible[m]);
+  // product-form tables
+  int neg_mask = 0;
+  auto code_of = [&](double nu, int k) -> int {
+    if (nu == 1.0) return k;
+    if (nu == 2.0) return n + k;
+    if (nu == -1.0) { neg_mask |= 1 << k; return 2 * n + k; }
+    if (nu == -2.0) { neg_mask |= 1 << k; return 3 * n + k; }
+    return -1;
+  };
+  dev.o_sec_pidx = (int)ints.size();
+  for (int i = 0; i < ns; ++i)
+    for (int s2 = 0; s2 < d->sec_nspec[i]; ++s2)
+      ints.push_back(code_of(d->sec_stoich[i * d->sec_stride + s2], d->sec_spec[i * d->sec_stride + s2]));
+  std::vector<int32_t> spair_idx, mpair_idx;
+  std::vector<double> spair_coef, mpair_coef;
+  dev.o_spair_ptr = (int)ints.size();
+  for (int i = 0; i < ns; ++i) {
+    ints.push_back((int32_t)spair_idx.size());
+    const int b = i * d->sec_stride, cnt = d->sec_nspec[i];
+    for (int p = 0; p < cnt; ++p)
+      for (int q = p; q < cnt; ++q) {
+        const int kp = d->sec_spec[b + p], kq = d->sec_spec[b + q];
+        const int lo = kp < kq ? kp : kq, hi = kp < kq ? kq : kp;
+        spair_idx.push_back(lo * n + hi);
+        spair_coef.push_back(d->sec_stoich[b + p] * d->sec_stoich[b + q]);
+      }
+  }
+  ints.push_back((int32_t)spair_idx.size());
+  dev.o_spair_idx = (int)ints.size();
+  ints.insert(ints.end(), spair_idx.begin(), spair_idx.end());
+  dev.o_mnrl_pidx = (int)ints.size();
+  for (int m = 0; m < nm; ++m)
+    for (int s2 = 0; s2 < d->mnrl_nspec[m]; ++s2)
+      ints.push_back(code_of(d->mnrl_stoich[m * d->mnrl_stride + s2], d->mnrl_spec[m * d->mnrl_stride + s2]));
+  dev.o_mpair_ptr = (int)ints.size();
+  for (int m = 0; m < nm; ++m) {
+    ints.push_back((int32_t)mpair_idx.size());
+    const int b = m * d->mnrl_stride, cnt = d->mnrl_nspec[m];
+    for (int p = 0; p < cnt; ++p)
+      for (int q = 0; q < cnt; ++q) {
+        mpair_idx.push_back(d->mnrl_spec[b + p] * n + d->mnrl_spec[b + q]);
+        mpair_coef.push_back(d->mnrl_stoich[b + p] * d->mnrl_stoich[b + q]);
+      }
+  }
+  ints.push_back((int32_t)mpair_idx.size());
+  dev.o_mpair_idx = (int)ints.size();
+  ints.insert(ints.end(), mpair_idx.begin(), mpair_idx.end());
+  dev.neg_mask = neg_mask;
   while (ints.size() % 4) ints.push_back(0);
   auto put = [&](const double* src, int count, double dflt) {
     int off = (int)dbls.size();
@@ -157,6 +207,8 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_msf = put(d->mnrl_min_scale_factor, nm, 1.0);
   dev.o_temkin = put(d->mnrl_Temkin_const, nm, 1.0);
   dev.o_power = put(d->mnrl_affinity_power, nm, 1.0);
+  dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);
+  dev.o_mpair_coef = put(mpair_coef.data(), (int)mpair_coef.size(), 0.0);
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
               (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |
@@ -201,6 +253,7 @@ int32_t pf_network_destroy(PfNetwork* net) {
   if (net->h_counters) cudaFreeHost(net->h_counters);
   if (net->d_arena) cudaFree(net->d_arena);
   if (net->d_ctype) cudaFree(net->d_ctype);
+  if (net->d_scratch) cudaFree(net->d_scratch);
   delete net;
   return PF_OK;
 }
@@ -214,6 +267,22 @@ int32_t pf_network_set_options(PfNetwork* net, const PfOptions* opts) {
     return PF_ERR_INVALID;
   net->dev.o = *opts;
   return PF_OK;
+}
+
+static int ensure_scratch(PfNetwork* net, int64_t ncells) {
+  const size_t need = batched_scratch_doubles(net->dev, ncells);
+  if (need <= net->scratch_cap) return PF_OK;
+  if (net->d_scratch) cudaFree(net->d_scratch);
+  net->d_scratch = nullptr;
+  net->scratch_cap = 0;
+  if (cudaMalloc(&net->d_scratch, need * sizeof(double)) != cudaSuccess) return PF_ERR_CUDA;
+  net->scratch_cap = need;
+  return PF_OK;
+}
+
+int32_t pf_network_reserve(PfNetwork* net, int64_t ncells) {
+  if (!net || ncells < 0) return PF_ERR_INVALID;
+  return ensure_scratch(net, ncells);
 }
 
 int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg) {
@@ -244,14 +313,18 @@ int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t ke
     return PF_OK;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  if (kernel == PF_KERNEL_BATCHED) {
+    rc = ensure_scratch(net, state->ncells);
+    if (rc) return rc;
+  }
   cudaError_t e = cudaMemsetAsync(net->d_counters, 0, 8 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return PF_ERR_CUDA;
   int lr;
   if (kernel == PF_KERNEL_PLAIN)
     lr = launch_rstep_plain(net->dev, *state, dt, net->d_counters + 1, s);
   else
-    lr = launch_rstep_batched(net->dev, *state, dt, net->launch, net->num_sms, net->d_counters,
-                              net->d_counters + 1, s);
+    lr = launch_rstep_batched(net->dev, *state, dt, net->launch, net->num_sms, net->d_scratch,
+                              net->d_counters, net->d_counters + 1, s);
   if (lr != 0) return PF_ERR_CUDA;
   if (!stats) return PF_OK;
   e = cudaMemcpyAsync(net->h_counters, net->d_counters, 8 * sizeof(unsigned long long),
@@ -366,6 +439,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
   d.status = (int32_t*)dptr[14];
   d.newton_its = (int32_t*)dptr[15];
   d.num_substeps = (int32_t*)dptr[16];
+  d.cell_order = nullptr;  // host-side orders are not carried to the device
   PfStepStats local{};
   rc = pf_rstep(net, &d, dt, kernel, nullptr, stats ? stats : &local);
   if (rc < 0) return rc;

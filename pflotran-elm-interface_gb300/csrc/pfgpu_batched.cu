@@ -10,11 +10,11 @@ namespace pfgpu {
 
 #define PF_DECL(N)                                                                               \
   int launch_batched_##N(const DevNet&, const PfCellState&, double, const PfLaunchConfig&, int, \
-                         unsigned long long*, unsigned long long*, cudaStream_t);
+                         const double*, unsigned long long*, unsigned long long*, cudaStream_t);
 PF_BATCHED_NCOMPS(PF_DECL)
 #undef PF_DECL
 
-static size_t lane_doubles(int n, bool js) { return (js ? (size_t)n * n : 0) + 3 * (size_t)n; }
+static size_t lane_doubles(int n, bool js) { return (js ? (size_t)n * n : 0) + 6 * (size_t)n; }
 
 size_t batched_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg) {
   const size_t tables = (size_t)net.int_words * 4 + (size_t)net.dbl_words * 8;
@@ -35,13 +35,69 @@ bool batched_supported(const DevNet& net) {
   }
 }
 
+// Per-cell setup pre-pass: everything a cell needs once, computed by all
+// lanes in step so the persistent kernel's refills are pure loads.
+//   scratch[i][cell]        TIMESTEP/OFF: exp(-logK_i(T) ln10) / gamma_i
+//                           NEWTON_ITER:  -logK_i(T) ln10
+//   scratch[ns+m][cell]     exp(-logK_m(T) ln10)  (NEWTON_ITER: the exponent)
+//   scratch[ns+nm+j][cell]  ln of the initial guess of component j
+// logK(T) is ReactionInterpolateLogK (reaction_aux.F90:1285-1312) with ln T,
+// 1/T and 1/T^2 formed once per cell.
+__global__ void cell_setup_kernel(DevNet net, PfCellState st, double* __restrict__ scratch) {
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= st.ncells) return;
+  const Tables T{net.ints, net.dbls, &net};
+  const SoA soa{st.ncells};
+  const int n = net.n, ns = net.ns, nm = net.nm;
+  const bool ni = net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER;
+  const double temp = st.temperature ? st.temperature[cell] : 25.0;
+  const double tk = temp + 273.15, lt = log(tk), it = 1.0 / tk, it2 = it * it;
+  const bool tsec = !net.o.isothermal && (net.flags & NETF_SEC_LOGKCOEF);
+  const bool tmin = !net.o.isothermal && (net.flags & NETF_MNRL_LOGKCOEF);
+  const int64_t N = st.ncells;
+  for (int i = 0; i < ns; ++i) {
+    double logK = T.sec_logK(i);
+    if (tsec) {
+      const double* c = T.sec_logKcoef(i);
+      logK = c[0] * lt + c[1] + c[2] * tk + c[3] * it + c[4] * it2;
+    }
+    const double x = -logK * LOG_TO_LN;
+    scratch[(size_t)i * N + cell] = ni ? x : exp(x) / st.sec_act_coef[soa.at(i, cell)];
+  }
+  for (int m = 0; m < nm; ++m) {
+    double logK = T.mnrl_logK(m);
+    if (tmin) {
+      const double* c = T.mnrl_logKcoef(m);
+      logK = c[0] * lt + c[1] + c[2] * tk + c[3] * it + c[4] * it2;
+    }
+    const double x = -logK * LOG_TO_LN;
+    scratch[(size_t)(ns + m) * N + cell] = ni ? x : exp(x);
+  }
+  for (int j = 0; j < n; ++j) {
+    double v = net.o.use_total_as_guess ? st.total[soa.at(j, cell)] : st.pri_molal[soa.at(j, cell)];
+    if (net.o.use_total_as_guess && v <= 1.0e-40) v = 1.0e-40;
+    scratch[(size_t)(ns + nm + j) * N + cell] = log(v);
+  }
+}
+
+size_t batched_scratch_doubles(const DevNet& net, int64_t ncells) {
+  return (size_t)(net.ns + net.nm + net.n) * (size_t)ncells;
+}
+
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
-                         int num_sms, unsigned long long* queue, unsigned long long* counters,
+                         int num_sms, double* scratch, unsigned long long* queue, unsigned long long* counters,
                          cudaStream_t stream) {
+  {
+    const int tpb = 128;
+    const int64_t blocks = (st.ncells + tpb - 1) / tpb;
+    if (blocks) cell_setup_kernel<<<blocks, tpb, 0, stream>>>(net, st, scratch);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+  }
   switch (net.n) {
 #define PF_CASE(N) \
   case N:          \
-    return launch_batched_##N(net, st, dt, cfg, num_sms, queue, counters, stream);
+    return launch_batched_##N(net, st, dt, cfg, num_sms, scratch, queue, counters, stream);
     PF_BATCHED_NCOMPS(PF_CASE)
 #undef PF_CASE
     default:

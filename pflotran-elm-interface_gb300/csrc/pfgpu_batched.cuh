@@ -1,33 +1,39 @@
 // pfgpu_batched.cuh -- batched persistent operator-split reaction kernel.
 //
 // Same step as RStep/RReact (src/pflotran/reaction.F90:3564-4055) per cell,
-// organised for GB300's FP64 pipe:
-//   * one lane per cell, ncomp a compile-time constant (all n-indexed loops
-//     unroll; c, ln c, ln gamma and totals live in registers);
+// organised for GB300's FP64 pipe (1/64 of the FP32 rate, so the count of
+// FP64 instructions per Newton trip and the fraction of active lanes decide
+// the throughput):
+//
+//   * one lane per cell, ncomp a compile-time constant, so the n-indexed
+//     loops unroll and c, ln c, gamma and totals live in registers;
 //   * persistent grid with a device work queue: a lane whose cell finished
-//     takes the next cell at the top of the following Newton trip, so lanes
-//     with different Newton/substep counts do not idle (warp-aggregated
-//     atomicAdd; the queue index only grows, so the loop is bounded);
-//   * reaction tables staged once per block into shared memory with a bulk
-//     TMA copy (cp.async.bulk + mbarrier, bounded wait);
-//   * per-lane vectors indexed by species id (ln a, secondary sums, rhs,
-//     pivot scales) and the Jacobian in shared memory, thread-strided so a
-//     warp's accesses are bank-conflict free (the Jacobian can be placed in
-//     local memory instead for large ncomp; chosen by the autotuner);
-//   * FP64 work reduced without changing the mathematics:
-//       - d total/d c (reaction.F90:4731-4744) uses exp(lnQK - ln m_j)/gamma_i
-//         = s_i/m_j, and in the log formulation RSolve multiplies column j by
-//         m_j (:5494-5499), so the log-space Jacobian column is
-//         den*(delta_kj m_j + sum_i nu_ik nu_ij s_i): no per-pair exp, no 1/m;
-//       - ln m is carried through the log update (ln m <- ln m - u) instead of
-//         re-taking log(m) every evaluation; ln gamma_i and logK(T) fold into
-//         one per-cell constant per secondary;
-//       - the Crout LU's implicit pivot scaling (utility.F90:621-666) makes the
-//         pivot sequence invariant to RSolve's explicit row normalisation
-//         (:5486-5492), which is therefore folded away;
-//       - RReact's final RTAuxVarCompute (:4052) and MineralUpdateKineticState's
-//         rate evaluation (reaction_mineral.F90:1490) are at the iterate of the
-//         last evaluation, so both reuse it.
+//     takes the next one at the top of the following Newton trip (warp-
+//     aggregated atomicAdd; the queue index only grows, so the loop is
+//     bounded).  An optional cell order (longest first, from the previous
+//     step's iteration counts) removes the tail of slow cells;
+//   * everything a cell needs once -- logK(T), 1/gamma of every complex,
+//     ln of the initial guess -- is computed by a convergent pre-pass
+//     (cell_setup_kernel) into scratch, so the refill of one lane costs the
+//     warp loads, not transcendentals;
+//   * reaction tables staged once per block into shared memory by a bulk TMA
+//     copy (cp.async.bulk + mbarrier, bounded wait);
+//   * speciation in product form: for integer stoichiometry nu in {+-1,+-2}
+//     s_i = exp(-logK_i ln10)/gamma_i * prod_j (m_j gamma_j)^nu_ij is
+//     exp(lnQK)/gamma_i of RTotalAqueous (reaction.F90:4711-4718) without the
+//     exp: a per-lane table of a, a^2, 1/a, 1/a^2 turns every factor into one
+//     multiply (other coefficients fall back to exp(nu ln a));
+//   * d total/d m (reaction.F90:4731-4744) is sum_i nu_ik nu_ij s_i / m_j; in
+//     the log formulation RSolve multiplies column j by m_j (:5494-5499), so
+//     the log-space Jacobian is a*(delta_kj m_j + G_kj) with the symmetric
+//     G = sum_i s_i nu_i nu_i^T, accumulated on one triangle and mirrored;
+//   * the Crout LU's implicit pivot scaling (utility.F90:621-666) makes the
+//     pivot sequence invariant under RSolve's row normalisation (:5486-5492),
+//     which is folded away; magnitude comparisons use the integer order of
+//     IEEE bit patterns, keeping them off the FP64 pipe;
+//   * RReact's closing RTAuxVarCompute (:4052) and MineralUpdateKineticState's
+//     rate evaluation (reaction_mineral.F90:1490) happen at the iterate of the
+//     last evaluation, so both reuse it.
 #pragma once
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
@@ -38,15 +44,16 @@ namespace batched {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr long long TMA_WAIT_LIMIT = 1 << 22;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long absbits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
 enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3 };
 
 template <int N, bool JS>
 struct Lane {
-  // thread-strided shared-memory vectors: element e of this lane at p[e*stride]
+  // thread-strided shared-memory vectors: element e of this lane at base[e*stride]
   double* base;
   int stride;
   double* Jl;  // local-memory Jacobian when !JS
@@ -54,92 +61,105 @@ struct Lane {
     if constexpr (JS) return base[(i * N + j) * stride];
     else return Jl[i * N + j];
   }
+  __device__ __forceinline__ double& Jf(int flat) {
+    if constexpr (JS) return base[flat * stride];
+    else return Jl[flat];
+  }
   static constexpr int OFF = JS ? N * N : 0;
-  __device__ __forceinline__ double& lna(int j) { return base[(OFF + j) * stride]; }
-  // S (secondary sums, live during the evaluation) and VV (pivot scales, live
-  // during the factorisation) share one slot
-  __device__ __forceinline__ double& S(int j) { return base[(OFF + N + j) * stride]; }
-  __device__ __forceinline__ double& VV(int j) { return base[(OFF + N + j) * stride]; }
-  __device__ __forceinline__ double& rhs(int j) { return base[(OFF + 2 * N + j) * stride]; }
-  static constexpr int DOUBLES = OFF + 3 * N;
+  // power table a, a^2, 1/a, 1/a^2 (live in the evaluation) shares storage
+  // with the pivot scales VV (live in the factorisation)
+  __device__ __forceinline__ double& P(int e) { return base[(OFF + e) * stride]; }
+  __device__ __forceinline__ double& VV(int j) { return base[(OFF + j) * stride]; }
+  __device__ __forceinline__ double& S(int j) { return base[(OFF + 4 * N + j) * stride]; }
+  __device__ __forceinline__ double& rhs(int j) { return base[(OFF + 5 * N + j) * stride]; }
+  static constexpr int DOUBLES = OFF + 6 * N;
 };
 
-// Crout LU with implicit partial pivoting (utility.F90:597-688) on the lane's
-// Jacobian, then the solve (utility.F90:692-735) in place on rhs.  The
-// reciprocal of each pivot is kept in VV(j) once row j is final.
+// Crout LU with implicit partial pivoting (utility.F90:597-688) and the
+// solve (utility.F90:692-735) in place on rhs.  VV(j) holds 1/pivot once row
+// j is final.  Returns 1 for a zero row (ierror of LUDecomposition).
 template <int N, bool JS>
 __device__ __forceinline__ int lu_solve(Lane<N, JS>& L, int* indx, int stride) {
-#pragma unroll 1
-  for (int i = 0; i < N; ++i) {
-    double aamax = 0.0;
+  constexpr int U = (N <= 12) ? N : 1;
 #pragma unroll
-    for (int j = 0; j < N; ++j) aamax = fmax(aamax, fabs(L.J(i, j)));
-    if (!(aamax > 0.0)) return 1;
-    L.VV(i) = 1.0 / aamax;
+  for (int i = 0; i < N; ++i) {
+    unsigned long long am = 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) am = max(am, absbits(L.J(i, j)));
+    if (am == 0ull || am > 0x7ff0000000000000ull) return 1;
+    L.VV(i) = 1.0 / __longlong_as_double((long long)am);
   }
-#pragma unroll 1
+#pragma unroll U
   for (int j = 0; j < N; ++j) {
-#pragma unroll 1
+#pragma unroll U
     for (int i = 1; i < j; ++i) {
       double sum = L.J(i, j);
+#pragma unroll U
       for (int k = 0; k < i; ++k) sum = fma(-L.J(i, k), L.J(k, j), sum);
       L.J(i, j) = sum;
     }
-    double aamax = 0.0;
+    unsigned long long amax = 0;
     int imax = j;
-#pragma unroll 1
+#pragma unroll U
     for (int i = j; i < N; ++i) {
       double sum = L.J(i, j);
+#pragma unroll U
       for (int k = 0; k < j; ++k) sum = fma(-L.J(i, k), L.J(k, j), sum);
       L.J(i, j) = sum;
-      double dum = L.VV(i) * fabs(sum);
-      if (dum >= aamax) { imax = i; aamax = dum; }
+      const unsigned long long dum = absbits(L.VV(i) * sum);
+      if (dum >= amax) { imax = i; amax = dum; }
     }
     // unconditional swap (a no-op when imax == j) keeps the warp converged
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-      double a = L.J(imax, k), b = L.J(j, k);
+      const double a = L.J(imax, k), b = L.J(j, k);
       L.J(imax, k) = b;
       L.J(j, k) = a;
     }
     L.VV(imax) = L.VV(j);
     indx[j * stride] = imax;
     double piv = L.J(j, j);
-    if (piv == 0.0) { piv = 1.0e-20; L.J(j, j) = piv; }
+    if (absbits(piv) == 0ull) { piv = 1.0e-20; L.J(j, j) = piv; }
     const double rp = 1.0 / piv;
     L.VV(j) = rp;
-#pragma unroll 1
+#pragma unroll U
     for (int i = j + 1; i < N; ++i) L.J(i, j) = L.J(i, j) * rp;
   }
-  // forward substitution with the row interchanges
-#pragma unroll 1
+#pragma unroll U
   for (int i = 0; i < N; ++i) {
     const int ll = indx[i * stride];
     double sum = L.rhs(ll);
     L.rhs(ll) = L.rhs(i);
+#pragma unroll U
     for (int j = 0; j < i; ++j) sum = fma(-L.J(i, j), L.rhs(j), sum);
     L.rhs(i) = sum;
   }
-#pragma unroll 1
+#pragma unroll U
   for (int i = N - 1; i >= 0; --i) {
     double sum = L.rhs(i);
+#pragma unroll U
     for (int j = i + 1; j < N; ++j) sum = fma(-L.J(i, j), L.rhs(j), sum);
     L.rhs(i) = sum * L.VV(i);
   }
   return 0;
 }
 
+// Debye-Hueckel ln gamma (the exponent of RActivityCoefficients, LAG form)
+__device__ __forceinline__ double dh_ln_gamma(double z, double a0, double sI, double I, const DevNet& net) {
+  return fabs(z) > 1.0e-10 ? (-z * z * sI * net.A / (1.0 + a0 * net.B * sI) + net.Bdot * I) * LOG_TO_LN : 0.0;
+}
+
 template <int N, bool JS>
 __global__ void __launch_bounds__(256)
-rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned long long* queue,
-                     unsigned long long* counters) {
+rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
+                     unsigned long long* queue, unsigned long long* counters) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) uint64_t tma_bar;
   const int tid = threadIdx.x;
   const int lane_id = tid & 31;
   const int stride = blockDim.x;
-  const uint32_t ibytes = (uint32_t)net.int_words * 4u;   // multiple of 16 (host pads)
-  const uint32_t dbytes = (uint32_t)net.dbl_words * 8u;   // multiple of 16 (host pads)
+  const uint32_t ibytes = (uint32_t)net.int_words * 4u;  // multiples of 16 (host pads)
+  const uint32_t dbytes = (uint32_t)net.dbl_words * 8u;
   int32_t* sI = reinterpret_cast<int32_t*>(smem);
   double* sD = reinterpret_cast<double*>(smem + ibytes);
 
@@ -153,16 +173,14 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&tma_bar)),
                  "r"(ibytes + dbytes)
                  : "memory");
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(sI)),
-        "l"(net.ints), "r"(ibytes), "r"(smem_u32(&tma_bar))
-        : "memory");
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(sD)),
-        "l"(net.dbls), "r"(dbytes), "r"(smem_u32(&tma_bar))
-        : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sI)),
+                 "l"(net.ints), "r"(ibytes), "r"(smem_u32(&tma_bar))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sD)),
+                 "l"(net.dbls), "r"(dbytes), "r"(smem_u32(&tma_bar))
+                 : "memory");
   }
   {
     uint32_t done = 0;
@@ -175,8 +193,8 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           : "memory");
       ++spins;
     }
-    // every thread saw the same barrier; a timeout (never expected) flags the
-    // launch and leaves without touching any cell
+    // every thread waited on the same barrier; a timeout (never expected)
+    // flags the launch and leaves without touching any cell
     if (__syncthreads_or(!done)) {
       if (tid == 0) atomicOr(&counters[2], 1ull);
       return;
@@ -192,21 +210,25 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
   const SoA soa{st.ncells};
   const PfOptions o = net.o;
   const int ns = net.ns, nm = net.nm;
-  const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN,
-             has_pw = net.flags & NETF_POWER;
-  const bool iso = o.isothermal != 0;
+  const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
   const bool logf = o.use_log_formulation != 0;
   const bool newton_iter_act = o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER;
+  const unsigned neg_mask = (unsigned)net.neg_mask;
+  const int64_t ncells = st.ncells;
+  const double* sc_sec = scratch;                                  // [ns][ncells]
+  const double* sc_min = scratch + (size_t)ns * ncells;            // [nm][ncells]
+  const double* sc_lnc = scratch + (size_t)(ns + nm) * ncells;     // [n][ncells]
 
   // per-lane state
   int phase = NEED;
   long long cell = -1;
-  double c[N], lnc[N], lng[N], tot[N];
-  double fixed[N], init_tot[N], guess[N], small_val[N];
-  double lnKeff[PF_MAX_NSEC];
-  double lnKm[PF_MAX_NMNRL], rate[PF_MAX_NMNRL], vf[PF_MAX_NMNRL];
+  double c[N], lnc[N], g[N], tot[N];
+  double fixed[N], init_tot[N], guess[N], lnguess[N], small_val[N];
+  double Ksec[PF_MAX_NSEC];
+  double Kmin[PF_MAX_NMNRL], rate[PF_MAX_NMNRL], vf[PF_MAX_NMNRL];
   double psv = 0, den_L = 0, den_k = 0, volume = 0, target = 0, cum = 0, dt = 0, inv_dt = 0, r0 = 0;
   double temp = 25.0;
+  double sqI = 0.0, lgI = 0.0;  // ionic strength of the last evaluation (NEWTON_ITER activity)
   bool dry = false;
   int its = 0, its_total = 0, nsub = 0, num_cuts = 0, n_const = 0;
   unsigned small_mask = 0;
@@ -222,10 +244,11 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
       if (lane_id == leader) base = atomicAdd(queue, (unsigned long long)__popc(need));
       base = __shfl_sync(FULL, base, leader);
       if (phase == NEED) {
-        cell = (long long)(base + __popc(need & ((1u << lane_id) - 1u)));
-        phase = (cell < st.ncells) ? START : DONE;
+        const long long q = (long long)(base + __popc(need & ((1u << lane_id) - 1u)));
+        phase = (q < ncells) ? START : DONE;
         if (phase == START) {
-          // load the cell (gather; rows are component-major)
+          cell = st.cell_order ? (long long)st.cell_order[q] : q;
+          // load the cell: pure loads, the transcendentals were done by the pre-pass
           const double por = st.porosity[cell], sat = st.saturation[cell];
           den_k = st.den_kg[cell];
           volume = st.volume[cell];
@@ -243,28 +266,16 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
               t = 1.0e-40;
             }
             tot[j] = t;
-            guess[j] = st.pri_molal[soa.at(j, cell)];
-            lng[j] = log(st.pri_act_coef[soa.at(j, cell)]);
+            guess[j] = o.use_total_as_guess ? t : st.pri_molal[soa.at(j, cell)];
+            lnguess[j] = sc_lnc[soa.at(j, cell)];
+            g[j] = st.pri_act_coef[soa.at(j, cell)];
           }
-          if (o.use_total_as_guess) {
-#pragma unroll
-            for (int j = 0; j < N; ++j) guess[j] = tot[j];
-          }
-          const double tk = temp + 273.15;
-          const bool tsec = !iso && (net.flags & NETF_SEC_LOGKCOEF);
-          const bool tmin = !iso && (net.flags & NETF_MNRL_LOGKCOEF);
-          for (int i = 0; i < ns; ++i) {
-            const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-            const double g = st.sec_act_coef[soa.at(i, cell)];
-            lnKeff[i] = -logK * LOG_TO_LN - (g == 1.0 ? 0.0 : log(g));
-          }
+          for (int i = 0; i < ns; ++i) Ksec[i] = sc_sec[soa.at(i, cell)];
           for (int m = 0; m < nm; ++m) {
-            const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
-            lnKm[m] = -logK * LOG_TO_LN;
+            Kmin[m] = sc_min[soa.at(m, cell)];
             vf[m] = st.mnrl_volfrac[soa.at(m, cell)];
             rate[m] = 0.0;
           }
-          (void)tk;
           target = st.dt_cell ? st.dt_cell[cell] : dt_uniform;
           cum = 0.0;
           dt = target;
@@ -294,7 +305,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
         fixed[j] = dry ? 0.0 : psv * tot[j];
         init_tot[j] = tot[j];
         c[j] = guess[j];
-        lnc[j] = log(c[j]);
+        lnc[j] = lnguess[j];
       }
       its = 0;
       r0 = 0.0;
@@ -307,7 +318,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
       its += 1;
       if (newton_iter_act) {
         // RActivityCoefficients LAG (reaction.F90:4553-4612) from this
-        // iterate's molalities and the previous evaluation's sec_molal
+        // iterate and the previous evaluation's sec_molal
         double I = 0.0;
 #pragma unroll
         for (int j = 0; j < N; ++j) I = I + c[j] * T.pri_Z(j) * T.pri_Z(j);
@@ -316,56 +327,54 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           I = I + st.sec_molal[soa.at(i, cell)] * z * z;
         }
         I = 0.5 * I;
-        const double sI_ = sqrt(I);
+        sqI = sqrt(I);
+        lgI = I;
 #pragma unroll
-        for (int j = 0; j < N; ++j) {
-          const double z = T.pri_Z(j);
-          lng[j] = fabs(z) > 1.0e-10
-                       ? (-z * z * sI_ * net.A / (1.0 + T.pri_a0(j) * net.B * sI_) + net.Bdot * I) * LOG_TO_LN
-                       : 0.0;
-        }
-        const bool tsec = !iso && (net.flags & NETF_SEC_LOGKCOEF);
-        for (int i = 0; i < ns; ++i) {
-          const double z = T.sec_Z(i);
-          const double lg = fabs(z) > 1.0e-10
-                                ? (-z * z * sI_ * net.A / (1.0 + T.sec_a0(i) * net.B * sI_) + net.Bdot * I) *
-                                      LOG_TO_LN
-                                : 0.0;
-          const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-          lnKeff[i] = -logK * LOG_TO_LN - lg;
-        }
+        for (int j = 0; j < N; ++j) g[j] = exp(dh_ln_gamma(T.pri_Z(j), T.pri_a0(j), sqI, I, net));
       }
-      // ---- RTotalAqueous in the factored form ---------------------------
+      // ---- power table and RTotalAqueous in product form -----------------
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        L.lna(j) = lnc[j] + lng[j];
+        const double a = c[j] * g[j];
+        L.P(j) = a;
+        L.P(N + j) = a * a;
+        if (neg_mask & (1u << j)) {
+          const double ia = 1.0 / a;
+          L.P(2 * N + j) = ia;
+          L.P(3 * N + j) = ia * ia;
+        }
         L.S(j) = 0.0;
       }
 #pragma unroll
       for (int i = 0; i < N; ++i)
 #pragma unroll
-        for (int j = 0; j < N; ++j) L.J(i, j) = 0.0;
+        for (int j = i; j < N; ++j) L.J(i, j) = 0.0;
+      const double a_acc = dry ? 1.0 : psv * inv_dt * den_L;  // psvd_t * den_kg_per_L
       for (int i = 0; i < ns; ++i) {
         const int b = T.sec_begin(i), e = T.sec_end(i);
-        double lnQK = lnKeff[i];
-        for (int p = b; p < e; ++p) lnQK = fma(T.sec_nu(p), L.lna(T.sec_idx(p)), lnQK);
-        const double s = exp(lnQK);
+        double s = newton_iter_act
+                       ? exp(Ksec[i] - dh_ln_gamma(T.sec_Z(i), T.sec_a0(i), sqI, lgI, net))
+                       : Ksec[i];
+        for (int p = b; p < e; ++p) {
+          const int pe = T.sec_pidx(p);
+          s *= (pe >= 0) ? L.P(pe) : exp(T.sec_nu(p) * log(L.P(T.sec_idx(p))));
+        }
         st.sec_molal[soa.at(i, cell)] = s;
+        const double sa = a_acc * s;
         for (int p = b; p < e; ++p) {
           const int kp = T.sec_idx(p);
-          const double t = T.sec_nu(p) * s;
-          L.S(kp) = L.S(kp) + t;
-          for (int q = b; q < e; ++q) {
-            const int kq = T.sec_idx(q);
-            L.J(kp, kq) = fma(T.sec_nu(q), t, L.J(kp, kq));
-          }
+          L.S(kp) = fma(T.sec_nu(p), sa, L.S(kp));
+        }
+        for (int q = T.spair_begin(i); q < T.spair_begin(i + 1); ++q) {
+          const int f = T.spair_idx(q);
+          L.Jf(f) = fma(T.spair_coef(q), sa, L.Jf(f));
         }
       }
-      const double a = psv * inv_dt * den_L;  // psvd_t * den_kg_per_L
+      const double b_tot = den_L / a_acc;
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        tot[j] = (c[j] + L.S(j)) * den_L;
-        L.rhs(j) = dry ? -fixed[j] * inv_dt : (psv * tot[j] - fixed[j]) * inv_dt;
+        tot[j] = fma(b_tot, L.S(j), den_L * c[j]);
+        L.rhs(j) = dry ? 0.0 : fma(a_acc, c[j], L.S(j)) - fixed[j] * inv_dt;
       }
       if (dry) {
 #pragma unroll
@@ -374,28 +383,39 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           for (int j = 0; j < N; ++j) L.J(i, j) = (i == j) ? (logf ? c[j] : 1.0) : 0.0;
       } else if (logf) {
 #pragma unroll
-        for (int i = 0; i < N; ++i)
+        for (int i = 0; i < N; ++i) {
 #pragma unroll
-          for (int j = 0; j < N; ++j) L.J(i, j) = (i == j) ? a * (c[j] + L.J(i, j)) : a * L.J(i, j);
-      } else {
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-          const double aic = a / c[j];
-#pragma unroll
-          for (int i = 0; i < N; ++i) L.J(i, j) = (i == j) ? a + aic * L.J(i, j) : aic * L.J(i, j);
+          for (int j = 0; j < i; ++j) L.J(i, j) = L.J(j, i);
+          L.J(i, i) = fma(a_acc, c[i], L.J(i, i));
         }
-      }
-      // ---- RKineticMineral (reaction_mineral.F90:647-1078) -----------------
-      if (!logf && nm > 0) {
+      } else {
+        // linear formulation: d/dm_j = column j of G divided by m_j
+        double ic[N];
 #pragma unroll
-        for (int j = 0; j < N; ++j) L.VV(j) = 1.0 / c[j];  // exp(-ln_conc) by species id
+        for (int j = 0; j < N; ++j) ic[j] = 1.0 / c[j];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+#pragma unroll
+          for (int j = 0; j < i; ++j) {
+            const double gv = L.J(j, i);
+            L.J(i, j) = gv * ic[j];
+            L.J(j, i) = gv * ic[i];
+          }
+          L.J(i, i) = fma(L.J(i, i), ic[i], a_acc);
+        }
+        // mineral columns below also need 1/m_j by species id: park it in S
+#pragma unroll
+        for (int j = 0; j < N; ++j) L.S(j) = ic[j];
       }
+      // ---- RKineticMineral (reaction_mineral.F90:647-1078) ---------------
       for (int m = 0; m < nm; ++m) {
         const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
         rate[m] = 0.0;
-        double lnQK = lnKm[m];
-        for (int p = b; p < e; ++p) lnQK = fma(T.mnrl_nu(p), L.lna(T.mnrl_idx(p)), lnQK);
-        const double QK = exp(lnQK);
+        double QK = Kmin[m];
+        for (int p = b; p < e; ++p) {
+          const int pe = T.mnrl_pidx(p);
+          QK *= (pe >= 0) ? L.P(pe) : exp(T.mnrl_nu(p) * log(L.P(T.mnrl_idx(p))));
+        }
         double aff;
         if (has_tk) aff = 1.0 - pow(QK, 1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m)));
         else if (has_msf) aff = 1.0 - pow(QK, 1.0 / T.msf(m));
@@ -412,8 +432,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
         const double k = T.rate(m) * arr;
         double Im_const = -st.mnrl_area[soa.at(m, cell)];
         if (has_msf) Im_const = Im_const / T.msf(m);
-        double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * k
-                           : Im_const * sign_ * fabs(aff) * k;
+        double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * k : Im_const * sign_ * fabs(aff) * k;
         rate[m] = Im;
         if (dry) continue;  // RReaction returns before minerals in a dry cell
         Im_const = Im_const * volume;
@@ -428,25 +447,22 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           const double den = 1.0 + (1.0 - aff) / rl;
           f = f * (1.0 + QK / rl / den) / den;
         }
-        for (int p = b; p < e; ++p) {
-          const int kp = T.mnrl_idx(p);
-          L.rhs(kp) = fma(T.mnrl_nu(p), Im, L.rhs(kp));
-          const double t = T.mnrl_nu(p) * f;
-          for (int q = b; q < e; ++q) {
-            const int kq = T.mnrl_idx(q);
-            // log form: the column scale m_q cancels the 1/m_q of dQK/dm_q
-            L.J(kp, kq) = logf ? fma(T.mnrl_nu(q), t, L.J(kp, kq))
-                               : fma(T.mnrl_nu(q) * t, L.VV(kq), L.J(kp, kq));
-          }
+        for (int p = b; p < e; ++p) L.rhs(T.mnrl_idx(p)) = fma(T.mnrl_nu(p), Im, L.rhs(T.mnrl_idx(p)));
+        // d R / d ln m (log form: the m_q of the column scale cancels 1/m_q)
+        for (int q = T.mpair_begin(m); q < T.mpair_begin(m + 1); ++q) {
+          const int fl = T.mpair_idx(q);
+          const double v = T.mpair_coef(q) * f;
+          L.Jf(fl) = fma(v, logf ? 1.0 : L.S(fl % N), L.Jf(fl));
         }
       }
       // ---- convergence tests on the residual (reaction.F90:3946-3953) -----
-      double dot = 0.0, mx = 0.0;
+      double dot = 0.0;
+      unsigned long long mxb = 0;
 #pragma unroll
       for (int j = 0; j < N; ++j) {
         const double r = L.rhs(j);
         dot = fma(r, r, dot);
-        mx = fmax(mx, fabs(r));
+        mxb = max(mxb, absbits(r));
       }
       const double two_norm = sqrt(dot);
       if (its == 1) r0 = two_norm;
@@ -455,7 +471,8 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
 #pragma unroll
         for (int j = 0; j < N; ++j) tot[j] = init_tot[j];
         react_end = 1;
-      } else if (mx < o.max_residual_tolerance || two_norm < o.max_rel_residual_tolerance * r0) {
+      } else if (__longlong_as_double((long long)mxb) < o.max_residual_tolerance ||
+                 two_norm < o.max_rel_residual_tolerance * r0) {
         react_end = 0;
       } else {
         if (lu_solve<N, JS>(L, indx, stride)) {
@@ -463,36 +480,31 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
         } else {
           const double tol = o.max_relative_change_tolerance;
           bool small = true;
-          double nc[N];
+          double nc[N], u[N];
 #pragma unroll
-          for (int j = 0; j < N; ++j) {
-            double u = o.fork_literal_rsolve ? 0.0 : L.rhs(j);
-            if (logf) {
-              u = fmin(fmax(u, -o.max_dlnC_rreact), o.max_dlnC_rreact);
-              nc[j] = c[j] * exp(-u);
-              L.rhs(j) = u;
-            } else {
-              nc[j] = c[j] - u;  // positivity scaling applied below
+          for (int j = 0; j < N; ++j) u[j] = o.fork_literal_rsolve ? 0.0 : L.rhs(j);
+          if (logf) {
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+              u[j] = fmin(fmax(u[j], -o.max_dlnC_rreact), o.max_dlnC_rreact);
+              nc[j] = c[j] * exp(-u[j]);
             }
-          }
-          if (!logf) {
+          } else {
             double min_ratio = 1.7976931348623157e308;
 #pragma unroll
             for (int j = 0; j < N; ++j)
-              if (c[j] <= L.rhs(j)) min_ratio = fmin(min_ratio, fabs(c[j] / L.rhs(j)));
-            if (min_ratio < 1.0) {
+              if (c[j] <= u[j]) min_ratio = fmin(min_ratio, fabs(c[j] / u[j]));
 #pragma unroll
-              for (int j = 0; j < N; ++j) nc[j] = c[j] - L.rhs(j) * min_ratio * 0.99;
-            }
+            for (int j = 0; j < N; ++j) nc[j] = c[j] - (min_ratio < 1.0 ? u[j] * min_ratio * 0.99 : u[j]);
           }
 #pragma unroll
-          for (int j = 0; j < N; ++j) small = small && (fabs(nc[j] - c[j]) < tol * c[j]);
+          for (int j = 0; j < N; ++j) small = small && (absbits(nc[j] - c[j]) < absbits(tol * c[j]));
           if (small) {
             react_end = 0;
           } else {
 #pragma unroll
             for (int j = 0; j < N; ++j) {
-              lnc[j] = logf ? lnc[j] - L.rhs(j) : log(nc[j]);
+              lnc[j] = logf ? lnc[j] - u[j] : log(nc[j]);
               c[j] = nc[j];
             }
           }
@@ -520,7 +532,10 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
           nsub += 1;
           n_const += 1;
 #pragma unroll
-          for (int j = 0; j < N; ++j) guess[j] = c[j];
+          for (int j = 0; j < N; ++j) {
+            guess[j] = c[j];
+            lnguess[j] = lnc[j];
+          }
           if (n_const >= 4) {
             num_cuts = num_cuts - 1;
             dt = fmin(2.0 * dt, target - cum);
@@ -542,15 +557,12 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
       for (int j = 0; j < N; ++j) {
         st.total[soa.at(j, cell)] = tot[j];
         st.pri_molal[soa.at(j, cell)] = c[j];
-        if (newton_iter_act) st.pri_act_coef[soa.at(j, cell)] = exp(lng[j]);
+        if (newton_iter_act) st.pri_act_coef[soa.at(j, cell)] = g[j];
       }
       if (newton_iter_act) {
-        // sec_act_coef = exp(lnKeff-part); recompute from the last lnKeff
-        const bool tsec = !iso && (net.flags & NETF_SEC_LOGKCOEF);
-        for (int i = 0; i < ns; ++i) {
-          const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-          st.sec_act_coef[soa.at(i, cell)] = exp(-logK * LOG_TO_LN - lnKeff[i]);
-        }
+        // gamma of the complexes at the last evaluation's ionic strength
+        for (int i = 0; i < ns; ++i)
+          st.sec_act_coef[soa.at(i, cell)] = exp(dh_ln_gamma(T.sec_Z(i), T.sec_a0(i), sqI, lgI, net));
       }
       for (int m = 0; m < nm; ++m) {
         st.mnrl_volfrac[soa.at(m, cell)] = vf[m];
@@ -587,8 +599,8 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, unsigned lon
 
 template <int N>
 int launch_batched_n(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
-                     int num_sms, unsigned long long* queue, unsigned long long* counters,
-                     cudaStream_t stream) {
+                     int num_sms, const double* scratch, unsigned long long* queue,
+                     unsigned long long* counters, cudaStream_t stream) {
   const size_t smem = batched_smem_bytes(net, cfg);
   const int tpb = cfg.threads_per_block;
   const int grid = num_sms * cfg.blocks_per_sm;
@@ -597,12 +609,12 @@ int launch_batched_n(const DevNet& net, const PfCellState& st, double dt, const 
     auto k = batched::rstep_batched_kernel<N, true>;
     err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
-    k<<<grid, tpb, smem, stream>>>(net, st, dt, queue, counters);
+    k<<<grid, tpb, smem, stream>>>(net, st, dt, scratch, queue, counters);
   } else {
     auto k = batched::rstep_batched_kernel<N, false>;
     err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
-    k<<<grid, tpb, smem, stream>>>(net, st, dt, queue, counters);
+    k<<<grid, tpb, smem, stream>>>(net, st, dt, scratch, queue, counters);
   }
   return (int)cudaGetLastError();
 }

@@ -3,8 +3,8 @@
 
 namespace pfgpu {
 int launch_batched_4(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
-                      int num_sms, unsigned long long* queue, unsigned long long* counters,
-                      cudaStream_t stream) {
-  return launch_batched_n<4>(net, st, dt, cfg, num_sms, queue, counters, stream);
+                      int num_sms, const double* scratch, unsigned long long* queue,
+                      unsigned long long* counters, cudaStream_t stream) {
+  return launch_batched_n<4>(net, st, dt, cfg, num_sms, scratch, queue, counters, stream);
 }
 }  // namespace pfgpu

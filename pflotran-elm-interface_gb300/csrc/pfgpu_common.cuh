@@ -46,6 +46,14 @@ struct DevNet {
   int32_t o_sec_nu, o_sec_logK, o_sec_logKcoef, o_pri_Z, o_pri_a0, o_sec_Z, o_sec_a0;
   int32_t o_mnrl_nu, o_mnrl_logK, o_mnrl_logKcoef, o_rate, o_ea, o_molar_vol, o_thresh,
       o_limiter, o_msf, o_temkin, o_power;
+  // product-form speciation tables (batched kernel): per CSR entry the index
+  // code*n + species into the lane's power table (code 0: a, 1: a^2, 2: 1/a,
+  // 3: 1/a^2; -1: other coefficient), and per reaction the (p <= q) species
+  // pairs as flat Jacobian index with coefficient nu_p*nu_q (minerals: all
+  // ordered pairs)
+  int32_t o_sec_pidx, o_spair_ptr, o_spair_idx, o_mnrl_pidx, o_mpair_ptr, o_mpair_idx;
+  int32_t o_spair_coef, o_mpair_coef;
+  int32_t neg_mask;  // bit j: species j carries a negative coefficient somewhere
   double A, B, Bdot;
   PfOptions o;
 };
@@ -80,6 +88,14 @@ struct Tables {
   __device__ __forceinline__ double msf(int m) const { return D[net->o_msf + m]; }
   __device__ __forceinline__ double temkin(int m) const { return D[net->o_temkin + m]; }
   __device__ __forceinline__ double power(int m) const { return D[net->o_power + m]; }
+  __device__ __forceinline__ int sec_pidx(int p) const { return I[net->o_sec_pidx + p]; }
+  __device__ __forceinline__ int spair_begin(int i) const { return I[net->o_spair_ptr + i]; }
+  __device__ __forceinline__ int spair_idx(int q) const { return I[net->o_spair_idx + q]; }
+  __device__ __forceinline__ double spair_coef(int q) const { return D[net->o_spair_coef + q]; }
+  __device__ __forceinline__ int mnrl_pidx(int p) const { return I[net->o_mnrl_pidx + p]; }
+  __device__ __forceinline__ int mpair_begin(int m) const { return I[net->o_mpair_ptr + m]; }
+  __device__ __forceinline__ int mpair_idx(int q) const { return I[net->o_mpair_idx + q]; }
+  __device__ __forceinline__ double mpair_coef(int q) const { return D[net->o_mpair_coef + q]; }
 };
 
 // Fortran SIGN(1.d0, x)

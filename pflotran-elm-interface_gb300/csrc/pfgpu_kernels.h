@@ -14,9 +14,11 @@ int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
 // counters[0] += Newton iterations, counters[1] += failed cells,
 // counters[2] = error flags (bit 0: table staging timed out).
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt,
-                         const PfLaunchConfig& cfg, int num_sms,
+                         const PfLaunchConfig& cfg, int num_sms, double* scratch,
                          unsigned long long* queue, unsigned long long* counters,
                          cudaStream_t stream);
+// doubles of per-cell scratch the batched kernel's setup pre-pass writes
+size_t batched_scratch_doubles(const DevNet& net, int64_t ncells);
 // shared memory bytes a batched launch of this config needs
 size_t batched_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg);
 bool batched_supported(const DevNet& net);

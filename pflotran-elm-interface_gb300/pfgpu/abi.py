@@ -90,6 +90,7 @@ class PfCellState(C.Structure):
         ("porosity", _dp), ("saturation", _dp), ("den_kg", _dp),
         ("volume", _dp), ("temperature", _dp), ("dt_cell", _dp),
         ("status", _ip), ("newton_its", _ip), ("num_substeps", _ip),
+        ("cell_order", C.POINTER(C.c_int64)),
     ]
 
 
@@ -118,6 +119,7 @@ SIGNATURES = {
     "pf_network_create": (C.c_int32, [C.POINTER(PfNetworkDesc), C.POINTER(_P)]),
     "pf_network_destroy": (C.c_int32, [_P]),
     "pf_network_set_options": (C.c_int32, [_P, C.POINTER(PfOptions)]),
+    "pf_network_reserve": (C.c_int32, [_P, C.c_int64]),
     "pf_rstep": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32, _P,
                              C.POINTER(PfStepStats)]),
     "pf_update_auxvars": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_int32, _P]),

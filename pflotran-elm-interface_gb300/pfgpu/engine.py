@@ -70,9 +70,18 @@ class ReactionEngine:
         return self.lib.pf_network_set_launch(self.handle, C.byref(cfg))
 
     # ------------------------------------------------------------ steps
+    def reserve(self, ncells: int):
+        abi.check("pf_network_reserve", self.lib.pf_network_reserve(self.handle, int(ncells)),
+                  allow_cell_failures=False)
+
     def rstep(self, state: CellState, dt: float, kernel: int = abi.PF_KERNEL_BATCHED, stream=None,
-              stats: bool = True):
+              stats: bool = True, order=None):
+        """order: optional int64 CUDA tensor, a permutation of the cells giving
+        the work-queue order of the batched kernel (results are unchanged)."""
         s = state.struct()
+        if order is not None:
+            assert order.dtype.is_floating_point is False and order.numel() == state.ncells
+            s.cell_order = C.cast(order.data_ptr(), C.POINTER(C.c_int64))
         st = abi.PfStepStats() if stats else None
         rc = self.lib.pf_rstep(self.handle, C.byref(s), float(dt), int(kernel), _stream_ptr(stream),
                                C.byref(st) if stats else None)
