@@ -329,16 +329,18 @@ def main():
         hs = CellState(net, {k: pin[k].numpy() for k in pin})
         h2d = sum(pin[k].numel() * pin[k].element_size() for k in pin if k not in ("mnrl_rate", "status",
                                                                                   "newton_its", "num_substeps"))
+        h2d += ncells * 8  # the work-queue order
         d2h = sum(pin[k].numel() * pin[k].element_size() for k in pin
                   if k in ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
                            "mnrl_rate", "status", "newton_its", "num_substeps"))
         src = {k: pristine[k].cpu().numpy() if k in pristine else host.a[k] for k in pin}
+        horder = order.cpu().numpy()
         times = []
         for k in range(args.warmup + args.steps):
             for f in pin:
                 np.copyto(hs.a[f], src[f])
             t = time.perf_counter()
-            eng.rstep_host(hs, dt)
+            eng.rstep_host(hs, dt, order=horder)
             el = time.perf_counter() - t
             if k >= args.warmup:
                 times.append(el)

@@ -397,6 +397,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
       {(void*)h->temperature, N * d8, true, false}, {(void*)h->dt_cell, N * d8, true, false},
       {h->status, N * i4, false, true},            {h->newton_its, N * i4, false, true},
       {h->num_substeps, N * i4, false, true},
+      {(void*)h->cell_order, N * sizeof(int64_t), true, false},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
   size_t need = 0;
@@ -439,7 +440,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
   d.status = (int32_t*)dptr[14];
   d.newton_its = (int32_t*)dptr[15];
   d.num_substeps = (int32_t*)dptr[16];
-  d.cell_order = nullptr;  // host-side orders are not carried to the device
+  d.cell_order = (const int64_t*)dptr[17];
   PfStepStats local{};
   rc = pf_rstep(net, &d, dt, kernel, nullptr, stats ? stats : &local);
   if (rc < 0) return rc;

@@ -90,8 +90,12 @@ class ReactionEngine:
             return None
         return {k: getattr(st, k) for k, _ in abi.PfStepStats._fields_}
 
-    def rstep_host(self, state: CellState, dt: float, kernel: int = abi.PF_KERNEL_BATCHED):
+    def rstep_host(self, state: CellState, dt: float, kernel: int = abi.PF_KERNEL_BATCHED, order=None):
+        """order: optional int64 numpy array (host), the work-queue order."""
         s = state.struct()
+        if order is not None:
+            self._host_order = np.ascontiguousarray(order, np.int64)
+            s.cell_order = C.cast(self._host_order.ctypes.data, C.POINTER(C.c_int64))
         st = abi.PfStepStats()
         rc = self.lib.pf_rstep_host(self.handle, C.byref(s), float(dt), int(kernel), C.byref(st))
         abi.check("pf_rstep_host", rc)

@@ -44,9 +44,13 @@ def default_options(**kw) -> dict:
 
 
 def tight_options(**kw) -> dict:
-    """Tolerances tight enough that every Newton solve converges to rounding
-    level; separates arithmetic error from stopping-rule noise."""
-    return default_options(max_relative_change_tolerance=1e-15,
+    """Tolerances four orders tighter than the defaults: the Newton solves run
+    until the relative update is below 1e-10, so the returned iterate is
+    within ~1e-10 of the root (quadratic convergence puts it far closer);
+    separates arithmetic error from stopping-rule noise.  (Tighter than this,
+    the update of a component whose total cancels to 1e-12 of its terms
+    stays at rounding noise and never passes the test.)"""
+    return default_options(max_relative_change_tolerance=1e-10,
                            max_residual_tolerance=1e-300,
                            max_rel_residual_tolerance=1e-300,
                            maximum_reaction_iterations=60, **kw)

@@ -61,6 +61,6 @@ def case(oracle, name, tight=False):
     return net, st.copy()
 
 
-CASE_DT = {"calcite": 3600.0, "random12": 86400.0}
+CASE_DT = {"calcite": 3600.0, "random12": 86400.0, "random12raw": 86400.0}
 CASE_DT.update({"hetero%d" % n: 86400.0 for n in (4, 6, 8, 10, 12, 16, 20, 24)})
 HETERO = (4, 6, 8, 10, 12, 16, 20, 24)
