@@ -246,6 +246,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--launch", default="", help="threads_per_block,blocks_per_sm,jac_in_shared (skips tuning)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -273,7 +274,11 @@ def main():
     pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}
     dt = cfg["dt"]
     tuned = None
-    if not args.no_tune:
+    if args.launch:
+        tpb, bps, js = (int(x) for x in args.launch.split(","))
+        if eng.set_launch_config(tpb, bps, js) != abi.PF_OK:
+            raise SystemExit("launch config %s rejected" % args.launch)
+    elif not args.no_tune:
         from pfgpu import autotune
         best, table = autotune.tune(eng, dev, dt, use_cache=False)
         tuned = {"best": best, "top": table[:6]}
