@@ -236,6 +236,25 @@ int32_t pf_update_activity_coefs(PfNetwork* net, const PfCellState* state,
 int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
                       double dt, int32_t kernel, PfStepStats* stats);
 
+/*
+ * pf_rstep_noalloc -- pf_rstep with the batched kernel, for callers that must
+ * not allocate device memory during the step.  No counterpart in the
+ * reference (PFLOTRAN's Fortran loop has no device memory to allocate).
+ * Callers that cannot let a library call cudaMalloc -- a host model whose GPU
+ * memory belongs to another framework's pool, a coupled run with a fixed
+ * device footprint, code recording the step into a CUDA graph -- use this
+ * instead of pf_rstep: the per-cell scratch lives in a fixed 32 MiB device
+ * array inside the library (held on every device that loads it until exit),
+ * and the call allocates nothing.  Limit: (ncomp + nsec + nmnrl) * ncells
+ * <= 4,194,304; larger states return PF_ERR_TOO_LARGE (split them across
+ * calls).  The first call on a device resolves the array's device address;
+ * make that first call before any stream capture.  All calls share the one
+ * array, so calls that overlap on the GPU (other streams, other threads)
+ * race; serialise them.  No statistics are reduced (use the per-cell
+ * status/newton_its arrays).
+ */
+int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream);
+
 /* ----------------------------------------------------------- constraints */
 /* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */
 enum {

@@ -246,6 +246,21 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   return PF_OK;
 }
 
+// Internal accessors for pfgpu_noalloc.cu (not part of the public header).
+int32_t pf_internal_network_view(PfNetwork* net, DevNet* dev, PfLaunchConfig* cfg, int* num_sms,
+                                 unsigned long long** counters) {
+  if (!net) return PF_ERR_INVALID;
+  *dev = net->dev;
+  *cfg = net->launch;
+  *num_sms = net->num_sms;
+  *counters = net->d_counters;
+  return PF_OK;
+}
+
+int32_t pf_internal_validate_state(PfNetwork* net, const PfCellState* state) {
+  return validate_state(net, state);
+}
+
 int32_t pf_network_destroy(PfNetwork* net) {
   if (!net) return PF_ERR_INVALID;
   if (net->d_tables) cudaFree(net->d_tables);

@@ -124,6 +124,7 @@ SIGNATURES = {
                              C.POINTER(PfStepStats)]),
     "pf_update_auxvars": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_int32, _P]),
     "pf_update_activity_coefs": (C.c_int32, [_P, C.POINTER(PfCellState), _P]),
+    "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
                                   C.POINTER(PfStepStats)]),
     "pf_equilibrate_constraint": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(C.c_int32),
