@@ -307,6 +307,31 @@ def main():
     value = world * ncells * args.steps / (total_ms * 1e-3)
     kern_avg = float(np.mean(kern_ms))
 
+    # adjoint of the step (loss sum w*(T_final - target)^2, w ~ U[0,1], target
+    # = forward output with 5 % lognormal noise): time of pf_adjoint, which
+    # recomputes the forward solve, over the forward step
+    for k in pristine:
+        dev.a[k].copy_(pristine[k])
+    eng.rstep(dev, dt, stats=False, order=order)
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    w = torch.rand(dev.a["total"].shape, dtype=torch.float64, device="cuda", generator=gen)
+    tgt = dev.a["total"] * torch.exp(0.05 * torch.randn(dev.a["total"].shape, dtype=torch.float64,
+                                                         device="cuda", generator=gen))
+    adj_ms = []
+    for k_ in range(1 + max(1, min(args.steps, 3))):
+        for k in pristine:
+            dev.a[k].copy_(pristine[k])
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        gout = eng.adjoint(dev, dt, weight=w, target=tgt, order=order)
+        a1.record()
+        torch.cuda.synchronize()
+        if k_:
+            adj_ms.append(a0.elapsed_time(a1))
+    adjoint = {"ms": float(np.mean(adj_ms)), "ratio_to_forward": float(np.mean(adj_ms)) / kern_avg,
+               "cells_with_gradient": int((gout["adj_status"] == 0).sum()),
+               "loss": float(gout["loss"][0])}
+
     # plain one-thread-per-cell form, same inputs
     p_total, p_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_PLAIN, max(1, min(args.steps, 3)), 1)
     plain_value = ncells * len(p_kern) / (p_total * 1e-3)
@@ -375,6 +400,7 @@ def main():
                 "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),
                                   "kernel_ms": float(np.mean(nat_kern))},
                 "speedup_vs_plain_gpu": value / plain_value,
+                "adjoint": adjoint,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "gpu_launches": args.steps}
         print(json.dumps(line), flush=True)

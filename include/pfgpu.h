@@ -255,6 +255,61 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
  */
 int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream);
 
+/* ----------------------------------------------------------------- adjoint */
+/* Largest number of RStep substeps (dt cuts) whose converged states the
+ * adjoint keeps per cell; cells with more report adj_status 2. */
+#define PF_ADJ_MAX_SUBSTEPS 16
+
+/*
+ * Arguments of pf_adjoint (device pointers, component-major like the state).
+ * The loss is L = sum_cells sum_k weight*(total_final - target)^2 when weight
+ * and target are given; otherwise dL/dtotal_final is taken from dL_dtotal
+ * (the backward pass of an autograd wrapper).  Gradients are with respect to
+ * an additive shift of every logK (secondary and mineral, applied at every
+ * temperature), ln of every rate constant, ln of every cell's mineral area,
+ * and every cell's initial (transported) total.
+ */
+typedef struct PfAdjointArgs {
+  const double* weight;      /* [ncomp][ncells] or NULL                      */
+  const double* target;      /* [ncomp][ncells] (with weight)                 */
+  const double* dL_dtotal;   /* [ncomp][ncells] used when weight == NULL     */
+  double* dL_dtotal0;        /* [ncomp][ncells] out                           */
+  double* dL_dlnarea;        /* [nmnrl][ncells] out                           */
+  double* dL_dlogK_sec;      /* [nsec]  out, summed over cells                */
+  double* dL_dlogK_mnrl;     /* [nmnrl] out, summed over cells                */
+  double* dL_dlnk;           /* [nmnrl] out, summed over cells                */
+  double* loss;              /* [1] out (weight given) or NULL                */
+  int32_t* adj_status;       /* [ncells] out: 0 ok, 1 forward failed (no
+                                gradient), 2 more than PF_ADJ_MAX_SUBSTEPS
+                                substeps, 3 singular adjoint system          */
+} PfAdjointArgs;
+
+/*
+ * pf_adjoint -- the operator-split step (as pf_rstep, batched kernel; the
+ * state is advanced exactly as pf_rstep would) followed, per cell, by the
+ * implicit-function-theorem adjoint of the step.  No counterpart in the
+ * reference (PFLOTRAN has no derivatives of RStep with respect to its
+ * parameters).  For each substep, from the last backwards, it solves
+ * J^T lambda = (dT/dln m)^T Tbar at that substep's converged free-ion
+ * molalities m, with the exact Jacobian of the residual
+ * (psv/dt)(T(m) - T_prev) + R(m) of RReact (reaction.F90:3899-3916), and
+ * accumulates the parameter gradients; Newton iterates are recomputed, not
+ * stored (only the substep end states are kept).  Output arrays are zeroed by
+ * the call.  Requires the log formulation or the linear one (both solve the
+ * same equations) and activity coefficients OFF or TIMESTEP.
+ */
+int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt,
+                   const PfAdjointArgs* args, void* stream);
+
+/* Shifts the network's parameters from their values at pf_network_create:
+ * logK of every secondary and kinetic mineral += dlogK (at every temperature:
+ * for temperature fits the constant coefficient moves), rate constants
+ * *= exp(dlnk).  Host arrays; NULL leaves that group at its base value.
+ * Used to evaluate losses away from the base point (finite differences,
+ * optimisation steps). */
+int32_t pf_network_shift_parameters(PfNetwork* net, const double* dlogK_sec,
+                                    const double* dlogK_mnrl, const double* dlnk);
+
 /* ----------------------------------------------------------- constraints */
 /* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */
 enum {

@@ -1,5 +1,6 @@
 // pfgpu_api.cu -- the C ABI (include/pfgpu.h): network upload, argument
 // checking, kernel dispatch, the status reduction and the host-buffer path.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -22,6 +23,8 @@ struct PfNetwork {
   int32_t* d_ctype = nullptr;                // constraint types [PF_MAX_NCOMP]
   double* d_scratch = nullptr;               // batched kernel per-cell scratch
   size_t scratch_cap = 0;                    // doubles
+  std::vector<double> dbls_base;             // host copy of the double block at create
+  size_t ib = 0;                             // byte offset of the double block
   PfLaunchConfig launch{};
   int device = 0;
   int num_sms = 0;
@@ -240,6 +243,8 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   }
   dev.ints = (const int32_t*)net->d_tables;
   dev.dbls = (const double*)((char*)net->d_tables + ib);
+  net->dbls_base = dbls;
+  net->ib = ib;
   net->dev = dev;
   net->launch = default_launch(dev);
   *out = net;
@@ -369,6 +374,54 @@ int32_t pf_update_activity_coefs(PfNetwork* net, const PfCellState* state, void*
   int rc = validate_state(net, state);
   if (rc) return rc;
   return launch_update_activity_coefs(net->dev, *state, (cudaStream_t)stream) ? PF_ERR_CUDA : PF_OK;
+}
+
+int32_t pf_network_shift_parameters(PfNetwork* net, const double* dlogK_sec, const double* dlogK_mnrl,
+                                    const double* dlnk) {
+  if (!net) return PF_ERR_INVALID;
+  const DevNet& d = net->dev;
+  std::vector<double> v = net->dbls_base;
+  const bool csec = d.flags & NETF_SEC_LOGKCOEF, cmin = d.flags & NETF_MNRL_LOGKCOEF;
+  for (int i = 0; dlogK_sec && i < d.ns; ++i) {
+    v[d.o_sec_logK + i] += dlogK_sec[i];
+    if (csec) v[d.o_sec_logKcoef + 5 * i + 1] += dlogK_sec[i];
+  }
+  for (int m = 0; dlogK_mnrl && m < d.nm; ++m) {
+    v[d.o_mnrl_logK + m] += dlogK_mnrl[m];
+    if (cmin) v[d.o_mnrl_logKcoef + 5 * m + 1] += dlogK_mnrl[m];
+  }
+  for (int m = 0; dlnk && m < d.nm; ++m) v[d.o_rate + m] = v[d.o_rate + m] * std::exp(dlnk[m]);
+  if (cudaMemcpy((char*)net->d_tables + net->ib, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return PF_ERR_CUDA;
+  return PF_OK;
+}
+
+int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const PfAdjointArgs* a, void* stream) {
+  int rc = validate_state(net, state);
+  if (rc) return rc;
+  if (!a || !(dt > 0.0 || state->dt_cell)) return PF_ERR_INVALID;
+  const DevNet& d = net->dev;
+  if (!batched_supported(d)) return PF_ERR_UNSUPPORTED;
+  if (d.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) return PF_ERR_UNSUPPORTED;
+  if (!a->dL_dtotal0 || (d.nm > 0 && (!a->dL_dlnarea || !a->dL_dlogK_mnrl || !a->dL_dlnk)) ||
+      (d.ns > 0 && !a->dL_dlogK_sec) || (!a->weight && !a->dL_dtotal) || (a->weight && !a->target))
+    return PF_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (state->ncells == 0) return PF_OK;
+  rc = ensure_scratch(net, state->ncells);
+  if (rc) return rc;
+  cudaError_t e = cudaSuccess;
+  if (d.ns) e = cudaMemsetAsync(a->dL_dlogK_sec, 0, d.ns * sizeof(double), s);
+  if (e == cudaSuccess && d.nm) e = cudaMemsetAsync(a->dL_dlogK_mnrl, 0, d.nm * sizeof(double), s);
+  if (e == cudaSuccess && d.nm) e = cudaMemsetAsync(a->dL_dlnk, 0, d.nm * sizeof(double), s);
+  if (e == cudaSuccess && a->loss) e = cudaMemsetAsync(a->loss, 0, sizeof(double), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(net->d_counters, 0, 8 * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return PF_ERR_CUDA;
+  if (launch_rstep_batched(d, *state, dt, net->launch, net->num_sms, net->d_scratch, net->d_counters,
+                           net->d_counters + 1, s, a) != 0)
+    return PF_ERR_CUDA;
+  return PF_OK;
 }
 
 int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, const int32_t* ctype,

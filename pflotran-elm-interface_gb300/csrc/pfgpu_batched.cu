@@ -10,7 +10,8 @@ namespace pfgpu {
 
 #define PF_DECL(N)                                                                               \
   int launch_batched_##N(const DevNet&, const PfCellState&, double, const PfLaunchConfig&, int, \
-                         const double*, unsigned long long*, unsigned long long*, cudaStream_t);
+                         const double*, unsigned long long*, unsigned long long*, const PfAdjointArgs*, \
+                         cudaStream_t);
 PF_BATCHED_NCOMPS(PF_DECL)
 #undef PF_DECL
 
@@ -86,7 +87,7 @@ size_t batched_scratch_doubles(const DevNet& net, int64_t ncells) {
 
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
                          int num_sms, double* scratch, unsigned long long* queue, unsigned long long* counters,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, const PfAdjointArgs* adj) {
   {
     const int tpb = 128;
     const int64_t blocks = (st.ncells + tpb - 1) / tpb;
@@ -97,7 +98,7 @@ int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, co
   switch (net.n) {
 #define PF_CASE(N) \
   case N:          \
-    return launch_batched_##N(net, st, dt, cfg, num_sms, scratch, queue, counters, stream);
+    return launch_batched_##N(net, st, dt, cfg, num_sms, scratch, queue, counters, adj, stream);
     PF_BATCHED_NCOMPS(PF_CASE)
 #undef PF_CASE
     default:

@@ -49,7 +49,7 @@ __device__ __forceinline__ unsigned long long absbits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
-enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3 };
+enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3, BACK = 4 };
 
 template <int N, bool JS>
 struct Lane {
@@ -149,10 +149,10 @@ __device__ __forceinline__ double dh_ln_gamma(double z, double a0, double sI, do
   return fabs(z) > 1.0e-10 ? (-z * z * sI * net.A / (1.0 + a0 * net.B * sI) + net.Bdot * I) * LOG_TO_LN : 0.0;
 }
 
-template <int N, bool JS>
+template <int N, bool JS, bool ADJ>
 __global__ void __launch_bounds__(256)
 rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
-                     unsigned long long* queue, unsigned long long* counters) {
+                     unsigned long long* queue, unsigned long long* counters, PfAdjointArgs adj) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) uint64_t tma_bar;
   const int tid = threadIdx.x;
@@ -230,6 +230,22 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
   double temp = 25.0;
   double sqI = 0.0, lgI = 0.0;  // ionic strength of the last evaluation (NEWTON_ITER activity)
   bool dry = false;
+  // adjoint state (ADJ): converged iterate and dt of every substep, the
+  // running dL/dT, direct dL/dT0 of floored components, per-lane gradient
+  // accumulators for the network parameters, per-cell area gradient
+  constexpr int SMAX = ADJ ? PF_ADJ_MAX_SUBSTEPS : 1;
+  constexpr int SADJ = ADJ ? PF_MAX_NSEC : 1;
+  constexpr int MADJ = ADJ ? PF_MAX_NMNRL : 1;
+  double cst[SMAX][N], dts[SMAX];
+  double Tbar[N], gdir[N];
+  double sloc[SADJ], mImV[MADJ], mdQ[MADJ];
+  double gK[SADJ], gKm[MADJ], glnk[MADJ], garea[MADJ];
+  double loss_acc = 0.0;
+  int sb = 0;
+  if constexpr (ADJ) {
+    for (int i = 0; i < ns; ++i) gK[i] = 0.0;
+    for (int m = 0; m < nm; ++m) { gKm[m] = 0.0; glnk[m] = 0.0; }
+  }
   int its = 0, its_total = 0, nsub = 0, num_cuts = 0, n_const = 0;
   unsigned small_mask = 0;
   bool zero_step = false;
@@ -292,6 +308,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
     if (__all_sync(FULL, phase == DONE)) break;
 
     bool finish_cell = false, cell_failed = false;
+    bool back_done_flag = false, back_fail_flag = false;
     if (zero_step) {
       finish_cell = true;
       zero_step = false;
@@ -314,8 +331,14 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
     }
 
     // ------------------------------------------------------- Newton trip
-    if (phase == ITER) {
-      its += 1;
+    if (phase == ITER || (ADJ && phase == BACK)) {
+      // A backward trip (adjoint, BACK) shares the evaluation and the
+      // factorisation with a forward Newton trip: at the converged iterate of
+      // substep sb it solves J^T lambda = (dT/dlnm)^T Tbar with the true
+      // Jacobian (J is symmetric in the log formulation), then accumulates
+      // the parameter gradients.
+      const bool back = ADJ && phase == BACK;
+      if (!back) its += 1;
       if (newton_iter_act) {
         // RActivityCoefficients LAG (reaction.F90:4553-4612) from this
         // iterate and the previous evaluation's sec_molal
@@ -359,7 +382,11 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           const int pe = T.sec_pidx(p);
           s *= (pe >= 0) ? L.P(pe) : exp(T.sec_nu(p) * log(L.P(T.sec_idx(p))));
         }
-        st.sec_molal[soa.at(i, cell)] = s;
+        if (back) {
+          if constexpr (ADJ) sloc[i] = s;
+        } else {
+          st.sec_molal[soa.at(i, cell)] = s;
+        }
         const double sa = a_acc * s;
         for (int p = b; p < e; ++p) {
           const int kp = T.sec_idx(p);
@@ -371,22 +398,34 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
         }
       }
       const double b_tot = den_L / a_acc;
+      if (!back) {
 #pragma unroll
-      for (int j = 0; j < N; ++j) {
-        tot[j] = fma(b_tot, L.S(j), den_L * c[j]);
-        L.rhs(j) = dry ? 0.0 : fma(a_acc, c[j], L.S(j)) - fixed[j] * inv_dt;
+        for (int j = 0; j < N; ++j) {
+          tot[j] = fma(b_tot, L.S(j), den_L * c[j]);
+          L.rhs(j) = dry ? 0.0 : fma(a_acc, c[j], L.S(j)) - fixed[j] * inv_dt;
+        }
       }
-      if (dry) {
+      if (dry && !back) {
 #pragma unroll
         for (int i = 0; i < N; ++i)
 #pragma unroll
           for (int j = 0; j < N; ++j) L.J(i, j) = (i == j) ? (logf ? c[j] : 1.0) : 0.0;
-      } else if (logf) {
+      } else if (logf || back) {
 #pragma unroll
         for (int i = 0; i < N; ++i) {
 #pragma unroll
           for (int j = 0; j < i; ++j) L.J(i, j) = L.J(j, i);
           L.J(i, i) = fma(a_acc, c[i], L.J(i, i));
+        }
+        if (back) {
+          // xbar = (dT/dln m)^T Tbar = den*(diag(m) + G) Tbar = (den/a) J Tbar
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            double acc = 0.0;
+#pragma unroll
+            for (int j = 0; j < N; ++j) acc = fma(L.J(i, j), Tbar[j], acc);
+            L.rhs(i) = b_tot * acc;
+          }
         }
       } else {
         // linear formulation: d/dm_j = column j of G divided by m_j
@@ -410,7 +449,8 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       // ---- RKineticMineral (reaction_mineral.F90:647-1078) ---------------
       for (int m = 0; m < nm; ++m) {
         const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
-        rate[m] = 0.0;
+        if (!back) rate[m] = 0.0;
+        if constexpr (ADJ) { mImV[m] = 0.0; mdQ[m] = 0.0; }
         double QK = Kmin[m];
         for (int p = b; p < e; ++p) {
           const int pe = T.mnrl_pidx(p);
@@ -433,7 +473,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
         double Im_const = -st.mnrl_area[soa.at(m, cell)];
         if (has_msf) Im_const = Im_const / T.msf(m);
         double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * k : Im_const * sign_ * fabs(aff) * k;
-        rate[m] = Im;
+        if (!back) rate[m] = Im;
         if (dry) continue;  // RReaction returns before minerals in a dry cell
         Im_const = Im_const * volume;
         Im = Im * volume;
@@ -442,12 +482,22 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           dIm_dQK = dIm_dQK * (1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m))) / QK * (1.0 - aff);
         else if (has_msf)
           dIm_dQK = dIm_dQK * (1.0 / T.msf(m)) / QK * (1.0 - aff);
-        double f = dIm_dQK * QK * den_k * 1.0e-3;
+        // dIm/dQK * QK with the rate-limiter chain rule: the true d Im / d ln Q
+        double ft = dIm_dQK * QK;
         if (rl > 0.0) {
           const double den = 1.0 + (1.0 - aff) / rl;
-          f = f * (1.0 + QK / rl / den) / den;
+          ft = ft * (1.0 + QK / rl / den) / den;
         }
-        for (int p = b; p < e; ++p) L.rhs(T.mnrl_idx(p)) = fma(T.mnrl_nu(p), Im, L.rhs(T.mnrl_idx(p)));
+        // the reference's Jacobian multiplies dQK/dm by den*1e-3
+        // (reaction_mineral.F90:944-947), treating molality as molarity;
+        // Newton keeps it (same iterates), the adjoint uses the derivative
+        const double f = back ? ft : ft * den_k * 1.0e-3;
+        if constexpr (ADJ) {
+          mImV[m] = Im;
+          mdQ[m] = ft;
+        }
+        if (!back)
+          for (int p = b; p < e; ++p) L.rhs(T.mnrl_idx(p)) = fma(T.mnrl_nu(p), Im, L.rhs(T.mnrl_idx(p)));
         // d R / d ln m (log form: the m_q of the column scale cancels 1/m_q)
         for (int q = T.mpair_begin(m); q < T.mpair_begin(m + 1); ++q) {
           const int fl = T.mpair_idx(q);
@@ -467,7 +517,42 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       const double two_norm = sqrt(dot);
       if (its == 1) r0 = two_norm;
       int react_end = -1;  // -1: continue, 0: converged, 1: failed
-      if (its > o.maximum_reaction_iterations) {
+      bool back_done = false, back_fail = false;
+      if (back) {
+        if (lu_solve<N, JS>(L, indx, stride)) {
+          back_fail = true;
+        } else if constexpr (ADJ) {
+          // lambda = rhs.  theta_bar += (dT/dtheta)^T (Tbar - (psv/dt) lambda)
+          // - (dR/dtheta)^T lambda;  Tbar(previous substep) = (psv/dt) lambda
+          const double pd = a_acc / den_L;
+#pragma unroll
+          for (int j = 0; j < N; ++j) L.S(j) = Tbar[j] - pd * L.rhs(j);
+          for (int i = 0; i < ns; ++i) {
+            double acc = 0.0;
+            for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) acc = fma(T.sec_nu(p), L.S(T.sec_idx(p)), acc);
+            gK[i] = fma(acc, -LOG_TO_LN * den_L * sloc[i], gK[i]);
+          }
+          for (int m = 0; m < nm; ++m) {
+            if (mImV[m] == 0.0 && mdQ[m] == 0.0) continue;
+            double lam = 0.0;
+            for (int p = T.mnrl_begin(m); p < T.mnrl_end(m); ++p)
+              lam = fma(T.mnrl_nu(p), L.rhs(T.mnrl_idx(p)), lam);
+            gKm[m] = fma(LOG_TO_LN * mdQ[m], lam, gKm[m]);
+            glnk[m] = fma(-mImV[m], lam, glnk[m]);
+            garea[m] = fma(-mImV[m], lam, garea[m]);
+          }
+#pragma unroll
+          for (int j = 0; j < N; ++j) Tbar[j] = pd * L.rhs(j);
+          sb -= 1;
+          if (sb >= 0) {
+#pragma unroll
+            for (int j = 0; j < N; ++j) c[j] = cst[sb][j];
+            inv_dt = 1.0 / dts[sb];
+          } else {
+            back_done = true;
+          }
+        }
+      } else if (its > o.maximum_reaction_iterations) {
 #pragma unroll
         for (int j = 0; j < N; ++j) tot[j] = init_tot[j];
         react_end = 1;
@@ -510,8 +595,10 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           }
         }
       }
+      back_done_flag = back_done;
+      back_fail_flag = back_fail;
       // ------------------------------------------------ RStep bookkeeping
-      if (react_end >= 0) {
+      if (!back && react_end >= 0) {
         its_total += its;
         if (react_end == 1) {
           num_cuts = num_cuts + 1;
@@ -528,6 +615,13 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
             const double v = vf[m] + rate[m] * T.molar_vol(m) * dt;
             vf[m] = v < 0.0 ? 0.0 : v;
           }
+          if constexpr (ADJ) {
+            if (nsub < SMAX) {
+#pragma unroll
+              for (int j = 0; j < N; ++j) cst[nsub][j] = c[j];
+              dts[nsub] = dt;
+            }
+          }
           cum = cum + dt;
           nsub += 1;
           n_const += 1;
@@ -543,6 +637,20 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           if (cum >= target) finish_cell = true;
           else phase = START;
         }
+      }
+    }
+
+    if constexpr (ADJ) {
+      // end of a backward pass: per-cell gradients
+      if (phase == BACK && (back_done_flag || back_fail_flag)) {
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+          adj.dL_dtotal0[soa.at(j, cell)] =
+              back_fail_flag ? 0.0 : ((small_mask & (1u << j)) ? gdir[j] : Tbar[j]);
+        for (int m = 0; m < nm; ++m) adj.dL_dlnarea[soa.at(m, cell)] = back_fail_flag ? 0.0 : garea[m];
+        if (adj.adj_status) adj.adj_status[cell] = back_fail_flag ? 3 : 0;
+        back_done_flag = back_fail_flag = false;
+        phase = NEED;
       }
     }
 
@@ -576,7 +684,63 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       my_maxits = max(my_maxits, (unsigned long long)its_total);
       my_maxsub = max(my_maxsub, (unsigned long long)nsub);
       phase = NEED;
+      if constexpr (ADJ) {
+        // loss contribution and dL/dT(final); start the backward pass
+        double gsum = 0.0;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          double gj;
+          if (adj.weight) {
+            const double w = adj.weight[soa.at(j, cell)], d = tot[j] - adj.target[soa.at(j, cell)];
+            loss_acc = fma(w * d, d, loss_acc);
+            gj = 2.0 * w * d;
+          } else {
+            gj = adj.dL_dtotal[soa.at(j, cell)];
+          }
+          // a floored component's final total is its restored input
+          // (reaction.F90:3721-3725): dL/dT0 directly, no path through m
+          const bool fl = small_mask & (1u << j);
+          gdir[j] = fl ? gj : 0.0;
+          Tbar[j] = fl ? 0.0 : gj;
+          gsum += fabs(gj);
+        }
+        for (int m = 0; m < nm; ++m) garea[m] = 0.0;
+        const int astat = cell_failed ? 1 : (nsub > SMAX ? 2 : 0);
+        if (astat != 0 || dry || nsub == 0) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) adj.dL_dtotal0[soa.at(j, cell)] = (astat == 0) ? gdir[j] : 0.0;
+          for (int m = 0; m < nm; ++m) adj.dL_dlnarea[soa.at(m, cell)] = 0.0;
+          if (adj.adj_status) adj.adj_status[cell] = astat;
+        } else {
+          (void)gsum;
+          sb = nsub - 1;
+#pragma unroll
+          for (int j = 0; j < N; ++j) c[j] = cst[sb][j];
+          inv_dt = 1.0 / dts[sb];
+          phase = BACK;
+        }
+      }
     }
+  }
+  if constexpr (ADJ) {
+    // network-parameter gradients and the loss: warp sums, one atomic each
+    auto wsum = [&](double v) {
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(FULL, v, off);
+      return v;
+    };
+    for (int i = 0; i < ns; ++i) {
+      const double v = wsum(gK[i]);
+      if (lane_id == 0 && v != 0.0) atomicAdd(&adj.dL_dlogK_sec[i], v);
+    }
+    for (int m = 0; m < nm; ++m) {
+      const double a = wsum(gKm[m]), b = wsum(glnk[m]);
+      if (lane_id == 0) {
+        if (a != 0.0) atomicAdd(&adj.dL_dlogK_mnrl[m], a);
+        if (b != 0.0) atomicAdd(&adj.dL_dlnk[m], b);
+      }
+    }
+    const double l = wsum(loss_acc);
+    if (lane_id == 0 && adj.loss && l != 0.0) atomicAdd(adj.loss, l);
   }
   if (counters) {
     // warp-level reduction, one atomic per warp
@@ -597,26 +761,33 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
 
 }  // namespace batched
 
+template <int N, bool JS, bool ADJ>
+int launch_batched_k(const DevNet& net, const PfCellState& st, double dt, size_t smem, int grid, int tpb,
+                     const double* scratch, unsigned long long* queue, unsigned long long* counters,
+                     const PfAdjointArgs& adj, cudaStream_t stream) {
+  auto k = batched::rstep_batched_kernel<N, JS, ADJ>;
+  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return (int)err;
+  k<<<grid, tpb, smem, stream>>>(net, st, dt, scratch, queue, counters, adj);
+  return (int)cudaGetLastError();
+}
+
 template <int N>
 int launch_batched_n(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
                      int num_sms, const double* scratch, unsigned long long* queue,
-                     unsigned long long* counters, cudaStream_t stream) {
+                     unsigned long long* counters, const PfAdjointArgs* adj, cudaStream_t stream) {
   const size_t smem = batched_smem_bytes(net, cfg);
   const int tpb = cfg.threads_per_block;
   const int grid = num_sms * cfg.blocks_per_sm;
-  cudaError_t err;
-  if (cfg.jac_in_shared) {
-    auto k = batched::rstep_batched_kernel<N, true>;
-    err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return (int)err;
-    k<<<grid, tpb, smem, stream>>>(net, st, dt, scratch, queue, counters);
-  } else {
-    auto k = batched::rstep_batched_kernel<N, false>;
-    err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return (int)err;
-    k<<<grid, tpb, smem, stream>>>(net, st, dt, scratch, queue, counters);
+  const PfAdjointArgs none{};
+  if (adj) {
+    if (cfg.jac_in_shared)
+      return launch_batched_k<N, true, true>(net, st, dt, smem, grid, tpb, scratch, queue, counters, *adj, stream);
+    return launch_batched_k<N, false, true>(net, st, dt, smem, grid, tpb, scratch, queue, counters, *adj, stream);
   }
-  return (int)cudaGetLastError();
+  if (cfg.jac_in_shared)
+    return launch_batched_k<N, true, false>(net, st, dt, smem, grid, tpb, scratch, queue, counters, none, stream);
+  return launch_batched_k<N, false, false>(net, st, dt, smem, grid, tpb, scratch, queue, counters, none, stream);
 }
 
 }  // namespace pfgpu

@@ -4,7 +4,7 @@
 namespace pfgpu {
 int launch_batched_24(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
                       int num_sms, const double* scratch, unsigned long long* queue,
-                      unsigned long long* counters, cudaStream_t stream) {
-  return launch_batched_n<24>(net, st, dt, cfg, num_sms, scratch, queue, counters, stream);
+                      unsigned long long* counters, const PfAdjointArgs* adj, cudaStream_t stream) {
+  return launch_batched_n<24>(net, st, dt, cfg, num_sms, scratch, queue, counters, adj, stream);
 }
 }  // namespace pfgpu

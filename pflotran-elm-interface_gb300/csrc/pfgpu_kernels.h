@@ -16,7 +16,7 @@ int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt,
                          const PfLaunchConfig& cfg, int num_sms, double* scratch,
                          unsigned long long* queue, unsigned long long* counters,
-                         cudaStream_t stream);
+                         cudaStream_t stream, const PfAdjointArgs* adj = nullptr);
 // doubles of per-cell scratch the batched kernel's setup pre-pass writes
 size_t batched_scratch_doubles(const DevNet& net, int64_t ncells);
 // shared memory bytes a batched launch of this config needs

@@ -102,6 +102,17 @@ class PfStepStats(C.Structure):
     ]
 
 
+PF_ADJ_MAX_SUBSTEPS = 16
+
+
+class PfAdjointArgs(C.Structure):
+    _fields_ = [
+        ("weight", _dp), ("target", _dp), ("dL_dtotal", _dp), ("dL_dtotal0", _dp),
+        ("dL_dlnarea", _dp), ("dL_dlogK_sec", _dp), ("dL_dlogK_mnrl", _dp), ("dL_dlnk", _dp),
+        ("loss", _dp), ("adj_status", _ip),
+    ]
+
+
 class PfLaunchConfig(C.Structure):
     _fields_ = [
         ("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
@@ -124,6 +135,8 @@ SIGNATURES = {
                              C.POINTER(PfStepStats)]),
     "pf_update_auxvars": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_int32, _P]),
     "pf_update_activity_coefs": (C.c_int32, [_P, C.POINTER(PfCellState), _P]),
+    "pf_adjoint": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.POINTER(PfAdjointArgs), _P]),
+    "pf_network_shift_parameters": (C.c_int32, [_P, _dp, _dp, _dp]),
     "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
                                   C.POINTER(PfStepStats)]),

@@ -121,6 +121,60 @@ class ReactionEngine:
                       _stream_ptr(stream)), allow_cell_failures=False)
         return its
 
+    def shift_parameters(self, dlogK_sec=None, dlogK_mnrl=None, dlnk=None):
+        """logK += shift for every secondary / kinetic mineral (at every
+        temperature), rate constants *= exp(dlnk), from the values at
+        creation.  Host sequences or None."""
+        def arr(a, n):
+            if a is None:
+                return None, None
+            a = np.ascontiguousarray(np.asarray(a, np.float64).reshape(n))
+            return a, a.ctypes.data_as(C.POINTER(C.c_double))
+        a1, p1 = arr(dlogK_sec, self.net.nsec)
+        a2, p2 = arr(dlogK_mnrl, self.net.nmnrl)
+        a3, p3 = arr(dlnk, self.net.nmnrl)
+        abi.check("pf_network_shift_parameters",
+                  self.lib.pf_network_shift_parameters(self.handle, p1, p2, p3), allow_cell_failures=False)
+
+    def adjoint(self, state: CellState, dt: float, weight=None, target=None, dL_dtotal=None, order=None,
+                stream=None):
+        """Forward step (state is advanced as by rstep) plus the adjoint of the
+        step.  Loss: sum weight*(total_final - target)^2 when weight/target
+        are given, else dL/dtotal_final = dL_dtotal.  Returns a dict of CUDA
+        tensors: dL_dtotal0 (ncomp, ncells), dL_dlnarea (nmnrl, ncells),
+        dL_dlogK_sec (nsec), dL_dlogK_mnrl (nmnrl), dL_dlnk (nmnrl), loss (1),
+        adj_status (ncells)."""
+        import torch
+        dev = state.a["porosity"].device
+        n, ns, nm, N = self.net.ncomp, self.net.nsec, self.net.nmnrl, state.ncells
+        f64 = dict(dtype=torch.float64, device=dev)
+        out = dict(dL_dtotal0=torch.zeros((n, N), **f64), dL_dlnarea=torch.zeros((max(nm, 1), N), **f64),
+                   dL_dlogK_sec=torch.zeros(max(ns, 1), **f64), dL_dlogK_mnrl=torch.zeros(max(nm, 1), **f64),
+                   dL_dlnk=torch.zeros(max(nm, 1), **f64), loss=torch.zeros(1, **f64),
+                   adj_status=torch.zeros(N, dtype=torch.int32, device=dev))
+        a = abi.PfAdjointArgs()
+
+        def ptr(t, ct=C.c_double):
+            return C.cast(None if t is None else t.contiguous().data_ptr(), C.POINTER(ct))
+        keep = [weight, target, dL_dtotal]
+        a.weight, a.target, a.dL_dtotal = ptr(weight), ptr(target), ptr(dL_dtotal)
+        a.dL_dtotal0, a.dL_dlnarea = ptr(out["dL_dtotal0"]), ptr(out["dL_dlnarea"])
+        a.dL_dlogK_sec, a.dL_dlogK_mnrl = ptr(out["dL_dlogK_sec"]), ptr(out["dL_dlogK_mnrl"])
+        a.dL_dlnk, a.loss = ptr(out["dL_dlnk"]), ptr(out["loss"])
+        a.adj_status = ptr(out["adj_status"], C.c_int32)
+        s = state.struct()
+        if order is not None:
+            s.cell_order = C.cast(order.data_ptr(), C.POINTER(C.c_int64))
+        abi.check("pf_adjoint", self.lib.pf_adjoint(self.handle, C.byref(s), float(dt), C.byref(a),
+                                                    _stream_ptr(stream)), allow_cell_failures=False)
+        del keep
+        if nm == 0:
+            for k in ("dL_dlnarea", "dL_dlogK_mnrl", "dL_dlnk"):
+                out[k] = out[k][:0]
+        if ns == 0:
+            out["dL_dlogK_sec"] = out["dL_dlogK_sec"][:0]
+        return out
+
     def update_activity_coefs(self, state: CellState, stream=None):
         s = state.struct()
         abi.check("pf_update_activity_coefs",
