@@ -53,16 +53,30 @@ def _gross_total(net, st):
     return g * st.a["den_kg"] * 1e-3
 
 
+def _cell_err(net, ref, got):
+    """Per-cell maximum relative difference over every compared quantity."""
+    def r(a, b, scale):
+        return (np.abs(a - b) / scale).reshape(-1, ref.ncells).max(axis=0)
+    e = r(got.a["pri_molal"], ref.a["pri_molal"], np.abs(ref.a["pri_molal"]))
+    if net.nsec:
+        e = np.maximum(e, r(got.a["sec_molal"], ref.a["sec_molal"], np.maximum(np.abs(ref.a["sec_molal"]), 1e-300)))
+    e = np.maximum(e, r(got.a["total"], ref.a["total"], _gross_total(net, ref)))
+    if net.nmnrl:
+        e = np.maximum(e, r(got.a["mnrl_rate"], ref.a["mnrl_rate"], np.maximum(np.abs(ref.a["mnrl_rate"]), 1e-30)))
+        e = np.maximum(e, r(got.a["mnrl_volfrac"], ref.a["mnrl_volfrac"],
+                            np.maximum(np.abs(ref.a["mnrl_volfrac"]), 1e-30)))
+    return e
+
+
 def _path_stats(net, ref, got):
     """(flips among single-RReact cells, path-identical single cells, count of
-    those with a pri_molal/sec_molal difference above REL)."""
+    those with any compared quantity differing by REL or more)."""
     single = (ref.a["num_substeps"] == 1) & (ref.a["status"] == 0) & \
         (ref.a["newton_its"] <= net.options["maximum_reaction_iterations"])
     path = (ref.a["newton_its"] == got.a["newton_its"]) & (ref.a["num_substeps"] == got.a["num_substeps"]) & \
         (ref.a["status"] == got.a["status"])
     same = single & path
-    e = np.abs(got.a["pri_molal"] - ref.a["pri_molal"]) / np.abs(ref.a["pri_molal"])
-    bad = same & (e.max(axis=0) >= REL)
+    bad = same & (_cell_err(net, ref, got) >= REL)
     return int((single & ~path).sum()), same, int(bad.sum())
 
 
@@ -79,8 +93,7 @@ def compare(net, ref, got, label, self_ref=None):
     if self_ref is not None:
         self_flips, _, self_out = _path_stats(net, ref, self_ref)
     # value errors over the compared cells that are not outliers
-    e_cell = (np.abs(got.a["pri_molal"] - ref.a["pri_molal"]) / np.abs(ref.a["pri_molal"])).max(axis=0)
-    same_ok = same & (e_cell < REL) if outliers else same
+    same_ok = same & (_cell_err(net, ref, got) < REL)
     errs = {}
 
     def rel(a, b, scale):
