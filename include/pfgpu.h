@@ -310,6 +310,47 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt,
 int32_t pf_network_shift_parameters(PfNetwork* net, const double* dlogK_sec,
                                     const double* dlogK_mnrl, const double* dlnk);
 
+/* ---------------------------------------------------- global implicit (GIRT) */
+/*
+ * Residual and Jacobian of the global-implicit reactive-transport system on a
+ * structured grid nx*ny*nz (cell index i + nx*(j + ny*k)), 7-point stencil,
+ * zero-flux outer boundary: replaces RTResidual (reactive_transport.F90:1964)
+ * and RTJacobian (:2788) for that grid -- per internal connection TFluxCoef/
+ * TFlux/TFluxDerivative (transport.F90:378-565) with the harmonic mean of
+ * TDispersion (:52-232), per cell RTAccumulation[Derivative] and
+ * RReaction[Derivative], ADD_VALUES in the reference's connection order,
+ * then the log-formulation column scaling (MatDiagonalScaleLocal, :2879).
+ * The state holds the current Newton iterate (pri_molal) and the activity
+ * coefficients; total and sec_molal are updated (RTUpdateAuxVars).
+ */
+typedef struct PfGirtArgs {
+  int32_t nx, ny, nz;
+  double dx, dy, dz;                 /* m (cell sizes; faces dy*dz, dx*dz, dx*dy) */
+  const double* qx;                  /* [nz][ny][nx-1] Darcy flux across x faces, m/s,
+                                        positive from cell i to cell i+1 */
+  const double* qy;                  /* [nz][ny-1][nx] */
+  const double* qz;                  /* [nz-1][ny][nx] */
+  double diffusion_coefficient;      /* m^2/s, all components */
+  double tortuosity;
+  double dispersivity;               /* longitudinal, m */
+  const double* total_k;             /* [ncomp][ncells] totals at the start of the
+                                        time step (fixed accumulation) */
+  double dt;                         /* s */
+  const int32_t* rowptr;             /* BAIJ pattern from pf_girt_pattern (device) */
+  const int32_t* colidx;
+  double* residual;                  /* [ncells*ncomp] out, PETSc block-interleaved */
+  double* values;                    /* [nnzb*ncomp*ncomp] out, SeqBAIJ blocks,
+                                        each column-major */
+} PfGirtArgs;
+
+/* Host: block-row pattern of the 7-point structured-grid matrix (block
+ * columns ascending).  rowptr[ncells+1], colidx[nnzb]; either may be NULL to
+ * query the size.  Returns nnzb (>= 0) or a PfStatus (< 0). */
+int32_t pf_girt_pattern(int32_t nx, int32_t ny, int32_t nz, int32_t* rowptr, int32_t* colidx);
+
+int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtArgs* args,
+                         void* stream);
+
 /* ----------------------------------------------------------- constraints */
 /* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */
 enum {

@@ -47,10 +47,13 @@ class Oracle:
         lib.oracle_update_activity_coefs.argtypes = [D, S, C.c_int]
         lib.oracle_equilibrate.argtypes = [D, S, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                            C.c_int, C.POINTER(C.c_int32), C.c_int]
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        lib.oracle_girt_assemble.argtypes = [D, S, ip, dp, dp, dp, dp, dp, C.c_double, ip, ip, dp, dp]
         lib.oracle_ifc67_density.argtypes = [C.c_double, C.c_double]
         lib.oracle_ifc67_density.restype = C.c_double
         for f in ("oracle_rstep", "oracle_rreact", "oracle_implicit_step", "oracle_update_kinetic_state",
-                  "oracle_update_auxvars", "oracle_update_activity_coefs", "oracle_equilibrate"):
+                  "oracle_update_auxvars", "oracle_update_activity_coefs", "oracle_equilibrate",
+                  "oracle_girt_assemble"):
             getattr(lib, f).restype = C.c_int
         self.lib = lib
 
@@ -95,6 +98,31 @@ class Oracle:
                                          int(use_prev), its.ctypes.data_as(C.POINTER(C.c_int32)),
                                          nthreads)
         return rc, its
+
+    def girt_assemble(self, net, state, grid, total_k, dt, rowptr, colidx):
+        """Global-implicit residual [ncells*ncomp] and SeqBAIJ values
+        [nnzb*ncomp*ncomp] (blocks column-major) of a structured grid.
+        grid: dict nx, ny, nz, dx, dy, dz, qx, qy, qz, diffusion, tortuosity,
+        dispersivity.  Updates state's total and sec_molal."""
+        d, s = self._args(net, state)
+        f = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+        gi = np.array([grid["nx"], grid["ny"], grid["nz"]], np.int32)
+        gd = f([grid["dx"], grid["dy"], grid["dz"], grid["diffusion"], grid["tortuosity"], grid["dispersivity"]])
+        q = [f(grid[k]) if np.size(grid[k]) else np.zeros(1) for k in ("qx", "qy", "qz")]
+        tk = f(total_k)
+        rp, ci = np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colidx, np.int32)
+        n = net.ncomp
+        r = np.zeros(state.ncells * n)
+        vals = np.zeros(int(rp[-1]) * n * n)
+        dp = C.POINTER(C.c_double)
+        P = lambda a: a.ctypes.data_as(dp)  # noqa: E731
+        rc = self.lib.oracle_girt_assemble(C.byref(d), C.byref(s), gi.ctypes.data_as(C.POINTER(C.c_int32)), P(gd),
+                                           P(q[0]), P(q[1]), P(q[2]), P(tk), float(dt),
+                                           rp.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           ci.ctypes.data_as(C.POINTER(C.c_int32)), P(r), P(vals))
+        if rc:
+            raise RuntimeError("oracle_girt_assemble: %d" % rc)
+        return r, vals
 
     def density(self, t, p):
         return self.lib.oracle_ifc67_density(t, p)

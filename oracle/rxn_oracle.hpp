@@ -841,4 +841,161 @@ inline int equilibrate_constraint(const Net& net, Cell& c, const int* ctype,
   return num_iterations;
 }
 
+// ---------------------------------------------------------------------------
+// Global-implicit residual and Jacobian on a structured grid (config: 7-point
+// stencil, zero-flux outer boundary, saturation 1, no dispersion beyond the
+// longitudinal term).  Restates
+//   RTResidualFlux   reactive_transport.F90:2052-2291 (internal connections)
+//   RTResidualNonFlux                     :2293-2669 (accumulation, reaction)
+//   RTJacobianFlux                        :2897-3086
+//   RTJacobianNonFlux                     :3088-3349 (incl. log scaling :3316-3340,
+//                                          MatDiagonalScaleLocal at :2879)
+//   TDispersion/TFluxCoef/TFlux/TFluxDerivative transport.F90:52-609
+// with the connection order of StructGridComputeInternConnect
+// (grid_structured.F90:969-1011): x faces, then y, then z, each with k, j, i
+// loops; every block is added in that order (ADD_VALUES), then accumulation,
+// then reaction.  Cell index: i + nx*(j + ny*k).  Output BAIJ: block rows in
+// cell order, block columns ascending, each bs x bs block column-major
+// (PETSc SeqBAIJ storage).
+struct GirtGrid {
+  int nx, ny, nz;
+  double dx, dy, dz;
+  const double* qx;   // [nz][ny][nx-1]
+  const double* qy;   // [nz][ny-1][nx]
+  const double* qz;   // [nz-1][ny][nx]
+  double diffusion;   // D_m, m^2/s
+  double tortuosity;
+  double dispersivity;  // longitudinal
+};
+
+// harmonic_tran_coefs_over_dist of TDispersion for one connection
+inline double girt_tran_coef(const Cell& up, const Cell& dn, double q, double dist, double dfrac,
+                             const GirtGrid& g) {
+  double dist_up = dist * dfrac;
+  double dist_dn = dist - dist_up;
+  if (up.sat < rt_min_saturation || dn.sat < rt_min_saturation) return 0.0;
+  double mech_up = g.dispersivity * std::fabs(q);
+  double mech_dn = g.dispersivity * std::fabs(q);
+  double hd_up = std::max(mech_up + 1.0 * up.sat * up.porosity * g.tortuosity * g.diffusion, 1.0e-40);
+  double hd_dn = std::max(mech_dn + 1.0 * dn.sat * dn.porosity * g.tortuosity * g.diffusion, 1.0e-40);
+  return (hd_up * hd_dn) / (hd_up * dist_dn + hd_dn * dist_up);
+}
+
+// r: [ncells*n] (block interleaved), values: [nnzb*n*n], rowptr/colidx: BAIJ
+// pattern, fixed_total: totals at the previous time (accum_k = psv*total_k).
+inline void girt_assemble(const Net& net, Cell* cells, const GirtGrid& g, const double* fixed_total,
+                          double dt, const int* rowptr, const int* colidx, double* r, double* values) {
+  const int n = net.n;
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const long long N = (long long)nx * ny * nz;
+  auto idx = [&](int i, int j, int k) { return (long long)i + (long long)nx * (j + (long long)ny * k); };
+  for (long long c = 0; c < N; ++c) {
+    set_logK(net, cells[c]);
+    total_aqueous(net, cells[c]);  // RTUpdateAuxVars
+  }
+  for (long long e = 0; e < N * n; ++e) r[e] = 0.0;
+  const long long nnzb = rowptr[N];
+  for (long long e = 0; e < nnzb * n * n; ++e) values[e] = 0.0;
+  auto block = [&](long long row, long long col) -> double* {
+    for (int b = rowptr[row]; b < rowptr[row + 1]; ++b)
+      if (colidx[b] == col) return values + (long long)b * n * n;
+    return nullptr;
+  };
+  // J(i,j) in column-major storage: blk[j*n + i]
+  auto connection = [&](long long up, long long dn, double q, double area, double dist) {
+    const Cell& cu = cells[up];
+    const Cell& cd = cells[dn];
+    double coef_up[MAXN], coef_dn[MAXN];
+    double tran = girt_tran_coef(cu, cd, q, dist, 0.5, g);
+    if (cd.sat < rt_min_saturation || cu.sat < rt_min_saturation) {
+      for (int k = 0; k < n; ++k) coef_up[k] = coef_dn[k] = 0.0;
+    } else {
+      for (int k = 0; k < n; ++k) {
+        double cup, cdn;
+        if (q > 0.0) { cup = tran + q; cdn = -tran; }
+        else { cup = tran; cdn = -tran + q; }
+        coef_up[k] = cup * area * 1000.0;
+        coef_dn[k] = cdn * area * 1000.0;
+      }
+    }
+    double Res[MAXN];
+    for (int k = 0; k < n; ++k) Res[k] = coef_up[k] * cu.total[k] + coef_dn[k] * cd.total[k];
+    for (int k = 0; k < n; ++k) {
+      r[up * n + k] = r[up * n + k] + Res[k];
+      r[dn * n + k] = r[dn * n + k] - Res[k];
+    }
+    double* b_uu = block(up, up);
+    double* b_ud = block(up, dn);
+    double* b_dd = block(dn, dn);
+    double* b_du = block(dn, up);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double Jup = cu.dtotal[i * MAXN + j] * coef_up[i];
+        double Jdn = cd.dtotal[i * MAXN + j] * coef_dn[i];
+        b_uu[j * n + i] = b_uu[j * n + i] + Jup;
+        b_ud[j * n + i] = b_ud[j * n + i] + Jdn;
+        b_dd[j * n + i] = b_dd[j * n + i] + (-Jdn);
+        b_du[j * n + i] = b_du[j * n + i] + (-Jup);
+      }
+  };
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx - 1; ++i)
+        connection(idx(i, j, k), idx(i + 1, j, k), g.qx[((long long)k * ny + j) * (nx - 1) + i], g.dy * g.dz, g.dx);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny - 1; ++j)
+      for (int i = 0; i < nx; ++i)
+        connection(idx(i, j, k), idx(i, j + 1, k), g.qy[((long long)k * (ny - 1) + j) * nx + i], g.dx * g.dz, g.dy);
+  for (int k = 0; k < nz - 1; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        connection(idx(i, j, k), idx(i, j, k + 1), g.qz[((long long)k * ny + j) * nx + i], g.dx * g.dy, g.dz);
+  // NonFlux: r = r - accum_k/dt; + accumulation/dt; + reaction
+  for (long long c = 0; c < N; ++c) {
+    Cell& cl = cells[c];
+    double psv_t = cl.porosity * cl.sat * 1000.0 * cl.volume;
+    for (int k = 0; k < n; ++k) {
+      double accum_k = cl.sat < rt_min_saturation ? 0.0 : psv_t * fixed_total[(long long)k * N + c];
+      r[c * n + k] = r[c * n + k] - accum_k / dt;
+    }
+    double Res[MAXN];
+    accumulation(net, cl, Res);
+    for (int k = 0; k < n; ++k) Res[k] = Res[k] / dt;
+    for (int k = 0; k < n; ++k) r[c * n + k] = r[c * n + k] + Res[k];
+  }
+  for (long long c = 0; c < N; ++c) {
+    double J[MAXN * MAXN];
+    accumulation_derivative(net, cells[c], dt, J);
+    double* b = block(c, c);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) b[j * n + i] = b[j * n + i] + J[i * MAXN + j];
+  }
+  for (long long c = 0; c < N; ++c) {
+    double Res[MAXN], J[MAXN * MAXN];
+    for (int k = 0; k < n; ++k) Res[k] = 0.0;
+    for (int e = 0; e < MAXN * MAXN; ++e) J[e] = 0.0;
+    reaction(net, cells[c], Res, J, false);
+    for (int k = 0; k < n; ++k) r[c * n + k] = r[c * n + k] + Res[k];
+  }
+  for (long long c = 0; c < N; ++c) {
+    double Res[MAXN], J[MAXN * MAXN];
+    for (int k = 0; k < n; ++k) Res[k] = 0.0;
+    for (int e = 0; e < MAXN * MAXN; ++e) J[e] = 0.0;
+    reaction_derivative(net, cells[c], Res, J);
+    double* b = block(c, c);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) b[j * n + i] = b[j * n + i] + J[i * MAXN + j];
+  }
+  // log formulation: right-scale every block column by the free-ion molality
+  if (net.o.use_log_formulation) {
+    for (long long row = 0; row < N; ++row)
+      for (int b = rowptr[row]; b < rowptr[row + 1]; ++b) {
+        const Cell& cc = cells[colidx[b]];
+        double* blk = values + (long long)b * n * n;
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i) blk[j * n + i] = blk[j * n + i] * cc.pri_molal[j];
+      }
+  }
+}
+
 }  // namespace oracle

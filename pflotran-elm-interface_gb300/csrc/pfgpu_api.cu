@@ -15,6 +15,10 @@ extern "C" int32_t pf_equilibrate_constraint_impl(const DevNet* net, const PfCel
                                                   const int32_t* ctype, const double* cconc, int use_prev,
                                                   int32_t* iterations, int max_iterations, void* stream);
 
+extern "C" int32_t pf_girt_assemble_impl(const DevNet* net, const PfCellState* st, const PfGirtArgs* a,
+                                         double* scratch, void* stream);
+extern "C" size_t pf_girt_scratch_doubles(int32_t n, int64_t ncells);
+
 struct PfNetwork {
   DevNet dev{};
   void* d_tables = nullptr;
@@ -289,8 +293,11 @@ int32_t pf_network_set_options(PfNetwork* net, const PfOptions* opts) {
   return PF_OK;
 }
 
+static int ensure_scratch_doubles(PfNetwork* net, size_t need);
 static int ensure_scratch(PfNetwork* net, int64_t ncells) {
-  const size_t need = batched_scratch_doubles(net->dev, ncells);
+  return ensure_scratch_doubles(net, batched_scratch_doubles(net->dev, ncells));
+}
+static int ensure_scratch_doubles(PfNetwork* net, size_t need) {
   if (need <= net->scratch_cap) return PF_OK;
   if (net->d_scratch) cudaFree(net->d_scratch);
   net->d_scratch = nullptr;
@@ -422,6 +429,20 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
                            net->d_counters + 1, s, a) != 0)
     return PF_ERR_CUDA;
   return PF_OK;
+}
+
+int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtArgs* a, void* stream) {
+  int rc = validate_state(net, state);
+  if (rc) return rc;
+  if (!a || a->nx < 1 || a->ny < 1 || a->nz < 1 || !(a->dt > 0.0) || !a->total_k || !a->rowptr ||
+      !a->colidx || !a->residual || !a->values || !(a->dx > 0) || !(a->dy > 0) || !(a->dz > 0))
+    return PF_ERR_INVALID;
+  if ((int64_t)a->nx * a->ny * a->nz != state->ncells) return PF_ERR_INVALID;
+  if ((a->nx > 1 && !a->qx) || (a->ny > 1 && !a->qy) || (a->nz > 1 && !a->qz)) return PF_ERR_INVALID;
+  if (!state->sec_molal && net->dev.ns) return PF_ERR_INVALID;
+  rc = ensure_scratch_doubles(net, pf_girt_scratch_doubles(net->dev.n, state->ncells));
+  if (rc) return rc;
+  return pf_girt_assemble_impl(&net->dev, state, a, net->d_scratch, stream);
 }
 
 int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, const int32_t* ctype,

@@ -418,13 +418,13 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           L.J(i, i) = fma(a_acc, c[i], L.J(i, i));
         }
         if (back) {
-          // xbar = (dT/dln m)^T Tbar = den*(diag(m) + G) Tbar = (den/a) J Tbar
+          // the backward solve is J u = B Tbar with B the minerals' part of
+          // J (u = Tbar - (psv/dt) lambda, formed without cancellation);
+          // Tbar by species id for the mineral loop goes to S
 #pragma unroll
           for (int i = 0; i < N; ++i) {
-            double acc = 0.0;
-#pragma unroll
-            for (int j = 0; j < N; ++j) acc = fma(L.J(i, j), Tbar[j], acc);
-            L.rhs(i) = b_tot * acc;
+            L.rhs(i) = 0.0;
+            L.S(i) = Tbar[i];
           }
         }
       } else {
@@ -496,13 +496,19 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           mImV[m] = Im;
           mdQ[m] = ft;
         }
-        if (!back)
+        if (!back) {
           for (int p = b; p < e; ++p) L.rhs(T.mnrl_idx(p)) = fma(T.mnrl_nu(p), Im, L.rhs(T.mnrl_idx(p)));
+        } else {
+          double nuT = 0.0;
+          for (int p = b; p < e; ++p) nuT = fma(T.mnrl_nu(p), L.S(T.mnrl_idx(p)), nuT);
+          for (int p = b; p < e; ++p)
+            L.rhs(T.mnrl_idx(p)) = fma(T.mnrl_nu(p) * f, nuT, L.rhs(T.mnrl_idx(p)));
+        }
         // d R / d ln m (log form: the m_q of the column scale cancels 1/m_q)
         for (int q = T.mpair_begin(m); q < T.mpair_begin(m + 1); ++q) {
           const int fl = T.mpair_idx(q);
           const double v = T.mpair_coef(q) * f;
-          L.Jf(fl) = fma(v, logf ? 1.0 : L.S(fl % N), L.Jf(fl));
+          L.Jf(fl) = fma(v, (logf || back) ? 1.0 : L.S(fl % N), L.Jf(fl));
         }
       }
       // ---- convergence tests on the residual (reaction.F90:3946-3953) -----
@@ -522,11 +528,15 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
         if (lu_solve<N, JS>(L, indx, stride)) {
           back_fail = true;
         } else if constexpr (ADJ) {
-          // lambda = rhs.  theta_bar += (dT/dtheta)^T (Tbar - (psv/dt) lambda)
-          // - (dR/dtheta)^T lambda;  Tbar(previous substep) = (psv/dt) lambda
+          // u = rhs; lambda = (Tbar - u)/(psv/dt).  theta_bar += (dT/dtheta)^T u
+          // - (dR/dtheta)^T lambda;  Tbar(previous substep) = Tbar - u
           const double pd = a_acc / den_L;
+          const double ipd = 1.0 / pd;
 #pragma unroll
-          for (int j = 0; j < N; ++j) L.S(j) = Tbar[j] - pd * L.rhs(j);
+          for (int j = 0; j < N; ++j) {
+            L.S(j) = L.rhs(j);                       // u
+            L.rhs(j) = (Tbar[j] - L.rhs(j)) * ipd;   // lambda
+          }
           for (int i = 0; i < ns; ++i) {
             double acc = 0.0;
             for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) acc = fma(T.sec_nu(p), L.S(T.sec_idx(p)), acc);
@@ -542,7 +552,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
             garea[m] = fma(-mImV[m], lam, garea[m]);
           }
 #pragma unroll
-          for (int j = 0; j < N; ++j) Tbar[j] = pd * L.rhs(j);
+          for (int j = 0; j < N; ++j) Tbar[j] = Tbar[j] - L.S(j);
           sb -= 1;
           if (sb >= 0) {
 #pragma unroll

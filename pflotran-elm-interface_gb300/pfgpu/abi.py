@@ -113,6 +113,17 @@ class PfAdjointArgs(C.Structure):
     ]
 
 
+class PfGirtArgs(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+        ("qx", _dp), ("qy", _dp), ("qz", _dp),
+        ("diffusion_coefficient", C.c_double), ("tortuosity", C.c_double), ("dispersivity", C.c_double),
+        ("total_k", _dp), ("dt", C.c_double), ("rowptr", _ip), ("colidx", _ip),
+        ("residual", _dp), ("values", _dp),
+    ]
+
+
 class PfLaunchConfig(C.Structure):
     _fields_ = [
         ("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
@@ -137,6 +148,8 @@ SIGNATURES = {
     "pf_update_activity_coefs": (C.c_int32, [_P, C.POINTER(PfCellState), _P]),
     "pf_adjoint": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.POINTER(PfAdjointArgs), _P]),
     "pf_network_shift_parameters": (C.c_int32, [_P, _dp, _dp, _dp]),
+    "pf_girt_pattern": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, _ip, _ip]),
+    "pf_girt_assemble": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(PfGirtArgs), _P]),
     "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
                                   C.POINTER(PfStepStats)]),

@@ -36,7 +36,10 @@ class RStepFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, engine, state: CellState, dt, dlogK_sec, dlogK_mnrl, dlnk, lnarea, total0):
         st = _prepared(engine, state, dlogK_sec, dlogK_mnrl, dlnk, lnarea, total0)
-        engine.rstep(st, dt, stats=False)
+        try:
+            engine.rstep(st, dt, stats=False)
+        finally:
+            engine.shift_parameters()
         ctx.engine, ctx.state, ctx.dt = engine, state, dt
         ctx.save_for_backward(dlogK_sec, dlogK_mnrl, dlnk, lnarea, total0)
         ctx.mark_non_differentiable()
@@ -47,7 +50,10 @@ class RStepFunction(torch.autograd.Function):
         dlogK_sec, dlogK_mnrl, dlnk, lnarea, total0 = ctx.saved_tensors
         eng = ctx.engine
         st = _prepared(eng, ctx.state, dlogK_sec, dlogK_mnrl, dlnk, lnarea, total0)
-        g = eng.adjoint(st, ctx.dt, dL_dtotal=grad_total.contiguous())
+        try:
+            g = eng.adjoint(st, ctx.dt, dL_dtotal=grad_total.contiguous())
+        finally:
+            eng.shift_parameters()
         return (None, None, None, g["dL_dlogK_sec"], g["dL_dlogK_mnrl"], g["dL_dlnk"], g["dL_dlnarea"],
                 g["dL_dtotal0"])
 

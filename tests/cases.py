@@ -64,3 +64,24 @@ def case(oracle, name, tight=False):
 CASE_DT = {"calcite": 3600.0, "random12": 86400.0, "random12raw": 86400.0}
 CASE_DT.update({"hetero%d" % n: 86400.0 for n in (4, 6, 8, 10, 12, 16, 20, 24)})
 HETERO = (4, 6, 8, 10, 12, 16, 20, 24)
+
+
+def girt_case(oracle, name, nx, ny, nz, seed=5, log_formulation=True, dry=()):
+    """A structured-grid GIRT case: the first nx*ny*nz prepared cells of
+    `name`, face Darcy fluxes |q| ~ U[1e-7, 1e-5] m/s with random sign,
+    D_m = 1e-9 m^2/s, tortuosity 0.5, dispersivity 0.1 m, and the previous
+    time level's totals = the current ones times 5 % lognormal noise."""
+    net, st = case(oracle, name)
+    net = net.with_options(use_log_formulation=int(log_formulation))
+    st = st.subset(np.arange(nx * ny * nz))
+    st.net = net
+    for c in dry:
+        st.a["saturation"][c] = 0.0
+    rng = np.random.default_rng(seed)
+
+    def q(shape):
+        return rng.uniform(1e-7, 1e-5, shape) * rng.choice([-1.0, 1.0], shape)
+    grid = dict(nx=nx, ny=ny, nz=nz, dx=2.0, dy=1.5, dz=0.5, qx=q((nz, ny, nx - 1)), qy=q((nz, ny - 1, nx)),
+                qz=q((nz - 1, ny, nx)), diffusion=1e-9, tortuosity=0.5, dispersivity=0.1)
+    total_k = st.a["total"] * np.exp(0.05 * rng.standard_normal(st.a["total"].shape))
+    return net, st, grid, total_k

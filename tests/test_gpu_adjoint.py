@@ -7,10 +7,15 @@ ln rate constants, per-cell ln areas and per-cell initial totals.
 
 Loss: sum over cells of w*(total_final - target)^2, w ~ U[0,1], target = the
 forward output perturbed by 5 % lognormal noise (the differentiation case of
-the benchmark).  Tolerances: FD truncation is O(h^2) ~ 1e-12 and the tight
-solver tolerance (relative update < 1e-10) bounds FD noise; the comparison
-allows 1e-4 relative on summed gradients and 1e-4 on per-cell gradients
-(reported maxima are far smaller).
+the benchmark).  Two cases: the 12-component synthetic network at dt = 1 day
+and the calcite system at dt = 1 h, where complexation controls the free Ca++
+and HCO3- activities and hence the calcite rate (so the logK gradients of the
+complexes are large enough for differences to resolve).  Tolerances: FD
+truncation is O(h^2) ~ 1e-12 and the tight solver tolerance (relative update
+< 1e-10) bounds FD noise; the comparison allows 1e-4 relative on summed and
+per-cell gradients, plus the rounding floor of the difference quotient
+(1e-14 * sum|loss| / h, ~100 ulp of the summed loss per step h): a gradient below that floor cannot be resolved by
+differences and is only checked to be below it.
 """
 import numpy as np
 import pytest
@@ -22,11 +27,13 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 H = 1e-6
-DT = 86400.0
+DTS = {"random12": 86400.0, "calcite": 3600.0}
+DT = None    # set per case by the fixture
+CASE = None
 
 
-def _setup(oracle, ncells=240):
-    net, st0 = cases.case(oracle, "random12", tight=True)
+def _setup(oracle, name, ncells=240):
+    net, st0 = cases.case(oracle, name, tight=True)
     st0 = st0.subset(np.arange(ncells))
     from pfgpu.engine import ReactionEngine
     eng = ReactionEngine(net)
@@ -91,20 +98,26 @@ def _unit(k, n, h):
 
 
 def _fd_global(lossfn, ns, nm):
-    """Central differences of the summed loss for every network parameter."""
-    out = {"dL_dlogK_sec": np.zeros(ns), "dL_dlogK_mnrl": np.zeros(nm), "dL_dlnk": np.zeros(nm)}
+    """Central differences, per cell, of the loss for every network parameter;
+    also the mask of cells whose Newton path is the same in every run (a
+    path that changes between +h and -h makes that cell's difference
+    quotient meaningless)."""
+    base_l, base_its = lossfn()
+    stable = np.ones_like(base_its, dtype=bool)
+    out = {"dL_dlogK_sec": [], "dL_dlogK_mnrl": [], "dL_dlnk": []}
+
+    def fd(key, shift_p, shift_m):
+        nonlocal stable
+        lp, ip = lossfn(shift=shift_p)
+        lm, im = lossfn(shift=shift_m)
+        stable &= (ip == base_its) & (im == base_its)
+        out[key].append((lp - lm) / (2 * H))
     for k in range(ns):
-        lp, _ = lossfn(shift=(_unit(k, ns, H), None, None))
-        lm, _ = lossfn(shift=(_unit(k, ns, -H), None, None))
-        out["dL_dlogK_sec"][k] = (lp.sum() - lm.sum()) / (2 * H)
+        fd("dL_dlogK_sec", (_unit(k, ns, H), None, None), (_unit(k, ns, -H), None, None))
     for k in range(nm):
-        lp, _ = lossfn(shift=(None, _unit(k, nm, H), None))
-        lm, _ = lossfn(shift=(None, _unit(k, nm, -H), None))
-        out["dL_dlogK_mnrl"][k] = (lp.sum() - lm.sum()) / (2 * H)
-        lp, _ = lossfn(shift=(None, None, _unit(k, nm, H)))
-        lm, _ = lossfn(shift=(None, None, _unit(k, nm, -H)))
-        out["dL_dlnk"][k] = (lp.sum() - lm.sum()) / (2 * H)
-    return out
+        fd("dL_dlogK_mnrl", (None, _unit(k, nm, H), None), (None, _unit(k, nm, -H), None))
+        fd("dL_dlnk", (None, None, _unit(k, nm, H)), (None, None, _unit(k, nm, -H)))
+    return {k: np.array(v) for k, v in out.items()}, stable
 
 
 def _rel(a, b):
@@ -112,9 +125,11 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / scale)
 
 
-@pytest.fixture(scope="module")
-def adjoint_case(oracle):
-    net, st0, eng, w, tgt = _setup(oracle)
+@pytest.fixture(scope="module", params=["random12", "calcite"])
+def adjoint_case(oracle, request):
+    global DT, CASE
+    DT, CASE = DTS[request.param], request.param
+    net, st0, eng, w, tgt = _setup(oracle, request.param)
     dev = st0.to("cuda")
     g = eng.adjoint(dev, DT, weight=torch.from_numpy(w).cuda(), target=torch.from_numpy(tgt).cuda())
     g = {k: v.cpu().numpy() for k, v in g.items()}
@@ -128,18 +143,36 @@ def test_adjoint_status_and_loss(adjoint_case):
     assert g["loss"][0] == pytest.approx(base.sum(), rel=1e-12)
 
 
+def _check_global(net, st0, eng, w, tgt, g, lossfn):
+    fd, stable = _fd_global(lossfn, net.nsec, net.nmnrl)
+    ok = stable & (g["adj_status"] == 0)
+    assert ok.mean() > 0.9, ok.mean()
+    idx = np.nonzero(ok)[0]
+    sub = st0.subset(idx)
+    gs = eng.adjoint(sub.to("cuda"), DT, weight=torch.from_numpy(np.ascontiguousarray(w[:, idx])).cuda(),
+                     target=torch.from_numpy(np.ascontiguousarray(tgt[:, idx])).cuda())
+    base, _ = lossfn()
+    floor = 1e-14 * np.abs(base[ok]).sum() / H
+    resolved = {}
+    for k, v in fd.items():
+        ref = v[:, ok].sum(axis=1)
+        got = gs[k].cpu().numpy()
+        err = np.abs(got - ref)
+        assert np.all(err <= 1e-4 * np.abs(ref).max() + floor), (k, got, ref, floor)
+        resolved[k] = int((np.abs(ref) > 30 * floor).sum())
+    # the calcite case resolves every parameter group
+    if CASE == "calcite":
+        assert min(resolved.values()) > 0, resolved
+
+
 def test_adjoint_global_vs_fd_gpu(adjoint_case):
     net, st0, eng, w, tgt, g = adjoint_case
-    fd = _fd_global(lambda **kw: _gpu_loss(eng, st0, w, tgt, **kw), net.nsec, net.nmnrl)
-    for k, v in fd.items():
-        assert _rel(g[k], v) < 1e-4, (k, _rel(g[k], v))
+    _check_global(net, st0, eng, w, tgt, g, lambda **kw: _gpu_loss(eng, st0, w, tgt, **kw))
 
 
 def test_adjoint_global_vs_fd_oracle(adjoint_case, oracle):
     net, st0, eng, w, tgt, g = adjoint_case
-    fd = _fd_global(lambda **kw: _oracle_loss(oracle, net, st0, w, tgt, **kw), net.nsec, net.nmnrl)
-    for k, v in fd.items():
-        assert _rel(g[k], v) < 1e-4, (k, _rel(g[k], v))
+    _check_global(net, st0, eng, w, tgt, g, lambda **kw: _oracle_loss(oracle, net, st0, w, tgt, **kw))
 
 
 @pytest.mark.parametrize("which", ["gpu", "oracle"])
@@ -178,6 +211,9 @@ def test_adjoint_per_cell_vs_fd(adjoint_case, oracle, which):
 
 
 def test_autograd_function_matches_adjoint(adjoint_case):
+    """The autograd wrapper returns exactly what pf_adjoint returns for the
+    same inputs and the same upstream gradient (up to the run-dependent
+    order of the atomic cell sums), and leaves the network unshifted."""
     from pfgpu.autograd import rstep_totals
     net, st0, eng, w, tgt, g = adjoint_case
     dev = st0.to("cuda")
@@ -190,9 +226,19 @@ def test_autograd_function_matches_adjoint(adjoint_case):
     W, TG = torch.from_numpy(w).cuda(), torch.from_numpy(tgt).cuda()
     loss = (W * (Tf - TG) ** 2).sum()
     loss.backward()
-    assert float(loss) == pytest.approx(float(g["loss"][0]), rel=1e-12)
-    assert _rel(dks.grad.cpu().numpy(), g["dL_dlogK_sec"]) < 1e-10
-    assert _rel(dkm.grad.cpu().numpy(), g["dL_dlogK_mnrl"]) < 1e-10
-    assert _rel(dlnk.grad.cpu().numpy(), g["dL_dlnk"]) < 1e-10
-    assert _rel(lnarea.grad.cpu().numpy(), g["dL_dlnarea"]) < 1e-10
-    assert _rel(total0.grad.cpu().numpy(), g["dL_dtotal0"]) < 1e-10
+    # exp(log(area)) differs from area by an ulp: the loss agrees to the
+    # solver tolerance, not bitwise
+    assert float(loss.detach()) == pytest.approx(float(g["loss"][0]), rel=1e-8)
+    same = dev.copy()
+    same.a["mnrl_area"].copy_(torch.exp(lnarea.detach()))
+    ref = eng.adjoint(same, DT, dL_dtotal=(2.0 * W * (Tf.detach() - TG)).contiguous())
+    ref = {k: v.cpu().numpy() for k, v in ref.items()}
+    assert _rel(dks.grad.cpu().numpy(), ref["dL_dlogK_sec"]) < 1e-9
+    assert _rel(dkm.grad.cpu().numpy(), ref["dL_dlogK_mnrl"]) < 1e-9
+    assert _rel(dlnk.grad.cpu().numpy(), ref["dL_dlnk"]) < 1e-9
+    np.testing.assert_array_equal(lnarea.grad.cpu().numpy(), ref["dL_dlnarea"])
+    np.testing.assert_array_equal(total0.grad.cpu().numpy(), ref["dL_dtotal0"])
+    # the forward and backward calls restore the network's parameters
+    after, _ = _gpu_loss(eng, st0, w, tgt)
+    before = g["loss"][0]
+    assert after.sum() == pytest.approx(before, rel=1e-12)
