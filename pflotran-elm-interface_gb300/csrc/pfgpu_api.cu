@@ -15,10 +15,6 @@ extern "C" int32_t pf_equilibrate_constraint_impl(const DevNet* net, const PfCel
                                                   const int32_t* ctype, const double* cconc, int use_prev,
                                                   int32_t* iterations, int max_iterations, void* stream);
 
-extern "C" int32_t pf_girt_assemble_impl(const DevNet* net, const PfCellState* st, const PfGirtArgs* a,
-                                         double* scratch, void* stream);
-extern "C" size_t pf_girt_scratch_doubles(int32_t n, int64_t ncells);
-
 struct PfNetwork {
   DevNet dev{};
   void* d_tables = nullptr;
@@ -28,6 +24,9 @@ struct PfNetwork {
   double* d_scratch = nullptr;               // batched kernel per-cell scratch
   size_t scratch_cap = 0;                    // doubles
   std::vector<double> dbls_base;             // host copy of the double block at create
+  std::vector<int32_t> ints_base;            // host copy of the int block
+  void* d_girt = nullptr;                    // global-implicit lookup tables (built on first use)
+  GirtTabs girt{};
   size_t ib = 0;                             // byte offset of the double block
   PfLaunchConfig launch{};
   int device = 0;
@@ -248,6 +247,7 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.ints = (const int32_t*)net->d_tables;
   dev.dbls = (const double*)((char*)net->d_tables + ib);
   net->dbls_base = dbls;
+  net->ints_base = ints;
   net->ib = ib;
   net->dev = dev;
   net->launch = default_launch(dev);
@@ -278,6 +278,7 @@ int32_t pf_network_destroy(PfNetwork* net) {
   if (net->d_arena) cudaFree(net->d_arena);
   if (net->d_ctype) cudaFree(net->d_ctype);
   if (net->d_scratch) cudaFree(net->d_scratch);
+  if (net->d_girt) cudaFree(net->d_girt);
   delete net;
   return PF_OK;
 }
@@ -440,9 +441,12 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
   if ((int64_t)a->nx * a->ny * a->nz != state->ncells) return PF_ERR_INVALID;
   if ((a->nx > 1 && !a->qx) || (a->ny > 1 && !a->qy) || (a->nz > 1 && !a->qz)) return PF_ERR_INVALID;
   if (!state->sec_molal && net->dev.ns) return PF_ERR_INVALID;
-  rc = ensure_scratch_doubles(net, pf_girt_scratch_doubles(net->dev.n, state->ncells));
-  if (rc) return rc;
-  return pf_girt_assemble_impl(&net->dev, state, a, net->d_scratch, stream);
+  if (girt_smem_bytes(net->dev, nullptr) > 227u * 1024u) return PF_ERR_TOO_LARGE;
+  if (!net->d_girt) {
+    rc = girt_build_tables(net->dev, net->ints_base.data(), net->dbls_base.data(), &net->d_girt, &net->girt);
+    if (rc) return rc;
+  }
+  return launch_girt_assemble(net->dev, net->girt, *state, *a, net->num_sms, (cudaStream_t)stream);
 }
 
 int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, const int32_t* ctype,

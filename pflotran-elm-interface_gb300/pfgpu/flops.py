@@ -57,3 +57,29 @@ def per_iteration(net, mineral_active=None):
     f += 3 * n + 2 * n
     tr += n
     return f, tr
+
+
+def girt_per_cell(net, offdiag_blocks: float):
+    """FP64 flops (FMA = 2) and transcendental calls per cell of one
+    global-implicit assembly (pf_girt_assemble): RTotal (secondary
+    molalities and totals), dtotal by entry lists, the kinetic minerals and
+    their derivative, the residual row, and the block column (diagonal block
+    plus `offdiag_blocks` scaled copies of dtotal diag(m))."""
+    n, ns, nm = net.ncomp, net.nsec, net.nmnrl
+    k_s = [int(c) for c in net.sec_nspec]
+    k_m = [int(c) for c in net.mnrl_nspec] if nm else []
+    nn = n * n
+    f = 0
+    f += sum(2 * k + 2 for k in k_s)        # ln Q, s = exp()/gamma, totals += nu s
+    f += 2 * n                              # den scaling of totals
+    f += sum(2 * k for k in k_s)            # t_p = nu (s / m)
+    f += sum(2 * k * k for k in k_s)        # dtotal entries (FMA)
+    f += nn                                 # den scaling of dtotal
+    f += sum(2 * k + 12 for k in k_m)       # ln QK, affinity, rate, dIm/dQK
+    f += sum(4 * k for k in k_m)            # u_p = nu QK / m den 1e-3
+    f += sum(3 * k * k for k in k_m)        # mineral derivative entries
+    f += n * (3 * 7 + 6)                    # residual row
+    f += nn * 5                             # diagonal block
+    f += nn * (1 + offdiag_blocks)          # E = d m and the scaled copies
+    tr = ns + 2 * n + nm                    # exp per secondary, ln m and ln gamma, exp per mineral
+    return float(f), float(tr)
