@@ -310,6 +310,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-girt", action="store_true")
+    ap.add_argument("--grid", default="128x128x64", help="global-implicit grid NXxNYxNZ")
     ap.add_argument("--launch", default="", help="threads_per_block,blocks_per_sm,jac_in_shared (skips tuning)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -336,7 +337,8 @@ def main():
     net, eng, dev = build_state("c2" if args.config == "c5" else args.config, ncells, "cuda", seed=2026 + rank)
     log("state built: %d cells in %.1f s" % (ncells, time.perf_counter() - t_build))
     if args.config == "c5":
-        gm = girt_measure(net, eng, dev, args.steps, args.warmup)
+        nx, ny, nz = (int(v) for v in args.grid.split("x"))
+        gm = girt_measure(net, eng, dev, args.steps, args.warmup, nx, ny, nz)
         if rank == 0:
             print(json.dumps({"metric": "global-implicit residual + SeqBAIJ Jacobian assemblies (cells/s)",
                               "value": gm["cells_per_s"] * world, "unit": "cells/s", "n_gpus": world,
@@ -417,8 +419,13 @@ def main():
     peak = fp64_peak(abi.load(), sms)
     achieved = flops_per_launch / (kern_avg * 1e-3) / 1e12
     state_bytes = sum(v.numel() * v.element_size() for v in dev.a.values())
+    # DRAM bytes per cell-solve of this kernel measured by ncu on the same
+    # workload at 200,000 cells (profiles/rstep_batched_kernel_n12_200k.txt:
+    # 5.437 GB read + 5.561 GB written per launch), scaled to this launch
+    traffic = (5.437e9 + 5.561e9) / 200_000 * ncells if args.config == "c2" else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak if peak else None, "traffic": None,
+                "frac": achieved / peak if peak else None, "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu, scaled by cells)",
                 "peak_source": "FP64 DFMA probe (pf_bench_fp64_fma) measured in this run",
                 "flops_per_cell_solve": f_it * its_mean, "transcendentals_per_cell_solve": tr_it * its_mean,
                 "hbm_gbs": state_bytes * 2 / (kern_avg * 1e-3) / 1e9}

@@ -14,19 +14,20 @@
 //   block (dn, dn) -= c_dn dtot_dn      block (dn, up) -= c_up dtot_up
 // Every block in block column X is therefore a scalar times dtot_X (times the
 // column scaling diag(m_X) in the log formulation), plus, on the diagonal, the
-// accumulation and reaction derivatives of X.  One warp owns one cell X and
-// writes its whole block column -- the diagonal block and the (Y, X) block of
-// every neighbour row Y -- each block as ncomp^2 consecutive doubles, so all
-// matrix stores are coalesced and nothing is scattered or accumulated in
-// memory.
+// accumulation and reaction derivatives of X.  The cell that owns column X
+// computes dtot_X once and writes the diagonal block and the (Y, X) block of
+// every neighbour row Y; nothing is accumulated in memory.
 //
-// Two launches per assembly:
-//   update_auxvars_kernel (pfgpu_aux.cu)  thread per cell: RTotal -> total,
-//                                         sec_molal (RTUpdateAuxVars)
-//   girt_column_kernel                    warp per cell: dtotal from sec_molal
-//                                         (no exp), kinetic-mineral rates and
-//                                         derivatives, the cell's residual row
-//                                         and its block column.
+// GB300 runs FP64 at ~1.7 lane-operations per clock per SM and a warp
+// instruction costs the same pipe time with idle lanes, so all FP64 work is
+// one cell per lane:
+//   girt_cell_kernel      RTotal (totals, sec_molal), kinetic minerals and
+//                         their derivative, dtotal entry by entry, the block
+//                         column, and the cell's reaction residual
+//   girt_residual_kernel  flux + accumulation terms of the residual row
+//                         (needs the neighbours' totals of the first launch)
+// Per-thread scratch (molalities, secondary molalities, mineral terms) lives
+// in shared memory, interleaved by thread so that accesses are conflict-free.
 // The diagonal flux term sums the connection coefficients first
 // ((sum_q c_q) dtot rather than sum_q (c_q dtot)); every c_q there is >= 0
 // (upwinding), so the two orders differ by rounding only.
@@ -47,11 +48,11 @@ struct Geo {
   const double* qz;
 };
 
-// doubles of per-warp shared memory: m, 1/m, ln a (n each), the secondary
-// column terms t (one per secondary CSR slot), the mineral column terms u (one
-// per mineral CSR slot), and per mineral the derivative factor and the rate
-__host__ __device__ inline int warp_doubles(const DevNet& net) {
-  return (3 * net.n + net.nnz_s + net.nnz_m + 2 * net.nm + 1) & ~1;
+// doubles of per-thread shared memory: m, 1/m, ln a, totals (n each), the
+// secondary molalities (ns), the mineral column terms u (one per mineral CSR
+// slot) and the mineral derivative factors (nm)
+__host__ __device__ inline int thread_doubles(const DevNet& net) {
+  return 4 * net.n + net.ns + net.nnz_m + net.nm;
 }
 
 // harmonic_tran_coefs_over_dist (transport.F90:199-225) for a connection at
@@ -65,209 +66,252 @@ __device__ __forceinline__ double tran_coef(double por_up, double sat_up, double
   return (hu * hd) / (hu * dist_dn + hd * dist_up);
 }
 
-__global__ void __launch_bounds__(256) girt_column_kernel(DevNet net, GirtTabs gt, PfCellState st, Geo g,
-                                                          const double* __restrict__ total_k, double dt,
-                                                          const int32_t* __restrict__ rowptr,
-                                                          const int32_t* __restrict__ colidx,
-                                                          double* __restrict__ r, double* __restrict__ values) {
-  extern __shared__ double smem[];
-  const int lane = threadIdx.x & 31;
-  const int n = net.n, nn = n * n, ns = net.ns, nm = net.nm;
-  double* W = smem + (threadIdx.x >> 5) * warp_doubles(net);
-  double* sm_m = W;
-  double* sm_ic = W + n;
-  double* sm_lna = W + 2 * n;
-  double* t = W + 3 * n;
-  double* u = t + net.nnz_s;
-  double* G = u + net.nnz_m;
-  double* Imv = G + nm;
-  const Tables T{net.ints, net.dbls, &net};
-  const long long N = st.ncells;
+// The six connections of cell X in the order the reference's x, y, z
+// connection loops reach it (x-, x+, y-, y+, z-, z+): neighbour, whether X is
+// the upstream (lower-index) cell, and TFluxCoef's T_up, T_dn (L/s).
+struct Conns {
+  int ex[6], other[6], up[6];
+  double cup[6], cdn[6];
+};
+
+__device__ __forceinline__ void connections(const PfCellState& st, const Geo& g, long long X, Conns& c) {
   const long long nxy = (long long)g.nx * g.ny;
+  const int i = (int)(X % g.nx), j = (int)((X / g.nx) % g.ny), k = (int)(X / nxy);
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int axis = q >> 1, plus = q & 1;
+    const int pos = axis == 0 ? i : (axis == 1 ? j : k);
+    const int lim = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    const int ex = plus ? (pos < lim - 1) : (pos > 0);
+    c.ex[q] = ex;
+    c.up[q] = plus;
+    c.other[q] = 0;
+    c.cup[q] = c.cdn[q] = 0.0;
+    if (!ex) continue;
+    const long long s = axis == 0 ? 1 : (axis == 1 ? (long long)g.nx : nxy);
+    const long long other = plus ? X + s : X - s;
+    c.other[q] = (int)other;
+    const int face = plus ? pos : pos - 1;
+    double qf, area, dist;
+    if (axis == 0) {
+      qf = g.qx[((long long)k * g.ny + j) * (g.nx - 1) + face];
+      area = g.dy * g.dz;
+      dist = g.dx;
+    } else if (axis == 1) {
+      qf = g.qy[((long long)k * (g.ny - 1) + face) * g.nx + i];
+      area = g.dx * g.dz;
+      dist = g.dy;
+    } else {
+      qf = g.qz[((long long)face * g.ny + j) * g.nx + i];
+      area = g.dx * g.dy;
+      dist = g.dz;
+    }
+    const long long cu = plus ? X : other, cd = plus ? other : X;
+    const double pu = st.porosity[cu], su = st.saturation[cu], pdn = st.porosity[cd], sdn = st.saturation[cd];
+    if (!(sdn < RT_MIN_SATURATION) && !(su < RT_MIN_SATURATION)) {
+      const double tr = tran_coef(pu, su, pdn, sdn, qf, dist, g);
+      double a, b;
+      if (qf > 0.0) { a = tr + qf; b = -tr; }
+      else { a = tr; b = -tr + qf; }
+      c.cup[q] = a * area * 1000.0;
+      c.cdn[q] = b * area * 1000.0;
+    }
+  }
+}
+
+__device__ __forceinline__ int find_block(const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                                          long long row, long long col) {
+  for (int b = rowptr[row]; b < rowptr[row + 1]; ++b)
+    if (colidx[b] == (int)col) return b;
+  return -1;
+}
+
+__global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt,
+                                                        const int32_t* __restrict__ rowptr,
+                                                        const int32_t* __restrict__ colidx, double* __restrict__ r,
+                                                        double* __restrict__ values, int vec2) {
+  extern __shared__ double smem[];
+  const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= st.ncells) return;
+  const int bd = blockDim.x;
+  double* P = smem + threadIdx.x;  // this thread's scratch: P[k * bd]
+  const int n = net.n, nn = n * n, ns = net.ns, nm = net.nm;
+  const int o_ic = n * bd, o_lna = 2 * n * bd, o_t = 3 * n * bd, o_s = 4 * n * bd, o_u = (4 * n + ns) * bd,
+            o_G = (4 * n + ns + net.nnz_m) * bd;
+  const Tables T{net.ints, net.dbls, &net};
+  const SoA soa{st.ncells};
   const bool logf = net.o.use_log_formulation != 0;
+  const bool tsec = !net.o.isothermal && (net.flags & NETF_SEC_LOGKCOEF);
   const bool tmin = !net.o.isothermal && (net.flags & NETF_MNRL_LOGKCOEF);
   const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
-  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long X = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); X < N; X += warps) {
-    const int i = (int)(X % g.nx), j = (int)((X / g.nx) % g.ny), k = (int)(X / nxy);
-    const double por = st.porosity[X], sat = st.saturation[X];
-    const bool dry = sat < RT_MIN_SATURATION;
-    // ---- connections: lane q < 6 takes x-, x+, y-, y+, z-, z+ (the order in
-    // which the reference's x, y, z connection loops reach this cell) and
-    // lane 6 finds the diagonal block
-    int ex = 0, other = 0, up = 0, blk = -1;
-    double cup = 0.0, cdn = 0.0;
-    if (lane < 6) {
-      const int axis = lane >> 1, plus = lane & 1;
-      const int pos = axis == 0 ? i : (axis == 1 ? j : k);
-      const int lim = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
-      ex = plus ? (pos < lim - 1) : (pos > 0);
-      if (ex) {
-        const long long s = axis == 0 ? 1 : (axis == 1 ? (long long)g.nx : nxy);
-        other = (int)(plus ? X + s : X - s);
-        up = plus;  // the lower-index cell is upstream of the connection
-        const int face = plus ? pos : pos - 1;
-        double q, area, dist;
-        if (axis == 0) {
-          q = g.qx[((long long)k * g.ny + j) * (g.nx - 1) + face];
-          area = g.dy * g.dz;
-          dist = g.dx;
-        } else if (axis == 1) {
-          q = g.qy[((long long)k * (g.ny - 1) + face) * g.nx + i];
-          area = g.dx * g.dz;
-          dist = g.dy;
+  const double temp = st.temperature ? st.temperature[X] : 25.0;
+  const double den_k = st.den_kg[X], den_L = den_k * 1.0e-3;
+  const double por = st.porosity[X], sat = st.saturation[X], volume = st.volume[X];
+  const bool dry = sat < RT_MIN_SATURATION;
+  // ---- RTotalAqueous (reaction.F90:4665-4759)
+  for (int jj = 0; jj < n; ++jj) {
+    const double m = st.pri_molal[soa.at(jj, X)];
+    P[jj * bd] = m;
+    P[o_ic + jj * bd] = 1.0 / m;
+    P[o_lna + jj * bd] = log(m) + log(st.pri_act_coef[soa.at(jj, X)]);
+  }
+  for (int jj = 0; jj < n; ++jj) P[o_t + jj * bd] = P[jj * bd];  // total = m, then += nu s
+  for (int i = 0; i < ns; ++i) {
+    const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
+    double lnQK = -logK * LOG_TO_LN;
+    const int b = T.sec_begin(i), e = T.sec_end(i);
+    for (int p = b; p < e; ++p) lnQK = lnQK + T.sec_nu(p) * P[o_lna + T.sec_idx(p) * bd];
+    const double sv = exp(lnQK) / st.sec_act_coef[soa.at(i, X)];
+    P[o_s + i * bd] = sv;
+    st.sec_molal[soa.at(i, X)] = sv;
+  }
+  // totals in the reference's order: per component, the secondaries ascending
+  for (int i = 0; i < ns; ++i) {
+    const double sv = P[o_s + i * bd];
+    for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) {
+      const int a = o_t + T.sec_idx(p) * bd;
+      P[a] = P[a] + T.sec_nu(p) * sv;
+    }
+  }
+  for (int jj = 0; jj < n; ++jj) st.total[soa.at(jj, X)] = P[o_t + jj * bd] * den_L;
+  // ---- RKineticMineral (reaction_mineral.F90:647-1078): rates, reaction
+  // residual (into r, finished by girt_residual_kernel), derivative factors
+  for (int jj = 0; jj < n; ++jj) r[X * n + jj] = 0.0;
+  for (int m = 0; m < nm; ++m) {
+    const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
+    double Gm = 0.0, QK = 0.0;
+    bool active = false;
+    if (!dry) {
+      const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
+      double lnQK = -logK * LOG_TO_LN;
+      for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * P[o_lna + T.mnrl_idx(p) * bd];
+      QK = exp(lnQK);
+      double aff;
+      if (has_tk) aff = 1.0 - pow(QK, 1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m)));
+      else if (has_msf) aff = 1.0 - pow(QK, 1.0 / T.msf(m));
+      else aff = 1.0 - QK;
+      const double sign_ = fsign1(aff);
+      const double vf = st.mnrl_volfrac[soa.at(m, X)];
+      active = (vf > 0 || sign_ < 0.0) && !(T.irreversible(m) == 1 && sign_ < 0.0) &&
+               !(T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m));
+      double rate_out = 0.0;
+      if (active) {
+        const double rl = T.limiter(m);
+        if (rl > 0.0) aff = aff / (1.0 + (1.0 - aff) / rl);
+        double arr = 1.0;
+        if (T.ea(m) > 0.0)
+          arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp + 273.15)));
+        const double kr = T.rate(m) * arr;
+        double Im_const = -st.mnrl_area[soa.at(m, X)];
+        if (has_msf) Im_const = Im_const / T.msf(m);
+        double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * kr : Im_const * sign_ * fabs(aff) * kr;
+        rate_out = Im;
+        Im_const = Im_const * volume;
+        Im = Im * volume;
+        for (int p = b; p < e; ++p) r[X * n + T.mnrl_idx(p)] = r[X * n + T.mnrl_idx(p)] + T.mnrl_nu(p) * Im;
+        double dIm_dQK = has_pw ? -Im * T.power(m) / fabs(aff) : -Im_const * kr;
+        if (has_tk)
+          dIm_dQK = dIm_dQK * (1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m))) / QK * (1.0 - aff);
+        else if (has_msf)
+          dIm_dQK = dIm_dQK * (1.0 / T.msf(m)) / QK * (1.0 - aff);
+        if (rl > 0.0) {
+          const double den = 1.0 + (1.0 - aff) / rl;
+          Gm = dIm_dQK * (1.0 + QK / rl / den) / den;
         } else {
-          q = g.qz[((long long)face * g.ny + j) * g.nx + i];
-          area = g.dx * g.dy;
-          dist = g.dz;
+          Gm = dIm_dQK;
         }
-        const long long cu = up ? X : other, cd = up ? other : X;
-        const double pu = st.porosity[cu], su = st.saturation[cu], pdn = st.porosity[cd], sdn = st.saturation[cd];
-        if (!(sdn < RT_MIN_SATURATION) && !(su < RT_MIN_SATURATION)) {
-          const double tr = tran_coef(pu, su, pdn, sdn, q, dist, g);
-          if (q > 0.0) { cup = tr + q; cdn = -tr; }
-          else { cup = tr; cdn = -tr + q; }
-          cup = cup * area * 1000.0;
-          cdn = cdn * area * 1000.0;
-        }
-        for (int b = rowptr[other]; b < rowptr[other + 1]; ++b)
-          if (colidx[b] == (int)X) { blk = b; break; }
       }
-    } else if (lane == 6) {
-      for (int b = rowptr[X]; b < rowptr[X + 1]; ++b)
-        if (colidx[b] == (int)X) { blk = b; break; }
+      st.mnrl_rate[soa.at(m, X)] = rate_out;
     }
-    // ---- species and secondary column terms t_p = nu_p s_i / m_species(p)
-    for (int jj = lane; jj < n; jj += 32) {
-      const double m = st.pri_molal[(size_t)jj * N + X];
-      sm_m[jj] = m;
-      sm_ic[jj] = 1.0 / m;
-      sm_lna[jj] = log(m) + log(st.pri_act_coef[(size_t)jj * N + X]);
-    }
-    __syncwarp();
-    for (int s = lane; s < ns; s += 32) {
-      const double sv = st.sec_molal[(size_t)s * N + X];
-      for (int p = T.sec_begin(s); p < T.sec_end(s); ++p) t[p] = T.sec_nu(p) * (sv * sm_ic[T.sec_idx(p)]);
-    }
-    // ---- RKineticMineral (reaction_mineral.F90:647-1078), lane m
-    const double den_k = st.den_kg[X], den_L = den_k * 1.0e-3;
-    const double temp = st.temperature ? st.temperature[X] : 25.0;
-    const double volume = st.volume[X];
-    for (int m = lane; m < nm; m += 32) {
-      const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
-      double Gm = 0.0, Im_v = 0.0, QK = 0.0, rate_out = 0.0;
-      bool active = false;
-      if (!dry) {
-        const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
-        double lnQK = -logK * LOG_TO_LN;
-        for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * sm_lna[T.mnrl_idx(p)];
-        QK = exp(lnQK);
-        double aff;
-        if (has_tk) aff = 1.0 - pow(QK, 1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m)));
-        else if (has_msf) aff = 1.0 - pow(QK, 1.0 / T.msf(m));
-        else aff = 1.0 - QK;
-        const double sign_ = fsign1(aff);
-        const double vf = st.mnrl_volfrac[(size_t)m * N + X];
-        active = (vf > 0 || sign_ < 0.0) && !(T.irreversible(m) == 1 && sign_ < 0.0) &&
-                 !(T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m));
-        if (active) {
-          const double rl = T.limiter(m);
-          if (rl > 0.0) aff = aff / (1.0 + (1.0 - aff) / rl);
-          double arr = 1.0;
-          if (T.ea(m) > 0.0)
-            arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp + 273.15)));
-          const double kr = T.rate(m) * arr;
-          double Im_const = -st.mnrl_area[(size_t)m * N + X];
-          if (has_msf) Im_const = Im_const / T.msf(m);
-          double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * kr : Im_const * sign_ * fabs(aff) * kr;
-          rate_out = Im;
-          Im_const = Im_const * volume;
-          Im = Im * volume;
-          Im_v = Im;
-          double dIm_dQK = has_pw ? -Im * T.power(m) / fabs(aff) : -Im_const * kr;
-          if (has_tk)
-            dIm_dQK = dIm_dQK * (1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m))) / QK * (1.0 - aff);
-          else if (has_msf)
-            dIm_dQK = dIm_dQK * (1.0 / T.msf(m)) / QK * (1.0 - aff);
-          if (rl > 0.0) {
-            const double den = 1.0 + (1.0 - aff) / rl;
-            Gm = dIm_dQK * (1.0 + QK / rl / den) / den;
-          } else {
-            Gm = dIm_dQK;
-          }
-        }
-        st.mnrl_rate[(size_t)m * N + X] = rate_out;
-      }
-      G[m] = Gm;
-      Imv[m] = Im_v;
-      // dQK/dm_j (the reference's den*1e-3 factor included, :944-947)
-      for (int p = b; p < e; ++p)
-        u[p] = active ? T.mnrl_nu(p) * QK * sm_ic[T.mnrl_idx(p)] * den_k * 1.0e-3 : 0.0;
-    }
-    // ---- broadcast the connections
-    int c_ex[6], c_other[6], c_up[6], c_blk[6];
-    double c_cup[6], c_cdn[6];
+    P[o_G + m * bd] = Gm;
+    // dQK/dm_j (the reference's den*1e-3 factor included, :944-947)
+    for (int p = b; p < e; ++p)
+      P[o_u + p * bd] = active ? T.mnrl_nu(p) * QK * P[o_ic + T.mnrl_idx(p) * bd] * den_k * 1.0e-3 : 0.0;
+  }
+  // ---- block column X
+  Conns c;
+  connections(st, g, X, c);
+  int blk[6];
+  double sc[6];
+  double csum = 0.0;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
-      c_ex[q] = __shfl_sync(0xffffffffu, ex, q);
-      c_other[q] = __shfl_sync(0xffffffffu, other, q);
-      c_up[q] = __shfl_sync(0xffffffffu, up, q);
-      c_blk[q] = __shfl_sync(0xffffffffu, blk, q);
-      c_cup[q] = __shfl_sync(0xffffffffu, cup, q);
-      c_cdn[q] = __shfl_sync(0xffffffffu, cdn, q);
-    }
-    const int dblk = __shfl_sync(0xffffffffu, blk, 6);
-    __syncwarp();
-    const double psv = por * sat * 1000.0 * volume;
-    const double psvd_t = psv / dt;
-    // ---- residual row (lane = component)
-    for (int row = lane; row < n; row += 32) {
-      const double tx = st.total[(size_t)row * N + X];
-      double v = 0.0;
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        if (!c_ex[q]) continue;
-        const double ty = st.total[(size_t)row * N + c_other[q]];
-        const double tu = c_up[q] ? tx : ty, td = c_up[q] ? ty : tx;
-        const double res = c_cup[q] * tu + c_cdn[q] * td;
-        v = c_up[q] ? v + res : v - res;
-      }
-      const double accum_k = dry ? 0.0 : psv * total_k[(size_t)row * N + X];
-      v = v - accum_k / dt;
-      v = v + (dry ? 0.0 : psv * tx) / dt;
-      if (!dry) {
-        double R = 0.0;
-        for (int q = gt.r_mn_ptr[row]; q < gt.r_mn_ptr[row + 1]; ++q) R = R + gt.r_mn_nu[q] * Imv[gt.r_mn_m[q]];
-        v = v + R;
-      }
-      r[X * n + row] = v;
-    }
-    // ---- block column X
-    double csum = 0.0;
-#pragma unroll
-    for (int q = 0; q < 6; ++q)
-      if (c_ex[q]) csum = csum + (c_up[q] ? c_cup[q] : -c_cdn[q]);
-    for (int fe = lane; fe < nn; fe += 32) {
-      const int col = fe / n, row = fe - col * n;
-      const int f = row * n + col;
-      double d = (row == col) ? 1.0 : 0.0;
-      for (int q = gt.e_sec_ptr[f]; q < gt.e_sec_ptr[f + 1]; ++q) d = fma(gt.e_sec_nr[q], t[gt.e_sec_p[q]], d);
-      d = d * den_L;
-      double jr = 0.0;
-      for (int q = gt.e_mn_ptr[f]; q < gt.e_mn_ptr[f + 1]; ++q)
-        jr = fma(gt.e_mn_nr[q] * G[gt.e_mn_m[q]], u[gt.e_mn_p[q]], jr);
-      if (fabs(jr) < 1.0e-40) jr = 0.0;  // reaction.F90:4232-4237
-      const double mc = logf ? sm_m[col] : 1.0;
-      double v = d * csum;
-      v = v + (dry ? ((row == col) ? 1.0 : 0.0) : d * psvd_t);
-      if (!dry) v = v + jr;
-      if (dblk >= 0) values[(size_t)dblk * nn + fe] = v * mc;
-      const double E = d * mc;
+  for (int q = 0; q < 6; ++q) {
+    blk[q] = c.ex[q] ? find_block(rowptr, colidx, c.other[q], X) : -1;
+    sc[q] = c.up[q] ? -c.cup[q] : c.cdn[q];  // block (Y, X) = sc * dtot_X
+    if (c.ex[q]) csum = csum + (c.up[q] ? c.cup[q] : -c.cdn[q]);
+  }
+  const int dblk = find_block(rowptr, colidx, X, X);
+  const double psvd_t = por * sat * 1000.0 * volume / dt;
+  const double cdiag = csum + psvd_t;
+  auto entry = [&](int fe, double& vdiag, double& e) {
+    const int col = fe / n, row = fe - col * n;
+    const int f = row * n + col;
+    double acc = 0.0;
+    for (int q = gt.e_sec_ptr[f]; q < gt.e_sec_ptr[f + 1]; ++q)
+      acc = fma(gt.e_sec_nr[q], P[o_s + gt.e_sec_p[q] * bd], acc);
+    const double d = ((row == col ? 1.0 : 0.0) + acc * P[o_ic + col * bd]) * den_L;
+    double jr = 0.0;
+    for (int q = gt.e_mn_ptr[f]; q < gt.e_mn_ptr[f + 1]; ++q)
+      jr = fma(gt.e_mn_nr[q] * P[o_G + gt.e_mn_m[q] * bd], P[o_u + gt.e_mn_p[q] * bd], jr);
+    if (fabs(jr) < 1.0e-40) jr = 0.0;  // reaction.F90:4232-4237
+    const double mc = logf ? P[col * bd] : 1.0;
+    const double v = dry ? fma(d, csum, (row == col) ? 1.0 : 0.0) : fma(d, cdiag, jr);
+    vdiag = v * mc;
+    e = d * mc;
+  };
+  if (vec2) {
+    for (int fe = 0; fe < nn; fe += 2) {
+      double v0, e0, v1, e1;
+      entry(fe, v0, e0);
+      entry(fe + 1, v1, e1);
+      if (dblk >= 0) *reinterpret_cast<double2*>(values + (size_t)dblk * nn + fe) = make_double2(v0, v1);
 #pragma unroll
       for (int q = 0; q < 6; ++q)
-        if (c_ex[q] && c_blk[q] >= 0) values[(size_t)c_blk[q] * nn + fe] = (c_up[q] ? -c_cup[q] : c_cdn[q]) * E;
+        if (blk[q] >= 0)
+          *reinterpret_cast<double2*>(values + (size_t)blk[q] * nn + fe) = make_double2(sc[q] * e0, sc[q] * e1);
     }
-    __syncwarp();
+  } else {
+    for (int fe = 0; fe < nn; ++fe) {
+      double v0, e0;
+      entry(fe, v0, e0);
+      if (dblk >= 0) values[(size_t)dblk * nn + fe] = v0;
+#pragma unroll
+      for (int q = 0; q < 6; ++q)
+        if (blk[q] >= 0) values[(size_t)blk[q] * nn + fe] = sc[q] * e0;
+    }
+  }
+}
+
+// residual row of cell X: connections (reference order), fixed and current
+// accumulation, then the reaction part the cell kernel left in r
+__global__ void __launch_bounds__(128) girt_residual_kernel(DevNet net, PfCellState st, Geo g,
+                                                            const double* __restrict__ total_k, double dt,
+                                                            double* __restrict__ r) {
+  const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= st.ncells) return;
+  const long long N = st.ncells;
+  const int n = net.n;
+  Conns c;
+  connections(st, g, X, c);
+  const double sat = st.saturation[X];
+  const bool dry = sat < RT_MIN_SATURATION;
+  const double psv = st.porosity[X] * sat * 1000.0 * st.volume[X];
+  for (int row = 0; row < n; ++row) {
+    const double tx = st.total[(size_t)row * N + X];
+    double v = 0.0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      if (!c.ex[q]) continue;
+      const double ty = st.total[(size_t)row * N + c.other[q]];
+      const double tu = c.up[q] ? tx : ty, td = c.up[q] ? ty : tx;
+      const double res = c.cup[q] * tu + c.cdn[q] * td;
+      v = c.up[q] ? v + res : v - res;
+    }
+    const double accum_k = dry ? 0.0 : psv * total_k[(size_t)row * N + X];
+    v = v - accum_k / dt;
+    v = v + (dry ? 0.0 : psv * tx) / dt;
+    if (!dry) v = v + r[X * n + row];
+    r[X * n + row] = v;
   }
 }
 
@@ -275,15 +319,15 @@ __global__ void __launch_bounds__(256) girt_column_kernel(DevNet net, GirtTabs g
 
 int girt_build_tables(const DevNet& net, const int32_t* I, const double* D, void** d_buf, GirtTabs* out) {
   const int n = net.n, nn = n * n;
-  std::vector<std::vector<int32_t>> sp(nn), mp(nn), mm(nn), rm(n);
-  std::vector<std::vector<double>> snr(nn), mnr(nn), rnu(n);
+  std::vector<std::vector<int32_t>> sp(nn), mp(nn), mm(nn);
+  std::vector<std::vector<double>> snr(nn), mnr(nn);
   for (int i = 0; i < net.ns; ++i) {
     const int b = I[net.o_sec_ptr + i], e = I[net.o_sec_ptr + i + 1];
     for (int pc = b; pc < e; ++pc)
       for (int pr = b; pr < e; ++pr) {
         const int f = I[net.o_sec_idx + pr] * n + I[net.o_sec_idx + pc];
-        sp[f].push_back(pc);
-        snr[f].push_back(D[net.o_sec_nu + pr]);
+        sp[f].push_back(i);
+        snr[f].push_back(D[net.o_sec_nu + pr] * D[net.o_sec_nu + pc]);
       }
   }
   for (int m = 0; m < net.nm; ++m) {
@@ -295,10 +339,6 @@ int girt_build_tables(const DevNet& net, const int32_t* I, const double* D, void
         mm[f].push_back(m);
         mnr[f].push_back(D[net.o_mnrl_nu + pr]);
       }
-    for (int p = b; p < e; ++p) {
-      rm[I[net.o_mnrl_idx + p]].push_back(m);
-      rnu[I[net.o_mnrl_idx + p]].push_back(D[net.o_mnrl_nu + p]);
-    }
   }
   std::vector<int32_t> ints;
   std::vector<double> dbls;
@@ -320,12 +360,11 @@ int girt_build_tables(const DevNet& net, const int32_t* I, const double* D, void
     for (auto& rw : rows) dbls.insert(dbls.end(), rw.begin(), rw.end());
     return o;
   };
-  int o_esp, o_esi, o_emp, o_emi, o_rmp, o_rmi;
+  int o_esp, o_esi, o_emp, o_emi;
   csr(sp, &o_esp, &o_esi);
   csr(mp, &o_emp, &o_emi);
   const int o_emm = flat(mm);
-  csr(rm, &o_rmp, &o_rmi);
-  const int d_esnr = flatd(snr), d_emnr = flatd(mnr), d_rmnu = flatd(rnu);
+  const int d_esnr = flatd(snr), d_emnr = flatd(mnr);
   if (dbls.empty()) dbls.push_back(0.0);
   const size_t ib = (ints.size() * 4 + 15) & ~size_t(15);
   void* buf = nullptr;
@@ -344,42 +383,39 @@ int girt_build_tables(const DevNet& net, const int32_t* I, const double* D, void
   out->e_mn_p = di + o_emi;
   out->e_mn_m = di + o_emm;
   out->e_mn_nr = dd + d_emnr;
-  out->r_mn_ptr = di + o_rmp;
-  out->r_mn_m = di + o_rmi;
-  out->r_mn_nu = dd + d_rmnu;
   *d_buf = buf;
   return PF_OK;
 }
 
-size_t girt_smem_bytes(const DevNet& net, int* warps_per_block) {
-  const size_t wbytes = (size_t)girt::warp_doubles(net) * sizeof(double);
-  int wpb = 8;
-  while (wpb > 1 && wpb * wbytes > 96u * 1024u) wpb /= 2;
-  if (warps_per_block) *warps_per_block = wpb;
-  return wpb * wbytes;
+// threads per block of the cell kernel and its shared memory
+size_t girt_smem_bytes(const DevNet& net, int* threads_per_block) {
+  const size_t tbytes = (size_t)girt::thread_doubles(net) * sizeof(double);
+  int tpb = 128;
+  while (tpb > 32 && tpb * tbytes > 72u * 1024u) tpb -= 32;
+  if (threads_per_block) *threads_per_block = tpb;
+  return tpb * tbytes;
 }
 
 int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const PfGirtArgs& a,
                          int num_sms, cudaStream_t s) {
+  (void)num_sms;
   if (st.ncells == 0) return PF_OK;
-  if (launch_update_auxvars(net, st, 0, s) != 0) return PF_ERR_CUDA;  // RTUpdateAuxVars: total, sec_molal
   girt::Geo g{a.nx, a.ny, a.nz, a.dx, a.dy, a.dz, a.diffusion_coefficient, a.tortuosity, a.dispersivity,
               a.qx, a.qy, a.qz};
-  int wpb = 1;
-  const size_t smem = girt_smem_bytes(net, &wpb);
+  int tpb = 32;
+  const size_t smem = girt_smem_bytes(net, &tpb);
   if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
-  auto k = girt::girt_column_kernel;
+  auto k = girt::girt_cell_kernel;
   if (smem > 48u * 1024u &&
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PF_ERR_CUDA;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * wpb, smem) != cudaSuccess || per_sm < 1)
-    return PF_ERR_CUDA;
-  const long long need = (st.ncells + wpb - 1) / wpb;
-  const long long cap = (long long)num_sms * per_sm;
-  const long long grid = need < cap ? need : cap;
-  k<<<(unsigned)grid, 32 * wpb, smem, s>>>(net, gt, st, g, a.total_k, a.dt, a.rowptr, a.colidx, a.residual,
-                                           a.values);
+  // 16-byte stores when every block starts on a 16-byte boundary
+  const int vec2 = ((net.n * net.n) % 2 == 0) && (((uintptr_t)a.values & 15) == 0);
+  const long long blocks = (st.ncells + tpb - 1) / tpb;
+  k<<<(unsigned)blocks, tpb, smem, s>>>(net, gt, st, g, a.dt, a.rowptr, a.colidx, a.residual, a.values, vec2);
+  if (cudaGetLastError() != cudaSuccess) return PF_ERR_CUDA;
+  const long long rblocks = (st.ncells + 127) / 128;
+  girt::girt_residual_kernel<<<(unsigned)rblocks, 128, 0, s>>>(net, st, g, a.total_k, a.dt, a.residual);
   return cudaGetLastError() == cudaSuccess ? PF_OK : PF_ERR_CUDA;
 }
 

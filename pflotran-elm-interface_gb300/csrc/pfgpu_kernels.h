@@ -29,11 +29,12 @@ int launch_update_auxvars(const DevNet& net, const PfCellState& st, int update_a
 int launch_update_activity_coefs(const DevNet& net, const PfCellState& st, cudaStream_t stream);
 
 // global-implicit assembly (pfgpu_girt.cu).  Per-network lookup tables, all
-// device pointers into one allocation:
-//   e_sec_*  per Jacobian entry f = row*n + col, the secondaries contributing
-//            to dtotal(row, col): CSR slot of the column species and nu_row
-//   e_mn_*   the same for the kinetic-mineral derivative (slot, mineral, nu_row)
-//   r_mn_*   per component row, the minerals in its residual (mineral, nu)
+// device pointers into one allocation, CSR over Jacobian entries
+// f = row*n + col:
+//   e_sec_*  the secondaries contributing to dtotal(row, col): secondary
+//            index and nu_row*nu_col, ascending secondary
+//   e_mn_*   the kinetic-mineral derivative terms: CSR slot of the column
+//            species in the mineral's reaction, mineral index, nu_row
 struct GirtTabs {
   const int32_t* e_sec_ptr;
   const int32_t* e_sec_p;
@@ -42,15 +43,12 @@ struct GirtTabs {
   const int32_t* e_mn_p;
   const int32_t* e_mn_m;
   const double* e_mn_nr;
-  const int32_t* r_mn_ptr;
-  const int32_t* r_mn_m;
-  const double* r_mn_nu;
 };
 // host: build the tables from the host copies of the packed network blocks
 // and upload them (*d_buf: the one device allocation)
 int girt_build_tables(const DevNet& net, const int32_t* h_ints, const double* h_dbls, void** d_buf,
                       GirtTabs* out);
-size_t girt_smem_bytes(const DevNet& net, int* warps_per_block);
+size_t girt_smem_bytes(const DevNet& net, int* threads_per_block);
 // RTUpdateAuxVars then the column kernel; a PfStatus
 int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const PfGirtArgs& a,
                          int num_sms, cudaStream_t stream);
