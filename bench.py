@@ -259,6 +259,133 @@ def girt_measure(net, eng, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11):
             "fp64_frac": tf / fp64 if fp64 else None, "kernels_per_assembly": 2}
 
 
+C3_NCOMP = (4, 6, 8, 10, 12, 16, 20, 24)
+
+
+def build_c3(cells_per_network, device, seed=3000):
+    """Eight networks generated like the 12/40/6 one with ncomp 4..24,
+    3*ncomp complexes and ncomp/2 kinetic minerals; per-cell dt log-uniform
+    in [1 h, 30 d]; cells equilibrated on the device."""
+    import torch
+
+    from pfgpu import generate
+    from pfgpu.engine import ReactionEngine
+    from pfgpu.network import default_options
+    members = []
+    for n in C3_NCOMP:
+        net = generate.random_network(n, 3 * n, max(1, n // 2), seed=seed + n, options=default_options(isothermal=0))
+        st, ct, cc = generate.random_cells(net, cells_per_network + cells_per_network // 10 + 64, seed=seed * 7 + n,
+                                           dt_range=(3600.0, 30 * 86400.0))
+        eng = ReactionEngine(net)
+        dev = st.to(device)
+        its = eng.equilibrate(dev, ct, torch.from_numpy(cc).to(device))
+        good = torch.nonzero(its > 0).flatten()[:cells_per_network]
+        if good.numel() < cells_per_network:
+            raise RuntimeError("ncomp %d: only %d of %d cells equilibrated" % (n, good.numel(), cells_per_network))
+        dev = dev.subset(good)
+        dev.a["pri_act_coef"].fill_(1.0)
+        dev.a["sec_act_coef"].fill_(1.0)
+        dev.a["sec_molal"].zero_()
+        eng.update_auxvars(dev, False)
+        eng.update_auxvars(dev, True)
+        eng.update_auxvars(dev, True)
+        eng.update_auxvars(dev, False)
+        eng.update_activity_coefs(dev)
+        members.append((eng, dev))
+    torch.cuda.synchronize()
+    return members
+
+
+def run_c3(args):
+    """Heterogeneous batching: 8 networks, per-cell dt, 50 operator-split
+    steps (RTUpdateAuxVars + TIMESTEP activities + RStep per network) in one
+    CUDA graph; value = cells x steps / graph time."""
+    import numpy as np
+    import torch
+
+    from pfgpu import abi, autotune
+    from pfgpu.timeloop import OperatorSplitLoop
+    per = args.cells or 500_000
+    nsteps = args.graph_steps
+    t0 = time.perf_counter()
+    members = build_c3(per, "cuda")
+    log("c3 state built: %d x %d cells in %.1f s" % (len(members), per, time.perf_counter() - t0))
+    tuned = {}
+    for eng, dev in members:
+        if args.no_tune:
+            continue
+        best, table = autotune.tune(eng, dev, 86400.0, max_cells=65536, reps=1, use_cache=False, quick=True)
+        tuned[eng.net.ncomp] = dict(best, ms_65k=table[0]["ms"])
+    log("c3 autotune:", json.dumps(tuned))
+    fields = [k for k in MUTABLE]
+    start = [{k: dev.a[k].clone() for k in fields if k in dev.a} for _, dev in members]
+
+    def reset(snap):
+        for (_, dev), sn in zip(members, snap):
+            for k, v in sn.items():
+                dev.a[k].copy_(v)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    # first step eagerly: per network, batched (natural order) vs plain
+    per_net = []
+    for i, (eng, dev) in enumerate(members):
+        reset(start)
+        b_ms = timed(lambda: eng.rstep(dev, 86400.0, stats=False))
+        its = dev.a["newton_its"].to(torch.float64)
+        reset(start)
+        p_ms = timed(lambda: eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_PLAIN, stats=False))
+        per_net.append(dict(ncomp=eng.net.ncomp, nsec=eng.net.nsec, nmnrl=eng.net.nmnrl, cells=dev.ncells,
+                            batched_ms=b_ms, plain_ms=p_ms, its_mean=float(its.mean()),
+                            its_p50=float(its.median()), its_max=int(its.max()),
+                            its_min=int(its.min())))
+    batched_first = sum(r["batched_ms"] for r in per_net)
+    plain_first = sum(r["plain_ms"] for r in per_net)
+    # one eager warm step of the loop (its Newton counts order the first graph step)
+    reset(start)
+    loop = OperatorSplitLoop(members, dt=86400.0, concurrent=args.concurrent)
+    loop.step()
+    torch.cuda.synchronize()
+    s0 = [{k: dev.a[k].clone() for k in fields if k in dev.a} for _, dev in members]
+    loop.capture(nsteps)
+    torch.cuda.synchronize()
+    graph_ms = []
+    with Clocks(0) as clk:
+        for _ in range(max(1, args.steps)):
+            reset(s0)
+            graph_ms.append(timed(loop.replay))
+    summary = loop.summary()
+    # the same steps eagerly (launch overhead comparison), a few steps only
+    k_e = min(nsteps, 5)
+    reset(s0)
+    eager_ms = timed(lambda: [loop.step() for _ in range(k_e)])
+    total_cells = sum(dev.ncells for _, dev in members)
+    g = float(np.min(graph_ms))
+    value = total_cells * nsteps / (g * 1e-3)
+    line = {"metric": "heterogeneous batched cell-solves/s, 8 networks, %d operator-split steps in one CUDA graph"
+            % nsteps, "value": value, "unit": UNIT, "n_gpus": 1, "steps": len(graph_ms), "warmup": 1,
+            "ms_per_step": g / nsteps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "8 synthetic networks ncomp %s, 3*ncomp complexes, ncomp/2 kinetic minerals, "
+                                   "%d cells each, per-cell dt log-U[1 h, 30 d], T U[5,60] C" % (C3_NCOMP, per),
+                       "graph_steps": nsteps, "concurrent_streams": bool(args.concurrent),
+                       "l2": "state > L2; reset D2D before each replay, outside the timed region"},
+            "graph_ms": g, "eager_ms_per_step": eager_ms / k_e,
+            "first_step": {"batched_ms": batched_first, "plain_ms": plain_first,
+                           "speedup_vs_plain_gpu": plain_first / batched_first, "per_network": per_net},
+            "last_step": summary, "autotune": tuned, "clocks": clk.summary(),
+            # per network per step: auxvars, activities, setup pre-pass, persistent kernel
+            "gpu_launches": len(graph_ms) * nsteps * 4 * len(members)}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     import numpy as np  # noqa: F401
     rank = int(os.environ.get("RANK", "0"))
@@ -303,8 +430,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"],
-                    help="c5: only the global-implicit assembly on 128x128x64 cells")
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c5"],
+                    help="c3: 8 heterogeneous networks, time loop in one CUDA graph; "
+                         "c5: only the global-implicit assembly on 128x128x64 cells")
+    ap.add_argument("--graph-steps", type=int, default=50, help="c3: operator-split steps in the graph")
+    ap.add_argument("--concurrent", action="store_true", help="c3: one stream per network inside the graph")
     ap.add_argument("--cells", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -331,6 +461,9 @@ def main():
         dist.init_process_group("nccl")
 
     from pfgpu import abi, flops
+    if args.config == "c3":
+        run_c3(args)
+        return
     cfg = workload(args.config)
     ncells = args.cells or cfg["cells"]
     t_build = time.perf_counter()

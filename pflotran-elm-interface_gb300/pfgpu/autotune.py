@@ -31,15 +31,17 @@ def network_key(eng) -> str:
                                   h.hexdigest()[:12])
 
 
-def candidates():
+def candidates(quick: bool = False):
+    tpbs = (64, 128, 192, 256) if quick else range(32, 257, 32)
+    bpss = (1, 2, 4) if quick else (1, 2, 3, 4)
     for js in (1, 0):
-        for tpb in range(32, 257, 32):
-            for bps in (1, 2, 3, 4):
+        for tpb in tpbs:
+            for bps in bpss:
                 yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=js)
 
 
 def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2, use_cache: bool = True,
-         verbose: bool = False):
+         verbose: bool = False, quick: bool = False):
     import torch
     key = network_key(eng)
     cache = {}
@@ -56,7 +58,7 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
     sample = state.subset(torch.arange(n, device=state.a["porosity"].device))
     pristine = {k: sample.a[k].clone() for k in MUTABLE if k in sample.a}
     table = []
-    for cfg in candidates():
+    for cfg in candidates(quick):
         if eng.set_launch_config(**cfg) != abi.PF_OK:
             continue
         best = None

@@ -1,0 +1,114 @@
+"""The reaction half of the operator-split time loop, captured in a CUDA graph.
+
+One operator-split time step of PFLOTRAN's OSRT mode does, for the cells
+(`pm_osrt.F90:115-153`, `pmc_subsurface_osrt.F90:276-386`):
+
+    RTUpdateAuxVars(cells, act coefs = F)        totals from pri_molal
+    RTUpdateActivityCoefficients                 when the frequency is TIMESTEP
+    (transport solve of the totals)              not part of this path
+    RStep in every cell                          the reaction step
+
+`OperatorSplitLoop` runs that sequence for one or more reaction networks
+(each with its own engine and cell state, as when a domain holds several
+chemical systems), with the batched kernel's work queue ordered by the
+previous step's Newton counts (longest cells first).  `capture(nsteps)`
+records `nsteps` consecutive steps of every network into one CUDA graph;
+`replay()` launches it.  Nothing in a step synchronises with the host, so
+the graph holds the whole time loop; the per-cell status and iteration
+arrays carry the results out.
+"""
+from __future__ import annotations
+
+from . import abi
+
+
+class OperatorSplitLoop:
+    def __init__(self, members, dt: float = 0.0, kernel: int = abi.PF_KERNEL_BATCHED, cost_order: bool = True,
+                 concurrent: bool = False):
+        """members: sequence of (ReactionEngine, CellState on the device).
+        dt: uniform step [s]; ignored for states that carry a per-cell dt.
+        concurrent: run each member's step on its own stream (forked from
+        and joined back into the calling stream every step), so that one
+        network's queue tail overlaps the next network's work."""
+        self.members = list(members)
+        self.dt = float(dt)
+        for _, st in self.members:
+            if not self.dt > 0.0 and st.a.get("dt_cell") is None:
+                raise ValueError("dt must be > 0 for states without a per-cell dt")
+        self.kernel = kernel
+        self.cost_order = cost_order
+        self.graph = None
+        self.nsteps = 0
+        self.concurrent = concurrent
+        self._streams = None
+
+    def _order(self, st):
+        import torch
+        if not self.cost_order or self.kernel != abi.PF_KERNEL_BATCHED:
+            return None
+        return torch.argsort(st.a["newton_its"].to(torch.int64), descending=True)
+
+    def _member_step(self, eng, st):
+        eng.update_auxvars(st, False)
+        if eng.net.options["act_coef_update_frequency"] == abi.PF_ACT_COEF_TIMESTEP:
+            eng.update_activity_coefs(st)
+        # a state's per-cell dt array, when present, overrides dt
+        dt = self.dt if self.dt > 0.0 else 1.0
+        eng.rstep(st, dt, kernel=self.kernel, stats=False, order=self._order(st))
+
+    def step(self):
+        """One operator-split reaction step of every member, enqueued on the
+        current stream (and, when concurrent, on per-member streams joined
+        back into it); no host synchronisation."""
+        import torch
+        if not self.concurrent:
+            for eng, st in self.members:
+                self._member_step(eng, st)
+            return
+        main = torch.cuda.current_stream()
+        if self._streams is None:
+            self._streams = [torch.cuda.Stream() for _ in self.members]
+        fork = torch.cuda.Event()
+        fork.record(main)
+        joins = []
+        for (eng, st), s in zip(self.members, self._streams):
+            s.wait_event(fork)
+            with torch.cuda.stream(s):
+                self._member_step(eng, st)
+                ev = torch.cuda.Event()
+                ev.record(s)
+                joins.append(ev)
+        for ev in joins:
+            main.wait_event(ev)
+
+    def capture(self, nsteps: int):
+        """Record nsteps steps into one CUDA graph.  Scratch is reserved
+        first, so nothing allocates inside the capture; run at least one step
+        eagerly before capturing (lazy initialisation of the sort and of the
+        kernels' launch attributes).  Capturing enqueues no work: the state
+        is unchanged until replay()."""
+        import torch
+        for eng, st in self.members:
+            eng.reserve(st.ncells)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(nsteps):
+                self.step()
+        self.graph, self.nsteps = g, nsteps
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            raise RuntimeError("capture() first")
+        self.graph.replay()
+
+    def summary(self):
+        """Host reduction of the per-cell outputs of the last step (the
+        reference's rstep_error MAX and iteration sums)."""
+        out = []
+        for eng, st in self.members:
+            its = st.a["newton_its"]
+            out.append(dict(ncomp=eng.net.ncomp, cells=st.ncells, failed_cells=int((st.a["status"] != 0).sum()),
+                            newton_iterations=int(its.sum()), max_newton_iterations=int(its.max()),
+                            max_substeps=int(st.a["num_substeps"].max())))
+        return out
