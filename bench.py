@@ -441,7 +441,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-girt", action="store_true")
     ap.add_argument("--grid", default="128x128x64", help="global-implicit grid NXxNYxNZ")
-    ap.add_argument("--launch", default="", help="threads_per_block,blocks_per_sm,jac_in_shared (skips tuning)")
+    ap.add_argument("--launch", default="",
+                    help="threads_per_block,blocks_per_sm,jac_in_shared[,lanes_per_cell] (skips tuning)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -484,8 +485,8 @@ def main():
     dt = cfg["dt"]
     tuned = None
     if args.launch:
-        tpb, bps, js = (int(x) for x in args.launch.split(","))
-        if eng.set_launch_config(tpb, bps, js) != abi.PF_OK:
+        vals = [int(x) for x in args.launch.split(",")]
+        if eng.set_launch_config(*vals) != abi.PF_OK:
             raise SystemExit("launch config %s rejected" % args.launch)
     elif not args.no_tune:
         from pfgpu import autotune

@@ -26,6 +26,8 @@ struct PfNetwork {
   std::vector<double> dbls_base;             // host copy of the double block at create
   std::vector<int32_t> ints_base;            // host copy of the int block
   void* d_girt = nullptr;                    // global-implicit lookup tables (built on first use)
+  void* d_group = nullptr;                   // group-kernel inverse lists (dev.grp points into it)
+  PfLaunchConfig launch_lane{};              // last one-lane-per-cell configuration (adjoint)
   GirtTabs girt{};
   size_t ib = 0;                             // byte offset of the double block
   PfLaunchConfig launch{};
@@ -249,8 +251,13 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   net->dbls_base = dbls;
   net->ints_base = ints;
   net->ib = ib;
+  if (group_build_tables(dev, ints.data(), &net->d_group, &dev.grp) != PF_OK) {
+    pf_network_destroy(net);
+    return PF_ERR_CUDA;
+  }
   net->dev = dev;
   net->launch = default_launch(dev);
+  net->launch_lane = net->launch;
   *out = net;
   return PF_OK;
 }
@@ -279,6 +286,7 @@ int32_t pf_network_destroy(PfNetwork* net) {
   if (net->d_ctype) cudaFree(net->d_ctype);
   if (net->d_scratch) cudaFree(net->d_scratch);
   if (net->d_girt) cudaFree(net->d_girt);
+  if (net->d_group) cudaFree(net->d_group);
   delete net;
   return PF_OK;
 }
@@ -318,8 +326,12 @@ int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg) {
   if (cfg->threads_per_block < 32 || cfg->threads_per_block > 256 || cfg->threads_per_block % 32 ||
       cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 16)
     return PF_ERR_INVALID;
+  const int G = cfg->lanes_per_cell;
+  if (G != 0 && G != 1 && G != 4 && G != 8) return PF_ERR_INVALID;
+  if (G > 1 && !group_supported(net->dev, G)) return PF_ERR_UNSUPPORTED;
   if (batched_smem_bytes(net->dev, *cfg) > 227u * 1024u) return PF_ERR_TOO_LARGE;
   net->launch = *cfg;
+  if (G <= 1) net->launch_lane = *cfg;
   return PF_OK;
 }
 
@@ -426,7 +438,7 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
   if (e == cudaSuccess && a->loss) e = cudaMemsetAsync(a->loss, 0, sizeof(double), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(net->d_counters, 0, 8 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return PF_ERR_CUDA;
-  if (launch_rstep_batched(d, *state, dt, net->launch, net->num_sms, net->d_scratch, net->d_counters,
+  if (launch_rstep_batched(d, *state, dt, net->launch_lane, net->num_sms, net->d_scratch, net->d_counters,
                            net->d_counters + 1, s, a) != 0)
     return PF_ERR_CUDA;
   return PF_OK;

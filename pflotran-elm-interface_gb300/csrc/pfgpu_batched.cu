@@ -18,6 +18,7 @@ PF_BATCHED_NCOMPS(PF_DECL)
 static size_t lane_doubles(int n, bool js) { return (js ? (size_t)n * n : 0) + 6 * (size_t)n; }
 
 size_t batched_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg) {
+  if (cfg.lanes_per_cell > 1) return group_smem_bytes(net, cfg);
   const size_t tables = (size_t)net.int_words * 4 + (size_t)net.dbl_words * 8;
   const size_t lane = lane_doubles(net.n, cfg.jac_in_shared != 0) * 8 + (size_t)net.n * 4;
   return tables + lane * (size_t)cfg.threads_per_block;
@@ -95,6 +96,8 @@ int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, co
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
   }
+  if (cfg.lanes_per_cell > 1 && !adj)
+    return launch_rstep_group(net, net.grp, st, dt, cfg, num_sms, scratch, queue, counters, stream);
   switch (net.n) {
 #define PF_CASE(N) \
   case N:          \

@@ -17,6 +17,15 @@ int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt,
                          const PfLaunchConfig& cfg, int num_sms, double* scratch,
                          unsigned long long* queue, unsigned long long* counters,
                          cudaStream_t stream, const PfAdjointArgs* adj = nullptr);
+// K3: the same step with a group of lanes per cell (pfgpu_group.cu); used by
+// launch_rstep_batched when cfg.lanes_per_cell > 1
+bool group_supported(const DevNet& net, int lanes_per_cell);
+size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg);
+int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState& st, double dt,
+                       const PfLaunchConfig& cfg, int num_sms, const double* scratch, unsigned long long* queue,
+                       unsigned long long* counters, cudaStream_t stream);
+// host: per-species inverse lists from the host copy of the int block
+int group_build_tables(const DevNet& net, const int32_t* h_ints, void** d_buf, GroupTabs* out);
 // doubles of per-cell scratch the batched kernel's setup pre-pass writes
 size_t batched_scratch_doubles(const DevNet& net, int64_t ncells);
 // shared memory bytes a batched launch of this config needs

@@ -127,7 +127,7 @@ class PfGirtArgs(C.Structure):
 class PfLaunchConfig(C.Structure):
     _fields_ = [
         ("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
-        ("jac_in_shared", C.c_int32), ("reserved", C.c_int32),
+        ("jac_in_shared", C.c_int32), ("lanes_per_cell", C.c_int32),
     ]
 
 

@@ -32,12 +32,19 @@ def network_key(eng) -> str:
 
 
 def candidates(quick: bool = False):
+    """One lane per cell: threads per block x blocks per SM x Jacobian in
+    shared or local memory; a group of 4 or 8 lanes per cell: threads per
+    block x blocks per SM (the library refuses what it cannot run)."""
     tpbs = (64, 128, 192, 256) if quick else range(32, 257, 32)
     bpss = (1, 2, 4) if quick else (1, 2, 3, 4)
     for js in (1, 0):
         for tpb in tpbs:
             for bps in bpss:
-                yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=js)
+                yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=js, lanes_per_cell=1)
+    for g in (4, 8):
+        for tpb in (64, 128, 192, 256):
+            for bps in (1, 2, 4):
+                yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=0, lanes_per_cell=g)
 
 
 def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2, use_cache: bool = True,
@@ -76,7 +83,7 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
         if verbose:
             print(cfg, "%.3f ms" % best)
     table.sort(key=lambda r: r["ms"])
-    top = {k: table[0][k] for k in ("threads_per_block", "blocks_per_sm", "jac_in_shared")}
+    top = {k: table[0][k] for k in ("threads_per_block", "blocks_per_sm", "jac_in_shared", "lanes_per_cell")}
     eng.set_launch_config(**top)
     for k, v in pristine.items():
         sample.a[k].copy_(v)

@@ -65,8 +65,10 @@ class ReactionEngine:
         abi.check("pf_network_get_launch", self.lib.pf_network_get_launch(self.handle, C.byref(cfg)))
         return {k: getattr(cfg, k) for k, _ in abi.PfLaunchConfig._fields_}
 
-    def set_launch_config(self, threads_per_block, blocks_per_sm, jac_in_shared):
-        cfg = abi.PfLaunchConfig(int(threads_per_block), int(blocks_per_sm), int(jac_in_shared), 0)
+    def set_launch_config(self, threads_per_block, blocks_per_sm, jac_in_shared=0, lanes_per_cell=1):
+        """Returns the PfStatus (PF_OK when the configuration is accepted)."""
+        cfg = abi.PfLaunchConfig(int(threads_per_block), int(blocks_per_sm), int(jac_in_shared),
+                                 int(lanes_per_cell))
         return self.lib.pf_network_set_launch(self.handle, C.byref(cfg))
 
     # ------------------------------------------------------------ steps

@@ -143,6 +143,9 @@ def compare(net, ref, got, label, self_ref=None):
 _SELF = {}
 
 
+GROUP = {"group4": 4, "group8": 8}
+
+
 def run_pair(oracle, name, kernel, tight=False):
     net, st0 = cases.case(oracle, name, tight=tight)
     dt = cases.CASE_DT[name]
@@ -157,6 +160,11 @@ def run_pair(oracle, name, kernel, tight=False):
             perts.append(pert)
         _SELF[(name, tight)] = perts
     eng = _engine(net)
+    if kernel in GROUP:
+        # the group-per-cell kernel, where the library accepts the shape
+        if eng.set_launch_config(128, 2, 0, GROUP[kernel]) != abi.PF_OK:
+            pytest.skip("%s: ncomp %d not covered" % (kernel, net.ncomp))
+        kernel = abi.PF_KERNEL_BATCHED
     dev = st0.to("cuda")
     stats = eng.rstep(dev, dt, kernel=kernel)
     torch.cuda.synchronize()
@@ -164,11 +172,12 @@ def run_pair(oracle, name, kernel, tight=False):
     return net, ref, got, stats, _SELF[(name, tight)]
 
 
-@pytest.mark.parametrize("kernel", [abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED], ids=["plain", "batched"])
+@pytest.mark.parametrize("kernel", [abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED, "group4", "group8"],
+                         ids=["plain", "batched", "group4", "group8"])
 @pytest.mark.parametrize("name", ["calcite", "random12"] + ["hetero%d" % n for n in cases.HETERO])
 def test_rstep_parity(oracle, name, kernel):
     net, ref, got, stats, pert = run_pair(oracle, name, kernel)
-    label = "%s/%s" % (name, "plain" if kernel == 0 else "batched")
+    label = "%s/%s" % (name, kernel if kernel in GROUP else ("plain" if kernel == 0 else "batched"))
     errs, flips, same, outliers, self_flips, self_out = compare(net, ref, got, label, pert)
     n_single = int(same.sum()) + flips
     slack = max(2, 0.01 * n_single)
@@ -181,12 +190,13 @@ def test_rstep_parity(oracle, name, kernel):
     assert stats["max_newton_iterations"] == int(got.a["newton_its"].max())
 
 
+@pytest.mark.parametrize("kernel", [abi.PF_KERNEL_BATCHED, "group8"], ids=["batched", "group8"])
 @pytest.mark.parametrize("name", ["calcite", "random12", "hetero16"])
-def test_rstep_parity_tight(oracle, name):
+def test_rstep_parity_tight(oracle, name, kernel):
     """Tight tolerances: every solve converges to rounding level, separating
     arithmetic error from stopping-rule noise."""
-    net, ref, got, stats, pert = run_pair(oracle, name, abi.PF_KERNEL_BATCHED, tight=True)
-    compare(net, ref, got, name + "/batched/tight", pert)
+    net, ref, got, stats, pert = run_pair(oracle, name, kernel, tight=True)
+    compare(net, ref, got, "%s/%s/tight" % (name, kernel if kernel in GROUP else "batched"), pert)
     # tight solves converge far below the 1e-10 exit test, so even cells
     # whose iteration count flipped agree
     ok = (ref.a["status"] == 0) & (got.a["status"] == 0) & (ref.a["num_substeps"] == 1) & \
@@ -282,3 +292,27 @@ def test_write_parity_report():
     os.makedirs(OUT, exist_ok=True)
     with open(os.path.join(OUT, "parity_report.json"), "w") as f:
         json.dump(_report, f, indent=1, sort_keys=True)
+
+
+@pytest.mark.parametrize("lanes", [4, 8])
+def test_group_kernel_order_invariant_and_close_to_one_lane(oracle, lanes):
+    """The group-per-cell kernel: results do not depend on the work-queue
+    order, and agree with the one-lane kernel to rounding on cells whose
+    Newton path is the same."""
+    net, st0 = cases.case(oracle, "random12")
+    eng = _engine(net)
+    assert eng.set_launch_config(128, 2, 0, lanes) == abi.PF_OK
+    a = st0.to("cuda")
+    eng.rstep(a, 86400.0)
+    b = st0.to("cuda")
+    order = torch.argsort(a.a["newton_its"].to(torch.int64), descending=True)
+    eng.rstep(b, 86400.0, order=order)
+    for k in ("total", "pri_molal", "sec_molal", "mnrl_rate", "mnrl_volfrac", "newton_its", "status"):
+        assert torch.equal(a.a[k], b.a[k]), k
+    one = _engine(net)
+    c = st0.to("cuda")
+    one.rstep(c, 86400.0)
+    same = (a.a["newton_its"] == c.a["newton_its"]) & (a.a["status"] == 0) & (c.a["status"] == 0)
+    assert same.float().mean() > 0.95
+    d = (a.a["pri_molal"] - c.a["pri_molal"]).abs() / c.a["pri_molal"]
+    assert float(d[:, same].max()) < 1e-10
