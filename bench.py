@@ -314,7 +314,8 @@ def run_c3(args):
     for eng, dev in members:
         if args.no_tune:
             continue
-        best, table = autotune.tune(eng, dev, 86400.0, max_cells=65536, reps=1, use_cache=False, quick=True)
+        best, table = autotune.tune(eng, dev, 86400.0, max_cells=max(65536, per // 4), reps=1, use_cache=False,
+                                    quick=True, cost_order=True)
         tuned[eng.net.ncomp] = dict(best, ms_65k=table[0]["ms"])
     log("c3 autotune:", json.dumps(tuned))
     fields = [k for k in MUTABLE]
@@ -490,7 +491,10 @@ def main():
             raise SystemExit("launch config %s rejected" % args.launch)
     elif not args.no_tune:
         from pfgpu import autotune
-        best, table = autotune.tune(eng, dev, dt, use_cache=False)
+        # the timed steps run with the cost-ordered queue: tune that way, on a
+        # quarter of the cells
+        best, table = autotune.tune(eng, dev, dt, use_cache=False, cost_order=True,
+                                    max_cells=max(65536, ncells // 4), reps=1)
         tuned = {"best": best, "top": table[:6]}
         log("autotune:", json.dumps(tuned))
 

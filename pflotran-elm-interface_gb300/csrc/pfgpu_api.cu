@@ -429,7 +429,12 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
     return PF_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   if (state->ncells == 0) return PF_OK;
-  rc = ensure_scratch(net, state->ncells);
+  // the group kernel carries the adjoint with a substep store after the
+  // setup scratch; otherwise one lane per cell with the last such config
+  const bool grp = net->launch.lanes_per_cell > 1 &&
+                   group_smem_bytes(d, net->launch, true) <= 227u * 1024u;
+  const size_t base = batched_scratch_doubles(d, state->ncells);
+  rc = ensure_scratch_doubles(net, base + (grp ? group_adj_store_doubles(d, state->ncells) : 0));
   if (rc) return rc;
   cudaError_t e = cudaSuccess;
   if (d.ns) e = cudaMemsetAsync(a->dL_dlogK_sec, 0, d.ns * sizeof(double), s);
@@ -438,8 +443,8 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
   if (e == cudaSuccess && a->loss) e = cudaMemsetAsync(a->loss, 0, sizeof(double), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(net->d_counters, 0, 8 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return PF_ERR_CUDA;
-  if (launch_rstep_batched(d, *state, dt, net->launch_lane, net->num_sms, net->d_scratch, net->d_counters,
-                           net->d_counters + 1, s, a) != 0)
+  if (launch_rstep_batched(d, *state, dt, grp ? net->launch : net->launch_lane, net->num_sms, net->d_scratch,
+                           net->d_counters, net->d_counters + 1, s, a, grp ? net->d_scratch + base : nullptr) != 0)
     return PF_ERR_CUDA;
   return PF_OK;
 }

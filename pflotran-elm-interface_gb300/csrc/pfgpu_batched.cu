@@ -88,7 +88,7 @@ size_t batched_scratch_doubles(const DevNet& net, int64_t ncells) {
 
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
                          int num_sms, double* scratch, unsigned long long* queue, unsigned long long* counters,
-                         cudaStream_t stream, const PfAdjointArgs* adj) {
+                         cudaStream_t stream, const PfAdjointArgs* adj, double* adj_store) {
   {
     const int tpb = 128;
     const int64_t blocks = (st.ncells + tpb - 1) / tpb;
@@ -96,8 +96,9 @@ int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, co
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
   }
-  if (cfg.lanes_per_cell > 1 && !adj)
-    return launch_rstep_group(net, net.grp, st, dt, cfg, num_sms, scratch, queue, counters, stream);
+  if (cfg.lanes_per_cell > 1 && (!adj || adj_store))
+    return launch_rstep_group(net, net.grp, st, dt, cfg, num_sms, scratch, queue, counters, stream, adj,
+                              adj_store);
   switch (net.n) {
 #define PF_CASE(N) \
   case N:          \

@@ -25,7 +25,17 @@
 //     group follows one control path.
 // The work queue hands out cells to groups exactly as the one-lane kernel
 // hands them to lanes.  Log formulation only (the launch falls back to the
-// one-lane kernel otherwise); no adjoint.
+// one-lane kernel otherwise).
+//
+// ADJ = true adds the implicit adjoint of the step (pf_adjoint), as in the
+// one-lane kernel: the converged iterate and dt of every substep go to a
+// global store [PF_ADJ_MAX_SUBSTEPS][n + 1][ncells]; when the group finishes
+// the forward step it walks the substeps backwards, rebuilding the exact
+// Jacobian at each stored iterate (true mineral derivative), solving
+// J u = B Tbar (B the minerals' part of J), lambda = (Tbar - u)/(psv/dt),
+// and accumulating theta_bar += (dT/dtheta)^T u - (dR/dtheta)^T lambda.
+// Gradients of the network parameters collect per lane over its own
+// complexes and minerals and are reduced over the warp at the end.
 #include <vector>
 
 #include "pfgpu_common.cuh"
@@ -42,12 +52,14 @@ __device__ __forceinline__ unsigned long long absbits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
-enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3 };
+enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3, BACK = 4 };
 
 // per-cell workspace (doubles): J n*n | power table 4n | s ns | Ksec' ns |
-// Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n
-__host__ __device__ inline int ws_doubles(const DevNet& net) {
-  return (net.n * net.n + 5 * net.n + 2 * net.ns + 5 * net.nm + 1) & ~1;
+// Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n; the adjoint
+// adds Tbar n | lambda n | nu.Tbar nm | area gradient nm
+__host__ __device__ inline int ws_doubles(const DevNet& net, bool adj) {
+  const int base = net.n * net.n + 5 * net.n + 2 * net.ns + 5 * net.nm;
+  return (base + (adj ? 2 * net.n + 2 * net.nm : 0) + 1) & ~1;
 }
 
 __device__ __forceinline__ double dh_ln_gamma(double z, double a0, double sI, double I, const DevNet& net) {
@@ -70,10 +82,11 @@ __device__ __forceinline__ unsigned long long gmax(unsigned long long v, unsigne
   return v;
 }
 
-template <int G, int R>
+template <int G, int R, bool ADJ>
 __global__ void __launch_bounds__(256)
 rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
-                   unsigned long long* queue, unsigned long long* counters) {
+                   unsigned long long* queue, unsigned long long* counters, PfAdjointArgs adj,
+                   double* __restrict__ adj_store) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) uint64_t tma_bar;
   const int tid = threadIdx.x;
@@ -125,7 +138,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << (gi * G));
   const int cells_per_block = (int)(blockDim.x / G);
   const int slot = tid / G;
-  const int WS = ws_doubles(net);
+  const int WS = ws_doubles(net, ADJ);
   double* wsbase = reinterpret_cast<double*>(smem + ibytes + dbytes);
   double* J = wsbase + (size_t)slot * WS;
   double* pw = J + n * n;
@@ -137,6 +150,10 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   double* mIm = ratem + nm;
   double* mf = mIm + nm;
   double* xs = mf + nm;
+  double* tb = xs + n;       // ADJ: Tbar of every species
+  double* lamv = tb + n;     // ADJ: lambda of every species
+  double* nuT = lamv + n;    // ADJ: nu_m . Tbar per mineral
+  double* garea = nuT + nm;  // ADJ: dL/dln area of this cell per mineral
   int* piv = reinterpret_cast<int*>(wsbase + (size_t)cells_per_block * WS) + slot * n;
 
   const SoA soa{st.ncells};
@@ -161,8 +178,23 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   int kstep[R];
   unsigned small_mask = 0;  // bit t: own species t was floored
   unsigned long long my_its = 0, my_fail = 0, my_maxits = 0, my_maxsub = 0;
+  // adjoint: running dL/dT of the own species, direct dL/dT0 of floored
+  // ones, the substep being walked back, per-lane parameter accumulators
+  // (own complexes s = r + G*q, own minerals m = r + G*q)
+  constexpr int QS = ADJ ? (PF_MAX_NSEC + G - 1) / G : 1;
+  constexpr int QM = ADJ ? (PF_MAX_NMNRL + G - 1) / G : 1;
+  double Tbar[R], gdir[R];
+  double gK[QS], gKm[QM], glnk[QM];
+  double loss_acc = 0.0;
+  int sb = 0;
+  bool back_done = false, back_fail = false;
+  if constexpr (ADJ) {
+    for (int q = 0; q < QS; ++q) gK[q] = 0.0;
+    for (int q = 0; q < QM; ++q) { gKm[q] = 0.0; glnk[q] = 0.0; }
+  }
 #pragma unroll
   for (int t = 0; t < R; ++t) {
+    Tbar[t] = gdir[t] = 0.0;
     c[t] = lnc[t] = g[t] = tot[t] = fixed[t] = init_tot[t] = guess[t] = lnguess[t] = small_val[t] = rhs[t] = 0.0;
     vv[t] = 0.0;
     kstep[t] = -1;
@@ -246,8 +278,10 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
     }
 
     // ---------------------------------------------------------- Newton trip
-    if (phase == ITER) {
-      its += 1;
+    // (a backward trip, BACK, shares the evaluation and the factorisation)
+    if (phase == ITER || (ADJ && phase == BACK)) {
+      const bool back = ADJ && phase == BACK;
+      if (!back) its += 1;
       if (newton_iter_act) {
         // RActivityCoefficients LAG from this iterate and the previous
         // evaluation's sec_molal (reaction.F90:4553-4612)
@@ -295,7 +329,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           v *= (pe >= 0) ? pw[pe] : exp(T.sec_nu(p) * log(pw[T.sec_idx(p)]));
         }
         sv[s] = v;
-        st.sec_molal[soa.at(s, cell)] = v;
+        if (!back) st.sec_molal[soa.at(s, cell)] = v;
       }
       // ---- kinetic minerals m = r, r+G, ... (reaction_mineral.F90:647-1078)
       for (int m = r; m < nm; m += G) {
@@ -340,12 +374,21 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
               ft = ft * (1.0 + QK / rl / den) / den;
             }
             Imv = Im;
-            fv = ft * den_k * 1.0e-3;  // the reference's den*1e-3 on dQK/dm (:944-947)
+            // the reference's den*1e-3 on dQK/dm (:944-947); the adjoint
+            // takes the true derivative
+            fv = back ? ft : ft * den_k * 1.0e-3;
           }
         }
-        ratem[m] = rv;
+        if (!back) ratem[m] = rv;
         mIm[m] = Imv;
         mf[m] = fv;
+        if constexpr (ADJ) {
+          if (back) {
+            double acc = 0.0;
+            for (int p = b; p < e; ++p) acc = fma(T.mnrl_nu(p), tb[T.mnrl_idx(p)], acc);
+            nuT[m] = acc;
+          }
+        }
       }
       __syncwarp(gmask);
       // ---- own rows: totals, residual, Jacobian row (log formulation)
@@ -370,13 +413,19 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
             Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
           }
         }
-        tot[t] = fma(b_tot, Sa, den_L * c[t]);
-        double rr = dry ? 0.0 : fma(a_acc, c[t], Sa) - fixed[t] * inv_dt;
+        double rr;
+        if (!back) {
+          tot[t] = fma(b_tot, Sa, den_L * c[t]);
+          rr = dry ? 0.0 : fma(a_acc, c[t], Sa) - fixed[t] * inv_dt;
+        } else {
+          rr = 0.0;  // backward solve J u = B Tbar
+        }
         Jr[i] = fma(a_acc, c[t], Jr[i]);
         for (int q = gt.mp_ptr[i]; q < gt.mp_ptr[i + 1]; ++q) {
           const int m = gt.mp_m[q];
           const double nui = T.mnrl_nu(gt.mp_p[q]);
-          if (!dry) rr = fma(nui, mIm[m], rr);
+          if (back) rr = fma(nui * mf[m], nuT[m], rr);
+          else if (!dry) rr = fma(nui, mIm[m], rr);
           const double co = nui * mf[m];
           for (int p = T.mnrl_begin(m); p < T.mnrl_end(m); ++p) {
             const int j = T.mnrl_idx(p);
@@ -392,16 +441,19 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
       // ---- convergence tests on the residual (reaction.F90:3946-3953)
       const double two_norm = sqrt(gsum<G>(dot_p, gmask));
       const unsigned long long mxb = gmax<G>(mx_p, gmask);
-      if (its == 1) r0 = two_norm;
+      if (!back && its == 1) r0 = two_norm;
       int react_end = -1;
-      if (its > o.maximum_reaction_iterations) {
+      if (back) {
+        // falls through to the factorisation below
+      } else if (its > o.maximum_reaction_iterations) {
 #pragma unroll
         for (int t = 0; t < R; ++t) tot[t] = init_tot[t];
         react_end = 1;
       } else if (__longlong_as_double((long long)mxb) < o.max_residual_tolerance ||
                  two_norm < o.max_rel_residual_tolerance * r0) {
         react_end = 0;
-      } else {
+      }
+      if (back || react_end < 0) {
         __syncwarp(gmask);
         // ---- implicit-pivot scales of the own rows (utility.F90:621-644)
         bool bad = false;
@@ -417,7 +469,8 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           }
         }
         if (__any_sync(gmask, bad)) {
-          react_end = 1;  // singular: no total restore (reaction.F90:3963-3966)
+          if (back) back_fail = true;
+          else react_end = 1;  // singular: no total restore (reaction.F90:3963-3966)
         } else {
           // ---- right-looking elimination, rhs alongside
           for (int k = 0; k < n; ++k) {
@@ -487,36 +540,85 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
             }
           }
           __syncwarp(gmask);
-          // ---- update of the own species (reaction.F90:3993-4046)
-          const double tol = o.max_relative_change_tolerance;
-          bool small = true;
-          double nc[R], u[R];
+          if constexpr (ADJ) {
+            if (back) {
+              // u = x; lambda = (Tbar - u)/(psv/dt); theta_bar += (dT/dtheta)^T u
+              // - (dR/dtheta)^T lambda; Tbar(previous substep) = Tbar - u
+              const double ipd = den_L / a_acc;
 #pragma unroll
-          for (int t = 0; t < R; ++t) {
-            const int i = r + G * t;
-            if (i < n) {
-              u[t] = o.fork_literal_rsolve ? 0.0 : xs[i];
-              u[t] = fmin(fmax(u[t], -o.max_dlnC_rreact), o.max_dlnC_rreact);
-              nc[t] = c[t] * exp(-u[t]);
-              small = small && (absbits(nc[t] - c[t]) < absbits(tol * c[t]));
+              for (int t = 0; t < R; ++t) {
+                const int i = r + G * t;
+                if (i < n) lamv[i] = (Tbar[t] - xs[i]) * ipd;
+              }
+              __syncwarp(gmask);
+              for (int s2 = r, q = 0; s2 < ns; s2 += G, ++q) {
+                double acc = 0.0;
+                for (int p = T.sec_begin(s2); p < T.sec_end(s2); ++p) acc = fma(T.sec_nu(p), xs[T.sec_idx(p)], acc);
+                gK[q] = fma(acc, -LOG_TO_LN * den_L * sv[s2], gK[q]);
+              }
+              for (int m = r, q = 0; m < nm; m += G, ++q) {
+                if (mIm[m] == 0.0 && mf[m] == 0.0) continue;
+                double lam = 0.0;
+                for (int p = T.mnrl_begin(m); p < T.mnrl_end(m); ++p)
+                  lam = fma(T.mnrl_nu(p), lamv[T.mnrl_idx(p)], lam);
+                gKm[q] = fma(LOG_TO_LN * mf[m], lam, gKm[q]);
+                glnk[q] = fma(-mIm[m], lam, glnk[q]);
+                garea[m] = fma(-mIm[m], lam, garea[m]);
+              }
+#pragma unroll
+              for (int t = 0; t < R; ++t) {
+                const int i = r + G * t;
+                if (i < n) {
+                  Tbar[t] = Tbar[t] - xs[i];
+                  tb[i] = Tbar[t];
+                }
+              }
+              sb -= 1;
+              if (sb >= 0) {
+#pragma unroll
+                for (int t = 0; t < R; ++t) {
+                  const int i = r + G * t;
+                  if (i < n) c[t] = adj_store[((size_t)sb * (n + 1) + i) * ncells + cell];
+                }
+                inv_dt = 1.0 / adj_store[((size_t)sb * (n + 1) + n) * ncells + cell];
+              } else {
+                back_done = true;
+              }
+              __syncwarp(gmask);
             }
           }
-          if (__all_sync(gmask, small)) {
-            react_end = 0;
-          } else {
+          if (!back) {
+            // ---- update of the own species (reaction.F90:3993-4046)
+            const double tol = o.max_relative_change_tolerance;
+            bool small = true;
+            double nc[R], u[R];
 #pragma unroll
             for (int t = 0; t < R; ++t) {
               const int i = r + G * t;
               if (i < n) {
-                lnc[t] = lnc[t] - u[t];
-                c[t] = nc[t];
+                u[t] = o.fork_literal_rsolve ? 0.0 : xs[i];
+                u[t] = fmin(fmax(u[t], -o.max_dlnC_rreact), o.max_dlnC_rreact);
+                nc[t] = c[t] * exp(-u[t]);
+                small = small && (absbits(nc[t] - c[t]) < absbits(tol * c[t]));
+              }
+            }
+            if (__all_sync(gmask, small)) {
+              react_end = 0;
+            } else {
+#pragma unroll
+              for (int t = 0; t < R; ++t) {
+                const int i = r + G * t;
+                if (i < n) {
+                  lnc[t] = lnc[t] - u[t];
+                  c[t] = nc[t];
+                }
               }
             }
           }
         }
       }
       // ---- RStep bookkeeping (reaction.F90:3650-3718)
-      if (react_end >= 0) {
+      if (!back && react_end >= 0) {
         its_total += its;
         if (react_end == 1) {
           num_cuts = num_cuts + 1;
@@ -533,6 +635,16 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
             const double v = vfm[m] + ratem[m] * T.molar_vol(m) * dt;
             vfm[m] = v < 0.0 ? 0.0 : v;
           }
+          if constexpr (ADJ) {
+            if (nsub < PF_ADJ_MAX_SUBSTEPS) {
+#pragma unroll
+              for (int t = 0; t < R; ++t) {
+                const int i = r + G * t;
+                if (i < n) adj_store[((size_t)nsub * (n + 1) + i) * ncells + cell] = c[t];
+              }
+              if (r == 0) adj_store[((size_t)nsub * (n + 1) + n) * ncells + cell] = dt;
+            }
+          }
           cum = cum + dt;
           nsub += 1;
           n_const += 1;
@@ -548,6 +660,22 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           if (cum >= target) finish_cell = true;
           else phase = START;
         }
+      }
+    }
+
+    if constexpr (ADJ) {
+      // end of a backward pass: per-cell gradients
+      if (phase == BACK && (back_done || back_fail)) {
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+          const int i = r + G * t;
+          if (i < n)
+            adj.dL_dtotal0[soa.at(i, cell)] = back_fail ? 0.0 : ((small_mask & (1u << t)) ? gdir[t] : Tbar[t]);
+        }
+        for (int m = r; m < nm; m += G) adj.dL_dlnarea[soa.at(m, cell)] = back_fail ? 0.0 : garea[m];
+        if (r == 0 && adj.adj_status) adj.adj_status[cell] = back_fail ? 3 : 0;
+        back_done = back_fail = false;
+        phase = NEED;
       }
     }
 
@@ -581,7 +709,76 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         my_maxsub = max(my_maxsub, (unsigned long long)nsub);
       }
       phase = NEED;
+      if constexpr (ADJ) {
+        // loss contribution and dL/dT(final); start the backward pass
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+          const int i = r + G * t;
+          if (i >= n) continue;
+          const double tv = (!cell_failed && (small_mask & (1u << t))) ? small_val[t] : tot[t];
+          double gj;
+          if (adj.weight) {
+            const double w = adj.weight[soa.at(i, cell)], d = tv - adj.target[soa.at(i, cell)];
+            loss_acc = fma(w * d, d, loss_acc);
+            gj = 2.0 * w * d;
+          } else {
+            gj = adj.dL_dtotal[soa.at(i, cell)];
+          }
+          // a floored component's final total is its restored input
+          // (reaction.F90:3721-3725): dL/dT0 directly, no path through m
+          const bool fl = small_mask & (1u << t);
+          gdir[t] = fl ? gj : 0.0;
+          Tbar[t] = fl ? 0.0 : gj;
+          tb[i] = Tbar[t];
+        }
+        for (int m = r; m < nm; m += G) garea[m] = 0.0;
+        const int astat = cell_failed ? 1 : (nsub > PF_ADJ_MAX_SUBSTEPS ? 2 : 0);
+        if (astat != 0 || dry || nsub == 0) {
+#pragma unroll
+          for (int t = 0; t < R; ++t) {
+            const int i = r + G * t;
+            if (i < n) adj.dL_dtotal0[soa.at(i, cell)] = (astat == 0) ? gdir[t] : 0.0;
+          }
+          for (int m = r; m < nm; m += G) adj.dL_dlnarea[soa.at(m, cell)] = 0.0;
+          if (r == 0 && adj.adj_status) adj.adj_status[cell] = astat;
+        } else {
+          sb = nsub - 1;
+#pragma unroll
+          for (int t = 0; t < R; ++t) {
+            const int i = r + G * t;
+            if (i < n) c[t] = adj_store[((size_t)sb * (n + 1) + i) * ncells + cell];
+          }
+          inv_dt = 1.0 / adj_store[((size_t)sb * (n + 1) + n) * ncells + cell];
+          phase = BACK;
+        }
+        __syncwarp(gmask);
+      }
     }
+  }
+  if constexpr (ADJ) {
+    // parameter gradients and the loss: sum the groups of the warp (lanes
+    // r, r+G, ... hold the same parameters), one atomic per parameter
+    auto across = [&](double v) {
+#pragma unroll
+      for (int off = 16; off >= G; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+      return v;
+    };
+    for (int q = 0; q < (ns + G - 1) / G; ++q) {
+      const double v = across(gK[q]);
+      const int s2 = r + G * q;
+      if (gi == 0 && s2 < ns && v != 0.0) atomicAdd(&adj.dL_dlogK_sec[s2], v);
+    }
+    for (int q = 0; q < (nm + G - 1) / G; ++q) {
+      const double a = across(gKm[q]), b = across(glnk[q]);
+      const int m = r + G * q;
+      if (gi == 0 && m < nm) {
+        if (a != 0.0) atomicAdd(&adj.dL_dlogK_mnrl[m], a);
+        if (b != 0.0) atomicAdd(&adj.dL_dlnk[m], b);
+      }
+    }
+    double l = loss_acc;
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(FULL, l, off);
+    if (lane_id == 0 && adj.loss && l != 0.0) atomicAdd(adj.loss, l);
   }
   if (counters) {
     for (int off = 16; off > 0; off >>= 1) {
@@ -602,11 +799,18 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
 template <int G, int R>
 int launch_k(const DevNet& net, const GroupTabs& gt, const PfCellState& st, double dt, size_t smem, int grid,
              int tpb, const double* scratch, unsigned long long* queue, unsigned long long* counters,
-             cudaStream_t stream) {
-  auto k = rstep_group_kernel<G, R>;
-  cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return (int)err;
-  k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters);
+             const PfAdjointArgs* adj, double* adj_store, cudaStream_t stream) {
+  if (adj) {
+    auto k = rstep_group_kernel<G, R, true>;
+    cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return (int)err;
+    k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, *adj, adj_store);
+  } else {
+    auto k = rstep_group_kernel<G, R, false>;
+    cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return (int)err;
+    k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, PfAdjointArgs{}, nullptr);
+  }
   return (int)cudaGetLastError();
 }
 
@@ -628,23 +832,29 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
   return group_rows_ok(lanes_per_cell, R);
 }
 
-size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg) {
+size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
   const size_t tables = (size_t)net.int_words * 4 + (size_t)net.dbl_words * 8;
   const int G = cfg.lanes_per_cell > 0 ? cfg.lanes_per_cell : 1;
   const size_t cells = (size_t)cfg.threads_per_block / (size_t)G;
-  return tables + cells * ((size_t)group::ws_doubles(net) * 8 + (size_t)net.n * 4);
+  return tables + cells * ((size_t)group::ws_doubles(net, adj) * 8 + (size_t)net.n * 4);
+}
+
+size_t group_adj_store_doubles(const DevNet& net, int64_t ncells) {
+  return (size_t)PF_ADJ_MAX_SUBSTEPS * (size_t)(net.n + 1) * (size_t)ncells;
 }
 
 int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState& st, double dt,
                        const PfLaunchConfig& cfg, int num_sms, const double* scratch, unsigned long long* queue,
-                       unsigned long long* counters, cudaStream_t stream) {
+                       unsigned long long* counters, cudaStream_t stream, const PfAdjointArgs* adj,
+                       double* adj_store) {
   const int G = cfg.lanes_per_cell;
   const int R = (net.n + G - 1) / G;
-  const size_t smem = group_smem_bytes(net, cfg);
+  const size_t smem = group_smem_bytes(net, cfg, adj != nullptr);
   const int tpb = cfg.threads_per_block;
   const int grid = num_sms * cfg.blocks_per_sm;
 #define PF_G(GG, RR) \
-  if (G == GG && R == RR) return group::launch_k<GG, RR>(net, gt, st, dt, smem, grid, tpb, scratch, queue, counters, stream);
+  if (G == GG && R == RR)                                                                                \
+    return group::launch_k<GG, RR>(net, gt, st, dt, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
   PF_G(4, 2)
   PF_G(4, 3)
   PF_G(4, 4)

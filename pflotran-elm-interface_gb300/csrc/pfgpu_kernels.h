@@ -13,17 +13,23 @@ int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
 // queue: device counter zeroed by the caller (cudaMemsetAsync) before launch.
 // counters[0] += Newton iterations, counters[1] += failed cells,
 // counters[2] = error flags (bit 0: table staging timed out).
+// cfg.lanes_per_cell > 1 runs the group kernel; with adj it needs adj_store
+// (group_adj_store_doubles), otherwise adj runs on one lane per cell.
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt,
                          const PfLaunchConfig& cfg, int num_sms, double* scratch,
                          unsigned long long* queue, unsigned long long* counters,
-                         cudaStream_t stream, const PfAdjointArgs* adj = nullptr);
+                         cudaStream_t stream, const PfAdjointArgs* adj = nullptr,
+                         double* adj_store = nullptr);
 // K3: the same step with a group of lanes per cell (pfgpu_group.cu); used by
 // launch_rstep_batched when cfg.lanes_per_cell > 1
 bool group_supported(const DevNet& net, int lanes_per_cell);
-size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg);
+size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg, bool adj = false);
+// doubles of the adjoint's substep store (iterate and dt of each substep)
+size_t group_adj_store_doubles(const DevNet& net, int64_t ncells);
 int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState& st, double dt,
                        const PfLaunchConfig& cfg, int num_sms, const double* scratch, unsigned long long* queue,
-                       unsigned long long* counters, cudaStream_t stream);
+                       unsigned long long* counters, cudaStream_t stream, const PfAdjointArgs* adj = nullptr,
+                       double* adj_store = nullptr);
 // host: per-species inverse lists from the host copy of the int block
 int group_build_tables(const DevNet& net, const int32_t* h_ints, void** d_buf, GroupTabs* out);
 // doubles of per-cell scratch the batched kernel's setup pre-pass writes

@@ -48,7 +48,11 @@ def candidates(quick: bool = False):
 
 
 def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2, use_cache: bool = True,
-         verbose: bool = False, quick: bool = False):
+         verbose: bool = False, quick: bool = False, cost_order: bool = False):
+    """cost_order: time every configuration with the work queue ordered by a
+    first step's Newton counts (longest cells first), as a time loop that
+    orders by the previous step runs; without it the sample's tail of slow
+    cells favours configurations that are only better on unordered queues."""
     import torch
     key = network_key(eng)
     cache = {}
@@ -64,6 +68,10 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
     n = min(state.ncells, max_cells)
     sample = state.subset(torch.arange(n, device=state.a["porosity"].device))
     pristine = {k: sample.a[k].clone() for k in MUTABLE if k in sample.a}
+    order = None
+    if cost_order:
+        eng.rstep(sample, dt, stats=False)
+        order = torch.argsort(sample.a["newton_its"].to(torch.int64), descending=True)
     table = []
     for cfg in candidates(quick):
         if eng.set_launch_config(**cfg) != abi.PF_OK:
@@ -74,7 +82,7 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
                 sample.a[k].copy_(v)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            eng.rstep(sample, dt, stats=False)
+            eng.rstep(sample, dt, stats=False, order=order)
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
@@ -83,11 +91,17 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
         if verbose:
             print(cfg, "%.3f ms" % best)
     table.sort(key=lambda r: r["ms"])
-    top = {k: table[0][k] for k in ("threads_per_block", "blocks_per_sm", "jac_in_shared", "lanes_per_cell")}
+    keys = ("threads_per_block", "blocks_per_sm", "jac_in_shared", "lanes_per_cell")
+    top = {k: table[0][k] for k in keys}
+    # the library keeps the last one-lane configuration for the adjoint:
+    # install the best one first, then the overall best
+    lane1 = [r for r in table if r["lanes_per_cell"] <= 1]
+    if lane1:
+        eng.set_launch_config(**{k: lane1[0][k] for k in keys})
     eng.set_launch_config(**top)
     for k, v in pristine.items():
         sample.a[k].copy_(v)
-    cache[key] = {"best": top, "table": table[:12], "cells": n}
+    cache[key] = {"best": top, "table": table[:12], "cells": n, "cost_order": bool(cost_order)}
     try:
         json.dump(cache, open(CACHE, "w"), indent=1)
     except OSError:

@@ -32,11 +32,13 @@ DT = None    # set per case by the fixture
 CASE = None
 
 
-def _setup(oracle, name, ncells=240):
+def _setup(oracle, name, lanes=1, ncells=240):
     net, st0 = cases.case(oracle, name, tight=True)
     st0 = st0.subset(np.arange(ncells))
     from pfgpu.engine import ReactionEngine
     eng = ReactionEngine(net)
+    if lanes > 1:
+        assert eng.set_launch_config(128, 2, 0, lanes) == abi.PF_OK
     dev = st0.to("cuda")
     eng.rstep(dev, DT)
     Tf = dev.a["total"].cpu().numpy()
@@ -125,11 +127,15 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / scale)
 
 
-@pytest.fixture(scope="module", params=["random12", "calcite"])
+@pytest.fixture(scope="module", params=[("random12", 1), ("random12", 8), ("calcite", 1), ("calcite", 8)],
+                ids=["random12-lane", "random12-group8", "calcite-lane", "calcite-group8"])
 def adjoint_case(oracle, request):
+    """Both step kernels carry the adjoint: one lane per cell, and a group of
+    8 lanes per cell (launch configuration lanes_per_cell = 8)."""
     global DT, CASE
-    DT, CASE = DTS[request.param], request.param
-    net, st0, eng, w, tgt = _setup(oracle, request.param)
+    name, lanes = request.param
+    DT, CASE = DTS[name], name
+    net, st0, eng, w, tgt = _setup(oracle, name, lanes)
     dev = st0.to("cuda")
     g = eng.adjoint(dev, DT, weight=torch.from_numpy(w).cuda(), target=torch.from_numpy(tgt).cuda())
     g = {k: v.cpu().numpy() for k, v in g.items()}
@@ -242,3 +248,30 @@ def test_autograd_function_matches_adjoint(adjoint_case):
     after, _ = _gpu_loss(eng, st0, w, tgt)
     before = g["loss"][0]
     assert after.sum() == pytest.approx(before, rel=1e-12)
+
+
+@pytest.mark.parametrize("lanes", [4, 8])
+def test_group_adjoint_matches_one_lane(oracle, lanes):
+    """The group kernel's adjoint and the one-lane kernel's agree per cell
+    wherever the two forward solves took the same Newton path."""
+    from pfgpu.engine import ReactionEngine
+    net, st0 = cases.case(oracle, "random12")
+    st0 = st0.subset(np.arange(1000))
+    rng = np.random.default_rng(5)
+    w = torch.from_numpy(rng.uniform(0, 1, st0.a["total"].shape)).cuda()
+    tgt = torch.from_numpy(st0.a["total"] * np.exp(0.05 * rng.standard_normal(st0.a["total"].shape))).cuda()
+    out = []
+    for g in (1, lanes):
+        eng = ReactionEngine(net)
+        if g > 1:
+            assert eng.set_launch_config(128, 2, 0, g) == abi.PF_OK
+        dev = st0.to("cuda")
+        gr = eng.adjoint(dev, 86400.0, weight=w, target=tgt)
+        out.append(({k: v.cpu().numpy() for k, v in gr.items()}, dev.numpy()))
+    (g1, s1), (g2, s2) = out
+    same = (s1.a["newton_its"] == s2.a["newton_its"]) & (g1["adj_status"] == 0) & (g2["adj_status"] == 0)
+    assert same.mean() > 0.95
+    for k in ("dL_dtotal0", "dL_dlnarea"):
+        a, b = g1[k][:, same], g2[k][:, same]
+        assert np.max(np.abs(a - b)) <= 1e-8 * max(np.max(np.abs(a)), 1e-300), k
+    assert g2["loss"][0] == pytest.approx(g1["loss"][0], rel=1e-9)
