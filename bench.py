@@ -314,7 +314,7 @@ def run_c3(args):
     for eng, dev in members:
         if args.no_tune:
             continue
-        best, table = autotune.tune(eng, dev, 86400.0, max_cells=max(65536, per // 4), reps=1, use_cache=False,
+        best, table = autotune.tune(eng, dev, 86400.0, max_cells=65536, reps=1, use_cache=False,
                                     quick=True, cost_order=True)
         tuned[eng.net.ncomp] = dict(best, ms_65k=table[0]["ms"])
     log("c3 autotune:", json.dumps(tuned))
@@ -557,10 +557,13 @@ def main():
     peak = fp64_peak(abi.load(), sms)
     achieved = flops_per_launch / (kern_avg * 1e-3) / 1e12
     state_bytes = sum(v.numel() * v.element_size() for v in dev.a.values())
-    # DRAM bytes per cell-solve of this kernel measured by ncu on the same
-    # workload at 200,000 cells (profiles/rstep_batched_kernel_n12_200k.txt:
-    # 5.437 GB read + 5.561 GB written per launch), scaled to this launch
-    traffic = (5.437e9 + 5.561e9) / 200_000 * ncells if args.config == "c2" else None
+    # DRAM bytes per cell-solve of the launched kernel measured by ncu on the
+    # same workload at 200,000 cells, scaled to this launch:
+    #   one lane per cell  profiles/rstep_batched_kernel_n12_200k.txt   5.437 + 5.561 GB
+    #   group of lanes     profiles/rstep_group_kernel_g4_n12_200k.txt  1.796 + 0.583 GB
+    grp = eng.launch_config()["lanes_per_cell"] > 1
+    per_launch_200k = (1.796e9 + 0.583e9) if grp else (5.437e9 + 5.561e9)
+    traffic = per_launch_200k / 200_000 * ncells if args.config == "c2" else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic,
                 "traffic_unit": "bytes per launch (ncu, scaled by cells)",
@@ -616,7 +619,10 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": cfg["workload"], "cells": ncells, "dt_s": dt,
                            "parallelism": "replicas" if world > 1 else "single-gpu",
-                           "l2": "state %.2f GB > L2; state reset D2D each step" % (state_bytes / 1e9),
+                           "l2": ("state %.2f GB > L2 (129 MB); state reset D2D each step" % (state_bytes / 1e9))
+                           if state_bytes > 129e6 else
+                           ("state %.1f MB fits in L2, not flushed: this small case is launch-bound; reset D2D "
+                            "each step" % (state_bytes / 1e6)),
                            "kernel": "batched persistent (PF_KERNEL_BATCHED)",
                            "cell_order": "descending Newton count of the previous step",
                            "launch": eng.launch_config(), "autotune": tuned},
