@@ -515,9 +515,11 @@ def main():
                                        order=order)
     nat_total, nat_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, max(1, min(args.steps, 3)), 1)
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        # replicas: the slowest rank's time, and the reference loop's
+        # rstep_error MAX / iteration sums over the ranks
+        from pfgpu.replicas import max_over_ranks, reduce_step_stats
+        total_ms = max_over_ranks(total_ms, device="cuda")
+        stats = reduce_step_stats(stats, device="cuda")
     value = world * ncells * args.steps / (total_ms * 1e-3)
     kern_avg = float(np.mean(kern_ms))
 
