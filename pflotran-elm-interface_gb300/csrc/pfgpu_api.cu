@@ -251,7 +251,7 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   net->dbls_base = dbls;
   net->ints_base = ints;
   net->ib = ib;
-  if (group_build_tables(dev, ints.data(), &net->d_group, &dev.grp) != PF_OK) {
+  if (group_build_tables(dev, ints.data(), dbls.data(), &net->d_group, &dev.grp) != PF_OK) {
     pf_network_destroy(net);
     return PF_ERR_CUDA;
   }

@@ -32,10 +32,10 @@ enum : int32_t {
 // pri_Z pri_a0 sec_Z sec_a0 mnrl_nu(nnz_m) mnrl_logK mnrl_logKcoef(5nm)
 // rate_constant activation_energy molar_vol affinity_threshold rate_limiter
 // msf temkin power]
-// Per-species inverse lists for the group-per-cell step kernel (device
-// pointers into one allocation): for species i, the secondary complexes
-// sp_s[sp_ptr[i]..sp_ptr[i+1]) that contain it with the CSR slot sp_p of i in
-// each, and the same for the kinetic minerals (mp_*).
+// Lookup tables of the group-per-cell step kernel (device pointers into one
+// allocation): for species i, the secondary complexes sp_s[sp_ptr[i] ..
+// sp_ptr[i+1]) that contain it with the CSR slot sp_p of i in each, and the
+// same for the kinetic minerals (mp_*).
 struct GroupTabs {
   const int32_t* sp_ptr;
   const int32_t* sp_s;

@@ -55,10 +55,11 @@ __device__ __forceinline__ unsigned long long absbits(double x) {
 enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3, BACK = 4 };
 
 // per-cell workspace (doubles): J n*n | power table 4n | s ns | Ksec' ns |
-// Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n; the adjoint
-// adds Tbar n | lambda n | nu.Tbar nm | area gradient nm
+// Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n | m n |
+// pivot scales n | rhs n; the adjoint adds Tbar n | lambda n | nu.Tbar nm |
+// area gradient nm; then ints: pivot order n | remaining rows n
 __host__ __device__ inline int ws_doubles(const DevNet& net, bool adj) {
-  const int base = net.n * net.n + 5 * net.n + 2 * net.ns + 5 * net.nm;
+  const int base = net.n * net.n + 8 * net.n + 2 * net.ns + 5 * net.nm;
   return (base + (adj ? 2 * net.n + 2 * net.nm : 0) + 1) & ~1;
 }
 
@@ -150,11 +151,15 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   double* mIm = ratem + nm;
   double* mf = mIm + nm;
   double* xs = mf + nm;
-  double* tb = xs + n;       // ADJ: Tbar of every species
+  double* cv = xs + n;       // molalities of the current iterate
+  double* vvs = cv + n;      // implicit-pivot scales, then 1/pivot
+  double* rhsv = vvs + n;    // residual / right-hand side, eliminated in place
+  double* tb = rhsv + n;     // ADJ: Tbar of every species
   double* lamv = tb + n;     // ADJ: lambda of every species
   double* nuT = lamv + n;    // ADJ: nu_m . Tbar per mineral
   double* garea = nuT + nm;  // ADJ: dL/dln area of this cell per mineral
-  int* piv = reinterpret_cast<int*>(wsbase + (size_t)cells_per_block * WS) + slot * n;
+  int* piv = reinterpret_cast<int*>(wsbase + (size_t)cells_per_block * WS) + slot * 2 * n;
+  int* rows = piv + n;
 
   const SoA soa{st.ncells};
   const PfOptions o = net.o;
@@ -174,8 +179,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   bool dry = false, zero_step = false;
   int its = 0, its_total = 0, nsub = 0, num_cuts = 0, n_const = 0;
   // own species / rows i = r + G*t
-  double c[R], lnc[R], g[R], tot[R], fixed[R], init_tot[R], guess[R], lnguess[R], small_val[R], rhs[R], vv[R];
-  int kstep[R];
+  double c[R], lnc[R], g[R], tot[R], fixed[R], init_tot[R], guess[R], lnguess[R], small_val[R];
   unsigned small_mask = 0;  // bit t: own species t was floored
   unsigned long long my_its = 0, my_fail = 0, my_maxits = 0, my_maxsub = 0;
   // adjoint: running dL/dT of the own species, direct dL/dT0 of floored
@@ -195,9 +199,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
 #pragma unroll
   for (int t = 0; t < R; ++t) {
     Tbar[t] = gdir[t] = 0.0;
-    c[t] = lnc[t] = g[t] = tot[t] = fixed[t] = init_tot[t] = guess[t] = lnguess[t] = small_val[t] = rhs[t] = 0.0;
-    vv[t] = 0.0;
-    kstep[t] = -1;
+    c[t] = lnc[t] = g[t] = tot[t] = fixed[t] = init_tot[t] = guess[t] = lnguess[t] = small_val[t] = 0.0;
   }
 
   for (;;) {
@@ -310,6 +312,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         const int i = r + G * t;
         if (i < n) {
           const double a = c[t] * g[t];
+          cv[i] = c[t];
           pw[i] = a;
           pw[n + i] = a * a;
           if (neg_mask & (1u << i)) {
@@ -391,7 +394,8 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         }
       }
       __syncwarp(gmask);
-      // ---- own rows: totals, residual, Jacobian row (log formulation)
+      // ---- own rows: totals, residual, Jacobian row (log formulation),
+      // from the tables staged in shared memory
       const double b_tot = den_L / a_acc;
       double dot_p = 0.0;
       unsigned long long mx_p = 0;
@@ -434,7 +438,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         }
         if (dry)
           for (int j = 0; j < n; ++j) Jr[j] = (i == j) ? c[t] : 0.0;
-        rhs[t] = rr;
+        rhsv[i] = rr;
         dot_p = fma(rr, rr, dot_p);
         mx_p = max(mx_p, absbits(rr));
       }
@@ -455,89 +459,77 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
       }
       if (back || react_end < 0) {
         __syncwarp(gmask);
-        // ---- implicit-pivot scales of the own rows (utility.F90:621-644)
+        // ---- implicit-pivot scales (utility.F90:621-644), rows over the lanes
         bool bad = false;
-#pragma unroll
-        for (int t = 0; t < R; ++t) {
-          const int i = r + G * t;
-          kstep[t] = -1;
-          if (i < n) {
-            unsigned long long am = 0;
-            for (int j = 0; j < n; ++j) am = max(am, absbits(J[i * n + j]));
-            if (am == 0ull || am > 0x7ff0000000000000ull) bad = true;
-            vv[t] = 1.0 / __longlong_as_double((long long)am);
-          }
+        for (int i = r; i < n; i += G) {
+          unsigned long long am = 0;
+          for (int j = 0; j < n; ++j) am = max(am, absbits(J[i * n + j]));
+          if (am == 0ull || am > 0x7ff0000000000000ull) bad = true;
+          vvs[i] = 1.0 / __longlong_as_double((long long)am);
+          rows[i] = i;
         }
         if (__any_sync(gmask, bad)) {
           if (back) back_fail = true;
           else react_end = 1;  // singular: no total restore (reaction.F90:3963-3966)
         } else {
-          // ---- right-looking elimination, rhs alongside
+          __syncwarp(gmask);
+          // ---- right-looking elimination over the remaining rows (compact
+          // list), rhs alongside; work split by (row, column) pairs
+          int nrem = n;
           for (int k = 0; k < n; ++k) {
             unsigned long long key = 0;
-            int prow = -1;
-#pragma unroll
-            for (int t = 0; t < R; ++t) {
-              const int i = r + G * t;
-              if (i < n && kstep[t] < 0) {
-                const unsigned long long dum = absbits(vv[t] * J[i * n + k]);
-                if (dum >= key) { key = dum; prow = i; }
-              }
+            int prow = -1, ppos = -1;
+            for (int e = r; e < nrem; e += G) {
+              const int i = rows[e];
+              const unsigned long long dum = absbits(vvs[i] * J[i * n + k]);
+              if (dum > key || (dum == key && i > prow)) { key = dum; prow = i; ppos = e; }
             }
 #pragma unroll
             for (int off = G / 2; off > 0; off >>= 1) {
               const unsigned long long ok = __shfl_xor_sync(gmask, key, off, G);
               const int orow = __shfl_xor_sync(gmask, prow, off, G);
-              if (ok > key || (ok == key && orow > prow)) { key = ok; prow = orow; }
+              const int opos = __shfl_xor_sync(gmask, ppos, off, G);
+              if (ok > key || (ok == key && orow > prow)) { key = ok; prow = orow; ppos = opos; }
             }
-            const int owner = prow % G, pt = prow / G;
-            double rp = 0.0, bp = 0.0;
-            if (r == owner) {
-              double a = J[prow * n + k];
-              if (absbits(a) == 0ull) { a = 1.0e-20; J[prow * n + k] = a; }
-              rp = 1.0 / a;
-#pragma unroll
-              for (int t = 0; t < R; ++t)
-                if (t == pt) {
-                  kstep[t] = k;
-                  vv[t] = rp;  // holds 1/pivot from here on
-                  bp = rhs[t];
-                }
+            double a = J[prow * n + k];
+            if (absbits(a) == 0ull) a = 1.0e-20;
+            const double rp = 1.0 / a;
+            const double bp = rhsv[prow];
+            __syncwarp(gmask);
+            if (r == 0) {
+              J[prow * n + k] = a;
+              vvs[prow] = rp;  // holds 1/pivot from here on
               piv[k] = prow;
+              rows[ppos] = rows[nrem - 1];
             }
-            rp = __shfl_sync(gmask, rp, owner, G);
-            bp = __shfl_sync(gmask, bp, owner, G);
+            nrem -= 1;
+            __syncwarp(gmask);
+            for (int e = r; e < nrem; e += G) {
+              const int i = rows[e];
+              const double l = J[i * n + k] * rp;
+              J[i * n + k] = l;
+              rhsv[i] = fma(-l, bp, rhsv[i]);
+            }
+            __syncwarp(gmask);
+            // rank-1 update of the remaining rows, columns split over the lanes
             const double* Jp = J + prow * n;
-#pragma unroll
-            for (int t = 0; t < R; ++t) {
-              const int i = r + G * t;
-              if (i < n && kstep[t] < 0) {
-                double* Ji = J + i * n;
-                const double l = Ji[k] * rp;
-                Ji[k] = l;
-                for (int j = k + 1; j < n; ++j) Ji[j] = fma(-l, Jp[j], Ji[j]);
-                rhs[t] = fma(-l, bp, rhs[t]);
-              }
+            for (int e = 0; e < nrem; ++e) {
+              double* Ji = J + rows[e] * n;
+              const double l = Ji[k];
+              for (int j = k + 1 + r; j < n; j += G) Ji[j] = fma(-l, Jp[j], Ji[j]);
             }
             __syncwarp(gmask);
           }
           // ---- back substitution by columns: x_k = (rhs_p - sum_{j>k} U_pj x_j)/U_pk
           for (int k = n - 1; k >= 0; --k) {
             const int prow = piv[k];
-            const int owner = prow % G, pt = prow / G;
-            double xk = 0.0;
-            if (r == owner) {
-#pragma unroll
-              for (int t = 0; t < R; ++t)
-                if (t == pt) xk = rhs[t] * vv[t];
-            }
-            xk = __shfl_sync(gmask, xk, owner, G);
+            const double xk = rhsv[prow] * vvs[prow];
             if (r == 0) xs[k] = xk;
-#pragma unroll
-            for (int t = 0; t < R; ++t) {
-              const int i = r + G * t;
-              if (i < n && kstep[t] >= 0 && kstep[t] < k) rhs[t] = fma(-J[i * n + k], xk, rhs[t]);
+            for (int kk = r; kk < k; kk += G) {
+              const int i = piv[kk];
+              rhsv[i] = fma(-J[i * n + k], xk, rhsv[i]);
             }
+            __syncwarp(gmask);
           }
           __syncwarp(gmask);
           if constexpr (ADJ) {
@@ -836,7 +828,7 @@ size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg, bool adj) 
   const size_t tables = (size_t)net.int_words * 4 + (size_t)net.dbl_words * 8;
   const int G = cfg.lanes_per_cell > 0 ? cfg.lanes_per_cell : 1;
   const size_t cells = (size_t)cfg.threads_per_block / (size_t)G;
-  return tables + cells * ((size_t)group::ws_doubles(net, adj) * 8 + (size_t)net.n * 4);
+  return tables + cells * ((size_t)group::ws_doubles(net, adj) * 8 + (size_t)net.n * 8);
 }
 
 size_t group_adj_store_doubles(const DevNet& net, int64_t ncells) {
@@ -865,7 +857,8 @@ int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState
   return -1;
 }
 
-int group_build_tables(const DevNet& net, const int32_t* I, void** d_buf, GroupTabs* out) {
+int group_build_tables(const DevNet& net, const int32_t* I, const double* D, void** d_buf, GroupTabs* out) {
+  (void)D;
   const int n = net.n;
   std::vector<std::vector<int32_t>> ss(n), sp(n), mm(n), mp(n);
   for (int s = 0; s < net.ns; ++s)

@@ -30,8 +30,10 @@ int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState
                        const PfLaunchConfig& cfg, int num_sms, const double* scratch, unsigned long long* queue,
                        unsigned long long* counters, cudaStream_t stream, const PfAdjointArgs* adj = nullptr,
                        double* adj_store = nullptr);
-// host: per-species inverse lists from the host copy of the int block
-int group_build_tables(const DevNet& net, const int32_t* h_ints, void** d_buf, GroupTabs* out);
+// host: the group kernel's lookup tables from the host copies of the packed
+// network blocks
+int group_build_tables(const DevNet& net, const int32_t* h_ints, const double* h_dbls, void** d_buf,
+                       GroupTabs* out);
 // doubles of per-cell scratch the batched kernel's setup pre-pass writes
 size_t batched_scratch_doubles(const DevNet& net, int64_t ncells);
 // shared memory bytes a batched launch of this config needs
