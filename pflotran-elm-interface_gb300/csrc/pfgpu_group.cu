@@ -55,11 +55,11 @@ __device__ __forceinline__ unsigned long long absbits(double x) {
 enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3, BACK = 4 };
 
 // per-cell workspace (doubles): J n*n | power table 4n | s ns | Ksec' ns |
-// Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n | m n |
+// Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n |
 // pivot scales n | rhs n; the adjoint adds Tbar n | lambda n | nu.Tbar nm |
 // area gradient nm; then ints: pivot order n | remaining rows n
 __host__ __device__ inline int ws_doubles(const DevNet& net, bool adj) {
-  const int base = net.n * net.n + 8 * net.n + 2 * net.ns + 5 * net.nm;
+  const int base = net.n * net.n + 7 * net.n + 2 * net.ns + 5 * net.nm;
   return (base + (adj ? 2 * net.n + 2 * net.nm : 0) + 1) & ~1;
 }
 
@@ -151,8 +151,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   double* mIm = ratem + nm;
   double* mf = mIm + nm;
   double* xs = mf + nm;
-  double* cv = xs + n;       // molalities of the current iterate
-  double* vvs = cv + n;      // implicit-pivot scales, then 1/pivot
+  double* vvs = xs + n;      // implicit-pivot scales, then 1/pivot
   double* rhsv = vvs + n;    // residual / right-hand side, eliminated in place
   double* tb = rhsv + n;     // ADJ: Tbar of every species
   double* lamv = tb + n;     // ADJ: lambda of every species
@@ -312,7 +311,6 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         const int i = r + G * t;
         if (i < n) {
           const double a = c[t] * g[t];
-          cv[i] = c[t];
           pw[i] = a;
           pw[n + i] = a * a;
           if (neg_mask & (1u << i)) {
