@@ -6,9 +6,9 @@ iteration (src/pflotran/reaction.F90 RReact :3851-4045 with RTotalAqueous
 reaction_mineral.F90:647-1078 without prefactors, RSolve :5457-5516 and the
 Crout LU utility.F90:597-735): add/sub/mul/div each 1, a fused multiply-add 2,
 sqrt 1.  exp/log/pow calls are counted separately as transcendentals.
-These are the units of the FP64 roofline ("algorithmic flops"); the counting
-build of the oracle measures the same quantity by instrumenting every
-operation (tests/test_flops.py checks that the two agree).
+These are the units of the FP64 roofline ("algorithmic flops").  The counts
+are read off the reference's loops (one term per statement, in the order of
+the routines named above), not measured by instrumenting a run.
 """
 from __future__ import annotations
 
