@@ -16,6 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+LIB_COUNT = os.path.join(HERE, "_build", "liboracle_count.so")
 
 _REPO = os.path.dirname(HERE)
 _PKG = os.path.join(_REPO, "pflotran-elm-interface_gb300")
@@ -28,8 +29,11 @@ CON_TOTAL, CON_FREE, CON_PH, CON_CHARGE_BAL, CON_LOG = 1, 2, 3, 4, 5
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "rxn_oracle.hpp")]
-    if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
+    srcs = [os.path.join(HERE, f) for f in ("oracle_capi.cpp", "oracle_count.cpp", "rxn_oracle.hpp",
+                                            "flop_real.hpp")]
+    stale = force or not all(os.path.exists(x) for x in (LIB, LIB_COUNT)) or any(
+        os.path.getmtime(s) > min(os.path.getmtime(LIB), os.path.getmtime(LIB_COUNT)) for s in srcs)
+    if stale:
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB
 
@@ -123,6 +127,28 @@ class Oracle:
         if rc:
             raise RuntimeError("oracle_girt_assemble: %d" % rc)
         return r, vals
+
+    def count_rstep(self, net, state, dt):
+        """RStep of every cell with counted arithmetic (single thread; the
+        state is advanced).  Returns per-cell (flops, transcendental calls,
+        Newton iterations) of the reference algorithm: add/sub/mul/div/sqrt
+        one flop, fma two; exp/log/pow counted apart."""
+        if not hasattr(self, "_count"):
+            lib = C.CDLL(LIB_COUNT)
+            lib.oracle_count_rstep.argtypes = [C.POINTER(abi.PfNetworkDesc), C.POINTER(abi.PfCellState),
+                                               C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+            lib.oracle_count_rstep.restype = C.c_int
+            self._count = lib
+        d, s = self._args(net, state)
+        n = state.ncells
+        fl = np.zeros(n, np.int64)
+        tr = np.zeros(n, np.int64)
+        its = np.zeros(n, np.int32)
+        rc = self._count.oracle_count_rstep(C.byref(d), C.byref(s), float(dt), fl.ctypes.data, tr.ctypes.data,
+                                            its.ctypes.data)
+        if rc:
+            raise RuntimeError("oracle_count_rstep: %d" % rc)
+        return fl, tr, its
 
     def density(self, t, p):
         return self.lib.oracle_ifc67_density(t, p)

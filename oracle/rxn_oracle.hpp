@@ -74,11 +74,13 @@ struct Net {
       ns(desc->nsec), nm(desc->nmnrl) {}
 };
 
-// ReactionInterpolateLogK, reaction_aux.F90:1285-1312
-inline void interpolate_logK(const double* coefs, double* logKs, double temp, int n) {
+// ReactionInterpolateLogK, reaction_aux.F90:1285-1312 (the coefficient type
+// is a parameter so that a counting build can read the network's doubles)
+template <class Coef>
+inline void interpolate_logK(const Coef* coefs, double* logKs, double temp, int n) {
   double temp_kelvin = temp + 273.15;
   for (int i = 0; i < n; ++i) {
-    const double* c = coefs + 5 * i;
+    const Coef* c = coefs + 5 * i;
     logKs[i] = c[0] * std::log(temp_kelvin) + c[1] + c[2] * temp_kelvin +
                c[3] / temp_kelvin + c[4] / (temp_kelvin * temp_kelvin);
   }
