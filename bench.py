@@ -53,7 +53,7 @@ def workload(name):
                          "operator-split RStep, non-isothermal", cells=1_000_000, dt=86400.0)
 
 
-def build_state(cfg_name, ncells, device, seed=2026):
+def build_state(cfg_name, ncells, device, seed=2026, keep_inputs=False):
     import torch
 
     from pfgpu import abi, generate
@@ -84,7 +84,46 @@ def build_state(cfg_name, ncells, device, seed=2026):
     eng.update_auxvars(dev, False)
     eng.update_activity_coefs(dev)
     torch.cuda.synchronize()
+    if keep_inputs:
+        return net, eng, dev, (st, ct, cc)
     return net, eng, dev
+
+
+def constraint_measure(net, eng, inputs, cpu=True, reps=3):
+    """Constraint equilibration of the cells' initial conditions
+    (pf_equilibrate_constraint: TOTAL for every component, charge balance on
+    H+), timed on the device from the same host inputs, and the oracle's
+    restatement on the host cores on a bounded sample."""
+    import numpy as np
+    import torch
+    st, ct, cc = inputs
+    cct = torch.from_numpy(cc).to("cuda")
+    ms = []
+    for k in range(reps + 1):
+        dev = st.to("cuda")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        its = eng.equilibrate(dev, ct, cct)
+        e1.record()
+        torch.cuda.synchronize()
+        if k:
+            ms.append(e0.elapsed_time(e1))
+    out = {"cells": st.ncells, "ms": float(np.min(ms)), "cells_per_s": st.ncells / (float(np.min(ms)) * 1e-3),
+           "newton_its_mean": float(its.to(torch.float64).clamp(min=0).mean()),
+           "failed": int((its <= 0).sum())}
+    if cpu:
+        from oracle.oracle import Oracle
+        o = Oracle()
+        cores = os.cpu_count() or 1
+        n = min(st.ncells, 50_000)
+        sub = st.subset(np.arange(n))
+        t = time.perf_counter()
+        o.equilibrate(net, sub, ct, cc[:, :n] if cc.ndim == 2 else cc, nthreads=cores)
+        el = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": n / el, "unit": "cells/s", "cores": cores, "kind": "port",
+                               "sample": "%d cells, %.2f s" % (n, el)}
+    return out
 
 
 class Clocks:
@@ -200,7 +239,7 @@ def cpu_baseline(net, host_state, dt, budget_s=15.0):
             "sample": "%d cells of the same workload, one RStep each, %.2f s" % (n, el)}
 
 
-def girt_measure(net, eng, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11):
+def girt_measure(net, eng, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, cpu=False):
     """Global-implicit residual + SeqBAIJ Jacobian assembly (pf_girt_assemble)
     on an nx*ny*nz structured grid with this network's cells (tiled over the
     grid), Darcy flux |q| ~ U[1e-7, 1e-5] m/s with random sign, D_m = 1e-9
@@ -252,7 +291,29 @@ def girt_measure(net, eng, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11):
     fl, tr = flops.girt_per_cell(net, (nnzb - N) / N)
     tf = fl * N / (ms * 1e-3) / 1e12
     fp64 = fp64_peak(abi.load(), torch.cuda.get_device_properties(0).multi_processor_count)
+    cpu_line = None
+    if cpu:
+        # the oracle's restatement of RTResidual/RTJacobian (one host core) on
+        # a 32x32x16 block of the same cells
+        from oracle.oracle import Oracle
+        from pfgpu.girt import girt_pattern
+        cx, cy, cz = 32, 32, 16
+        Nc = cx * cy * cz
+        host = st.subset(torch.arange(Nc, device=st.a["porosity"].device)).numpy()
+        qh = {k: np.ascontiguousarray(v) for k, v in (("qx", q((cz, cy, cx - 1))), ("qy", q((cz, cy - 1, cx))),
+                                                        ("qz", q((cz - 1, cy, cx))))}
+        gd = dict(nx=cx, ny=cy, nz=cz, dx=1.0, dy=1.0, dz=1.0, diffusion=1e-9, tortuosity=1.0, dispersivity=0.0,
+                  **qh)
+        rp, ci = girt_pattern(cx, cy, cz)
+        tkh = np.ascontiguousarray(host.a["total"] * 1.01)
+        o = Oracle()
+        t = time.perf_counter()
+        o.girt_assemble(net, host, gd, tkh, dt, rp, ci)
+        el = time.perf_counter() - t
+        cpu_line = {"value": Nc / el, "unit": "cells/s", "cores": 1, "kind": "port",
+                    "sample": "32x32x16 grid of the same cells, one assembly, %.3f s" % el}
     return {"grid": "%dx%dx%d" % (nx, ny, nz), "cells": N, "ncomp": n, "nnzb": nnzb, "ms": ms,
+            "cpu_baseline": cpu_line,
             "cells_per_s": N / (ms * 1e-3), "algorithmic_bytes": alg, "achieved_gbs": gbs, "peak_gbs": peak,
             "hbm_frac": gbs / peak if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
             "flops_per_cell": fl, "transcendentals_per_cell": tr, "achieved_tflops": tf, "fp64_peak_tflops": fp64,
@@ -469,11 +530,12 @@ def main():
     cfg = workload(args.config)
     ncells = args.cells or cfg["cells"]
     t_build = time.perf_counter()
-    net, eng, dev = build_state("c2" if args.config == "c5" else args.config, ncells, "cuda", seed=2026 + rank)
+    net, eng, dev, inputs = build_state("c2" if args.config == "c5" else args.config, ncells, "cuda",
+                                        seed=2026 + rank, keep_inputs=True)
     log("state built: %d cells in %.1f s" % (ncells, time.perf_counter() - t_build))
     if args.config == "c5":
         nx, ny, nz = (int(v) for v in args.grid.split("x"))
-        gm = girt_measure(net, eng, dev, args.steps, args.warmup, nx, ny, nz)
+        gm = girt_measure(net, eng, dev, args.steps, args.warmup, nx, ny, nz, cpu=not args.no_cpu)
         if rank == 0:
             print(json.dumps({"metric": "global-implicit residual + SeqBAIJ Jacobian assemblies (cells/s)",
                               "value": gm["cells_per_s"] * world, "unit": "cells/s", "n_gpus": world,
@@ -601,11 +663,16 @@ def main():
         e2e = {"value": ncells * len(times) / sum(times), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
+    constraint = None
+    if args.config == "c2":
+        constraint = constraint_measure(net, eng, inputs, cpu=(rank == 0 and not args.no_cpu))
+        log("constraint:", json.dumps(constraint))
+
     girt = None
     if not args.no_girt and args.config == "c2":
         for k in pristine:
             dev.a[k].copy_(pristine[k])
-        girt = girt_measure(net, eng, dev, max(3, args.steps), max(3, args.warmup))
+        girt = girt_measure(net, eng, dev, max(3, args.steps), max(3, args.warmup), cpu=(rank == 0 and not args.no_cpu))
         log("girt:", json.dumps(girt))
 
     cpu = None
@@ -634,7 +701,7 @@ def main():
                 "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),
                                   "kernel_ms": float(np.mean(nat_kern))},
                 "speedup_vs_plain_gpu": value / plain_value,
-                "adjoint": adjoint, "girt_assembly": girt,
+                "adjoint": adjoint, "girt_assembly": girt, "constraint_equilibration": constraint,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(),
                 # per step: the setup pre-pass and the persistent kernel
