@@ -782,22 +782,31 @@ int launch_batched_k(const DevNet& net, const PfCellState& st, double dt, size_t
   return (int)cudaGetLastError();
 }
 
+// forward variants (Jacobian in shared or local memory) and adjoint variants
+// live in separate translation units so that they compile in parallel
 template <int N>
-int launch_batched_n(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
-                     int num_sms, const double* scratch, unsigned long long* queue,
-                     unsigned long long* counters, const PfAdjointArgs* adj, cudaStream_t stream) {
+int launch_batched_fwd(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
+                       int num_sms, const double* scratch, unsigned long long* queue,
+                       unsigned long long* counters, cudaStream_t stream) {
   const size_t smem = batched_smem_bytes(net, cfg);
   const int tpb = cfg.threads_per_block;
   const int grid = num_sms * cfg.blocks_per_sm;
   const PfAdjointArgs none{};
-  if (adj) {
-    if (cfg.jac_in_shared)
-      return launch_batched_k<N, true, true>(net, st, dt, smem, grid, tpb, scratch, queue, counters, *adj, stream);
-    return launch_batched_k<N, false, true>(net, st, dt, smem, grid, tpb, scratch, queue, counters, *adj, stream);
-  }
   if (cfg.jac_in_shared)
     return launch_batched_k<N, true, false>(net, st, dt, smem, grid, tpb, scratch, queue, counters, none, stream);
   return launch_batched_k<N, false, false>(net, st, dt, smem, grid, tpb, scratch, queue, counters, none, stream);
+}
+
+template <int N>
+int launch_batched_adj(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
+                       int num_sms, const double* scratch, unsigned long long* queue,
+                       unsigned long long* counters, const PfAdjointArgs& adj, cudaStream_t stream) {
+  const size_t smem = batched_smem_bytes(net, cfg);
+  const int tpb = cfg.threads_per_block;
+  const int grid = num_sms * cfg.blocks_per_sm;
+  if (cfg.jac_in_shared)
+    return launch_batched_k<N, true, true>(net, st, dt, smem, grid, tpb, scratch, queue, counters, adj, stream);
+  return launch_batched_k<N, false, true>(net, st, dt, smem, grid, tpb, scratch, queue, counters, adj, stream);
 }
 
 }  // namespace pfgpu
