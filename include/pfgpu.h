@@ -382,14 +382,14 @@ int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state,
 /* Kernel launch configuration for the batched form; chosen by the
  * autotuner (pfgpu.autotune) and settable per network.
  * lanes_per_cell 0 or 1: one lane per cell (ncomp-specialised kernel);
- * 4 or 8: a group of lanes shares each cell, the Jacobian in shared memory
+ * 2, 4 or 8: a group of lanes shares each cell, the Jacobian in shared memory
  * (larger networks; log formulation only; pf_adjoint always uses one lane
  * per cell with the last such configuration set, or the default). */
 typedef struct PfLaunchConfig {
   int32_t threads_per_block;  /* multiple of 32                        */
   int32_t blocks_per_sm;      /* persistent grid = SMs * blocks_per_sm */
   int32_t jac_in_shared;      /* 1: Jacobian in shared memory, 0: local (one lane per cell) */
-  int32_t lanes_per_cell;     /* 0/1, 4 or 8                           */
+  int32_t lanes_per_cell;     /* 0/1, 2, 4 or 8                        */
 } PfLaunchConfig;
 int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg);
 int32_t pf_network_get_launch(const PfNetwork* net, PfLaunchConfig* cfg);

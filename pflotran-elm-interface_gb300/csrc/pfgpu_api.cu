@@ -327,7 +327,7 @@ int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg) {
       cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 16)
     return PF_ERR_INVALID;
   const int G = cfg->lanes_per_cell;
-  if (G != 0 && G != 1 && G != 4 && G != 8) return PF_ERR_INVALID;
+  if (G != 0 && G != 1 && G != 2 && G != 4 && G != 8) return PF_ERR_INVALID;
   if (G > 1 && !group_supported(net->dev, G)) return PF_ERR_UNSUPPORTED;
   if (batched_smem_bytes(net->dev, *cfg) > 227u * 1024u) return PF_ERR_TOO_LARGE;
   net->launch = *cfg;

@@ -41,7 +41,7 @@ def candidates(quick: bool = False):
         for tpb in tpbs:
             for bps in bpss:
                 yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=js, lanes_per_cell=1)
-    for g in (4, 8):
+    for g in (2, 4, 8):
         for tpb in (64, 128, 192, 256):
             for bps in (1, 2, 4):
                 yield dict(threads_per_block=tpb, blocks_per_sm=bps, jac_in_shared=0, lanes_per_cell=g)

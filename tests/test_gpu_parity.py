@@ -143,7 +143,7 @@ def compare(net, ref, got, label, self_ref=None):
 _SELF = {}
 
 
-GROUP = {"group4": 4, "group8": 8}
+GROUP = {"group2": 2, "group4": 4, "group8": 8}
 
 
 def run_pair(oracle, name, kernel, tight=False):
@@ -172,8 +172,8 @@ def run_pair(oracle, name, kernel, tight=False):
     return net, ref, got, stats, _SELF[(name, tight)]
 
 
-@pytest.mark.parametrize("kernel", [abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED, "group4", "group8"],
-                         ids=["plain", "batched", "group4", "group8"])
+@pytest.mark.parametrize("kernel", [abi.PF_KERNEL_PLAIN, abi.PF_KERNEL_BATCHED, "group2", "group4", "group8"],
+                         ids=["plain", "batched", "group2", "group4", "group8"])
 @pytest.mark.parametrize("name", ["calcite", "random12"] + ["hetero%d" % n for n in cases.HETERO])
 def test_rstep_parity(oracle, name, kernel):
     net, ref, got, stats, pert = run_pair(oracle, name, kernel)
@@ -294,7 +294,7 @@ def test_write_parity_report():
         json.dump(_report, f, indent=1, sort_keys=True)
 
 
-@pytest.mark.parametrize("lanes", [4, 8])
+@pytest.mark.parametrize("lanes", [2, 4, 8])
 def test_group_kernel_order_invariant_and_close_to_one_lane(oracle, lanes):
     """The group-per-cell kernel: results do not depend on the work-queue
     order, and agree with the one-lane kernel to rounding on cells whose
