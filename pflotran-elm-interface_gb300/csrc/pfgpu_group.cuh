@@ -22,9 +22,14 @@ enum Phase : int { NEED = 0, START = 1, ITER = 2, DONE = 3, BACK = 4 };
 // Kmin' nm | volfrac nm | rate nm | Im nm | dIm/dlnQ nm | x n |
 // pivot scales n | rhs n; the adjoint adds Tbar n | lambda n | nu.Tbar nm |
 // area gradient nm; then ints: pivot order n | remaining rows n
-__host__ __device__ inline int ws_doubles(const DevNet& net, bool adj) {
-  const int base = net.n * net.n + 7 * net.n + 2 * net.ns + 5 * net.nm;
-  return (base + (adj ? 2 * net.n + 2 * net.nm : 0) + 1) & ~1;
+// The size is padded to G (mod 16) doubles: shared memory serves a warp's
+// 8-byte accesses 16 lanes at a time, and the groups of a half-warp then
+// start G bank pairs apart, so G consecutive doubles per group (the
+// column-split rank-1 update) never collide.
+__host__ __device__ inline int ws_doubles(const DevNet& net, bool adj, int G) {
+  const int base = net.n * net.n + 7 * net.n + 2 * net.ns + 5 * net.nm + (adj ? 2 * net.n + 2 * net.nm : 0);
+  const int g = G % 16;
+  return base + ((g - base % 16) + 16) % 16;
 }
 
 __device__ __forceinline__ double dh_ln_gamma(double z, double a0, double sI, double I, const DevNet& net) {
@@ -103,7 +108,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << (gi * G));
   const int cells_per_block = (int)(blockDim.x / G);
   const int slot = tid / G;
-  const int WS = ws_doubles(net, ADJ);
+  const int WS = ws_doubles(net, ADJ, G);
   double* wsbase = reinterpret_cast<double*>(smem + ibytes + dbytes);
   double* J = wsbase + (size_t)slot * WS;
   double* pw = J + n * n;

@@ -1,0 +1,269 @@
+"""PFLOTRAN thermodynamic database (.dat) reader and the basis set-up that
+turns a chemistry block into a ReactionNetwork.
+
+Database format (DatabaseRead, src/pflotran/reaction_database.F90:26-811):
+
+    'temperature points' n  T_1 ... T_n                              (C)
+    'name' a0 Z MW                        primary species, until 'null'
+    'name' k (nu 'species')*k logK*n a0 Z MW     aqueous complexes, until 'null'
+    'name' Vm k (nu 'species')*k logK*n MW       gases, until 'null'
+    'name' Vm k (nu 'species')*k logK*n MW       minerals (Vm in cm^3/mol), until 'null'
+
+(tokens are whitespace-separated, names quoted; Fortran 'd' exponents
+accepted; a logK of 500 marks a temperature with no data).  Surface
+complexes and later sections are not read.
+
+Basis set-up (the subset of BasisInit, reaction_database.F90:812-4040, that
+this engine needs): the primary species must be basis species of the
+database (no basis swapping); water drops out of every reaction (its
+activity is one: ln a_H2O = 0 in ln Q); logK at the reference temperature
+follows ReactionInitializeLogK (reaction_aux.F90:1236-1281: the database
+column when the run is isothermal at a database temperature, else the fit);
+the five-term temperature fit follows ReactionFitLogKCoef
+(reaction_aux.F90:1159-1232: normal equations over the temperatures with
+data, solved with the Crout LU of utility.F90:597-735); Debye-Hueckel A, B,
+Bdot are interpolated linearly in the table of reaction_database.F90:931-1022.
+"""
+from __future__ import annotations
+
+import math
+import os
+import shlex
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .network import ReactionNetwork, default_options
+
+MISSING_LOGK = 500.0
+
+# Debye-Hueckel A, B, Bdot at 0, 25, 60, 100, 150, 200, 250, 300 C
+# (reaction_database.F90:931-1022; physical data)
+_DH_T = (0.0, 25.0, 60.0, 100.0, 150.0, 200.0, 250.0, 300.0)
+_DH_A = (0.4939, 0.5114, 0.5465, 0.5995, 0.6855, 0.7994, 0.9593, 1.2180)
+_DH_B = (0.3253, 0.3288, 0.3346, 0.3421, 0.3525, 0.3639, 0.3766, 0.3925)
+_DH_BDOT = (0.0374, 0.0410, 0.0440, 0.0460, 0.0470, 0.0470, 0.0340, 0.0000)
+
+
+def _num(tok: str) -> float:
+    return float(tok.lower().replace("d", "e"))
+
+
+@dataclass
+class Reaction:
+    stoich: list            # [(species, nu)], in database order, water included
+    logK: list              # one per database temperature
+    a0: float = 0.0
+    Z: float = 0.0
+    molar_vol_cm3: float = 0.0
+
+
+@dataclass
+class Database:
+    temperatures: list
+    primary: dict = field(default_factory=dict)     # name -> (a0, Z, MW)
+    secondary: dict = field(default_factory=dict)   # name -> Reaction
+    gases: dict = field(default_factory=dict)       # name -> Reaction
+    minerals: dict = field(default_factory=dict)    # name -> Reaction
+
+
+def read_database(source: str) -> Database:
+    """Parse a database from a path or from its text."""
+    text = open(source).read() if os.path.exists(source) else source
+    toks = shlex.split(text)
+    if len(toks) < 2 or toks[0] != "temperature points":
+        raise ValueError("not a PFLOTRAN database: expected 'temperature points'")
+    nt = int(_num(toks[1]))
+    temps = [_num(t) for t in toks[2:2 + nt]]
+    i = 2 + nt
+    db = Database(temperatures=temps)
+    # primary species: name a0 Z MW
+    while toks[i] != "null":
+        db.primary[toks[i]] = (_num(toks[i + 1]), _num(toks[i + 2]), _num(toks[i + 3]))
+        i += 4
+    i += 4  # the 'null' record has the same four fields
+
+    def pairs(i, k):
+        st = []
+        for _ in range(k):
+            st.append((toks[i + 1], _num(toks[i])))
+            i += 2
+        return st, i
+
+    # aqueous complexes: name k pairs logK*nt a0 Z MW
+    while True:
+        name = toks[i]
+        k = int(_num(toks[i + 1]))
+        st, i = pairs(i + 2, k)
+        logK = [_num(t) for t in toks[i:i + nt]]
+        i += nt
+        a0, Z = _num(toks[i]), _num(toks[i + 1])
+        i += 3
+        if name == "null":
+            break
+        db.secondary[name] = Reaction(st, logK, a0=a0, Z=Z)
+    # gases, then minerals: name Vm k pairs logK*nt MW
+    for table in (db.gases, db.minerals):
+        while i < len(toks):
+            name = toks[i]
+            vm = _num(toks[i + 1])
+            k = int(_num(toks[i + 2]))
+            st, i = pairs(i + 3, k)
+            logK = [_num(t) for t in toks[i:i + nt]]
+            i += nt + 1
+            if name == "null":
+                break
+            table[name] = Reaction(st, logK, molar_vol_cm3=vm)
+    return db
+
+
+def _crout_solve(a, b):
+    """Crout LU with implicit pivoting and the substitutions
+    (utility.F90:597-735) for the small normal-equation systems of the fit."""
+    n = len(b)
+    a = [list(map(float, row)) for row in a]
+    b = list(map(float, b))
+    vv = []
+    for i in range(n):
+        big = max(abs(x) for x in a[i])
+        if big == 0.0:
+            raise ZeroDivisionError("singular logK fit")
+        vv.append(1.0 / big)
+    indx = [0] * n
+    for j in range(n):
+        for i in range(j):
+            s = a[i][j]
+            for k in range(i):
+                s = s - a[i][k] * a[k][j]
+            a[i][j] = s
+        big, imax = 0.0, j
+        for i in range(j, n):
+            s = a[i][j]
+            for k in range(j):
+                s = s - a[i][k] * a[k][j]
+            a[i][j] = s
+            dum = vv[i] * abs(s)
+            if dum >= big:
+                big, imax = dum, i
+        if j != imax:
+            a[imax], a[j] = a[j], a[imax]
+            vv[imax] = vv[j]
+        indx[j] = imax
+        if a[j][j] == 0.0:
+            a[j][j] = 1.0e-20
+        if j != n - 1:
+            dum = 1.0 / a[j][j]
+            for i in range(j + 1, n):
+                a[i][j] = a[i][j] * dum
+    ii = -1
+    for i in range(n):
+        ll = indx[i]
+        s = b[ll]
+        b[ll] = b[i]
+        if ii >= 0:
+            for j in range(ii, i):
+                s = s - a[i][j] * b[j]
+        elif s != 0.0:
+            ii = i
+        b[i] = s
+    for i in range(n - 1, -1, -1):
+        s = b[i]
+        for j in range(i + 1, n):
+            s = s - a[i][j] * b[j]
+        b[i] = s / a[i][i]
+    return b
+
+
+def fit_logK_coefs(temperatures, logK):
+    """The five coefficients c of logK(T) = c1 ln T + c2 + c3 T + c4/T + c5/T^2
+    (T in K) fitted over the temperatures whose logK is not 500."""
+    rows, ys = [], []
+    for t, k in zip(temperatures, logK):
+        if abs(k - MISSING_LOGK) < 1.0e-10:
+            continue
+        tk = t + 273.15
+        rows.append((math.log(tk), 1.0, tk, 1.0 / tk, 1.0 / (tk * tk)))
+        ys.append(k)
+    rhs = [sum(r[j] * y for r, y in zip(rows, ys)) for j in range(5)]
+    a = [[sum(r[j] * r[k] for r in rows) for k in range(5)] for j in range(5)]
+    return _crout_solve(a, rhs)
+
+
+def eval_logK(coefs, t_c):
+    tk = t_c + 273.15
+    return coefs[0] * math.log(tk) + coefs[1] + coefs[2] * tk + coefs[3] / tk + coefs[4] / (tk * tk)
+
+
+def debye_huckel(t_c: float):
+    """(A, B, Bdot) at the reference temperature t_c (C)."""
+    if t_c <= 0.01:
+        return _DH_A[0], _DH_B[0], _DH_BDOT[0]
+    if t_c > 300.0:
+        return _DH_A[-1], _DH_B[-1], _DH_BDOT[-1]
+    for k in range(1, len(_DH_T)):
+        lo, hi = _DH_T[k - 1], _DH_T[k]
+        if lo < t_c <= hi:
+            w = (t_c - lo) / (hi - lo)
+            return tuple(v[k - 1] + w * (v[k] - v[k - 1]) for v in (_DH_A, _DH_B, _DH_BDOT))
+    raise AssertionError("unreachable")
+
+
+def _reference_logK(db: Database, rxn: Reaction, coefs, t_ref: float, isothermal: bool):
+    if isothermal:
+        for k, t in enumerate(db.temperatures):
+            if abs(t - t_ref) < 1.0e-10:
+                return rxn.logK[k]
+    return eval_logK(coefs, t_ref)
+
+
+def _drop_water(stoich, primary):
+    out = {}
+    for sp, nu in stoich:
+        if sp == "H2O":
+            continue
+        if sp not in primary:
+            raise KeyError("species %s is not a primary species of this network (no basis swapping)" % sp)
+        out[sp] = out.get(sp, 0.0) + nu
+    return out
+
+
+def build_network(db: Database, primary, secondary=None, minerals=None, options=None,
+                  reference_temperature: float = 25.0) -> ReactionNetwork:
+    """ReactionNetwork of `primary` (basis species of the database), the
+    complexes `secondary` (None: every complex made of the primaries and
+    water, in database order) and the kinetic minerals `minerals`, a dict
+    name -> rate parameters {rate (mol/m^2/s), [activation_energy,
+    affinity_threshold, rate_limiter, irreversible, min_scale_factor,
+    Temkin_const, affinity_power]}.  options: solver options
+    (default_options()); isothermal runs take logK at the reference
+    temperature, others the temperature fits."""
+    options = dict(options) if options is not None else default_options()
+    isothermal = bool(options.get("isothermal", 1))
+    for p in primary:
+        if p not in db.primary:
+            raise KeyError("%s is not a basis species of the database" % p)
+    pset = set(primary)
+    if secondary is None:
+        secondary = [name for name, r in db.secondary.items()
+                     if all(sp in pset or sp == "H2O" for sp, _ in r.stoich)]
+    secs = []
+    for name in secondary:
+        r = db.secondary[name]
+        coefs = fit_logK_coefs(db.temperatures, r.logK)
+        secs.append(dict(name=name, stoich=_drop_water(r.stoich, pset),
+                         logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
+                         logKcoef=coefs, Z=r.Z, a0=r.a0))
+    mins = []
+    for name, par in (minerals or {}).items():
+        r = db.minerals[name]
+        coefs = fit_logK_coefs(db.temperatures, r.logK)
+        m = dict(name=name, stoich=_drop_water(r.stoich, pset),
+                 logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
+                 logKcoef=coefs, molar_vol=r.molar_vol_cm3 * 1.0e-6)
+        m.update(par)
+        if "rate" not in m:
+            raise KeyError("mineral %s: a rate constant is required" % name)
+        mins.append(m)
+    return ReactionNetwork.build(list(primary), [db.primary[p][1] for p in primary],
+                                 [db.primary[p][0] for p in primary], secs, mins,
+                                 debye=debye_huckel(reference_temperature), options=options)

@@ -19,6 +19,8 @@ import shlex
 import sys
 
 ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                                "pflotran-elm-interface_gb300"))
 BATCH = os.path.join(ROOT, "regression_tests", "ascem", "batch")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
@@ -36,53 +38,14 @@ def fnum(s):
 
 
 def read_dat(path):
-    """Parse the PFLOTRAN .dat database format (reaction_database.F90:26)."""
-    toks = shlex.split(open(path).read())
-    i = 0
-    assert toks[i] == "temperature points"
-    ntemp = int(toks[i + 1])
-    temps = [fnum(t) for t in toks[i + 2:i + 2 + ntemp]]
-    i += 2 + ntemp
-    primary = {}
-    while toks[i] != "null":
-        primary[toks[i]] = dict(a0=fnum(toks[i + 1]), Z=fnum(toks[i + 2]))
-        i += 4
-    i += 4
-
-    def aq_record(i):  # name ns (nu sp)*ns logK*ntemp a0 Z mw
-        name = toks[i]; ns = int(fnum(toks[i + 1])); i += 2
-        st = []
-        for _ in range(ns):
-            st.append((toks[i + 1], fnum(toks[i]))); i += 2
-        logK = [fnum(t) for t in toks[i:i + ntemp]]; i += ntemp
-        rec = dict(stoich=st, logK=logK, a0=fnum(toks[i]), Z=fnum(toks[i + 1]))
-        return name, rec, i + 3
-
-    def solid_record(i):  # name molar_vol ns (nu sp)*ns logK*ntemp mw
-        name = toks[i]; mv = fnum(toks[i + 1]); ns = int(fnum(toks[i + 2])); i += 3
-        st = []
-        for _ in range(ns):
-            st.append((toks[i + 1], fnum(toks[i]))); i += 2
-        logK = [fnum(t) for t in toks[i:i + ntemp]]; i += ntemp
-        return name, dict(stoich=st, logK=logK, molar_vol_cm3=mv), i + 1
-
-    secondary = {}
-    while True:
-        name, rec, i = aq_record(i)
-        if name == "null":
-            break
-        secondary[name] = rec
-    while True:  # gases
-        name, rec, i = solid_record(i)
-        if name == "null":
-            break
-    minerals = {}
-    while True:
-        name, rec, i = solid_record(i)
-        if name == "null":
-            break
-        minerals[name] = rec
-    return temps, primary, secondary, minerals
+    """The database through the package's reader (pfgpu.database), in the
+    dictionaries this script uses."""
+    from pfgpu.database import read_database
+    db = read_database(path)
+    primary = {k: dict(a0=v[0], Z=v[1]) for k, v in db.primary.items()}
+    secondary = {k: dict(stoich=r.stoich, logK=r.logK, a0=r.a0, Z=r.Z) for k, r in db.secondary.items()}
+    minerals = {k: dict(stoich=r.stoich, logK=r.logK, molar_vol_cm3=r.molar_vol_cm3) for k, r in db.minerals.items()}
+    return db.temperatures, primary, secondary, minerals
 
 
 def block(lines, start):

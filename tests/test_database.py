@@ -1,0 +1,172 @@
+"""The .dat database reader and basis set-up (pfgpu.database).
+
+Against the reference: the known-answer fixtures (tests/golden/kat_batch.json)
+were generated from the reference's regression databases through this
+reader; where the reference tree is present (PFGPU_REFERENCE_ROOT), the
+networks built by build_network from those databases are compared with the
+fixtures' networks.  Everywhere: a synthetic database round trip, the logK
+temperature fit (ReactionFitLogKCoef), the Debye-Hueckel table, water and
+basis handling."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from pfgpu import database as dbm
+
+REF = os.environ.get("PFGPU_REFERENCE_ROOT", "/root/reference")
+BATCH = os.path.join(REF, "regression_tests", "ascem", "batch")
+
+
+def _coef_fn(c, t):
+    tk = t + 273.15
+    return c[0] * math.log(tk) + c[1] + c[2] * tk + c[3] / tk + c[4] / (tk * tk)
+
+
+def _synthetic(seed=3):
+    """A database text with 4 basis species, 5 complexes (one with water),
+    a gas and 2 minerals, logK from known five-term functions; one logK at
+    300 C marked missing (500)."""
+    rng = np.random.default_rng(seed)
+    temps = [0.0, 25.0, 60.0, 100.0, 150.0, 200.0, 250.0, 300.0]
+    prim = [("H+", 9.0, 1.0), ("Ca++", 6.0, 2.0), ("HCO3-", 4.0, -1.0), ("Mg++", 8.0, 2.0)]
+    coefs = {}
+    lines = ["'temperature points' 8 " + " ".join("%.1f" % t for t in temps)]
+    for name, a0, z in prim:
+        lines.append("'%s' %.1f %.1f 1.0" % (name, a0, z))
+    lines.append("'null' 0. 0. 0.")
+
+    def logks(name, missing=False):
+        c = [rng.uniform(-1, 1) * 1e-2, rng.uniform(-5, 5), rng.uniform(-1, 1) * 1e-3,
+             rng.uniform(-1, 1) * 1e2, rng.uniform(-1, 1) * 1e3]
+        coefs[name] = c
+        vals = [_coef_fn(c, t) for t in temps]
+        if missing:
+            vals[-1] = 500.0
+        return " ".join("%.12e" % v for v in vals)
+    secs = [("OH-", [(1.0, "H2O"), (-1.0, "H+")], -1.0), ("CO3--", [(-1.0, "H+"), (1.0, "HCO3-")], -2.0),
+            ("CaHCO3+", [(1.0, "Ca++"), (1.0, "HCO3-")], 1.0), ("MgCO3(aq)", [(-1.0, "H+"), (1.0, "Mg++"),
+                                                                          (1.0, "HCO3-")], 0.0),
+            ("NaCl(aq)", [(1.0, "Na+"), (1.0, "Cl-")], 0.0)]
+    for name, st, z in secs:
+        pairs = " ".join("%.1f '%s'" % (nu, sp) for nu, sp in st)
+        lines.append("'%s' %d %s %s 4.0 %.1f 10.0" % (name, len(st), pairs, logks(name, name == "CO3--"), z))
+    lines.append("'null' 1 0. 'null' " + " ".join(["0."] * 8) + " 0. 0. 0.")
+    lines.append("'CO2(g)' 22.4 3 -1.0 'H2O' 1.0 'H+' 1.0 'HCO3-' %s 44.0" % logks("CO2(g)"))
+    lines.append("'null' 0. 1 0. 'null' " + " ".join(["0."] * 8) + " 0.")
+    lines.append("'Calcite' 36.934 3 -1.0 'H+' 1.0 'Ca++' 1.0 'HCO3-' %s 100.0" % logks("Calcite"))
+    lines.append("'Dolomite' 64.34 5 -2.0 'H+' 1.0 'Ca++' 1.0 'Mg++' 2.0 'HCO3-' 0.0 'H2O' %s 184.4"
+                 % logks("Dolomite"))
+    lines.append("'null' 0. 1 0. 'null' " + " ".join(["0."] * 8) + " 0.")
+    return "\n".join(lines) + "\n", temps, coefs
+
+
+def test_synthetic_round_trip():
+    text, temps, coefs = _synthetic()
+    db = dbm.read_database(text)
+    assert db.temperatures == temps
+    assert list(db.primary) == ["H+", "Ca++", "HCO3-", "Mg++"]
+    assert db.primary["Ca++"][:2] == (6.0, 2.0)
+    assert list(db.secondary) == ["OH-", "CO3--", "CaHCO3+", "MgCO3(aq)", "NaCl(aq)"]
+    assert db.secondary["OH-"].stoich == [("H2O", 1.0), ("H+", -1.0)]
+    assert db.secondary["CO3--"].logK[-1] == 500.0
+    assert list(db.gases) == ["CO2(g)"]
+    assert list(db.minerals) == ["Calcite", "Dolomite"]
+    assert db.minerals["Dolomite"].molar_vol_cm3 == 64.34
+
+
+def test_logK_fit_recovers_the_function():
+    text, temps, coefs = _synthetic()
+    db = dbm.read_database(text)
+    for name in ("CaHCO3+", "Calcite"):
+        r = db.secondary.get(name) or db.minerals[name]
+        c = dbm.fit_logK_coefs(temps, r.logK)
+        for t in (5.0, 25.0, 42.0, 90.0, 280.0):
+            assert abs(dbm.eval_logK(c, t) - _coef_fn(coefs[name], t)) < 1e-7, (name, t)
+    # a missing value (500) is left out of the fit
+    c = dbm.fit_logK_coefs(temps, db.secondary["CO3--"].logK)
+    assert abs(dbm.eval_logK(c, 250.0) - _coef_fn(coefs["CO3--"], 250.0)) < 1e-6
+
+
+def test_debye_huckel_table():
+    assert dbm.debye_huckel(25.0) == (0.5114, 0.3288, 0.0410)
+    a, b, bd = dbm.debye_huckel(42.5)
+    assert a == pytest.approx(0.5 * (0.5114 + 0.5465))
+    assert b == pytest.approx(0.5 * (0.3288 + 0.3346))
+    assert bd == pytest.approx(0.5 * (0.0410 + 0.0440))
+    assert dbm.debye_huckel(0.0) == (0.4939, 0.3253, 0.0374)
+    assert dbm.debye_huckel(400.0) == (1.2180, 0.3925, 0.0)
+
+
+def test_build_network_basis_water_and_selection():
+    text, temps, coefs = _synthetic()
+    db = dbm.read_database(text)
+    net = dbm.build_network(db, ["H+", "Ca++", "HCO3-"], minerals={"Calcite": dict(rate=1e-6)})
+    # automatic selection: complexes made of the primaries (and water)
+    assert net.secondary == ["OH-", "CO3--", "CaHCO3+"]
+    oh = net.secondary.index("OH-")
+    assert net.sec_nspec[oh] == 1 and net.primary[net.sec_spec[oh, 0]] == "H+"
+    assert net.sec_stoich[oh, 0] == -1.0
+    # isothermal at a database temperature: the database column
+    assert net.sec_logK[2] == db.secondary["CaHCO3+"].logK[1]
+    assert net.mnrl_molar_vol[0] == pytest.approx(36.934e-6)
+    assert (net.debyeA, net.debyeB, net.debyeBdot) == (0.5114, 0.3288, 0.0410)
+    # non-isothermal: the fit's coefficients travel with the network
+    hot = dbm.build_network(db, ["H+", "Ca++", "HCO3-"], options=dict(isothermal=0), reference_temperature=30.0)
+    assert hot.sec_logKcoef.shape == (3, 5)
+    assert hot.sec_logK[2] == pytest.approx(_coef_fn(coefs["CaHCO3+"], 30.0), abs=1e-7)
+    # no basis swapping: a complex of a non-primary species is refused
+    with pytest.raises(KeyError):
+        dbm.build_network(db, ["H+", "Ca++", "HCO3-"], secondary=["MgCO3(aq)"])
+    with pytest.raises(KeyError):
+        dbm.build_network(db, ["H+", "Na+"])
+
+
+@pytest.mark.skipif(not os.path.isdir(BATCH), reason="reference regression databases not present")
+def test_reference_databases_build_the_fixture_networks():
+    import kat
+    from golden import make_golden
+    for name, fx in kat.KAT.items():
+        if name.startswith("_"):
+            continue
+        deck = make_golden.read_deck(os.path.join(BATCH, name + ".in"))
+        db = dbm.read_database(os.path.join(BATCH, deck["database"].lstrip("./")))
+        mins = {m["name"]: dict(rate=m["rate"]) for m in fx["minerals"]}
+        net = dbm.build_network(db, fx["primary"], secondary=[s["name"] for s in fx["secondaries"]],
+                                minerals=mins)
+        assert list(net.pri_Z) == fx["pri_Z"] and list(net.pri_a0) == fx["pri_a0"]
+        for i, s in enumerate(fx["secondaries"]):
+            assert net.sec_logK[i] == s["logK"] and net.sec_Z[i] == s["Z"] and net.sec_a0[i] == s["a0"]
+            got = {net.primary[net.sec_spec[i, k]]: net.sec_stoich[i, k] for k in range(net.sec_nspec[i])}
+            assert got == s["stoich"], (name, s["name"])
+        for m, mx in enumerate(fx["minerals"]):
+            assert net.mnrl_logK[m] == mx["logK"] and net.mnrl_molar_vol[m] == mx["molar_vol"]
+
+
+@pytest.mark.gpu
+def test_database_network_runs_on_the_gpu(oracle):
+    """A network read from a database (non-isothermal, two kinetic minerals)
+    goes through the C ABI: the GPU step agrees with the oracle."""
+    torch = pytest.importorskip("torch")
+    import cases
+    from pfgpu import generate
+    from pfgpu.engine import ReactionEngine
+    from pfgpu.network import default_options
+    text, temps, coefs = _synthetic()
+    db = dbm.read_database(text)
+    net = dbm.build_network(db, ["H+", "Ca++", "HCO3-", "Mg++"],
+                            minerals={"Calcite": dict(rate=1e-7), "Dolomite": dict(rate=1e-9)},
+                            options=default_options(isothermal=0))
+    st, ct, cc = generate.random_cells(net, 500, seed=77)
+    st, nfail = cases.prepare(oracle, net, st, ct, cc)
+    assert st.ncells > 450
+    ref = st.copy()
+    oracle.rstep(net, ref, 86400.0, nthreads=8)
+    dev = st.to("cuda")
+    ReactionEngine(net).rstep(dev, 86400.0)
+    got = dev.numpy()
+    same = (got.a["newton_its"] == ref.a["newton_its"]) & (ref.a["status"] == 0)
+    assert same.mean() > 0.9
+    err = np.max(np.abs(got.a["pri_molal"][:, same] - ref.a["pri_molal"][:, same]) / ref.a["pri_molal"][:, same])
+    assert err < 1e-10, err
