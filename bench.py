@@ -448,6 +448,67 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
+def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, rtol=1e-10):
+    """The transport half of the operator-split step (pf_transport_step) on
+    the same grid as the global-implicit measurement: every component's
+    totals transported over dt = 1 day by Jacobi-BiCGStab to rtol.
+    Roofline: HBM; algorithmic bytes per iteration = (17 + 19 n) doubles per
+    cell (the 7 stencil coefficients and the diagonal read by each of the
+    two stencil products, the n-vectors p, r0, r, s, t, v, x read and
+    written once by the kernels that use them), plus the set-up."""
+    import numpy as np
+    import torch
+
+    from pfgpu.girt import StructuredGrid
+    from pfgpu.network import CellState
+    from pfgpu.transport import OSTransport
+    N = nx * ny * nz
+    idx = torch.arange(N, device=dev.a["porosity"].device) % dev.ncells
+    src = dev.subset(idx)
+    rng = np.random.default_rng(seed)
+
+    def q(shape):
+        return rng.uniform(1e-7, 1e-5, shape) * rng.choice([-1.0, 1.0], shape)
+    grid = StructuredGrid(nx, ny, nz, 1.0, 1.0, 1.0, q((nz, ny, nx - 1)), q((nz, ny - 1, nx)), q((nz - 1, ny, nx)),
+                          diffusion=1e-9, tortuosity=1.0, dispersivity=0.0)
+    n = net.ncomp
+    tr = OSTransport(grid, n)
+    st = CellState.__new__(CellState)
+    st.net, st.ncells = net, N
+    st.a = {k: src.a[k] for k in ("porosity", "saturation", "volume")}
+    t0 = src.a["total"].clone()
+    st.a["total"] = t0.clone()
+    dt = 86400.0
+    for _ in range(warmup):
+        st.a["total"].copy_(t0)
+        stats = tr.step(st, dt, rtol=rtol)
+    torch.cuda.synchronize()
+    ms, its = [], []
+    for _ in range(steps):
+        st.a["total"].copy_(t0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        stats = tr.step(st, dt, rtol=rtol)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        its.append(stats["iterations"])
+    t = float(np.mean(ms))
+    it = float(np.mean(its))
+    alg = 8.0 * N * ((17 + 19 * n) * it + (16 + 3 * n))
+    gbs = alg / (t * 1e-3) / 1e9
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except Exception:
+        pass
+    return {"grid": "%dx%dx%d" % (nx, ny, nz), "cells": N, "ncomp": n, "ms": t, "iterations": it,
+            "rel_residual": stats["max_rel_residual"], "rtol": rtol,
+            "cells_per_s": N / (t * 1e-3), "algorithmic_bytes": alg, "achieved_gbs": gbs, "peak_gbs": peak,
+            "hbm_frac": gbs / peak if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+
+
 def run_reference(args):
     import numpy as np  # noqa: F401
     rank = int(os.environ.get("RANK", "0"))
@@ -675,6 +736,13 @@ def main():
         girt = girt_measure(net, eng, dev, max(3, args.steps), max(3, args.warmup), cpu=(rank == 0 and not args.no_cpu))
         log("girt:", json.dumps(girt))
 
+    transport = None
+    if not args.no_girt and args.config == "c2":
+        for k in pristine:
+            dev.a[k].copy_(pristine[k])
+        transport = transport_measure(net, dev, max(3, args.steps), max(2, min(args.warmup, 3)))
+        log("transport:", json.dumps(transport))
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         host = dev.numpy()
@@ -702,6 +770,7 @@ def main():
                                   "kernel_ms": float(np.mean(nat_kern))},
                 "speedup_vs_plain_gpu": value / plain_value,
                 "adjoint": adjoint, "girt_assembly": girt, "constraint_equilibration": constraint,
+                "osrt_transport": transport,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(),
                 # per step: the setup pre-pass and the persistent kernel

@@ -351,6 +351,53 @@ int32_t pf_girt_pattern(int32_t nx, int32_t ny, int32_t nz, int32_t* rowptr, int
 int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtArgs* args,
                          void* stream);
 
+/* ------------------------------------------------- operator-split transport */
+/*
+ * The transport half of an operator-split step on a structured grid
+ * nx*ny*nz (cell index i + nx*(j + ny*k)), zero-flux outer boundaries, no
+ * sources: replaces the transport solve of PMCSubsurfaceOSRTStepDT
+ * (src/pflotran/pmc_subsurface_osrt.F90:259-330) -- the fixed accumulation
+ * psv*T_k, the matrix of RTCalculateTransportMatrix
+ * (reactive_transport.F90:1469-1703) with TFluxCoef (transport.F90:495-565)
+ * and the harmonic-mean dispersion of TDispersion, the right-hand side
+ * psv*T_k/dt of RTCalculateRHS_t1, and one linear solve per component
+ * (all components share the matrix).  Solved on the device by Jacobi-
+ * preconditioned BiCGStab, all components at once, to ||r|| <= rtol ||b||.
+ * No counterpart in the reference for the solver choice (PETSc KSP there).
+ */
+typedef struct PfTransportArgs {
+  int32_t nx, ny, nz, ncomp;
+  double dx, dy, dz;                 /* m */
+  const double* qx;                  /* [nz][ny][nx-1] Darcy flux, m/s, + from i to i+1 */
+  const double* qy;                  /* [nz][ny-1][nx] */
+  const double* qz;                  /* [nz-1][ny][nx] */
+  double diffusion_coefficient;      /* m^2/s */
+  double tortuosity;
+  double dispersivity;               /* m */
+  const double* porosity;            /* [ncells] */
+  const double* saturation;          /* [ncells] */
+  const double* volume;              /* [ncells] m^3 */
+  double dt;                         /* s (option%tran_dt) */
+  double* total;                     /* [ncomp][ncells] mol/L: in T_k, out T_k+1 */
+  double rtol;                       /* relative residual tolerance */
+  int32_t max_iterations;
+} PfTransportArgs;
+
+typedef struct PfTransportStats {
+  int32_t iterations;                /* BiCGStab iterations (all components in step) */
+  int32_t converged;                 /* 1 when every component met rtol */
+  double max_rel_residual;           /* max over components of ||r|| / ||b|| */
+} PfTransportStats;
+
+typedef struct PfTransport PfTransport;  /* opaque: device work space of one grid */
+
+int32_t pf_transport_create(int32_t nx, int32_t ny, int32_t nz, int32_t ncomp, PfTransport** out);
+int32_t pf_transport_destroy(PfTransport* t);
+/* PF_OK, PF_CELL_FAILURES (not converged within max_iterations; totals hold
+ * the last iterate) or PF_ERR_*. */
+int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* args, void* stream,
+                          PfTransportStats* stats);
+
 /* ----------------------------------------------------------- constraints */
 /* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */
 enum {

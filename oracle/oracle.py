@@ -128,6 +128,28 @@ class Oracle:
             raise RuntimeError("oracle_girt_assemble: %d" % rc)
         return r, vals
 
+    def transport_matrix(self, grid, porosity, saturation, volume, dt, rowptr, colidx):
+        """Values of the operator-split transport matrix (7-point pattern,
+        block size 1) of a structured grid, as RTCalculateTransportMatrix
+        assembles it."""
+        f = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+        gi = np.array([grid["nx"], grid["ny"], grid["nz"]], np.int32)
+        gd = f([grid["dx"], grid["dy"], grid["dz"], grid["diffusion"], grid["tortuosity"], grid["dispersivity"]])
+        q = [f(grid[k]) if np.size(grid[k]) else np.zeros(1) for k in ("qx", "qy", "qz")]
+        por, sat, vol = f(porosity), f(saturation), f(volume)
+        rp, ci = np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colidx, np.int32)
+        vals = np.zeros(int(rp[-1]))
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        P = lambda a: a.ctypes.data_as(dp)  # noqa: E731
+        fn = self.lib.oracle_transport_matrix
+        fn.argtypes = [ip, dp, dp, dp, dp, dp, dp, dp, C.c_double, ip, ip, dp]
+        fn.restype = C.c_int
+        rc = fn(gi.ctypes.data_as(ip), P(gd), P(q[0]), P(q[1]), P(q[2]), P(por), P(sat), P(vol), float(dt),
+                rp.ctypes.data_as(ip), ci.ctypes.data_as(ip), P(vals))
+        if rc:
+            raise RuntimeError("oracle_transport_matrix: %d" % rc)
+        return vals
+
     def count_rstep(self, net, state, dt):
         """RStep of every cell with counted arithmetic (single thread; the
         state is advanced).  Returns per-cell (flops, transcendental calls,

@@ -255,4 +255,27 @@ int oracle_girt_assemble(const PfNetworkDesc* d, const PfCellState* s, const int
   return PF_OK;
 }
 
+// Operator-split transport matrix on a structured grid (see
+// transport_matrix); grid_i = {nx, ny, nz}, grid_d = {dx, dy, dz, D_m,
+// tortuosity, dispersivity}; porosity/saturation/volume per cell.
+int oracle_transport_matrix(const int32_t* grid_i, const double* grid_d, const double* qx, const double* qy,
+                            const double* qz, const double* porosity, const double* saturation,
+                            const double* volume, double dt, const int32_t* rowptr, const int32_t* colidx,
+                            double* values) {
+  GirtGrid g{grid_i[0], grid_i[1], grid_i[2], grid_d[0], grid_d[1], grid_d[2], qx, qy, qz,
+             grid_d[3], grid_d[4], grid_d[5]};
+  const int64_t N = (int64_t)g.nx * g.ny * g.nz;
+  std::vector<Cell> cells(N);
+  for (int64_t i = 0; i < N; ++i) {
+    cells[i].porosity = porosity[i];
+    cells[i].sat = saturation[i];
+    cells[i].volume = volume[i];
+  }
+  std::vector<int> rp(N + 1), ci(rowptr[N]);
+  for (int64_t i = 0; i <= N; ++i) rp[i] = rowptr[i];
+  for (int64_t b = 0; b < rowptr[N]; ++b) ci[b] = colidx[b];
+  transport_matrix(cells.data(), g, dt, rp.data(), ci.data(), values);
+  return PF_OK;
+}
+
 }  // extern "C"

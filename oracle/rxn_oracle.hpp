@@ -1000,4 +1000,60 @@ inline void girt_assemble(const Net& net, Cell* cells, const GirtGrid& g, const 
   }
 }
 
+// The scalar operator-split transport matrix of RTCalculateTransportMatrix
+// (reactive_transport.F90:1469-1703) on a structured grid: per internal
+// connection (x, then y, then z; k, j, i loops) TFluxCoef's T_up, T_dn
+// (transport.F90:495-565; flux only when both saturations reach
+// rt_min_saturation) added at (up,up) += T_up, (up,dn) += T_dn, (dn,dn) -= T_dn,
+// (dn,up) -= T_up; then psv/dt on the diagonal of every cell.  values follow
+// the 7-point pattern rowptr/colidx (block size 1).  The right-hand side of
+// the operator-split solve is psv*T_k/dt (RTCalculateRHS_t1 with no
+// boundary or source terms).
+inline void transport_matrix(const Cell* cells, const GirtGrid& g, double dt, const int* rowptr,
+                             const int* colidx, double* values) {
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const long long N = (long long)nx * ny * nz;
+  auto idx = [&](int i, int j, int k) { return (long long)i + (long long)nx * (j + (long long)ny * k); };
+  for (long long e = 0; e < rowptr[N]; ++e) values[e] = 0.0;
+  auto at = [&](long long row, long long col) -> double& {
+    for (int b = rowptr[row]; b < rowptr[row + 1]; ++b)
+      if (colidx[b] == col) return values[b];
+    return values[rowptr[row]];  // unreachable for the 7-point pattern
+  };
+  auto connection = [&](long long up, long long dn, double q, double area, double dist) {
+    const Cell& cu = cells[up];
+    const Cell& cd = cells[dn];
+    double T_up = 0.0, T_dn = 0.0;
+    if (!(cd.sat < rt_min_saturation) && !(cu.sat < rt_min_saturation)) {
+      double tran = girt_tran_coef(cu, cd, q, dist, 0.5, g);
+      double coef_up, coef_dn;
+      if (q > 0.0) { coef_up = tran + q; coef_dn = -tran; }
+      else { coef_up = tran; coef_dn = -tran + q; }
+      T_up = coef_up * area * 1000.0;
+      T_dn = coef_dn * area * 1000.0;
+    }
+    at(up, up) = at(up, up) + T_up;
+    at(up, dn) = at(up, dn) + T_dn;
+    at(dn, dn) = at(dn, dn) + (-T_dn);
+    at(dn, up) = at(dn, up) + (-T_up);
+  };
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx - 1; ++i)
+        connection(idx(i, j, k), idx(i + 1, j, k), g.qx[((long long)k * ny + j) * (nx - 1) + i], g.dy * g.dz, g.dx);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny - 1; ++j)
+      for (int i = 0; i < nx; ++i)
+        connection(idx(i, j, k), idx(i, j + 1, k), g.qy[((long long)k * (ny - 1) + j) * nx + i], g.dx * g.dz, g.dy);
+  for (int k = 0; k < nz - 1; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        connection(idx(i, j, k), idx(i, j, k + 1), g.qz[((long long)k * ny + j) * nx + i], g.dx * g.dy, g.dz);
+  for (long long c = 0; c < N; ++c) {
+    const Cell& cl = cells[c];
+    const double coef = cl.porosity * cl.sat * 1000.0 * cl.volume / dt;
+    at(c, c) = at(c, c) + coef;
+  }
+}
+
 }  // namespace oracle

@@ -124,6 +124,21 @@ class PfGirtArgs(C.Structure):
     ]
 
 
+class PfTransportArgs(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("ncomp", C.c_int32),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+        ("qx", _dp), ("qy", _dp), ("qz", _dp),
+        ("diffusion_coefficient", C.c_double), ("tortuosity", C.c_double), ("dispersivity", C.c_double),
+        ("porosity", _dp), ("saturation", _dp), ("volume", _dp),
+        ("dt", C.c_double), ("total", _dp), ("rtol", C.c_double), ("max_iterations", C.c_int32),
+    ]
+
+
+class PfTransportStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("max_rel_residual", C.c_double)]
+
+
 class PfLaunchConfig(C.Structure):
     _fields_ = [
         ("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
@@ -149,6 +164,9 @@ SIGNATURES = {
     "pf_adjoint": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.POINTER(PfAdjointArgs), _P]),
     "pf_network_shift_parameters": (C.c_int32, [_P, _dp, _dp, _dp]),
     "pf_girt_pattern": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, _ip, _ip]),
+    "pf_transport_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_P)]),
+    "pf_transport_destroy": (C.c_int32, [_P]),
+    "pf_transport_step": (C.c_int32, [_P, C.POINTER(PfTransportArgs), _P, C.POINTER(PfTransportStats)]),
     "pf_girt_assemble": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(PfGirtArgs), _P]),
     "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
