@@ -144,6 +144,34 @@ def test_reference_databases_build_the_fixture_networks():
             assert net.mnrl_logK[m] == mx["logK"] and net.mnrl_molar_vol[m] == mx["molar_vol"]
 
 
+def _carbonate_like():
+    """A small carbonate-system database in the .dat format: logK near
+    typical 25 C values, varying linearly with temperature (values chosen
+    for this test, not taken from any database)."""
+    temps = [0.0, 25.0, 60.0, 100.0, 150.0, 200.0, 250.0, 300.0]
+
+    def col(k25, slope):
+        return " ".join("%.6f" % (k25 + slope * (t - 25.0)) for t in temps)
+    lines = ["'temperature points' 8 " + " ".join("%.1f" % t for t in temps),
+             "'H+' 9.0 1.0 1.0", "'Ca++' 6.0 2.0 40.0", "'HCO3-' 4.0 -1.0 61.0", "'Mg++' 8.0 2.0 24.3",
+             "'null' 0. 0. 0."]
+    secs = [("OH-", "2 1.0 'H2O' -1.0 'H+'", col(14.0, -0.03), 3.5, -1.0),
+            ("CO3--", "2 -1.0 'H+' 1.0 'HCO3-'", col(10.3, -0.01), 4.5, -2.0),
+            ("CO2(aq)", "3 -1.0 'H2O' 1.0 'H+' 1.0 'HCO3-'", col(-6.3, 0.005), 3.0, 0.0),
+            ("CaHCO3+", "2 1.0 'Ca++' 1.0 'HCO3-'", col(-1.0, -0.005), 4.0, 1.0),
+            ("CaCO3(aq)", "3 -1.0 'H+' 1.0 'Ca++' 1.0 'HCO3-'", col(7.0, -0.02), 3.0, 0.0),
+            ("MgHCO3+", "2 1.0 'Mg++' 1.0 'HCO3-'", col(-1.0, -0.004), 4.0, 1.0)]
+    for name, st, ks, a0, z in secs:
+        lines.append("'%s' %s %s %.1f %.1f 1.0" % (name, st, ks, a0, z))
+    lines.append("'null' 1 0. 'null' " + " ".join(["0."] * 8) + " 0. 0. 0.")
+    lines.append("'null' 0. 1 0. 'null' " + " ".join(["0."] * 8) + " 0.")
+    lines.append("'Calcite' 36.9 3 -1.0 'H+' 1.0 'Ca++' 1.0 'HCO3-' %s 100.0" % col(1.85, -0.012))
+    lines.append("'Dolomite' 64.3 5 -2.0 'H+' 1.0 'Ca++' 1.0 'Mg++' 2.0 'HCO3-' 0.0 'H2O' %s 184.0"
+                 % col(2.5, -0.02))
+    lines.append("'null' 0. 1 0. 'null' " + " ".join(["0."] * 8) + " 0.")
+    return "\n".join(lines) + "\n"
+
+
 @pytest.mark.gpu
 def test_database_network_runs_on_the_gpu(oracle):
     """A network read from a database (non-isothermal, two kinetic minerals)
@@ -153,11 +181,11 @@ def test_database_network_runs_on_the_gpu(oracle):
     from pfgpu import generate
     from pfgpu.engine import ReactionEngine
     from pfgpu.network import default_options
-    text, temps, coefs = _synthetic()
-    db = dbm.read_database(text)
+    db = dbm.read_database(_carbonate_like())
     net = dbm.build_network(db, ["H+", "Ca++", "HCO3-", "Mg++"],
                             minerals={"Calcite": dict(rate=1e-7), "Dolomite": dict(rate=1e-9)},
                             options=default_options(isothermal=0))
+    assert net.sec_logKcoef is not None and net.nsec == 6
     st, ct, cc = generate.random_cells(net, 500, seed=77)
     st, nfail = cases.prepare(oracle, net, st, ct, cc)
     assert st.ncells > 450

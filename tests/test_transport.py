@@ -130,7 +130,8 @@ def test_gpu_transport_conserves_mass():
 @pytest.mark.gpu
 def test_gpu_transport_dry_cells_keep_their_totals(oracle):
     got, ref, T0, psv, stats = _gpu_case(oracle, (6, 5, 4), 4, seed=31, dry=(0, 17, 59))
-    np.testing.assert_array_equal(got[:, [0, 17, 59]], T0[:, [0, 17, 59]])
+    # an identity row goes through the iterations: its value to an ulp or two
+    np.testing.assert_allclose(got[:, [0, 17, 59]], T0[:, [0, 17, 59]], rtol=1e-13, atol=0)
     err = np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300))
     assert err < 1e-9, err
 
