@@ -451,11 +451,18 @@ def run_c3(args):
 def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, rtol=1e-10):
     """The transport half of the operator-split step (pf_transport_step) on
     the same grid as the global-implicit measurement: every component's
-    totals transported over dt = 1 day by Jacobi-BiCGStab to rtol.
-    Roofline: HBM; algorithmic bytes per iteration = (17 + 19 n) doubles per
-    cell (the 7 stencil coefficients and the diagonal read by each of the
-    two stencil products, the n-vectors p, r0, r, s, t, v, x read and
-    written once by the kernels that use them), plus the set-up."""
+    totals transported over dt = 1 day to rtol by mixed-precision iterative
+    refinement (FP32 Jacobi-BiCGStab corrections, FP64 residuals).
+    Roofline: HBM; algorithmic bytes, per cell, with n components:
+      inner FP32 iteration   76 n + 48  (the n-vectors read and written once
+                             by the five kernels that use them: 19 floats;
+                             the six scaled coefficients read by each of the
+                             two stencil products)
+      FP64 residual          24 n + 80  (x, T_k in, r out; 7 coefficients,
+                             porosity, saturation, volume)
+      refinement update      44 n + 8   (scaled start of the inner solve,
+                             x += D^-1 y)
+      set-up and copies      32 n + 200"""
     import numpy as np
     import torch
 
@@ -483,7 +490,7 @@ def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, r
         st.a["total"].copy_(t0)
         stats = tr.step(st, dt, rtol=rtol)
     torch.cuda.synchronize()
-    ms, its = [], []
+    ms, its, refs = [], [], []
     for _ in range(steps):
         st.a["total"].copy_(t0)
         torch.cuda.synchronize()
@@ -494,16 +501,18 @@ def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, r
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
         its.append(stats["iterations"])
+        refs.append(stats["refinements"])
     t = float(np.mean(ms))
     it = float(np.mean(its))
-    alg = 8.0 * N * ((17 + 19 * n) * it + (16 + 3 * n))
+    ref = float(np.mean(refs))
+    alg = float(N) * ((76 * n + 48) * it + (24 * n + 80) * (ref + 1) + (44 * n + 8) * ref + 32 * n + 200)
     gbs = alg / (t * 1e-3) / 1e9
     peak = None
     try:
         peak = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except Exception:
         pass
-    return {"grid": "%dx%dx%d" % (nx, ny, nz), "cells": N, "ncomp": n, "ms": t, "iterations": it,
+    return {"grid": "%dx%dx%d" % (nx, ny, nz), "cells": N, "ncomp": n, "ms": t, "iterations": it, "refinements": ref,
             "rel_residual": stats["max_rel_residual"], "rtol": rtol,
             "cells_per_s": N / (t * 1e-3), "algorithmic_bytes": alg, "achieved_gbs": gbs, "peak_gbs": peak,
             "hbm_frac": gbs / peak if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
@@ -596,13 +605,18 @@ def main():
     log("state built: %d cells in %.1f s" % (ncells, time.perf_counter() - t_build))
     if args.config == "c5":
         nx, ny, nz = (int(v) for v in args.grid.split("x"))
-        gm = girt_measure(net, eng, dev, args.steps, args.warmup, nx, ny, nz, cpu=not args.no_cpu)
+        gm = None if args.no_girt else girt_measure(net, eng, dev, args.steps, args.warmup, nx, ny, nz,
+                                                    cpu=not args.no_cpu)
+        tm = transport_measure(net, dev, args.steps, max(2, min(args.warmup, 3)), nx, ny, nz)
+        if gm is None:
+            gm = {"cells_per_s": float("nan"), "ms": float("nan")}
         if rank == 0:
             print(json.dumps({"metric": "global-implicit residual + SeqBAIJ Jacobian assemblies (cells/s)",
                               "value": gm["cells_per_s"] * world, "unit": "cells/s", "n_gpus": world,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": gm["ms"],
                               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                               "data": "synthetic", "config": {"workload": cfg["workload"]}, "girt_assembly": gm,
+                              "osrt_transport": tm,
                               "gpu_launches": 2 * args.steps}), flush=True)
         return
     pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}

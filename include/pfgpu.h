@@ -361,9 +361,11 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
  * (reactive_transport.F90:1469-1703) with TFluxCoef (transport.F90:495-565)
  * and the harmonic-mean dispersion of TDispersion, the right-hand side
  * psv*T_k/dt of RTCalculateRHS_t1, and one linear solve per component
- * (all components share the matrix).  Solved on the device by Jacobi-
- * preconditioned BiCGStab, all components at once, to ||r|| <= rtol ||b||.
- * No counterpart in the reference for the solver choice (PETSc KSP there).
+ * (all components share the matrix).  Solved on the device, all components
+ * at once, by mixed-precision iterative refinement (FP64 residual and
+ * update, FP32 Jacobi-preconditioned BiCGStab corrections) from T_k to
+ * ||b - A x|| <= rtol ||b|| in FP64.  No counterpart in the reference for
+ * the solver choice (PETSc KSP there).
  */
 typedef struct PfTransportArgs {
   int32_t nx, ny, nz, ncomp;
@@ -384,9 +386,11 @@ typedef struct PfTransportArgs {
 } PfTransportArgs;
 
 typedef struct PfTransportStats {
-  int32_t iterations;                /* BiCGStab iterations (all components in step) */
+  int32_t iterations;                /* inner (FP32) BiCGStab iterations, all components in step */
   int32_t converged;                 /* 1 when every component met rtol */
-  double max_rel_residual;           /* max over components of ||r|| / ||b|| */
+  double max_rel_residual;           /* max over components of the FP64 ||b - A x|| / ||b|| */
+  int32_t refinements;               /* FP64 refinement cycles (residual, inner solve, update) */
+  int32_t reserved;
 } PfTransportStats;
 
 typedef struct PfTransport PfTransport;  /* opaque: device work space of one grid */

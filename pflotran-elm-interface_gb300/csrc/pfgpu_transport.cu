@@ -11,15 +11,22 @@
 // source terms), and one linear solve per component (the reference's
 // KSPSolve loop over idof), all components sharing the matrix.
 //
-// GPU form: the matrix is never assembled.  A coefficient pass stores per
+// GPU form.  The matrix is never assembled: a coefficient pass stores per
 // cell the diagonal and the six face coefficients (the same harmonic-mean
-// dispersion and upwinding as the global-implicit assembly); every component
-// is then solved at once by Jacobi-preconditioned BiCGStab, the n systems
-// advancing in lock step with their own scalars (kept on the device) and
-// frozen one by one as they converge.  One iteration is two 7-point stencil
-// products and a few vector updates over n x ncells doubles: HBM-bound.
-// Dot products are two-stage (per-block partials, then a fixed-order sum), so
-// results do not depend on scheduling.
+// dispersion and upwinding as the global-implicit assembly).  On GB300 the
+// FP64 pipe, not HBM, bounds a Krylov solve (a 7-point product is ~9 FP64
+// operations per 24 bytes; GB300 delivers one FP64 operation per ~13 bytes of
+// HBM bandwidth), so the solve is mixed-precision iterative refinement
+// (Wilkinson's, with a Krylov inner solver as in GMRES-IR):
+//   r = b - A x                      FP64, all components
+//   solve (A D^-1) y = r to ~1e-5    FP32 Jacobi-right-preconditioned
+//                                    BiCGStab, all components in lock step
+//   x += D^-1 y                      FP64
+// until ||b - A x|| <= rtol ||b|| in FP64 for every component; x starts at
+// T_k.  The FP32 inner iterations run at the FP32 rate on half the bytes;
+// the answer is the FP64 one.  Dot products are two-stage (per-block
+// partials, then a fixed-order sum in FP64), so results do not depend on
+// scheduling.
 #include <cmath>
 #include <new>
 
@@ -30,15 +37,35 @@ namespace pfgpu {
 namespace tr {
 
 constexpr int TPB = 256;
-constexpr int RED_BLOCKS = 304;  // 2 x 152 SMs worth of partial sums per dot product
+constexpr int RED_BLOCKS = 304;  // at most this many blocks (partial sums) per component (chunk)
+constexpr int SPMV_CELLS = 2;    // cells per thread and pass in the stencil products
+constexpr int VEC_PAD = 64;      // floats added to each vector's stride (not a power of two)
+constexpr int CH = 4;            // components per stencil pass
+constexpr double INNER_RTOL = 3.0e-6;  // inner reduction per cycle (floor)
+constexpr double INNER_SAFETY = 0.3;    // last cycle: solve to 0.3 rtol ||b|| / ||r||
+constexpr int INNER_MAX = 60;    // inner iterations per refinement cycle
+constexpr int OUTER_MAX = 30;
 
 struct Grid {
   int nx, ny, nz;
   long long N, nxy;
+  long long Np;  // stride of the solver's own vectors: N rounded up to 64, plus padding
 };
 
-// coefficient layout [7][N]: 0 diag, 1 x-, 2 x+, 3 y-, 4 y+, 5 z-, 6 z+
-// (off-diagonals are the coefficient of the neighbour's value in this row)
+// per-component scalars, one device array S[field][c]
+enum Scalar { RHO = 0, ALPHA, OMEGA, BETA, BNORM2, RNORM2, ACTIVE, ORES2, RHS2, RSCALE, ITOL2, NSCALAR };
+
+__device__ __forceinline__ void cell_ijk(const Grid& g, long long X, int& i, int& j, int& k) {
+  const unsigned ux = (unsigned)X, unx = (unsigned)g.nx, uny = (unsigned)g.ny;
+  const unsigned row = ux / unx;
+  i = (int)(ux - row * unx);
+  j = (int)(row % uny);
+  k = (int)(row / uny);
+}
+
+// A[8][N] FP64: 0 diag, 1 x-, 2 x+, 3 y-, 4 y+, 5 z-, 6 z+ (the coefficient of
+// the neighbour's value in this row; 0 where there is none), 7 the right-hand
+// side's scale (b = A[7] T_k)
 __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const double* __restrict__ qx,
                             const double* __restrict__ qy, const double* __restrict__ qz, double diffusion,
                             double tortuosity, double dispersivity, const double* __restrict__ por,
@@ -46,7 +73,8 @@ __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const doubl
                             double* __restrict__ A, double* __restrict__ inv_diag) {
   const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (X >= g.N) return;
-  const int i = (int)(X % g.nx), j = (int)((X / g.nx) % g.ny), k = (int)(X / g.nxy);
+  int i, j, k;
+  cell_ijk(g, X, i, j, k);
   const double psv = por[X] * sat[X] * 1000.0 * vol[X];
   double diag = 0.0, off[6] = {0, 0, 0, 0, 0, 0};
   // connections in the reference's order (x, y, z); this cell is the
@@ -57,8 +85,8 @@ __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const doubl
     const int pos = axis == 0 ? i : (axis == 1 ? j : k);
     const int lim = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
     if (plus ? !(pos < lim - 1) : !(pos > 0)) continue;
-    const long long s = axis == 0 ? 1 : (axis == 1 ? (long long)g.nx : g.nxy);
-    const long long other = plus ? X + s : X - s;
+    const long long st = axis == 0 ? 1 : (axis == 1 ? (long long)g.nx : g.nxy);
+    const long long other = plus ? X + st : X - st;
     const int face = plus ? pos : pos - 1;
     double qf, area, dist;
     if (axis == 0) {
@@ -96,41 +124,51 @@ __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const doubl
       off[q] = -cup;
     }
   }
-  diag = diag + psv / dt;
+  const double storage = psv / dt;
+  diag = diag + storage;
   // a cell with neither storage nor connections (dry: saturation below
   // rt_min_saturation) has an empty row; it becomes an identity row whose
   // right-hand side is its own total, so the cell keeps its totals
-  if (diag == 0.0) diag = 1.0;
+  double bscale = storage;  // b = bscale * T_k
+  if (diag == 0.0) {
+    diag = 1.0;
+    bscale = 1.0;
+  }
   A[X] = diag;
 #pragma unroll
   for (int q = 0; q < 6; ++q) A[(size_t)(q + 1) * g.N + X] = off[q];
+  A[(size_t)7 * g.N + X] = bscale;
   inv_diag[X] = 1.0 / diag;
 }
 
-// (A invD x) at cell X: the 7-point product of the right-preconditioned operator
-__device__ __forceinline__ double stencil(const Grid& g, const double* __restrict__ A, const double* __restrict__ invD,
-                                          const double* __restrict__ x, long long X) {
-  const int i = (int)(X % g.nx), j = (int)((X / g.nx) % g.ny), k = (int)(X / g.nxy);
-  double v = A[X] * (invD[X] * x[X]);
-  if (i > 0) v = fma(A[g.N + X], invD[X - 1] * x[X - 1], v);
-  if (i < g.nx - 1) v = fma(A[2 * g.N + X], invD[X + 1] * x[X + 1], v);
-  if (j > 0) v = fma(A[3 * g.N + X], invD[X - g.nx] * x[X - g.nx], v);
-  if (j < g.ny - 1) v = fma(A[4 * g.N + X], invD[X + g.nx] * x[X + g.nx], v);
-  if (k > 0) v = fma(A[5 * g.N + X], invD[X - g.nxy] * x[X - g.nxy], v);
-  if (k < g.nz - 1) v = fma(A[6 * g.N + X], invD[X + g.nxy] * x[X + g.nxy], v);
-  return v;
+// Ah[6][N] FP32: the off-diagonals of A D^-1 (column q scaled by the
+// neighbour's 1/diag); its diagonal is 1
+__global__ void scale_kernel(Grid g, const double* __restrict__ A, const double* __restrict__ invD,
+                             float* __restrict__ Ah) {
+  const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= g.N) return;
+  int i, j, k;
+  cell_ijk(g, X, i, j, k);
+  const long long step[6] = {-1, 1, -(long long)g.nx, (long long)g.nx, -g.nxy, g.nxy};
+  const bool has[6] = {i > 0, i < g.nx - 1, j > 0, j < g.ny - 1, k > 0, k < g.nz - 1};
+#pragma unroll
+  for (int q = 0; q < 6; ++q)
+    Ah[(size_t)q * g.N + X] = has[q] ? (float)(A[(size_t)(q + 1) * g.N + X] * invD[X + step[q]]) : 0.0f;
 }
 
-template <int NW>
-__device__ __forceinline__ void block_partials(double (&v)[NW], double* __restrict__ partials, int c, int ncomp) {
-  // block-wide sums of NW values, written to partials[(w*ncomp + c)*gridDim + block]
+template <int NW, class T>
+__device__ __forceinline__ void block_partials(T (&v)[NW], double* __restrict__ partials, int c, int ncomp) {
+  // block-wide sums of NW values (accumulated and summed over the warp in
+  // T, the warps' sums added in FP64), written to
+  // partials[(w*ncomp + c)*gridDim + block].  FP32 shuffles for the inner
+  // solve's dot products: FP64 arithmetic runs at 1/64 of the FP32 rate
   __shared__ double sh[NW][TPB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int w = 0; w < NW; ++w) {
-    double s = v[w];
+    T s = v[w];
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    if (lane == 0) sh[w][wid] = s;
+    if (lane == 0) sh[w][wid] = (double)s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -144,165 +182,354 @@ __device__ __forceinline__ void block_partials(double (&v)[NW], double* __restri
   __syncthreads();
 }
 
-// the per-component scalars live in one device array S[field][c]
-enum Scalar { RHO = 0, ALPHA, OMEGA, BETA, BNORM2, RNORM2, ACTIVE, NSCALAR };
-
-__global__ void spmv_dot_kernel(Grid g, const double* __restrict__ A, const double* __restrict__ invD,
-                                const double* __restrict__ x, const double* __restrict__ w, double* __restrict__ y,
-                                const double* __restrict__ S, int ncomp, double* __restrict__ partials) {
-  const int c = blockIdx.y;
-  const bool active = S[ACTIVE * ncomp + c] != 0.0;
-  const double* xc = x + (size_t)c * g.N;
-  const double* wc = w + (size_t)c * g.N;
-  double* yc = y + (size_t)c * g.N;
-  double acc[1] = {0.0};
-  if (active) {
-    for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < g.N; X += (long long)gridDim.x * blockDim.x) {
-      const double v = stencil(g, A, invD, xc, X);
-      yc[X] = v;
-      acc[0] = fma(wc[X], v, acc[0]);
-    }
+template <int NW, class T>
+__device__ __forceinline__ void block_partials_chunk(T (&v)[NW][CH], double* __restrict__ partials, int c0,
+                                                     int ncomp) {
+#pragma unroll
+  for (int cc = 0; cc < CH; ++cc) {
+    T t[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) t[w] = v[w][cc];
+    if (c0 + cc < ncomp) block_partials<NW, T>(t, partials, c0 + cc, ncomp);
   }
-  block_partials<1>(acc, partials, c, ncomp);
 }
 
-// t = A invD s, partial dots (t.s, t.t)
-__global__ void spmv_dot2_kernel(Grid g, const double* __restrict__ A, const double* __restrict__ invD,
-                                 const double* __restrict__ s, double* __restrict__ t, const double* __restrict__ S,
-                                 int ncomp, double* __restrict__ partials) {
-  const int c = blockIdx.y;
-  const bool active = S[ACTIVE * ncomp + c] != 0.0;
-  const double* sc = s + (size_t)c * g.N;
-  double* tc = t + (size_t)c * g.N;
-  double acc[2] = {0.0, 0.0};
-  if (active) {
-    for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < g.N; X += (long long)gridDim.x * blockDim.x) {
-      const double v = stencil(g, A, invD, sc, X);
-      tc[X] = v;
-      acc[0] = fma(v, sc[X], acc[0]);
-      acc[1] = fma(v, v, acc[1]);
-    }
-  }
-  block_partials<2>(acc, partials, c, ncomp);
+// The seven cells a row reads: itself and its x-, x+, y-, y+, z-, z+
+// neighbours.  Where a neighbour does not exist the row's coefficient is 0
+// (coef_kernel, scale_kernel), so the index only has to stay inside the
+// array: it is clamped to [0, N-1] and the product adds 0 * (a finite
+// value).  No integer division; N < 2^31, so X + nx*ny fits in 32 bits.
+__device__ __forceinline__ void nbr_index(const Grid& g, unsigned X, unsigned (&idx)[7]) {
+  const unsigned last = (unsigned)g.N - 1u, nx = (unsigned)g.nx, nxy = (unsigned)g.nxy;
+  idx[0] = X;
+  idx[1] = X > 0u ? X - 1u : 0u;
+  idx[2] = min(X + 1u, last);
+  idx[3] = X >= nx ? X - nx : 0u;
+  idx[4] = min(X + nx, last);
+  idx[5] = X >= nxy ? X - nxy : 0u;
+  idx[6] = min(X + nxy, last);
 }
 
-// s = r - alpha v (active components)
-__global__ void axpy_s_kernel(long long N, const double* __restrict__ r, const double* __restrict__ v,
-                              double* __restrict__ s, const double* __restrict__ S, int ncomp) {
+// number of components in chunk blockIdx.y (CH, or the remainder)
+__device__ __forceinline__ int chunk_size(int ncomp) { return min(CH, ncomp - (int)blockIdx.y * CH); }
+
+__device__ __forceinline__ bool chunk_active(const double* __restrict__ S, int ncomp, int c0, int nc) {
+  bool any = false;
+  for (int cc = 0; cc < nc; ++cc) any = any || S[ACTIVE * ncomp + c0 + cc] != 0.0;
+  return any;
+}
+
+// ---------------------------------------------------------------- FP64 outer
+// r = b - A x with b = B T_k (B = psv/dt, or 1 on identity rows); partials
+// ||r||^2 (w = 0) and, on the first call, ||b||^2 (w = 1)
+template <int NC>
+__device__ __forceinline__ void residual_body(const Grid& g, const double* __restrict__ A,
+                                              const double* __restrict__ total_k, const double* __restrict__ x,
+                                              double* __restrict__ r64, bool first, double (&acc)[2][CH]) {
+  const size_t o0 = (size_t)blockIdx.y * CH * (size_t)g.Np;  // x, r64
+  const size_t t0 = (size_t)blockIdx.y * CH * (size_t)g.N;   // the caller's totals
+  for (unsigned X = blockIdx.x * blockDim.x + threadIdx.x; X < (unsigned)g.N; X += gridDim.x * blockDim.x) {
+    unsigned idx[7];
+    nbr_index(g, X, idx);
+    double w[7], xv[NC][7], tk[NC];
+    // all loads before the first store (see spmv_body)
+#pragma unroll
+    for (int q = 0; q < 7; ++q) w[q] = A[(size_t)q * g.N + X];
+    const double bs = A[(size_t)7 * g.N + X];
+#pragma unroll
+    for (int cc = 0; cc < NC; ++cc) {
+      const double* xc = x + o0 + (size_t)cc * g.Np;
+#pragma unroll
+      for (int q = 0; q < 7; ++q) xv[cc][q] = xc[idx[q]];
+      tk[cc] = total_k[t0 + (size_t)cc * g.N + X];
+    }
+#pragma unroll
+    for (int cc = 0; cc < NC; ++cc) {
+      const double b = bs * tk[cc];
+      double ax = w[0] * xv[cc][0];
+#pragma unroll
+      for (int q = 1; q < 7; ++q) ax = fma(w[q], xv[cc][q], ax);
+      const double rv = b - ax;
+      r64[o0 + (size_t)cc * g.Np + X] = rv;
+      acc[0][cc] = fma(rv, rv, acc[0][cc]);
+      if (first) acc[1][cc] = fma(b, b, acc[1][cc]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TPB) residual_kernel(Grid g, const double* __restrict__ A,
+                                                       const double* __restrict__ total_k,
+                                                       const double* __restrict__ x, double* __restrict__ r64,
+                                                       int ncomp, int first, double* __restrict__ partials) {
+  const int c0 = blockIdx.y * CH, nc = chunk_size(ncomp);
+  double acc[2][CH] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  switch (nc) {
+    case 4: residual_body<4>(g, A, total_k, x, r64, first != 0, acc); break;
+    case 3: residual_body<3>(g, A, total_k, x, r64, first != 0, acc); break;
+    case 2: residual_body<2>(g, A, total_k, x, r64, first != 0, acc); break;
+    default: residual_body<1>(g, A, total_k, x, r64, first != 0, acc); break;
+  }
+  block_partials_chunk<2, double>(acc, partials, c0, ncomp);
+}
+
+// x += ||r|| D^-1 y (the inner correction, which solved for r / ||r||) for
+// the components that ran
+__global__ void update64_kernel(long long N, long long Np, const double* __restrict__ invD,
+                                const float* __restrict__ y, double* __restrict__ x, const double* __restrict__ S,
+                                int ncomp) {
+  const int c = blockIdx.y;
+  if (S[RHS2 * ncomp + c] == 0.0) return;  // no inner solve for this component
+  const double scale = S[RSCALE * ncomp + c];
+  const size_t o = (size_t)c * Np;
+  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x)
+    x[o + X] = fma(invD[X] * scale, (double)y[o + X], x[o + X]);
+}
+
+// dst[c][X] = src[c][X] for X < N, component c = blockIdx.y, given strides
+__global__ void copy_kernel(long long N, long long src_stride, long long dst_stride, const double* __restrict__ src,
+                            double* __restrict__ dst) {
+  const double* sc = src + (size_t)blockIdx.y * src_stride;
+  double* dc = dst + (size_t)blockIdx.y * dst_stride;
+  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x)
+    dc[X] = sc[X];
+}
+
+// ---------------------------------------------------------------- FP32 inner
+// r = r64 / ||r64|| in FP32 (unit norm whatever the totals' magnitude);
+// y = 0; r0 = p = r; partial r.r
+__global__ void inner_init_kernel(long long Np, const double* __restrict__ r64, const double* __restrict__ S,
+                                  float* __restrict__ r, float* __restrict__ r0, float* __restrict__ p,
+                                  float* __restrict__ y, int ncomp, double* __restrict__ partials) {
+  // over the padded length: the padding of r64 is 0, so is that of r, r0, p, y
+  const int c = blockIdx.y;
+  const size_t o = (size_t)c * Np;
+  const double rs = S[RSCALE * ncomp + c];
+  const double inv = rs > 0.0 ? 1.0 / rs : 0.0;
+  float acc[1] = {0.0f};
+  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < Np; X += (long long)gridDim.x * blockDim.x) {
+    const float rv = (float)(r64[o + X] * inv);
+    r[o + X] = rv;
+    r0[o + X] = rv;
+    p[o + X] = rv;
+    y[o + X] = 0.0f;
+    acc[0] = fmaf(rv, rv, acc[0]);
+  }
+  block_partials<1, float>(acc, partials, c, ncomp);
+}
+
+// y = (A D^-1) x for the chunk's NC components; TWO = false: partial w.y;
+// TWO = true: partials (y.x, y.y)
+template <int NC, bool TWO>
+__device__ __forceinline__ void spmv_body(const Grid& g, const float* __restrict__ Ah, const float* __restrict__ x,
+                                          const float* __restrict__ w, float* __restrict__ y,
+                                          float (&acc)[2][CH]) {
+  // SPMV_CELLS cells per thread and pass (X, X + stride, ...).  Every load
+  // of a pass (coefficients, the NC components' seven values, w) is issued
+  // before the first store: a store between two loads orders them, and the
+  // pass would wait for memory once per component instead of once
+  constexpr int U = SPMV_CELLS;
+  const size_t o0 = (size_t)blockIdx.y * CH * (size_t)g.Np;
+  const unsigned N = (unsigned)g.N, stride = gridDim.x * blockDim.x;
+  for (unsigned X0 = blockIdx.x * blockDim.x + threadIdx.x; X0 < N; X0 += U * stride) {
+    unsigned idx[U][7];
+    float a[U][6], xv[U][NC][7], wv[U][NC];
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const unsigned X = X0 + u * stride;
+      ok[u] = X < N;
+      const unsigned Xc = ok[u] ? X : N - 1u;  // a cell past the end repeats the last (not stored)
+      nbr_index(g, Xc, idx[u]);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) a[u][q] = Ah[(size_t)q * g.N + Xc];
+#pragma unroll
+      for (int cc = 0; cc < NC; ++cc) {
+        const float* xc = x + o0 + (size_t)cc * g.Np;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) xv[u][cc][q] = xc[idx[u][q]];
+        if (!TWO) wv[u][cc] = w[o0 + (size_t)cc * g.Np + Xc];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+#pragma unroll
+      for (int cc = 0; cc < NC; ++cc) {
+        float v = xv[u][cc][0];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) v = fmaf(a[u][q], xv[u][cc][q + 1], v);
+        if (!ok[u]) continue;
+        y[o0 + (size_t)cc * g.Np + idx[u][0]] = v;
+        if (TWO) {
+          acc[0][cc] = fmaf(v, xv[u][cc][0], acc[0][cc]);
+          acc[1][cc] = fmaf(v, v, acc[1][cc]);
+        } else {
+          acc[0][cc] = fmaf(wv[u][cc], v, acc[0][cc]);
+        }
+      }
+    }
+  }
+}
+
+template <bool TWO>
+__device__ __forceinline__ void spmv_chunk(const Grid& g, const float* __restrict__ Ah, const float* __restrict__ x,
+                                           const float* __restrict__ w, float* __restrict__ y,
+                                           const double* __restrict__ S, int ncomp, double* __restrict__ partials) {
+  const int c0 = blockIdx.y * CH, nc = chunk_size(ncomp);
+  float acc[2][CH] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  // a chunk with no active component skips the product; an active chunk
+  // computes all its components (vectors of converged components are not
+  // read again, their partials are ignored)
+  if (chunk_active(S, ncomp, c0, nc)) {
+    switch (nc) {
+      case 4: spmv_body<4, TWO>(g, Ah, x, w, y, acc); break;
+      case 3: spmv_body<3, TWO>(g, Ah, x, w, y, acc); break;
+      case 2: spmv_body<2, TWO>(g, Ah, x, w, y, acc); break;
+      default: spmv_body<1, TWO>(g, Ah, x, w, y, acc); break;
+    }
+  }
+  if (TWO) block_partials_chunk<2, float>(acc, partials, c0, ncomp);
+  else {
+    float a1[1][CH] = {{acc[0][0], acc[0][1], acc[0][2], acc[0][3]}};
+    block_partials_chunk<1, float>(a1, partials, c0, ncomp);
+  }
+}
+
+// v = (A D^-1) p, partial r0.v
+__global__ void __launch_bounds__(TPB) spmv_dot_kernel(Grid g, const float* __restrict__ Ah,
+                                                       const float* __restrict__ x, const float* __restrict__ w,
+                                                       float* __restrict__ y, const double* __restrict__ S,
+                                                       int ncomp, double* __restrict__ partials) {
+  spmv_chunk<false>(g, Ah, x, w, y, S, ncomp, partials);
+}
+
+// t = (A D^-1) s, partials (t.s, t.t)
+__global__ void __launch_bounds__(TPB) spmv_dot2_kernel(Grid g, const float* __restrict__ Ah,
+                                                        const float* __restrict__ s, float* __restrict__ t,
+                                                        const double* __restrict__ S, int ncomp,
+                                                        double* __restrict__ partials) {
+  spmv_chunk<true>(g, Ah, s, nullptr, t, S, ncomp, partials);
+}
+
+// The vector updates run over float4 of the padded vectors (Np is a
+// multiple of 4 and every vector starts on a 256-byte boundary); the padding
+// is 0 in every vector and stays 0 under these updates.
+
+// s = r - alpha v
+__global__ void axpy_s_kernel(long long Np4, const float4* __restrict__ r, const float4* __restrict__ v,
+                              float4* __restrict__ s, const double* __restrict__ S, int ncomp) {
   const int c = blockIdx.y;
   if (S[ACTIVE * ncomp + c] == 0.0) return;
-  const double alpha = S[ALPHA * ncomp + c];
-  const size_t o = (size_t)c * N;
-  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x)
-    s[o + X] = fma(-alpha, v[o + X], r[o + X]);
+  const float alpha = (float)S[ALPHA * ncomp + c];
+  const size_t o = (size_t)c * Np4;
+  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < Np4; X += (long long)gridDim.x * blockDim.x) {
+    const float4 rv = r[o + X], vv = v[o + X];
+    s[o + X] = make_float4(fmaf(-alpha, vv.x, rv.x), fmaf(-alpha, vv.y, rv.y), fmaf(-alpha, vv.z, rv.z),
+                           fmaf(-alpha, vv.w, rv.w));
+  }
 }
 
-// x += invD (alpha p + omega s); r = s - omega t; partial dots (r0.r, r.r)
-__global__ void update_xr_kernel(long long N, const double* __restrict__ invD, double* __restrict__ x,
-                                 double* __restrict__ r, const double* __restrict__ p, const double* __restrict__ s,
-                                 const double* __restrict__ t, const double* __restrict__ r0,
+// y += alpha p + omega s; r = s - omega t; partials (r0.r, r.r)
+__global__ void update_yr_kernel(long long Np4, float4* __restrict__ y, float4* __restrict__ r,
+                                 const float4* __restrict__ p, const float4* __restrict__ s,
+                                 const float4* __restrict__ t, const float4* __restrict__ r0,
                                  const double* __restrict__ S, int ncomp, double* __restrict__ partials) {
   const int c = blockIdx.y;
   const bool active = S[ACTIVE * ncomp + c] != 0.0;
-  double acc[2] = {0.0, 0.0};
+  float acc[2] = {0.0f, 0.0f};
   if (active) {
-    const double alpha = S[ALPHA * ncomp + c], omega = S[OMEGA * ncomp + c];
-    const size_t o = (size_t)c * N;
-    for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x) {
-      const double sv = s[o + X];
-      x[o + X] = fma(invD[X], fma(alpha, p[o + X], omega * sv), x[o + X]);
-      const double rv = fma(-omega, t[o + X], sv);
-      r[o + X] = rv;
-      acc[0] = fma(r0[o + X], rv, acc[0]);
-      acc[1] = fma(rv, rv, acc[1]);
+    const float alpha = (float)S[ALPHA * ncomp + c], omega = (float)S[OMEGA * ncomp + c];
+    const size_t o = (size_t)c * Np4;
+    for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < Np4; X += (long long)gridDim.x * blockDim.x) {
+      const float4 sv = s[o + X], pv = p[o + X], yv = y[o + X], tv = t[o + X], zv = r0[o + X];
+      float4 yn, rn;
+      yn.x = fmaf(alpha, pv.x, fmaf(omega, sv.x, yv.x));
+      yn.y = fmaf(alpha, pv.y, fmaf(omega, sv.y, yv.y));
+      yn.z = fmaf(alpha, pv.z, fmaf(omega, sv.z, yv.z));
+      yn.w = fmaf(alpha, pv.w, fmaf(omega, sv.w, yv.w));
+      rn.x = fmaf(-omega, tv.x, sv.x);
+      rn.y = fmaf(-omega, tv.y, sv.y);
+      rn.z = fmaf(-omega, tv.z, sv.z);
+      rn.w = fmaf(-omega, tv.w, sv.w);
+      y[o + X] = yn;
+      r[o + X] = rn;
+      acc[0] = fmaf(zv.x, rn.x, fmaf(zv.y, rn.y, fmaf(zv.z, rn.z, fmaf(zv.w, rn.w, acc[0]))));
+      acc[1] = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, fmaf(rn.z, rn.z, fmaf(rn.w, rn.w, acc[1]))));
     }
   }
-  block_partials<2>(acc, partials, c, ncomp);
+  block_partials<2, float>(acc, partials, c, ncomp);
 }
 
 // p = r + beta (p - omega v)
-__global__ void update_p_kernel(long long N, double* __restrict__ p, const double* __restrict__ r,
-                                const double* __restrict__ v, const double* __restrict__ S, int ncomp) {
+__global__ void update_p_kernel(long long Np4, float4* __restrict__ p, const float4* __restrict__ r,
+                                const float4* __restrict__ v, const double* __restrict__ S, int ncomp) {
   const int c = blockIdx.y;
   if (S[ACTIVE * ncomp + c] == 0.0) return;
-  const double beta = S[BETA * ncomp + c], omega = S[OMEGA * ncomp + c];
-  const size_t o = (size_t)c * N;
-  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x)
-    p[o + X] = fma(beta, fma(-omega, v[o + X], p[o + X]), r[o + X]);
-}
-
-// initial state: x0 = 0, b = psv T / dt, r = r0 = p = b (right Jacobi
-// preconditioning: BiCGStab on A invD for y = D x, with x itself updated by
-// invD times the y increments); partial sums of b.b
-__global__ void init_kernel(long long N, const double* __restrict__ A, const double* __restrict__ total,
-                            const double* __restrict__ por,
-                            const double* __restrict__ sat, const double* __restrict__ vol, double dt,
-                            double* __restrict__ x, double* __restrict__ r, double* __restrict__ r0,
-                            double* __restrict__ p, int ncomp, double* __restrict__ partials) {
-  const int c = blockIdx.y;
-  const size_t o = (size_t)c * N;
-  double acc[1] = {0.0};
-  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x) {
-    const double psv = por[X] * sat[X] * 1000.0 * vol[X];
-    // identity rows (see coef_kernel) carry the cell's own total
-    const bool ident = psv == 0.0 && A[X] == 1.0 && A[N + X] == 0.0 && A[2 * N + X] == 0.0 &&
-                       A[3 * N + X] == 0.0 && A[4 * N + X] == 0.0 && A[5 * N + X] == 0.0 && A[6 * N + X] == 0.0;
-    const double b = ident ? total[o + X] : psv * total[o + X] / dt;
-    x[o + X] = 0.0;
-    r[o + X] = b;
-    r0[o + X] = b;
-    p[o + X] = b;
-    acc[0] = fma(b, b, acc[0]);
+  const float beta = (float)S[BETA * ncomp + c], omega = (float)S[OMEGA * ncomp + c];
+  const size_t o = (size_t)c * Np4;
+  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < Np4; X += (long long)gridDim.x * blockDim.x) {
+    const float4 pv = p[o + X], rv = r[o + X], vv = v[o + X];
+    p[o + X] = make_float4(fmaf(beta, fmaf(-omega, vv.x, pv.x), rv.x), fmaf(beta, fmaf(-omega, vv.y, pv.y), rv.y),
+                           fmaf(beta, fmaf(-omega, vv.z, pv.z), rv.z), fmaf(beta, fmaf(-omega, vv.w, pv.w), rv.w));
   }
-  block_partials<1>(acc, partials, c, ncomp);
 }
 
-// fixed-order sums of the partials, then the BiCGStab scalar recurrences;
-// one thread per component.  stage: 0 init, 1 alpha, 2 omega, 3 rho/beta
-__global__ void scalar_kernel(int stage, int nparts, const double* __restrict__ partials, double* __restrict__ S,
-                              int ncomp, double rtol2) {
-  const int c = threadIdx.x;
-  if (c >= ncomp) return;
+// Fixed-order sums of the partials (one warp per component: lane l sums
+// partials l, l+32, ..., then a fixed shuffle tree) and the scalar updates.
+// stage 0: outer residual (ORES2, and BNORM2 on the first call, first=1)
+// stage 1: inner start (RHO, RHS2, RNORM2; ACTIVE unless the component is
+//          converged in the outer sense; ITOL2: the inner target, no
+//          tighter than what brings the outer residual to rtol)
+// stage 2: alpha; stage 3: omega; stage 4: rho, beta and the inner test
+__global__ void scalar_kernel(int stage, int first, int nparts, const double* __restrict__ partials,
+                              double* __restrict__ S, int ncomp, double rtol2, double inner_rtol2) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= ncomp) return;  // whole warps leave together
   auto sum = [&](int w) {
     double s = 0.0;
-    for (int b = 0; b < nparts; ++b) s += partials[((size_t)w * ncomp + c) * nparts + b];
-    return s;
+    const double* p = partials + ((size_t)w * ncomp + c) * nparts;
+    for (int b = lane; b < nparts; b += 32) s += p[b];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    return __shfl_sync(0xffffffffu, s, 0);
   };
+  const bool two = stage == 0 || stage == 3 || stage == 4;
+  const double s0 = sum(0);
+  const double s1 = two ? sum(1) : 0.0;
+  if (lane != 0) return;
+  double* Sc = S + c;
   if (stage == 0) {
-    const double bb = sum(0);
-    S[RHO * ncomp + c] = bb;
-    S[BNORM2 * ncomp + c] = bb;
-    S[RNORM2 * ncomp + c] = bb;
-    S[ALPHA * ncomp + c] = 0.0;
-    S[OMEGA * ncomp + c] = 0.0;
-    S[BETA * ncomp + c] = 0.0;
-    S[ACTIVE * ncomp + c] = bb > 0.0 ? 1.0 : 0.0;  // b = 0: x = 0 is the solution
+    Sc[ORES2 * ncomp] = s0;
+    Sc[RSCALE * ncomp] = sqrt(s0);
+    if (first) Sc[BNORM2 * ncomp] = s1;
     return;
   }
-  if (S[ACTIVE * ncomp + c] == 0.0) return;
   if (stage == 1) {
-    const double r0v = sum(0);
-    if (r0v == 0.0) { S[ACTIVE * ncomp + c] = 0.0; S[ALPHA * ncomp + c] = 0.0; return; }  // breakdown
-    S[ALPHA * ncomp + c] = S[RHO * ncomp + c] / r0v;
-  } else if (stage == 2) {
-    const double ts = sum(0), tt = sum(1);
-    S[OMEGA * ncomp + c] = tt > 0.0 ? ts / tt : 0.0;
-  } else {
-    const double rho_new = sum(0), rr = sum(1);
-    const double rho = S[RHO * ncomp + c], omega = S[OMEGA * ncomp + c];
-    S[RNORM2 * ncomp + c] = rr;
-    S[BETA * ncomp + c] = (rho != 0.0 && omega != 0.0) ? (rho_new / rho) * (S[ALPHA * ncomp + c] / omega) : 0.0;
-    S[RHO * ncomp + c] = rho_new;
-    if (rr <= rtol2 * S[BNORM2 * ncomp + c] || omega == 0.0 || rho_new == 0.0) S[ACTIVE * ncomp + c] = 0.0;
+    const bool done = Sc[ORES2 * ncomp] <= rtol2 * Sc[BNORM2 * ncomp];
+    Sc[RHO * ncomp] = s0;
+    Sc[RNORM2 * ncomp] = s0;
+    Sc[RHS2 * ncomp] = done ? 0.0 : s0;
+    Sc[ALPHA * ncomp] = 0.0;
+    Sc[OMEGA * ncomp] = 0.0;
+    Sc[BETA * ncomp] = 0.0;
+    Sc[ACTIVE * ncomp] = (!done && s0 > 0.0) ? 1.0 : 0.0;
+    const double need = INNER_SAFETY * INNER_SAFETY * rtol2 * Sc[BNORM2 * ncomp] / Sc[ORES2 * ncomp];
+    Sc[ITOL2 * ncomp] = done ? 0.0 : fmax(inner_rtol2, need);
+    return;
   }
-}
-
-// the solution back into the totals
-__global__ void finish_kernel(long long N, const double* __restrict__ x, double* __restrict__ total) {
-  const int c = blockIdx.y;
-  const size_t o = (size_t)c * N;
-  for (long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x; X < N; X += (long long)gridDim.x * blockDim.x)
-    total[o + X] = x[o + X];
+  if (Sc[ACTIVE * ncomp] == 0.0) return;
+  if (stage == 2) {
+    if (s0 == 0.0) { Sc[ACTIVE * ncomp] = 0.0; Sc[ALPHA * ncomp] = 0.0; return; }  // breakdown
+    Sc[ALPHA * ncomp] = Sc[RHO * ncomp] / s0;
+  } else if (stage == 3) {
+    Sc[OMEGA * ncomp] = s1 > 0.0 ? s0 / s1 : 0.0;
+  } else {
+    const double rho_new = s0, rr = s1;
+    const double rho = Sc[RHO * ncomp], omega = Sc[OMEGA * ncomp];
+    Sc[RNORM2 * ncomp] = rr;
+    Sc[BETA * ncomp] = (rho != 0.0 && omega != 0.0) ? (rho_new / rho) * (Sc[ALPHA * ncomp] / omega) : 0.0;
+    Sc[RHO * ncomp] = rho_new;
+    if (rr <= Sc[ITOL2 * ncomp] * Sc[RHS2 * ncomp] || omega == 0.0 || rho_new == 0.0) Sc[ACTIVE * ncomp] = 0.0;
+  }
 }
 
 }  // namespace tr
@@ -312,23 +539,81 @@ using namespace pfgpu;
 
 struct PfTransport {
   int nx = 0, ny = 0, nz = 0, ncomp = 0;
-  long long N = 0;
-  double* buf = nullptr;     // A[7N] invD[N] x r r0 p v s t [n N each] partials S
-  double* h_scalars = nullptr;  // pinned copy of S for the convergence check
+  long long N = 0, Np = 0;
+  void* buf = nullptr;          // see transport_layout
+  double* h_scalars = nullptr;  // pinned copy of S for the convergence checks
   size_t bytes = 0;
+  // blocks per component (vector kernels) or per component chunk (stencil
+  // kernels): one full wave of the kernel's resident blocks
+  int gx_res = 1, gx_sp1 = 1, gx_sp2 = 1, gx_vec = 1;
 };
+
+namespace {
+struct Layout {
+  double *A, *invD, *x, *r64, *partials, *S;
+  float *Ah, *r, *r0, *p, *v, *s, *t, *y;
+};
+
+// Work space, every array on a 256-byte boundary: FP64 A[8][N], invD[N],
+// x and r64 [ncomp][Np], partials, S; FP32 Ah[6][N] and the inner solver's
+// r, r0, p, v, s, t, y [ncomp][Np].  With base == nullptr only the size.
+size_t transport_layout(char* base, long long N, long long Np, int n, Layout* L) {
+  size_t cur = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base ? base + cur : nullptr;
+    cur += (bytes + 255) & ~(size_t)255;
+    return p;
+  };
+  const size_t vec = (size_t)n * (size_t)Np;
+  Layout l;
+  l.A = (double*)take(8 * (size_t)N * 8);
+  l.invD = (double*)take((size_t)N * 8);
+  l.x = (double*)take(vec * 8);
+  l.r64 = (double*)take(vec * 8);
+  l.partials = (double*)take(2 * (size_t)tr::RED_BLOCKS * n * 8);
+  l.S = (double*)take((size_t)tr::NSCALAR * n * 8);
+  l.Ah = (float*)take(6 * (size_t)N * 4);
+  l.r = (float*)take(vec * 4);
+  l.r0 = (float*)take(vec * 4);
+  l.p = (float*)take(vec * 4);
+  l.v = (float*)take(vec * 4);
+  l.s = (float*)take(vec * 4);
+  l.t = (float*)take(vec * 4);
+  l.y = (float*)take(vec * 4);
+  if (L) *L = l;
+  return cur;
+}
+
+int wave_blocks(const void* kernel, int parts) {
+  int dev = 0, sms = 0, occ = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, tr::TPB, 0) != cudaSuccess || occ < 1)
+    return -1;
+  const int b = sms * occ / (parts > 0 ? parts : 1);
+  return b < 1 ? 1 : (b > tr::RED_BLOCKS ? tr::RED_BLOCKS : b);
+}
+}  // namespace
 
 extern "C" int32_t pf_transport_create(int32_t nx, int32_t ny, int32_t nz, int32_t ncomp, PfTransport** out) {
   if (!out || nx < 1 || ny < 1 || nz < 1 || ncomp < 1 || ncomp > PF_MAX_NCOMP) return PF_ERR_INVALID;
   *out = nullptr;
+  // 32-bit cell indices, with the padded stride
+  if ((long long)nx * ny * nz > 0x7fffffffll - 4096) return PF_ERR_TOO_LARGE;
   PfTransport* t = new (std::nothrow) PfTransport();
   if (!t) return PF_ERR_INVALID;
   t->nx = nx; t->ny = ny; t->nz = nz; t->ncomp = ncomp;
   t->N = (long long)nx * ny * nz;
-  const size_t vec = (size_t)ncomp * (size_t)t->N;
-  const size_t doubles = 8 * (size_t)t->N + 7 * vec + 2 * (size_t)tr::RED_BLOCKS * ncomp + tr::NSCALAR * ncomp;
-  t->bytes = doubles * sizeof(double);
-  if (cudaMalloc(&t->buf, t->bytes) != cudaSuccess ||
+  t->Np = ((t->N + 63) / 64) * 64 + tr::VEC_PAD;
+  t->bytes = transport_layout(nullptr, t->N, t->Np, ncomp, nullptr);
+  const int chunks = (ncomp + tr::CH - 1) / tr::CH;
+  t->gx_res = wave_blocks((const void*)tr::residual_kernel, chunks);
+  t->gx_sp1 = wave_blocks((const void*)tr::spmv_dot_kernel, chunks);
+  t->gx_sp2 = wave_blocks((const void*)tr::spmv_dot2_kernel, chunks);
+  t->gx_vec = wave_blocks((const void*)tr::update_yr_kernel, ncomp);
+  if (t->gx_res < 0 || t->gx_sp1 < 0 || t->gx_sp2 < 0 || t->gx_vec < 0 ||
+      cudaMalloc(&t->buf, t->bytes) != cudaSuccess ||
+      cudaMemset(t->buf, 0, t->bytes) != cudaSuccess ||  // the vectors' padding stays 0
       cudaMallocHost(&t->h_scalars, tr::NSCALAR * ncomp * sizeof(double)) != cudaSuccess) {
     if (t->buf) cudaFree(t->buf);
     delete t;
@@ -355,71 +640,91 @@ extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, v
     return PF_ERR_INVALID;
   if ((t->nx > 1 && !a->qx) || (t->ny > 1 && !a->qy) || (t->nz > 1 && !a->qz)) return PF_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  const long long N = t->N;
+  const long long N = t->N, Np = t->Np, Np4 = Np / 4;
   const int n = t->ncomp;
-  const size_t vec = (size_t)n * (size_t)N;
-  double* A = t->buf;
-  double* invD = A + 7 * N;
-  double* x = invD + N;
-  double* r = x + vec;
-  double* r0 = r + vec;
-  double* p = r0 + vec;
-  double* v = p + vec;
-  double* sv = v + vec;
-  double* tv = sv + vec;
-  double* partials = tv + vec;
-  double* S = partials + 2 * (size_t)RED_BLOCKS * n;
-  Grid g{t->nx, t->ny, t->nz, N, (long long)t->nx * t->ny};
+  Layout L;
+  transport_layout(static_cast<char*>(t->buf), N, Np, n, &L);
+  Grid g{t->nx, t->ny, t->nz, N, (long long)t->nx * t->ny, Np};
   const unsigned cblocks = (unsigned)((N + TPB - 1) / TPB);
   coef_kernel<<<cblocks, TPB, 0, s>>>(g, a->dx, a->dy, a->dz, a->qx, a->qy, a->qz, a->diffusion_coefficient,
                                       a->tortuosity, a->dispersivity, a->porosity, a->saturation, a->volume, a->dt,
-                                      A, invD);
-  const long long want = (N + TPB - 1) / TPB;
-  const dim3 grid((unsigned)(want < RED_BLOCKS ? want : RED_BLOCKS), (unsigned)n);
-  const int nparts = (int)grid.x;
-  const double rtol2 = a->rtol * a->rtol;
-  init_kernel<<<grid, TPB, 0, s>>>(N, A, a->total, a->porosity, a->saturation, a->volume, a->dt, x, r, r0, p, n,
-                                   partials);
-  scalar_kernel<<<1, 32, 0, s>>>(0, nparts, partials, S, n, rtol2);
-  if (cudaGetLastError() != cudaSuccess) return PF_ERR_CUDA;
-  int it = 0;
-  bool done = false;
-  const int check_every = 4;
-  while (it < a->max_iterations && !done) {
-    spmv_dot_kernel<<<grid, TPB, 0, s>>>(g, A, invD, p, r0, v, S, n, partials);       // v = A invD p, r0.v
-    scalar_kernel<<<1, 32, 0, s>>>(1, nparts, partials, S, n, rtol2);                  // alpha
-    axpy_s_kernel<<<grid, TPB, 0, s>>>(N, r, v, sv, S, n);                              // s = r - alpha v
-    spmv_dot2_kernel<<<grid, TPB, 0, s>>>(g, A, invD, sv, tv, S, n, partials);         // t = A invD s
-    scalar_kernel<<<1, 32, 0, s>>>(2, nparts, partials, S, n, rtol2);                  // omega
-    update_xr_kernel<<<grid, TPB, 0, s>>>(N, invD, x, r, p, sv, tv, r0, S, n, partials);
-    scalar_kernel<<<1, 32, 0, s>>>(3, nparts, partials, S, n, rtol2);                  // rho, beta, test
-    update_p_kernel<<<grid, TPB, 0, s>>>(N, p, r, v, S, n);
-    ++it;
-    if (it % check_every == 0 || it == a->max_iterations) {
-      if (cudaMemcpyAsync(t->h_scalars, S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess)
-        return PF_ERR_CUDA;
-      done = true;
-      for (int c = 0; c < n; ++c) done = done && t->h_scalars[ACTIVE * n + c] == 0.0;
+                                      L.A, L.invD);
+  scale_kernel<<<cblocks, TPB, 0, s>>>(g, L.A, L.invD, L.Ah);
+  // blocks: one wave, but no more than the cells need
+  auto cap = [&](int gx) { return (unsigned)((long long)gx < (long long)cblocks ? gx : (int)cblocks); };
+  const unsigned chunks = (unsigned)((n + CH - 1) / CH);
+  const dim3 g_res(cap(t->gx_res), chunks), g_sp1(cap(t->gx_sp1), chunks), g_sp2(cap(t->gx_sp2), chunks);
+  const dim3 g_vec(cap(t->gx_vec), (unsigned)n);
+  const double rtol2 = a->rtol * a->rtol, irtol2 = INNER_RTOL * INNER_RTOL;
+  const unsigned sblocks = (unsigned)((n + 3) / 4);
+  auto scalar = [&](int stage, int first, const dim3& producer) {
+    scalar_kernel<<<sblocks, 128, 0, s>>>(stage, first, (int)producer.x, L.partials, L.S, n, rtol2, irtol2);
+  };
+  copy_kernel<<<g_vec, TPB, 0, s>>>(N, N, Np, a->total, L.x);  // x0 = T_k
+  auto outer_residual = [&](int first) {
+    residual_kernel<<<g_res, TPB, 0, s>>>(g, L.A, a->total, L.x, L.r64, n, first, L.partials);
+    scalar(0, first, g_res);
+  };
+  auto fetch = [&]() {
+    return cudaMemcpyAsync(t->h_scalars, L.S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) ==
+               cudaSuccess &&
+           cudaStreamSynchronize(s) == cudaSuccess;
+  };
+  auto all_done = [&]() {
+    for (int c = 0; c < n; ++c)
+      if (t->h_scalars[ORES2 * n + c] > rtol2 * t->h_scalars[BNORM2 * n + c]) return false;
+    return true;
+  };
+  float4 *r4 = (float4*)L.r, *p4 = (float4*)L.p, *v4 = (float4*)L.v, *s4 = (float4*)L.s, *t4 = (float4*)L.t,
+         *y4 = (float4*)L.y, *z4 = (float4*)L.r0;
+  outer_residual(1);
+  if (cudaGetLastError() != cudaSuccess || !fetch()) return PF_ERR_CUDA;
+  int inner_total = 0, outer = 0;
+  while (!all_done() && inner_total < a->max_iterations && outer < OUTER_MAX) {
+    // FP32 correction: (A D^-1) y = r / ||r||
+    inner_init_kernel<<<g_vec, TPB, 0, s>>>(Np, L.r64, L.S, L.r, L.r0, L.p, L.y, n, L.partials);
+    scalar(1, 0, g_vec);
+    int it = 0;
+    bool inner_done = false;
+    while (!inner_done && it < INNER_MAX && inner_total < a->max_iterations) {
+      spmv_dot_kernel<<<g_sp1, TPB, 0, s>>>(g, L.Ah, L.p, L.r0, L.v, L.S, n, L.partials);
+      scalar(2, 0, g_sp1);
+      axpy_s_kernel<<<g_vec, TPB, 0, s>>>(Np4, r4, v4, s4, L.S, n);
+      spmv_dot2_kernel<<<g_sp2, TPB, 0, s>>>(g, L.Ah, L.s, L.t, L.S, n, L.partials);
+      scalar(3, 0, g_sp2);
+      update_yr_kernel<<<g_vec, TPB, 0, s>>>(Np4, y4, r4, p4, s4, t4, z4, L.S, n, L.partials);
+      scalar(4, 0, g_vec);
+      update_p_kernel<<<g_vec, TPB, 0, s>>>(Np4, p4, r4, v4, L.S, n);
+      ++it;
+      ++inner_total;
+      if (it % 2 == 0) {
+        if (!fetch()) return PF_ERR_CUDA;
+        inner_done = true;
+        for (int c = 0; c < n; ++c) inner_done = inner_done && t->h_scalars[ACTIVE * n + c] == 0.0;
+      }
     }
+    // FP64: x += ||r|| D^-1 y, new residual
+    update64_kernel<<<g_vec, TPB, 0, s>>>(N, Np, L.invD, L.y, L.x, L.S, n);
+    outer_residual(0);
+    if (cudaGetLastError() != cudaSuccess || !fetch()) return PF_ERR_CUDA;
+    ++outer;
   }
-  finish_kernel<<<grid, TPB, 0, s>>>(N, x, a->total);
-  if (cudaGetLastError() != cudaSuccess) return PF_ERR_CUDA;
-  if (cudaMemcpyAsync(t->h_scalars, S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return PF_ERR_CUDA;
+  copy_kernel<<<g_vec, TPB, 0, s>>>(N, Np, N, L.x, a->total);
+  if (cudaGetLastError() != cudaSuccess || !fetch()) return PF_ERR_CUDA;
   double worst = 0.0;
   bool conv = true;
   for (int c = 0; c < n; ++c) {
-    const double bb = t->h_scalars[BNORM2 * n + c], rr = t->h_scalars[RNORM2 * n + c];
+    const double bb = t->h_scalars[BNORM2 * n + c], rr = t->h_scalars[ORES2 * n + c];
     const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
     worst = rel > worst ? rel : worst;
     conv = conv && !(rel > a->rtol);
   }
   if (stats) {
-    stats->iterations = it;
+    stats->iterations = inner_total;
     stats->max_rel_residual = worst;
     stats->converged = conv ? 1 : 0;
+    stats->refinements = outer;
+    stats->reserved = 0;
   }
   return conv ? PF_OK : PF_CELL_FAILURES;
 }

@@ -136,7 +136,8 @@ class PfTransportArgs(C.Structure):
 
 
 class PfTransportStats(C.Structure):
-    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("max_rel_residual", C.c_double)]
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("max_rel_residual", C.c_double),
+                ("refinements", C.c_int32), ("reserved", C.c_int32)]
 
 
 class PfLaunchConfig(C.Structure):

@@ -47,7 +47,13 @@ class OSTransport:
         """Transport the totals of `state` (a CellState of CUDA tensors on
         this grid) over dt, in place.  Returns the solver statistics; raises
         PfError if the solve did not converge within max_iterations."""
+        import torch
         g = self.grid
+        N = g.nx * g.ny * g.nz
+        for key, size in (("porosity", N), ("saturation", N), ("volume", N), ("total", self.ncomp * N)):
+            t = state.a[key]
+            if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous() or t.numel() != size:
+                raise ValueError("state.%s must be a contiguous float64 CUDA tensor of %d values" % (key, size))
         a = abi.PfTransportArgs()
         dp = C.POINTER(C.c_double)
         a.nx, a.ny, a.nz, a.ncomp = g.nx, g.ny, g.nz, self.ncomp

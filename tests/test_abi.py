@@ -47,30 +47,34 @@ def test_version(lib):
     assert lib.pf_version().startswith(b"pfgpu")
 
 
-_LAYOUT_C = r"""
-#include <stdio.h>
-#include <stddef.h>
-#include "pfgpu.h"
-#define F(T, f) printf("%s.%s %zu\n", #T, #f, offsetof(T, f));
-int main(void) {
-  printf("PfOptions %zu\n", sizeof(PfOptions));
-  printf("PfNetworkDesc %zu\n", sizeof(PfNetworkDesc));
-  printf("PfCellState %zu\n", sizeof(PfCellState));
-  printf("PfStepStats %zu\n", sizeof(PfStepStats));
-  printf("PfLaunchConfig %zu\n", sizeof(PfLaunchConfig));
-  F(PfNetworkDesc, opts) F(PfNetworkDesc, debyeA) F(PfNetworkDesc, mnrl_affinity_power)
-  F(PfNetworkDesc, sec_nspec) F(PfCellState, dt_cell) F(PfCellState, num_substeps)
-  F(PfOptions, max_dlnC_rreact) F(PfStepStats, max_substeps)
-  return 0;
-}
-"""
+def _structs():
+    return [v for v in vars(abi).values()
+            if isinstance(v, type) and issubclass(v, C.Structure) and v.__name__.startswith("Pf")]
+
+
+def _layout_c():
+    """A C program printing sizeof and every field offset of each ctypes
+    mirror, compiled against the header."""
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "pfgpu.h"', "int main(void) {"]
+    for t in _structs():
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (t.__name__, t.__name__))
+        for f, _ in t._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (t.__name__, f, t.__name__, f))
+    lines += ["  return 0;", "}"]
+    return "\n".join(lines) + "\n"
 
 
 def test_struct_layout_matches_c(tmp_path):
+    """Every struct of the ctypes mirror: size and every field offset equal
+    the header's (the check a Fortran binding repeats with c_sizeof)."""
+    structs = _structs()
+    assert {t.__name__ for t in structs} >= {"PfOptions", "PfNetworkDesc", "PfCellState", "PfStepStats",
+                                             "PfAdjointArgs", "PfGirtArgs", "PfTransportArgs",
+                                             "PfTransportStats", "PfLaunchConfig"}
     src = tmp_path / "layout.c"
-    src.write_text(_LAYOUT_C)
+    src.write_text(_layout_c())
     exe = tmp_path / "layout"
-    subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    subprocess.run(["gcc", "-Wall", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
     seen = 0
     for line in out:
@@ -84,7 +88,7 @@ def test_struct_layout_matches_c(tmp_path):
         else:
             assert C.sizeof(getattr(abi, key)) == val, key
         seen += 1
-    assert seen == 13
+    assert seen == sum(1 + len(t._fields_) for t in structs)
 
 
 def test_invalid_network_rejected_without_gpu(lib):
