@@ -448,7 +448,7 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
-def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, rtol=1e-10):
+def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, rtol=1e-10, cpu=False):
     """The transport half of the operator-split step (pf_transport_step) on
     the same grid as the global-implicit measurement: every component's
     totals transported over dt = 1 day to rtol by mixed-precision iterative
@@ -462,7 +462,11 @@ def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, r
                              porosity, saturation, volume)
       refinement update      44 n + 8   (scaled start of the inner solve,
                              x += D^-1 y)
-      set-up and copies      32 n + 200"""
+      set-up and copies      32 n + 200
+    CPU baseline (cpu=True): the oracle's transport matrix (the restatement
+    of RTCalculateTransportMatrix) and scipy's Jacobi-preconditioned BiCGStab
+    per component to the same rtol, one host core, on a 32x32x16 grid of the
+    same cells."""
     import numpy as np
     import torch
 
@@ -512,7 +516,44 @@ def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, r
         peak = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except Exception:
         pass
+    cpu_line = None
+    if cpu:
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spla
+
+        from oracle.oracle import Oracle
+        from pfgpu.girt import girt_pattern
+        cx, cy, cz = 32, 32, 16
+        Nc = cx * cy * cz
+        crng = np.random.default_rng(seed + 1)
+
+        def cq(shape):
+            return crng.uniform(1e-7, 1e-5, shape) * crng.choice([-1.0, 1.0], shape)
+        gd = dict(nx=cx, ny=cy, nz=cz, dx=1.0, dy=1.0, dz=1.0, diffusion=1e-9, tortuosity=1.0, dispersivity=0.0,
+                  qx=cq((cz, cy, cx - 1)), qy=cq((cz, cy - 1, cx)), qz=cq((cz - 1, cy, cx)))
+        por, sat, vol = (st.a[k][:Nc].cpu().numpy() for k in ("porosity", "saturation", "volume"))
+        T = t0.reshape(n, -1)[:, :Nc].cpu().numpy()
+        rp, ci = girt_pattern(cx, cy, cz)
+        o = Oracle()
+        tc = time.perf_counter()
+        vals = o.transport_matrix(gd, por, sat, vol, dt, rp, ci)
+        A = sp.csr_matrix((vals, ci, rp), shape=(Nc, Nc))
+        psv = por * sat * 1000.0 * vol
+        d = A.diagonal().copy()
+        d[d == 0.0] = 1.0
+        M = sp.diags(1.0 / d)
+        for c in range(n):
+            b = psv * T[c] / dt
+            try:
+                spla.bicgstab(A, b, x0=T[c].copy(), rtol=rtol, atol=0.0, M=M, maxiter=1000)
+            except TypeError:
+                spla.bicgstab(A, b, x0=T[c].copy(), tol=rtol, atol=0.0, M=M, maxiter=1000)
+        el = time.perf_counter() - tc
+        cpu_line = {"value": Nc / el, "unit": "cells/s", "cores": 1, "kind": "port",
+                    "sample": "32x32x16 grid, %d components: oracle transport matrix + scipy Jacobi-BiCGStab to "
+                              "rtol %g, %.3f s" % (n, rtol, el)}
     return {"grid": "%dx%dx%d" % (nx, ny, nz), "cells": N, "ncomp": n, "ms": t, "iterations": it, "refinements": ref,
+            "cpu_baseline": cpu_line,
             "rel_residual": stats["max_rel_residual"], "rtol": rtol,
             "cells_per_s": N / (t * 1e-3), "algorithmic_bytes": alg, "achieved_gbs": gbs, "peak_gbs": peak,
             "hbm_frac": gbs / peak if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
@@ -607,7 +648,8 @@ def main():
         nx, ny, nz = (int(v) for v in args.grid.split("x"))
         gm = None if args.no_girt else girt_measure(net, eng, dev, args.steps, args.warmup, nx, ny, nz,
                                                     cpu=not args.no_cpu)
-        tm = transport_measure(net, dev, args.steps, max(2, min(args.warmup, 3)), nx, ny, nz)
+        tm = transport_measure(net, dev, args.steps, max(2, min(args.warmup, 3)), nx, ny, nz,
+                               cpu=rank == 0 and not args.no_cpu)
         if gm is None:
             gm = {"cells_per_s": float("nan"), "ms": float("nan")}
         if rank == 0:
@@ -754,7 +796,8 @@ def main():
     if not args.no_girt and args.config == "c2":
         for k in pristine:
             dev.a[k].copy_(pristine[k])
-        transport = transport_measure(net, dev, max(3, args.steps), max(2, min(args.warmup, 3)))
+        transport = transport_measure(net, dev, max(3, args.steps), max(2, min(args.warmup, 3)),
+                                      cpu=(rank == 0 and not args.no_cpu))
         log("transport:", json.dumps(transport))
 
     cpu = None

@@ -38,7 +38,7 @@ namespace tr {
 
 constexpr int TPB = 256;
 constexpr int RED_BLOCKS = 304;  // at most this many blocks (partial sums) per component (chunk)
-constexpr int SPMV_CELLS = 2;    // cells per thread and pass in the stencil products
+constexpr int SPMV_CELLS = 1;    // cells per thread and pass in the stencil products
 constexpr int VEC_PAD = 64;      // floats added to each vector's stride (not a power of two)
 constexpr int CH = 4;            // components per stencil pass
 constexpr double INNER_RTOL = 3.0e-6;  // inner reduction per cycle (floor)
@@ -194,6 +194,90 @@ __device__ __forceinline__ void block_partials_chunk(T (&v)[NW][CH], double* __r
   }
 }
 
+// Fixed-order sums of one component's partials (one warp: lane l sums
+// partials l, l+32, ..., then a fixed shuffle tree) and its scalar updates.
+// stage 0: outer residual (ORES2, and BNORM2 on the first call, first=1)
+// stage 1: inner start (RHO, RHS2, RNORM2; ACTIVE unless the component is
+//          converged in the outer sense; ITOL2: the inner target, no
+//          tighter than what brings the outer residual to rtol)
+// stage 2: alpha; stage 3: omega; stage 4: rho, beta and the inner test
+__device__ __noinline__ void scalar_component(int stage, int first, int nparts, const double* __restrict__ partials,
+                                 double* __restrict__ S, int ncomp, double rtol2, double inner_rtol2, int c,
+                                 int lane) {
+  auto sum = [&](int w) {
+    double s = 0.0;
+    const double* p = partials + ((size_t)w * ncomp + c) * nparts;
+    for (int b = lane; b < nparts; b += 32) s += __ldcg(p + b);  // other blocks' writes: read from L2
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    return __shfl_sync(0xffffffffu, s, 0);
+  };
+  const bool two = stage == 0 || stage == 3 || stage == 4;
+  const double s0 = sum(0);
+  const double s1 = two ? sum(1) : 0.0;
+  if (lane != 0) return;
+  double* Sc = S + c;
+  if (stage == 0) {
+    Sc[ORES2 * ncomp] = s0;
+    Sc[RSCALE * ncomp] = sqrt(s0);
+    if (first) Sc[BNORM2 * ncomp] = s1;
+    return;
+  }
+  if (stage == 1) {
+    const bool done = Sc[ORES2 * ncomp] <= rtol2 * Sc[BNORM2 * ncomp];
+    Sc[RHO * ncomp] = s0;
+    Sc[RNORM2 * ncomp] = s0;
+    Sc[RHS2 * ncomp] = done ? 0.0 : s0;
+    Sc[ALPHA * ncomp] = 0.0;
+    Sc[OMEGA * ncomp] = 0.0;
+    Sc[BETA * ncomp] = 0.0;
+    Sc[ACTIVE * ncomp] = (!done && s0 > 0.0) ? 1.0 : 0.0;
+    const double need = INNER_SAFETY * INNER_SAFETY * rtol2 * Sc[BNORM2 * ncomp] / Sc[ORES2 * ncomp];
+    Sc[ITOL2 * ncomp] = done ? 0.0 : fmax(inner_rtol2, need);
+    return;
+  }
+  if (Sc[ACTIVE * ncomp] == 0.0) return;
+  if (stage == 2) {
+    if (s0 == 0.0) { Sc[ACTIVE * ncomp] = 0.0; Sc[ALPHA * ncomp] = 0.0; return; }  // breakdown
+    Sc[ALPHA * ncomp] = Sc[RHO * ncomp] / s0;
+  } else if (stage == 3) {
+    Sc[OMEGA * ncomp] = s1 > 0.0 ? s0 / s1 : 0.0;
+  } else {
+    const double rho_new = s0, rr = s1;
+    const double rho = Sc[RHO * ncomp], omega = Sc[OMEGA * ncomp];
+    Sc[RNORM2 * ncomp] = rr;
+    Sc[BETA * ncomp] = (rho != 0.0 && omega != 0.0) ? (rho_new / rho) * (Sc[ALPHA * ncomp] / omega) : 0.0;
+    Sc[RHO * ncomp] = rho_new;
+    if (rr <= Sc[ITOL2 * ncomp] * Sc[RHS2 * ncomp] || omega == 0.0 || rho_new == 0.0) Sc[ACTIVE * ncomp] = 0.0;
+  }
+}
+
+
+struct Stage {
+  int stage, first;
+  double rtol2, inner_rtol2;
+  unsigned* counter;  // blocks of the current launch that have written their partials
+};
+
+// Called by every block after its partials are written: the last block of
+// the launch to arrive sums every component's partials (in block order, so
+// the result does not depend on which block is last) and makes the scalar
+// update, then re-arms the counter.  Replaces a separate scalar launch.
+__device__ __forceinline__ void finish_stage(const Stage& st, const double* __restrict__ partials,
+                                             double* __restrict__ S, int ncomp) {
+  __shared__ unsigned ticket;
+  if (threadIdx.x == 0) {
+    __threadfence();  // this block's partials before its ticket
+    ticket = atomicAdd(st.counter, 1u);
+  }
+  __syncthreads();
+  if (ticket != gridDim.x * gridDim.y - 1u) return;
+  __threadfence();  // every block's partials are visible
+  const int nwarps = blockDim.x >> 5, wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = wid; c < ncomp; c += nwarps)
+    scalar_component(st.stage, st.first, gridDim.x, partials, S, ncomp, st.rtol2, st.inner_rtol2, c, lane);
+  if (threadIdx.x == 0) *st.counter = 0u;
+}
+
 // The seven cells a row reads: itself and its x-, x+, y-, y+, z-, z+
 // neighbours.  Where a neighbour does not exist the row's coefficient is 0
 // (coef_kernel, scale_kernel), so the index only has to stay inside the
@@ -260,16 +344,19 @@ __device__ __forceinline__ void residual_body(const Grid& g, const double* __res
 __global__ void __launch_bounds__(TPB) residual_kernel(Grid g, const double* __restrict__ A,
                                                        const double* __restrict__ total_k,
                                                        const double* __restrict__ x, double* __restrict__ r64,
-                                                       int ncomp, int first, double* __restrict__ partials) {
+                                                       int ncomp, double* __restrict__ partials,
+                                                       double* __restrict__ S, Stage st) {
   const int c0 = blockIdx.y * CH, nc = chunk_size(ncomp);
+  const bool first = st.first != 0;
   double acc[2][CH] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   switch (nc) {
-    case 4: residual_body<4>(g, A, total_k, x, r64, first != 0, acc); break;
-    case 3: residual_body<3>(g, A, total_k, x, r64, first != 0, acc); break;
-    case 2: residual_body<2>(g, A, total_k, x, r64, first != 0, acc); break;
-    default: residual_body<1>(g, A, total_k, x, r64, first != 0, acc); break;
+    case 4: residual_body<4>(g, A, total_k, x, r64, first, acc); break;
+    case 3: residual_body<3>(g, A, total_k, x, r64, first, acc); break;
+    case 2: residual_body<2>(g, A, total_k, x, r64, first, acc); break;
+    default: residual_body<1>(g, A, total_k, x, r64, first, acc); break;
   }
   block_partials_chunk<2, double>(acc, partials, c0, ncomp);
+  finish_stage(st, partials, S, ncomp);
 }
 
 // x += ||r|| D^-1 y (the inner correction, which solved for r / ||r||) for
@@ -297,9 +384,9 @@ __global__ void copy_kernel(long long N, long long src_stride, long long dst_str
 // ---------------------------------------------------------------- FP32 inner
 // r = r64 / ||r64|| in FP32 (unit norm whatever the totals' magnitude);
 // y = 0; r0 = p = r; partial r.r
-__global__ void inner_init_kernel(long long Np, const double* __restrict__ r64, const double* __restrict__ S,
+__global__ void __launch_bounds__(TPB) inner_init_kernel(long long Np, const double* __restrict__ r64, double* __restrict__ S,
                                   float* __restrict__ r, float* __restrict__ r0, float* __restrict__ p,
-                                  float* __restrict__ y, int ncomp, double* __restrict__ partials) {
+                                  float* __restrict__ y, int ncomp, double* __restrict__ partials, Stage st) {
   // over the padded length: the padding of r64 is 0, so is that of r, r0, p, y
   const int c = blockIdx.y;
   const size_t o = (size_t)c * Np;
@@ -315,6 +402,7 @@ __global__ void inner_init_kernel(long long Np, const double* __restrict__ r64, 
     acc[0] = fmaf(rv, rv, acc[0]);
   }
   block_partials<1, float>(acc, partials, c, ncomp);
+  finish_stage(st, partials, S, ncomp);
 }
 
 // y = (A D^-1) x for the chunk's NC components; TWO = false: partial w.y;
@@ -373,7 +461,8 @@ __device__ __forceinline__ void spmv_body(const Grid& g, const float* __restrict
 template <bool TWO>
 __device__ __forceinline__ void spmv_chunk(const Grid& g, const float* __restrict__ Ah, const float* __restrict__ x,
                                            const float* __restrict__ w, float* __restrict__ y,
-                                           const double* __restrict__ S, int ncomp, double* __restrict__ partials) {
+                                           double* __restrict__ S, int ncomp, double* __restrict__ partials,
+                                           const Stage& st) {
   const int c0 = blockIdx.y * CH, nc = chunk_size(ncomp);
   float acc[2][CH] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   // a chunk with no active component skips the product; an active chunk
@@ -392,22 +481,23 @@ __device__ __forceinline__ void spmv_chunk(const Grid& g, const float* __restric
     float a1[1][CH] = {{acc[0][0], acc[0][1], acc[0][2], acc[0][3]}};
     block_partials_chunk<1, float>(a1, partials, c0, ncomp);
   }
+  finish_stage(st, partials, S, ncomp);
 }
 
 // v = (A D^-1) p, partial r0.v
 __global__ void __launch_bounds__(TPB) spmv_dot_kernel(Grid g, const float* __restrict__ Ah,
                                                        const float* __restrict__ x, const float* __restrict__ w,
-                                                       float* __restrict__ y, const double* __restrict__ S,
-                                                       int ncomp, double* __restrict__ partials) {
-  spmv_chunk<false>(g, Ah, x, w, y, S, ncomp, partials);
+                                                       float* __restrict__ y, double* __restrict__ S,
+                                                       int ncomp, double* __restrict__ partials, Stage st) {
+  spmv_chunk<false>(g, Ah, x, w, y, S, ncomp, partials, st);
 }
 
 // t = (A D^-1) s, partials (t.s, t.t)
 __global__ void __launch_bounds__(TPB) spmv_dot2_kernel(Grid g, const float* __restrict__ Ah,
                                                         const float* __restrict__ s, float* __restrict__ t,
-                                                        const double* __restrict__ S, int ncomp,
-                                                        double* __restrict__ partials) {
-  spmv_chunk<true>(g, Ah, s, nullptr, t, S, ncomp, partials);
+                                                        double* __restrict__ S, int ncomp,
+                                                        double* __restrict__ partials, Stage st) {
+  spmv_chunk<true>(g, Ah, s, nullptr, t, S, ncomp, partials, st);
 }
 
 // The vector updates run over float4 of the padded vectors (Np is a
@@ -415,7 +505,7 @@ __global__ void __launch_bounds__(TPB) spmv_dot2_kernel(Grid g, const float* __r
 // is 0 in every vector and stays 0 under these updates.
 
 // s = r - alpha v
-__global__ void axpy_s_kernel(long long Np4, const float4* __restrict__ r, const float4* __restrict__ v,
+__global__ void __launch_bounds__(TPB) axpy_s_kernel(long long Np4, const float4* __restrict__ r, const float4* __restrict__ v,
                               float4* __restrict__ s, const double* __restrict__ S, int ncomp) {
   const int c = blockIdx.y;
   if (S[ACTIVE * ncomp + c] == 0.0) return;
@@ -429,10 +519,10 @@ __global__ void axpy_s_kernel(long long Np4, const float4* __restrict__ r, const
 }
 
 // y += alpha p + omega s; r = s - omega t; partials (r0.r, r.r)
-__global__ void update_yr_kernel(long long Np4, float4* __restrict__ y, float4* __restrict__ r,
+__global__ void __launch_bounds__(TPB) update_yr_kernel(long long Np4, float4* __restrict__ y, float4* __restrict__ r,
                                  const float4* __restrict__ p, const float4* __restrict__ s,
                                  const float4* __restrict__ t, const float4* __restrict__ r0,
-                                 const double* __restrict__ S, int ncomp, double* __restrict__ partials) {
+                                 double* __restrict__ S, int ncomp, double* __restrict__ partials, Stage st) {
   const int c = blockIdx.y;
   const bool active = S[ACTIVE * ncomp + c] != 0.0;
   float acc[2] = {0.0f, 0.0f};
@@ -457,10 +547,11 @@ __global__ void update_yr_kernel(long long Np4, float4* __restrict__ y, float4* 
     }
   }
   block_partials<2, float>(acc, partials, c, ncomp);
+  finish_stage(st, partials, S, ncomp);
 }
 
 // p = r + beta (p - omega v)
-__global__ void update_p_kernel(long long Np4, float4* __restrict__ p, const float4* __restrict__ r,
+__global__ void __launch_bounds__(TPB) update_p_kernel(long long Np4, float4* __restrict__ p, const float4* __restrict__ r,
                                 const float4* __restrict__ v, const double* __restrict__ S, int ncomp) {
   const int c = blockIdx.y;
   if (S[ACTIVE * ncomp + c] == 0.0) return;
@@ -470,65 +561,6 @@ __global__ void update_p_kernel(long long Np4, float4* __restrict__ p, const flo
     const float4 pv = p[o + X], rv = r[o + X], vv = v[o + X];
     p[o + X] = make_float4(fmaf(beta, fmaf(-omega, vv.x, pv.x), rv.x), fmaf(beta, fmaf(-omega, vv.y, pv.y), rv.y),
                            fmaf(beta, fmaf(-omega, vv.z, pv.z), rv.z), fmaf(beta, fmaf(-omega, vv.w, pv.w), rv.w));
-  }
-}
-
-// Fixed-order sums of the partials (one warp per component: lane l sums
-// partials l, l+32, ..., then a fixed shuffle tree) and the scalar updates.
-// stage 0: outer residual (ORES2, and BNORM2 on the first call, first=1)
-// stage 1: inner start (RHO, RHS2, RNORM2; ACTIVE unless the component is
-//          converged in the outer sense; ITOL2: the inner target, no
-//          tighter than what brings the outer residual to rtol)
-// stage 2: alpha; stage 3: omega; stage 4: rho, beta and the inner test
-__global__ void scalar_kernel(int stage, int first, int nparts, const double* __restrict__ partials,
-                              double* __restrict__ S, int ncomp, double rtol2, double inner_rtol2) {
-  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (c >= ncomp) return;  // whole warps leave together
-  auto sum = [&](int w) {
-    double s = 0.0;
-    const double* p = partials + ((size_t)w * ncomp + c) * nparts;
-    for (int b = lane; b < nparts; b += 32) s += p[b];
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    return __shfl_sync(0xffffffffu, s, 0);
-  };
-  const bool two = stage == 0 || stage == 3 || stage == 4;
-  const double s0 = sum(0);
-  const double s1 = two ? sum(1) : 0.0;
-  if (lane != 0) return;
-  double* Sc = S + c;
-  if (stage == 0) {
-    Sc[ORES2 * ncomp] = s0;
-    Sc[RSCALE * ncomp] = sqrt(s0);
-    if (first) Sc[BNORM2 * ncomp] = s1;
-    return;
-  }
-  if (stage == 1) {
-    const bool done = Sc[ORES2 * ncomp] <= rtol2 * Sc[BNORM2 * ncomp];
-    Sc[RHO * ncomp] = s0;
-    Sc[RNORM2 * ncomp] = s0;
-    Sc[RHS2 * ncomp] = done ? 0.0 : s0;
-    Sc[ALPHA * ncomp] = 0.0;
-    Sc[OMEGA * ncomp] = 0.0;
-    Sc[BETA * ncomp] = 0.0;
-    Sc[ACTIVE * ncomp] = (!done && s0 > 0.0) ? 1.0 : 0.0;
-    const double need = INNER_SAFETY * INNER_SAFETY * rtol2 * Sc[BNORM2 * ncomp] / Sc[ORES2 * ncomp];
-    Sc[ITOL2 * ncomp] = done ? 0.0 : fmax(inner_rtol2, need);
-    return;
-  }
-  if (Sc[ACTIVE * ncomp] == 0.0) return;
-  if (stage == 2) {
-    if (s0 == 0.0) { Sc[ACTIVE * ncomp] = 0.0; Sc[ALPHA * ncomp] = 0.0; return; }  // breakdown
-    Sc[ALPHA * ncomp] = Sc[RHO * ncomp] / s0;
-  } else if (stage == 3) {
-    Sc[OMEGA * ncomp] = s1 > 0.0 ? s0 / s1 : 0.0;
-  } else {
-    const double rho_new = s0, rr = s1;
-    const double rho = Sc[RHO * ncomp], omega = Sc[OMEGA * ncomp];
-    Sc[RNORM2 * ncomp] = rr;
-    Sc[BETA * ncomp] = (rho != 0.0 && omega != 0.0) ? (rho_new / rho) * (Sc[ALPHA * ncomp] / omega) : 0.0;
-    Sc[RHO * ncomp] = rho_new;
-    if (rr <= Sc[ITOL2 * ncomp] * Sc[RHS2 * ncomp] || omega == 0.0 || rho_new == 0.0) Sc[ACTIVE * ncomp] = 0.0;
   }
 }
 
@@ -552,10 +584,11 @@ namespace {
 struct Layout {
   double *A, *invD, *x, *r64, *partials, *S;
   float *Ah, *r, *r0, *p, *v, *s, *t, *y;
+  unsigned* counter;
 };
 
 // Work space, every array on a 256-byte boundary: FP64 A[8][N], invD[N],
-// x and r64 [ncomp][Np], partials, S; FP32 Ah[6][N] and the inner solver's
+// x and r64 [ncomp][Np], partials, S; the stage counter; FP32 Ah[6][N] and the inner solver's
 // r, r0, p, v, s, t, y [ncomp][Np].  With base == nullptr only the size.
 size_t transport_layout(char* base, long long N, long long Np, int n, Layout* L) {
   size_t cur = 0;
@@ -572,6 +605,7 @@ size_t transport_layout(char* base, long long N, long long Np, int n, Layout* L)
   l.r64 = (double*)take(vec * 8);
   l.partials = (double*)take(2 * (size_t)tr::RED_BLOCKS * n * 8);
   l.S = (double*)take((size_t)tr::NSCALAR * n * 8);
+  l.counter = (unsigned*)take(4);
   l.Ah = (float*)take(6 * (size_t)N * 4);
   l.r = (float*)take(vec * 4);
   l.r0 = (float*)take(vec * 4);
@@ -656,14 +690,11 @@ extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, v
   const dim3 g_res(cap(t->gx_res), chunks), g_sp1(cap(t->gx_sp1), chunks), g_sp2(cap(t->gx_sp2), chunks);
   const dim3 g_vec(cap(t->gx_vec), (unsigned)n);
   const double rtol2 = a->rtol * a->rtol, irtol2 = INNER_RTOL * INNER_RTOL;
-  const unsigned sblocks = (unsigned)((n + 3) / 4);
-  auto scalar = [&](int stage, int first, const dim3& producer) {
-    scalar_kernel<<<sblocks, 128, 0, s>>>(stage, first, (int)producer.x, L.partials, L.S, n, rtol2, irtol2);
-  };
+  auto stage = [&](int k, int first) { return Stage{k, first, rtol2, irtol2, L.counter}; };
+  if (cudaMemsetAsync(L.counter, 0, sizeof(unsigned), s) != cudaSuccess) return PF_ERR_CUDA;
   copy_kernel<<<g_vec, TPB, 0, s>>>(N, N, Np, a->total, L.x);  // x0 = T_k
   auto outer_residual = [&](int first) {
-    residual_kernel<<<g_res, TPB, 0, s>>>(g, L.A, a->total, L.x, L.r64, n, first, L.partials);
-    scalar(0, first, g_res);
+    residual_kernel<<<g_res, TPB, 0, s>>>(g, L.A, a->total, L.x, L.r64, n, L.partials, L.S, stage(0, first));
   };
   auto fetch = [&]() {
     return cudaMemcpyAsync(t->h_scalars, L.S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) ==
@@ -682,18 +713,14 @@ extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, v
   int inner_total = 0, outer = 0;
   while (!all_done() && inner_total < a->max_iterations && outer < OUTER_MAX) {
     // FP32 correction: (A D^-1) y = r / ||r||
-    inner_init_kernel<<<g_vec, TPB, 0, s>>>(Np, L.r64, L.S, L.r, L.r0, L.p, L.y, n, L.partials);
-    scalar(1, 0, g_vec);
+    inner_init_kernel<<<g_vec, TPB, 0, s>>>(Np, L.r64, L.S, L.r, L.r0, L.p, L.y, n, L.partials, stage(1, 0));
     int it = 0;
     bool inner_done = false;
     while (!inner_done && it < INNER_MAX && inner_total < a->max_iterations) {
-      spmv_dot_kernel<<<g_sp1, TPB, 0, s>>>(g, L.Ah, L.p, L.r0, L.v, L.S, n, L.partials);
-      scalar(2, 0, g_sp1);
+      spmv_dot_kernel<<<g_sp1, TPB, 0, s>>>(g, L.Ah, L.p, L.r0, L.v, L.S, n, L.partials, stage(2, 0));
       axpy_s_kernel<<<g_vec, TPB, 0, s>>>(Np4, r4, v4, s4, L.S, n);
-      spmv_dot2_kernel<<<g_sp2, TPB, 0, s>>>(g, L.Ah, L.s, L.t, L.S, n, L.partials);
-      scalar(3, 0, g_sp2);
-      update_yr_kernel<<<g_vec, TPB, 0, s>>>(Np4, y4, r4, p4, s4, t4, z4, L.S, n, L.partials);
-      scalar(4, 0, g_vec);
+      spmv_dot2_kernel<<<g_sp2, TPB, 0, s>>>(g, L.Ah, L.s, L.t, L.S, n, L.partials, stage(3, 0));
+      update_yr_kernel<<<g_vec, TPB, 0, s>>>(Np4, y4, r4, p4, s4, t4, z4, L.S, n, L.partials, stage(4, 0));
       update_p_kernel<<<g_vec, TPB, 0, s>>>(Np4, p4, r4, v4, L.S, n);
       ++it;
       ++inner_total;
