@@ -357,6 +357,69 @@ def build_c3(cells_per_network, device, seed=3000):
     return members
 
 
+def grid_dims(n):
+    """(nx, ny, nz) with nx*ny*nz = n, as close to a cube as the divisors of n
+    allow (nx >= ny >= nz)."""
+    best = (n, 1, 1)
+    z = 1
+    while z * z * z <= n:
+        if n % z == 0:
+            m = n // z
+            y = int(m ** 0.5)
+            while y >= z and m % y:
+                y -= 1
+            if y >= z and max(m // y, y, z) < max(best):
+                best = (m // y, y, z)
+        z += 1
+    return best
+
+
+def transport_launches(stage):
+    """Kernel launches of one fixed-schedule transport solve: coefficients,
+    scaling, start copy, first residual; per cycle the inner start, five
+    kernels per inner iteration, the FP64 update and residual; final copy."""
+    return 4 + stage.refinements * (1 + 5 * stage.inner_iterations + 2) + 1
+
+
+def c3_transport(members, seed=4000):
+    """A structured grid per network (unit cells, Darcy flux U[1e-7, 1e-5]
+    m/s with random sign, D_m = 1e-9 m^2/s), uniform dt = 1 day instead of
+    the per-cell dt, and a fixed transport schedule from one adaptive step
+    (taken on a copy of the totals)."""
+    import numpy as np
+    import torch
+
+    from pfgpu.girt import StructuredGrid
+    from pfgpu.network import CellState
+    from pfgpu.timeloop import TransportStage
+    from pfgpu.transport import OSTransport
+    stages, info = [], []
+    for i, (eng, dev) in enumerate(members):
+        dev.a.pop("dt_cell", None)
+        nx, ny, nz = grid_dims(dev.ncells)
+        rng = np.random.default_rng(seed + i)
+
+        def q(shape):
+            return rng.uniform(1e-7, 1e-5, shape) * rng.choice([-1.0, 1.0], shape)
+        grid = StructuredGrid(nx, ny, nz, 1.0, 1.0, 1.0, q((nz, ny, nx - 1)), q((nz, ny - 1, nx)),
+                              q((nz - 1, ny, nx)), diffusion=1e-9, tortuosity=1.0, dispersivity=0.0)
+        solver = OSTransport(grid, eng.net.ncomp)
+        probe = CellState.__new__(CellState)
+        probe.net, probe.ncells = dev.net, dev.ncells
+        probe.a = {k: dev.a[k] for k in ("porosity", "saturation", "volume")}
+        probe.a["total"] = dev.a["total"].clone()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        stats = solver.step(probe, 86400.0)
+        torch.cuda.synchronize()
+        inner, refs = OSTransport.schedule(stats)
+        stages.append(TransportStage(solver, inner, refs))
+        info.append(dict(ncomp=eng.net.ncomp, grid="%dx%dx%d" % (nx, ny, nz), adaptive_ms=1e3 * (time.perf_counter() - t),
+                         adaptive_iterations=stats["iterations"], adaptive_refinements=stats["refinements"],
+                         schedule=[inner, refs]))
+    return stages, info
+
+
 def run_c3(args):
     """Heterogeneous batching: 8 networks, per-cell dt, 50 operator-split
     steps (RTUpdateAuxVars + TIMESTEP activities + RStep per network) in one
@@ -371,6 +434,11 @@ def run_c3(args):
     t0 = time.perf_counter()
     members = build_c3(per, "cuda")
     log("c3 state built: %d x %d cells in %.1f s" % (len(members), per, time.perf_counter() - t0))
+    stages = [None] * len(members)
+    transport_info = None
+    if args.transport:
+        stages, transport_info = c3_transport(members)
+        log("c3 transport:", json.dumps(transport_info))
     tuned = {}
     for eng, dev in members:
         if args.no_tune:
@@ -412,7 +480,8 @@ def run_c3(args):
     plain_first = sum(r["plain_ms"] for r in per_net)
     # one eager warm step of the loop (its Newton counts order the first graph step)
     reset(start)
-    loop = OperatorSplitLoop(members, dt=86400.0, concurrent=args.concurrent)
+    loop = OperatorSplitLoop([(eng, dev, tr) for (eng, dev), tr in zip(members, stages)], dt=86400.0,
+                             concurrent=args.concurrent)
     loop.step()
     torch.cuda.synchronize()
     s0 = [{k: dev.a[k].clone() for k in fields if k in dev.a} for _, dev in members]
@@ -436,15 +505,19 @@ def run_c3(args):
             "ms_per_step": g / nsteps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": "8 synthetic networks ncomp %s, 3*ncomp complexes, ncomp/2 kinetic minerals, "
-                                   "%d cells each, per-cell dt log-U[1 h, 30 d], T U[5,60] C" % (C3_NCOMP, per),
+                                   "%d cells each, %s, T U[5,60] C" % (
+                                       C3_NCOMP, per, "structured grid per network, transport solve + reaction "
+                                       "each step, dt 1 d" if args.transport else "per-cell dt log-U[1 h, 30 d]"),
                        "graph_steps": nsteps, "concurrent_streams": bool(args.concurrent),
                        "l2": "state > L2; reset D2D before each replay, outside the timed region"},
             "graph_ms": g, "eager_ms_per_step": eager_ms / k_e,
             "first_step": {"batched_ms": batched_first, "plain_ms": plain_first,
                            "speedup_vs_plain_gpu": plain_first / batched_first, "per_network": per_net},
-            "last_step": summary, "autotune": tuned, "clocks": clk.summary(),
+            "last_step": summary, "autotune": tuned, "clocks": clk.summary(), "transport": transport_info,
             # per network per step: auxvars, activities, setup pre-pass, persistent kernel
-            "gpu_launches": len(graph_ms) * nsteps * 4 * len(members)}
+            # (+ the transport schedule's launches)
+            "gpu_launches": len(graph_ms) * nsteps * (4 * len(members) + sum(
+                transport_launches(tr) for tr in stages if tr is not None))}
     print(json.dumps(line), flush=True)
 
 
@@ -608,6 +681,9 @@ def main():
                          "c5: only the global-implicit assembly on 128x128x64 cells")
     ap.add_argument("--graph-steps", type=int, default=50, help="c3: operator-split steps in the graph")
     ap.add_argument("--concurrent", action="store_true", help="c3: one stream per network inside the graph")
+    ap.add_argument("--transport", action="store_true",
+                    help="c3: each network on a structured grid, transport solve before every reaction step "
+                         "(uniform dt = 1 day)")
     ap.add_argument("--cells", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -390,7 +390,7 @@ typedef struct PfTransportStats {
   int32_t converged;                 /* 1 when every component met rtol */
   double max_rel_residual;           /* max over components of the FP64 ||b - A x|| / ||b|| */
   int32_t refinements;               /* FP64 refinement cycles (residual, inner solve, update) */
-  int32_t reserved;
+  int32_t max_cycle_iterations;      /* most inner iterations any component took in one cycle */
 } PfTransportStats;
 
 typedef struct PfTransport PfTransport;  /* opaque: device work space of one grid */
@@ -401,6 +401,18 @@ int32_t pf_transport_destroy(PfTransport* t);
  * the last iterate) or PF_ERR_*. */
 int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* args, void* stream,
                           PfTransportStats* stats);
+/* The same solve with a fixed schedule: `refinements` cycles of
+ * `inner_iterations` inner iterations, enqueued on `stream` with no host
+ * synchronisation (capturable in a CUDA graph; converged components make
+ * the remaining work no-ops).  args->max_iterations is not used.  Returns
+ * PF_OK once enqueued; pf_transport_read_stats then reports whether the
+ * schedule met args->rtol (pf_transport_step's stats give a schedule:
+ * refinements + 1 cycles of max_cycle_iterations + 2). */
+int32_t pf_transport_enqueue(PfTransport* t, const PfTransportArgs* args, int32_t inner_iterations,
+                             int32_t refinements, void* stream);
+/* Synchronises `stream` and fills stats from the last solve's device
+ * counters: PF_OK if every component met rtol, else PF_CELL_FAILURES. */
+int32_t pf_transport_read_stats(PfTransport* t, double rtol, void* stream, PfTransportStats* stats);
 
 /* ----------------------------------------------------------- constraints */
 /* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */

@@ -53,7 +53,9 @@ struct Grid {
 };
 
 // per-component scalars, one device array S[field][c]
-enum Scalar { RHO = 0, ALPHA, OMEGA, BETA, BNORM2, RNORM2, ACTIVE, ORES2, RHS2, RSCALE, ITOL2, NSCALAR };
+enum Scalar { RHO = 0, ALPHA, OMEGA, BETA, BNORM2, RNORM2, ACTIVE, ORES2, RHS2, RSCALE, ITOL2,
+              ITS, REFS, CYC, MAXCYC,  // counters: inner iterations, cycles, per cycle
+              NSCALAR };
 
 __device__ __forceinline__ void cell_ijk(const Grid& g, long long X, int& i, int& j, int& k) {
   const unsigned ux = (unsigned)X, unx = (unsigned)g.nx, uny = (unsigned)g.ny;
@@ -219,7 +221,12 @@ __device__ __noinline__ void scalar_component(int stage, int first, int nparts, 
   if (stage == 0) {
     Sc[ORES2 * ncomp] = s0;
     Sc[RSCALE * ncomp] = sqrt(s0);
-    if (first) Sc[BNORM2 * ncomp] = s1;
+    if (first) {
+      Sc[BNORM2 * ncomp] = s1;
+      Sc[ITS * ncomp] = 0.0;
+      Sc[REFS * ncomp] = 0.0;
+      Sc[MAXCYC * ncomp] = 0.0;
+    }
     return;
   }
   if (stage == 1) {
@@ -233,10 +240,15 @@ __device__ __noinline__ void scalar_component(int stage, int first, int nparts, 
     Sc[ACTIVE * ncomp] = (!done && s0 > 0.0) ? 1.0 : 0.0;
     const double need = INNER_SAFETY * INNER_SAFETY * rtol2 * Sc[BNORM2 * ncomp] / Sc[ORES2 * ncomp];
     Sc[ITOL2 * ncomp] = done ? 0.0 : fmax(inner_rtol2, need);
+    Sc[CYC * ncomp] = 0.0;
+    if (!done) Sc[REFS * ncomp] += 1.0;
     return;
   }
   if (Sc[ACTIVE * ncomp] == 0.0) return;
   if (stage == 2) {
+    Sc[ITS * ncomp] += 1.0;  // an inner iteration of this component starts
+    Sc[CYC * ncomp] += 1.0;
+    Sc[MAXCYC * ncomp] = fmax(Sc[MAXCYC * ncomp], Sc[CYC * ncomp]);
     if (s0 == 0.0) { Sc[ACTIVE * ncomp] = 0.0; Sc[ALPHA * ncomp] = 0.0; return; }  // breakdown
     Sc[ALPHA * ncomp] = Sc[RHO * ncomp] / s0;
   } else if (stage == 3) {
@@ -665,15 +677,56 @@ extern "C" int32_t pf_transport_destroy(PfTransport* t) {
   return PF_OK;
 }
 
-extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, void* stream, PfTransportStats* stats) {
+namespace {
+// Device counters and residuals of the last solve -> stats (synchronises s).
+int32_t read_stats(PfTransport* t, cudaStream_t s, double rtol, PfTransportStats* stats, bool* conv_out) {
   using namespace tr;
+  const int n = t->ncomp;
+  Layout L;
+  transport_layout(static_cast<char*>(t->buf), t->N, t->Np, n, &L);
+  if (cudaMemcpyAsync(t->h_scalars, L.S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return PF_ERR_CUDA;
+  const double* h = t->h_scalars;
+  double worst = 0.0, its = 0.0, refs = 0.0, cyc = 0.0;
+  bool conv = true;
+  for (int c = 0; c < n; ++c) {
+    const double bb = h[BNORM2 * n + c], rr = h[ORES2 * n + c];
+    const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+    worst = rel > worst ? rel : worst;
+    conv = conv && !(rel > rtol);
+    its = fmax(its, h[ITS * n + c]);
+    refs = fmax(refs, h[REFS * n + c]);
+    cyc = fmax(cyc, h[MAXCYC * n + c]);
+  }
+  if (stats) {
+    stats->iterations = (int32_t)its;
+    stats->max_rel_residual = worst;
+    stats->converged = conv ? 1 : 0;
+    stats->refinements = (int32_t)refs;
+    stats->max_cycle_iterations = (int32_t)cyc;
+  }
+  if (conv_out) *conv_out = conv;
+  return PF_OK;
+}
+
+int32_t check_args(const PfTransport* t, const PfTransportArgs* a) {
   if (!t || !a) return PF_ERR_INVALID;
   if (a->nx != t->nx || a->ny != t->ny || a->nz != t->nz || a->ncomp != t->ncomp) return PF_ERR_INVALID;
   if (!(a->dt > 0.0) || !(a->dx > 0.0) || !(a->dy > 0.0) || !(a->dz > 0.0) || !a->total || !a->porosity ||
       !a->saturation || !a->volume || a->max_iterations < 1 || !(a->rtol > 0.0))
     return PF_ERR_INVALID;
   if ((t->nx > 1 && !a->qx) || (t->ny > 1 && !a->qy) || (t->nz > 1 && !a->qz)) return PF_ERR_INVALID;
-  cudaStream_t s = (cudaStream_t)stream;
+  return PF_OK;
+}
+
+// The solve.  fixed_inner == 0: adaptive, the host checks convergence every
+// two inner iterations and after every refinement.  fixed_inner > 0: exactly
+// fixed_cycles refinement cycles of fixed_inner inner iterations each, no
+// host synchronisation (capturable in a CUDA graph); components that have
+// converged make the remaining launches no-ops.
+int32_t transport_run(PfTransport* t, const PfTransportArgs* a, cudaStream_t s, int fixed_inner, int fixed_cycles) {
+  using namespace tr;
   const long long N = t->N, Np = t->Np, Np4 = Np / 4;
   const int n = t->ncomp;
   Layout L;
@@ -708,20 +761,38 @@ extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, v
   };
   float4 *r4 = (float4*)L.r, *p4 = (float4*)L.p, *v4 = (float4*)L.v, *s4 = (float4*)L.s, *t4 = (float4*)L.t,
          *y4 = (float4*)L.y, *z4 = (float4*)L.r0;
+  auto inner_iteration = [&]() {
+    spmv_dot_kernel<<<g_sp1, TPB, 0, s>>>(g, L.Ah, L.p, L.r0, L.v, L.S, n, L.partials, stage(2, 0));
+    axpy_s_kernel<<<g_vec, TPB, 0, s>>>(Np4, r4, v4, s4, L.S, n);
+    spmv_dot2_kernel<<<g_sp2, TPB, 0, s>>>(g, L.Ah, L.s, L.t, L.S, n, L.partials, stage(3, 0));
+    update_yr_kernel<<<g_vec, TPB, 0, s>>>(Np4, y4, r4, p4, s4, t4, z4, L.S, n, L.partials, stage(4, 0));
+    update_p_kernel<<<g_vec, TPB, 0, s>>>(Np4, p4, r4, v4, L.S, n);
+  };
+  auto cycle_start = [&]() {  // FP32 correction: (A D^-1) y = r / ||r||
+    inner_init_kernel<<<g_vec, TPB, 0, s>>>(Np, L.r64, L.S, L.r, L.r0, L.p, L.y, n, L.partials, stage(1, 0));
+  };
+  auto cycle_end = [&]() {  // FP64: x += ||r|| D^-1 y, new residual
+    update64_kernel<<<g_vec, TPB, 0, s>>>(N, Np, L.invD, L.y, L.x, L.S, n);
+    outer_residual(0);
+  };
   outer_residual(1);
+  if (fixed_inner > 0) {
+    for (int cyc = 0; cyc < fixed_cycles; ++cyc) {
+      cycle_start();
+      for (int it = 0; it < fixed_inner; ++it) inner_iteration();
+      cycle_end();
+    }
+    copy_kernel<<<g_vec, TPB, 0, s>>>(N, Np, N, L.x, a->total);
+    return cudaGetLastError() == cudaSuccess ? PF_OK : PF_ERR_CUDA;
+  }
   if (cudaGetLastError() != cudaSuccess || !fetch()) return PF_ERR_CUDA;
   int inner_total = 0, outer = 0;
   while (!all_done() && inner_total < a->max_iterations && outer < OUTER_MAX) {
-    // FP32 correction: (A D^-1) y = r / ||r||
-    inner_init_kernel<<<g_vec, TPB, 0, s>>>(Np, L.r64, L.S, L.r, L.r0, L.p, L.y, n, L.partials, stage(1, 0));
+    cycle_start();
     int it = 0;
     bool inner_done = false;
     while (!inner_done && it < INNER_MAX && inner_total < a->max_iterations) {
-      spmv_dot_kernel<<<g_sp1, TPB, 0, s>>>(g, L.Ah, L.p, L.r0, L.v, L.S, n, L.partials, stage(2, 0));
-      axpy_s_kernel<<<g_vec, TPB, 0, s>>>(Np4, r4, v4, s4, L.S, n);
-      spmv_dot2_kernel<<<g_sp2, TPB, 0, s>>>(g, L.Ah, L.s, L.t, L.S, n, L.partials, stage(3, 0));
-      update_yr_kernel<<<g_vec, TPB, 0, s>>>(Np4, y4, r4, p4, s4, t4, z4, L.S, n, L.partials, stage(4, 0));
-      update_p_kernel<<<g_vec, TPB, 0, s>>>(Np4, p4, r4, v4, L.S, n);
+      inner_iteration();
       ++it;
       ++inner_total;
       if (it % 2 == 0) {
@@ -730,28 +801,39 @@ extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, v
         for (int c = 0; c < n; ++c) inner_done = inner_done && t->h_scalars[ACTIVE * n + c] == 0.0;
       }
     }
-    // FP64: x += ||r|| D^-1 y, new residual
-    update64_kernel<<<g_vec, TPB, 0, s>>>(N, Np, L.invD, L.y, L.x, L.S, n);
-    outer_residual(0);
+    cycle_end();
     if (cudaGetLastError() != cudaSuccess || !fetch()) return PF_ERR_CUDA;
     ++outer;
   }
   copy_kernel<<<g_vec, TPB, 0, s>>>(N, Np, N, L.x, a->total);
-  if (cudaGetLastError() != cudaSuccess || !fetch()) return PF_ERR_CUDA;
-  double worst = 0.0;
-  bool conv = true;
-  for (int c = 0; c < n; ++c) {
-    const double bb = t->h_scalars[BNORM2 * n + c], rr = t->h_scalars[ORES2 * n + c];
-    const double rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
-    worst = rel > worst ? rel : worst;
-    conv = conv && !(rel > a->rtol);
-  }
-  if (stats) {
-    stats->iterations = inner_total;
-    stats->max_rel_residual = worst;
-    stats->converged = conv ? 1 : 0;
-    stats->refinements = outer;
-    stats->reserved = 0;
-  }
+  return cudaGetLastError() == cudaSuccess ? PF_OK : PF_ERR_CUDA;
+}
+}  // namespace
+
+extern "C" int32_t pf_transport_step(PfTransport* t, const PfTransportArgs* a, void* stream, PfTransportStats* stats) {
+  const int32_t chk = check_args(t, a);
+  if (chk != PF_OK) return chk;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int32_t rc = transport_run(t, a, s, 0, 0);
+  if (rc != PF_OK) return rc;
+  bool conv = false;
+  const int32_t rs = read_stats(t, s, a->rtol, stats, &conv);
+  if (rs != PF_OK) return rs;
+  return conv ? PF_OK : PF_CELL_FAILURES;
+}
+
+extern "C" int32_t pf_transport_enqueue(PfTransport* t, const PfTransportArgs* a, int32_t inner_iterations,
+                                        int32_t refinements, void* stream) {
+  const int32_t chk = check_args(t, a);
+  if (chk != PF_OK) return chk;
+  if (inner_iterations < 1 || inner_iterations > 10000 || refinements < 1 || refinements > 100) return PF_ERR_INVALID;
+  return transport_run(t, a, (cudaStream_t)stream, inner_iterations, refinements);
+}
+
+extern "C" int32_t pf_transport_read_stats(PfTransport* t, double rtol, void* stream, PfTransportStats* stats) {
+  if (!t || !(rtol > 0.0)) return PF_ERR_INVALID;
+  bool conv = false;
+  const int32_t rs = read_stats(t, (cudaStream_t)stream, rtol, stats, &conv);
+  if (rs != PF_OK) return rs;
   return conv ? PF_OK : PF_CELL_FAILURES;
 }

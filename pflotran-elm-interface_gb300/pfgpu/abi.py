@@ -137,7 +137,7 @@ class PfTransportArgs(C.Structure):
 
 class PfTransportStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("max_rel_residual", C.c_double),
-                ("refinements", C.c_int32), ("reserved", C.c_int32)]
+                ("refinements", C.c_int32), ("max_cycle_iterations", C.c_int32)]
 
 
 class PfLaunchConfig(C.Structure):
@@ -168,6 +168,8 @@ SIGNATURES = {
     "pf_transport_create": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_P)]),
     "pf_transport_destroy": (C.c_int32, [_P]),
     "pf_transport_step": (C.c_int32, [_P, C.POINTER(PfTransportArgs), _P, C.POINTER(PfTransportStats)]),
+    "pf_transport_enqueue": (C.c_int32, [_P, C.POINTER(PfTransportArgs), C.c_int32, C.c_int32, _P]),
+    "pf_transport_read_stats": (C.c_int32, [_P, C.c_double, _P, C.POINTER(PfTransportStats)]),
     "pf_girt_assemble": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(PfGirtArgs), _P]),
     "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,

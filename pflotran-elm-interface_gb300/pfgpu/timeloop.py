@@ -5,7 +5,8 @@ One operator-split time step of PFLOTRAN's OSRT mode does, for the cells
 
     RTUpdateAuxVars(cells, act coefs = F)        totals from pri_molal
     RTUpdateActivityCoefficients                 when the frequency is TIMESTEP
-    (transport solve of the totals)              not part of this path
+    transport solve of the totals                optional (TransportStage,
+                                                 pmc_subsurface_osrt.F90:259-330)
     RStep in every cell                          the reaction step
 
 `OperatorSplitLoop` runs that sequence for one or more reaction networks
@@ -13,28 +14,44 @@ One operator-split time step of PFLOTRAN's OSRT mode does, for the cells
 chemical systems), with the batched kernel's work queue ordered by the
 previous step's Newton counts (longest cells first).  `capture(nsteps)`
 records `nsteps` consecutive steps of every network into one CUDA graph;
-`replay()` launches it.  Nothing in a step synchronises with the host, so
-the graph holds the whole time loop; the per-cell status and iteration
-arrays carry the results out.
+`replay()` launches it.  Nothing in a step synchronises with the host (the
+transport solve runs a fixed schedule, pf_transport_enqueue), so the graph
+holds the whole time loop; the per-cell status and iteration arrays and the
+transport solver's counters carry the results out.
 """
 from __future__ import annotations
 
+from dataclasses import dataclass
+
 from . import abi
+
+
+@dataclass
+class TransportStage:
+    """The transport solve of a member's totals before its reaction step: a
+    pfgpu.transport.OSTransport on the member's grid and a fixed schedule
+    (OSTransport.schedule() of an adaptive step gives one)."""
+    solver: object
+    inner_iterations: int
+    refinements: int
+    rtol: float = 1e-10
 
 
 class OperatorSplitLoop:
     def __init__(self, members, dt: float = 0.0, kernel: int = abi.PF_KERNEL_BATCHED, cost_order: bool = True,
                  concurrent: bool = False):
-        """members: sequence of (ReactionEngine, CellState on the device).
-        dt: uniform step [s]; ignored for states that carry a per-cell dt.
+        """members: sequence of (ReactionEngine, CellState on the device) or
+        (ReactionEngine, CellState, TransportStage).
+        dt: uniform step [s]; ignored by the reaction step of states that
+        carry a per-cell dt; a member with transport needs dt > 0.
         concurrent: run each member's step on its own stream (forked from
         and joined back into the calling stream every step), so that one
         network's queue tail overlaps the next network's work."""
-        self.members = list(members)
+        self.members = [tuple(m) if len(m) == 3 else (m[0], m[1], None) for m in members]
         self.dt = float(dt)
-        for _, st in self.members:
-            if not self.dt > 0.0 and st.a.get("dt_cell") is None:
-                raise ValueError("dt must be > 0 for states without a per-cell dt")
+        for _, st, tr in self.members:
+            if not self.dt > 0.0 and (st.a.get("dt_cell") is None or tr is not None):
+                raise ValueError("dt must be > 0 for states without a per-cell dt and for transport")
         self.kernel = kernel
         self.cost_order = cost_order
         self.graph = None
@@ -48,10 +65,12 @@ class OperatorSplitLoop:
             return None
         return torch.argsort(st.a["newton_its"].to(torch.int64), descending=True)
 
-    def _member_step(self, eng, st):
+    def _member_step(self, eng, st, tr):
         eng.update_auxvars(st, False)
         if eng.net.options["act_coef_update_frequency"] == abi.PF_ACT_COEF_TIMESTEP:
             eng.update_activity_coefs(st)
+        if tr is not None:
+            tr.solver.enqueue(st, self.dt, tr.inner_iterations, tr.refinements, tr.rtol)
         # a state's per-cell dt array, when present, overrides dt
         dt = self.dt if self.dt > 0.0 else 1.0
         eng.rstep(st, dt, kernel=self.kernel, stats=False, order=self._order(st))
@@ -62,8 +81,8 @@ class OperatorSplitLoop:
         back into it); no host synchronisation."""
         import torch
         if not self.concurrent:
-            for eng, st in self.members:
-                self._member_step(eng, st)
+            for eng, st, tr in self.members:
+                self._member_step(eng, st, tr)
             return
         main = torch.cuda.current_stream()
         if self._streams is None:
@@ -71,10 +90,10 @@ class OperatorSplitLoop:
         fork = torch.cuda.Event()
         fork.record(main)
         joins = []
-        for (eng, st), s in zip(self.members, self._streams):
+        for (eng, st, tr), s in zip(self.members, self._streams):
             s.wait_event(fork)
             with torch.cuda.stream(s):
-                self._member_step(eng, st)
+                self._member_step(eng, st, tr)
                 ev = torch.cuda.Event()
                 ev.record(s)
                 joins.append(ev)
@@ -88,7 +107,7 @@ class OperatorSplitLoop:
         kernels' launch attributes).  Capturing enqueues no work: the state
         is unchanged until replay()."""
         import torch
-        for eng, st in self.members:
+        for eng, st, _ in self.members:
             eng.reserve(st.ncells)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
@@ -106,9 +125,12 @@ class OperatorSplitLoop:
         """Host reduction of the per-cell outputs of the last step (the
         reference's rstep_error MAX and iteration sums)."""
         out = []
-        for eng, st in self.members:
+        for eng, st, tr in self.members:
             its = st.a["newton_its"]
-            out.append(dict(ncomp=eng.net.ncomp, cells=st.ncells, failed_cells=int((st.a["status"] != 0).sum()),
-                            newton_iterations=int(its.sum()), max_newton_iterations=int(its.max()),
-                            max_substeps=int(st.a["num_substeps"].max())))
+            row = dict(ncomp=eng.net.ncomp, cells=st.ncells, failed_cells=int((st.a["status"] != 0).sum()),
+                       newton_iterations=int(its.sum()), max_newton_iterations=int(its.max()),
+                       max_substeps=int(st.a["num_substeps"].max()))
+            if tr is not None:
+                row["transport"] = tr.solver.read_stats(tr.rtol)
+            out.append(row)
         return out

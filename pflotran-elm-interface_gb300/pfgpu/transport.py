@@ -43,10 +43,7 @@ class OSTransport:
         except Exception:
             pass
 
-    def step(self, state, dt: float, rtol: float = 1e-10, max_iterations: int = 1000, stream=None) -> dict:
-        """Transport the totals of `state` (a CellState of CUDA tensors on
-        this grid) over dt, in place.  Returns the solver statistics; raises
-        PfError if the solve did not converge within max_iterations."""
+    def _args(self, state, dt: float, rtol: float, max_iterations: int):
         import torch
         g = self.grid
         N = g.nx * g.ny * g.nz
@@ -67,7 +64,44 @@ class OSTransport:
         a.total = C.cast(state.a["total"].data_ptr(), dp)
         a.rtol = float(rtol)
         a.max_iterations = int(max_iterations)
+        return a
+
+    @staticmethod
+    def _stats(st):
+        return {k: getattr(st, k) for k, _ in abi.PfTransportStats._fields_}
+
+    def step(self, state, dt: float, rtol: float = 1e-10, max_iterations: int = 1000, stream=None) -> dict:
+        """Transport the totals of `state` (a CellState of CUDA tensors on
+        this grid) over dt, in place.  Returns the solver statistics; raises
+        PfError if the solve did not converge within max_iterations."""
+        a = self._args(state, dt, rtol, max_iterations)
         st = abi.PfTransportStats()
         rc = self.lib.pf_transport_step(self.handle, C.byref(a), _stream_ptr(stream), C.byref(st))
         abi.check("pf_transport_step", rc, allow_cell_failures=False)
-        return {k: getattr(st, k) for k, _ in abi.PfTransportStats._fields_}
+        return self._stats(st)
+
+    def enqueue(self, state, dt: float, inner_iterations: int, refinements: int, rtol: float = 1e-10,
+                stream=None) -> None:
+        """The same solve with a fixed schedule (refinements cycles of
+        inner_iterations inner iterations), enqueued without host
+        synchronisation, so that it can be captured in a CUDA graph.  The
+        pointers of `state` are baked into a captured graph.  Check the
+        outcome with read_stats()."""
+        a = self._args(state, dt, rtol, 1)
+        abi.check("pf_transport_enqueue",
+                  self.lib.pf_transport_enqueue(self.handle, C.byref(a), int(inner_iterations), int(refinements),
+                                                _stream_ptr(stream)), allow_cell_failures=False)
+
+    def read_stats(self, rtol: float = 1e-10, stream=None) -> dict:
+        """Statistics of the last solve (synchronises the stream); key
+        'converged' tells whether a fixed schedule met rtol."""
+        st = abi.PfTransportStats()
+        rc = self.lib.pf_transport_read_stats(self.handle, float(rtol), _stream_ptr(stream), C.byref(st))
+        abi.check("pf_transport_read_stats", rc, allow_cell_failures=True)
+        return self._stats(st)
+
+    @staticmethod
+    def schedule(stats: dict) -> tuple:
+        """A fixed schedule (inner_iterations, refinements) with margin from
+        an adaptive step's statistics."""
+        return int(stats["max_cycle_iterations"]) + 2, int(stats["refinements"]) + 1

@@ -141,3 +141,78 @@ def test_gpu_transport_reports_non_convergence(oracle):
     from pfgpu import abi
     with pytest.raises(abi.PfError):
         _gpu_case(oracle, (10, 7, 6), 3, seed=5, max_iterations=2)
+
+
+def _state(dims, ncomp, seed):
+    torch = pytest.importorskip("torch")
+    from pfgpu.network import CellState
+    N = int(np.prod(dims))
+    por, sat, vol = _cells(N, seed + 1)
+    rng = np.random.default_rng(seed + 2)
+    T0 = 10.0 ** rng.uniform(-6, -2, (ncomp, N))
+    st = CellState.__new__(CellState)
+    st.a = {"porosity": torch.from_numpy(por).cuda(), "saturation": torch.from_numpy(sat).cuda(),
+            "volume": torch.from_numpy(vol).cuda(), "total": torch.from_numpy(T0.copy()).cuda()}
+    st.ncells, st.net = N, None
+    return st, T0
+
+
+@pytest.mark.gpu
+def test_gpu_fixed_schedule_equals_adaptive():
+    """pf_transport_enqueue with the schedule an adaptive step suggests gives
+    bit for bit the adaptive step's totals (converged components make the
+    extra launches no-ops); a schedule that is too short is reported by
+    pf_transport_read_stats, and it leaves a partly converged answer."""
+    torch = pytest.importorskip("torch")
+    from pfgpu.girt import StructuredGrid
+    from pfgpu.transport import OSTransport
+    dims, ncomp = (12, 9, 7), 6
+    tr = OSTransport(StructuredGrid(**_grid(*dims, seed=41)), ncomp)
+    st, T0 = _state(dims, ncomp, 42)
+    stats = tr.step(st, 86400.0, rtol=1e-12)
+    ref = st.a["total"].clone()
+    inner, refs = OSTransport.schedule(stats)
+    assert stats["converged"] == 1 and stats["iterations"] >= stats["max_cycle_iterations"] >= 1
+    st.a["total"].copy_(torch.from_numpy(T0))
+    tr.enqueue(st, 86400.0, inner, refs, rtol=1e-12)
+    fixed = tr.read_stats(1e-12)
+    assert fixed["converged"] == 1
+    assert fixed["iterations"] == stats["iterations"] and fixed["refinements"] == stats["refinements"]
+    assert torch.equal(st.a["total"], ref)
+    st.a["total"].copy_(torch.from_numpy(T0))
+    tr.enqueue(st, 86400.0, 1, 1, rtol=1e-12)
+    short = tr.read_stats(1e-12)
+    assert short["converged"] == 0 and short["max_rel_residual"] > 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_fixed_schedule_in_cuda_graph():
+    """The fixed schedule captured in a CUDA graph and replayed equals the
+    same schedule enqueued eagerly."""
+    torch = pytest.importorskip("torch")
+    from pfgpu.girt import StructuredGrid
+    from pfgpu.transport import OSTransport
+    dims, ncomp = (16, 8, 8), 5
+    tr = OSTransport(StructuredGrid(**_grid(*dims, seed=51)), ncomp)
+    st, T0 = _state(dims, ncomp, 52)
+    tr.enqueue(st, 3600.0, 12, 3)
+    tr.enqueue(st, 3600.0, 12, 3)
+    torch.cuda.synchronize()
+    eager = st.a["total"].clone()
+    st.a["total"].copy_(torch.from_numpy(T0))
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):  # warm-up outside the capture
+        tr.enqueue(st, 3600.0, 12, 3)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    st.a["total"].copy_(torch.from_numpy(T0))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        tr.enqueue(st, 3600.0, 12, 3)
+        tr.enqueue(st, 3600.0, 12, 3)
+    st.a["total"].copy_(torch.from_numpy(T0))
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(st.a["total"], eager)
+    assert tr.read_stats(1e-10)["converged"] == 1
