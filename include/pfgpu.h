@@ -415,14 +415,30 @@ int32_t pf_transport_enqueue(PfTransport* t, const PfTransportArgs* args, int32_
 int32_t pf_transport_read_stats(PfTransport* t, double rtol, void* stream, PfTransportStats* stats);
 
 /* ----------------------------------------------------------- constraints */
-/* Aqueous constraint types (transport_constraint_rt.F90:22-34 subset). */
+/* Constraint types (transport_constraint_rt.F90:22-34 subset). */
 enum {
   PF_CONSTRAINT_TOTAL = 1,
   PF_CONSTRAINT_FREE = 2,
   PF_CONSTRAINT_PH = 3,
   PF_CONSTRAINT_CHARGE_BAL = 4,
-  PF_CONSTRAINT_LOG = 5
+  PF_CONSTRAINT_LOG = 5,
+  PF_CONSTRAINT_MINERAL = 6,  /* equilibrium with a mineral: ln(Q/K) = 0 (reaction.F90:1755-1779) */
+  PF_CONSTRAINT_GAS = 7       /* a gas partial pressure: ln(Q/K) = ln p (reaction.F90:1781-1811) */
 };
+
+/* The reaction of a MINERAL or GAS constraint row: the mineral's or gas's
+ * reaction in the primary species (water dropped, its activity is one), as
+ * the reference holds it in mineral%mnrlspecid/mnrlstoich/mnrl_logK and
+ * gas%paseqspecid/paseqstoich/paseqlogK.  Any mineral or gas of the
+ * database, kinetic or not. */
+typedef struct PfConstraintReaction {
+  int32_t nspec;                  /* species in the reaction, 1..ncomp */
+  int32_t temperature_dependent;  /* 1: logK from logKcoef at the cell temperature */
+  int32_t spec[PF_MAX_NCOMP];     /* primary indices, 0-based */
+  double stoich[PF_MAX_NCOMP];
+  double logK;                    /* used when temperature_dependent = 0 */
+  double logKcoef[5];             /* c1 ln T + c2 + c3 T + c4/T + c5/T^2, T in K */
+} PfConstraintReaction;
 
 /*
  * pf_equilibrate_constraint -- ReactionEquilibrateConstraint
@@ -440,6 +456,14 @@ int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state,
                                   const int32_t* ctype, const double* cconc,
                                   int32_t use_prev_soln_as_guess,
                                   int32_t* iterations, void* stream);
+/* The same with MINERAL and GAS rows.  creact: host array [ncomp]; entry j
+ * is read only when ctype[j] is MINERAL or GAS (may be NULL when no row is).
+ * cconc for a MINERAL row: the free-ion guess (mol/L); for a GAS row: the
+ * partial pressure (bar), or its log10 when <= 0. */
+int32_t pf_equilibrate_constraint_ex(PfNetwork* net, const PfCellState* state,
+                                     const int32_t* ctype, const PfConstraintReaction* creact,
+                                     const double* cconc, int32_t use_prev_soln_as_guess,
+                                     int32_t* iterations, void* stream);
 
 /* ------------------------------------------------------------ capabilities */
 /* Kernel launch configuration for the batched form; chosen by the

@@ -49,7 +49,7 @@ class Oracle:
         lib.oracle_implicit_step.argtypes = [D, S, C.c_double, C.c_double, C.c_int]
         lib.oracle_update_auxvars.argtypes = [D, S, C.c_int, C.c_int]
         lib.oracle_update_activity_coefs.argtypes = [D, S, C.c_int]
-        lib.oracle_equilibrate.argtypes = [D, S, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+        lib.oracle_equilibrate.argtypes = [D, S, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_double),
                                            C.c_int, C.POINTER(C.c_int32), C.c_int]
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
         lib.oracle_girt_assemble.argtypes = [D, S, ip, dp, dp, dp, dp, dp, C.c_double, ip, ip, dp, dp]
@@ -91,13 +91,19 @@ class Oracle:
         d, s = self._args(net, state)
         return self.lib.oracle_update_activity_coefs(C.byref(d), C.byref(s), nthreads)
 
-    def equilibrate(self, net, state, ctype, cconc, use_prev=False, nthreads=1):
+    def equilibrate(self, net, state, ctype, cconc, use_prev=False, nthreads=1, reactions=None):
+        """reactions: None, or per component a dict (species indices, stoich,
+        logK, logKcoef) for MINERAL/GAS rows (pfgpu.abi.constraint_reactions
+        builds the C array)."""
+        from pfgpu import abi
         d, s = self._args(net, state)
         ct = np.ascontiguousarray(ctype, np.int32)
         cc = np.ascontiguousarray(cconc, np.float64)
         its = np.zeros(state.ncells, np.int32)
+        cr = abi.constraint_reactions(len(ct), reactions) if reactions else None
         rc = self.lib.oracle_equilibrate(C.byref(d), C.byref(s),
                                          ct.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         C.cast(cr, C.c_void_p) if cr is not None else None,
                                          cc.ctypes.data_as(C.POINTER(C.c_double)),
                                          int(use_prev), its.ctypes.data_as(C.POINTER(C.c_int32)),
                                          nthreads)

@@ -203,8 +203,8 @@ int oracle_update_activity_coefs(const PfNetworkDesc* d, const PfCellState* s, i
 // ReactionEquilibrateConstraint subset for every cell; ctype[ncomp] shared,
 // cconc[k*ncells+i] per cell.  iterations[i] = count or -1 on failure.
 int oracle_equilibrate(const PfNetworkDesc* d, const PfCellState* s, const int32_t* ctype,
-                       const double* cconc, int use_prev_soln_as_guess, int32_t* iterations,
-                       int nthreads) {
+                       const PfConstraintReaction* creact, const double* cconc, int use_prev_soln_as_guess,
+                       int32_t* iterations, int nthreads) {
   int rc = check(d, s);
   if (rc) return rc;
   Net net(d);
@@ -216,7 +216,7 @@ int oracle_equilibrate(const PfNetworkDesc* d, const PfCellState* s, const int32
     int ct[MAXN];
     double cc[MAXN];
     for (int k = 0; k < net.n; ++k) { ct[k] = ctype[k]; cc[k] = cconc[k * N + i]; }
-    int its = equilibrate_constraint(net, c, ct, cc, use_prev_soln_as_guess != 0);
+    int its = equilibrate_constraint(net, c, ct, cc, use_prev_soln_as_guess != 0, creact);
     scatter(net, s, i, c);
     if (iterations) iterations[i] = its;
     if (its < 0) {

@@ -714,15 +714,19 @@ inline double ifc67_density(double t, double p) {
 }
 
 // Constraint types (transport_constraint_rt.F90:22-34 subset)
-enum { CON_TOTAL = 1, CON_FREE = 2, CON_PH = 3, CON_CHARGE_BAL = 4, CON_LOG = 5 };
+enum { CON_TOTAL = 1, CON_FREE = 2, CON_PH = 3, CON_CHARGE_BAL = 4, CON_LOG = 5, CON_MINERAL = 6, CON_GAS = 7 };
 
 // ReactionEquilibrateConstraint, reaction.F90:1328-2115, for the
-// TOTAL/FREE/LOG/PH/CHARGE_BAL subset with no minerals, sorption or gases
+// TOTAL/FREE/LOG/PH/CHARGE_BAL/MINERAL/GAS subset with no sorption
 // (initialize_with_molality = false, use_prev_soln_as_guess as given).
+// creact[i]: the mineral or gas reaction of a MINERAL/GAS row (:1755-1811);
+// its logK follows the cell temperature in non-isothermal runs
+// (RUpdateTempDependentCoefs at :1482-1484).
 // Returns the iteration count, or -1 when the iteration limit is reached /
 // a concentration goes non-positive / the decomposition is singular.
 inline int equilibrate_constraint(const Net& net, Cell& c, const int* ctype,
                                   const double* cconc, bool use_prev_soln_as_guess,
+                                  const PfConstraintReaction* creact = nullptr,
                                   int max_iterations = 10000) {
   const PfNetworkDesc* d = net.d;
   const int n = net.n;
@@ -742,6 +746,12 @@ inline int equilibrate_constraint(const Net& net, Cell& c, const int* ctype,
         if (!use_prev_soln_as_guess) free_conc[i] = cconc[i] * convert_molar_to_molal;
         break;
       case CON_PH: free_conc[i] = std::pow(10.0, -cconc[i]); break;
+      case CON_MINERAL:
+        if (!use_prev_soln_as_guess) free_conc[i] = cconc[i] * convert_molar_to_molal;  // guess
+        break;
+      case CON_GAS:  // partial pressure (bar); log10 form when <= 0
+        total_conc[i] = cconc[i] <= 0.0 ? std::pow(10.0, cconc[i]) : cconc[i];
+        break;
       default: return -1;
     }
   }
@@ -790,6 +800,19 @@ inline int equilibrate_constraint(const Net& net, Cell& c, const int* ctype,
           c.pri_molal[i] = std::pow(10.0, -cconc[i]) / c.pri_act_coef[i];
           J[i * MAXN + i] = 1.0;
           break;
+        case CON_MINERAL:
+        case CON_GAS: {
+          const PfConstraintReaction& R = creact[i];
+          double logK = R.logK;
+          if (!net.o.isothermal && R.temperature_dependent) interpolate_logK(R.logKcoef, &logK, c.temp, 1);
+          double lnQK = -logK * LOG_TO_LN;
+          for (int p = 0; p < R.nspec; ++p)
+            lnQK = lnQK + R.stoich[p] * std::log(c.pri_molal[R.spec[p]] * c.pri_act_coef[R.spec[p]]);
+          Res[i] = ctype[i] == CON_MINERAL ? lnQK : lnQK - std::log(total_conc[i]);
+          for (int j = 0; j < n; ++j) J[i * MAXN + j] = 0.0;
+          for (int p = 0; p < R.nspec; ++p) J[i * MAXN + R.spec[p]] = R.stoich[p] / c.pri_molal[R.spec[p]];
+          break;
+        }
       }
     }
     double maximum_residual = 0.0;

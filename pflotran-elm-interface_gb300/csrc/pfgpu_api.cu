@@ -12,15 +12,17 @@
 using namespace pfgpu;
 
 extern "C" int32_t pf_equilibrate_constraint_impl(const DevNet* net, const PfCellState* st,
-                                                  const int32_t* ctype, const double* cconc, int use_prev,
-                                                  int32_t* iterations, int max_iterations, void* stream);
+                                                  const int32_t* ctype, const PfConstraintReaction* creact,
+                                                  const double* cconc, int use_prev, int32_t* iterations,
+                                                  int max_iterations, void* stream);
 
 struct PfNetwork {
   DevNet dev{};
   void* d_tables = nullptr;
   unsigned long long* d_counters = nullptr;  // [0] queue [1] its [2] fails [3] err [4] max its [5] max substeps
   unsigned long long* h_counters = nullptr;  // pinned mirror
-  int32_t* d_ctype = nullptr;                // constraint types [PF_MAX_NCOMP]
+  int32_t* d_ctype = nullptr;                // constraint types [PF_MAX_NCOMP], then reactions
+  PfConstraintReaction* d_creact = nullptr;  // [PF_MAX_NCOMP], inside the d_ctype allocation
   double* d_scratch = nullptr;               // batched kernel per-cell scratch
   size_t scratch_cap = 0;                    // doubles
   std::vector<double> dbls_base;             // host copy of the double block at create
@@ -241,7 +243,11 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
     e = cudaMemcpy((char*)net->d_tables + ib, dbls.data(), dbls.size() * 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&net->d_counters, 8 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost(&net->h_counters, 8 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&net->d_ctype, PF_MAX_NCOMP * sizeof(int32_t));
+  if (e == cudaSuccess)
+    e = cudaMalloc(&net->d_ctype, pad16(PF_MAX_NCOMP * sizeof(int32_t)) + PF_MAX_NCOMP * sizeof(PfConstraintReaction));
+  if (e == cudaSuccess)
+    net->d_creact = reinterpret_cast<PfConstraintReaction*>(reinterpret_cast<char*>(net->d_ctype) +
+                                                            pad16(PF_MAX_NCOMP * sizeof(int32_t)));
   if (e != cudaSuccess) {
     pf_network_destroy(net);
     return PF_ERR_CUDA;
@@ -466,23 +472,45 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
   return launch_girt_assemble(net->dev, net->girt, *state, *a, net->num_sms, (cudaStream_t)stream);
 }
 
-int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, const int32_t* ctype,
-                                  const double* cconc, int32_t use_prev, int32_t* iterations, void* stream) {
+int32_t pf_equilibrate_constraint_ex(PfNetwork* net, const PfCellState* state, const int32_t* ctype,
+                                     const PfConstraintReaction* creact, const double* cconc, int32_t use_prev,
+                                     int32_t* iterations, void* stream) {
   int rc = validate_state(net, state);
   if (rc) return rc;
   if (!ctype || !cconc || (net->dev.ns > 0 && !state->sec_act_coef)) return PF_ERR_INVALID;
+  const int n = net->dev.n;
   int ncb = 0;
-  for (int j = 0; j < net->dev.n; ++j) {
-    if (ctype[j] < PF_CONSTRAINT_TOTAL || ctype[j] > PF_CONSTRAINT_LOG) return PF_ERR_INVALID;
+  bool reactions = false;
+  for (int j = 0; j < n; ++j) {
+    if (ctype[j] < PF_CONSTRAINT_TOTAL || ctype[j] > PF_CONSTRAINT_GAS) return PF_ERR_INVALID;
     ncb += ctype[j] == PF_CONSTRAINT_CHARGE_BAL;
+    if (ctype[j] == PF_CONSTRAINT_MINERAL || ctype[j] == PF_CONSTRAINT_GAS) {
+      if (!creact) return PF_ERR_INVALID;
+      const PfConstraintReaction& R = creact[j];
+      if (R.nspec < 1 || R.nspec > n) return PF_ERR_INVALID;
+      for (int p = 0; p < R.nspec; ++p)
+        if (R.spec[p] < 0 || R.spec[p] >= n) return PF_ERR_INVALID;
+      reactions = true;
+    }
   }
   if (ncb > 1) return PF_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemcpyAsync(net->d_ctype, ctype, net->dev.n * sizeof(int32_t), cudaMemcpyHostToDevice, s) !=
-      cudaSuccess)
+  if (cudaMemcpyAsync(net->d_ctype, ctype, n * sizeof(int32_t), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return PF_ERR_CUDA;
-  return pf_equilibrate_constraint_impl(&net->dev, state, net->d_ctype, cconc, use_prev, iterations, 10000,
-                                        stream);
+  if (reactions &&
+      cudaMemcpyAsync(net->d_creact, creact, n * sizeof(PfConstraintReaction), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
+    return PF_ERR_CUDA;
+  return pf_equilibrate_constraint_impl(&net->dev, state, net->d_ctype, net->d_creact, cconc, use_prev,
+                                        iterations, 10000, stream);
+}
+
+int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, const int32_t* ctype,
+                                  const double* cconc, int32_t use_prev, int32_t* iterations, void* stream) {
+  if (net && ctype)
+    for (int j = 0; j < net->dev.n; ++j)
+      if (ctype[j] == PF_CONSTRAINT_MINERAL || ctype[j] == PF_CONSTRAINT_GAS) return PF_ERR_INVALID;
+  return pf_equilibrate_constraint_ex(net, state, ctype, nullptr, cconc, use_prev, iterations, stream);
 }
 
 int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t kernel, PfStepStats* stats) {

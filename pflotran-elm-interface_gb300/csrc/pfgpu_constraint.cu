@@ -1,13 +1,16 @@
 // pfgpu_constraint.cu -- constraint equilibration, one thread per cell.
 //
 // ReactionEquilibrateConstraint (src/pflotran/reaction.F90:1328-2115) for the
-// aqueous constraint types TOTAL, FREE, LOG, PH and CHARGE_BAL: the Newton
-// iteration on free-ion molalities with the log/linear alternation of
+// constraint types TOTAL, FREE, LOG, PH, CHARGE_BAL, MINERAL and GAS: the
+// Newton iteration on free-ion molalities with the log/linear alternation of
 // iterations 4-8 (:1902-1913), RSolve (:5457-5516), the dlnC clip
 // reaction%max_dlnC (:1932-1935), and activity coefficients switched on after
-// the first converged iterate (:2036-2047).  It produces the initial
-// conditions of the step kernels; minerals, sorption and gases are not
-// constraint types here.
+// the first converged iterate (:2036-2047).  MINERAL rows hold ln(Q/K) of a
+// mineral at zero (:1755-1779), GAS rows ln(Q/K) at the log of a partial
+// pressure (:1781-1811); their logK follow the cell temperature in
+// non-isothermal runs (RUpdateTempDependentCoefs, :1482-1484).  It produces
+// the initial conditions of the step kernels; sorption constraints are not
+// built.
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
 
@@ -39,6 +42,7 @@ __device__ void activity_lag(const DevNet& net, const Tables& T, const double* c
 }
 
 __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellState st, const int32_t* ctype,
+                                                          const PfConstraintReaction* creact,
                                                           const double* cconc, int use_prev,
                                                           int32_t* iterations, int max_iterations) {
   const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,6 +68,8 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
       case 5: free_conc[j] = pow(10.0, v) * molar_to_molal; break;        // LOG
       case 4: if (!use_prev) free_conc[j] = v * molar_to_molal; break;    // CHARGE_BAL guess
       case 3: free_conc[j] = pow(10.0, -v); break;                        // PH
+      case 6: if (!use_prev) free_conc[j] = v * molar_to_molal; break;    // MINERAL guess
+      case 7: total_conc[j] = v <= 0.0 ? pow(10.0, v) : v; break;         // GAS partial pressure
       default: break;
     }
     c[j] = free_conc[j];
@@ -138,6 +144,18 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
           for (int k = 0; k < n; ++k) J[j * NM + k] = (j == k) ? 1.0 : 0.0;
           c[j] = pow(10.0, -cconc[soa.at(j, cell)]) / gam[j];
           break;
+        case 6:
+        case 7: {
+          const PfConstraintReaction& R = creact[j];
+          const double logK =
+              (!net.o.isothermal && R.temperature_dependent) ? interp_logK(R.logKcoef, temp) : R.logK;
+          double lnQK = -logK * LOG_TO_LN;
+          for (int p = 0; p < R.nspec; ++p) lnQK = lnQK + R.stoich[p] * log(c[R.spec[p]] * gam[R.spec[p]]);
+          Res[j] = ctype[j] == 6 ? lnQK : lnQK - log(total_conc[j]);
+          for (int k = 0; k < n; ++k) J[j * NM + k] = 0.0;
+          for (int p = 0; p < R.nspec; ++p) J[j * NM + R.spec[p]] = R.stoich[p] / c[R.spec[p]];
+          break;
+        }
         default: break;
       }
     }
@@ -242,12 +260,13 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
 using namespace pfgpu;
 
 extern "C" int32_t pf_equilibrate_constraint_impl(const DevNet* net, const PfCellState* st,
-                                                  const int32_t* ctype, const double* cconc, int use_prev,
-                                                  int32_t* iterations, int max_iterations, void* stream) {
+                                                  const int32_t* ctype, const PfConstraintReaction* creact,
+                                                  const double* cconc, int use_prev, int32_t* iterations,
+                                                  int max_iterations, void* stream) {
   const int tpb = 128;
   const int64_t blocks = (st->ncells + tpb - 1) / tpb;
   if (blocks)
-    constraint::equilibrate_kernel<<<blocks, tpb, 0, (cudaStream_t)stream>>>(*net, *st, ctype, cconc, use_prev,
-                                                                             iterations, max_iterations);
+    constraint::equilibrate_kernel<<<blocks, tpb, 0, (cudaStream_t)stream>>>(
+        *net, *st, ctype, creact, cconc, use_prev, iterations, max_iterations);
   return cudaGetLastError() == cudaSuccess ? PF_OK : PF_ERR_CUDA;
 }

@@ -35,6 +35,8 @@ PF_CONSTRAINT_FREE = 2
 PF_CONSTRAINT_PH = 3
 PF_CONSTRAINT_CHARGE_BAL = 4
 PF_CONSTRAINT_LOG = 5
+PF_CONSTRAINT_MINERAL = 6
+PF_CONSTRAINT_GAS = 7
 
 PF_MAX_NCOMP = 24
 PF_MAX_NSEC = 96
@@ -140,6 +142,37 @@ class PfTransportStats(C.Structure):
                 ("refinements", C.c_int32), ("max_cycle_iterations", C.c_int32)]
 
 
+class PfConstraintReaction(C.Structure):
+    _fields_ = [("nspec", C.c_int32), ("temperature_dependent", C.c_int32),
+                ("spec", C.c_int32 * PF_MAX_NCOMP), ("stoich", C.c_double * PF_MAX_NCOMP),
+                ("logK", C.c_double), ("logKcoef", C.c_double * 5)]
+
+
+def constraint_reactions(ncomp: int, reactions):
+    """A PfConstraintReaction array [ncomp] from {component index: dict(spec=
+    [primary indices], stoich=[...], logK=..., logKcoef=[5] or None)} (the
+    MINERAL/GAS rows; other entries stay empty).  Returns None for no
+    reactions."""
+    if not reactions:
+        return None
+    arr = (PfConstraintReaction * ncomp)()
+    for j, r in reactions.items():
+        e = arr[int(j)]
+        spec, stoich = list(r["spec"]), list(r["stoich"])
+        if not 1 <= len(spec) <= ncomp or len(spec) != len(stoich):
+            raise ValueError("constraint reaction of component %d: bad species list" % j)
+        e.nspec = len(spec)
+        for p, (k, nu) in enumerate(zip(spec, stoich)):
+            e.spec[p], e.stoich[p] = int(k), float(nu)
+        e.logK = float(r["logK"])
+        coef = r.get("logKcoef")
+        e.temperature_dependent = 1 if coef is not None else 0
+        if coef is not None:
+            for p in range(5):
+                e.logKcoef[p] = float(coef[p])
+    return arr
+
+
 class PfLaunchConfig(C.Structure):
     _fields_ = [
         ("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32),
@@ -176,6 +209,8 @@ SIGNATURES = {
                                   C.POINTER(PfStepStats)]),
     "pf_equilibrate_constraint": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(C.c_int32),
                                               _P, C.c_int32, _P, _P]),
+    "pf_equilibrate_constraint_ex": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(C.c_int32), _P,
+                                                 _P, C.c_int32, _P, _P]),
     "pf_network_set_launch": (C.c_int32, [_P, C.POINTER(PfLaunchConfig)]),
     "pf_network_get_launch": (C.c_int32, [_P, C.POINTER(PfLaunchConfig)]),
     "pf_version": (C.c_char_p, []),

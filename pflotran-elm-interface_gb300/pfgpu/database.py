@@ -267,3 +267,24 @@ def build_network(db: Database, primary, secondary=None, minerals=None, options=
     return ReactionNetwork.build(list(primary), [db.primary[p][1] for p in primary],
                                  [db.primary[p][0] for p in primary], secs, mins,
                                  debye=debye_huckel(reference_temperature), options=options)
+
+
+def constraint_reaction(db: Database, primary, name: str, kind: str = "mineral",
+                        reference_temperature: float = 25.0, isothermal: bool = True) -> dict:
+    """The reaction of a MINERAL or GAS constraint row (any mineral or gas of
+    the database, kinetic or not) in the network's primaries, water dropped:
+    dict(spec=[primary indices], stoich=[...], logK=logK at the reference
+    temperature, logKcoef=the five-term fit, or None when isothermal), for
+    ReactionEngine.equilibrate(..., reactions={component: ...})."""
+    table = db.minerals if kind == "mineral" else db.gases
+    if kind not in ("mineral", "gas"):
+        raise ValueError("kind must be 'mineral' or 'gas'")
+    r = table[name]
+    pset = set(primary)
+    nu = _drop_water(r.stoich, pset)
+    index = {p: k for k, p in enumerate(primary)}
+    coefs = fit_logK_coefs(db.temperatures, r.logK)
+    return dict(spec=[index[sp] for sp in nu], stoich=[nu[sp] for sp in nu],
+                logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
+                logKcoef=None if isothermal else coefs)
+

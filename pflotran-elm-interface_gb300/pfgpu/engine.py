@@ -109,16 +109,20 @@ class ReactionEngine:
                   self.lib.pf_update_auxvars(self.handle, C.byref(s), int(update_activity_coefs),
                                              _stream_ptr(stream)), allow_cell_failures=False)
 
-    def equilibrate(self, state: CellState, ctype, cconc, use_prev: bool = False, stream=None):
+    def equilibrate(self, state: CellState, ctype, cconc, use_prev: bool = False, stream=None, reactions=None):
         """Constraint equilibration on the device; cconc is a (ncomp, ncells)
-        CUDA tensor.  Returns the per-cell iteration counts (-1 = failed)."""
+        CUDA tensor.  reactions: {component: dict(spec, stoich, logK,
+        logKcoef)} for MINERAL/GAS rows (pfgpu.database.constraint_reaction).
+        Returns the per-cell iteration counts (-1 = failed)."""
         import torch
         ct = np.ascontiguousarray(ctype, np.int32)
         its = torch.empty(state.ncells, dtype=torch.int32, device=cconc.device)
         s = state.struct()
-        abi.check("pf_equilibrate_constraint",
-                  self.lib.pf_equilibrate_constraint(
+        cr = abi.constraint_reactions(len(ct), reactions)
+        abi.check("pf_equilibrate_constraint_ex",
+                  self.lib.pf_equilibrate_constraint_ex(
                       self.handle, C.byref(s), ct.ctypes.data_as(C.POINTER(C.c_int32)),
+                      C.cast(cr, C.c_void_p) if cr is not None else None,
                       C.c_void_p(cconc.contiguous().data_ptr()), int(use_prev), C.c_void_p(its.data_ptr()),
                       _stream_ptr(stream)), allow_cell_failures=False)
         return its
