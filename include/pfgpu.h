@@ -67,6 +67,48 @@ enum {
 #define PF_MAX_NSEC 96
 #define PF_MAX_NMNRL 16
 #define PF_MAX_SPEC_PER_RXN 24
+#define PF_MAX_NKD 8            /* isotherm (K_D) reactions            */
+#define PF_MAX_NIONX 4          /* ion-exchange reactions              */
+#define PF_MAX_IONX_CATIONS 8   /* cations per ion-exchange reaction   */
+
+/* isotherm types (reaction_isotherm_aux.F90 SORPTION_*) */
+enum { PF_SORPTION_LINEAR = 1, PF_SORPTION_LANGMUIR = 2, PF_SORPTION_FREUNDLICH = 3 };
+/* K_D units (isotherm%ikd_units) */
+enum { PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1 };
+
+/*
+ * Equilibrium sorption (RTotalSorb, reaction.F90:4783-4832): K_D isotherms
+ * (RTotalSorbKD, reaction_isotherm.F90:273-359) and equilibrium ion
+ * exchange (RTotalSorbEqIonx, reaction.F90:4906-5140), added to the
+ * accumulation as total_sorb * volume (RAccumulationSorb[Derivative],
+ * reaction.F90:5144-5210).  Surface complexation and dynamic K_D are not
+ * built.  Supported by pf_update_auxvars, pf_equilibrate_constraint[_ex]
+ * and pf_rstep with the one-lane batched kernel; the plain and group
+ * kernels, pf_adjoint and pf_girt_assemble return PF_ERR_UNSUPPORTED for a
+ * network with sorption.
+ */
+typedef struct PfSorptionDesc {
+  int32_t nkd;                    /* isotherm reactions, <= PF_MAX_NKD             */
+  int32_t kd_units;               /* PF_KD_UNIT_*                                   */
+  const int32_t* kd_spec;         /* [nkd] primary index (isotherm%eqkdspecid - 1)  */
+  const int32_t* kd_type;         /* [nkd] PF_SORPTION_*                            */
+  const double* kd_coeff;         /* [nkd] eqisothermcoeff                          */
+  const double* kd_langmuir_b;    /* [nkd] or NULL                                  */
+  const double* kd_freundlich_n;  /* [nkd] or NULL                                  */
+  const int32_t* kd_mineral;      /* [nkd] kinetic mineral scaling K_D by its volume
+                                     fraction (eqkdmineral - 1), -1 none; or NULL */
+  double soil_particle_density;   /* kg/m^3, used with PF_KD_UNIT_MLW_GSOIL        */
+  int32_t nionx;                  /* ion-exchange reactions, <= PF_MAX_NIONX        */
+  int32_t ionx_stride;            /* row stride of ionx_cation / ionx_k             */
+  const int32_t* ionx_ncation;    /* [nionx] eqionx_rxn_cationid(0,:)               */
+  const int32_t* ionx_cation;     /* [nionx*stride] primary index; the first is the
+                                     reference cation                              */
+  const double* ionx_k;           /* [nionx*stride] selectivity eqionx_rxn_k         */
+  const double* ionx_cec;         /* [nionx] eqionx_rxn_CEC, mol/m^3 bulk            */
+  const int32_t* ionx_mineral;    /* [nionx] kinetic mineral whose volume fraction
+                                     scales the CEC (eqionx_rxn_to_surf - 1), -1
+                                     none; or NULL                                 */
+} PfSorptionDesc;
 
 /*
  * Solver options: the CHEMISTRY-block fields of reaction_rt_type with the
@@ -138,6 +180,7 @@ typedef struct PfNetworkDesc {
   const double* mnrl_affinity_power;  /* [nmnrl] or NULL       */
   double debyeA, debyeB, debyeBdot;   /* reaction_database.F90:931-1022 */
   PfOptions opts;
+  const PfSorptionDesc* sorption;     /* NULL: no sorption                        */
 } PfNetworkDesc;
 
 /*
@@ -168,6 +211,13 @@ typedef struct PfCellState {
                               which the batched kernel's work queue hands out
                               cells (e.g. descending previous iteration count);
                               NULL = natural order.  Results do not depend on it. */
+  /* networks with sorption only (NULL otherwise): */
+  double* total_sorb;      /* [ncomp] total_sorb_eq, mol/m^3 bulk; in: the
+                              sorbed total of the fixed accumulation; out: at
+                              the solution                                     */
+  double* ionx_ref_sorbed; /* [nionx] eqionx_ref_cation_sorbed_conc: the ion-
+                              exchange Newton's warm start, carried between
+                              calls as the reference carries it                */
 } PfCellState;
 
 typedef struct PfStepStats {

@@ -38,6 +38,9 @@ inline void gather(const Net& net, const PfCellState* s, int64_t i, Cell& c) {
   c.temp = s->temperature ? s->temperature[i] : 25.0;
   c.ln_act_h2o = 0.0;
   c.ierror = 0;
+  for (int k = 0; k < net.n; ++k) c.total_sorb[k] = s->total_sorb ? s->total_sorb[k * N + i] : 0.0;
+  const int nionx = net.sorb ? net.sorb->nionx : 0;
+  for (int k = 0; k < nionx; ++k) c.ionx_ref[k] = s->ionx_ref_sorbed ? s->ionx_ref_sorbed[k * N + i] : 1.0e-9;
   set_logK(net, c);
 }
 
@@ -57,6 +60,10 @@ inline void scatter(const Net& net, const PfCellState* s, int64_t i, const Cell&
     s->mnrl_area[k * N + i] = c.mnrl_area[k];
     s->mnrl_rate[k * N + i] = c.mnrl_rate[k];
   }
+  if (s->total_sorb)
+    for (int k = 0; k < net.n; ++k) s->total_sorb[k * N + i] = c.total_sorb[k];
+  if (s->ionx_ref_sorbed && net.sorb)
+    for (int k = 0; k < net.sorb->nionx; ++k) s->ionx_ref_sorbed[k * N + i] = c.ionx_ref[k];
 }
 
 int check(const PfNetworkDesc* d, const PfCellState* s) {
@@ -180,7 +187,7 @@ int oracle_update_auxvars(const PfNetworkDesc* d, const PfCellState* s, int upda
     Cell c;
     gather(net, s, i, c);
     if (update_act) activity_coefficients(net, c);
-    total_aqueous(net, c);
+    total(net, c);
     scatter(net, s, i, c);
   });
   return PF_OK;

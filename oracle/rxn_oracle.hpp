@@ -60,6 +60,11 @@ struct Cell {
   double sec_logK[MAXS];
   double mnrl_logK[MAXM];
   int ierror;  // option%ierror side channel (activity-coefficient failure)
+  // sorption (reactive_transport_aux.F90:21-74: total_sorb_eq, dtotal_sorb_eq,
+  // eqionx_ref_cation_sorbed_conc)
+  double total_sorb[MAXN];
+  double dtotal_sorb[MAXN * MAXN];
+  double ionx_ref[PF_MAX_NIONX];
 };
 
 struct Net {
@@ -70,8 +75,11 @@ struct Net {
   double sst(int i, int s) const { return d->sec_stoich[i * d->sec_stride + s]; }
   int mid(int m, int s) const { return d->mnrl_spec[m * d->mnrl_stride + s]; }
   double mst(int m, int s) const { return d->mnrl_stoich[m * d->mnrl_stride + s]; }
+  const PfSorptionDesc* sorb;  // null: no sorption
   explicit Net(const PfNetworkDesc* desc) : d(desc), o(desc->opts), n(desc->ncomp),
-      ns(desc->nsec), nm(desc->nmnrl) {}
+      ns(desc->nsec), nm(desc->nmnrl),
+      sorb(desc->sorption && (desc->sorption->nkd > 0 || desc->sorption->nionx > 0) ? desc->sorption
+                                                                                      : nullptr) {}
 };
 
 // ReactionInterpolateLogK, reaction_aux.F90:1285-1312 (the coefficient type
@@ -248,6 +256,161 @@ inline void total_aqueous(const Net& net, Cell& c) {
   for (int j = 0; j < n; ++j) c.total[j] = c.total[j] * den_kg_per_L;
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) c.dtotal[i * MAXN + j] = c.dtotal[i * MAXN + j] * den_kg_per_L;
+}
+
+// RTotalSorbEqIonx, reaction.F90:4906-5140 (the "#if 1" implementation:
+// Newton on the reference cation's K_D when the charges differ, :4964-5081;
+// the closed form when they are all equal, :5083-5097).  Returns 1 after
+// 20000 Newton iterations (the ierror branch, :4983-4986).
+inline int total_sorb_eq_ionx(const Net& net, Cell& c) {
+  const PfSorptionDesc* sd = net.sorb;
+  const auto* Z = net.d->pri_Z;
+  const double tol = 1.0e-12;
+  for (int irxn = 0; irxn < sd->nionx; ++irxn) {
+    const int ncat = sd->ionx_ncation[irxn];
+    const int32_t* cat = sd->ionx_cation + irxn * sd->ionx_stride;
+    const auto* kk = sd->ionx_k + irxn * sd->ionx_stride;
+    const int mi = sd->ionx_mineral ? sd->ionx_mineral[irxn] : -1;
+    double omega;
+    if (mi >= 0)
+      omega = std::max(sd->ionx_cec[irxn] * c.mnrl_volfrac[mi], 1.0e-40);
+    else
+      omega = sd->ionx_cec[irxn];
+    // eqionx_rxn_Z_flag (reaction_database.F90:2905-2919)
+    bool zflag = false;
+    for (int i = 0; i < ncat && !zflag; ++i)
+      for (int j = 0; j < ncat; ++j)
+        if (std::fabs(Z[cat[i]] - Z[cat[j]]) > 0.1) { zflag = true; break; }
+    double cation_X[PF_MAX_IONX_CATIONS];
+    for (int j = 0; j < ncat; ++j) cation_X[j] = 0.0;
+    if (zflag) {
+      int icomp = cat[0];
+      double ref_cation_conc = c.pri_molal[icomp] * c.pri_act_coef[icomp];
+      double ref_cation_Z = Z[icomp];
+      double ref_cation_k = kk[0];
+      double ref_cation_X = ref_cation_Z * c.ionx_ref[irxn] / omega;
+      bool one_more = false;
+      double KDj = ref_cation_X / (ref_cation_k * ref_cation_conc);
+      int it = 0;
+      for (;;) {
+        it = it + 1;
+        if (it > 20000) return 1;
+        ref_cation_X = KDj * (ref_cation_k * ref_cation_conc);
+        cation_X[0] = ref_cation_X;
+        double total = ref_cation_X;
+        double dres_dKDj = 0.0;
+        for (int j = 1; j < ncat; ++j) {
+          icomp = cat[j];
+          cation_X[j] = kk[j] * c.pri_molal[icomp] * c.pri_act_coef[icomp] * std::pow(KDj, Z[icomp] / ref_cation_Z);
+          total = total + cation_X[j];
+          dres_dKDj = dres_dKDj + cation_X[j] / KDj * Z[icomp];
+        }
+        dres_dKDj = dres_dKDj / ref_cation_Z + (ref_cation_k * ref_cation_conc);
+        double res = 1.0 - total;
+        if (one_more) break;
+        double delta_KDj = res / dres_dKDj;
+        KDj = KDj + delta_KDj;
+        KDj = std::max(KDj, 1.0e-40);
+        if (std::fabs(delta_KDj / KDj) < tol) one_more = true;
+      }
+      c.ionx_ref[irxn] = ref_cation_X * omega / ref_cation_Z;
+    } else {
+      double sumkm = 0.0;
+      for (int j = 0; j < ncat; ++j) {
+        const int icomp = cat[j];
+        cation_X[j] = c.pri_molal[icomp] * c.pri_act_coef[icomp] * kk[j];
+        sumkm = sumkm + cation_X[j];
+      }
+      for (int j = 0; j < ncat; ++j) cation_X[j] = cation_X[j] / sumkm;
+    }
+    double sumZX = 0.0;
+    for (int i = 0; i < ncat; ++i) sumZX = sumZX + Z[cat[i]] * cation_X[i];
+    for (int i = 0; i < ncat; ++i) {
+      const int icomp = cat[i];
+      const double tempreal1 = cation_X[i] * omega / Z[icomp];
+      c.total_sorb[icomp] = c.total_sorb[icomp] + tempreal1;
+      const double tempreal2 = Z[icomp] / sumZX;
+      for (int j = 0; j < ncat; ++j) {
+        const int jcomp = cat[j];
+        if (i == j)
+          c.dtotal_sorb[icomp * MAXN + jcomp] =
+              c.dtotal_sorb[icomp * MAXN + jcomp] + tempreal1 * (1.0 - (tempreal2 * cation_X[j])) / c.pri_molal[jcomp];
+        else
+          c.dtotal_sorb[icomp * MAXN + jcomp] =
+              c.dtotal_sorb[icomp * MAXN + jcomp] + (-tempreal1) * tempreal2 * cation_X[j] / c.pri_molal[jcomp];
+      }
+    }
+  }
+  return 0;
+}
+
+// RTotalSorbKD, reaction_isotherm.F90:273-359
+inline void total_sorb_kd(const Net& net, Cell& c) {
+  const PfSorptionDesc* sd = net.sorb;
+  for (int irxn = 0; irxn < sd->nkd; ++irxn) {
+    const int icomp = sd->kd_spec[irxn];
+    const double molality = c.pri_molal[icomp];
+    double kd_kgw_m3b;
+    if (sd->kd_units == PF_KD_UNIT_MLW_GSOIL)
+      kd_kgw_m3b = sd->kd_coeff[irxn] * c.den_kg * (1.0 - c.porosity) * sd->soil_particle_density * 1.0e-3;
+    else
+      kd_kgw_m3b = sd->kd_coeff[irxn];
+    const int mi = sd->kd_mineral ? sd->kd_mineral[irxn] : -1;
+    if (mi >= 0) kd_kgw_m3b = kd_kgw_m3b * (c.mnrl_volfrac[mi]);
+    double res, dres_dc;
+    switch (sd->kd_type[irxn]) {
+      case PF_SORPTION_LINEAR:
+        res = kd_kgw_m3b * molality;
+        dres_dc = kd_kgw_m3b;
+        break;
+      case PF_SORPTION_LANGMUIR: {
+        const double tempreal = kd_kgw_m3b * molality;
+        res = tempreal * sd->kd_langmuir_b[irxn] / (1.0 + tempreal);
+        dres_dc = res / molality - res / (1.0 + tempreal) * tempreal / molality;
+        break;
+      }
+      case PF_SORPTION_FREUNDLICH: {
+        const double one_over_n = 1.0 / sd->kd_freundlich_n[irxn];
+        res = kd_kgw_m3b * std::pow(molality, one_over_n);
+        dres_dc = res / molality * one_over_n;
+        break;
+      }
+      default:
+        res = 0.0;
+        dres_dc = 0.0;
+    }
+    c.total_sorb[icomp] = c.total_sorb[icomp] + res;
+    c.dtotal_sorb[icomp * MAXN + icomp] = c.dtotal_sorb[icomp * MAXN + icomp] + dres_dc;
+  }
+}
+
+// RTotalSorb, reaction.F90:4783-4832 (RZeroSorb :4763-4779, then ion
+// exchange, then K_D; no surface complexation, no dynamic K_D).  Returns the
+// ion exchange's ierror.
+inline int total_sorb(const Net& net, Cell& c) {
+  for (int i = 0; i < net.n; ++i) {
+    c.total_sorb[i] = 0.0;
+    for (int j = 0; j < net.n; ++j) c.dtotal_sorb[i * MAXN + j] = 0.0;
+  }
+  if (net.sorb->nionx > 0 && total_sorb_eq_ionx(net, c) != 0) return 1;
+  if (net.sorb->nkd > 0) total_sorb_kd(net, c);
+  return 0;
+}
+
+// RTotal, reaction.F90:4618-4661: aqueous, then sorbed.  Returns ierror.
+inline int total(const Net& net, Cell& c) {
+  total_aqueous(net, c);
+  return net.sorb ? total_sorb(net, c) : 0;
+}
+
+// RAccumulationSorb / RAccumulationSorbDerivative, reaction.F90:5144-5210
+inline void accumulation_sorb(const Net& net, const Cell& c, double* res) {
+  for (int j = 0; j < net.n; ++j) res[j] = res[j] + c.total_sorb[j] * c.volume;
+}
+inline void accumulation_sorb_derivative(const Net& net, const Cell& c, double dt, double* J) {
+  const double v_t = c.volume / dt;
+  for (int i = 0; i < net.n; ++i)
+    for (int j = 0; j < net.n; ++j) J[i * MAXN + j] = J[i * MAXN + j] + c.dtotal_sorb[i * MAXN + j] * v_t;
 }
 
 // RTAccumulation, reaction.F90:5710-5771 (aqueous, single phase)
@@ -514,14 +677,18 @@ inline int rreact(const Net& net, Cell& c, const double* guess, double dt, int* 
   *num_iterations = 0;
   c.ierror = 0;
   set_logK(net, c);
+  // the fixed accumulation holds the sorbed total of the last RTotal
+  // (:3836-3839), restored or not after a failed RReact
   accumulation(net, c, fixed_accum);
+  if (net.sorb) accumulation_sorb(net, c, fixed_accum);
   for (int j = 0; j < n; ++j) initial_total[j] = c.total[j];
   for (int j = 0; j < n; ++j) c.pri_molal[j] = guess[j];
   for (int j = 0; j < n; ++j) update[j] = 0.0;
   for (;;) {
     *num_iterations = *num_iterations + 1;
     if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) activity_coefficients(net, c);
-    total_aqueous(net, c);
+    // RTAuxVarCompute; a failed ion-exchange solve fails RReact (:3861-3865)
+    if (total(net, c) != 0) return 1;
     if (*num_iterations > o.maximum_reaction_iterations) {
       ierror = 1;
       for (int j = 0; j < n; ++j) c.total[j] = initial_total[j];
@@ -529,6 +696,10 @@ inline int rreact(const Net& net, Cell& c, const double* guess, double dt, int* 
     }
     accumulation(net, c, residual);
     accumulation_derivative(net, c, dt, J);
+    if (net.sorb) {
+      accumulation_sorb(net, c, residual);
+      accumulation_sorb_derivative(net, c, dt, J);
+    }
     for (int j = 0; j < n; ++j) residual[j] = (residual[j] - fixed_accum[j]) / dt;
     reaction(net, c, residual, J, true);
     if (c.ierror != 0) return c.ierror;
@@ -569,7 +740,7 @@ inline int rreact(const Net& net, Cell& c, const double* guess, double dt, int* 
     if (max_rel < o.max_relative_change_tolerance) break;
     for (int j = 0; j < n; ++j) c.pri_molal[j] = latest_solution[j];
   }
-  total_aqueous(net, c);  // "one last update", reaction.F90:4052
+  total(net, c);  // "one last update", reaction.F90:4051-4052
   return ierror;
 }
 
@@ -585,13 +756,18 @@ inline int implicit_step(const Net& net, Cell& c, double dt, double rel_tol, int
   double fixed_accum[MAXN], residual[MAXN], update[MAXN], J[MAXN * MAXN], conc[MAXN];
   set_logK(net, c);
   accumulation(net, c, fixed_accum);
+  if (net.sorb) accumulation_sorb(net, c, fixed_accum);
   *num_iterations = 0;
   for (;;) {
     *num_iterations += 1;
     if (net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) activity_coefficients(net, c);
-    total_aqueous(net, c);
+    if (total(net, c) != 0) return 1;
     accumulation(net, c, residual);
     accumulation_derivative(net, c, dt, J);
+    if (net.sorb) {
+      accumulation_sorb(net, c, residual);
+      accumulation_sorb_derivative(net, c, dt, J);
+    }
     for (int j = 0; j < n; ++j) residual[j] = (residual[j] - fixed_accum[j]) / dt;
     reaction(net, c, residual, J, true);
     for (int j = 0; j < n; ++j) conc[j] = c.pri_molal[j];
@@ -606,7 +782,7 @@ inline int implicit_step(const Net& net, Cell& c, double dt, double rel_tol, int
     if (max_rel < rel_tol) break;
     if (*num_iterations >= max_its) return 1;
   }
-  total_aqueous(net, c);
+  total(net, c);
   return 0;
 }
 
@@ -765,7 +941,7 @@ inline int equilibrate_constraint(const Net& net, Cell& c, const int* ctype,
       if (ctype[i] == CON_FREE || ctype[i] == CON_LOG) c.pri_molal[i] = free_conc[i];
     if (net.o.act_coef_update_frequency != PF_ACT_COEF_OFF && compute_activity_coefs)
       activity_coefficients(net, c);
-    total_aqueous(net, c);
+    total(net, c);  // RTotal without ierror (:1594): sorbed totals follow the iterate
     for (int i = 0; i < n * MAXN; ++i) J[i] = 0.0;
     for (int i = 0; i < n; ++i) {
       switch (ctype[i]) {

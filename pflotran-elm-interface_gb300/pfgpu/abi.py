@@ -42,6 +42,14 @@ PF_MAX_NCOMP = 24
 PF_MAX_NSEC = 96
 PF_MAX_NMNRL = 16
 PF_MAX_SPEC_PER_RXN = 24
+PF_MAX_NKD = 8
+PF_MAX_NIONX = 4
+PF_MAX_IONX_CATIONS = 8
+PF_SORPTION_LINEAR = 1
+PF_SORPTION_LANGMUIR = 2
+PF_SORPTION_FREUNDLICH = 3
+PF_KD_UNIT_KG_M3_BULK = 0
+PF_KD_UNIT_MLW_GSOIL = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -64,6 +72,16 @@ class PfOptions(C.Structure):
     ]
 
 
+class PfSorptionDesc(C.Structure):
+    _fields_ = [
+        ("nkd", C.c_int32), ("kd_units", C.c_int32),
+        ("kd_spec", _ip), ("kd_type", _ip), ("kd_coeff", _dp), ("kd_langmuir_b", _dp),
+        ("kd_freundlich_n", _dp), ("kd_mineral", _ip), ("soil_particle_density", C.c_double),
+        ("nionx", C.c_int32), ("ionx_stride", C.c_int32),
+        ("ionx_ncation", _ip), ("ionx_cation", _ip), ("ionx_k", _dp), ("ionx_cec", _dp), ("ionx_mineral", _ip),
+    ]
+
+
 class PfNetworkDesc(C.Structure):
     _fields_ = [
         ("ncomp", C.c_int32), ("nsec", C.c_int32), ("nmnrl", C.c_int32),
@@ -80,6 +98,7 @@ class PfNetworkDesc(C.Structure):
         ("mnrl_affinity_power", _dp),
         ("debyeA", C.c_double), ("debyeB", C.c_double), ("debyeBdot", C.c_double),
         ("opts", PfOptions),
+        ("sorption", C.POINTER(PfSorptionDesc)),
     ]
 
 
@@ -93,6 +112,7 @@ class PfCellState(C.Structure):
         ("volume", _dp), ("temperature", _dp), ("dt_cell", _dp),
         ("status", _ip), ("newton_its", _ip), ("num_substeps", _ip),
         ("cell_order", C.POINTER(C.c_int64)),
+        ("total_sorb", _dp), ("ionx_ref_sorbed", _dp),
     ]
 
 

@@ -96,6 +96,24 @@ class ReactionNetwork:
     debyeB: float = 0.3288
     debyeBdot: float = 0.0410
     options: dict = field(default_factory=default_options)
+    # equilibrium sorption (None: none): dict(kd=[dict(species, type ('linear',
+    # 'langmuir', 'freundlich'), coeff, [b], [n], [mineral])], kd_units
+    # ('kg/m3 bulk' or 'mL/g soil'), soil_particle_density, ionx=[dict(
+    # cations=[(name, k), ...] (the first is the reference cation), cec,
+    # [mineral])])
+    sorption: dict = None
+
+    @property
+    def nkd(self):
+        return len((self.sorption or {}).get("kd", ()))
+
+    @property
+    def nionx(self):
+        return len((self.sorption or {}).get("ionx", ()))
+
+    @property
+    def has_sorption(self):
+        return self.nkd + self.nionx > 0
 
     @property
     def ncomp(self):
@@ -225,7 +243,49 @@ class ReactionNetwork:
         d.mnrl_affinity_power = _ptr(arr(self.mnrl_affinity_power, f64), C.c_double)
         d.debyeA, d.debyeB, d.debyeBdot = self.debyeA, self.debyeB, self.debyeBdot
         d.opts = self.options_struct()
+        if self.has_sorption:
+            self._sorb = self._sorption_desc(arr)
+            d.sorption = C.pointer(self._sorb)
         return d
+
+    def _sorption_desc(self, arr) -> abi.PfSorptionDesc:
+        sp = self.sorption
+        idx = {s: i for i, s in enumerate(self.primary)}
+        mins = {m: i for i, m in enumerate(self.minerals)}
+        i32, f64 = np.int32, np.float64
+        kinds = {"linear": abi.PF_SORPTION_LINEAR, "langmuir": abi.PF_SORPTION_LANGMUIR,
+                 "freundlich": abi.PF_SORPTION_FREUNDLICH}
+        sd = abi.PfSorptionDesc()
+        kd = list(sp.get("kd", ()))
+        sd.nkd = len(kd)
+        sd.kd_units = {"kg/m3 bulk": abi.PF_KD_UNIT_KG_M3_BULK,
+                       "mL/g soil": abi.PF_KD_UNIT_MLW_GSOIL}[sp.get("kd_units", "kg/m3 bulk")]
+        sd.soil_particle_density = float(sp.get("soil_particle_density", 2650.0))
+        if kd:
+            sd.kd_spec = _ptr(arr([idx[r["species"]] for r in kd], i32), C.c_int32)
+            sd.kd_type = _ptr(arr([kinds[r.get("type", "linear")] for r in kd], i32), C.c_int32)
+            sd.kd_coeff = _ptr(arr([r["coeff"] for r in kd], f64), C.c_double)
+            sd.kd_langmuir_b = _ptr(arr([r.get("b", 0.0) for r in kd], f64), C.c_double)
+            sd.kd_freundlich_n = _ptr(arr([r.get("n", 1.0) for r in kd], f64), C.c_double)
+            sd.kd_mineral = _ptr(arr([mins[r["mineral"]] if r.get("mineral") else -1 for r in kd], i32),
+                                 C.c_int32)
+        ix = list(sp.get("ionx", ()))
+        sd.nionx = len(ix)
+        if ix:
+            stride = max(len(r["cations"]) for r in ix)
+            cat = np.zeros((len(ix), stride), i32)
+            kk = np.zeros((len(ix), stride), f64)
+            for i, r in enumerate(ix):
+                for j, (name, k) in enumerate(r["cations"]):
+                    cat[i, j], kk[i, j] = idx[name], k
+            sd.ionx_stride = stride
+            sd.ionx_ncation = _ptr(arr([len(r["cations"]) for r in ix], i32), C.c_int32)
+            sd.ionx_cation = _ptr(arr(cat, i32), C.c_int32)
+            sd.ionx_k = _ptr(arr(kk, f64), C.c_double)
+            sd.ionx_cec = _ptr(arr([r["cec"] for r in ix], f64), C.c_double)
+            sd.ionx_mineral = _ptr(arr([mins[r["mineral"]] if r.get("mineral") else -1 for r in ix], i32),
+                                   C.c_int32)
+        return sd
 
     def options_struct(self) -> abi.PfOptions:
         o = abi.PfOptions()
@@ -245,12 +305,15 @@ STATE_FIELDS = {
     "den_kg": (1, np.float64), "volume": (1, np.float64),
     "temperature": (1, np.float64), "dt_cell": (1, np.float64),
     "status": (1, np.int32), "newton_its": (1, np.int32), "num_substeps": (1, np.int32),
+    # networks with sorption only
+    "total_sorb": ("n", np.float64), "ionx_ref_sorbed": ("x", np.float64),
 }
 OPTIONAL_FIELDS = ("dt_cell",)
+SORPTION_FIELDS = ("total_sorb", "ionx_ref_sorbed")
 
 
 def _rows(net, r):
-    return {"n": net.ncomp, "s": net.nsec, "m": net.nmnrl}.get(r, r)
+    return {"n": net.ncomp, "s": net.nsec, "m": net.nmnrl, "x": net.nionx}.get(r, r)
 
 
 class CellState:
@@ -268,8 +331,12 @@ class CellState:
         for k, (r, dt) in STATE_FIELDS.items():
             if k in OPTIONAL_FIELDS and not with_dt:
                 continue
+            if k in SORPTION_FIELDS and not net.has_sorption:
+                continue
             rows = _rows(net, r)
             a[k] = np.zeros((rows, ncells), dt) if r != 1 else np.zeros(ncells, dt)
+        if net.has_sorption:
+            a["ionx_ref_sorbed"][:] = 1.0e-9  # reactive_transport_aux.F90:282
         a["pri_act_coef"][:] = 1.0
         a["sec_act_coef"][:] = 1.0
         a["saturation"][:] = 1.0
