@@ -83,9 +83,9 @@ enum { PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1 };
  * accumulation as total_sorb * volume (RAccumulationSorb[Derivative],
  * reaction.F90:5144-5210).  Surface complexation and dynamic K_D are not
  * built.  Supported by pf_update_auxvars, pf_equilibrate_constraint[_ex]
- * and pf_rstep with the one-lane batched kernel; the plain and group
- * kernels, pf_adjoint and pf_girt_assemble return PF_ERR_UNSUPPORTED for a
- * network with sorption.
+ * and pf_rstep (the plain kernel and the one-lane batched kernel; a launch
+ * configuration with several lanes per cell is refused); pf_adjoint and
+ * pf_girt_assemble return PF_ERR_UNSUPPORTED for a network with sorption.
  */
 typedef struct PfSorptionDesc {
   int32_t nkd;                    /* isotherm reactions, <= PF_MAX_NKD             */

@@ -76,6 +76,32 @@ int validate_desc(const PfNetworkDesc* d) {
     }
   }
   if (d->opts.maximum_reaction_iterations < 1 || d->opts.maximum_reaction_cuts < 0) return PF_ERR_INVALID;
+  if (const PfSorptionDesc* sd = d->sorption) {
+    if (sd->nkd < 0 || sd->nionx < 0) return PF_ERR_INVALID;
+    if (sd->nkd > PF_MAX_NKD || sd->nionx > PF_MAX_NIONX) return PF_ERR_TOO_LARGE;
+    if (sd->kd_units != PF_KD_UNIT_KG_M3_BULK && sd->kd_units != PF_KD_UNIT_MLW_GSOIL) return PF_ERR_INVALID;
+    if (sd->nkd > 0 && (!sd->kd_spec || !sd->kd_type || !sd->kd_coeff)) return PF_ERR_INVALID;
+    for (int r = 0; r < sd->nkd; ++r) {
+      if (sd->kd_spec[r] < 0 || sd->kd_spec[r] >= d->ncomp) return PF_ERR_INVALID;
+      if (sd->kd_type[r] < PF_SORPTION_LINEAR || sd->kd_type[r] > PF_SORPTION_FREUNDLICH) return PF_ERR_INVALID;
+      if (sd->kd_type[r] == PF_SORPTION_LANGMUIR && !sd->kd_langmuir_b) return PF_ERR_INVALID;
+      if (sd->kd_type[r] == PF_SORPTION_FREUNDLICH && !sd->kd_freundlich_n) return PF_ERR_INVALID;
+      if (sd->kd_mineral && (sd->kd_mineral[r] < -1 || sd->kd_mineral[r] >= d->nmnrl)) return PF_ERR_INVALID;
+    }
+    if (sd->nionx > 0 && (!sd->ionx_ncation || !sd->ionx_cation || !sd->ionx_k || !sd->ionx_cec ||
+                          sd->ionx_stride < 1))
+      return PF_ERR_INVALID;
+    for (int r = 0; r < sd->nionx; ++r) {
+      if (sd->ionx_ncation[r] < 1 || sd->ionx_ncation[r] > sd->ionx_stride ||
+          sd->ionx_ncation[r] > PF_MAX_IONX_CATIONS)
+        return PF_ERR_INVALID;
+      for (int j = 0; j < sd->ionx_ncation[r]; ++j) {
+        const int k = sd->ionx_cation[r * sd->ionx_stride + j];
+        if (k < 0 || k >= d->ncomp || d->pri_Z[k] == 0.0) return PF_ERR_INVALID;  // cations carry charge
+      }
+      if (sd->ionx_mineral && (sd->ionx_mineral[r] < -1 || sd->ionx_mineral[r] >= d->nmnrl)) return PF_ERR_INVALID;
+    }
+  }
   if (d->opts.act_coef_update_frequency < 0 || d->opts.act_coef_update_frequency > 2) return PF_ERR_INVALID;
   return PF_OK;
 }
@@ -90,6 +116,8 @@ int validate_state(const PfNetwork* net, const PfCellState* s) {
   if (net->dev.ns > 0 && (!s->sec_act_coef || !s->sec_molal)) return PF_ERR_INVALID;
   if (net->dev.nm > 0 && (!s->mnrl_volfrac || !s->mnrl_area || !s->mnrl_rate)) return PF_ERR_INVALID;
   if (!net->dev.o.isothermal && !s->temperature) return PF_ERR_INVALID;
+  if (net->dev.nkd + net->dev.nionx > 0 && !s->total_sorb) return PF_ERR_INVALID;
+  if (net->dev.nionx > 0 && !s->ionx_ref_sorbed) return PF_ERR_INVALID;
   return PF_OK;
 }
 
@@ -189,6 +217,42 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_mpair_idx = (int)ints.size();
   ints.insert(ints.end(), mpair_idx.begin(), mpair_idx.end());
   dev.neg_mask = neg_mask;
+  // sorption: K_D rows; ion-exchange reactions as CSR over their cations
+  const PfSorptionDesc* sd = d->sorption;
+  const int nkd = sd ? sd->nkd : 0, nix = sd ? sd->nionx : 0;
+  dev.nkd = nkd;
+  dev.nionx = nix;
+  dev.kd_units = sd ? sd->kd_units : 0;
+  dev.soil_density = sd ? sd->soil_particle_density : 0.0;
+  dev.o_kd_spec = (int)ints.size();
+  for (int r = 0; r < nkd; ++r) ints.push_back(sd->kd_spec[r]);
+  dev.o_kd_type = (int)ints.size();
+  for (int r = 0; r < nkd; ++r) ints.push_back(sd->kd_type[r]);
+  dev.o_kd_min = (int)ints.size();
+  for (int r = 0; r < nkd; ++r) ints.push_back(sd->kd_mineral ? sd->kd_mineral[r] : -1);
+  dev.o_ix_ptr = (int)ints.size();
+  {
+    int cnt = 0;
+    for (int r = 0; r < nix; ++r) { ints.push_back(cnt); cnt += sd->ionx_ncation[r]; }
+    ints.push_back(cnt);
+  }
+  dev.o_ix_cat = (int)ints.size();
+  for (int r = 0; r < nix; ++r)
+    for (int j = 0; j < sd->ionx_ncation[r]; ++j) ints.push_back(sd->ionx_cation[r * sd->ionx_stride + j]);
+  dev.o_ix_min = (int)ints.size();
+  for (int r = 0; r < nix; ++r) ints.push_back(sd->ionx_mineral ? sd->ionx_mineral[r] : -1);
+  dev.o_ix_zflag = (int)ints.size();
+  for (int r = 0; r < nix; ++r) {  // eqionx_rxn_Z_flag, reaction_database.F90:2905-2919
+    bool zf = false;
+    for (int i = 0; i < sd->ionx_ncation[r] && !zf; ++i)
+      for (int j = 0; j < sd->ionx_ncation[r]; ++j)
+        if (std::fabs(d->pri_Z[sd->ionx_cation[r * sd->ionx_stride + i]] -
+                      d->pri_Z[sd->ionx_cation[r * sd->ionx_stride + j]]) > 0.1) {
+          zf = true;
+          break;
+        }
+    ints.push_back(zf ? 1 : 0);
+  }
   while (ints.size() % 4) ints.push_back(0);
   auto put = [&](const double* src, int count, double dflt) {
     int off = (int)dbls.size();
@@ -219,6 +283,13 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_power = put(d->mnrl_affinity_power, nm, 1.0);
   dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);
   dev.o_mpair_coef = put(mpair_coef.data(), (int)mpair_coef.size(), 0.0);
+  dev.o_kd_coeff = put(nkd ? sd->kd_coeff : nullptr, nkd, 0.0);
+  dev.o_kd_b = put(nkd ? sd->kd_langmuir_b : nullptr, nkd, 0.0);
+  dev.o_kd_n = put(nkd ? sd->kd_freundlich_n : nullptr, nkd, 1.0);
+  dev.o_ix_k = (int)dbls.size();
+  for (int r = 0; r < nix; ++r)
+    for (int j = 0; j < sd->ionx_ncation[r]; ++j) dbls.push_back(sd->ionx_k[r * sd->ionx_stride + j]);
+  dev.o_ix_cec = put(nix ? sd->ionx_cec : nullptr, nix, 0.0);
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
               (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |
@@ -430,6 +501,7 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
   const DevNet& d = net->dev;
   if (!batched_supported(d)) return PF_ERR_UNSUPPORTED;
   if (d.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) return PF_ERR_UNSUPPORTED;
+  if (d.nkd + d.nionx > 0) return PF_ERR_UNSUPPORTED;  // no adjoint of the sorption terms
   if (!a->dL_dtotal0 || (d.nm > 0 && (!a->dL_dlnarea || !a->dL_dlogK_mnrl || !a->dL_dlnk)) ||
       (d.ns > 0 && !a->dL_dlogK_sec) || (!a->weight && !a->dL_dtotal) || (a->weight && !a->target))
     return PF_ERR_INVALID;
@@ -462,6 +534,7 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
       !a->colidx || !a->residual || !a->values || !(a->dx > 0) || !(a->dy > 0) || !(a->dz > 0))
     return PF_ERR_INVALID;
   if ((int64_t)a->nx * a->ny * a->nz != state->ncells) return PF_ERR_INVALID;
+  if (net->dev.nkd + net->dev.nionx > 0) return PF_ERR_UNSUPPORTED;  // no sorbed accumulation here
   if ((a->nx > 1 && !a->qx) || (a->ny > 1 && !a->qy) || (a->nz > 1 && !a->qz)) return PF_ERR_INVALID;
   if (!state->sec_molal && net->dev.ns) return PF_ERR_INVALID;
   if (girt_smem_bytes(net->dev, nullptr) > 227u * 1024u) return PF_ERR_TOO_LARGE;
@@ -536,6 +609,8 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
       {h->status, N * i4, false, true},            {h->newton_its, N * i4, false, true},
       {h->num_substeps, N * i4, false, true},
       {(void*)h->cell_order, N * sizeof(int64_t), true, false},
+      {h->total_sorb, n * N * d8, true, true},
+      {h->ionx_ref_sorbed, (size_t)net->dev.nionx * N * d8, true, true},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
   size_t need = 0;
@@ -579,6 +654,8 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
   d.newton_its = (int32_t*)dptr[15];
   d.num_substeps = (int32_t*)dptr[16];
   d.cell_order = (const int64_t*)dptr[17];
+  d.total_sorb = (double*)dptr[18];
+  d.ionx_ref_sorbed = (double*)dptr[19];
   PfStepStats local{};
   rc = pf_rstep(net, &d, dt, kernel, nullptr, stats ? stats : &local);
   if (rc < 0) return rc;

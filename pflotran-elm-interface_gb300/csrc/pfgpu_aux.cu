@@ -3,7 +3,9 @@
 //   update_auxvars          RTUpdateAuxVars for cells (reactive_transport.F90:
 //                           3625-3660): optional RActivityCoefficients, then
 //                           RTotal/RTotalAqueous (reaction.F90:4618-4759) ->
-//                           total, sec_molal.
+//                           total, sec_molal; with sorption RTotalSorb
+//                           (:4783-4832) -> total_sorb, the ion-exchange warm
+//                           start.
 //   update_activity_coefs   RTUpdateActivityCoefficients (reactive_transport.F90:
 //                           3441-3521): RActivityCoefficients only, both the LAG
 //                           (reaction.F90:4553-4612) and NEWTON (:4403-4551)
@@ -12,6 +14,7 @@
 // the step kernels, so consecutive threads read consecutive cells.
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
 namespace aux {
@@ -131,6 +134,17 @@ __device__ void total(const DevNet& net, const Tables& T, const PfCellState& st,
   }
   const double den_L = st.den_kg[cell] * 1.0e-3;
   for (int j = 0; j < n; ++j) st.total[soa.at(j, cell)] = tot[j] * den_L;
+  if (net.nkd + net.nionx > 0) {
+    for (int j = 0; j < n; ++j) st.total_sorb[soa.at(j, cell)] = 0.0;
+    // RTotal without ierror (RTUpdateAuxVars): a failed ion-exchange solve
+    // leaves the last iterate, as the reference's message-and-continue does
+    total_sorb(
+        net, T, [&](int j) { return st.pri_molal[soa.at(j, cell)]; },
+        [&](int j) { return st.pri_act_coef[soa.at(j, cell)]; },
+        [&](int m) { return st.mnrl_volfrac[soa.at(m, cell)]; }, st.porosity[cell], st.den_kg[cell],
+        st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr, st.ncells,
+        [&](int j, double v) { st.total_sorb[soa.at(j, cell)] += v; }, [](int, int, double) {});
+  }
 }
 
 __global__ void update_auxvars_kernel(DevNet net, PfCellState st, int update_act) {

@@ -37,6 +37,7 @@
 #pragma once
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
 namespace batched {
@@ -214,6 +215,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
   const bool logf = o.use_log_formulation != 0;
   const bool newton_iter_act = o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER;
   const unsigned neg_mask = (unsigned)net.neg_mask;
+  const bool has_sorb = !ADJ && net.nkd + net.nionx > 0;  // the adjoint refuses sorption
   const int64_t ncells = st.ncells;
   const double* sc_sec = scratch;                                  // [ns][ncells]
   const double* sc_min = scratch + (size_t)ns * ncells;            // [nm][ncells]
@@ -323,6 +325,12 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
         init_tot[j] = tot[j];
         c[j] = guess[j];
         lnc[j] = lnguess[j];
+      }
+      if (has_sorb) {
+        // RAccumulationSorb into the fixed accumulation (reaction.F90:3836-3839):
+        // the sorbed total of the last evaluation, as the reference keeps it
+#pragma unroll
+        for (int j = 0; j < N; ++j) fixed[j] = fma(st.total_sorb[soa.at(j, cell)], volume, fixed[j]);
       }
       its = 0;
       r0 = 0.0;
@@ -511,6 +519,29 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
           L.Jf(fl) = fma(v, (logf || back) ? 1.0 : L.S(fl % N), L.Jf(fl));
         }
       }
+      // ---- equilibrium sorption: RTotalSorb inside RTAuxVarCompute, with
+      // RAccumulationSorb[Derivative] (reaction.F90:3861-3865, 3904-3909).
+      // The power table is dead after the minerals: it holds molality and
+      // gamma by species for the sorption routine.
+      bool sorb_fail = false;
+      if (has_sorb && !back) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          L.P(N + j) = c[j];
+          L.P(2 * N + j) = g[j];
+          st.total_sorb[soa.at(j, cell)] = 0.0;
+        }
+        const double v_t = volume * inv_dt;
+        sorb_fail = !total_sorb(
+            net, T, [&](int j) { return L.P(N + j); }, [&](int j) { return L.P(2 * N + j); },
+            [&](int m) { return vf[m]; }, st.porosity[cell], den_k,
+            st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr, ncells,
+            [&](int j, double v) {
+              st.total_sorb[soa.at(j, cell)] += v;
+              L.rhs(j) = fma(v_t, v, L.rhs(j));
+            },
+            [&](int i, int j, double v) { L.J(i, j) = fma(v_t * v, logf ? L.P(N + j) : 1.0, L.J(i, j)); });
+      }
       // ---- convergence tests on the residual (reaction.F90:3946-3953) -----
       double dot = 0.0;
       unsigned long long mxb = 0;
@@ -562,6 +593,8 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
             back_done = true;
           }
         }
+      } else if (sorb_fail) {
+        react_end = 1;  // RTAuxVarCompute's ierror: no total restore (reaction.F90:3861-3865)
       } else if (its > o.maximum_reaction_iterations) {
 #pragma unroll
         for (int j = 0; j < N; ++j) tot[j] = init_tot[j];

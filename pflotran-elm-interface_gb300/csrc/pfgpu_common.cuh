@@ -67,6 +67,11 @@ struct DevNet {
   int32_t o_sec_pidx, o_spair_ptr, o_spair_idx, o_mnrl_pidx, o_mpair_ptr, o_mpair_idx;
   int32_t o_spair_coef, o_mpair_coef;
   int32_t neg_mask;  // bit j: species j carries a negative coefficient somewhere
+  // equilibrium sorption (PfSorptionDesc): K_D rows and ion-exchange CSR
+  int32_t nkd, nionx, kd_units;
+  int32_t o_kd_spec, o_kd_type, o_kd_min, o_ix_ptr, o_ix_cat, o_ix_min, o_ix_zflag;
+  int32_t o_kd_coeff, o_kd_b, o_kd_n, o_ix_k, o_ix_cec;
+  double soil_density;
   double A, B, Bdot;
   PfOptions o;
   GroupTabs grp;
@@ -110,6 +115,19 @@ struct Tables {
   __device__ __forceinline__ int mpair_begin(int m) const { return I[net->o_mpair_ptr + m]; }
   __device__ __forceinline__ int mpair_idx(int q) const { return I[net->o_mpair_idx + q]; }
   __device__ __forceinline__ double mpair_coef(int q) const { return D[net->o_mpair_coef + q]; }
+  __device__ __forceinline__ int kd_spec(int r) const { return I[net->o_kd_spec + r]; }
+  __device__ __forceinline__ int kd_type(int r) const { return I[net->o_kd_type + r]; }
+  __device__ __forceinline__ int kd_min(int r) const { return I[net->o_kd_min + r]; }
+  __device__ __forceinline__ double kd_coeff(int r) const { return D[net->o_kd_coeff + r]; }
+  __device__ __forceinline__ double kd_b(int r) const { return D[net->o_kd_b + r]; }
+  __device__ __forceinline__ double kd_n(int r) const { return D[net->o_kd_n + r]; }
+  __device__ __forceinline__ int ix_begin(int r) const { return I[net->o_ix_ptr + r]; }
+  __device__ __forceinline__ int ix_end(int r) const { return I[net->o_ix_ptr + r + 1]; }
+  __device__ __forceinline__ int ix_cat(int p) const { return I[net->o_ix_cat + p]; }
+  __device__ __forceinline__ double ix_k(int p) const { return D[net->o_ix_k + p]; }
+  __device__ __forceinline__ double ix_cec(int r) const { return D[net->o_ix_cec + r]; }
+  __device__ __forceinline__ int ix_min(int r) const { return I[net->o_ix_min + r]; }
+  __device__ __forceinline__ int ix_zflag(int r) const { return I[net->o_ix_zflag + r]; }
 };
 
 // Fortran SIGN(1.d0, x)

@@ -7,8 +7,12 @@
 // the Crout LU (utility.F90:597-735) -- on per-thread arrays sized for the
 // largest ncomp of its bucket.  It is the baseline the batched kernel is
 // measured against, and a second, independent GPU statement of the algorithm.
+// With equilibrium sorption RTAuxVarCompute adds RTotalSorb and the
+// accumulation RAccumulationSorb[Derivative] (reaction.F90:3836-3839,
+// 3861-3865, 3904-3909), any ncomp.
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
 namespace plain {
@@ -19,6 +23,8 @@ struct Work {
   double dtotal[NMAX * NMAX];
   double J[NMAX * NMAX];
   double res[NMAX], fixed[NMAX], init_total[NMAX], update[NMAX];
+  double sorb[NMAX];          // total_sorb of the last evaluation
+  double dsorb[NMAX * NMAX];  // dtotal_sorb of the last evaluation
 };
 
 struct CellScalars {
@@ -252,6 +258,25 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
   int num_cuts = 0, n_const = 0, nsub = 0, its_total = 0, ierror_step = 0;
   const double psv_t = cs.porosity * cs.sat * 1000.0 * cs.volume;
   const bool dry = cs.sat < RT_MIN_SATURATION;
+  const bool has_sorb = net.nkd + net.nionx > 0;
+  double* ionx_ref = st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr;
+  // RTotalSorb (RZeroSorb first) at the current iterate into w.sorb,
+  // w.dsorb and the state
+  auto sorb_eval = [&]() {
+    for (int j = 0; j < n; ++j) {
+      w.sorb[j] = 0.0;
+      for (int k = 0; k < n; ++k) w.dsorb[j * NMAX + k] = 0.0;
+    }
+    const bool ok = total_sorb(
+        net, T, [&](int j) { return w.c[j]; }, [&](int j) { return w.gamma[j]; },
+        [&](int m) { return st.mnrl_volfrac[soa.at(m, cell)]; }, cs.porosity, cs.den_kg, ionx_ref, st.ncells,
+        [&](int j, double v) { w.sorb[j] = w.sorb[j] + v; },
+        [&](int i, int j, double v) { w.dsorb[i * NMAX + j] = w.dsorb[i * NMAX + j] + v; });
+    for (int j = 0; j < n; ++j) st.total_sorb[soa.at(j, cell)] = w.sorb[j];
+    return ok;
+  };
+  if (has_sorb)
+    for (int j = 0; j < n; ++j) w.sorb[j] = st.total_sorb[soa.at(j, cell)];
   for (;;) {
     if (cumulative >= target_time) break;
     // ------------------------------------------------------------- RReact
@@ -259,6 +284,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
     double r0 = 0.0;
     for (int j = 0; j < n; ++j) {
       w.fixed[j] = dry ? 0.0 : psv_t * total_io[j];
+      if (has_sorb) w.fixed[j] = w.fixed[j] + w.sorb[j] * cs.volume;  // RAccumulationSorb
       w.init_total[j] = total_io[j];
       w.c[j] = guess[j];
     }
@@ -266,6 +292,11 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
       its = its + 1;
       total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
       for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
+      // RTotalSorb; a failed ion-exchange solve fails RReact, no restore (:3861-3865)
+      if (has_sorb && !sorb_eval()) {
+        ierror = 1;
+        break;
+      }
       if (its > o.maximum_reaction_iterations) {
         ierror = 1;
         for (int j = 0; j < n; ++j) total_io[j] = w.init_total[j];
@@ -283,6 +314,16 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
           for (int k = 0; k < n; ++k) w.J[j * NMAX + k] = w.dtotal[j * NMAX + k] * psvd_t;
         }
         if (nm > 0) kinetic_mineral<NMAX>(T, net, n, mnrl_logK, cell, soa, st, cs, w, w.res, w.J);
+      }
+      if (has_sorb) {
+        // residual with the sorbed accumulation: (psv T + V S - fixed)/dt,
+        // Jacobian + dtotal_sorb V/dt; the minerals' terms are already in
+        // res, so add V S/dt to it (the same sum up to the order of terms)
+        const double v_t = cs.volume / dt;
+        for (int j = 0; j < n; ++j) {
+          w.res[j] = w.res[j] + w.sorb[j] * cs.volume / dt;
+          for (int k = 0; k < n; ++k) w.J[j * NMAX + k] = w.J[j * NMAX + k] + w.dsorb[j * NMAX + k] * v_t;
+        }
       }
       double dot = 0.0, mx = 0.0;
       for (int j = 0; j < n; ++j) {
@@ -324,6 +365,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
       // final RTAuxVarCompute (reaction.F90:4052)
       total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
       for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
+      if (has_sorb) sorb_eval();
     }
     its_total += its;
     // ---------------------------------------------------------- RStep control
