@@ -125,6 +125,17 @@ PfLaunchConfig default_launch(const DevNet& dev) {
   PfLaunchConfig c{};
   c.threads_per_block = 128;
   c.blocks_per_sm = 1;
+  if (!lane_supported(dev)) {
+    // no one-lane instantiation for this ncomp: a group of lanes per cell
+    for (int g : {4, 8, 2}) {
+      if (!group_supported(dev, g)) continue;
+      c.lanes_per_cell = g;
+      while (c.threads_per_block > 32 && batched_smem_bytes(dev, c) > 227u * 1024u) c.threads_per_block -= 32;
+      if (batched_smem_bytes(dev, c) <= 227u * 1024u) return c;
+      c.threads_per_block = 128;
+    }
+    c.lanes_per_cell = 0;
+  }
   c.jac_in_shared = dev.n <= 12 ? 1 : 0;
   // shrink until one block fits the 227 KB opt-in shared memory
   while (c.threads_per_block > 32 && batched_smem_bytes(dev, c) > 227u * 1024u) c.threads_per_block -= 32;
@@ -406,6 +417,7 @@ int32_t pf_network_set_launch(PfNetwork* net, const PfLaunchConfig* cfg) {
   const int G = cfg->lanes_per_cell;
   if (G != 0 && G != 1 && G != 2 && G != 4 && G != 8) return PF_ERR_INVALID;
   if (G > 1 && !group_supported(net->dev, G)) return PF_ERR_UNSUPPORTED;
+  if (G <= 1 && !lane_supported(net->dev)) return PF_ERR_UNSUPPORTED;
   if (batched_smem_bytes(net->dev, *cfg) > 227u * 1024u) return PF_ERR_TOO_LARGE;
   net->launch = *cfg;
   if (G <= 1) net->launch_lane = *cfg;
@@ -511,6 +523,7 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
   // setup scratch; otherwise one lane per cell with the last such config
   const bool grp = net->launch.lanes_per_cell > 1 &&
                    group_smem_bytes(d, net->launch, true) <= 227u * 1024u;
+  if (!grp && !lane_supported(d)) return PF_ERR_UNSUPPORTED;
   const size_t base = batched_scratch_doubles(d, state->ncells);
   rc = ensure_scratch_doubles(net, base + (grp ? group_adj_store_doubles(d, state->ncells) : 0));
   if (rc) return rc;

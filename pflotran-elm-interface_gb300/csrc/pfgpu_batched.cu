@@ -25,6 +25,13 @@ size_t batched_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg) {
 }
 
 bool batched_supported(const DevNet& net) {
+  if (lane_supported(net)) return true;
+  for (int g : {2, 4, 8})
+    if (group_supported(net, g)) return true;
+  return false;
+}
+
+bool lane_supported(const DevNet& net) {
   switch (net.n) {
 #define PF_CASE(N) case N:
     PF_BATCHED_NCOMPS(PF_CASE)

@@ -39,6 +39,8 @@ size_t batched_scratch_doubles(const DevNet& net, int64_t ncells);
 // shared memory bytes a batched launch of this config needs
 size_t batched_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg);
 bool batched_supported(const DevNet& net);
+// one lane per cell: ncomp has an instantiation of the persistent kernel
+bool lane_supported(const DevNet& net);
 
 // auxvar kernels (pfgpu_aux.cu)
 int launch_update_auxvars(const DevNet& net, const PfCellState& st, int update_act,

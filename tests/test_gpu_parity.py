@@ -316,3 +316,41 @@ def test_group_kernel_order_invariant_and_close_to_one_lane(oracle, lanes):
     assert same.float().mean() > 0.95
     d = (a.a["pri_molal"] - c.a["pri_molal"]).abs() / c.a["pri_molal"]
     assert float(d[:, same].max()) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ncomp", [5, 7, 9, 11, 14])
+def test_component_counts_without_one_lane_kernel(oracle, ncomp):
+    """ncomp values with no one-lane instantiation run through the batched
+    path on a group of lanes per cell (the default launch picks one) and meet
+    the same parity bar as the other networks: path-identical cells to
+    1e-10, flips and outliers within the oracle's own one-ulp sensitivity."""
+    from pfgpu import abi, generate
+    from pfgpu.engine import ReactionEngine
+    from pfgpu.network import default_options
+    net = generate.random_network(ncomp, 3 * ncomp, max(1, ncomp // 2), seed=900 + ncomp,
+                                  options=default_options(isothermal=0))
+    st, ct, cc = generate.random_cells(net, 400, seed=901 + ncomp, dt_range=(3600.0, 30 * 86400.0))
+    st, _ = cases.prepare(oracle, net, st, ct, cc)
+    ref = st.copy()
+    oracle.rstep(net, ref, 86400.0, nthreads=8)
+    perts = []
+    for key, to in (("total", np.inf), ("total", -np.inf), ("pri_molal", np.inf)):
+        p = st.copy()
+        p.a[key][:] = np.nextafter(p.a[key], to)
+        oracle.rstep(net, p, 86400.0, nthreads=8)
+        perts.append(p)
+    eng = ReactionEngine(net)
+    assert eng.launch_config()["lanes_per_cell"] > 1
+    assert eng.set_launch_config(128, 1, 0, 1) == abi.PF_ERR_UNSUPPORTED  # no one-lane kernel for this ncomp
+    dev = st.to("cuda")
+    eng.rstep(dev, 86400.0)
+    got = dev.numpy()
+    errs, flips, same, outliers, self_flips, self_out = compare(net, ref, got, "odd%d/default" % ncomp, perts)
+    n_single = int(same.sum()) + flips
+    slack = max(2, 0.01 * n_single)
+    assert same.sum() > 50
+    assert flips <= 2 * self_flips + slack, (flips, self_flips)
+    assert outliers <= 2 * self_out + slack, (outliers, self_out)
+    for k, v in errs.items():
+        assert v < REL, (k, v, errs)
