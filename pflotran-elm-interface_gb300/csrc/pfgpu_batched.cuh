@@ -145,6 +145,47 @@ __device__ __forceinline__ int lu_solve(Lane<N, JS>& L, int* indx, int stride) {
   return 0;
 }
 
+// LDL^T of the symmetric positive definite log-form Jacobian (the upper
+// triangle is read: J = U^T D U with U unit upper, stored above the
+// diagonal), solving J x = rhs in place; D^-1 in VV.  Half the flops of the
+// LU and no pivot search; the solution is that of the pivoted LU up to
+// rounding.  Returns 1 when a pivot is not positive and finite (the caller
+// then factorises again with the pivoted LU).
+template <int N, bool JS>
+__device__ __forceinline__ int ldl_solve(Lane<N, JS>& L) {
+  constexpr int U = (N <= 12) ? N : 1;
+#pragma unroll U
+  for (int k = 0; k < N; ++k) {
+    const double dk = L.J(k, k);
+    if (!(dk > 0.0) || absbits(dk) >= 0x7ff0000000000000ull) return 1;
+    const double inv = 1.0 / dk;
+#pragma unroll U
+    for (int i = k + 1; i < N; ++i) {
+      const double t = L.J(k, i) * inv;
+#pragma unroll U
+      for (int j = i; j < N; ++j) L.J(i, j) = fma(-t, L.J(k, j), L.J(i, j));
+    }
+    const double yk = L.rhs(k);
+#pragma unroll U
+    for (int i = k + 1; i < N; ++i) {
+      const double u = L.J(k, i) * inv;
+      L.J(k, i) = u;
+      L.rhs(i) = fma(-u, yk, L.rhs(i));
+    }
+    L.VV(k) = inv;
+  }
+#pragma unroll
+  for (int k = 0; k < N; ++k) L.rhs(k) = L.rhs(k) * L.VV(k);
+#pragma unroll U
+  for (int k = N - 1; k >= 0; --k) {
+    double xk = L.rhs(k);
+#pragma unroll U
+    for (int j = k + 1; j < N; ++j) xk = fma(-L.J(k, j), L.rhs(j), xk);
+    L.rhs(k) = xk;
+  }
+  return 0;
+}
+
 // Debye-Hueckel ln gamma (the exponent of RActivityCoefficients, LAG form)
 __device__ __forceinline__ double dh_ln_gamma(double z, double a0, double sI, double I, const DevNet& net) {
   return fabs(z) > 1.0e-10 ? (-z * z * sI * net.A / (1.0 + a0 * net.B * sI) + net.Bdot * I) * LOG_TO_LN : 0.0;
@@ -232,6 +273,10 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
   double temp = 25.0;
   double sqI = 0.0, lgI = 0.0;  // ionic strength of the last evaluation (NEWTON_ITER activity)
   bool dry = false;
+  // LDL^T unless a pivot failed on this evaluation (then it is redone, its
+  // count unchanged, with the pivoted LU) or activity coefficients follow
+  // each iteration (a redone evaluation would see this one's complexes)
+  bool use_lu = false, redo = false;
   // adjoint state (ADJ): converged iterate and dt of every substep, the
   // running dL/dT, direct dL/dT0 of floored components, per-lane gradient
   // accumulators for the network parameters, per-cell area gradient
@@ -346,7 +391,9 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       // Jacobian (J is symmetric in the log formulation), then accumulates
       // the parameter gradients.
       const bool back = ADJ && phase == BACK;
-      if (!back) its += 1;
+      if (!back && !redo) its += 1;
+      redo = false;
+      const bool ldl = (logf || back || dry) && !use_lu && !newton_iter_act;
       if (newton_iter_act) {
         // RActivityCoefficients LAG (reaction.F90:4553-4612) from this
         // iterate and the previous evaluation's sec_molal
@@ -421,8 +468,10 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       } else if (logf || back) {
 #pragma unroll
         for (int i = 0; i < N; ++i) {
+          if (!ldl) {  // LDL^T reads the upper triangle only
 #pragma unroll
-          for (int j = 0; j < i; ++j) L.J(i, j) = L.J(j, i);
+            for (int j = 0; j < i; ++j) L.J(i, j) = L.J(j, i);
+          }
           L.J(i, i) = fma(a_acc, c[i], L.J(i, i));
         }
         if (back) {
@@ -556,7 +605,12 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       int react_end = -1;  // -1: continue, 0: converged, 1: failed
       bool back_done = false, back_fail = false;
       if (back) {
-        if (lu_solve<N, JS>(L, indx, stride)) {
+        const int fr = ldl ? ldl_solve<N, JS>(L) : lu_solve<N, JS>(L, indx, stride);
+        if (!ldl) use_lu = false;
+        if (ldl && fr) {
+          use_lu = true;
+          redo = true;
+        } else if (fr) {
           back_fail = true;
         } else if constexpr (ADJ) {
           // u = rhs; lambda = (Tbar - u)/(psv/dt).  theta_bar += (dT/dtheta)^T u
@@ -603,7 +657,12 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
                  two_norm < o.max_rel_residual_tolerance * r0) {
         react_end = 0;
       } else {
-        if (lu_solve<N, JS>(L, indx, stride)) {
+        const int fr = ldl ? ldl_solve<N, JS>(L) : lu_solve<N, JS>(L, indx, stride);
+        if (!ldl) use_lu = false;
+        if (ldl && fr) {
+          use_lu = true;  // react_end stays -1: the evaluation repeats with the pivoted LU
+          redo = true;
+        } else if (fr) {
           react_end = 1;  // singular: no total restore (reaction.F90:3963-3966)
         } else {
           const double tol = o.max_relative_change_tolerance;

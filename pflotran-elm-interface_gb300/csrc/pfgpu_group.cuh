@@ -145,6 +145,12 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   double psv = 0, den_L = 0, den_k = 0, volume = 0, target = 0, cum = 0, dt = 0, inv_dt = 0, r0 = 0;
   double sqI = 0.0, lgI = 0.0;
   bool dry = false, zero_step = false;
+  // factorisation: LDL^T of the symmetric positive definite log-form
+  // Jacobian; the pivoted LU on the rare trip where a pivot of LDL^T is not
+  // positive (the evaluation is then redone, its count unchanged), and
+  // always when activity coefficients follow each Newton iteration (a redone
+  // evaluation would see this evaluation's complexes)
+  bool use_lu = false, redo = false;
   int its = 0, its_total = 0, nsub = 0, num_cuts = 0, n_const = 0;
   // own species / rows i = r + G*t
   double c[R], lnc[R], g[R], tot[R], fixed[R], init_tot[R], guess[R], lnguess[R], small_val[R];
@@ -251,7 +257,9 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
     // (a backward trip, BACK, shares the evaluation and the factorisation)
     if (phase == ITER || (ADJ && phase == BACK)) {
       const bool back = ADJ && phase == BACK;
-      if (!back) its += 1;
+      if (!back && !redo) its += 1;
+      redo = false;
+      const bool ldl = !use_lu && !newton_iter_act;
       if (newton_iter_act) {
         // RActivityCoefficients LAG from this iterate and the previous
         // evaluation's sec_molal (reaction.F90:4553-4612)
@@ -371,7 +379,8 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         const int i = r + G * t;
         if (i >= n) continue;
         double* Jr = J + i * n;
-        for (int j = 0; j < n; ++j) Jr[j] = 0.0;
+        const int jend = ldl ? i + 1 : n;  // LDL^T reads the lower triangle only
+        for (int j = 0; j < jend; ++j) Jr[j] = 0.0;
         double Sa = 0.0;
         for (int q = gt.sp_ptr[i]; q < gt.sp_ptr[i + 1]; ++q) {
           const int s = gt.sp_s[q];
@@ -381,7 +390,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           const double co = nui * sa;
           for (int p = T.sec_begin(s); p < T.sec_end(s); ++p) {
             const int j = T.sec_idx(p);
-            Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
+            if (j < jend) Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
           }
         }
         double rr;
@@ -400,11 +409,11 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           const double co = nui * mf[m];
           for (int p = T.mnrl_begin(m); p < T.mnrl_end(m); ++p) {
             const int j = T.mnrl_idx(p);
-            Jr[j] = fma(T.mnrl_nu(p), co, Jr[j]);
+            if (j < jend) Jr[j] = fma(T.mnrl_nu(p), co, Jr[j]);
           }
         }
         if (dry)
-          for (int j = 0; j < n; ++j) Jr[j] = (i == j) ? c[t] : 0.0;
+          for (int j = 0; j < jend; ++j) Jr[j] = (i == j) ? c[t] : 0.0;
         rhsv[i] = rr;
         dot_p = fma(rr, rr, dot_p);
         mx_p = max(mx_p, absbits(rr));
@@ -426,6 +435,51 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
       }
       if (back || react_end < 0) {
         __syncwarp(gmask);
+        bool solved = false;
+        if (ldl) {
+          // ---- LDL^T, right-looking over the lower triangle; the forward
+          // solve L y = rhs rides along; D^-1 in vvs, L below the diagonal
+          bool fail = false;
+          for (int k = 0; k < n; ++k) {
+            const double dk = J[k * n + k];
+            if (!(dk > 0.0) || absbits(dk) >= 0x7ff0000000000000ull) {  // same value in every lane
+              fail = true;
+              break;
+            }
+            const double inv = 1.0 / dk;
+            const int i0 = k + 1 + ((r - (k + 1)) % G + G) % G;  // first own row below k
+            for (int i = i0; i < n; i += G) {
+              const double tl = J[i * n + k] * inv;
+              double* Ji = J + i * n;
+              for (int j = k + 1; j <= i; ++j) Ji[j] = fma(-tl, J[j * n + k], Ji[j]);
+            }
+            __syncwarp(gmask);
+            const double yk = rhsv[k];
+            for (int i = i0; i < n; i += G) {
+              const double l = J[i * n + k] * inv;
+              J[i * n + k] = l;
+              rhsv[i] = fma(-l, yk, rhsv[i]);
+            }
+            if (r == k % G) vvs[k] = inv;
+            __syncwarp(gmask);
+          }
+          if (fail) {
+            use_lu = true;  // factorise this evaluation again with pivoting
+            redo = true;
+          } else {
+            // D^-1, then the backward solve L^T x = z by columns
+            for (int i = r; i < n; i += G) rhsv[i] = rhsv[i] * vvs[i];
+            __syncwarp(gmask);
+            for (int k = n - 1; k >= 0; --k) {
+              const double xk = rhsv[k];
+              if (r == 0) xs[k] = xk;
+              for (int i = r; i < k; i += G) rhsv[i] = fma(-J[k * n + i], xk, rhsv[i]);
+              __syncwarp(gmask);
+            }
+            solved = true;
+          }
+        } else {
+        use_lu = false;
         // ---- implicit-pivot scales (utility.F90:621-644), rows over the lanes
         bool bad = false;
         for (int i = r; i < n; i += G) {
@@ -498,6 +552,10 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
             }
             __syncwarp(gmask);
           }
+          solved = true;
+        }
+        }
+        if (solved) {
           __syncwarp(gmask);
           if constexpr (ADJ) {
             if (back) {
