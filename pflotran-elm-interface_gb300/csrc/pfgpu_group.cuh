@@ -448,19 +448,30 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
             }
             const double inv = 1.0 / dk;
             const int i0 = k + 1 + ((r - (k + 1)) % G + G) % G;  // first own row below k
-            for (int i = i0; i < n; i += G) {
-              const double tl = J[i * n + k] * inv;
-              double* Ji = J + i * n;
-              for (int j = k + 1; j <= i; ++j) Ji[j] = fma(-tl, J[j * n + k], Ji[j]);
-            }
-            __syncwarp(gmask);
+            // column k: keep the unscaled values (xs is free until the
+            // solve), store l_ik = a_ik / d_k, forward-eliminate the rhs
             const double yk = rhsv[k];
             for (int i = i0; i < n; i += G) {
-              const double l = J[i * n + k] * inv;
+              const double a = J[i * n + k];
+              xs[i] = a;
+              const double l = a * inv;
               J[i * n + k] = l;
               rhsv[i] = fma(-l, yk, rhsv[i]);
             }
             if (r == k % G) vvs[k] = inv;
+            __syncwarp(gmask);
+            // trailing update a_ij -= l_ik a_jk over the (n-k-1)(n-k)/2
+            // entries k < j <= i, dealt round-robin to the lanes (rows of
+            // unequal length would leave lanes idle)
+            {
+              int i = k + 1, j = k + 1 + r;  // entry r of the row-major triangle
+              while (i < n && j > i) { j -= i - k; i += 1; }
+              while (i < n) {
+                J[i * n + j] = fma(-J[i * n + k], xs[j], J[i * n + j]);
+                j += G;
+                while (i < n && j > i) { j -= i - k; i += 1; }
+              }
+            }
             __syncwarp(gmask);
           }
           if (fail) {
