@@ -228,6 +228,49 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_mpair_idx = (int)ints.size();
   ints.insert(ints.end(), mpair_idx.begin(), mpair_idx.end());
   dev.neg_mask = neg_mask;
+  // per-entry Jacobian assembly (group kernel, LDL^T): every lower-triangle
+  // entry (i >= j, row-major, e = i(i+1)/2 + j) with the complexes and the
+  // minerals that contain both species and the coefficient nu_i nu_j
+  std::vector<int32_t> ent_sc, ent_mm;
+  std::vector<double> ent_cf, ent_mcf;
+  {
+    std::vector<std::vector<std::pair<int, double>>> es(n * (n + 1) / 2), em(n * (n + 1) / 2);
+    for (int sx = 0; sx < ns; ++sx)
+      for (int a = 0; a < d->sec_nspec[sx]; ++a)
+        for (int b = 0; b < d->sec_nspec[sx]; ++b) {
+          const int i = d->sec_spec[sx * d->sec_stride + a], j = d->sec_spec[sx * d->sec_stride + b];
+          if (j > i) continue;
+          es[i * (i + 1) / 2 + j].push_back(
+              {sx, d->sec_stoich[sx * d->sec_stride + a] * d->sec_stoich[sx * d->sec_stride + b]});
+        }
+    for (int m = 0; m < nm; ++m)
+      for (int a = 0; a < d->mnrl_nspec[m]; ++a)
+        for (int b = 0; b < d->mnrl_nspec[m]; ++b) {
+          const int i = d->mnrl_spec[m * d->mnrl_stride + a], j = d->mnrl_spec[m * d->mnrl_stride + b];
+          if (j > i) continue;
+          em[i * (i + 1) / 2 + j].push_back(
+              {m, d->mnrl_stoich[m * d->mnrl_stride + a] * d->mnrl_stoich[m * d->mnrl_stride + b]});
+        }
+    dev.o_ent_ij = (int)ints.size();
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j <= i; ++j) ints.push_back(i * n + j);
+    dev.o_ent_ptr = (int)ints.size();
+    for (auto& v : es) {
+      ints.push_back((int32_t)ent_sc.size());
+      for (auto& pr : v) { ent_sc.push_back(pr.first); ent_cf.push_back(pr.second); }
+    }
+    ints.push_back((int32_t)ent_sc.size());
+    dev.o_ent_sc = (int)ints.size();
+    ints.insert(ints.end(), ent_sc.begin(), ent_sc.end());
+    dev.o_ent_mptr = (int)ints.size();
+    for (auto& v : em) {
+      ints.push_back((int32_t)ent_mm.size());
+      for (auto& pr : v) { ent_mm.push_back(pr.first); ent_mcf.push_back(pr.second); }
+    }
+    ints.push_back((int32_t)ent_mm.size());
+    dev.o_ent_mm = (int)ints.size();
+    ints.insert(ints.end(), ent_mm.begin(), ent_mm.end());
+  }
   // sorption: K_D rows; ion-exchange reactions as CSR over their cations
   const PfSorptionDesc* sd = d->sorption;
   const int nkd = sd ? sd->nkd : 0, nix = sd ? sd->nionx : 0;
@@ -294,6 +337,8 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_power = put(d->mnrl_affinity_power, nm, 1.0);
   dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);
   dev.o_mpair_coef = put(mpair_coef.data(), (int)mpair_coef.size(), 0.0);
+  dev.o_ent_cf = put(ent_cf.data(), (int)ent_cf.size(), 0.0);
+  dev.o_ent_mcf = put(ent_mcf.data(), (int)ent_mcf.size(), 0.0);
   dev.o_kd_coeff = put(nkd ? sd->kd_coeff : nullptr, nkd, 0.0);
   dev.o_kd_b = put(nkd ? sd->kd_langmuir_b : nullptr, nkd, 0.0);
   dev.o_kd_n = put(nkd ? sd->kd_freundlich_n : nullptr, nkd, 1.0);

@@ -66,6 +66,9 @@ struct DevNet {
   // ordered pairs)
   int32_t o_sec_pidx, o_spair_ptr, o_spair_idx, o_mnrl_pidx, o_mpair_ptr, o_mpair_idx;
   int32_t o_spair_coef, o_mpair_coef;
+  // per-entry assembly of the lower triangle (group kernel): entry e -> flat
+  // index i*n+j; CSR over contributing complexes / minerals with nu_i nu_j
+  int32_t o_ent_ij, o_ent_ptr, o_ent_sc, o_ent_mptr, o_ent_mm, o_ent_cf, o_ent_mcf;
   int32_t neg_mask;  // bit j: species j carries a negative coefficient somewhere
   // equilibrium sorption (PfSorptionDesc): K_D rows and ion-exchange CSR
   int32_t nkd, nionx, kd_units;
@@ -115,6 +118,15 @@ struct Tables {
   __device__ __forceinline__ int mpair_begin(int m) const { return I[net->o_mpair_ptr + m]; }
   __device__ __forceinline__ int mpair_idx(int q) const { return I[net->o_mpair_idx + q]; }
   __device__ __forceinline__ double mpair_coef(int q) const { return D[net->o_mpair_coef + q]; }
+  __device__ __forceinline__ int ent_ij(int e) const { return I[net->o_ent_ij + e]; }
+  __device__ __forceinline__ int ent_begin(int e) const { return I[net->o_ent_ptr + e]; }
+  __device__ __forceinline__ int ent_end(int e) const { return I[net->o_ent_ptr + e + 1]; }
+  __device__ __forceinline__ int ent_sc(int q) const { return I[net->o_ent_sc + q]; }
+  __device__ __forceinline__ double ent_cf(int q) const { return D[net->o_ent_cf + q]; }
+  __device__ __forceinline__ int ent_mbegin(int e) const { return I[net->o_ent_mptr + e]; }
+  __device__ __forceinline__ int ent_mend(int e) const { return I[net->o_ent_mptr + e + 1]; }
+  __device__ __forceinline__ int ent_mm(int q) const { return I[net->o_ent_mm + q]; }
+  __device__ __forceinline__ double ent_mcf(int q) const { return D[net->o_ent_mcf + q]; }
   __device__ __forceinline__ int kd_spec(int r) const { return I[net->o_kd_spec + r]; }
   __device__ __forceinline__ int kd_type(int r) const { return I[net->o_kd_type + r]; }
   __device__ __forceinline__ int kd_min(int r) const { return I[net->o_kd_min + r]; }

@@ -290,6 +290,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           const double a = c[t] * g[t];
           pw[i] = a;
           pw[n + i] = a * a;
+          xs[i] = c[t];  // molality by species for the entry assembly (xs is free until the solve)
           if (neg_mask & (1u << i)) {
             const double ia = 1.0 / a;
             pw[2 * n + i] = ia;
@@ -379,18 +380,21 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         const int i = r + G * t;
         if (i >= n) continue;
         double* Jr = J + i * n;
-        const int jend = ldl ? i + 1 : n;  // LDL^T reads the lower triangle only
-        for (int j = 0; j < jend; ++j) Jr[j] = 0.0;
+        // the pivoted LU (fallback) assembles full rows here; LDL^T assembles
+        // the lower triangle entry by entry below
+        if (!ldl)
+          for (int j = 0; j < n; ++j) Jr[j] = 0.0;
         double Sa = 0.0;
         for (int q = gt.sp_ptr[i]; q < gt.sp_ptr[i + 1]; ++q) {
           const int s = gt.sp_s[q];
           const double sa = a_acc * sv[s];
           const double nui = T.sec_nu(gt.sp_p[q]);
           Sa = fma(nui, sa, Sa);
+          if (ldl) continue;
           const double co = nui * sa;
           for (int p = T.sec_begin(s); p < T.sec_end(s); ++p) {
             const int j = T.sec_idx(p);
-            if (j < jend) Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
+            Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
           }
         }
         double rr;
@@ -400,23 +404,41 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         } else {
           rr = 0.0;  // backward solve J u = B Tbar
         }
-        Jr[i] = fma(a_acc, c[t], Jr[i]);
+        if (!ldl) Jr[i] = fma(a_acc, c[t], Jr[i]);
         for (int q = gt.mp_ptr[i]; q < gt.mp_ptr[i + 1]; ++q) {
           const int m = gt.mp_m[q];
           const double nui = T.mnrl_nu(gt.mp_p[q]);
           if (back) rr = fma(nui * mf[m], nuT[m], rr);
           else if (!dry) rr = fma(nui, mIm[m], rr);
+          if (ldl) continue;
           const double co = nui * mf[m];
           for (int p = T.mnrl_begin(m); p < T.mnrl_end(m); ++p) {
             const int j = T.mnrl_idx(p);
-            if (j < jend) Jr[j] = fma(T.mnrl_nu(p), co, Jr[j]);
+            Jr[j] = fma(T.mnrl_nu(p), co, Jr[j]);
           }
         }
-        if (dry)
-          for (int j = 0; j < jend; ++j) Jr[j] = (i == j) ? c[t] : 0.0;
+        if (dry && !ldl)
+          for (int j = 0; j < n; ++j) Jr[j] = (i == j) ? c[t] : 0.0;
         rhsv[i] = rr;
         dot_p = fma(rr, rr, dot_p);
         mx_p = max(mx_p, absbits(rr));
+      }
+      if (ldl) {
+        // ---- lower triangle entry by entry, dealt round-robin to the lanes:
+        // J_ij = a_acc (m_i d_ij + sum_s nu_si nu_sj s_s) + sum_m nu_mi nu_mj f_m
+        // from the per-entry lists of complexes and minerals (one store per entry)
+        const int ne = n * (n + 1) / 2;
+        for (int e = r; e < ne; e += G) {
+          const int f = T.ent_ij(e);
+          const int i = f / n, j = f - i * n;
+          double acc = 0.0;
+          for (int q = T.ent_begin(e); q < T.ent_end(e); ++q) acc = fma(T.ent_cf(q), sv[T.ent_sc(q)], acc);
+          if (i == j) acc = acc + xs[i];
+          double v = a_acc * acc;
+          for (int q = T.ent_mbegin(e); q < T.ent_mend(e); ++q) v = fma(T.ent_mcf(q), mf[T.ent_mm(q)], v);
+          if (dry) v = (i == j) ? xs[i] : 0.0;
+          J[f] = v;
+        }
       }
       // ---- convergence tests on the residual (reaction.F90:3946-3953)
       const double two_norm = sqrt(gsum<G>(dot_p, gmask));
