@@ -193,11 +193,14 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   for (int i = 0; i < ns; ++i)
     for (int s2 = 0; s2 < d->sec_nspec[i]; ++s2)
       ints.push_back(code_of(d->sec_stoich[i * d->sec_stride + s2], d->sec_spec[i * d->sec_stride + s2]));
-  std::vector<int32_t> spair_idx, mpair_idx;
+  // the pair tables of the one-lane kernel go to the end of the blocks
+  // (lane_ints / pair coefficients, offsets fixed up there), so that the
+  // group kernel stages only the prefix it reads
+  std::vector<int32_t> spair_idx, mpair_idx, lane_ints;
   std::vector<double> spair_coef, mpair_coef;
-  dev.o_spair_ptr = (int)ints.size();
+  dev.o_spair_ptr = (int)lane_ints.size();
   for (int i = 0; i < ns; ++i) {
-    ints.push_back((int32_t)spair_idx.size());
+    lane_ints.push_back((int32_t)spair_idx.size());
     const int b = i * d->sec_stride, cnt = d->sec_nspec[i];
     for (int p = 0; p < cnt; ++p)
       for (int q = p; q < cnt; ++q) {
@@ -207,16 +210,16 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
         spair_coef.push_back(d->sec_stoich[b + p] * d->sec_stoich[b + q]);
       }
   }
-  ints.push_back((int32_t)spair_idx.size());
-  dev.o_spair_idx = (int)ints.size();
-  ints.insert(ints.end(), spair_idx.begin(), spair_idx.end());
+  lane_ints.push_back((int32_t)spair_idx.size());
+  dev.o_spair_idx = (int)lane_ints.size();
+  lane_ints.insert(lane_ints.end(), spair_idx.begin(), spair_idx.end());
   dev.o_mnrl_pidx = (int)ints.size();
   for (int m = 0; m < nm; ++m)
     for (int s2 = 0; s2 < d->mnrl_nspec[m]; ++s2)
       ints.push_back(code_of(d->mnrl_stoich[m * d->mnrl_stride + s2], d->mnrl_spec[m * d->mnrl_stride + s2]));
-  dev.o_mpair_ptr = (int)ints.size();
+  dev.o_mpair_ptr = (int)lane_ints.size();
   for (int m = 0; m < nm; ++m) {
-    ints.push_back((int32_t)mpair_idx.size());
+    lane_ints.push_back((int32_t)mpair_idx.size());
     const int b = m * d->mnrl_stride, cnt = d->mnrl_nspec[m];
     for (int p = 0; p < cnt; ++p)
       for (int q = 0; q < cnt; ++q) {
@@ -224,9 +227,9 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
         mpair_coef.push_back(d->mnrl_stoich[b + p] * d->mnrl_stoich[b + q]);
       }
   }
-  ints.push_back((int32_t)mpair_idx.size());
-  dev.o_mpair_idx = (int)ints.size();
-  ints.insert(ints.end(), mpair_idx.begin(), mpair_idx.end());
+  lane_ints.push_back((int32_t)mpair_idx.size());
+  dev.o_mpair_idx = (int)lane_ints.size();
+  lane_ints.insert(lane_ints.end(), mpair_idx.begin(), mpair_idx.end());
   dev.neg_mask = neg_mask;
   // per-entry Jacobian assembly (group kernel, LDL^T): every lower-triangle
   // entry (i >= j, row-major, e = i(i+1)/2 + j) with the complexes and the
@@ -307,6 +310,16 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
         }
     ints.push_back(zf ? 1 : 0);
   }
+  while (ints.size() % 4) ints.push_back(0);  // 16-byte boundary: the group kernel's staged prefix ends here
+  dev.int_words_grp = (int)ints.size();
+  {
+    const int base = (int)ints.size();
+    dev.o_spair_ptr += base;
+    dev.o_spair_idx += base;
+    dev.o_mpair_ptr += base;
+    dev.o_mpair_idx += base;
+    ints.insert(ints.end(), lane_ints.begin(), lane_ints.end());
+  }
   while (ints.size() % 4) ints.push_back(0);
   auto put = [&](const double* src, int count, double dflt) {
     int off = (int)dbls.size();
@@ -335,8 +348,6 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_msf = put(d->mnrl_min_scale_factor, nm, 1.0);
   dev.o_temkin = put(d->mnrl_Temkin_const, nm, 1.0);
   dev.o_power = put(d->mnrl_affinity_power, nm, 1.0);
-  dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);
-  dev.o_mpair_coef = put(mpair_coef.data(), (int)mpair_coef.size(), 0.0);
   dev.o_ent_cf = put(ent_cf.data(), (int)ent_cf.size(), 0.0);
   dev.o_ent_mcf = put(ent_mcf.data(), (int)ent_mcf.size(), 0.0);
   dev.o_kd_coeff = put(nkd ? sd->kd_coeff : nullptr, nkd, 0.0);
@@ -346,6 +357,10 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   for (int r = 0; r < nix; ++r)
     for (int j = 0; j < sd->ionx_ncation[r]; ++j) dbls.push_back(sd->ionx_k[r * sd->ionx_stride + j]);
   dev.o_ix_cec = put(nix ? sd->ionx_cec : nullptr, nix, 0.0);
+  while (dbls.size() % 2) dbls.push_back(0.0);  // 16-byte boundary: end of the group kernel's prefix
+  dev.dbl_words_grp = (int)dbls.size();
+  dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);
+  dev.o_mpair_coef = put(mpair_coef.data(), (int)mpair_coef.size(), 0.0);
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
               (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |

@@ -51,6 +51,8 @@ struct DevNet {
   int32_t flags;
   int32_t int_words;     // number of int32 words in the int block
   int32_t dbl_words;     // number of doubles in the double block
+  int32_t int_words_grp; // the prefixes the group kernel stages (it reads
+  int32_t dbl_words_grp; //   no pair table of the one-lane kernel)
   const int32_t* ints;   // device: start of int block (16-byte aligned)
   const double* dbls;    // device: start of double block (16-byte aligned)
   // offsets (in elements) into the int block

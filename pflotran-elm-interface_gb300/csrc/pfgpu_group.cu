@@ -69,7 +69,7 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
 }
 
 size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
-  const size_t tables = (size_t)net.int_words * 4 + (size_t)net.dbl_words * 8;
+  const size_t tables = (size_t)net.int_words_grp * 4 + (size_t)net.dbl_words_grp * 8;
   const int G = cfg.lanes_per_cell > 0 ? cfg.lanes_per_cell : 1;
   const size_t cells = (size_t)cfg.threads_per_block / (size_t)G;
   return tables + cells * ((size_t)group::ws_doubles(net, adj, G) * 8 + (size_t)net.n * 8);

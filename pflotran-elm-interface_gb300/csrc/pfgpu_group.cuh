@@ -61,8 +61,8 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   __shared__ __align__(8) uint64_t tma_bar;
   const int tid = threadIdx.x;
   const int lane_id = tid & 31;
-  const uint32_t ibytes = (uint32_t)net.int_words * 4u;
-  const uint32_t dbytes = (uint32_t)net.dbl_words * 8u;
+  const uint32_t ibytes = (uint32_t)net.int_words_grp * 4u;  // the prefixes this kernel reads
+  const uint32_t dbytes = (uint32_t)net.dbl_words_grp * 8u;
   int32_t* sI = reinterpret_cast<int32_t*>(smem);
   double* sD = reinterpret_cast<double*>(smem + ibytes);
 
