@@ -43,6 +43,8 @@ struct GroupTabs {
   const int32_t* mp_ptr;
   const int32_t* mp_m;
   const int32_t* mp_p;
+  const double* sp_nu;  // nu of species i in complex sp_s[q] / mineral mp_m[q]
+  const double* mp_nu;
 };
 
 struct DevNet {

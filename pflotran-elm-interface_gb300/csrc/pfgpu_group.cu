@@ -95,7 +95,6 @@ int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState
 }
 
 int group_build_tables(const DevNet& net, const int32_t* I, const double* D, void** d_buf, GroupTabs* out) {
-  (void)D;
   const int n = net.n;
   std::vector<std::vector<int32_t>> ss(n), sp(n), mm(n), mp(n);
   for (int s = 0; s < net.ns; ++s)
@@ -123,13 +122,26 @@ int group_build_tables(const DevNet& net, const int32_t* I, const double* D, voi
   int o1, o2, o3, o4, o5, o6;
   csr(ss, sp, &o1, &o2, &o3);
   csr(mm, mp, &o4, &o5, &o6);
+  // the stoichiometric coefficients along the same lists, after the ints
+  std::vector<double> nus;
+  for (auto& rw : sp)
+    for (int p : rw) nus.push_back(D[net.o_sec_nu + p]);
+  const size_t o_mnu = nus.size();
+  for (auto& rw : mp)
+    for (int p : rw) nus.push_back(D[net.o_mnrl_nu + p]);
+  while (ints.size() % 4) ints.push_back(0);
+  const size_t ibytes = ints.size() * 4;
   void* buf = nullptr;
-  if (cudaMalloc(&buf, ints.size() * 4) != cudaSuccess) return PF_ERR_CUDA;
-  if (cudaMemcpy(buf, ints.data(), ints.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (cudaMalloc(&buf, ibytes + nus.size() * 8 + 8) != cudaSuccess) return PF_ERR_CUDA;
+  if (cudaMemcpy(buf, ints.data(), ibytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+      (!nus.empty() &&
+       cudaMemcpy((char*)buf + ibytes, nus.data(), nus.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess)) {
     cudaFree(buf);
     return PF_ERR_CUDA;
   }
   const int32_t* d = (const int32_t*)buf;
+  out->sp_nu = reinterpret_cast<const double*>((const char*)buf + ibytes);
+  out->mp_nu = out->sp_nu + o_mnu;
   out->sp_ptr = d + o1;
   out->sp_s = d + o2;
   out->sp_p = d + o3;

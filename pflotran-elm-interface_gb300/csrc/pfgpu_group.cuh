@@ -385,16 +385,20 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         if (!ldl)
           for (int j = 0; j < n; ++j) Jr[j] = 0.0;
         double Sa = 0.0;
-        for (int q = gt.sp_ptr[i]; q < gt.sp_ptr[i + 1]; ++q) {
-          const int s = gt.sp_s[q];
-          const double sa = a_acc * sv[s];
-          const double nui = T.sec_nu(gt.sp_p[q]);
-          Sa = fma(nui, sa, Sa);
-          if (ldl) continue;
-          const double co = nui * sa;
-          for (int p = T.sec_begin(s); p < T.sec_end(s); ++p) {
-            const int j = T.sec_idx(p);
-            Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
+        if (ldl) {
+          for (int q = gt.sp_ptr[i]; q < gt.sp_ptr[i + 1]; ++q) Sa = fma(gt.sp_nu[q], sv[gt.sp_s[q]], Sa);
+          Sa = a_acc * Sa;
+        } else {
+          for (int q = gt.sp_ptr[i]; q < gt.sp_ptr[i + 1]; ++q) {
+            const int s = gt.sp_s[q];
+            const double sa = a_acc * sv[s];
+            const double nui = T.sec_nu(gt.sp_p[q]);
+            Sa = fma(nui, sa, Sa);
+            const double co = nui * sa;
+            for (int p = T.sec_begin(s); p < T.sec_end(s); ++p) {
+              const int j = T.sec_idx(p);
+              Jr[j] = fma(T.sec_nu(p), co, Jr[j]);
+            }
           }
         }
         double rr;
@@ -407,7 +411,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         if (!ldl) Jr[i] = fma(a_acc, c[t], Jr[i]);
         for (int q = gt.mp_ptr[i]; q < gt.mp_ptr[i + 1]; ++q) {
           const int m = gt.mp_m[q];
-          const double nui = T.mnrl_nu(gt.mp_p[q]);
+          const double nui = gt.mp_nu[q];
           if (back) rr = fma(nui * mf[m], nuT[m], rr);
           else if (!dry) rr = fma(nui, mIm[m], rr);
           if (ldl) continue;
