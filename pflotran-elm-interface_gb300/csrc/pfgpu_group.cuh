@@ -213,7 +213,12 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
               c[t] = guess[t];
             }
           }
-          for (int s = r; s < ns; s += G) Ks[s] = sc_sec[soa.at(s, cell)];
+          for (int s = r; s < ns; s += G) {
+            Ks[s] = sc_sec[soa.at(s, cell)];
+            // the complexes' molalities live in sv for the whole cell (the
+            // last evaluation's, as rt_auxvar holds them); written back once
+            sv[s] = st.sec_molal[soa.at(s, cell)];
+          }
           for (int m = r; m < nm; m += G) {
             Km[m] = sc_min[soa.at(m, cell)];
             vfm[m] = st.mnrl_volfrac[soa.at(m, cell)];
@@ -271,7 +276,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         }
         for (int s = r; s < ns; s += G) {
           const double z = T.sec_Z(s);
-          Ip = Ip + st.sec_molal[soa.at(s, cell)] * z * z;
+          Ip = Ip + sv[s] * z * z;
         }
         const double I = 0.5 * gsum<G>(Ip, gmask);
         sqI = sqrt(I);
@@ -308,7 +313,6 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           v *= (pe >= 0) ? pw[pe] : exp(T.sec_nu(p) * log(pw[T.sec_idx(p)]));
         }
         sv[s] = v;
-        if (!back) st.sec_molal[soa.at(s, cell)] = v;
       }
       // ---- kinetic minerals m = r, r+G, ... (reaction_mineral.F90:647-1078)
       for (int m = r; m < nm; m += G) {
@@ -746,6 +750,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
           if (newton_iter_act) st.pri_act_coef[soa.at(i, cell)] = g[t];
         }
       }
+      for (int s = r; s < ns; s += G) st.sec_molal[soa.at(s, cell)] = sv[s];
       if (newton_iter_act)
         for (int s = r; s < ns; s += G)
           st.sec_act_coef[soa.at(s, cell)] = exp(dh_ln_gamma(T.sec_Z(s), T.sec_a0(s), sqI, lgI, net));
