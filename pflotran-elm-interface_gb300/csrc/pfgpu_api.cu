@@ -234,7 +234,7 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   // per-entry Jacobian assembly (group kernel, LDL^T): every lower-triangle
   // entry (i >= j, row-major, e = i(i+1)/2 + j) with the complexes and the
   // minerals that contain both species and the coefficient nu_i nu_j
-  std::vector<int32_t> ent_sc, ent_mm;
+  std::vector<int32_t> ent_sc, ent_mm, ent_ints;
   std::vector<double> ent_cf, ent_mcf;
   {
     std::vector<std::vector<std::pair<int, double>>> es(n * (n + 1) / 2), em(n * (n + 1) / 2);
@@ -254,25 +254,26 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
           em[i * (i + 1) / 2 + j].push_back(
               {m, d->mnrl_stoich[m * d->mnrl_stride + a] * d->mnrl_stoich[m * d->mnrl_stride + b]});
         }
-    dev.o_ent_ij = (int)ints.size();
+    // into ent_ints (offsets relative to it, fixed up where it is appended)
+    dev.o_ent_ij = (int)ent_ints.size();
     for (int i = 0; i < n; ++i)
-      for (int j = 0; j <= i; ++j) ints.push_back(i * n + j);
-    dev.o_ent_ptr = (int)ints.size();
+      for (int j = 0; j <= i; ++j) ent_ints.push_back(i * n + j);
+    dev.o_ent_ptr = (int)ent_ints.size();
     for (auto& v : es) {
-      ints.push_back((int32_t)ent_sc.size());
+      ent_ints.push_back((int32_t)ent_sc.size());
       for (auto& pr : v) { ent_sc.push_back(pr.first); ent_cf.push_back(pr.second); }
     }
-    ints.push_back((int32_t)ent_sc.size());
-    dev.o_ent_sc = (int)ints.size();
-    ints.insert(ints.end(), ent_sc.begin(), ent_sc.end());
-    dev.o_ent_mptr = (int)ints.size();
+    ent_ints.push_back((int32_t)ent_sc.size());
+    dev.o_ent_sc = (int)ent_ints.size();
+    ent_ints.insert(ent_ints.end(), ent_sc.begin(), ent_sc.end());
+    dev.o_ent_mptr = (int)ent_ints.size();
     for (auto& v : em) {
-      ints.push_back((int32_t)ent_mm.size());
+      ent_ints.push_back((int32_t)ent_mm.size());
       for (auto& pr : v) { ent_mm.push_back(pr.first); ent_mcf.push_back(pr.second); }
     }
-    ints.push_back((int32_t)ent_mm.size());
-    dev.o_ent_mm = (int)ints.size();
-    ints.insert(ints.end(), ent_mm.begin(), ent_mm.end());
+    ent_ints.push_back((int32_t)ent_mm.size());
+    dev.o_ent_mm = (int)ent_ints.size();
+    ent_ints.insert(ent_ints.end(), ent_mm.begin(), ent_mm.end());
   }
   // sorption: K_D rows; ion-exchange reactions as CSR over their cations
   const PfSorptionDesc* sd = d->sorption;
@@ -309,6 +310,19 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
           break;
         }
     ints.push_back(zf ? 1 : 0);
+  }
+  // staged prefixes of the group kernel: [core] without, [grp] with the
+  // per-entry tables (staged when they fit beside a block's cells)
+  while (ints.size() % 4) ints.push_back(0);
+  dev.int_words_core = (int)ints.size();
+  {
+    const int base = (int)ints.size();
+    dev.o_ent_ij += base;
+    dev.o_ent_ptr += base;
+    dev.o_ent_sc += base;
+    dev.o_ent_mptr += base;
+    dev.o_ent_mm += base;
+    ints.insert(ints.end(), ent_ints.begin(), ent_ints.end());
   }
   while (ints.size() % 4) ints.push_back(0);  // 16-byte boundary: the group kernel's staged prefix ends here
   dev.int_words_grp = (int)ints.size();
@@ -348,8 +362,6 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_msf = put(d->mnrl_min_scale_factor, nm, 1.0);
   dev.o_temkin = put(d->mnrl_Temkin_const, nm, 1.0);
   dev.o_power = put(d->mnrl_affinity_power, nm, 1.0);
-  dev.o_ent_cf = put(ent_cf.data(), (int)ent_cf.size(), 0.0);
-  dev.o_ent_mcf = put(ent_mcf.data(), (int)ent_mcf.size(), 0.0);
   dev.o_kd_coeff = put(nkd ? sd->kd_coeff : nullptr, nkd, 0.0);
   dev.o_kd_b = put(nkd ? sd->kd_langmuir_b : nullptr, nkd, 0.0);
   dev.o_kd_n = put(nkd ? sd->kd_freundlich_n : nullptr, nkd, 1.0);
@@ -357,6 +369,10 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   for (int r = 0; r < nix; ++r)
     for (int j = 0; j < sd->ionx_ncation[r]; ++j) dbls.push_back(sd->ionx_k[r * sd->ionx_stride + j]);
   dev.o_ix_cec = put(nix ? sd->ionx_cec : nullptr, nix, 0.0);
+  while (dbls.size() % 2) dbls.push_back(0.0);
+  dev.dbl_words_core = (int)dbls.size();
+  dev.o_ent_cf = put(ent_cf.data(), (int)ent_cf.size(), 0.0);
+  dev.o_ent_mcf = put(ent_mcf.data(), (int)ent_mcf.size(), 0.0);
   while (dbls.size() % 2) dbls.push_back(0.0);  // 16-byte boundary: end of the group kernel's prefix
   dev.dbl_words_grp = (int)dbls.size();
   dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);

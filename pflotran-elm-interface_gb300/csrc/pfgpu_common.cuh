@@ -54,7 +54,9 @@ struct DevNet {
   int32_t int_words;     // number of int32 words in the int block
   int32_t dbl_words;     // number of doubles in the double block
   int32_t int_words_grp; // the prefixes the group kernel stages (it reads
-  int32_t dbl_words_grp; //   no pair table of the one-lane kernel)
+  int32_t dbl_words_grp; //   no pair table of the one-lane kernel) ...
+  int32_t int_words_core, dbl_words_core;  // ... or these, without the per-entry tables
+  int32_t ent_staged;    // group launch: the per-entry tables are in shared memory
   const int32_t* ints;   // device: start of int block (16-byte aligned)
   const double* dbls;    // device: start of double block (16-byte aligned)
   // offsets (in elements) into the int block

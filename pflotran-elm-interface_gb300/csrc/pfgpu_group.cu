@@ -68,11 +68,23 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
   return group_rows_ok(lanes_per_cell, R);
 }
 
-size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
-  const size_t tables = (size_t)net.int_words_grp * 4 + (size_t)net.dbl_words_grp * 8;
+// the per-entry assembly tables are staged in shared memory when they fit
+// beside the block's cells, else read through L1
+static bool group_entries_staged(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
   const int G = cfg.lanes_per_cell > 0 ? cfg.lanes_per_cell : 1;
   const size_t cells = (size_t)cfg.threads_per_block / (size_t)G;
-  return tables + cells * ((size_t)group::ws_doubles(net, adj, G) * 8 + (size_t)net.n * 8);
+  const size_t ws = cells * ((size_t)group::ws_doubles(net, adj, G) * 8 + (size_t)net.n * 8);
+  return (size_t)net.int_words_grp * 4 + (size_t)net.dbl_words_grp * 8 + ws <= 227u * 1024u;
+}
+
+size_t group_smem_bytes(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
+  const int G = cfg.lanes_per_cell > 0 ? cfg.lanes_per_cell : 1;
+  const size_t cells = (size_t)cfg.threads_per_block / (size_t)G;
+  const size_t ws = cells * ((size_t)group::ws_doubles(net, adj, G) * 8 + (size_t)net.n * 8);
+  const bool full = group_entries_staged(net, cfg, adj);
+  const size_t tables = full ? (size_t)net.int_words_grp * 4 + (size_t)net.dbl_words_grp * 8
+                             : (size_t)net.int_words_core * 4 + (size_t)net.dbl_words_core * 8;
+  return tables + ws;
 }
 
 size_t group_adj_store_doubles(const DevNet& net, int64_t ncells) {
@@ -88,9 +100,11 @@ int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState
   const size_t smem = group_smem_bytes(net, cfg, adj != nullptr);
   const int tpb = cfg.threads_per_block;
   const int grid = num_sms * cfg.blocks_per_sm;
-  if (G == 2) return launch_group_g2(net, gt, st, dt, R, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
-  if (G == 4) return launch_group_g4(net, gt, st, dt, R, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
-  if (G == 8) return launch_group_g8(net, gt, st, dt, R, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
+  DevNet nl = net;
+  nl.ent_staged = group_entries_staged(net, cfg, adj != nullptr) ? 1 : 0;
+  if (G == 2) return launch_group_g2(nl, gt, st, dt, R, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
+  if (G == 4) return launch_group_g4(nl, gt, st, dt, R, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
+  if (G == 8) return launch_group_g8(nl, gt, st, dt, R, smem, grid, tpb, scratch, queue, counters, adj, adj_store, stream);
   return -1;
 }
 

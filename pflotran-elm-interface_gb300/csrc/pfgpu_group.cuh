@@ -61,8 +61,9 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   __shared__ __align__(8) uint64_t tma_bar;
   const int tid = threadIdx.x;
   const int lane_id = tid & 31;
-  const uint32_t ibytes = (uint32_t)net.int_words_grp * 4u;  // the prefixes this kernel reads
-  const uint32_t dbytes = (uint32_t)net.dbl_words_grp * 8u;
+  // the prefixes this kernel reads, with or without the per-entry tables
+  const uint32_t ibytes = (uint32_t)(net.ent_staged ? net.int_words_grp : net.int_words_core) * 4u;
+  const uint32_t dbytes = (uint32_t)(net.ent_staged ? net.dbl_words_grp : net.dbl_words_core) * 8u;
   int32_t* sI = reinterpret_cast<int32_t*>(smem);
   double* sD = reinterpret_cast<double*>(smem + ibytes);
 
@@ -436,14 +437,15 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
         // J_ij = a_acc (m_i d_ij + sum_s nu_si nu_sj s_s) + sum_m nu_mi nu_mj f_m
         // from the per-entry lists of complexes and minerals (one store per entry)
         const int ne = n * (n + 1) / 2;
+        const Tables TE = net.ent_staged ? T : Tables{net.ints, net.dbls, &net};
         for (int e = r; e < ne; e += G) {
-          const int f = T.ent_ij(e);
+          const int f = TE.ent_ij(e);
           const int i = f / n, j = f - i * n;
           double acc = 0.0;
-          for (int q = T.ent_begin(e); q < T.ent_end(e); ++q) acc = fma(T.ent_cf(q), sv[T.ent_sc(q)], acc);
+          for (int q = TE.ent_begin(e); q < TE.ent_end(e); ++q) acc = fma(TE.ent_cf(q), sv[TE.ent_sc(q)], acc);
           if (i == j) acc = acc + xs[i];
           double v = a_acc * acc;
-          for (int q = T.ent_mbegin(e); q < T.ent_mend(e); ++q) v = fma(T.ent_mcf(q), mf[T.ent_mm(q)], v);
+          for (int q = TE.ent_mbegin(e); q < TE.ent_mend(e); ++q) v = fma(TE.ent_mcf(q), mf[TE.ent_mm(q)], v);
           if (dry) v = (i == j) ? xs[i] : 0.0;
           J[f] = v;
         }
