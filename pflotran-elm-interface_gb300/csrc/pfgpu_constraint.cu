@@ -18,8 +18,7 @@
 namespace pfgpu {
 namespace constraint {
 
-constexpr int NM = PF_MAX_NCOMP;
-
+template <int NM>
 __device__ void activity_lag(const DevNet& net, const Tables& T, const double* c, const PfCellState& st,
                              const SoA& soa, int64_t cell, double* gam) {
   double I = 0.0;
@@ -42,6 +41,9 @@ __device__ void activity_lag(const DevNet& net, const Tables& T, const double* c
   }
 }
 
+// per-thread arrays sized for the bucket of ncomp (4, 8, 12, 16, 24), so that
+// small networks keep them in registers and L1
+template <int NM>
 __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellState st, const int32_t* ctype,
                                                           const PfConstraintReaction* creact,
                                                           const double* cconc, int use_prev,
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
     for (int j = 0; j < n; ++j)
       if (ctype[j] == 2 || ctype[j] == 5) c[j] = free_conc[j];
     if (net.o.act_coef_update_frequency != PF_ACT_COEF_OFF && act)
-      activity_lag(net, T, c, st, soa, cell, gam);
+      activity_lag<NM>(net, T, c, st, soa, cell, gam);
     // RTotalAqueous
     for (int j = 0; j < n; ++j) {
       lnc[j] = log(c[j]);
@@ -276,8 +278,17 @@ extern "C" int32_t pf_equilibrate_constraint_impl(const DevNet* net, const PfCel
                                                   int max_iterations, void* stream) {
   const int tpb = 128;
   const int64_t blocks = (st->ncells + tpb - 1) / tpb;
-  if (blocks)
-    constraint::equilibrate_kernel<<<blocks, tpb, 0, (cudaStream_t)stream>>>(
-        *net, *st, ctype, creact, cconc, use_prev, iterations, max_iterations);
+  if (blocks) {
+    cudaStream_t s = (cudaStream_t)stream;
+#define PF_EQ(NMX) \
+  constraint::equilibrate_kernel<NMX><<<blocks, tpb, 0, s>>>(*net, *st, ctype, creact, cconc, use_prev, iterations, \
+                                                             max_iterations)
+    if (net->n <= 4) PF_EQ(4);
+    else if (net->n <= 8) PF_EQ(8);
+    else if (net->n <= 12) PF_EQ(12);
+    else if (net->n <= 16) PF_EQ(16);
+    else PF_EQ(24);
+#undef PF_EQ
+  }
   return cudaGetLastError() == cudaSuccess ? PF_OK : PF_ERR_CUDA;
 }
