@@ -817,9 +817,9 @@ def main():
     # DRAM bytes per cell-solve of the launched kernel measured by ncu on the
     # same workload at 200,000 cells, scaled to this launch:
     #   one lane per cell  profiles/rstep_batched_kernel_n12_200k.txt   6.431 + 4.639 GB
-    #   group of lanes     profiles/rstep_group_kernel_g4_n12_200k.txt  1.789 + 0.581 GB
+    #   group of lanes     profiles/rstep_group_kernel_g4_n12_200k.txt  2.303 + 0.433 GB
     grp = eng.launch_config()["lanes_per_cell"] > 1
-    per_launch_200k = (1.789e9 + 0.581e9) if grp else (6.431e9 + 4.639e9)
+    per_launch_200k = (2.303e9 + 0.433e9) if grp else (6.431e9 + 4.639e9)
     traffic = per_launch_200k / 200_000 * ncells if args.config == "c2" else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic,
