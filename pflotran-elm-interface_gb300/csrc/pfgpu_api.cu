@@ -513,6 +513,11 @@ int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t ke
   if (!(dt > 0.0) && !state->dt_cell) return PF_ERR_INVALID;
   if (kernel != PF_KERNEL_PLAIN && kernel != PF_KERNEL_BATCHED) return PF_ERR_INVALID;
   if (kernel == PF_KERNEL_BATCHED && !batched_supported(net->dev)) return PF_ERR_UNSUPPORTED;
+  // activity coefficients by the NEWTON algorithm at every Newton iteration
+  // are not built in the step kernels (LAG is)
+  if (net->dev.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
+      net->dev.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON)
+    return PF_ERR_UNSUPPORTED;
   if (state->ncells == 0) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return PF_OK;

@@ -79,8 +79,10 @@ __global__ void cell_setup_kernel(DevNet net, PfCellState st, double* __restrict
       const double* c = T.mnrl_logKcoef(m);
       logK = c[0] * lt + c[1] + c[2] * tk + c[3] * it + c[4] * it2;
     }
-    const double x = -logK * LOG_TO_LN;
-    scratch[(size_t)(ns + m) * N + cell] = ni ? x : exp(x);
+    // K = 10^-logK in every mode: Q/K multiplies it by the activities'
+    // powers (only the complexes' constants carry gamma and stay in log
+    // form when gamma follows each Newton iteration)
+    scratch[(size_t)(ns + m) * N + cell] = exp(-logK * LOG_TO_LN);
   }
   for (int j = 0; j < n; ++j) {
     double v = net.o.use_total_as_guess ? st.total[soa.at(j, cell)] : st.pri_molal[soa.at(j, cell)];

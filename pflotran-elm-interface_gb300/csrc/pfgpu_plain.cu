@@ -290,6 +290,29 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
     }
     for (;;) {
       its = its + 1;
+      if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) {
+        // RActivityCoefficients, LAG (reaction.F90:3857-3860, 4553-4612):
+        // ionic strength from this iterate and the previous evaluation's
+        // complexes
+        double I = 0.0;
+        for (int j = 0; j < n; ++j) I = I + w.c[j] * T.pri_Z(j) * T.pri_Z(j);
+        for (int i = 0; i < ns; ++i) I = I + st.sec_molal[soa.at(i, cell)] * T.sec_Z(i) * T.sec_Z(i);
+        I = 0.5 * I;
+        const double sI = sqrt(I);
+        for (int j = 0; j < n; ++j) {
+          const double z = T.pri_Z(j);
+          w.gamma[j] = fabs(z) > 1.0e-10
+                           ? exp((-z * z * sI * net.A / (1.0 + T.pri_a0(j) * net.B * sI) + net.Bdot * I) * LOG_TO_LN)
+                           : 1.0;
+        }
+        for (int i = 0; i < ns; ++i) {
+          const double z = T.sec_Z(i);
+          st.sec_act_coef[soa.at(i, cell)] =
+              fabs(z) > 1.0e-10
+                  ? exp((-z * z * sI * net.A / (1.0 + T.sec_a0(i) * net.B * sI) + net.Bdot * I) * LOG_TO_LN)
+                  : 1.0;
+        }
+      }
       total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
       for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
       // RTotalSorb; a failed ion-exchange solve fails RReact, no restore (:3861-3865)
@@ -404,6 +427,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
   for (int j = 0; j < n; ++j) {
     st.total[soa.at(j, cell)] = total_io[j];
     st.pri_molal[soa.at(j, cell)] = w.c[j];
+    if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) st.pri_act_coef[soa.at(j, cell)] = w.gamma[j];
   }
   const int status = ierror_step ? PF_CELL_TOO_MANY_CUTS : PF_CELL_OK;
   if (st.status) st.status[cell] = status;

@@ -354,3 +354,79 @@ def test_component_counts_without_one_lane_kernel(oracle, ncomp):
     assert outliers <= 2 * self_out + slack, (outliers, self_out)
     for k, v in errs.items():
         assert v < REL, (k, v, errs)
+
+
+def _newton_iter_case(oracle):
+    from pfgpu import abi, generate
+    from pfgpu.network import default_options
+    opts = default_options(isothermal=0)
+    opts["act_coef_update_frequency"] = abi.PF_ACT_COEF_NEWTON_ITER
+    net = generate.random_network(12, 40, 6, seed=12, options=opts)
+    st, ct, cc = generate.random_cells(net, 600, seed=4242)
+    st, _ = cases.prepare(oracle, net, st, ct, cc)
+    return net, st
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["batched", "group4", "group8", "plain"])
+def test_activity_each_newton_iteration(oracle, kernel):
+    """act_coef_update_frequency = NEWTON_ITERATION: the LAG activity
+    coefficients follow every Newton iterate from the previous evaluation's
+    complexes (reaction.F90:3857-3860); each kernel form against the oracle
+    with the flip-aware comparison."""
+    from pfgpu import abi
+    from pfgpu.engine import ReactionEngine
+    net, st = _newton_iter_case(oracle)
+    ref = st.copy()
+    oracle.rstep(net, ref, 86400.0, nthreads=8)
+    perts = []
+    for key, to in (("total", np.inf), ("total", -np.inf), ("pri_molal", np.inf)):
+        p = st.copy()
+        p.a[key][:] = np.nextafter(p.a[key], to)
+        oracle.rstep(net, p, 86400.0, nthreads=8)
+        perts.append(p)
+    eng = ReactionEngine(net)
+    k = abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED
+    if kernel.startswith("group"):
+        assert eng.set_launch_config(128, 2, 0, int(kernel[5:])) == abi.PF_OK
+    dev = st.to("cuda")
+    eng.rstep(dev, 86400.0, kernel=k)
+    got = dev.numpy()
+    errs, flips, same, outliers, self_flips, self_out = compare(net, ref, got, "newton_iter/" + kernel, perts)
+    n_single = int(same.sum()) + flips
+    slack = max(2, 0.01 * n_single)
+    assert same.sum() > 100
+    assert flips <= 2 * self_flips + slack, (flips, self_flips)
+    assert outliers <= 2 * self_out + slack, (outliers, self_out)
+    for kk, v in errs.items():
+        assert v < REL, (kk, v, errs)
+    np.testing.assert_allclose(got.a["pri_act_coef"][:, same], ref.a["pri_act_coef"][:, same], rtol=1e-10)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["batched", "group4", "plain"])
+def test_non_finite_cell_fails_alone(oracle, kernel):
+    """A cell with a non-finite total fails (status != 0, its factorisation
+    falls back and gives up), and every other cell's result is bitwise the
+    result of the same run without it."""
+    from pfgpu import abi
+    from pfgpu.engine import ReactionEngine
+    net, st0 = cases.case(oracle, "random12")
+    st = st0.subset(np.arange(300))
+    bad = st.copy()
+    bad.a["total"][3, 17] = np.nan
+    eng = ReactionEngine(net)
+    k = abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED
+    if kernel == "group4":
+        assert eng.set_launch_config(128, 2, 0, 4) == abi.PF_OK
+    outs = []
+    for s in (st, bad):
+        dev = s.to("cuda")
+        eng.rstep(dev, 86400.0, kernel=k)
+        outs.append(dev.numpy())
+    good, gotbad = outs
+    assert gotbad.a["status"][17] != 0
+    keep = np.ones(300, bool)
+    keep[17] = False
+    for key in ("pri_molal", "total", "sec_molal", "mnrl_rate", "status", "newton_its"):
+        np.testing.assert_array_equal(gotbad.a[key][..., keep], good.a[key][..., keep], err_msg=key)
