@@ -430,3 +430,73 @@ def test_non_finite_cell_fails_alone(oracle, kernel):
     keep[17] = False
     for key in ("pri_molal", "total", "sec_molal", "mnrl_rate", "status", "newton_its"):
         np.testing.assert_array_equal(gotbad.a[key][..., keep], good.a[key][..., keep], err_msg=key)
+
+
+def _mineral_options_case(oracle, log_formulation):
+    """An 8-component network whose four kinetic minerals exercise every
+    optional branch of RKineticMineral (reaction_mineral.F90:647-1078): rate
+    limiter, Temkin constant with a minimum scale factor, affinity power,
+    irreversibility with an affinity threshold, Arrhenius activation energy."""
+    from pfgpu import generate
+    from pfgpu.network import default_options
+    opts = default_options(isothermal=0)
+    opts["use_log_formulation"] = int(log_formulation)
+    net = generate.random_network(8, 24, 4, seed=818, options=opts)
+    nm = net.nmnrl
+    net.mnrl_rate_limiter = np.array([0.5, 0.0, 0.0, 0.0])[:nm]
+    net.mnrl_Temkin_const = np.array([1.0, 2.0, 1.0, 1.0])[:nm]
+    net.mnrl_min_scale_factor = np.array([1.0, 1.5, 1.0, 1.0])[:nm]
+    net.mnrl_affinity_power = np.array([1.0, 1.0, 2.0, 1.0])[:nm]
+    net.mnrl_irreversible = np.array([0, 0, 0, 1], np.int32)[:nm]
+    net.mnrl_affinity_threshold = np.array([0.0, 0.0, 0.0, 1.0e-3])[:nm]
+    net.mnrl_activation_energy = np.array([3.0e4, 0.0, 5.0e4, 0.0])[:nm]
+    st, ct, cc = generate.random_cells(net, 600, seed=8181)
+    st, _ = cases.prepare(oracle, net, st, ct, cc)
+    # put each mineral's logK at the median log Q of the cells, so that about
+    # half of them precipitate (the threshold and irreversibility branches)
+    la = np.log10(st.a["pri_molal"] * st.a["pri_act_coef"])
+    for m in range(nm):
+        lq = sum(net.mnrl_stoich[m, k] * la[net.mnrl_spec[m, k]] for k in range(net.mnrl_nspec[m]))
+        delta = float(np.median(lq)) - net.mnrl_logK[m]
+        net.mnrl_logK[m] += delta
+        if net.mnrl_logKcoef is not None:
+            net.mnrl_logKcoef[m, 1] += delta
+    return net, st
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel,log_formulation", [("batched", True), ("group4", True), ("plain", True),
+                                                     ("batched", False), ("plain", False)])
+def test_mineral_rate_law_branches(oracle, kernel, log_formulation):
+    from pfgpu import abi
+    from pfgpu.engine import ReactionEngine
+    net, st = _mineral_options_case(oracle, log_formulation)
+    ref = st.copy()
+    oracle.rstep(net, ref, 3600.0, nthreads=8)
+    perts = []
+    for key, to in (("total", np.inf), ("total", -np.inf), ("pri_molal", np.inf)):
+        p = st.copy()
+        p.a[key][:] = np.nextafter(p.a[key], to)
+        oracle.rstep(net, p, 3600.0, nthreads=8)
+        perts.append(p)
+    eng = ReactionEngine(net)
+    k = abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED
+    if kernel.startswith("group"):
+        assert eng.set_launch_config(128, 2, 0, int(kernel[5:])) == abi.PF_OK
+    dev = st.to("cuda")
+    eng.rstep(dev, 3600.0, kernel=k)
+    got = dev.numpy()
+    label = "mineral_options/%s/%s" % (kernel, "log" if log_formulation else "linear")
+    errs, flips, same, outliers, self_flips, self_out = compare(net, ref, got, label, perts)
+    n_single = int(same.sum()) + flips
+    slack = max(2, 0.01 * n_single)
+    assert same.sum() > 300, same.sum()
+    assert flips <= 2 * self_flips + slack, (flips, self_flips)
+    assert outliers <= 2 * self_out + slack, (outliers, self_out)
+    for kk, v in errs.items():
+        assert v < REL, (kk, v, errs)
+    # every branch was taken somewhere: the reversible minerals both dissolve
+    # and precipitate among the compared cells
+    rates = ref.a["mnrl_rate"][:, same]
+    for m in range(3):
+        assert (rates[m] > 0).any() and (rates[m] < 0).any(), m
