@@ -285,15 +285,6 @@ def test_failing_cells_report_status(oracle):
         assert stats["failed_cells"] == int((ref.a["status"] != 0).sum())
 
 
-def test_write_parity_report():
-    """Writes the per-case error/flip/iteration summary collected above."""
-    if not _report:
-        pytest.skip("no parity cases ran")
-    os.makedirs(OUT, exist_ok=True)
-    with open(os.path.join(OUT, "parity_report.json"), "w") as f:
-        json.dump(_report, f, indent=1, sort_keys=True)
-
-
 @pytest.mark.parametrize("lanes", [2, 4, 8])
 def test_group_kernel_order_invariant_and_close_to_one_lane(oracle, lanes):
     """The group-per-cell kernel: results do not depend on the work-queue
@@ -500,3 +491,12 @@ def test_mineral_rate_law_branches(oracle, kernel, log_formulation):
     rates = ref.a["mnrl_rate"][:, same]
     for m in range(3):
         assert (rates[m] > 0).any() and (rates[m] < 0).any(), m
+
+
+def test_write_parity_report():
+    """Writes the per-case error/flip/iteration summary collected by the tests above (kept last in the module)."""
+    if not _report:
+        pytest.skip("no parity cases ran")
+    os.makedirs(OUT, exist_ok=True)
+    with open(os.path.join(OUT, "parity_report.json"), "w") as f:
+        json.dump(_report, f, indent=1, sort_keys=True)
