@@ -84,8 +84,10 @@ enum { PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1 };
  * reaction.F90:5144-5210).  Surface complexation and dynamic K_D are not
  * built.  Supported by pf_update_auxvars, pf_equilibrate_constraint[_ex]
  * and pf_rstep (the plain kernel and the one-lane batched kernel; a launch
- * configuration with several lanes per cell is refused); pf_adjoint and
- * pf_girt_assemble return PF_ERR_UNSUPPORTED for a network with sorption.
+ * configuration with several lanes per cell is refused) and
+ * pf_girt_assemble (sorbed accumulation S*V/dt and its derivative
+ * dS/dm*V/dt on the diagonal block, reactive_transport.F90:2412, 3183);
+ * pf_adjoint returns PF_ERR_UNSUPPORTED for a network with sorption.
  */
 typedef struct PfSorptionDesc {
   int32_t nkd;                    /* isotherm reactions, <= PF_MAX_NKD             */
@@ -371,7 +373,8 @@ int32_t pf_network_shift_parameters(PfNetwork* net, const double* dlogK_sec,
  * RReaction[Derivative], ADD_VALUES in the reference's connection order,
  * then the log-formulation column scaling (MatDiagonalScaleLocal, :2879).
  * The state holds the current Newton iterate (pri_molal) and the activity
- * coefficients; total and sec_molal are updated (RTUpdateAuxVars).
+ * coefficients; total and sec_molal are updated (RTUpdateAuxVars), and with
+ * sorption total_sorb and the ion-exchange warm start.
  */
 typedef struct PfGirtArgs {
   int32_t nx, ny, nz;
@@ -391,6 +394,11 @@ typedef struct PfGirtArgs {
   double* residual;                  /* [ncells*ncomp] out, PETSc block-interleaved */
   double* values;                    /* [nnzb*ncomp*ncomp] out, SeqBAIJ blocks,
                                         each column-major */
+  const double* total_sorb_k;        /* [ncomp][ncells] sorbed totals at the start of
+                                        the step, mol/m^3 bulk (the sorbed part of the
+                                        fixed accumulation, RAccumulationSorb at
+                                        reactive_transport.F90:1026); required when the
+                                        network has sorption, else ignored (NULL) */
 } PfGirtArgs;
 
 /* Host: block-row pattern of the 7-point structured-grid matrix (block

@@ -1083,16 +1083,22 @@ inline double girt_tran_coef(const Cell& up, const Cell& dn, double q, double di
 }
 
 // r: [ncells*n] (block interleaved), values: [nnzb*n*n], rowptr/colidx: BAIJ
-// pattern, fixed_total: totals at the previous time (accum_k = psv*total_k).
+// pattern, fixed_total: totals at the previous time (accum_k = psv*total_k),
+// fixed_sorb: sorbed totals at the previous time (accum_k += S_k*V,
+// RTUpdateFixedAccumulation, reactive_transport.F90:1020-1031), used when
+// the network has sorption.
 inline void girt_assemble(const Net& net, Cell* cells, const GirtGrid& g, const double* fixed_total,
-                          double dt, const int* rowptr, const int* colidx, double* r, double* values) {
+                          const double* fixed_sorb, double dt, const int* rowptr, const int* colidx, double* r,
+                          double* values) {
   const int n = net.n;
   const int nx = g.nx, ny = g.ny, nz = g.nz;
   const long long N = (long long)nx * ny * nz;
   auto idx = [&](int i, int j, int k) { return (long long)i + (long long)nx * (j + (long long)ny * k); };
   for (long long c = 0; c < N; ++c) {
     set_logK(net, cells[c]);
-    total_aqueous(net, cells[c]);  // RTUpdateAuxVars
+    // RTUpdateAuxVars: RTotal without ierror (a failed ion-exchange solve is
+    // reported and the run continues with the last iterate)
+    total(net, cells[c]);
   }
   for (long long e = 0; e < N * n; ++e) r[e] = 0.0;
   const long long nnzb = rowptr[N];
@@ -1157,16 +1163,19 @@ inline void girt_assemble(const Net& net, Cell* cells, const GirtGrid& g, const 
     double psv_t = cl.porosity * cl.sat * 1000.0 * cl.volume;
     for (int k = 0; k < n; ++k) {
       double accum_k = cl.sat < rt_min_saturation ? 0.0 : psv_t * fixed_total[(long long)k * N + c];
+      if (net.sorb) accum_k = accum_k + fixed_sorb[(long long)k * N + c] * cl.volume;
       r[c * n + k] = r[c * n + k] - accum_k / dt;
     }
     double Res[MAXN];
     accumulation(net, cl, Res);
+    if (net.sorb) accumulation_sorb(net, cl, Res);
     for (int k = 0; k < n; ++k) Res[k] = Res[k] / dt;
     for (int k = 0; k < n; ++k) r[c * n + k] = r[c * n + k] + Res[k];
   }
   for (long long c = 0; c < N; ++c) {
     double J[MAXN * MAXN];
     accumulation_derivative(net, cells[c], dt, J);
+    if (net.sorb) accumulation_sorb_derivative(net, cells[c], dt, J);
     double* b = block(c, c);
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) b[j * n + i] = b[j * n + i] + J[i * MAXN + j];

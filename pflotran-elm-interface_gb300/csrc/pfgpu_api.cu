@@ -628,7 +628,7 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
       !a->colidx || !a->residual || !a->values || !(a->dx > 0) || !(a->dy > 0) || !(a->dz > 0))
     return PF_ERR_INVALID;
   if ((int64_t)a->nx * a->ny * a->nz != state->ncells) return PF_ERR_INVALID;
-  if (net->dev.nkd + net->dev.nionx > 0) return PF_ERR_UNSUPPORTED;  // no sorbed accumulation here
+  if (net->dev.nkd + net->dev.nionx > 0 && !a->total_sorb_k) return PF_ERR_INVALID;
   if ((a->nx > 1 && !a->qx) || (a->ny > 1 && !a->qy) || (a->nz > 1 && !a->qz)) return PF_ERR_INVALID;
   if (!state->sec_molal && net->dev.ns) return PF_ERR_INVALID;
   if (girt_smem_bytes(net->dev, nullptr) > 227u * 1024u) return PF_ERR_TOO_LARGE;

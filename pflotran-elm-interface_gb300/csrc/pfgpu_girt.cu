@@ -26,6 +26,11 @@
 //                         column, and the cell's reaction residual
 //   girt_residual_kernel  flux + accumulation terms of the residual row
 //                         (needs the neighbours' totals of the first launch)
+// With equilibrium sorption the cell kernel also runs RTotalSorb (total_sorb,
+// the ion-exchange warm start) and adds dtotal_sorb * V/dt to its diagonal
+// block (RAccumulationSorbDerivative, reactive_transport.F90:3183); the
+// residual kernel adds (S - S_k) * V/dt (RAccumulationSorb, :1026 and :2412).
+// Both are unconditional in the reference, dry cells included.
 // Per-thread scratch (molalities, secondary molalities, mineral terms) lives
 // in shared memory, interleaved by thread so that accesses are conflict-free.
 // The diagonal flux term sums the connection coefficients first
@@ -35,6 +40,7 @@
 
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
 namespace girt {
@@ -280,12 +286,27 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
         if (blk[q] >= 0) values[(size_t)blk[q] * nn + fe] = sc[q] * e0;
     }
   }
+  // ---- equilibrium sorption (RTotalSorb in RTUpdateAuxVars; a failed
+  // ion-exchange solve leaves the last iterate, the reference's
+  // message-and-continue).  Only this thread writes its diagonal block.
+  if (net.nkd + net.nionx > 0 && dblk >= 0) {
+    for (int jj = 0; jj < n; ++jj) st.total_sorb[soa.at(jj, X)] = 0.0;
+    double* D = values + (size_t)dblk * nn;
+    const double v_t = volume / dt;
+    total_sorb(
+        net, T, [&](int j) { return P[j * bd]; }, [&](int j) { return st.pri_act_coef[soa.at(j, X)]; },
+        [&](int m) { return st.mnrl_volfrac[soa.at(m, X)]; }, por, den_k,
+        st.ionx_ref_sorbed ? st.ionx_ref_sorbed + X : nullptr, st.ncells,
+        [&](int j, double v) { st.total_sorb[soa.at(j, X)] += v; },
+        [&](int i, int j, double v) { D[j * n + i] = fma(v * v_t, logf ? P[j * bd] : 1.0, D[j * n + i]); });
+  }
 }
 
 // residual row of cell X: connections (reference order), fixed and current
 // accumulation, then the reaction part the cell kernel left in r
 __global__ void __launch_bounds__(128) girt_residual_kernel(DevNet net, PfCellState st, Geo g,
-                                                            const double* __restrict__ total_k, double dt,
+                                                            const double* __restrict__ total_k,
+                                                            const double* __restrict__ sorb_k, double dt,
                                                             double* __restrict__ r) {
   const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (X >= st.ncells) return;
@@ -296,6 +317,7 @@ __global__ void __launch_bounds__(128) girt_residual_kernel(DevNet net, PfCellSt
   const double sat = st.saturation[X];
   const bool dry = sat < RT_MIN_SATURATION;
   const double psv = st.porosity[X] * sat * 1000.0 * st.volume[X];
+  const bool sorb = net.nkd + net.nionx > 0;
   for (int row = 0; row < n; ++row) {
     const double tx = st.total[(size_t)row * N + X];
     double v = 0.0;
@@ -307,9 +329,14 @@ __global__ void __launch_bounds__(128) girt_residual_kernel(DevNet net, PfCellSt
       const double res = c.cup[q] * tu + c.cdn[q] * td;
       v = c.up[q] ? v + res : v - res;
     }
-    const double accum_k = dry ? 0.0 : psv * total_k[(size_t)row * N + X];
+    double accum_k = dry ? 0.0 : psv * total_k[(size_t)row * N + X];
+    double accum = dry ? 0.0 : psv * tx;
+    if (sorb) {
+      accum_k = accum_k + sorb_k[(size_t)row * N + X] * st.volume[X];
+      accum = accum + st.total_sorb[(size_t)row * N + X] * st.volume[X];
+    }
     v = v - accum_k / dt;
-    v = v + (dry ? 0.0 : psv * tx) / dt;
+    v = v + accum / dt;
     if (!dry) v = v + r[X * n + row];
     r[X * n + row] = v;
   }
@@ -415,7 +442,8 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   k<<<(unsigned)blocks, tpb, smem, s>>>(net, gt, st, g, a.dt, a.rowptr, a.colidx, a.residual, a.values, vec2);
   if (cudaGetLastError() != cudaSuccess) return PF_ERR_CUDA;
   const long long rblocks = (st.ncells + 127) / 128;
-  girt::girt_residual_kernel<<<(unsigned)rblocks, 128, 0, s>>>(net, st, g, a.total_k, a.dt, a.residual);
+  girt::girt_residual_kernel<<<(unsigned)rblocks, 128, 0, s>>>(net, st, g, a.total_k, a.total_sorb_k, a.dt,
+                                                                a.residual);
   return cudaGetLastError() == cudaSuccess ? PF_OK : PF_ERR_CUDA;
 }
 

@@ -85,3 +85,54 @@ def girt_case(oracle, name, nx, ny, nz, seed=5, log_formulation=True, dry=()):
                 qz=q((nz - 1, ny, nx)), diffusion=1e-9, tortuosity=0.5, dispersivity=0.1)
     total_k = st.a["total"] * np.exp(0.05 * rng.standard_normal(st.a["total"].shape))
     return net, st, grid, total_k
+
+
+# a six-primary network with equilibrium sorption (ion exchange of four
+# cations, a Langmuir isotherm or a mineral-scaled Freundlich one) for the
+# global-implicit assembly
+SORB_PRIMARY = ["Na+", "Ca++", "K+", "Cl-", "Tr", "Mg++"]
+SORB_Z = [1.0, 2.0, 1.0, -1.0, 0.0, 2.0]
+SORB_A0 = [4.0, 6.0, 3.0, 3.0, 3.0, 8.0]
+SORB_SECS = [dict(name="NaCl(aq)", stoich={"Na+": 1.0, "Cl-": 1.0}, logK=0.5, Z=0.0, a0=3.0),
+             dict(name="CaCl+", stoich={"Ca++": 1.0, "Cl-": 1.0}, logK=-0.4, Z=1.0, a0=4.0)]
+SORB_MINS = [dict(name="Sylvite-like", stoich={"K+": 1.0, "Cl-": 1.0}, logK=-2.0, rate=1e-8, molar_vol=3.7e-5)]
+SORPTIONS = {
+    "ionx+langmuir": dict(kd=[dict(species="Tr", type="langmuir", coeff=80.0, b=3.0)],
+                          ionx=[dict(cations=[("Na+", 1.0), ("Ca++", 0.3), ("K+", 5.0), ("Mg++", 0.4)],
+                                     cec=250.0)]),
+    "mineral-scaled": dict(kd=[dict(species="Tr", type="freundlich", coeff=20.0, n=1.5, mineral="Sylvite-like")],
+                           ionx=[dict(cations=[("Na+", 1.0), ("K+", 3.0)], cec=4000.0, mineral="Sylvite-like")]),
+}
+
+
+def girt_sorption_case(oracle, sorb, nx, ny, nz, seed=9, log_formulation=True, dry=(), den=997.0):
+    """A GIRT case on the sorption network: random molalities, porosity and
+    mineral state, auxvars and activity coefficients from the oracle, the
+    grid of girt_case, and the previous time level's aqueous and sorbed
+    totals = the current ones times 5 % lognormal noise."""
+    from pfgpu.network import ReactionNetwork
+    net = ReactionNetwork.build(SORB_PRIMARY, SORB_Z, SORB_A0, SORB_SECS, SORB_MINS,
+                                options=default_options(use_log_formulation=int(log_formulation)))
+    net.sorption = SORPTIONS[sorb]
+    N = nx * ny * nz
+    rng = np.random.default_rng(seed)
+    st = CellState.empty(net, N)
+    st.a["pri_molal"][:] = 10.0 ** rng.uniform(-4.0, -2.0, (net.ncomp, N))
+    st.a["porosity"][:] = rng.uniform(0.2, 0.4, N)
+    st.a["saturation"][:] = rng.uniform(0.5, 1.0, N)
+    st.a["den_kg"][:] = den
+    st.a["mnrl_volfrac"][:] = rng.uniform(0.01, 0.1, (net.nmnrl, N))
+    st.a["mnrl_area"][:] = rng.uniform(1.0, 50.0, (net.nmnrl, N))
+    oracle.update_auxvars(net, st, False)
+    oracle.update_activity_coefs(net, st)
+    oracle.update_auxvars(net, st, False)
+    for c in dry:
+        st.a["saturation"][c] = 0.0
+
+    def q(shape):
+        return rng.uniform(1e-7, 1e-5, shape) * rng.choice([-1.0, 1.0], shape)
+    grid = dict(nx=nx, ny=ny, nz=nz, dx=2.0, dy=1.5, dz=0.5, qx=q((nz, ny, nx - 1)), qy=q((nz, ny - 1, nx)),
+                qz=q((nz - 1, ny, nx)), diffusion=1e-9, tortuosity=0.5, dispersivity=0.1)
+    total_k = st.a["total"] * np.exp(0.05 * rng.standard_normal(st.a["total"].shape))
+    sorb_k = st.a["total_sorb"] * np.exp(0.05 * rng.standard_normal(st.a["total_sorb"].shape))
+    return net, st, grid, total_k, sorb_k

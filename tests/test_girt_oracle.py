@@ -118,3 +118,51 @@ def test_oracle_dry_cell_rows(oracle):
     np.testing.assert_array_equal(A[2 * n:3 * n, 2 * n:3 * n], np.diag(st.a["pri_molal"][:, 2]))
     off = np.concatenate([A[2 * n:3 * n, :2 * n], A[2 * n:3 * n, 3 * n:]], axis=1)
     assert np.all(off == 0.0)
+
+
+@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
+@pytest.mark.parametrize("sorb", ["ionx+langmuir", "mineral-scaled"])
+def test_oracle_jacobian_with_sorption_matches_fd(oracle, sorb, logf):
+    """With equilibrium sorption the diagonal blocks carry dtotal_sorb*V/dt
+    (RAccumulationSorbDerivative) on top of the aqueous terms; a dry cell
+    keeps its sorbed accumulation (the reference adds it unconditionally)."""
+    nx, ny, nz = 3, 2, 1
+    net, st, grid, tk, sk = cases.girt_sorption_case(oracle, sorb, nx, ny, nz, log_formulation=logf,
+                                                     dry=(4,), den=1000.0)
+    rp, ci = girt_pattern(nx, ny, nz)
+    dt = 86400.0
+    r0, vals = oracle.girt_assemble(net, st.copy(), grid, tk, dt, rp, ci, total_sorb_k=sk)
+    A = _dense(net, rp, ci, vals)
+    n, N = net.ncomp, st.ncells
+    # the dry cell's identity (RTAccumulationDerivative) is no derivative of
+    # the residual: take it out before comparing with the differences
+    A[4 * n:5 * n, 4 * n:5 * n] -= np.diag(st.a["pri_molal"][:, 4] if logf else np.ones(n))
+    h = 1e-6
+    fd = np.zeros_like(A)
+    for c in range(N):
+        for j in range(n):
+            cols = []
+            for sgn in (1.0, -1.0):
+                s2 = st.copy()
+                s2.a["pri_molal"][j, c] *= np.exp(sgn * h)
+                r, _ = oracle.girt_assemble(net, s2, grid, tk, dt, rp, ci, total_sorb_k=sk)
+                cols.append(r)
+            fd[:, c * n + j] = (cols[0] - cols[1]) / (2 * h) / (1.0 if logf else st.a["pri_molal"][j, c])
+    scale = np.maximum(np.abs(fd).max(axis=0, keepdims=True), 1e-300)
+    err = np.abs(A - fd) / scale
+    assert err.max() < 1e-5, err.max()
+    # the dry cell: no aqueous accumulation, connections or reaction; its row
+    # is the sorbed accumulation alone and its block is I (x m) + dS V/dt
+    st2 = st.copy()
+    oracle.girt_assemble(net, st2, grid, tk, dt, rp, ci, total_sorb_k=sk)
+    V = st.a["volume"][4]
+    want = (st2.a["total_sorb"][:, 4] - sk[:, 4]) * V / dt
+    np.testing.assert_allclose(r0.reshape(-1, n)[4], want, rtol=1e-13, atol=0)
+    assert np.any(np.abs(want) > 0)
+
+
+def test_oracle_girt_sorption_needs_fixed_sorbed_totals(oracle):
+    net, st, grid, tk, sk = cases.girt_sorption_case(oracle, "ionx+langmuir", 2, 1, 1)
+    rp, ci = girt_pattern(2, 1, 1)
+    with pytest.raises(RuntimeError):
+        oracle.girt_assemble(net, st.copy(), grid, tk, 3600.0, rp, ci)

@@ -38,7 +38,7 @@ def _run(oracle, name, dims, logf, dry=()):
     return net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt
 
 
-def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt):
+def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt, sk=None):
     n, N = net.ncomp, st.ncells
     # matrix: per block row (cell, component i)
     blocks = v.reshape(-1, n, n)          # [b][col][row]
@@ -53,6 +53,8 @@ def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt):
     # residual
     psv = st.a["porosity"] * st.a["saturation"] * 1000.0 * st.a["volume"]
     acc = (psv * np.maximum(np.abs(tk), np.abs(ref_st.a["total"])) / dt).T  # [cell][comp]
+    if sk is not None:
+        acc = acc + (st.a["volume"] * np.maximum(np.abs(sk), np.abs(ref_st.a["total_sorb"])) / dt).T
     scale = np.maximum(acc.max(axis=0, keepdims=True), 1e-300)
     er = np.abs(r - r_ref).reshape(N, n) / scale
     assert er.max() < REL, ("residual", er.max())
@@ -60,6 +62,9 @@ def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt):
     np.testing.assert_allclose(got_st.a["total"], ref_st.a["total"], rtol=1e-13, atol=0)
     if net.nsec:
         np.testing.assert_allclose(got_st.a["sec_molal"], ref_st.a["sec_molal"], rtol=1e-13, atol=1e-300)
+    if sk is not None:
+        for k in ("total_sorb", "ionx_ref_sorbed"):
+            np.testing.assert_allclose(got_st.a[k], ref_st.a[k], rtol=1e-12, atol=0, err_msg=k)
     return err.max(), er.max()
 
 
@@ -68,6 +73,29 @@ def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt):
                                        ("hetero24", (7, 6, 4))])
 def test_girt_parity(oracle, name, dims, logf):
     _check(*_run(oracle, name, dims, logf))
+
+
+@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
+@pytest.mark.parametrize("sorb", ["ionx+langmuir", "mineral-scaled"])
+def test_girt_parity_with_sorption(oracle, sorb, logf):
+    """Sorbed accumulation (S - S_k) V/dt in the residual and dS/dm V/dt on
+    the diagonal blocks, dry cells included, against the oracle."""
+    from pfgpu.engine import ReactionEngine
+    from pfgpu.girt import GirtAssembler, StructuredGrid
+    net, st, grid, tk, sk = cases.girt_sorption_case(oracle, sorb, 9, 7, 5, log_formulation=logf,
+                                                     dry=(0, 11, 100, 314))
+    dt = 86400.0
+    eng = ReactionEngine(net)
+    asm = GirtAssembler(eng, StructuredGrid(**grid))
+    dev = st.to("cuda")
+    with pytest.raises(ValueError):
+        asm.assemble(dev, torch.from_numpy(tk).cuda(), dt)
+    r, v = asm.assemble(dev, torch.from_numpy(tk).cuda(), dt, total_sorb_k=torch.from_numpy(sk).cuda())
+    torch.cuda.synchronize()
+    ref_st = st.copy()
+    r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host,
+                                        total_sorb_k=sk)
+    _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt, sk=sk)
 
 
 def test_girt_parity_dry_cells_and_thin_grids(oracle):

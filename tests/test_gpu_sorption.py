@@ -1,7 +1,8 @@
 """Equilibrium sorption on the GPU (K_D isotherms and ion exchange in RTotal,
 with the sorbed accumulation of RReact) against the oracle: the auxvar
 update, constraint equilibration and the operator-split step (one-lane
-batched kernel), and the entry points that refuse a network with sorption."""
+batched kernel), and the entry points that refuse a network with sorption.
+The global-implicit assembly with sorption is in test_gpu_girt.py."""
 import numpy as np
 import pytest
 
