@@ -113,6 +113,40 @@ typedef struct PfSorptionDesc {
 } PfSorptionDesc;
 
 /*
+ * Kinetic-mineral rate prefactors (the PREFACTOR blocks of a mineral's
+ * kinetics; kinmnrl_num_prefactors, kinmnrl_pref_*, kinmnrl_prefactor_id of
+ * mineral_type, reaction_mineral_aux.F90:118-125, filled at
+ * reaction_database.F90:2280-2335).  A mineral with num_prefactors > 0 uses
+ *   sum_p rate_p * Arrhenius_p * prod_s exp(alpha_s ln a_s - ln(1 + K_s a_s^beta_s))
+ * in place of its rate constant times its Arrhenius factor
+ * (RKineticMineral, reaction_mineral.F90:820-858), with the derivative of
+ * :976-1070.  Species: primary j as j (0-based), secondary complex i as
+ * -(i+1) (the reference's negative ids).  Arrays are dense:
+ * [nmnrl][PF_MAX_PREFACTORS] and [nmnrl][PF_MAX_PREFACTORS]
+ * [PF_MAX_PREFACTOR_SPECIES].  Supported by the plain step kernel
+ * (PF_KERNEL_PLAIN) and the global-implicit assembly; PF_KERNEL_BATCHED,
+ * pf_set_launch_config and pf_adjoint return PF_ERR_UNSUPPORTED for such a
+ * network.  pf_network_create returns PF_ERR_UNSUPPORTED when a primary
+ * prefactor species follows a secondary one whose complex has more species
+ * than the mineral (the reference's derivative would index past the
+ * mineral's species there, reaction_mineral.F90:1033-1046).
+ */
+#define PF_MAX_PREFACTORS 4
+#define PF_MAX_PREFACTOR_SPECIES 4
+typedef struct PfPrefactorDesc {
+  const int32_t* num_prefactors;     /* [nmnrl] 0..PF_MAX_PREFACTORS             */
+  const double* rate;                /* kinmnrl_pref_rate, mol/m^2/s              */
+  const double* activation_energy;   /* kinmnrl_pref_activation_energy, J/mol (0 =
+                                        none)                                    */
+  const int32_t* nspec;              /* kinmnrl_prefactor_id(0,:,:)               */
+  const int32_t* spec;               /* species ids as above                      */
+  const double* alpha;               /* kinmnrl_pref_alpha                        */
+  const double* beta;                /* kinmnrl_pref_beta                         */
+  const double* atten_coef;          /* kinmnrl_pref_atten_coef (0 allowed: no
+                                        denominator)                             */
+} PfPrefactorDesc;
+
+/*
  * Solver options: the CHEMISTRY-block fields of reaction_rt_type with the
  * defaults of ReactionCreate (src/pflotran/reaction_aux.F90:371-556).
  */
@@ -183,6 +217,7 @@ typedef struct PfNetworkDesc {
   double debyeA, debyeB, debyeBdot;   /* reaction_database.F90:931-1022 */
   PfOptions opts;
   const PfSorptionDesc* sorption;     /* NULL: no sorption                        */
+  const PfPrefactorDesc* prefactors;  /* NULL: no mineral has rate prefactors     */
 } PfNetworkDesc;
 
 /*

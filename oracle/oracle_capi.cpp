@@ -66,12 +66,39 @@ inline void scatter(const Net& net, const PfCellState* s, int64_t i, const Cell&
     for (int k = 0; k < net.sorb->nionx; ++k) s->ionx_ref_sorbed[k * N + i] = c.ionx_ref[k];
 }
 
+// Rate prefactors: counts and ids in range; a primary prefactor species that
+// follows a secondary one in the same mineral may not see a count above the
+// mineral's own (the reference would read past the mineral's species list).
+int check_prefactors(const PfNetworkDesc* d) {
+  const PfPrefactorDesc* pf = d->prefactors;
+  if (!pf) return PF_OK;
+  if (!pf->num_prefactors || !pf->rate || !pf->activation_energy || !pf->nspec || !pf->spec || !pf->alpha ||
+      !pf->beta || !pf->atten_coef)
+    return PF_ERR_INVALID;
+  for (int m = 0; m < d->nmnrl; ++m) {
+    const int np = pf->num_prefactors[m];
+    if (np < 0 || np > PF_MAX_PREFACTORS) return PF_ERR_INVALID;
+    int cnt = d->mnrl_nspec[m];
+    for (int p = 0; p < np; ++p) {
+      const int ns = pf->nspec[m * PF_MAX_PREFACTORS + p];
+      if (ns < 0 || ns > PF_MAX_PREFACTOR_SPECIES) return PF_ERR_INVALID;
+      for (int k = 0; k < ns; ++k) {
+        const int id = pf->spec[(m * PF_MAX_PREFACTORS + p) * PF_MAX_PREFACTOR_SPECIES + k];
+        if (id >= d->ncomp || -id - 1 >= d->nsec) return PF_ERR_INVALID;
+        if (id < 0) cnt = d->sec_nspec[-id - 1];
+        else if (cnt > d->mnrl_nspec[m]) return PF_ERR_UNSUPPORTED;
+      }
+    }
+  }
+  return PF_OK;
+}
+
 int check(const PfNetworkDesc* d, const PfCellState* s) {
   if (!d || !s) return PF_ERR_INVALID;
   if (d->ncomp < 1 || d->ncomp > MAXN || d->nsec < 0 || d->nsec > MAXS || d->nmnrl < 0 ||
       d->nmnrl > MAXM)
     return PF_ERR_TOO_LARGE;
-  return PF_OK;
+  return check_prefactors(d);
 }
 
 template <class F>

@@ -76,10 +76,17 @@ struct Net {
   int mid(int m, int s) const { return d->mnrl_spec[m * d->mnrl_stride + s]; }
   double mst(int m, int s) const { return d->mnrl_stoich[m * d->mnrl_stride + s]; }
   const PfSorptionDesc* sorb;  // null: no sorption
+  const PfPrefactorDesc* pref;  // null: no rate prefactors
   explicit Net(const PfNetworkDesc* desc) : d(desc), o(desc->opts), n(desc->ncomp),
       ns(desc->nsec), nm(desc->nmnrl),
       sorb(desc->sorption && (desc->sorption->nkd > 0 || desc->sorption->nionx > 0) ? desc->sorption
-                                                                                      : nullptr) {}
+                                                                                      : nullptr),
+      pref(desc->prefactors) {}
+  // kinmnrl_num_prefactors, kinmnrl_prefactor_id(0,p,m) and the per-prefactor
+  // and per-species arrays (dense [nm][MP] and [nm][MP][MS], 0-based)
+  int npref(int m) const { return pref ? pref->num_prefactors[m] : 0; }
+  int pidx(int m, int p) const { return m * PF_MAX_PREFACTORS + p; }
+  int psidx(int m, int p, int s) const { return (m * PF_MAX_PREFACTORS + p) * PF_MAX_PREFACTOR_SPECIES + s; }
 };
 
 // ReactionInterpolateLogK, reaction_aux.F90:1285-1312 (the coefficient type
@@ -435,16 +442,26 @@ inline void accumulation_derivative(const Net& net, const Cell& c, double dt, do
     for (int j = 0; j < n; ++j) J[i * MAXN + j] = c.dtotal[i * MAXN + j] * psvd_t;
 }
 
-// RKineticMineral, reaction_mineral.F90:647-1078 (no prefactors, no solid
-// solution, no water activity).  J may be null when !compute_derivative.
+// RKineticMineral, reaction_mineral.F90:647-1078 (no solid solution, no water
+// activity).  J may be null when !compute_derivative.  Rate prefactors
+// (:820-858, derivative :976-1070) as written, two behaviours included:
+// a secondary prefactor species' derivative goes to the rows of the
+// complex's own species with the complex's stoichiometry (:1058-1066), and
+// it reassigns ncomp, the count the later primary prefactor species of the
+// same mineral then use for the mineral's species (:1046, :1033-1038; the
+// networks where that count exceeds the mineral's are refused at set-up).
+// ln_sec_act (:707-710) is formed only when a prefactor uses it.
 inline void kinetic_mineral(const Net& net, Cell& c, double* Res, double* J,
                             bool compute_derivative) {
   const PfNetworkDesc* d = net.d;
+  const PfPrefactorDesc* pf = net.pref;
   double ln_conc[MAXN], ln_act[MAXN];
   for (int j = 0; j < net.n; ++j) {
     ln_conc[j] = std::log(c.pri_molal[j]);
     ln_act[j] = ln_conc[j] + std::log(c.pri_act_coef[j]);
   }
+  auto ln_sec_act = [&](int i) { return std::log(c.sec_molal[i]) + std::log(c.sec_act_coef[i]); };
+  double prefactor[PF_MAX_PREFACTORS], ln_prefactor_spec[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
   for (int m = 0; m < net.nm; ++m) c.mnrl_rate[m] = 0.0;
   for (int m = 0; m < net.nm; ++m) {
     double lnQK = -c.mnrl_logK[m] * LOG_TO_LN;
@@ -472,12 +489,36 @@ inline void kinetic_mineral(const Net& net, Cell& c, double* Res, double* J,
       if (d->mnrl_rate_limiter[m] > 0.0) {
         affinity_factor = affinity_factor / (1.0 + (1.0 - affinity_factor) / d->mnrl_rate_limiter[m]);
       }
-      double arrhenius_factor = 1.0;
-      if (d->mnrl_activation_energy[m] > 0.0) {
-        arrhenius_factor = std::exp(d->mnrl_activation_energy[m] / IDEAL_GAS_CONSTANT *
-                                    (1.0 / (25.0 + 273.15) - 1.0 / (c.temp + 273.15)));
+      if (net.npref(m) > 0) {
+        sum_prefactor_rate = 0.0;
+        for (int p = 0; p < net.npref(m); ++p) {
+          double ln_prefactor = 0.0;
+          for (int s = 0; s < pf->nspec[net.pidx(m, p)]; ++s) {
+            const int q = net.psidx(m, p, s), id = pf->spec[q];
+            const double ln_spec_act = id >= 0 ? ln_act[id] : ln_sec_act(-id - 1);
+            const double ln_numerator = pf->alpha[q] * ln_spec_act;
+            const double ln_denominator =
+                std::log(1.0 + std::exp(std::log(pf->atten_coef[q]) + pf->beta[q] * ln_spec_act));
+            ln_prefactor = ln_prefactor + ln_numerator;
+            ln_prefactor = ln_prefactor - ln_denominator;
+            ln_prefactor_spec[p][s] = ln_numerator - ln_denominator;
+          }
+          prefactor[p] = std::exp(ln_prefactor);
+          double arrhenius_factor = 1.0;
+          if (pf->activation_energy[net.pidx(m, p)] > 0.0) {
+            arrhenius_factor = std::exp(pf->activation_energy[net.pidx(m, p)] / IDEAL_GAS_CONSTANT *
+                                        (1.0 / (25.0 + 273.15) - 1.0 / (c.temp + 273.15)));
+          }
+          sum_prefactor_rate = sum_prefactor_rate + prefactor[p] * pf->rate[net.pidx(m, p)] * arrhenius_factor;
+        }
+      } else {
+        double arrhenius_factor = 1.0;
+        if (d->mnrl_activation_energy[m] > 0.0) {
+          arrhenius_factor = std::exp(d->mnrl_activation_energy[m] / IDEAL_GAS_CONSTANT *
+                                      (1.0 / (25.0 + 273.15) - 1.0 / (c.temp + 273.15)));
+        }
+        sum_prefactor_rate = d->mnrl_rate_constant[m] * arrhenius_factor;
       }
-      sum_prefactor_rate = d->mnrl_rate_constant[m] * arrhenius_factor;
       Im_const = -c.mnrl_area[m];
       if (d->mnrl_min_scale_factor) Im_const = Im_const / d->mnrl_min_scale_factor[m];
       if (d->mnrl_affinity_power) {
@@ -532,6 +573,58 @@ inline void kinetic_mineral(const Net& net, Cell& c, double* Res, double* J,
           int ic = net.mid(m, si);
           J[ic * MAXN + jc] = J[ic * MAXN + jc] +
                               net.mst(m, si) * dIm_dQK * (1.0 + QK / rl / den) * dQK_dmj / den;
+        }
+      }
+    }
+    if (net.npref(m) > 0) {
+      const double dIm_dsum_prefactor_rate = Im / sum_prefactor_rate;
+      int ncomp = nsp;  // reassigned by a secondary prefactor species below
+      for (int p = 0; p < net.npref(m); ++p) {
+        double arrhenius_factor = 1.0;
+        if (pf->activation_energy[net.pidx(m, p)] > 0.0) {
+          arrhenius_factor = std::exp(pf->activation_energy[net.pidx(m, p)] / IDEAL_GAS_CONSTANT *
+                                      (1.0 / (25.0 + 273.15) - 1.0 / (c.temp + 273.15)));
+        }
+        const double ln_prefactor = std::log(prefactor[p]);
+        for (int s = 0; s < pf->nspec[net.pidx(m, p)]; ++s) {
+          const int q = net.psidx(m, p, s), id = pf->spec[q];
+          const double dprefactor_dprefactor_spec = std::exp(ln_prefactor - ln_prefactor_spec[p][s]);
+          double ln_spec_act, spec_act_coef;
+          if (id >= 0) {
+            ln_spec_act = ln_act[id];
+            spec_act_coef = c.pri_act_coef[id];
+          } else {
+            ln_spec_act = ln_sec_act(-id - 1);
+            spec_act_coef = c.sec_act_coef[-id - 1];
+          }
+          const double dnum = pf->alpha[q] * std::exp(ln_prefactor_spec[p][s] - ln_spec_act);
+          const double ln_gam_m_beta = pf->beta[q] * ln_spec_act;
+          const double denominator = 1.0 + std::exp(std::log(pf->atten_coef[q]) + ln_gam_m_beta);
+          const double dden = -1.0 * std::exp(ln_prefactor_spec[p][s]) / denominator * pf->atten_coef[q] *
+                              pf->beta[q] * std::exp(ln_gam_m_beta - ln_spec_act);
+          double dprefactor_spec_dspec = dnum + dden;
+          dprefactor_spec_dspec = dprefactor_spec_dspec * spec_act_coef;
+          const double dIm_dspec = dIm_dsum_prefactor_rate * dprefactor_dprefactor_spec * dprefactor_spec_dspec *
+                                   pf->rate[net.pidx(m, p)] * arrhenius_factor;
+          if (id >= 0) {
+            for (int i = 0; i < ncomp; ++i) {
+              const int jc = net.mid(m, i);
+              J[jc * MAXN + id] = J[jc * MAXN + id] + net.mst(m, i) * dIm_dspec;
+            }
+          } else {
+            const int icplx = -id - 1;
+            double lnQK2 = -c.sec_logK[icplx] * LOG_TO_LN;
+            ncomp = d->sec_nspec[icplx];
+            for (int i = 0; i < ncomp; ++i) lnQK2 = lnQK2 + net.sst(icplx, i) * ln_act[net.sid(icplx, i)];
+            for (int j = 0; j < ncomp; ++j) {
+              const int jc = net.sid(icplx, j);
+              const double tempreal = net.sst(icplx, j) * std::exp(lnQK2 - ln_conc[jc]) / c.sec_act_coef[icplx];
+              for (int i = 0; i < ncomp; ++i) {
+                const int ic = net.sid(icplx, i);
+                J[ic * MAXN + jc] = J[ic * MAXN + jc] + net.sst(icplx, i) * tempreal * dIm_dspec;
+              }
+            }
+          }
         }
       }
     }

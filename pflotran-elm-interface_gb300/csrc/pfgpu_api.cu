@@ -102,6 +102,30 @@ int validate_desc(const PfNetworkDesc* d) {
       if (sd->ionx_mineral && (sd->ionx_mineral[r] < -1 || sd->ionx_mineral[r] >= d->nmnrl)) return PF_ERR_INVALID;
     }
   }
+  if (const PfPrefactorDesc* pf = d->prefactors) {
+    if (!pf->num_prefactors || !pf->rate || !pf->activation_energy || !pf->nspec || !pf->spec || !pf->alpha ||
+        !pf->beta || !pf->atten_coef)
+      return PF_ERR_INVALID;
+    for (int m = 0; m < d->nmnrl; ++m) {
+      const int np = pf->num_prefactors[m];
+      if (np < 0 || np > PF_MAX_PREFACTORS) return PF_ERR_INVALID;
+      // the derivative of a secondary prefactor species leaves the complex's
+      // species count in place of the mineral's (reaction_mineral.F90:1046);
+      // a later primary species of the same mineral then walks that many of
+      // the mineral's species (:1033-1038), which must exist
+      int cnt = d->mnrl_nspec[m];
+      for (int p = 0; p < np; ++p) {
+        const int ns = pf->nspec[m * PF_MAX_PREFACTORS + p];
+        if (ns < 0 || ns > PF_MAX_PREFACTOR_SPECIES) return PF_ERR_INVALID;
+        for (int k = 0; k < ns; ++k) {
+          const int id = pf->spec[(m * PF_MAX_PREFACTORS + p) * PF_MAX_PREFACTOR_SPECIES + k];
+          if (id >= d->ncomp || -id - 1 >= d->nsec) return PF_ERR_INVALID;
+          if (id < 0) cnt = d->sec_nspec[-id - 1];
+          else if (cnt > d->mnrl_nspec[m]) return PF_ERR_UNSUPPORTED;
+        }
+      }
+    }
+  }
   if (d->opts.act_coef_update_frequency < 0 || d->opts.act_coef_update_frequency > 2) return PF_ERR_INVALID;
   return PF_OK;
 }
@@ -334,6 +358,17 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
     dev.o_mpair_idx += base;
     ints.insert(ints.end(), lane_ints.begin(), lane_ints.end());
   }
+  // rate prefactors (read from global memory by the kernels that carry them)
+  const PfPrefactorDesc* pfd = d->prefactors;
+  bool any_pref = false;
+  for (int m = 0; pfd && m < nm; ++m) any_pref = any_pref || pfd->num_prefactors[m] > 0;
+  const int MP = PF_MAX_PREFACTORS, MPS = PF_MAX_PREFACTORS * PF_MAX_PREFACTOR_SPECIES;
+  dev.o_pf_cnt = (int)ints.size();
+  for (int m = 0; m < nm; ++m) ints.push_back(any_pref ? pfd->num_prefactors[m] : 0);
+  dev.o_pf_nsp = (int)ints.size();
+  for (int k = 0; k < nm * MP; ++k) ints.push_back(any_pref ? pfd->nspec[k] : 0);
+  dev.o_pf_id = (int)ints.size();
+  for (int k = 0; k < nm * MPS; ++k) ints.push_back(any_pref ? pfd->spec[k] : 0);
   while (ints.size() % 4) ints.push_back(0);
   auto put = [&](const double* src, int count, double dflt) {
     int off = (int)dbls.size();
@@ -377,10 +412,15 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.dbl_words_grp = (int)dbls.size();
   dev.o_spair_coef = put(spair_coef.data(), (int)spair_coef.size(), 0.0);
   dev.o_mpair_coef = put(mpair_coef.data(), (int)mpair_coef.size(), 0.0);
+  dev.o_pf_rate = put(any_pref ? pfd->rate : nullptr, nm * MP, 0.0);
+  dev.o_pf_ea = put(any_pref ? pfd->activation_energy : nullptr, nm * MP, 0.0);
+  dev.o_pf_alpha = put(any_pref ? pfd->alpha : nullptr, nm * MPS, 0.0);
+  dev.o_pf_beta = put(any_pref ? pfd->beta : nullptr, nm * MPS, 0.0);
+  dev.o_pf_atten = put(any_pref ? pfd->atten_coef : nullptr, nm * MPS, 0.0);
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
               (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |
-              (d->mnrl_affinity_power ? NETF_POWER : 0);
+              (d->mnrl_affinity_power ? NETF_POWER : 0) | (any_pref ? NETF_PREFACTOR : 0);
   dev.int_words = (int)ints.size();
   dev.dbl_words = (int)dbls.size();
   dev.A = d->debyeA;

@@ -36,7 +36,9 @@ bool lane_supported(const DevNet& net) {
 #define PF_CASE(N) case N:
     PF_BATCHED_NCOMPS(PF_CASE)
 #undef PF_CASE
-      return net.ns <= PF_MAX_NSEC && net.nm <= PF_MAX_NMNRL &&
+      // rate prefactors add non-symmetric Jacobian terms the factorisation
+      // here does not carry: the plain kernel runs those networks
+      return net.ns <= PF_MAX_NSEC && net.nm <= PF_MAX_NMNRL && !(net.flags & NETF_PREFACTOR) &&
              !(net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
                net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON);
     default:

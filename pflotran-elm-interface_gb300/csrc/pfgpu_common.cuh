@@ -24,6 +24,7 @@ enum : int32_t {
   NETF_MSF = 4,
   NETF_TEMKIN = 8,
   NETF_POWER = 16,
+  NETF_PREFACTOR = 32,  // some mineral has rate prefactors
 };
 
 // Device view of a network.  All pointers index one packed allocation whose
@@ -81,6 +82,11 @@ struct DevNet {
   int32_t o_kd_spec, o_kd_type, o_kd_min, o_ix_ptr, o_ix_cat, o_ix_min, o_ix_zflag;
   int32_t o_kd_coeff, o_kd_b, o_kd_n, o_ix_k, o_ix_cec;
   double soil_density;
+  // kinetic-mineral rate prefactors (PfPrefactorDesc), dense [nm][MP] and
+  // [nm][MP][MS]: counts, species ids (primary j, secondary i as -(i+1));
+  // rate, activation energy, alpha, beta, attenuation coefficient
+  int32_t o_pf_cnt, o_pf_nsp, o_pf_id;
+  int32_t o_pf_rate, o_pf_ea, o_pf_alpha, o_pf_beta, o_pf_atten;
   double A, B, Bdot;
   PfOptions o;
   GroupTabs grp;
@@ -146,6 +152,17 @@ struct Tables {
   __device__ __forceinline__ double ix_cec(int r) const { return D[net->o_ix_cec + r]; }
   __device__ __forceinline__ int ix_min(int r) const { return I[net->o_ix_min + r]; }
   __device__ __forceinline__ int ix_zflag(int r) const { return I[net->o_ix_zflag + r]; }
+  __device__ __forceinline__ int pf_cnt(int m) const { return I[net->o_pf_cnt + m]; }
+  __device__ __forceinline__ int pf_nsp(int m, int p) const { return I[net->o_pf_nsp + m * PF_MAX_PREFACTORS + p]; }
+  __device__ __forceinline__ double pf_rate(int m, int p) const {
+    return D[net->o_pf_rate + m * PF_MAX_PREFACTORS + p];
+  }
+  __device__ __forceinline__ double pf_ea(int m, int p) const { return D[net->o_pf_ea + m * PF_MAX_PREFACTORS + p]; }
+  // species slot q = (m*MP + p)*MS + s
+  __device__ __forceinline__ int pf_id(int q) const { return I[net->o_pf_id + q]; }
+  __device__ __forceinline__ double pf_alpha(int q) const { return D[net->o_pf_alpha + q]; }
+  __device__ __forceinline__ double pf_beta(int q) const { return D[net->o_pf_beta + q]; }
+  __device__ __forceinline__ double pf_atten(int q) const { return D[net->o_pf_atten + q]; }
 };
 
 // Fortran SIGN(1.d0, x)

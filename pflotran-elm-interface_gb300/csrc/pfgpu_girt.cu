@@ -30,7 +30,9 @@
 // the ion-exchange warm start) and adds dtotal_sorb * V/dt to its diagonal
 // block (RAccumulationSorbDerivative, reactive_transport.F90:3183); the
 // residual kernel adds (S - S_k) * V/dt (RAccumulationSorb, :1026 and :2412).
-// Both are unconditional in the reference, dry cells included.
+// Both are unconditional in the reference, dry cells included.  Minerals with
+// rate prefactors take their rate from prefactor_rate, and the cell kernel
+// adds the prefactor derivative to its diagonal block the same way.
 // Per-thread scratch (molalities, secondary molalities, mineral terms) lives
 // in shared memory, interleaved by thread so that accesses are conflict-free.
 // The diagonal flux term sums the connection coefficients first
@@ -40,6 +42,7 @@
 
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_prefactor.cuh"
 #include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
@@ -132,6 +135,40 @@ __device__ __forceinline__ int find_block(const int32_t* __restrict__ rowptr, co
   return -1;
 }
 
+// Rate prefactors (the girt_cell_kernel<true> instantiation only).  P: the thread's scratch (m at P[j*bd], ln a at
+// P[o_lna + j*bd], complexes at P[o_s + i*bd]).
+__device__ __noinline__ double pref_rate(const Tables& T, const PfCellState& st, long long X, const double* P,
+                                         int bd, int o_lna, int o_s, double temp, int m) {
+  const SoA soa{st.ncells};
+  double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
+  return prefactor_rate(
+      T, m, [&](int j) { return P[o_lna + j * bd]; },
+      [&](int i) { return log(P[o_s + i * bd]) + log(st.sec_act_coef[soa.at(i, X)]); }, temp, pref, lnps);
+}
+
+// adds the prefactor part of the reaction Jacobian of the minerals in mask
+// to the diagonal block D (column-major, columns scaled by m when logf)
+__device__ __noinline__ void pref_jacobian(const DevNet& net, const Tables& T, const PfCellState& st, long long X,
+                                           const double* P, int bd, int o_lna, int o_s, double temp,
+                                           double volume, bool logf, bool tsec, unsigned mask, double* D) {
+  const SoA soa{st.ncells};
+  const int n = net.n;
+  auto ln_act = [&](int j) { return P[o_lna + j * bd]; };
+  auto ln_sec_act = [&](int i) { return log(P[o_s + i * bd]) + log(st.sec_act_coef[soa.at(i, X)]); };
+  for (int m = 0; m < net.nm; ++m) {
+    if (!((mask >> m) & 1u)) continue;
+    double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
+    const double sum = prefactor_rate(T, m, ln_act, ln_sec_act, temp, pref, lnps);
+    prefactor_derivative(
+        T, m, st.mnrl_rate[soa.at(m, X)] * volume, sum, pref, lnps, ln_act, ln_sec_act,
+        [&](int j) { return st.pri_act_coef[soa.at(j, X)]; }, [&](int i) { return st.sec_act_coef[soa.at(i, X)]; },
+        [&](int j) { return log(P[j * bd]); },
+        [&](int i) { return tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i); }, temp,
+        [&](int r, int c, double v) { D[c * n + r] = fma(v, logf ? P[c * bd] : 1.0, D[c * n + r]); });
+  }
+}
+
+template <bool HAS_PF>
 __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt,
                                                         const int32_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ colidx, double* __restrict__ r,
@@ -150,6 +187,8 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   const bool tsec = !net.o.isothermal && (net.flags & NETF_SEC_LOGKCOEF);
   const bool tmin = !net.o.isothermal && (net.flags & NETF_MNRL_LOGKCOEF);
   const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
+  constexpr bool has_pf = HAS_PF;  // rate prefactors: a separate instantiation
+  unsigned pf_active = 0;  // minerals whose prefactor derivative is due
   const double temp = st.temperature ? st.temperature[X] : 25.0;
   const double den_k = st.den_kg[X], den_L = den_k * 1.0e-3;
   const double por = st.porosity[X], sat = st.saturation[X], volume = st.volume[X];
@@ -204,10 +243,16 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
       if (active) {
         const double rl = T.limiter(m);
         if (rl > 0.0) aff = aff / (1.0 + (1.0 - aff) / rl);
-        double arr = 1.0;
-        if (T.ea(m) > 0.0)
-          arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp + 273.15)));
-        const double kr = T.rate(m) * arr;
+        double kr;
+        if (has_pf && T.pf_cnt(m) > 0) {
+          kr = pref_rate(T, st, X, P, bd, o_lna, o_s, temp, m);
+          pf_active |= 1u << m;
+        } else {
+          double arr = 1.0;
+          if (T.ea(m) > 0.0)
+            arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp + 273.15)));
+          kr = T.rate(m) * arr;
+        }
         double Im_const = -st.mnrl_area[soa.at(m, X)];
         if (has_msf) Im_const = Im_const / T.msf(m);
         double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * kr : Im_const * sign_ * fabs(aff) * kr;
@@ -286,6 +331,11 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
         if (blk[q] >= 0) values[(size_t)blk[q] * nn + fe] = sc[q] * e0;
     }
   }
+  // ---- rate-prefactor part of the reaction Jacobian (its residual part is in
+  // the rates above), added to the diagonal block in the column scaling
+  if (has_pf && pf_active && dblk >= 0)
+    pref_jacobian(net, T, st, X, P, bd, o_lna, o_s, temp, volume, logf, tsec, pf_active,
+                  values + (size_t)dblk * nn);
   // ---- equilibrium sorption (RTotalSorb in RTUpdateAuxVars; a failed
   // ion-exchange solve leaves the last iterate, the reference's
   // message-and-continue).  Only this thread writes its diagonal block.
@@ -432,7 +482,7 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   int tpb = 32;
   const size_t smem = girt_smem_bytes(net, &tpb);
   if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
-  auto k = girt::girt_cell_kernel;
+  auto k = (net.flags & NETF_PREFACTOR) ? girt::girt_cell_kernel<true> : girt::girt_cell_kernel<false>;
   if (smem > 48u * 1024u &&
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PF_ERR_CUDA;

@@ -9,9 +9,11 @@
 // measured against, and a second, independent GPU statement of the algorithm.
 // With equilibrium sorption RTAuxVarCompute adds RTotalSorb and the
 // accumulation RAccumulationSorb[Derivative] (reaction.F90:3836-3839,
-// 3861-3865, 3904-3909), any ncomp.
+// 3861-3865, 3904-3909), any ncomp; kinetic-mineral rate prefactors
+// (reaction_mineral.F90:820-858, 976-1070) run here only.
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_prefactor.cuh"
 #include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
@@ -68,13 +70,20 @@ __device__ void total_aqueous(const Tables& T, int n, int ns, const double* sec_
     for (int j = 0; j < n; ++j) w.dtotal[i * NMAX + j] = w.dtotal[i * NMAX + j] * den_kg_per_L;
 }
 
-// RKineticMineral without prefactors.  Jac may be null (derivative = false).
-template <int NMAX>
+// RKineticMineral.  Jac may be null (derivative = false).  sec_logK: the
+// complexes' logK at the cell's temperature (prefactor derivative).  PF:
+// the network has rate prefactors (a separate instantiation, so that the
+// common one keeps its registers).
+template <int NMAX, bool PF>
 __device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const double* mnrl_logK,
-                                int64_t cell, const SoA& soa, const PfCellState& st,
+                                const double* sec_logK, int64_t cell, const SoA& soa, const PfCellState& st,
                                 const CellScalars& cs, Work<NMAX>& w, double* Res, double* Jac) {
   const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN,
              has_pw = net.flags & NETF_POWER;
+  constexpr bool has_pf = PF;
+  double prefactor[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
+  auto ln_act = [&](int j) { return w.lna[j]; };
+  auto ln_sec_act = [&](int i) { return log(st.sec_molal[soa.at(i, cell)]) + log(st.sec_act_coef[soa.at(i, cell)]); };
   for (int m = 0; m < net.nm; ++m) st.mnrl_rate[soa.at(m, cell)] = 0.0;
   for (int m = 0; m < net.nm; ++m) {
     const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
@@ -97,10 +106,14 @@ __device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const
       if (T.irreversible(m) == 1 && sign_ < 0.0) continue;
       if (T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m)) continue;
       if (T.limiter(m) > 0.0) aff = aff / (1.0 + (1.0 - aff) / T.limiter(m));
-      double arr = 1.0;
-      if (T.ea(m) > 0.0)
-        arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (cs.temp + 273.15)));
-      k = T.rate(m) * arr;
+      if (has_pf && T.pf_cnt(m) > 0) {
+        k = prefactor_rate(T, m, ln_act, ln_sec_act, cs.temp, prefactor, lnps);
+      } else {
+        double arr = 1.0;
+        if (T.ea(m) > 0.0)
+          arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (cs.temp + 273.15)));
+        k = T.rate(m) * arr;
+      }
       Im_const = -st.mnrl_area[soa.at(m, cell)];
       if (has_msf) Im_const = Im_const / T.msf(m);
       if (has_pw) Im = Im_const * sign_ * pow(fabs(aff), T.power(m)) * k;
@@ -139,6 +152,12 @@ __device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const
                                 T.mnrl_nu(pi) * dIm_dQK * (1.0 + QK / rl / den) * dQK_dmj / den;
       }
     }
+    if (has_pf && T.pf_cnt(m) > 0)
+      prefactor_derivative(
+          T, m, Im, k, prefactor, lnps, ln_act, ln_sec_act, [&](int j) { return w.gamma[j]; },
+          [&](int i) { return st.sec_act_coef[soa.at(i, cell)]; }, [&](int j) { return w.lnc[j]; },
+          [&](int i) { return sec_logK[i]; }, cs.temp,
+          [&](int r, int c, double v) { Jac[r * NMAX + c] = Jac[r * NMAX + c] + v; });
   }
 }
 
@@ -217,7 +236,7 @@ __device__ int rsolve(int n, double* J, const double* conc, const double* Res, d
   return 0;
 }
 
-template <int NMAX>
+template <int NMAX, bool PF>
 __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellState st, double dt_uniform,
                                                           unsigned long long* counters) {
   const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -336,7 +355,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
           w.res[j] = (psv_t * w.total[j] - w.fixed[j]) / dt;
           for (int k = 0; k < n; ++k) w.J[j * NMAX + k] = w.dtotal[j * NMAX + k] * psvd_t;
         }
-        if (nm > 0) kinetic_mineral<NMAX>(T, net, n, mnrl_logK, cell, soa, st, cs, w, w.res, w.J);
+        if (nm > 0) kinetic_mineral<NMAX, PF>(T, net, n, mnrl_logK, sec_logK, cell, soa, st, cs, w, w.res, w.J);
       }
       if (has_sorb) {
         // residual with the sorbed accumulation: (psv T + V S - fixed)/dt,
@@ -405,7 +424,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
       if (nm > 0) {
         double dummy[NMAX];
         for (int j = 0; j < n; ++j) dummy[j] = 0.0;
-        kinetic_mineral<NMAX>(T, net, n, mnrl_logK, cell, soa, st, cs, w, dummy, nullptr);
+        kinetic_mineral<NMAX, PF>(T, net, n, mnrl_logK, sec_logK, cell, soa, st, cs, w, dummy, nullptr);
         for (int m = 0; m < nm; ++m) {
           double vf = st.mnrl_volfrac[soa.at(m, cell)] + st.mnrl_rate[soa.at(m, cell)] * T.molar_vol(m) * dt;
           st.mnrl_volfrac[soa.at(m, cell)] = vf < 0.0 ? 0.0 : vf;
@@ -448,11 +467,15 @@ int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
   const int tpb = 128;
   const int64_t blocks = (st.ncells + tpb - 1) / tpb;
   if (blocks == 0) return 0;
-  if (net.n <= 4) plain::rstep_plain_kernel<4><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
-  else if (net.n <= 8) plain::rstep_plain_kernel<8><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
-  else if (net.n <= 12) plain::rstep_plain_kernel<12><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
-  else if (net.n <= 16) plain::rstep_plain_kernel<16><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
-  else plain::rstep_plain_kernel<24><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  if (net.flags & NETF_PREFACTOR) {  // rate prefactors: three size buckets
+    if (net.n <= 8) plain::rstep_plain_kernel<8, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+    else if (net.n <= 12) plain::rstep_plain_kernel<12, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+    else plain::rstep_plain_kernel<24, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  } else if (net.n <= 4) plain::rstep_plain_kernel<4, false><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else if (net.n <= 8) plain::rstep_plain_kernel<8, false><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else if (net.n <= 12) plain::rstep_plain_kernel<12, false><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else if (net.n <= 16) plain::rstep_plain_kernel<16, false><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
+  else plain::rstep_plain_kernel<24, false><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
   return (int)cudaGetLastError();
 }
 

@@ -82,6 +82,17 @@ class PfSorptionDesc(C.Structure):
     ]
 
 
+PF_MAX_PREFACTORS = 4
+PF_MAX_PREFACTOR_SPECIES = 4
+
+
+class PfPrefactorDesc(C.Structure):
+    _fields_ = [
+        ("num_prefactors", _ip), ("rate", _dp), ("activation_energy", _dp), ("nspec", _ip), ("spec", _ip),
+        ("alpha", _dp), ("beta", _dp), ("atten_coef", _dp),
+    ]
+
+
 class PfNetworkDesc(C.Structure):
     _fields_ = [
         ("ncomp", C.c_int32), ("nsec", C.c_int32), ("nmnrl", C.c_int32),
@@ -99,6 +110,7 @@ class PfNetworkDesc(C.Structure):
         ("debyeA", C.c_double), ("debyeB", C.c_double), ("debyeBdot", C.c_double),
         ("opts", PfOptions),
         ("sorption", C.POINTER(PfSorptionDesc)),
+        ("prefactors", C.POINTER(PfPrefactorDesc)),
     ]
 
 

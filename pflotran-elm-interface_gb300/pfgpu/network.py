@@ -102,6 +102,14 @@ class ReactionNetwork:
     # cations=[(name, k), ...] (the first is the reference cation), cec,
     # [mineral])])
     sorption: dict = None
+    # kinetic-mineral rate prefactors (None: none): {mineral name: [dict(rate,
+    # [activation_energy], species=[dict(name (primary or secondary), [alpha],
+    # [beta], [atten_coef])])]}, the PREFACTOR blocks of the mineral's kinetics
+    prefactors: dict = None
+
+    @property
+    def has_prefactors(self):
+        return bool(self.prefactors) and any(len(v) for v in self.prefactors.values())
 
     @property
     def nkd(self):
@@ -246,7 +254,50 @@ class ReactionNetwork:
         if self.has_sorption:
             self._sorb = self._sorption_desc(arr)
             d.sorption = C.pointer(self._sorb)
+        if self.has_prefactors:
+            self._pref = self._prefactor_desc(arr)
+            d.prefactors = C.pointer(self._pref)
         return d
+
+    def _prefactor_desc(self, arr) -> abi.PfPrefactorDesc:
+        MP, MS = abi.PF_MAX_PREFACTORS, abi.PF_MAX_PREFACTOR_SPECIES
+        nm = self.nmnrl
+        pidx = {s: i for i, s in enumerate(self.primary)}
+        sidx = {s: i for i, s in enumerate(self.secondary)}
+        i32, f64 = np.int32, np.float64
+        cnt = np.zeros(nm, i32)
+        rate, ea = np.zeros((nm, MP), f64), np.zeros((nm, MP), f64)
+        nsp = np.zeros((nm, MP), i32)
+        spec = np.zeros((nm, MP, MS), i32)
+        alpha, beta, atten = (np.zeros((nm, MP, MS), f64) for _ in range(3))
+        for name, prefs in self.prefactors.items():
+            m = self.minerals.index(name)
+            if len(prefs) > MP:
+                raise ValueError("mineral %s: more than %d prefactors" % (name, MP))
+            cnt[m] = len(prefs)
+            for p, pr in enumerate(prefs):
+                rate[m, p] = pr["rate"]
+                ea[m, p] = pr.get("activation_energy", 0.0)
+                sps = list(pr.get("species", ()))
+                if len(sps) > MS:
+                    raise ValueError("mineral %s: more than %d prefactor species" % (name, MS))
+                nsp[m, p] = len(sps)
+                for k, sp in enumerate(sps):
+                    nm_ = sp["name"]
+                    spec[m, p, k] = pidx[nm_] if nm_ in pidx else -(sidx[nm_] + 1)
+                    alpha[m, p, k] = sp.get("alpha", 0.0)
+                    beta[m, p, k] = sp.get("beta", 0.0)
+                    atten[m, p, k] = sp.get("atten_coef", 0.0)
+        pd = abi.PfPrefactorDesc()
+        pd.num_prefactors = _ptr(arr(cnt, i32), C.c_int32)
+        pd.rate = _ptr(arr(rate, f64), C.c_double)
+        pd.activation_energy = _ptr(arr(ea, f64), C.c_double)
+        pd.nspec = _ptr(arr(nsp, i32), C.c_int32)
+        pd.spec = _ptr(arr(spec, i32), C.c_int32)
+        pd.alpha = _ptr(arr(alpha, f64), C.c_double)
+        pd.beta = _ptr(arr(beta, f64), C.c_double)
+        pd.atten_coef = _ptr(arr(atten, f64), C.c_double)
+        return pd
 
     def _sorption_desc(self, arr) -> abi.PfSorptionDesc:
         sp = self.sorption

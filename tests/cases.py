@@ -136,3 +136,50 @@ def girt_sorption_case(oracle, sorb, nx, ny, nz, seed=9, log_formulation=True, d
     total_k = st.a["total"] * np.exp(0.05 * rng.standard_normal(st.a["total"].shape))
     sorb_k = st.a["total_sorb"] * np.exp(0.05 * rng.standard_normal(st.a["total_sorb"].shape))
     return net, st, grid, total_k, sorb_k
+
+
+def prefactor_network(net, with_secondary=True):
+    """Attach rate prefactors to the five minerals of the 10-component test
+    network: M0 an H+ term with a denominator (alpha 0.37, K 1e9, beta 1) and
+    a plain power of P4; M1 two parallel prefactors, one with an activation
+    energy; M2 a secondary species followed by a primary one (the primary
+    species' derivative then walks the complex's species count, 3 of M2's 4
+    species); M3 none; M4 a secondary species alone.  with_secondary=False
+    keeps only the primary-species terms."""
+    k = net.mnrl_rate_constant
+    three = next(net.secondary[i] for i in range(net.nsec) if net.sec_nspec[i] == 3)
+    two = next(net.secondary[i] for i in range(net.nsec) if net.sec_nspec[i] == 2)
+    pf = {
+        "M0": [dict(rate=k[0], species=[dict(name="H+", alpha=0.37, atten_coef=1e9, beta=1.0),
+                                        dict(name="P4", alpha=0.31)])],
+        "M1": [dict(rate=k[1], activation_energy=2.0e4,
+                    species=[dict(name="P2", alpha=0.5, atten_coef=10.0, beta=0.5)]),
+               dict(rate=0.3 * k[1], species=[dict(name="P6", alpha=1.0)])],
+        "M2": [dict(rate=k[2], species=([dict(name=three, alpha=0.25, atten_coef=3.0, beta=0.7)]
+                                        if with_secondary else []) + [dict(name="P5", alpha=0.2)])],
+    }
+    if with_secondary:
+        pf["M4"] = [dict(rate=2.0 * k[4], species=[dict(name=two, alpha=0.4, atten_coef=5.0, beta=0.8)])]
+    net.prefactors = pf
+    return net
+
+
+def prefactor_case(oracle, ncells=600, log_formulation=True, with_secondary=True):
+    """The 10-component network (30 complexes, 5 kinetic minerals) with rate
+    prefactors, cells from the constraint equilibrator, and each mineral's
+    logK at the cells' median log Q so that about half of them precipitate."""
+    opts = default_options(isothermal=0)
+    opts["use_log_formulation"] = int(log_formulation)
+    net = generate.random_network(10, 30, 5, seed=710, options=opts)
+    st, ct, cc = generate.random_cells(net, ncells, seed=7101)
+    st, _ = prepare(oracle, net, st, ct, cc)
+    la = np.log10(st.a["pri_molal"] * st.a["pri_act_coef"])
+    for m in range(net.nmnrl):
+        lq = sum(net.mnrl_stoich[m, j] * la[net.mnrl_spec[m, j]] for j in range(net.mnrl_nspec[m]))
+        delta = float(np.median(lq)) - net.mnrl_logK[m]
+        net.mnrl_logK[m] += delta
+        if net.mnrl_logKcoef is not None:
+            net.mnrl_logKcoef[m, 1] += delta
+    prefactor_network(net, with_secondary)
+    st.net = net
+    return net, st

@@ -6,8 +6,9 @@ Both sum every entry in the reference's order (connections x, y, z; then
 accumulation; then reaction; then the log column scaling), so the entries
 agree to rounding of the per-cell derivative terms.  Tolerance: 1e-10
 relative to the largest entry of the same block row (matrix) and to the
-accumulation scale psv*|total|/dt of the same component (residual, whose
-terms cancel at convergence).
+gross magnitude of the same component's residual terms -- the accumulation
+psv*|total|/dt, the sorbed V*|S|/dt, the minerals' sum |nu| |rate| V --
+(residual, whose terms cancel at convergence).
 """
 import numpy as np
 import pytest
@@ -50,11 +51,15 @@ def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt, sk=None):
     assert err.max() < REL, ("values", err.max())
     # exact zeros where the reference has exact zeros (dry cells, connections)
     assert np.array_equal(blocks == 0.0, blocks_ref == 0.0)
-    # residual
+    # residual, relative to the gross magnitude of its terms per component
     psv = st.a["porosity"] * st.a["saturation"] * 1000.0 * st.a["volume"]
     acc = (psv * np.maximum(np.abs(tk), np.abs(ref_st.a["total"])) / dt).T  # [cell][comp]
     if sk is not None:
         acc = acc + (st.a["volume"] * np.maximum(np.abs(sk), np.abs(ref_st.a["total_sorb"])) / dt).T
+    # the kinetic-mineral terms' gross magnitude sum_m |nu_mj| |rate_m| V
+    for m in range(net.nmnrl):
+        for j in range(net.mnrl_nspec[m]):
+            acc[:, net.mnrl_spec[m, j]] += np.abs(net.mnrl_stoich[m, j] * ref_st.a["mnrl_rate"][m]) * st.a["volume"]
     scale = np.maximum(acc.max(axis=0, keepdims=True), 1e-300)
     er = np.abs(r - r_ref).reshape(N, n) / scale
     assert er.max() < REL, ("residual", er.max())

@@ -1,0 +1,86 @@
+"""Kinetic-mineral rate prefactors on the GPU against the oracle: the plain
+step kernel (RStep with the prefactor rate and derivative of
+RKineticMineral, reaction_mineral.F90:820-858, 976-1070) in the log and
+linear formulations, the global-implicit assembly, and the entry points that
+refuse such a network."""
+import numpy as np
+import pytest
+
+import cases
+from pfgpu import abi
+from test_gpu_parity import compare
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
+def test_plain_rstep_with_prefactors_matches_oracle(oracle, logf):
+    from pfgpu.engine import ReactionEngine
+    net, st = cases.prefactor_case(oracle, ncells=1000, log_formulation=logf)
+    ref = st.copy()
+    assert oracle.rstep(net, ref, 3600.0, nthreads=8) == 0
+    # the oracle on one-ulp-perturbed inputs: how far rounding alone moves
+    # it (minerals near equilibrium amplify it by 1/|1 - Q/K|)
+    perts = []
+    for key, to in (("total", np.inf), ("total", -np.inf), ("pri_molal", np.inf)):
+        p = st.copy()
+        p.a[key][:] = np.nextafter(p.a[key], to)
+        oracle.rstep(net, p, 3600.0, nthreads=8)
+        perts.append(p)
+    eng = ReactionEngine(net)
+    dev = st.to("cuda")
+    eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_PLAIN)
+    got = dev.numpy()
+    errs, flips, same, outliers, self_flips, self_out = compare(
+        net, ref, got, "prefactors/plain/%s" % ("log" if logf else "linear"), perts)
+    slack = max(2, 0.01 * (int(same.sum()) + flips))
+    assert same.sum() > 0.9 * st.ncells, same.sum()
+    assert flips <= 2 * self_flips + slack, (flips, self_flips)
+    assert outliers <= 2 * self_out + slack, (outliers, self_out)
+    for k, v in errs.items():
+        assert v < REL, (k, v, errs)
+    r = ref.a["mnrl_rate"][:, same]
+    assert all((r[m] > 0).any() and (r[m] < 0).any() for m in range(net.nmnrl))
+
+
+def test_kernels_without_prefactors_refuse_them(oracle):
+    from pfgpu.engine import ReactionEngine
+    net, st = cases.prefactor_case(oracle, ncells=64)
+    eng = ReactionEngine(net)
+    dev = st.to("cuda")
+    with pytest.raises(abi.PfError) as e:
+        eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_BATCHED)
+    assert e.value.code == abi.PF_ERR_UNSUPPORTED
+    for lanes in (1, 2, 4, 8):
+        assert eng.set_launch_config(128, 1, 0, lanes) == abi.PF_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
+def test_girt_with_prefactors_matches_oracle(oracle, logf):
+    from pfgpu.engine import ReactionEngine
+    from pfgpu.girt import GirtAssembler, StructuredGrid
+    from test_gpu_girt import _check
+    nx, ny, nz = 8, 6, 5
+    net, st = cases.prefactor_case(oracle, ncells=600, log_formulation=logf)
+    st = st.subset(np.arange(nx * ny * nz))
+    st.net = net
+    st.a["saturation"][[3, 77]] = 0.0  # dry cells
+    rng = np.random.default_rng(17)
+
+    def q(shape):
+        return rng.uniform(1e-7, 1e-5, shape) * rng.choice([-1.0, 1.0], shape)
+    grid = dict(nx=nx, ny=ny, nz=nz, dx=2.0, dy=1.5, dz=0.5, qx=q((nz, ny, nx - 1)), qy=q((nz, ny - 1, nx)),
+                qz=q((nz - 1, ny, nx)), diffusion=1e-9, tortuosity=0.5, dispersivity=0.1)
+    tk = st.a["total"] * np.exp(0.05 * rng.standard_normal(st.a["total"].shape))
+    dt = 86400.0
+    asm = GirtAssembler(ReactionEngine(net), StructuredGrid(**grid))
+    dev = st.to("cuda")
+    r, v = asm.assemble(dev, torch.from_numpy(tk).cuda(), dt)
+    torch.cuda.synchronize()
+    ref_st = st.copy()
+    r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host)
+    _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt)
+    np.testing.assert_allclose(dev.numpy().a["mnrl_rate"], ref_st.a["mnrl_rate"], rtol=1e-12, atol=1e-300)
