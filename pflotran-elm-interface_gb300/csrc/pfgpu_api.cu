@@ -1,5 +1,6 @@
 // pfgpu_api.cu -- the C ABI (include/pfgpu.h): network upload, argument
 // checking, kernel dispatch, the status reduction and the host-buffer path.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -38,6 +39,14 @@ struct PfNetwork {
   // host-path arena (grow-only)
   void* d_arena = nullptr;
   size_t arena_bytes = 0;
+  // host-path pipeline: copy-in, compute and copy-out streams, per-chunk
+  // events, counters and the chunk-local work-queue orders (pinned)
+  cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+  cudaEvent_t ev_in[16] = {}, ev_comp[16] = {}, ev_start = nullptr;
+  unsigned long long* d_ccounters = nullptr;  // [16][8]
+  unsigned long long* h_ccounters = nullptr;
+  int64_t* h_order = nullptr;
+  size_t h_order_cap = 0;
 };
 
 namespace {
@@ -487,6 +496,17 @@ int32_t pf_network_destroy(PfNetwork* net) {
   if (net->d_counters) cudaFree(net->d_counters);
   if (net->h_counters) cudaFreeHost(net->h_counters);
   if (net->d_arena) cudaFree(net->d_arena);
+  for (int c = 0; c < 16; ++c) {
+    if (net->ev_in[c]) cudaEventDestroy(net->ev_in[c]);
+    if (net->ev_comp[c]) cudaEventDestroy(net->ev_comp[c]);
+  }
+  if (net->ev_start) cudaEventDestroy(net->ev_start);
+  if (net->s_in) cudaStreamDestroy(net->s_in);
+  if (net->s_comp) cudaStreamDestroy(net->s_comp);
+  if (net->s_out) cudaStreamDestroy(net->s_out);
+  if (net->d_ccounters) cudaFree(net->d_ccounters);
+  if (net->h_ccounters) cudaFreeHost(net->h_ccounters);
+  if (net->h_order) cudaFreeHost(net->h_order);
   if (net->d_ctype) cudaFree(net->d_ctype);
   if (net->d_scratch) cudaFree(net->d_scratch);
   if (net->d_girt) cudaFree(net->d_girt);
@@ -546,8 +566,7 @@ int32_t pf_network_get_launch(const PfNetwork* net, PfLaunchConfig* cfg) {
   return PF_OK;
 }
 
-int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel, void* stream,
-                 PfStepStats* stats) {
+static int check_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel) {
   int rc = validate_state(net, state);
   if (rc) return rc;
   if (!(dt > 0.0) && !state->dt_cell) return PF_ERR_INVALID;
@@ -558,6 +577,27 @@ int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t ke
   if (net->dev.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
       net->dev.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON)
     return PF_ERR_UNSUPPORTED;
+  return PF_OK;
+}
+
+// zero counters[0..8) and launch the step on stream s ([0] is the work queue;
+// scratch: the batched kernel's per-cell set-up values for these cells)
+static int enqueue_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel,
+                         unsigned long long* counters, double* scratch, cudaStream_t s) {
+  if (cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess) return PF_ERR_CUDA;
+  int lr;
+  if (kernel == PF_KERNEL_PLAIN)
+    lr = launch_rstep_plain(net->dev, *state, dt, counters + 1, s);
+  else
+    lr = launch_rstep_batched(net->dev, *state, dt, net->launch, net->num_sms, scratch, counters, counters + 1,
+                              s);
+  return lr != 0 ? PF_ERR_CUDA : PF_OK;
+}
+
+int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel, void* stream,
+                 PfStepStats* stats) {
+  int rc = check_rstep(net, state, dt, kernel);
+  if (rc) return rc;
   if (state->ncells == 0) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return PF_OK;
@@ -567,16 +607,10 @@ int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t ke
     rc = ensure_scratch(net, state->ncells);
     if (rc) return rc;
   }
-  cudaError_t e = cudaMemsetAsync(net->d_counters, 0, 8 * sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return PF_ERR_CUDA;
-  int lr;
-  if (kernel == PF_KERNEL_PLAIN)
-    lr = launch_rstep_plain(net->dev, *state, dt, net->d_counters + 1, s);
-  else
-    lr = launch_rstep_batched(net->dev, *state, dt, net->launch, net->num_sms, net->d_scratch,
-                              net->d_counters, net->d_counters + 1, s);
-  if (lr != 0) return PF_ERR_CUDA;
+  rc = enqueue_rstep(net, state, dt, kernel, net->d_counters, net->d_scratch, s);
+  if (rc) return rc;
   if (!stats) return PF_OK;
+  cudaError_t e;
   e = cudaMemcpyAsync(net->h_counters, net->d_counters, 8 * sizeof(unsigned long long),
                       cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -720,36 +754,51 @@ int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, cons
   return pf_equilibrate_constraint_ex(net, state, ctype, nullptr, cconc, use_prev, iterations, stream);
 }
 
+// Host-buffer step, pipelined over chunks of cells: chunk c's inputs go in on
+// one stream while earlier chunks compute on a second and finished chunks'
+// results come back on a third.  Each chunk has its own counters and set-up
+// scratch.  (Chunks computing side by side on several streams were slower:
+// the persistent kernels then compete for the SMs.)  On the
+// device each chunk is its own compact SoA block (every field's rows for the
+// chunk gathered from the host's strided rows by one 2-D copy); a chunk's
+// work-queue order is the caller's order restricted to the chunk, renumbered
+// locally.
 int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t kernel, PfStepStats* stats) {
-  int rc = validate_state(net, h);
+  int rc = check_rstep(net, h, dt, kernel);
   if (rc) return rc;
   const int64_t N = h->ncells;
   if (N == 0) return pf_rstep(net, h, dt, kernel, nullptr, stats);
-  const int n = net->dev.n, ns = net->dev.ns, nm = net->dev.nm;
+  const int n = net->dev.n, ns = net->dev.ns, nm = net->dev.nm, nx = net->dev.nionx;
   struct Field {
     void* host;
-    size_t bytes;
+    int rows;
+    int esize;
     bool in, out;
   };
-  const size_t d8 = sizeof(double), i4 = sizeof(int32_t);
+  const int d8 = sizeof(double), i4 = sizeof(int32_t);
   Field f[] = {
-      {h->total, n * N * d8, true, true},          {h->pri_molal, n * N * d8, true, true},
-      {h->pri_act_coef, n * N * d8, true, true},   {h->sec_act_coef, ns * N * d8, true, true},
-      {h->sec_molal, ns * N * d8, true, true},     {h->mnrl_volfrac, nm * N * d8, true, true},
-      {h->mnrl_area, nm * N * d8, true, false},    {h->mnrl_rate, nm * N * d8, false, true},
-      {(void*)h->porosity, N * d8, true, false},   {(void*)h->saturation, N * d8, true, false},
-      {(void*)h->den_kg, N * d8, true, false},     {(void*)h->volume, N * d8, true, false},
-      {(void*)h->temperature, N * d8, true, false}, {(void*)h->dt_cell, N * d8, true, false},
-      {h->status, N * i4, false, true},            {h->newton_its, N * i4, false, true},
-      {h->num_substeps, N * i4, false, true},
-      {(void*)h->cell_order, N * sizeof(int64_t), true, false},
-      {h->total_sorb, n * N * d8, true, true},
-      {h->ionx_ref_sorbed, (size_t)net->dev.nionx * N * d8, true, true},
+      {h->total, n, d8, true, true},           {h->pri_molal, n, d8, true, true},
+      {h->pri_act_coef, n, d8, true, true},    {h->sec_act_coef, ns, d8, true, true},
+      {h->sec_molal, ns, d8, true, true},      {h->mnrl_volfrac, nm, d8, true, true},
+      {h->mnrl_area, nm, d8, true, false},     {h->mnrl_rate, nm, d8, false, true},
+      {(void*)h->porosity, 1, d8, true, false}, {(void*)h->saturation, 1, d8, true, false},
+      {(void*)h->den_kg, 1, d8, true, false},  {(void*)h->volume, 1, d8, true, false},
+      {(void*)h->temperature, 1, d8, true, false}, {(void*)h->dt_cell, 1, d8, true, false},
+      {h->status, 1, i4, false, true},         {h->newton_its, 1, i4, false, true},
+      {h->num_substeps, 1, i4, false, true},
+      {(void*)h->cell_order, 1, (int)sizeof(int64_t), false, false},  // remapped per chunk below
+      {h->total_sorb, n, d8, true, true},      {h->ionx_ref_sorbed, nx, d8, true, true},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
-  size_t need = 0;
+  // chunks of about 2^18 cells (at most 16); of 1, 2 and 4 chunks at 10^6
+  // cells, 4 hid the most copy time behind the compute
+  const int64_t target = 262144;
+  const int K = (int)std::min<int64_t>(16, (N + target - 1) / target);
+  const int64_t chunk = ((N + K - 1) / K + 63) / 64 * 64;  // whole 64-cell groups: aligned slices
+  size_t per_chunk = 0;
   for (int k = 0; k < nf; ++k)
-    if (f[k].host) need += pad16(f[k].bytes);
+    if (f[k].host) per_chunk += pad16((size_t)f[k].rows * chunk * f[k].esize);
+  const size_t need = per_chunk * K;
   if (need > net->arena_bytes) {
     if (net->d_arena) cudaFree(net->d_arena);
     net->d_arena = nullptr;
@@ -757,47 +806,129 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     if (cudaMalloc(&net->d_arena, need) != cudaSuccess) return PF_ERR_CUDA;
     net->arena_bytes = need;
   }
-  void* dptr[32];
-  size_t off = 0;
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < nf; ++k) {
-    dptr[k] = nullptr;
-    if (!f[k].host) continue;
-    dptr[k] = (char*)net->d_arena + off;
-    off += pad16(f[k].bytes);
-    if (f[k].in && f[k].bytes && e == cudaSuccess)
-      e = cudaMemcpyAsync(dptr[k], f[k].host, f[k].bytes, cudaMemcpyHostToDevice, 0);
+  if (!net->s_in) {
+    for (cudaStream_t* st : {&net->s_in, &net->s_comp, &net->s_out})
+      if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
+    for (int c = 0; c < 16 && e == cudaSuccess; ++c) {
+      e = cudaEventCreateWithFlags(&net->ev_in[c], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&net->ev_comp[c], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&net->ev_start, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&net->d_ccounters, 16 * 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&net->h_ccounters, 16 * 8 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return PF_ERR_CUDA;
   }
+  if (kernel == PF_KERNEL_BATCHED) {
+    rc = ensure_scratch(net, chunk * K);
+    if (rc) return rc;
+  }
+  const size_t scratch_chunk = batched_scratch_doubles(net->dev, chunk);
+  // the step's device buffers may still be in use by work on the legacy stream
+  e = cudaEventRecord(net->ev_start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(net->s_in, net->ev_start, 0);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(net->s_comp, net->ev_start, 0);
   if (e != cudaSuccess) return PF_ERR_CUDA;
-  PfCellState d = *h;
-  d.total = (double*)dptr[0];
-  d.pri_molal = (double*)dptr[1];
-  d.pri_act_coef = (double*)dptr[2];
-  d.sec_act_coef = (double*)dptr[3];
-  d.sec_molal = (double*)dptr[4];
-  d.mnrl_volfrac = (double*)dptr[5];
-  d.mnrl_area = (double*)dptr[6];
-  d.mnrl_rate = (double*)dptr[7];
-  d.porosity = (const double*)dptr[8];
-  d.saturation = (const double*)dptr[9];
-  d.den_kg = (const double*)dptr[10];
-  d.volume = (const double*)dptr[11];
-  d.temperature = (const double*)dptr[12];
-  d.dt_cell = (const double*)dptr[13];
-  d.status = (int32_t*)dptr[14];
-  d.newton_its = (int32_t*)dptr[15];
-  d.num_substeps = (int32_t*)dptr[16];
-  d.cell_order = (const int64_t*)dptr[17];
-  d.total_sorb = (double*)dptr[18];
-  d.ionx_ref_sorbed = (double*)dptr[19];
-  PfStepStats local{};
-  rc = pf_rstep(net, &d, dt, kernel, nullptr, stats ? stats : &local);
-  if (rc < 0) return rc;
-  for (int k = 0; k < nf; ++k)
-    if (f[k].host && f[k].out && f[k].bytes && e == cudaSuccess)
-      e = cudaMemcpyAsync(f[k].host, dptr[k], f[k].bytes, cudaMemcpyDeviceToHost, 0);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
-  return e == cudaSuccess ? rc : PF_ERR_CUDA;
+  auto cells_of = [&](int c) { return std::min(chunk, N - c * chunk); };
+  // chunk c's block of field k (nullptr for a field the caller did not pass)
+  auto dev_field = [&](int c, int k) -> char* {
+    if (!f[k].host) return nullptr;
+    size_t off = per_chunk * c;
+    for (int q = 0; q < k; ++q)
+      if (f[q].host) off += pad16((size_t)f[q].rows * chunk * f[q].esize);
+    return (char*)net->d_arena + off;
+  };
+  // an error after copies were enqueued: let them finish before returning,
+  // they read and write the caller's buffers
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(net->s_in);
+    cudaStreamSynchronize(net->s_comp);
+    cudaStreamSynchronize(net->s_out);
+    return code;
+  };
+  // 2-D copy of field k for chunk c: rows of nc elements, host pitch N, device pitch nc
+  auto copy = [&](int c, int k, bool to_dev, cudaStream_t st) {
+    const int64_t nc = cells_of(c);
+    const size_t es = f[k].esize, w = (size_t)nc * es;
+    char* hp = (char*)f[k].host + (size_t)c * chunk * es;
+    char* dp = dev_field(c, k);
+    return to_dev ? cudaMemcpy2DAsync(dp, w, hp, (size_t)N * es, w, f[k].rows, cudaMemcpyHostToDevice, st)
+                  : cudaMemcpy2DAsync(hp, (size_t)N * es, dp, w, w, f[k].rows, cudaMemcpyDeviceToHost, st);
+  };
+  for (int c = 0; c < K && e == cudaSuccess; ++c) {
+    for (int k = 0; k < nf && e == cudaSuccess; ++k)
+      if (f[k].host && f[k].in && f[k].rows > 0) e = copy(c, k, true, net->s_in);
+    if (e == cudaSuccess) e = cudaEventRecord(net->ev_in[c], net->s_in);
+  }
+  if (e != cudaSuccess) return fail(PF_ERR_CUDA);
+  // chunk-local orders, built while the inputs are in flight
+  const int kord = 17;
+  if (h->cell_order) {
+    if (net->h_order_cap < (size_t)N) {
+      if (net->h_order) cudaFreeHost(net->h_order);
+      net->h_order = nullptr;
+      net->h_order_cap = 0;
+      if (cudaMallocHost(&net->h_order, (size_t)N * sizeof(int64_t)) != cudaSuccess) return fail(PF_ERR_CUDA);
+      net->h_order_cap = (size_t)N;
+    }
+    int64_t pos[16];
+    for (int c = 0; c < K; ++c) pos[c] = c * chunk;
+    for (int64_t i = 0; i < N; ++i) {
+      const int64_t o = h->cell_order[i];
+      if (o < 0 || o >= N) return fail(PF_ERR_INVALID);
+      const int c = (int)(o / chunk);
+      if (pos[c] >= c * chunk + cells_of(c)) return fail(PF_ERR_INVALID);  // not a permutation
+      net->h_order[pos[c]++] = o - c * chunk;
+    }
+  }
+  for (int c = 0; c < K && e == cudaSuccess; ++c) {
+    const int64_t nc = cells_of(c);
+    PfCellState d = *h;
+    d.ncells = nc;
+    double** dfl[] = {&d.total, &d.pri_molal, &d.pri_act_coef, &d.sec_act_coef, &d.sec_molal, &d.mnrl_volfrac,
+                      &d.mnrl_area, &d.mnrl_rate};
+    for (int k = 0; k < 8; ++k) *dfl[k] = (double*)dev_field(c, k);
+    const double** cfl[] = {&d.porosity, &d.saturation, &d.den_kg, &d.volume, &d.temperature, &d.dt_cell};
+    for (int k = 0; k < 6; ++k) *cfl[k] = (const double*)dev_field(c, 8 + k);
+    d.status = (int32_t*)dev_field(c, 14);
+    d.newton_its = (int32_t*)dev_field(c, 15);
+    d.num_substeps = (int32_t*)dev_field(c, 16);
+    d.cell_order = (const int64_t*)dev_field(c, kord);
+    d.total_sorb = (double*)dev_field(c, 18);
+    d.ionx_ref_sorbed = (double*)dev_field(c, 19);
+    cudaStream_t sc = net->s_comp;
+    e = cudaStreamWaitEvent(sc, net->ev_in[c], 0);
+    if (e == cudaSuccess && h->cell_order)
+      e = cudaMemcpyAsync(dev_field(c, kord), net->h_order + c * chunk, (size_t)nc * sizeof(int64_t),
+                          cudaMemcpyHostToDevice, sc);
+    if (e != cudaSuccess) break;
+    rc = enqueue_rstep(net, &d, dt, kernel, net->d_ccounters + 8 * c,
+                       net->d_scratch ? net->d_scratch + scratch_chunk * c : nullptr, sc);
+    if (rc) return fail(rc);
+    e = cudaEventRecord(net->ev_comp[c], sc);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(net->s_out, net->ev_comp[c], 0);
+    for (int k = 0; k < nf && e == cudaSuccess; ++k)
+      if (f[k].host && f[k].out && f[k].rows > 0) e = copy(c, k, false, net->s_out);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(net->h_ccounters, net->d_ccounters, (size_t)K * 8 * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, net->s_out);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(net->s_out);
+  if (e != cudaSuccess) return fail(PF_ERR_CUDA);
+  PfStepStats st{};
+  st.cells = N;
+  bool timeout = false;
+  for (int c = 0; c < K; ++c) {
+    const unsigned long long* q = net->h_ccounters + 8 * c;
+    st.newton_iterations += (int64_t)q[1];
+    st.failed_cells += (int64_t)q[2];
+    timeout = timeout || q[3];
+    st.max_newton_iterations = std::max(st.max_newton_iterations, (int32_t)q[4]);
+    st.max_substeps = std::max(st.max_substeps, (int32_t)q[5]);
+  }
+  if (stats) *stats = st;
+  if (timeout) return PF_ERR_TIMEOUT;
+  return st.failed_cells ? PF_CELL_FAILURES : PF_OK;
 }
 
 }  // extern "C"

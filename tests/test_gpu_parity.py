@@ -31,6 +31,7 @@ import pytest
 
 import cases
 from pfgpu import abi
+from pfgpu.network import CellState
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -216,6 +217,40 @@ def test_rstep_host_path_matches_device(oracle):
     d = dev.numpy()
     for k in ("total", "pri_molal", "sec_molal", "mnrl_rate", "mnrl_volfrac", "newton_its"):
         np.testing.assert_array_equal(host.a[k], d.a[k])
+
+
+@pytest.mark.parametrize("with_order", [False, True], ids=["natural", "permuted"])
+def test_rstep_host_pipeline_over_chunks_matches_device(oracle, with_order):
+    """pf_rstep_host cuts a large state into chunks of 2^18 cells (copy-in,
+    compute and copy-out overlapped on three streams, the work-queue order
+    restricted to each chunk): 600,000 cells (three chunks, the last one
+    short) give the device path's results bit for bit, with the same
+    statistics; an order that is not a permutation is refused."""
+    net, st0 = cases.case(oracle, "random12")
+    reps = -(-600000 // st0.ncells)
+    big = CellState(net, {k: (np.tile(v, reps)[..., :600000] if v.ndim == 1 else np.tile(v, (1, reps))[:, :600000])
+                          for k, v in st0.a.items()})
+    big.a["total"][:] *= np.random.default_rng(5).uniform(0.9, 1.1, big.a["total"].shape)
+    eng = _engine(net)
+    order_dev = order_host = None
+    if with_order:
+        perm = np.random.default_rng(6).permutation(600000).astype(np.int64)
+        order_host, order_dev = perm, torch.from_numpy(perm).cuda()
+    dev = big.to("cuda")
+    s_dev = eng.rstep(dev, 86400.0, order=order_dev)
+    host = big.copy()
+    s_host = eng.rstep_host(host, 86400.0, order=order_host)
+    d = dev.numpy()
+    for k in ("total", "pri_molal", "pri_act_coef", "sec_molal", "mnrl_rate", "mnrl_volfrac", "newton_its",
+              "num_substeps", "status"):
+        np.testing.assert_array_equal(host.a[k], d.a[k], err_msg=k)
+    assert s_host == s_dev
+    if with_order:
+        bad = order_host.copy()
+        bad[7] = bad[8]
+        with pytest.raises(abi.PfError) as e:
+            eng.rstep_host(big.copy(), 86400.0, order=bad)
+        assert e.value.code == abi.PF_ERR_INVALID
 
 
 def test_cell_order_does_not_change_results(oracle):
