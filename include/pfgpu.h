@@ -434,6 +434,13 @@ typedef struct PfGirtArgs {
                                         fixed accumulation, RAccumulationSorb at
                                         reactive_transport.F90:1026); required when the
                                         network has sorption, else ignored (NULL) */
+  int32_t numerical_derivatives;     /* option%transport%numerical_derivatives: the
+                                        reaction part of the diagonal blocks by
+                                        forward differences (RReactionDerivative,
+                                        reaction.F90:4176-4230; perturbation 1e-5 m_j)
+                                        instead of analytically.  pf_rstep has no such
+                                        mode: the reference stops there for OSRT
+                                        (reaction.F90:3918-3920) */
 } PfGirtArgs;
 
 /* Host: block-row pattern of the 7-point structured-grid matrix (block

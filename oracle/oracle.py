@@ -52,7 +52,7 @@ class Oracle:
         lib.oracle_equilibrate.argtypes = [D, S, C.POINTER(C.c_int32), C.c_void_p, C.POINTER(C.c_double),
                                            C.c_int, C.POINTER(C.c_int32), C.c_int]
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
-        lib.oracle_girt_assemble.argtypes = [D, S, ip, dp, dp, dp, dp, dp, dp, C.c_double, ip, ip, dp, dp]
+        lib.oracle_girt_assemble.argtypes = [D, S, ip, dp, dp, dp, dp, dp, dp, C.c_double, ip, ip, dp, dp, C.c_int]
         lib.oracle_ifc67_density.argtypes = [C.c_double, C.c_double]
         lib.oracle_ifc67_density.restype = C.c_double
         for f in ("oracle_rstep", "oracle_rreact", "oracle_implicit_step", "oracle_update_kinetic_state",
@@ -109,13 +109,15 @@ class Oracle:
                                          nthreads)
         return rc, its
 
-    def girt_assemble(self, net, state, grid, total_k, dt, rowptr, colidx, total_sorb_k=None):
+    def girt_assemble(self, net, state, grid, total_k, dt, rowptr, colidx, total_sorb_k=None,
+                      numerical_derivatives=False):
         """Global-implicit residual [ncells*ncomp] and SeqBAIJ values
         [nnzb*ncomp*ncomp] (blocks column-major) of a structured grid.
         grid: dict nx, ny, nz, dx, dy, dz, qx, qy, qz, diffusion, tortuosity,
         dispersivity; total_sorb_k: sorbed totals at the start of the step
-        (networks with sorption).  Updates state's total and sec_molal (and
-        total_sorb, the ion-exchange warm start)."""
+        (networks with sorption); numerical_derivatives: the reaction
+        Jacobian by forward differences.  Updates state's total and sec_molal
+        (and total_sorb, the ion-exchange warm start)."""
         d, s = self._args(net, state)
         f = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
         gi = np.array([grid["nx"], grid["ny"], grid["nz"]], np.int32)
@@ -133,7 +135,8 @@ class Oracle:
                                            P(q[0]), P(q[1]), P(q[2]), P(tk),
                                            P(sk) if sk is not None else None, float(dt),
                                            rp.ctypes.data_as(C.POINTER(C.c_int32)),
-                                           ci.ctypes.data_as(C.POINTER(C.c_int32)), P(r), P(vals))
+                                           ci.ctypes.data_as(C.POINTER(C.c_int32)), P(r), P(vals),
+                                           int(bool(numerical_derivatives)))
         if rc:
             raise RuntimeError("oracle_girt_assemble: %d" % rc)
         return r, vals

@@ -271,7 +271,8 @@ double oracle_ifc67_density(double t, double p) { return ifc67_density(t, p); }
 int oracle_girt_assemble(const PfNetworkDesc* d, const PfCellState* s, const int32_t* grid_i,
                          const double* grid_d, const double* qx, const double* qy, const double* qz,
                          const double* fixed_total, const double* fixed_sorb, double dt,
-                         const int32_t* rowptr, const int32_t* colidx, double* r, double* values) {
+                         const int32_t* rowptr, const int32_t* colidx, double* r, double* values,
+                         int numerical_derivatives) {
   int rc = check(d, s);
   if (rc) return rc;
   Net net(d);
@@ -285,7 +286,8 @@ int oracle_girt_assemble(const PfNetworkDesc* d, const PfCellState* s, const int
   std::vector<int> rp(N + 1), ci(rowptr[N]);
   for (int64_t i = 0; i <= N; ++i) rp[i] = rowptr[i];
   for (int64_t b = 0; b < rowptr[N]; ++b) ci[b] = colidx[b];
-  girt_assemble(net, cells.data(), g, fixed_total, fixed_sorb, dt, rp.data(), ci.data(), r, values);
+  girt_assemble(net, cells.data(), g, fixed_total, fixed_sorb, dt, rp.data(), ci.data(), r, values,
+                numerical_derivatives != 0);
   for (int64_t i = 0; i < N; ++i) scatter(net, s, i, cells[i]);
   return PF_OK;
 }

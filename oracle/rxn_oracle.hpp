@@ -637,14 +637,34 @@ inline void reaction(const Net& net, Cell& c, double* Res, double* J, bool deriv
   if (net.nm > 0) kinetic_mineral(net, c, Res, J, derivative);
 }
 
-// RReactionDerivative, reaction.F90:4134-4240 (analytical branch)
-inline void reaction_derivative(const Net& net, Cell& c, double* Res, double* J) {
+// RReactionDerivative, reaction.F90:4134-4240: the analytical branch, or with
+// numerical = true the forward differences of :4176-4230 (each primary
+// molality raised by 1e-5 of itself on a copy of the auxvars, RTotal, then
+// RReaction; Res stays zero there, as in the reference)
+constexpr double perturbation_tolerance = 1.0e-5;  // reaction.F90:41
+inline void reaction_derivative(const Net& net, Cell& c, double* Res, double* J, bool numerical = false) {
   if (c.sat < rt_min_saturation) return;
   for (int i = 0; i < net.n; ++i) {
     Res[i] = 0.0;
     for (int j = 0; j < net.n; ++j) J[i * MAXN + j] = 0.0;
   }
-  reaction(net, c, Res, J, true);
+  if (!numerical) {
+    reaction(net, c, Res, J, true);
+  } else {
+    double Res_orig[MAXN], Res_pert[MAXN];
+    for (int i = 0; i < net.n; ++i) Res_orig[i] = 0.0;
+    reaction(net, c, Res_orig, nullptr, false);
+    for (int jc = 0; jc < net.n; ++jc) {
+      for (int i = 0; i < net.n; ++i) Res_pert[i] = 0.0;
+      Cell cp = c;
+      const double pert = cp.pri_molal[jc] * perturbation_tolerance;
+      cp.pri_molal[jc] = cp.pri_molal[jc] + pert;
+      total(net, cp);
+      reaction(net, cp, Res_pert, nullptr, false);
+      for (int ic = 0; ic < net.n; ++ic)
+        J[ic * MAXN + jc] = J[ic * MAXN + jc] + (Res_pert[ic] - Res_orig[ic]) / pert;
+    }
+  }
   for (int i = 0; i < net.n; ++i)
     for (int j = 0; j < net.n; ++j)
       if (std::fabs(J[i * MAXN + j]) < 1.0e-40) J[i * MAXN + j] = 0.0;
@@ -1182,7 +1202,7 @@ inline double girt_tran_coef(const Cell& up, const Cell& dn, double q, double di
 // the network has sorption.
 inline void girt_assemble(const Net& net, Cell* cells, const GirtGrid& g, const double* fixed_total,
                           const double* fixed_sorb, double dt, const int* rowptr, const int* colidx, double* r,
-                          double* values) {
+                          double* values, bool numerical_derivatives = false) {
   const int n = net.n;
   const int nx = g.nx, ny = g.ny, nz = g.nz;
   const long long N = (long long)nx * ny * nz;
@@ -1284,7 +1304,7 @@ inline void girt_assemble(const Net& net, Cell* cells, const GirtGrid& g, const 
     double Res[MAXN], J[MAXN * MAXN];
     for (int k = 0; k < n; ++k) Res[k] = 0.0;
     for (int e = 0; e < MAXN * MAXN; ++e) J[e] = 0.0;
-    reaction_derivative(net, cells[c], Res, J);
+    reaction_derivative(net, cells[c], Res, J, numerical_derivatives);
     double* b = block(c, c);
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) b[j * n + i] = b[j * n + i] + J[i * MAXN + j];

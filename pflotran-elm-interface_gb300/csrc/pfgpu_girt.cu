@@ -168,7 +168,95 @@ __device__ __noinline__ void pref_jacobian(const DevNet& net, const Tables& T, c
   }
 }
 
-template <bool HAS_PF>
+// The mineral part of RReaction's residual for one cell (RKineticMineral
+// without the derivative, reaction_mineral.F90:647-913), at primary ln
+// activities lna[] and complexes' ln activities ln_sec_act(i): the same
+// arithmetic as the cell kernel's mineral loop.
+template <class LnSecAct>
+__device__ void mineral_residual(const DevNet& net, const Tables& T, const PfCellState& st, long long X,
+                                 const double* lna, LnSecAct ln_sec_act, double temp, double volume, double* Res) {
+  const SoA soa{st.ncells};
+  const bool tmin = !net.o.isothermal && (net.flags & NETF_MNRL_LOGKCOEF);
+  const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
+  for (int m = 0; m < net.nm; ++m) {
+    const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
+    const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
+    double lnQK = -logK * LOG_TO_LN;
+    for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * lna[T.mnrl_idx(p)];
+    const double QK = exp(lnQK);
+    double aff;
+    if (has_tk) aff = 1.0 - pow(QK, 1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m)));
+    else if (has_msf) aff = 1.0 - pow(QK, 1.0 / T.msf(m));
+    else aff = 1.0 - QK;
+    const double sign_ = fsign1(aff);
+    const double vf = st.mnrl_volfrac[soa.at(m, X)];
+    const bool active = (vf > 0 || sign_ < 0.0) && !(T.irreversible(m) == 1 && sign_ < 0.0) &&
+                        !(T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m));
+    if (!active) continue;
+    const double rl = T.limiter(m);
+    if (rl > 0.0) aff = aff / (1.0 + (1.0 - aff) / rl);
+    double kr;
+    if ((net.flags & NETF_PREFACTOR) && T.pf_cnt(m) > 0) {
+      double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
+      kr = prefactor_rate(T, m, [&](int j) { return lna[j]; }, ln_sec_act, temp, pref, lnps);
+    } else {
+      double arr = 1.0;
+      if (T.ea(m) > 0.0) arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp + 273.15)));
+      kr = T.rate(m) * arr;
+    }
+    double Im_const = -st.mnrl_area[soa.at(m, X)];
+    if (has_msf) Im_const = Im_const / T.msf(m);
+    double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * kr : Im_const * sign_ * fabs(aff) * kr;
+    Im = Im * volume;
+    for (int p = b; p < e; ++p) Res[T.mnrl_idx(p)] = Res[T.mnrl_idx(p)] + T.mnrl_nu(p) * Im;
+  }
+}
+
+// The reaction part of the diagonal block by forward differences
+// (RReactionDerivative's numerical branch, reaction.F90:4176-4230): each
+// primary molality raised by 1e-5 of itself, RTotal's complexes at the
+// raised value, the mineral residual again; columns below 1e-40 in magnitude
+// zeroed, then added to D in the column scaling.
+__device__ __noinline__ void numerical_reaction_jacobian(const DevNet& net, const Tables& T, const PfCellState& st,
+                                                         long long X, const double* P, int bd, int o_lna, int o_s,
+                                                         double temp, double volume, bool logf, bool tsec,
+                                                         double* D) {
+  const SoA soa{st.ncells};
+  const int n = net.n;
+  double lna[PF_MAX_NCOMP], res0[PF_MAX_NCOMP], res1[PF_MAX_NCOMP];
+  for (int j = 0; j < n; ++j) {
+    lna[j] = P[o_lna + j * bd];
+    res0[j] = 0.0;
+  }
+  mineral_residual(
+      net, T, st, X, lna, [&](int i) { return log(P[o_s + i * bd]) + log(st.sec_act_coef[soa.at(i, X)]); }, temp,
+      volume, res0);
+  for (int jc = 0; jc < n; ++jc) {
+    const double m0 = P[jc * bd];
+    const double pert = m0 * 1.0e-5;  // perturbation_tolerance, reaction.F90:41
+    const double saved = lna[jc];
+    lna[jc] = log(m0 + pert) + log(st.pri_act_coef[soa.at(jc, X)]);
+    for (int i = 0; i < n; ++i) res1[i] = 0.0;
+    auto ln_sec_act = [&](int i) {  // RTotal of the perturbed copy, complex i
+      double lnQK = -(tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i)) * LOG_TO_LN;
+      for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
+      const double g = st.sec_act_coef[soa.at(i, X)];
+      return log(exp(lnQK) / g) + log(g);
+    };
+    mineral_residual(net, T, st, X, lna, ln_sec_act, temp, volume, res1);
+    lna[jc] = saved;
+    const double mc = logf ? m0 : 1.0;
+    for (int ic = 0; ic < n; ++ic) {
+      double J = (res1[ic] - res0[ic]) / pert;
+      if (fabs(J) < 1.0e-40) J = 0.0;
+      D[jc * n + ic] = fma(J, mc, D[jc * n + ic]);
+    }
+  }
+}
+
+// HAS_PF: rate prefactors; NUMJAC: the reaction Jacobian by forward
+// differences (instantiated with HAS_PF, whose rate code it needs)
+template <bool HAS_PF, bool NUMJAC>
 __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt,
                                                         const int32_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ colidx, double* __restrict__ r,
@@ -302,8 +390,9 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
       acc = fma(gt.e_sec_nr[q], P[o_s + gt.e_sec_p[q] * bd], acc);
     const double d = ((row == col ? 1.0 : 0.0) + acc * P[o_ic + col * bd]) * den_L;
     double jr = 0.0;
-    for (int q = gt.e_mn_ptr[f]; q < gt.e_mn_ptr[f + 1]; ++q)
-      jr = fma(gt.e_mn_nr[q] * P[o_G + gt.e_mn_m[q] * bd], P[o_u + gt.e_mn_p[q] * bd], jr);
+    if (!NUMJAC)
+      for (int q = gt.e_mn_ptr[f]; q < gt.e_mn_ptr[f + 1]; ++q)
+        jr = fma(gt.e_mn_nr[q] * P[o_G + gt.e_mn_m[q] * bd], P[o_u + gt.e_mn_p[q] * bd], jr);
     if (fabs(jr) < 1.0e-40) jr = 0.0;  // reaction.F90:4232-4237
     const double mc = logf ? P[col * bd] : 1.0;
     const double v = dry ? fma(d, csum, (row == col) ? 1.0 : 0.0) : fma(d, cdiag, jr);
@@ -333,7 +422,10 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   }
   // ---- rate-prefactor part of the reaction Jacobian (its residual part is in
   // the rates above), added to the diagonal block in the column scaling
-  if (has_pf && pf_active && dblk >= 0)
+  if (NUMJAC && !dry && dblk >= 0)
+    numerical_reaction_jacobian(net, T, st, X, P, bd, o_lna, o_s, temp, volume, logf, tsec,
+                                values + (size_t)dblk * nn);
+  else if (has_pf && pf_active && dblk >= 0)
     pref_jacobian(net, T, st, X, P, bd, o_lna, o_s, temp, volume, logf, tsec, pf_active,
                   values + (size_t)dblk * nn);
   // ---- equilibrium sorption (RTotalSorb in RTUpdateAuxVars; a failed
@@ -482,7 +574,9 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   int tpb = 32;
   const size_t smem = girt_smem_bytes(net, &tpb);
   if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
-  auto k = (net.flags & NETF_PREFACTOR) ? girt::girt_cell_kernel<true> : girt::girt_cell_kernel<false>;
+  auto k = a.numerical_derivatives ? girt::girt_cell_kernel<true, true>
+           : (net.flags & NETF_PREFACTOR) ? girt::girt_cell_kernel<true, false>
+                                          : girt::girt_cell_kernel<false, false>;
   if (smem > 48u * 1024u &&
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PF_ERR_CUDA;

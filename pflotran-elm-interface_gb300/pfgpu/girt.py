@@ -83,7 +83,7 @@ class GirtAssembler:
     def nnzb(self) -> int:
         return len(self.colidx_host)
 
-    def args(self, total_k, dt: float, total_sorb_k=None) -> abi.PfGirtArgs:
+    def args(self, total_k, dt: float, total_sorb_k=None, numerical_derivatives=False) -> abi.PfGirtArgs:
         g = self.grid
         a = abi.PfGirtArgs()
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
@@ -97,20 +97,24 @@ class GirtAssembler:
         a.residual, a.values = C.cast(self.residual.data_ptr(), dp), C.cast(self.values.data_ptr(), dp)
         if total_sorb_k is not None:
             a.total_sorb_k = C.cast(total_sorb_k.data_ptr(), dp)
+        a.numerical_derivatives = int(bool(numerical_derivatives))
         return a
 
-    def assemble(self, state: CellState, total_k, dt: float, stream=None, total_sorb_k=None):
+    def assemble(self, state: CellState, total_k, dt: float, stream=None, total_sorb_k=None,
+                 numerical_derivatives=False):
         """Residual and Jacobian values at the iterate in `state` (CUDA
         tensors); total_k: totals at the start of the step [ncomp][ncells];
         total_sorb_k: the sorbed totals at the start of the step (required
-        when the network has sorption).  Returns (residual, values), views of
-        this assembler's buffers."""
+        when the network has sorption); numerical_derivatives: the reaction
+        part of the Jacobian by forward differences (the reference's
+        NUMERICAL_JACOBIAN transport option).  Returns (residual, values),
+        views of this assembler's buffers."""
         total_k = total_k.contiguous()
         if self.engine.net.has_sorption and total_sorb_k is None:
             raise ValueError("a network with sorption needs total_sorb_k")
         if total_sorb_k is not None:
             total_sorb_k = total_sorb_k.contiguous()
-        a = self.args(total_k, dt, total_sorb_k)
+        a = self.args(total_k, dt, total_sorb_k, numerical_derivatives)
         s = state.struct()
         abi.check("pf_girt_assemble",
                   self.engine.lib.pf_girt_assemble(self.engine.handle, C.byref(s), C.byref(a), _stream_ptr(stream)),

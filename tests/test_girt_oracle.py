@@ -166,3 +166,37 @@ def test_oracle_girt_sorption_needs_fixed_sorbed_totals(oracle):
     rp, ci = girt_pattern(2, 1, 1)
     with pytest.raises(RuntimeError):
         oracle.girt_assemble(net, st.copy(), grid, tk, 3600.0, rp, ci)
+
+
+@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
+@pytest.mark.parametrize("name", ["random12", "prefactors"])
+def test_oracle_numerical_reaction_derivative(oracle, name, logf):
+    """RReactionDerivative's forward differences (reaction.F90:4176-4230):
+    the residual is the analytical mode's bit for bit, the Jacobian agrees
+    with the analytical one to the forward-difference error (perturbation
+    1e-5 of each molality), dry cells keep their identity block."""
+    nx, ny, nz = 3, 2, 2
+    if name == "prefactors":
+        net, st = cases.prefactor_case(oracle, ncells=40, log_formulation=logf, with_secondary=False)
+        st = st.subset(np.arange(nx * ny * nz))
+        st.net = net
+        grid = dict(nx=nx, ny=ny, nz=nz, dx=2.0, dy=1.5, dz=0.5, qx=np.full((nz, ny, nx - 1), 2e-6),
+                    qy=np.full((nz, ny - 1, nx), -1e-6), qz=np.full((nz - 1, ny, nx), 3e-6), diffusion=1e-9,
+                    tortuosity=0.5, dispersivity=0.1)
+        tk = st.a["total"] * 1.01
+    else:
+        net, st, grid, tk = cases.girt_case(oracle, name, nx, ny, nz, log_formulation=logf)
+    st.a["saturation"][5] = 0.0
+    st.a["den_kg"][:] = 1000.0  # the analytical mineral derivative's den*1e-3 factor is then 1
+    rp, ci = girt_pattern(nx, ny, nz)
+    r_a, v_a = oracle.girt_assemble(net, st.copy(), grid, tk, 86400.0, rp, ci)
+    r_n, v_n = oracle.girt_assemble(net, st.copy(), grid, tk, 86400.0, rp, ci, numerical_derivatives=True)
+    np.testing.assert_array_equal(r_n, r_a)
+    A, B = _dense(net, rp, ci, v_a), _dense(net, rp, ci, v_n)
+    n = net.ncomp
+    assert np.array_equal(A[5 * n:6 * n, 5 * n:6 * n], B[5 * n:6 * n, 5 * n:6 * n])
+    a = np.abs(A)
+    scale = np.maximum(np.maximum(a.max(axis=0, keepdims=True), a.max(axis=1, keepdims=True)), 1e-300)
+    err = np.abs(A - B) / scale
+    assert err.max() < 1e-3, err.max()
+    assert np.any(A != B)  # the reaction blocks did come from differences

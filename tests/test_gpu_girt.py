@@ -5,7 +5,10 @@ RTResidual / RTJacobian.
 Both sum every entry in the reference's order (connections x, y, z; then
 accumulation; then reaction; then the log column scaling), so the entries
 agree to rounding of the per-cell derivative terms.  Tolerance: 1e-10
-relative to the largest entry of the same block row (matrix) and to the
+relative to the largest entry of the same block row (matrix; with the
+reaction part by forward differences, 1e-6 of it on the diagonal blocks
+plus 4x the oracle's own movement under a 64-eps change of the molalities,
+see fd_noise) and to the
 gross magnitude of the same component's residual terms -- the accumulation
 psv*|total|/dt, the sorbed V*|S|/dt, the minerals' sum |nu| |rate| V --
 (residual, whose terms cancel at convergence).
@@ -22,7 +25,7 @@ pytestmark = pytest.mark.gpu
 REL = 1e-10
 
 
-def _run(oracle, name, dims, logf, dry=()):
+def _run(oracle, name, dims, logf, dry=(), numjac=False):
     from pfgpu.engine import ReactionEngine
     from pfgpu.girt import GirtAssembler, StructuredGrid
     nx, ny, nz = dims
@@ -32,14 +35,49 @@ def _run(oracle, name, dims, logf, dry=()):
     g = StructuredGrid(**grid)
     asm = GirtAssembler(eng, g)
     dev = st.to("cuda")
-    r, v = asm.assemble(dev, torch.from_numpy(tk).cuda(), dt)
+    r, v = asm.assemble(dev, torch.from_numpy(tk).cuda(), dt, numerical_derivatives=numjac)
     torch.cuda.synchronize()
     ref_st = st.copy()
-    r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host)
-    return net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt
+    r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host,
+                                        numerical_derivatives=numjac)
+    out = (net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt)
+    if numjac:
+        return out, fd_noise(oracle, net, st, grid, tk, dt, asm.rowptr_host, asm.colidx_host)
+    return out
 
 
-def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt, sk=None):
+def _mineral_gross(net, ref_st):
+    """[cell][comp] sum over minerals of |nu| |rate| V: the gross size of the
+    kinetic-mineral terms of each residual row."""
+    g = np.zeros((ref_st.ncells, net.ncomp))
+    for m in range(net.nmnrl):
+        for j in range(net.mnrl_nspec[m]):
+            g[:, net.mnrl_spec[m, j]] += np.abs(net.mnrl_stoich[m, j] * ref_st.a["mnrl_rate"][m]) * ref_st.a["volume"]
+    return g
+
+
+def fd_noise(oracle, net, st, grid, tk, dt, rp, ci, total_sorb_k=None):
+    """How far the oracle's forward-difference Jacobian moves when the
+    molalities move by 64 eps of themselves either way (elementwise maximum):
+    the step of 1e-5 m_j turns last-bit differences of the mineral residual
+    into 1e5 times larger ones, more still next to equilibrium where 1 - Q/K
+    cancels.  64 eps in ln m is the size of the rounding of ln Q/K itself (a
+    sum of terms of magnitude 10-50, fused into multiply-adds on the GPU and
+    not on the host), which a one-ulp change of m (1e-16 in ln m) does not
+    reach."""
+    _, v0 = oracle.girt_assemble(net, st.copy(), grid, tk, dt, rp, ci, total_sorb_k=total_sorb_k,
+                                 numerical_derivatives=True)
+    noise = np.zeros_like(v0)
+    for sgn in (1.0, -1.0):
+        p = st.copy()
+        p.a["pri_molal"][:] *= 1.0 + sgn * 64 * np.finfo(float).eps
+        _, vp = oracle.girt_assemble(net, p, grid, tk, dt, rp, ci, total_sorb_k=total_sorb_k,
+                                     numerical_derivatives=True)
+        noise = np.maximum(noise, np.abs(vp - v0))
+    return noise
+
+
+def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt, sk=None, noise=None):
     n, N = net.ncomp, st.ncells
     # matrix: per block row (cell, component i)
     blocks = v.reshape(-1, n, n)          # [b][col][row]
@@ -47,8 +85,18 @@ def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt, sk=None):
     rows = np.repeat(np.arange(N), np.diff(asm.rowptr_host))
     row_scale = np.zeros((N, n))
     np.maximum.at(row_scale, rows, np.abs(blocks_ref).max(axis=1))
-    err = np.abs(blocks - blocks_ref).max(axis=1) / np.maximum(row_scale[rows], 1e-300)
-    assert err.max() < REL, ("values", err.max())
+    tol = REL * np.maximum(row_scale[rows], 1e-300)[:, None, :] * np.ones((1, n, 1))
+    if noise is not None:
+        # reaction part by forward differences (diagonal blocks): 1e-6 of the
+        # block row plus 4x the oracle's own spread (fd_noise); a wrong step or
+        # a missing term would be O(1) there, rounding through the 1e-5 step
+        # reaches ~1e-9.  Off-diagonal (flux) blocks keep the 1e-10.
+        diag = asm.colidx_host == rows
+        tol[diag] = 1e-6 * np.maximum(row_scale[rows[diag]], 1e-300)[:, None, :] + \
+            4 * noise.reshape(blocks.shape)[diag]
+    diff = np.abs(blocks - blocks_ref)
+    assert np.all(diff <= tol), ("values", float((diff / tol).max()))
+    err = diff.max(axis=1) / np.maximum(row_scale[rows], 1e-300)
     # exact zeros where the reference has exact zeros (dry cells, connections)
     assert np.array_equal(blocks == 0.0, blocks_ref == 0.0)
     # residual, relative to the gross magnitude of its terms per component
@@ -57,9 +105,7 @@ def _check(net, st, ref_st, got_st, asm, r, v, r_ref, v_ref, tk, dt, sk=None):
     if sk is not None:
         acc = acc + (st.a["volume"] * np.maximum(np.abs(sk), np.abs(ref_st.a["total_sorb"])) / dt).T
     # the kinetic-mineral terms' gross magnitude sum_m |nu_mj| |rate_m| V
-    for m in range(net.nmnrl):
-        for j in range(net.mnrl_nspec[m]):
-            acc[:, net.mnrl_spec[m, j]] += np.abs(net.mnrl_stoich[m, j] * ref_st.a["mnrl_rate"][m]) * st.a["volume"]
+    acc = acc + _mineral_gross(net, ref_st)
     scale = np.maximum(acc.max(axis=0, keepdims=True), 1e-300)
     er = np.abs(r - r_ref).reshape(N, n) / scale
     assert er.max() < REL, ("residual", er.max())
@@ -101,6 +147,17 @@ def test_girt_parity_with_sorption(oracle, sorb, logf):
     r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host,
                                         total_sorb_k=sk)
     _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt, sk=sk)
+
+
+@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
+def test_girt_parity_numerical_reaction_derivative(oracle, logf):
+    """The reaction Jacobian by forward differences (the reference's
+    NUMERICAL_JACOBIAN transport option) against the oracle's, with dry
+    cells; a network whose minerals react (16 components)."""
+    out, noise = _run(oracle, "hetero16", (7, 6, 4), logf, dry=(2, 50), numjac=True)
+    _check(*out, noise=noise)
+    # the allowance stays small: most entries agree to the analytical tolerance
+    assert np.median(noise[noise > 0] / np.abs(out[8][noise > 0])) < 1e-8
 
 
 def test_girt_parity_dry_cells_and_thin_grids(oracle):

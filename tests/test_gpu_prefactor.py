@@ -58,11 +58,12 @@ def test_kernels_without_prefactors_refuse_them(oracle):
         assert eng.set_launch_config(128, 1, 0, lanes) == abi.PF_ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("numjac", [False, True], ids=["analytical", "numerical"])
 @pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
-def test_girt_with_prefactors_matches_oracle(oracle, logf):
+def test_girt_with_prefactors_matches_oracle(oracle, logf, numjac):
     from pfgpu.engine import ReactionEngine
     from pfgpu.girt import GirtAssembler, StructuredGrid
-    from test_gpu_girt import _check
+    from test_gpu_girt import _check, fd_noise
     nx, ny, nz = 8, 6, 5
     net, st = cases.prefactor_case(oracle, ncells=600, log_formulation=logf)
     st = st.subset(np.arange(nx * ny * nz))
@@ -78,9 +79,12 @@ def test_girt_with_prefactors_matches_oracle(oracle, logf):
     dt = 86400.0
     asm = GirtAssembler(ReactionEngine(net), StructuredGrid(**grid))
     dev = st.to("cuda")
-    r, v = asm.assemble(dev, torch.from_numpy(tk).cuda(), dt)
+    r, v = asm.assemble(dev, torch.from_numpy(tk).cuda(), dt, numerical_derivatives=numjac)
     torch.cuda.synchronize()
     ref_st = st.copy()
-    r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host)
-    _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt)
+    r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, dt, asm.rowptr_host, asm.colidx_host,
+                                        numerical_derivatives=numjac)
+    noise = fd_noise(oracle, net, st, grid, tk, dt, asm.rowptr_host, asm.colidx_host) if numjac else None
+    _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt,
+           noise=noise)
     np.testing.assert_allclose(dev.numpy().a["mnrl_rate"], ref_st.a["mnrl_rate"], rtol=1e-12, atol=1e-300)
