@@ -35,7 +35,7 @@ for _p in (REPO, PKG):
 METRIC = "cell chemistry solves/s at 1e-10 rel. tol vs plain GPU; adjoint/forward time ratio"
 UNIT = "cell-solves/s"
 MUTABLE = ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
-           "mnrl_rate", "status", "newton_its", "num_substeps", "total_sorb", "ionx_ref_sorbed")
+           "mnrl_rate", "status", "newton_its", "num_substeps", "total_sorb", "ionx_ref_sorbed", "ln_act_h2o")
 
 
 def log(*a):

@@ -166,6 +166,12 @@ typedef struct PfOptions {
   double max_relative_change_tolerance; /* 1e-6                                */
   double max_residual_tolerance;        /* 1e-12                               */
   double max_rel_residual_tolerance;    /* 1e-8                                */
+  int32_t use_activity_h2o;             /* reaction%use_activity_h2o (deck:
+                                           ACTIVITY_H2O): RActivityCoefficients
+                                           sets ln a_H2O = ln(1 - 0.017 (sum of
+                                           molalities)) (reaction.F90:4537-4547,
+                                           4604-4611), added with each reaction's
+                                           water coefficient to its ln Q/K.  0   */
 } PfOptions;
 
 /*
@@ -218,6 +224,9 @@ typedef struct PfNetworkDesc {
   PfOptions opts;
   const PfSorptionDesc* sorption;     /* NULL: no sorption                        */
   const PfPrefactorDesc* prefactors;  /* NULL: no mineral has rate prefactors     */
+  const double* sec_h2o_stoich;       /* [nsec] eqcplxh2ostoich (0: no water in the
+                                         reaction, eqcplxh2oid = 0), or NULL      */
+  const double* mnrl_h2o_stoich;      /* [nmnrl] kinmnrlh2ostoich, or NULL         */
 } PfNetworkDesc;
 
 /*
@@ -255,6 +264,9 @@ typedef struct PfCellState {
   double* ionx_ref_sorbed; /* [nionx] eqionx_ref_cation_sorbed_conc: the ion-
                               exchange Newton's warm start, carried between
                               calls as the reference carries it                */
+  double* ln_act_h2o;      /* [1] rt_auxvar%ln_act_h2o (in; out where activity
+                              coefficients are updated); NULL reads as 0.
+                              Required when use_activity_h2o                   */
 } PfCellState;
 
 typedef struct PfStepStats {

@@ -36,7 +36,9 @@ inline void gather(const Net& net, const PfCellState* s, int64_t i, Cell& c) {
   c.den_kg = s->den_kg[i];
   c.volume = s->volume[i];
   c.temp = s->temperature ? s->temperature[i] : 25.0;
-  c.ln_act_h2o = 0.0;
+  // rt_auxvar%ln_act_h2o: RTAuxVarInit's 0 unless the water activity option
+  // computes it
+  c.ln_act_h2o = (net.o.use_activity_h2o && s->ln_act_h2o) ? s->ln_act_h2o[i] : 0.0;
   c.ierror = 0;
   for (int k = 0; k < net.n; ++k) c.total_sorb[k] = s->total_sorb ? s->total_sorb[k * N + i] : 0.0;
   const int nionx = net.sorb ? net.sorb->nionx : 0;
@@ -64,6 +66,7 @@ inline void scatter(const Net& net, const PfCellState* s, int64_t i, const Cell&
     for (int k = 0; k < net.n; ++k) s->total_sorb[k * N + i] = c.total_sorb[k];
   if (s->ionx_ref_sorbed && net.sorb)
     for (int k = 0; k < net.sorb->nionx; ++k) s->ionx_ref_sorbed[k * N + i] = c.ionx_ref[k];
+  if (s->ln_act_h2o) s->ln_act_h2o[i] = c.ln_act_h2o;
 }
 
 // Rate prefactors: counts and ids in range; a primary prefactor species that

@@ -85,6 +85,9 @@ struct Net {
   // kinmnrl_num_prefactors, kinmnrl_prefactor_id(0,p,m) and the per-prefactor
   // and per-species arrays (dense [nm][MP] and [nm][MP][MS], 0-based)
   int npref(int m) const { return pref ? pref->num_prefactors[m] : 0; }
+  // eqcplxh2ostoich / kinmnrlh2ostoich (0: no water in the reaction)
+  double h2o_sec(int i) const { return d->sec_h2o_stoich ? d->sec_h2o_stoich[i] : 0.0; }
+  double h2o_mnrl(int m) const { return d->mnrl_h2o_stoich ? d->mnrl_h2o_stoich[m] : 0.0; }
   int pidx(int m, int p) const { return m * PF_MAX_PREFACTORS + p; }
   int psidx(int m, int p, int s) const { return (m * PF_MAX_PREFACTORS + p) * PF_MAX_PREFACTOR_SPECIES + s; }
 };
@@ -117,10 +120,22 @@ inline void set_logK(const Net& net, Cell& c) {
   }
 }
 
-// RActivityCoefficients, reaction.F90:4368-4614 (use_activity_h2o = false)
+// ln a_H2O from the molalities' sum, reaction.F90:4537-4547 and 4604-4611
+inline void water_activity(Cell& c, double sum_pri_molal, double sum_sec_molal) {
+  c.ln_act_h2o = 1.0 - 0.017 * (sum_pri_molal + sum_sec_molal);
+  if (c.ln_act_h2o > 0.0) c.ln_act_h2o = std::log(c.ln_act_h2o);
+  else c.ln_act_h2o = 0.0;
+}
+
+// RActivityCoefficients, reaction.F90:4368-4614 (no water primary species:
+// sum_pri_molal is over all primaries, :4394-4400)
 inline void activity_coefficients(const Net& net, Cell& c) {
   const PfNetworkDesc* d = net.d;
   const double A = d->debyeA, B = d->debyeB, Bdot = d->debyeBdot;
+  const bool h2o = net.o.use_activity_h2o != 0;
+  double sum_pri_molal = 0.0;
+  if (h2o)
+    for (int j = 0; j < net.n; ++j) sum_pri_molal = sum_pri_molal + c.pri_molal[j];
   if (net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON) {
     // reaction.F90:4403-4551
     double ln_conc[MAXN], ln_act[MAXN];
@@ -189,6 +204,7 @@ inline void activity_coefficients(const Net& net, Cell& c) {
           c.pri_act_coef[j] = 1.0;
         }
       }
+      double sum_sec_molal = 0.0;
       for (int i = 0; i < net.ns; ++i) {
         if (std::fabs(d->sec_Z[i]) > 0.0) {
           c.sec_act_coef[i] = std::exp((-d->sec_Z[i] * d->sec_Z[i] * sqrt_I * A /
@@ -197,10 +213,13 @@ inline void activity_coefficients(const Net& net, Cell& c) {
           c.sec_act_coef[i] = 1.0;
         }
         double lnQK = -c.sec_logK[i] * LOG_TO_LN;
+        if (net.h2o_sec(i) != 0.0) lnQK = lnQK + net.h2o_sec(i) * c.ln_act_h2o;
         int nsp = d->sec_nspec[i];
         for (int s = 0; s < nsp; ++s) lnQK = lnQK + net.sst(i, s) * ln_act[net.sid(i, s)];
         c.sec_molal[i] = std::exp(lnQK) / c.sec_act_coef[i];
+        sum_sec_molal = sum_sec_molal + c.sec_molal[i];
       }
+      if (h2o) water_activity(c, sum_pri_molal, sum_sec_molal);
     }
     return;
   }
@@ -218,6 +237,7 @@ inline void activity_coefficients(const Net& net, Cell& c) {
       c.pri_act_coef[j] = 1.0;
     }
   }
+  double sum_sec_molal = 0.0;
   for (int i = 0; i < net.ns; ++i) {
     if (std::fabs(d->sec_Z[i]) > 1.0e-10) {
       c.sec_act_coef[i] = std::exp((-d->sec_Z[i] * d->sec_Z[i] * sqrt_I * A /
@@ -225,7 +245,9 @@ inline void activity_coefficients(const Net& net, Cell& c) {
     } else {
       c.sec_act_coef[i] = 1.0;
     }
+    sum_sec_molal = sum_sec_molal + c.sec_molal[i];
   }
+  if (h2o) water_activity(c, sum_pri_molal, sum_sec_molal);
 }
 
 // RTotalAqueous, reaction.F90:4665-4759 (RTotal :4618 -> aqueous only).
@@ -244,6 +266,7 @@ inline void total_aqueous(const Net& net, Cell& c) {
     for (int j = 0; j < n; ++j) c.dtotal[i * MAXN + j] = (i == j) ? 1.0 : 0.0;
   for (int i = 0; i < net.ns; ++i) {
     double lnQK = -c.sec_logK[i] * LOG_TO_LN;
+    if (net.h2o_sec(i) != 0.0) lnQK = lnQK + net.h2o_sec(i) * c.ln_act_h2o;  // :4715-4717
     int nsp = d->sec_nspec[i];
     for (int s = 0; s < nsp; ++s) lnQK = lnQK + net.sst(i, s) * ln_act[net.sid(i, s)];
     c.sec_molal[i] = std::exp(lnQK) / c.sec_act_coef[i];
@@ -465,6 +488,7 @@ inline void kinetic_mineral(const Net& net, Cell& c, double* Res, double* J,
   for (int m = 0; m < net.nm; ++m) c.mnrl_rate[m] = 0.0;
   for (int m = 0; m < net.nm; ++m) {
     double lnQK = -c.mnrl_logK[m] * LOG_TO_LN;
+    if (net.h2o_mnrl(m) != 0.0) lnQK = lnQK + net.h2o_mnrl(m) * c.ln_act_h2o;  // reaction_mineral.F90:769-772
     int nsp = d->mnrl_nspec[m];
     for (int s = 0; s < nsp; ++s) lnQK = lnQK + net.mst(m, s) * ln_act[net.mid(m, s)];
     double QK = std::exp(lnQK);
@@ -614,6 +638,7 @@ inline void kinetic_mineral(const Net& net, Cell& c, double* Res, double* J,
           } else {
             const int icplx = -id - 1;
             double lnQK2 = -c.sec_logK[icplx] * LOG_TO_LN;
+            if (net.h2o_sec(icplx) != 0.0) lnQK2 = lnQK2 + net.h2o_sec(icplx) * c.ln_act_h2o;
             ncomp = d->sec_nspec[icplx];
             for (int i = 0; i < ncomp; ++i) lnQK2 = lnQK2 + net.sst(icplx, i) * ln_act[net.sid(icplx, i)];
             for (int j = 0; j < ncomp; ++j) {

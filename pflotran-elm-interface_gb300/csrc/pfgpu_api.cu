@@ -151,6 +151,7 @@ int validate_state(const PfNetwork* net, const PfCellState* s) {
   if (!net->dev.o.isothermal && !s->temperature) return PF_ERR_INVALID;
   if (net->dev.nkd + net->dev.nionx > 0 && !s->total_sorb) return PF_ERR_INVALID;
   if (net->dev.nionx > 0 && !s->ionx_ref_sorbed) return PF_ERR_INVALID;
+  if (net->dev.o.use_activity_h2o && !s->ln_act_h2o) return PF_ERR_INVALID;
   return PF_OK;
 }
 
@@ -426,10 +427,16 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   dev.o_pf_alpha = put(any_pref ? pfd->alpha : nullptr, nm * MPS, 0.0);
   dev.o_pf_beta = put(any_pref ? pfd->beta : nullptr, nm * MPS, 0.0);
   dev.o_pf_atten = put(any_pref ? pfd->atten_coef : nullptr, nm * MPS, 0.0);
+  dev.o_sec_h2o = put(d->sec_h2o_stoich, ns, 0.0);
+  dev.o_mnrl_h2o = put(d->mnrl_h2o_stoich, nm, 0.0);
+  bool any_h2o = false;
+  for (int i = 0; d->sec_h2o_stoich && i < ns; ++i) any_h2o = any_h2o || d->sec_h2o_stoich[i] != 0.0;
+  for (int m = 0; d->mnrl_h2o_stoich && m < nm; ++m) any_h2o = any_h2o || d->mnrl_h2o_stoich[m] != 0.0;
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
               (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |
-              (d->mnrl_affinity_power ? NETF_POWER : 0) | (any_pref ? NETF_PREFACTOR : 0);
+              (d->mnrl_affinity_power ? NETF_POWER : 0) | (any_pref ? NETF_PREFACTOR : 0) |
+              (any_h2o ? NETF_H2O : 0);
   dev.int_words = (int)ints.size();
   dev.dbl_words = (int)dbls.size();
   dev.A = d->debyeA;
@@ -788,6 +795,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
       {h->num_substeps, 1, i4, false, true},
       {(void*)h->cell_order, 1, (int)sizeof(int64_t), false, false},  // remapped per chunk below
       {h->total_sorb, n, d8, true, true},      {h->ionx_ref_sorbed, nx, d8, true, true},
+      {h->ln_act_h2o, 1, d8, true, true},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
   // chunks of about 2^18 cells (at most 16); of 1, 2 and 4 chunks at 10^6
@@ -896,6 +904,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     d.cell_order = (const int64_t*)dev_field(c, kord);
     d.total_sorb = (double*)dev_field(c, 18);
     d.ionx_ref_sorbed = (double*)dev_field(c, 19);
+    d.ln_act_h2o = (double*)dev_field(c, 20);
     cudaStream_t sc = net->s_comp;
     e = cudaStreamWaitEvent(sc, net->ev_in[c], 0);
     if (e == cudaSuccess && h->cell_order)

@@ -27,7 +27,12 @@ __device__ __forceinline__ double dh_lngamma(double z, double a0, double sqrtI, 
 __device__ void activity(const DevNet& net, const Tables& T, const PfCellState& st, const SoA& soa,
                          int64_t cell, double temp) {
   const int n = net.n, ns = net.ns;
+  const bool h2o = net.o.use_activity_h2o != 0;  // validate_state: st.ln_act_h2o is then present
+  double sum_pri_molal = 0.0;
+  if (h2o)
+    for (int j = 0; j < n; ++j) sum_pri_molal = sum_pri_molal + st.pri_molal[soa.at(j, cell)];
   if (net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON) {
+    double lnaw = cell_lnaw(net, st, cell);
     double ln_act[PF_MAX_NCOMP];
     for (int j = 0; j < n; ++j)
       ln_act[j] = log(st.pri_molal[soa.at(j, cell)]) + log(st.pri_act_coef[soa.at(j, cell)]);
@@ -86,14 +91,21 @@ __device__ void activity(const DevNet& net, const Tables& T, const PfCellState& 
         const double z = T.pri_Z(j);
         st.pri_act_coef[soa.at(j, cell)] = fabs(z) > 0.0 ? exp(dh_lngamma(z, T.pri_a0(j), sqrt_I, I, net)) : 1.0;
       }
+      double sum_sec_molal = 0.0;
       for (int i = 0; i < ns; ++i) {
         const double z = T.sec_Z(i);
         const double g = fabs(z) > 0.0 ? exp(dh_lngamma(z, T.sec_a0(i), sqrt_I, I, net)) : 1.0;
         st.sec_act_coef[soa.at(i, cell)] = g;
         const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-        double lnQK = -logK * LOG_TO_LN;
+        double lnQK = add_h2o(-logK * LOG_TO_LN, T.sec_h2o(i), lnaw);
         for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * ln_act[T.sec_idx(p)];
-        st.sec_molal[soa.at(i, cell)] = exp(lnQK) / g;
+        const double sm = exp(lnQK) / g;
+        st.sec_molal[soa.at(i, cell)] = sm;
+        sum_sec_molal = sum_sec_molal + sm;
+      }
+      if (h2o) {
+        lnaw = water_activity(sum_pri_molal, sum_sec_molal);
+        st.ln_act_h2o[cell] = lnaw;
       }
     }
     return;
@@ -107,10 +119,13 @@ __device__ void activity(const DevNet& net, const Tables& T, const PfCellState& 
     const double z = T.pri_Z(j);
     st.pri_act_coef[soa.at(j, cell)] = fabs(z) > 1.0e-10 ? exp(dh_lngamma(z, T.pri_a0(j), sqrt_I, I, net)) : 1.0;
   }
+  double sum_sec_molal = 0.0;
   for (int i = 0; i < ns; ++i) {
     const double z = T.sec_Z(i);
     st.sec_act_coef[soa.at(i, cell)] = fabs(z) > 1.0e-10 ? exp(dh_lngamma(z, T.sec_a0(i), sqrt_I, I, net)) : 1.0;
+    sum_sec_molal = sum_sec_molal + st.sec_molal[soa.at(i, cell)];
   }
+  if (h2o) st.ln_act_h2o[cell] = water_activity(sum_pri_molal, sum_sec_molal);
 }
 
 __device__ void total(const DevNet& net, const Tables& T, const PfCellState& st, const SoA& soa, int64_t cell,
@@ -124,9 +139,10 @@ __device__ void total(const DevNet& net, const Tables& T, const PfCellState& st,
     tot[j] = m;
   }
   const bool tsec = !net.o.isothermal && (net.flags & NETF_SEC_LOGKCOEF);
+  const double lnaw = cell_lnaw(net, st, cell);
   for (int i = 0; i < ns; ++i) {
     const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-    double lnQK = -logK * LOG_TO_LN;
+    double lnQK = add_h2o(-logK * LOG_TO_LN, T.sec_h2o(i), lnaw);
     for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
     const double s = exp(lnQK) / st.sec_act_coef[soa.at(i, cell)];
     st.sec_molal[soa.at(i, cell)] = s;

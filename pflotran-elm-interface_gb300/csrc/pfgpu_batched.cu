@@ -38,9 +38,11 @@ bool lane_supported(const DevNet& net) {
 #undef PF_CASE
       // rate prefactors add non-symmetric Jacobian terms the factorisation
       // here does not carry: the plain kernel runs those networks
+      // water activity moving each Newton iteration: the plain kernel
       return net.ns <= PF_MAX_NSEC && net.nm <= PF_MAX_NMNRL && !(net.flags & NETF_PREFACTOR) &&
              !(net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
-               net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON);
+               net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON) &&
+             !(net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER && net.o.use_activity_h2o);
     default:
       return false;
   }
@@ -50,8 +52,10 @@ bool lane_supported(const DevNet& net) {
 // lanes in step so the persistent kernel's refills are pure loads.
 //   scratch[i][cell]        TIMESTEP/OFF: exp(-logK_i(T) ln10) / gamma_i
 //                           NEWTON_ITER:  -logK_i(T) ln10
-//   scratch[ns+m][cell]     exp(-logK_m(T) ln10)  (NEWTON_ITER: the exponent)
+//   scratch[ns+m][cell]     exp(-logK_m(T) ln10)
 //   scratch[ns+nm+j][cell]  ln of the initial guess of component j
+// (the complexes' and minerals' entries with their reaction's water term,
+// coefficient times ln a_H2O, in the exponent)
 // logK(T) is ReactionInterpolateLogK (reaction_aux.F90:1285-1312) with ln T,
 // 1/T and 1/T^2 formed once per cell.
 __global__ void cell_setup_kernel(DevNet net, PfCellState st, double* __restrict__ scratch) {
@@ -66,13 +70,19 @@ __global__ void cell_setup_kernel(DevNet net, PfCellState st, double* __restrict
   const bool tsec = !net.o.isothermal && (net.flags & NETF_SEC_LOGKCOEF);
   const bool tmin = !net.o.isothermal && (net.flags & NETF_MNRL_LOGKCOEF);
   const int64_t N = st.ncells;
+  // ln a_H2O is constant over the step here (it follows the activity
+  // coefficients, which move each Newton iteration only in a mode these
+  // kernels refuse together with the water activity option)
+  const bool h2o = water_on(net);
+  const double lnaw = cell_lnaw(net, st, cell);
   for (int i = 0; i < ns; ++i) {
     double logK = T.sec_logK(i);
     if (tsec) {
       const double* c = T.sec_logKcoef(i);
       logK = c[0] * lt + c[1] + c[2] * tk + c[3] * it + c[4] * it2;
     }
-    const double x = -logK * LOG_TO_LN;
+    double x = -logK * LOG_TO_LN;
+    if (h2o) x = add_h2o(x, T.sec_h2o(i), lnaw);
     scratch[(size_t)i * N + cell] = ni ? x : exp(x) / st.sec_act_coef[soa.at(i, cell)];
   }
   for (int m = 0; m < nm; ++m) {
@@ -84,7 +94,9 @@ __global__ void cell_setup_kernel(DevNet net, PfCellState st, double* __restrict
     // K = 10^-logK in every mode: Q/K multiplies it by the activities'
     // powers (only the complexes' constants carry gamma and stay in log
     // form when gamma follows each Newton iteration)
-    scratch[(size_t)(ns + m) * N + cell] = exp(-logK * LOG_TO_LN);
+    double x = -logK * LOG_TO_LN;
+    if (h2o) x = add_h2o(x, T.mnrl_h2o(m), lnaw);
+    scratch[(size_t)(ns + m) * N + cell] = exp(x);
   }
   for (int j = 0; j < n; ++j) {
     double v = net.o.use_total_as_guess ? st.total[soa.at(j, cell)] : st.pri_molal[soa.at(j, cell)];

@@ -25,6 +25,7 @@ enum : int32_t {
   NETF_TEMKIN = 8,
   NETF_POWER = 16,
   NETF_PREFACTOR = 32,  // some mineral has rate prefactors
+  NETF_H2O = 64,        // some complex or mineral has water in its reaction
 };
 
 // Device view of a network.  All pointers index one packed allocation whose
@@ -87,12 +88,38 @@ struct DevNet {
   // rate, activation energy, alpha, beta, attenuation coefficient
   int32_t o_pf_cnt, o_pf_nsp, o_pf_id;
   int32_t o_pf_rate, o_pf_ea, o_pf_alpha, o_pf_beta, o_pf_atten;
+  // water coefficients of the complexes' and minerals' reactions (0: none)
+  int32_t o_sec_h2o, o_mnrl_h2o;
   double A, B, Bdot;
   PfOptions o;
   GroupTabs grp;
 };
 
 // Table accessor over either global or shared copies of the packed blocks.
+// Water activity in ln Q/K: some reaction has water and the option is on
+// (otherwise ln a_H2O stays at RTAuxVarInit's 0 in the reference)
+__host__ __device__ __forceinline__ bool water_on(const DevNet& net) {
+  return (net.flags & NETF_H2O) && net.o.use_activity_h2o;
+}
+// the cell's ln a_H2O (0 when the water activity is off or not carried)
+__device__ __forceinline__ double cell_lnaw(const DevNet& net, const PfCellState& st, int64_t cell) {
+  return (water_on(net) && st.ln_act_h2o) ? st.ln_act_h2o[cell] : 0.0;
+}
+
+// ln Q/K's water term: the reaction's water coefficient times ln a_H2O
+// (reaction.F90:4715-4717, reaction_mineral.F90:769-772), skipped for a
+// reaction without water as the reference skips it
+__device__ __forceinline__ double add_h2o(double lnQK, double coef, double ln_act_h2o) {
+  return coef != 0.0 ? lnQK + coef * ln_act_h2o : lnQK;
+}
+
+// ln a_H2O = ln(1 - 0.017 (sum of molalities)), 0 when the argument is not
+// positive (reaction.F90:4539-4547, 4604-4611)
+__device__ __forceinline__ double water_activity(double sum_pri_molal, double sum_sec_molal) {
+  const double a = 1.0 - 0.017 * (sum_pri_molal + sum_sec_molal);
+  return a > 0.0 ? log(a) : 0.0;
+}
+
 struct Tables {
   const int32_t* I;
   const double* D;
@@ -153,6 +180,8 @@ struct Tables {
   __device__ __forceinline__ int ix_min(int r) const { return I[net->o_ix_min + r]; }
   __device__ __forceinline__ int ix_zflag(int r) const { return I[net->o_ix_zflag + r]; }
   __device__ __forceinline__ int pf_cnt(int m) const { return I[net->o_pf_cnt + m]; }
+  __device__ __forceinline__ double sec_h2o(int i) const { return D[net->o_sec_h2o + i]; }
+  __device__ __forceinline__ double mnrl_h2o(int m) const { return D[net->o_mnrl_h2o + m]; }
   __device__ __forceinline__ int pf_nsp(int m, int p) const { return I[net->o_pf_nsp + m * PF_MAX_PREFACTORS + p]; }
   __device__ __forceinline__ double pf_rate(int m, int p) const {
     return D[net->o_pf_rate + m * PF_MAX_PREFACTORS + p];

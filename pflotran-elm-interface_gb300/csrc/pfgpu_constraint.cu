@@ -18,9 +18,10 @@
 namespace pfgpu {
 namespace constraint {
 
+// RActivityCoefficients (LAG), with ln a_H2O (lnaw) when use_activity_h2o
 template <int NM>
 __device__ void activity_lag(const DevNet& net, const Tables& T, const double* c, const PfCellState& st,
-                             const SoA& soa, int64_t cell, double* gam) {
+                             const SoA& soa, int64_t cell, double* gam, double& lnaw) {
   double I = 0.0;
   for (int j = 0; j < net.n; ++j) I = I + c[j] * T.pri_Z(j) * T.pri_Z(j);
   for (int i = 0; i < net.ns; ++i) I = I + st.sec_molal[soa.at(i, cell)] * T.sec_Z(i) * T.sec_Z(i);
@@ -32,12 +33,19 @@ __device__ void activity_lag(const DevNet& net, const Tables& T, const double* c
                  ? exp((-z * z * sI * net.A / (1.0 + T.pri_a0(j) * net.B * sI) + net.Bdot * I) * LOG_TO_LN)
                  : 1.0;
   }
+  double sum_sec_molal = 0.0;
   for (int i = 0; i < net.ns; ++i) {
     const double z = T.sec_Z(i);
     st.sec_act_coef[soa.at(i, cell)] =
         fabs(z) > 1.0e-10
             ? exp((-z * z * sI * net.A / (1.0 + T.sec_a0(i) * net.B * sI) + net.Bdot * I) * LOG_TO_LN)
             : 1.0;
+    sum_sec_molal = sum_sec_molal + st.sec_molal[soa.at(i, cell)];
+  }
+  if (net.o.use_activity_h2o) {
+    double sum_pri_molal = 0.0;
+    for (int j = 0; j < net.n; ++j) sum_pri_molal = sum_pri_molal + c[j];
+    lnaw = water_activity(sum_pri_molal, sum_sec_molal);
   }
 }
 
@@ -60,6 +68,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
   double c[NM], gam[NM], free_conc[NM], total_conc[NM], tot[NM], lnc[NM], lna[NM];
   double J[NM * NM], Res[NM], prev[NM], VV[NM];
   int indx[NM];
+  double lnaw = cell_lnaw(net, st, cell);
   for (int j = 0; j < n; ++j) {
     gam[j] = st.pri_act_coef[soa.at(j, cell)];
     free_conc[j] = use_prev ? st.pri_molal[soa.at(j, cell)] : 1.0e-9;
@@ -84,7 +93,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
     for (int j = 0; j < n; ++j)
       if (ctype[j] == 2 || ctype[j] == 5) c[j] = free_conc[j];
     if (net.o.act_coef_update_frequency != PF_ACT_COEF_OFF && act)
-      activity_lag<NM>(net, T, c, st, soa, cell, gam);
+      activity_lag<NM>(net, T, c, st, soa, cell, gam, lnaw);
     // RTotalAqueous
     for (int j = 0; j < n; ++j) {
       lnc[j] = log(c[j]);
@@ -94,7 +103,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
     }
     for (int i = 0; i < ns; ++i) {
       const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-      double lnQK = -logK * LOG_TO_LN;
+      double lnQK = add_h2o(-logK * LOG_TO_LN, T.sec_h2o(i), lnaw);
       for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
       const double g = st.sec_act_coef[soa.at(i, cell)];
       const double s = exp(lnQK) / g;
@@ -264,6 +273,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
     st.pri_act_coef[soa.at(j, cell)] = gam[j];
     st.total[soa.at(j, cell)] = tot[j];
   }
+  if (net.o.use_activity_h2o) st.ln_act_h2o[cell] = lnaw;
   if (iterations) iterations[cell] = result;
 }
 

@@ -163,7 +163,11 @@ __device__ __noinline__ void pref_jacobian(const DevNet& net, const Tables& T, c
         T, m, st.mnrl_rate[soa.at(m, X)] * volume, sum, pref, lnps, ln_act, ln_sec_act,
         [&](int j) { return st.pri_act_coef[soa.at(j, X)]; }, [&](int i) { return st.sec_act_coef[soa.at(i, X)]; },
         [&](int j) { return log(P[j * bd]); },
-        [&](int i) { return tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i); }, temp,
+        [&](int i) {
+          return add_h2o(-(tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i)) * LOG_TO_LN, T.sec_h2o(i),
+                         cell_lnaw(net, st, X));
+        },
+        temp,
         [&](int r, int c, double v) { D[c * n + r] = fma(v, logf ? P[c * bd] : 1.0, D[c * n + r]); });
   }
 }
@@ -182,6 +186,7 @@ __device__ void mineral_residual(const DevNet& net, const Tables& T, const PfCel
     const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
     const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
     double lnQK = -logK * LOG_TO_LN;
+    if (water_on(net)) lnQK = add_h2o(lnQK, T.mnrl_h2o(m), cell_lnaw(net, st, X));
     for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * lna[T.mnrl_idx(p)];
     const double QK = exp(lnQK);
     double aff;
@@ -239,6 +244,7 @@ __device__ __noinline__ void numerical_reaction_jacobian(const DevNet& net, cons
     for (int i = 0; i < n; ++i) res1[i] = 0.0;
     auto ln_sec_act = [&](int i) {  // RTotal of the perturbed copy, complex i
       double lnQK = -(tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i)) * LOG_TO_LN;
+      if (water_on(net)) lnQK = add_h2o(lnQK, T.sec_h2o(i), cell_lnaw(net, st, X));
       for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
       const double g = st.sec_act_coef[soa.at(i, X)];
       return log(exp(lnQK) / g) + log(g);
@@ -278,6 +284,8 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   constexpr bool has_pf = HAS_PF;  // rate prefactors: a separate instantiation
   unsigned pf_active = 0;  // minerals whose prefactor derivative is due
   const double temp = st.temperature ? st.temperature[X] : 25.0;
+  const bool has_h2o = water_on(net);
+  const double lnaw = cell_lnaw(net, st, X);
   const double den_k = st.den_kg[X], den_L = den_k * 1.0e-3;
   const double por = st.porosity[X], sat = st.saturation[X], volume = st.volume[X];
   const bool dry = sat < RT_MIN_SATURATION;
@@ -292,6 +300,7 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   for (int i = 0; i < ns; ++i) {
     const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
     double lnQK = -logK * LOG_TO_LN;
+    if (has_h2o) lnQK = add_h2o(lnQK, T.sec_h2o(i), lnaw);
     const int b = T.sec_begin(i), e = T.sec_end(i);
     for (int p = b; p < e; ++p) lnQK = lnQK + T.sec_nu(p) * P[o_lna + T.sec_idx(p) * bd];
     const double sv = exp(lnQK) / st.sec_act_coef[soa.at(i, X)];
@@ -317,6 +326,7 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
     if (!dry) {
       const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
       double lnQK = -logK * LOG_TO_LN;
+      if (has_h2o) lnQK = add_h2o(lnQK, T.mnrl_h2o(m), lnaw);
       for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * P[o_lna + T.mnrl_idx(p) * bd];
       QK = exp(lnQK);
       double aff;

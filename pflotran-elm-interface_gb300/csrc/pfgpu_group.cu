@@ -65,6 +65,8 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
   if (net.ns > PF_MAX_NSEC || net.nm > PF_MAX_NMNRL) return false;
   if (net.nkd + net.nionx > 0) return false;  // sorption: one lane per cell
   if (net.flags & NETF_PREFACTOR) return false;  // rate prefactors: the plain kernel
+  if (net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER && net.o.use_activity_h2o)
+    return false;  // water activity moving each Newton iteration: the plain kernel
   const int R = (net.n + lanes_per_cell - 1) / lanes_per_cell;
   return group_rows_ok(lanes_per_cell, R);
 }

@@ -31,9 +31,10 @@ struct Work {
 
 struct CellScalars {
   double porosity, sat, den_kg, volume, temp;
+  double lnaw;  // ln a_H2O (rt_auxvar%ln_act_h2o)
 };
 
-template <int NMAX>
+template <int NMAX, bool EXT>
 __device__ void total_aqueous(const Tables& T, int n, int ns, const double* sec_logK,
                               const double* sec_gamma, double* sec_molal_out, int64_t cell,
                               const SoA& soa, const CellScalars& cs, Work<NMAX>& w) {
@@ -48,6 +49,7 @@ __device__ void total_aqueous(const Tables& T, int n, int ns, const double* sec_
   for (int i = 0; i < ns; ++i) {
     const int b = T.sec_begin(i), e = T.sec_end(i);
     double lnQK = -sec_logK[i] * LOG_TO_LN;
+    if (EXT && water_on(*T.net)) lnQK = add_h2o(lnQK, T.sec_h2o(i), cs.lnaw);
     for (int p = b; p < e; ++p) lnQK = lnQK + T.sec_nu(p) * w.lna[T.sec_idx(p)];
     const double g = sec_gamma[soa.at(i, cell)];
     const double s = exp(lnQK) / g;
@@ -72,8 +74,8 @@ __device__ void total_aqueous(const Tables& T, int n, int ns, const double* sec_
 
 // RKineticMineral.  Jac may be null (derivative = false).  sec_logK: the
 // complexes' logK at the cell's temperature (prefactor derivative).  PF:
-// the network has rate prefactors (a separate instantiation, so that the
-// common one keeps its registers).
+// the extended instantiation (rate prefactors, water activity), separate so
+// that the common one keeps its registers.
 template <int NMAX, bool PF>
 __device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const double* mnrl_logK,
                                 const double* sec_logK, int64_t cell, const SoA& soa, const PfCellState& st,
@@ -88,6 +90,7 @@ __device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const
   for (int m = 0; m < net.nm; ++m) {
     const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
     double lnQK = -mnrl_logK[m] * LOG_TO_LN;
+    if (PF && water_on(net)) lnQK = add_h2o(lnQK, T.mnrl_h2o(m), cs.lnaw);
     for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * w.lna[T.mnrl_idx(p)];
     double QK = exp(lnQK);
     double aff;
@@ -156,7 +159,7 @@ __device__ void kinetic_mineral(const Tables& T, const DevNet& net, int n, const
       prefactor_derivative(
           T, m, Im, k, prefactor, lnps, ln_act, ln_sec_act, [&](int j) { return w.gamma[j]; },
           [&](int i) { return st.sec_act_coef[soa.at(i, cell)]; }, [&](int j) { return w.lnc[j]; },
-          [&](int i) { return sec_logK[i]; }, cs.temp,
+          [&](int i) { return add_h2o(-sec_logK[i] * LOG_TO_LN, T.sec_h2o(i), cs.lnaw); }, cs.temp,
           [&](int r, int c, double v) { Jac[r * NMAX + c] = Jac[r * NMAX + c] + v; });
   }
 }
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
   const PfOptions& o = net.o;
   Work<NMAX> w;
   CellScalars cs{st.porosity[cell], st.saturation[cell], st.den_kg[cell], st.volume[cell],
-                 st.temperature ? st.temperature[cell] : 25.0};
+                 st.temperature ? st.temperature[cell] : 25.0, PF ? cell_lnaw(net, st, cell) : 0.0};
   // per-cell logK (RUpdateTempDependentCoefs mutates the shared arrays; kept per thread here)
   double sec_logK[PF_MAX_NSEC], mnrl_logK[PF_MAX_NMNRL];
   const bool iso = o.isothermal != 0;
@@ -324,15 +327,22 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
                            ? exp((-z * z * sI * net.A / (1.0 + T.pri_a0(j) * net.B * sI) + net.Bdot * I) * LOG_TO_LN)
                            : 1.0;
         }
+        double sum_sec_molal = 0.0;
         for (int i = 0; i < ns; ++i) {
           const double z = T.sec_Z(i);
           st.sec_act_coef[soa.at(i, cell)] =
               fabs(z) > 1.0e-10
                   ? exp((-z * z * sI * net.A / (1.0 + T.sec_a0(i) * net.B * sI) + net.Bdot * I) * LOG_TO_LN)
                   : 1.0;
+          sum_sec_molal = sum_sec_molal + st.sec_molal[soa.at(i, cell)];
+        }
+        if (PF && o.use_activity_h2o) {  // reaction.F90:4604-4611
+          double sum_pri_molal = 0.0;
+          for (int j = 0; j < n; ++j) sum_pri_molal = sum_pri_molal + w.c[j];
+          cs.lnaw = water_activity(sum_pri_molal, sum_sec_molal);
         }
       }
-      total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
+      total_aqueous<NMAX, PF>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
       for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
       // RTotalSorb; a failed ion-exchange solve fails RReact, no restore (:3861-3865)
       if (has_sorb && !sorb_eval()) {
@@ -405,7 +415,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
     }
     if (ierror == 0) {
       // final RTAuxVarCompute (reaction.F90:4052)
-      total_aqueous<NMAX>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
+      total_aqueous<NMAX, PF>(T, n, ns, sec_logK, st.sec_act_coef, st.sec_molal, cell, soa, cs, w);
       for (int j = 0; j < n; ++j) total_io[j] = w.total[j];
       if (has_sorb) sorb_eval();
     }
@@ -448,6 +458,8 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
     st.pri_molal[soa.at(j, cell)] = w.c[j];
     if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) st.pri_act_coef[soa.at(j, cell)] = w.gamma[j];
   }
+  if (PF && o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER && o.use_activity_h2o)
+    st.ln_act_h2o[cell] = cs.lnaw;
   const int status = ierror_step ? PF_CELL_TOO_MANY_CUTS : PF_CELL_OK;
   if (st.status) st.status[cell] = status;
   if (st.newton_its) st.newton_its[cell] = its_total;
@@ -467,7 +479,8 @@ int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
   const int tpb = 128;
   const int64_t blocks = (st.ncells + tpb - 1) / tpb;
   if (blocks == 0) return 0;
-  if (net.flags & NETF_PREFACTOR) {  // rate prefactors: three size buckets
+  if ((net.flags & NETF_PREFACTOR) || net.o.use_activity_h2o) {
+    // rate prefactors or water activity: the extended instantiation, three size buckets
     if (net.n <= 8) plain::rstep_plain_kernel<8, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
     else if (net.n <= 12) plain::rstep_plain_kernel<12, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
     else plain::rstep_plain_kernel<24, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);

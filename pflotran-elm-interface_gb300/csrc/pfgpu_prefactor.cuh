@@ -54,13 +54,14 @@ __device__ double prefactor_rate(const Tables& T, int m, LnAct ln_act, LnSecAct 
 // The prefactor part of the mineral's Jacobian: add(row, col, v) adds v to
 // J(row, col).  Im: the rate times the cell volume (mol/s); sum_rate,
 // prefactor, lnps: from prefactor_rate.  pri_gam(j), sec_gam(i): activity
-// coefficients; ln_conc(j) = ln m_j; sec_logK(i): logK of complex i at the
-// cell's temperature.
-template <class LnAct, class LnSecAct, class PriGam, class SecGam, class LnConc, class SecLogK, class Add>
+// coefficients; ln_conc(j) = ln m_j; sec_lnK(i): the constant part of
+// complex i's ln Q/K, -logK ln10 at the cell's temperature plus its water
+// term (:1048-1053).
+template <class LnAct, class LnSecAct, class PriGam, class SecGam, class LnConc, class SecLnK, class Add>
 __device__ void prefactor_derivative(const Tables& T, int m, double Im, double sum_rate, const double* prefactor,
                                      const double (*lnps)[PF_MAX_PREFACTOR_SPECIES], LnAct ln_act,
                                      LnSecAct ln_sec_act, PriGam pri_gam, SecGam sec_gam, LnConc ln_conc,
-                                     SecLogK sec_logK, double temp, Add add) {
+                                     SecLnK sec_lnK, double temp, Add add) {
   const double dIm_dsum_prefactor_rate = Im / sum_rate;
   const int mb = T.mnrl_begin(m);
   int ncomp = T.mnrl_end(m) - mb;  // the count the primary species below walk
@@ -93,7 +94,7 @@ __device__ void prefactor_derivative(const Tables& T, int m, double Im, double s
         for (int i = 0; i < ncomp; ++i) add(T.mnrl_idx(mb + i), id, T.mnrl_nu(mb + i) * dIm_dspec);
       } else {
         const int icplx = -id - 1, cb = T.sec_begin(icplx);
-        double lnQK = -sec_logK(icplx) * LOG_TO_LN;
+        double lnQK = sec_lnK(icplx);
         ncomp = T.sec_end(icplx) - cb;
         for (int i = 0; i < ncomp; ++i) lnQK = lnQK + T.sec_nu(cb + i) * ln_act(T.sec_idx(cb + i));
         for (int j = 0; j < ncomp; ++j) {

@@ -69,6 +69,7 @@ class PfOptions(C.Structure):
         ("max_relative_change_tolerance", C.c_double),
         ("max_residual_tolerance", C.c_double),
         ("max_rel_residual_tolerance", C.c_double),
+        ("use_activity_h2o", C.c_int32),
     ]
 
 
@@ -111,6 +112,7 @@ class PfNetworkDesc(C.Structure):
         ("opts", PfOptions),
         ("sorption", C.POINTER(PfSorptionDesc)),
         ("prefactors", C.POINTER(PfPrefactorDesc)),
+        ("sec_h2o_stoich", _dp), ("mnrl_h2o_stoich", _dp),
     ]
 
 
@@ -124,7 +126,7 @@ class PfCellState(C.Structure):
         ("volume", _dp), ("temperature", _dp), ("dt_cell", _dp),
         ("status", _ip), ("newton_its", _ip), ("num_substeps", _ip),
         ("cell_order", C.POINTER(C.c_int64)),
-        ("total_sorb", _dp), ("ionx_ref_sorbed", _dp),
+        ("total_sorb", _dp), ("ionx_ref_sorbed", _dp), ("ln_act_h2o", _dp),
     ]
 
 

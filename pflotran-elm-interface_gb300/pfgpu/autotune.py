@@ -18,7 +18,7 @@ from .network import CellState
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "autotune_cache.json")
 MUTABLE = ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
-           "mnrl_rate", "status", "newton_its", "num_substeps", "total_sorb", "ionx_ref_sorbed")
+           "mnrl_rate", "status", "newton_its", "num_substeps", "total_sorb", "ionx_ref_sorbed", "ln_act_h2o")
 
 
 def network_key(eng) -> str:

@@ -15,8 +15,10 @@ complexes and later sections are not read.
 
 Basis set-up (the subset of BasisInit, reaction_database.F90:812-4040, that
 this engine needs): the primary species must be basis species of the
-database (no basis swapping); water drops out of every reaction (its
-activity is one: ln a_H2O = 0 in ln Q); logK at the reference temperature
+database (no basis swapping); water leaves the species list of every
+reaction and its coefficient is kept apart (eqcplxh2ostoich,
+kinmnrlh2ostoich), entering ln Q times ln a_H2O, which is 0 unless the
+ACTIVITY_H2O option (use_activity_h2o) computes it; logK at the reference temperature
 follows ReactionInitializeLogK (reaction_aux.F90:1236-1281: the database
 column when the run is isothermal at a database temperature, else the fit);
 the five-term temperature fit follows ReactionFitLogKCoef
@@ -217,6 +219,8 @@ def _reference_logK(db: Database, rxn: Reaction, coefs, t_ref: float, isothermal
 
 
 def _drop_water(stoich, primary):
+    """The reaction's primary-species coefficients; water is left out (see
+    _water)."""
     out = {}
     for sp, nu in stoich:
         if sp == "H2O":
@@ -225,6 +229,11 @@ def _drop_water(stoich, primary):
             raise KeyError("species %s is not a primary species of this network (no basis swapping)" % sp)
         out[sp] = out.get(sp, 0.0) + nu
     return out
+
+
+def _water(stoich):
+    """The reaction's water coefficient (eqcplxh2ostoich / kinmnrlh2ostoich)."""
+    return sum(nu for sp, nu in stoich if sp == "H2O")
 
 
 def build_network(db: Database, primary, secondary=None, minerals=None, options=None,
@@ -250,14 +259,14 @@ def build_network(db: Database, primary, secondary=None, minerals=None, options=
     for name in secondary:
         r = db.secondary[name]
         coefs = fit_logK_coefs(db.temperatures, r.logK)
-        secs.append(dict(name=name, stoich=_drop_water(r.stoich, pset),
+        secs.append(dict(name=name, stoich=_drop_water(r.stoich, pset), h2o=_water(r.stoich),
                          logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
                          logKcoef=coefs, Z=r.Z, a0=r.a0))
     mins = []
     for name, par in (minerals or {}).items():
         r = db.minerals[name]
         coefs = fit_logK_coefs(db.temperatures, r.logK)
-        m = dict(name=name, stoich=_drop_water(r.stoich, pset),
+        m = dict(name=name, stoich=_drop_water(r.stoich, pset), h2o=_water(r.stoich),
                  logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
                  logKcoef=coefs, molar_vol=r.molar_vol_cm3 * 1.0e-6)
         m.update(par)

@@ -38,6 +38,7 @@ def default_options(**kw) -> dict:
         max_relative_change_tolerance=1e-6,
         max_residual_tolerance=1e-12,
         max_rel_residual_tolerance=1e-8,
+        use_activity_h2o=0,
     )
     o.update(kw)
     return o
@@ -92,6 +93,9 @@ class ReactionNetwork:
     mnrl_min_scale_factor: np.ndarray = None
     mnrl_Temkin_const: np.ndarray = None
     mnrl_affinity_power: np.ndarray = None
+    # water in the reactions (eqcplxh2ostoich, kinmnrlh2ostoich; None: none)
+    sec_h2o_stoich: np.ndarray = None
+    mnrl_h2o_stoich: np.ndarray = None
     debyeA: float = 0.5114
     debyeB: float = 0.3288
     debyeBdot: float = 0.0410
@@ -171,6 +175,8 @@ class ReactionNetwork:
         net.sec_logK = np.array([r["logK"] for r in secondaries], np.float64)
         net.sec_Z = np.array([r["Z"] for r in secondaries], np.float64)
         net.sec_a0 = np.array([r["a0"] for r in secondaries], np.float64)
+        if any(r.get("h2o", 0.0) for r in secondaries):
+            net.sec_h2o_stoich = np.array([r.get("h2o", 0.0) for r in secondaries], np.float64)
         if secondaries and all("logKcoef" in r for r in secondaries):
             net.sec_logKcoef = np.array([r["logKcoef"] for r in secondaries], np.float64)
         mins = list(minerals)
@@ -186,6 +192,8 @@ class ReactionNetwork:
                                                np.float64)
         net.mnrl_rate_limiter = np.array([r.get("rate_limiter", 0.0) for r in mins], np.float64)
         net.mnrl_irreversible = np.array([r.get("irreversible", 0) for r in mins], np.int32)
+        if any(r.get("h2o", 0.0) for r in mins):
+            net.mnrl_h2o_stoich = np.array([r.get("h2o", 0.0) for r in mins], np.float64)
         if mins and all("logKcoef" in r for r in mins):
             net.mnrl_logKcoef = np.array([r["logKcoef"] for r in mins], np.float64)
         for key in ("min_scale_factor", "Temkin_const", "affinity_power"):
@@ -250,6 +258,8 @@ class ReactionNetwork:
         d.mnrl_Temkin_const = _ptr(arr(self.mnrl_Temkin_const, f64), C.c_double)
         d.mnrl_affinity_power = _ptr(arr(self.mnrl_affinity_power, f64), C.c_double)
         d.debyeA, d.debyeB, d.debyeBdot = self.debyeA, self.debyeB, self.debyeBdot
+        d.sec_h2o_stoich = _ptr(arr(self.sec_h2o_stoich, f64), C.c_double)
+        d.mnrl_h2o_stoich = _ptr(arr(self.mnrl_h2o_stoich, f64), C.c_double)
         d.opts = self.options_struct()
         if self.has_sorption:
             self._sorb = self._sorption_desc(arr)
@@ -358,9 +368,12 @@ STATE_FIELDS = {
     "status": (1, np.int32), "newton_its": (1, np.int32), "num_substeps": (1, np.int32),
     # networks with sorption only
     "total_sorb": ("n", np.float64), "ionx_ref_sorbed": ("x", np.float64),
+    # networks with the water activity option only
+    "ln_act_h2o": (1, np.float64),
 }
 OPTIONAL_FIELDS = ("dt_cell",)
 SORPTION_FIELDS = ("total_sorb", "ionx_ref_sorbed")
+H2O_FIELDS = ("ln_act_h2o",)
 
 
 def _rows(net, r):
@@ -383,6 +396,8 @@ class CellState:
             if k in OPTIONAL_FIELDS and not with_dt:
                 continue
             if k in SORPTION_FIELDS and not net.has_sorption:
+                continue
+            if k in H2O_FIELDS and not net.options.get("use_activity_h2o"):
                 continue
             rows = _rows(net, r)
             a[k] = np.zeros((rows, ncells), dt) if r != 1 else np.zeros(ncells, dt)

@@ -183,3 +183,28 @@ def prefactor_case(oracle, ncells=600, log_formulation=True, with_secondary=True
     prefactor_network(net, with_secondary)
     st.net = net
     return net, st
+
+
+def water_case(oracle, ncells=600, **opts):
+    """The 8-component random network (24 complexes, 4 minerals) with water
+    in a third of the complexes' and in two minerals' reactions and the
+    ACTIVITY_H2O option on; cells from the constraint equilibrator, each
+    mineral's logK at the cells' median log Q (log Q with the water term)."""
+    o = default_options(isothermal=0, use_activity_h2o=1)
+    o.update(opts)
+    net = generate.random_network(8, 24, 4, seed=818, options=o)
+    rng = np.random.default_rng(8188)
+    net.sec_h2o_stoich = np.where(rng.uniform(size=net.nsec) < 0.35, rng.choice([-2.0, -1.0, 1.0, 3.0], net.nsec), 0.0)
+    net.mnrl_h2o_stoich = np.array([1.0, 0.0, -2.0, 0.0])[:net.nmnrl]
+    st, ct, cc = generate.random_cells(net, ncells, seed=8181)
+    assert "ln_act_h2o" in st.a
+    st, _ = prepare(oracle, net, st, ct, cc)
+    la = np.log10(st.a["pri_molal"] * st.a["pri_act_coef"])
+    for m in range(net.nmnrl):
+        lq = sum(net.mnrl_stoich[m, k] * la[net.mnrl_spec[m, k]] for k in range(net.mnrl_nspec[m]))
+        lq = lq + net.mnrl_h2o_stoich[m] * st.a["ln_act_h2o"] / np.log(10.0)
+        delta = float(np.median(lq)) - net.mnrl_logK[m]
+        net.mnrl_logK[m] += delta
+        if net.mnrl_logKcoef is not None:
+            net.mnrl_logKcoef[m, 1] += delta
+    return net, st
