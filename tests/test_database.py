@@ -108,6 +108,9 @@ def test_build_network_basis_water_and_selection():
     oh = net.secondary.index("OH-")
     assert net.sec_nspec[oh] == 1 and net.primary[net.sec_spec[oh, 0]] == "H+"
     assert net.sec_stoich[oh, 0] == -1.0
+    # water leaves the species list and is kept as the reaction's water
+    # coefficient (eqcplxh2ostoich): OH- = H2O - H+, the others have none
+    np.testing.assert_array_equal(net.sec_h2o_stoich, [1.0, 0.0, 0.0])
     # isothermal at a database temperature: the database column
     assert net.sec_logK[2] == db.secondary["CaHCO3+"].logK[1]
     assert net.mnrl_molar_vol[0] == pytest.approx(36.934e-6)
