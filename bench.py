@@ -14,8 +14,9 @@ cuts, kinetic-state update).  value = cells x steps / time.
   e2e          pf_rstep_host: host buffers, H2D + step + D2H inside the call
   plain_gpu    the plain one-thread-per-cell form on the same inputs
   cpu_baseline the CPU restatement of the reference (oracle) on the host cores
---impl reference times that CPU restatement alone (the reference itself is
-Fortran on PETSc and cannot be built here).
+--impl reference times that CPU restatement alone, on inputs it prepares
+itself on the host (the reference itself is Fortran on PETSc and cannot be
+built here).
 """
 from __future__ import annotations
 
@@ -632,21 +633,52 @@ def transport_measure(net, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, r
             "hbm_frac": gbs / peak if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
 
 
+def build_state_host(cfg_name, pool, nsample, seed=2026, nthreads=1):
+    """The first nsample cells of build_state(cfg_name, pool, ...), prepared on
+    the host by the oracle alone (constraint equilibration, initial auxvars,
+    TIMESTEP activity update), so that no library kernel touches the
+    reference arm's inputs and the arm runs without a GPU."""
+    import numpy as np
+    from pfgpu import generate
+    from pfgpu.network import default_options
+    from oracle.oracle import Oracle
+    o = Oracle()
+    if cfg_name == "c1":
+        net = generate.calcite_network()
+        st, ct, cc = generate.calcite_cells(net, pool + pool // 20 + 64, seed=20261203)
+    else:
+        net = generate.random_network(12, 40, 6, seed=12, options=default_options(isothermal=0))
+        st, ct, cc = generate.random_cells(net, pool + pool // 20 + 64, seed=seed)
+    # the same cells as the device build: equilibrate a prefix a little longer
+    # than the sample and keep its first nsample successes, in order
+    m = min(st.ncells, nsample + nsample // 10 + 64)
+    st = st.subset(np.arange(m))
+    _, its = o.equilibrate(net, st, ct, np.ascontiguousarray(cc[:, :m]), nthreads=nthreads)
+    good = np.nonzero(its > 0)[0][:nsample]
+    if good.size < nsample:
+        raise RuntimeError("only %d of %d cells equilibrated" % (good.size, nsample))
+    st = st.subset(good)
+    st.a["pri_act_coef"][:] = 1.0
+    st.a["sec_act_coef"][:] = 1.0
+    st.a["sec_molal"][:] = 0.0
+    for act in (False, True, True, False):
+        o.update_auxvars(net, st, act, nthreads=nthreads)
+    o.update_activity_coefs(net, st, nthreads=nthreads)
+    return net, st, o
+
+
 def run_reference(args):
     import numpy as np  # noqa: F401
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import torch
     cfg = workload(args.config)
-    # inputs: the same generator and device equilibration as our arm when a GPU
-    # is present; the CPU restatement is then timed on the host cores
-    net, eng, dev = build_state(args.config, min(cfg["cells"], 200_000), "cuda")
-    host = dev.numpy()
-    from oracle.oracle import Oracle
-    o = Oracle()
     cores = os.cpu_count() or 1
-    n = min(host.ncells, 20000 if args.config != "c1" else 1000)
+    n = min(cfg["cells"], 20000 if args.config != "c1" else 1000)
+    # inputs: the same generator and cells as our arm, equilibrated by the
+    # CPU restatement itself; that restatement is then timed on the host cores
+    net, host, o = build_state_host("c2" if args.config == "c5" else args.config,
+                                    min(cfg["cells"], 200_000), n, nthreads=cores)
     vals = []
     for k in range(args.warmup + args.steps):
         sub = host.subset(range(n))
@@ -667,7 +699,6 @@ def run_reference(args):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is Fortran+PETSc (no Fortran compiler here); timed its C++ restatement"}
     print(json.dumps(line), flush=True)
-    del torch
 
 
 def main():

@@ -1,0 +1,41 @@
+"""bench.py's reference arm on the host alone: the oracle prepares its own
+inputs (constraint equilibration, initial auxvars) and times its RStep, so
+the arm needs no GPU and runs no library kernel."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("config", ["c1"])
+def test_reference_arm_line(config):
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    out = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference",
+                          "--config", config, "--steps", "1", "--warmup", "3"],
+                         capture_output=True, text=True, timeout=600, env=env, cwd=REPO)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["cells_per_step_sample"] == 1000
+
+
+def test_host_inputs_step_cleanly():
+    """The host-built reference-arm cells are the first successes of the
+    seeded draw, with positive molalities, and every one of them steps."""
+    import numpy as np
+    sys.path.insert(0, REPO)
+    import bench
+    net, st, o = bench.build_state_host("c1", 1000, 200)
+    assert st.ncells == 200
+    assert np.all(st.a["pri_molal"] > 0) and np.all(np.isfinite(st.a["sec_act_coef"]))
+    o.rstep(net, st, 3600.0)
+    assert np.all(st.a["status"] == 0) and np.all(st.a["newton_its"] > 0)
