@@ -58,6 +58,7 @@ class Reaction:
     a0: float = 0.0
     Z: float = 0.0
     molar_vol_cm3: float = 0.0
+    molar_weight: float = 0.0   # g/mol (gases and minerals)
 
 
 @dataclass
@@ -112,11 +113,63 @@ def read_database(source: str) -> Database:
             k = int(_num(toks[i + 2]))
             st, i = pairs(i + 3, k)
             logK = [_num(t) for t in toks[i:i + nt]]
+            mw = _num(toks[i + nt]) if i + nt < len(toks) else 0.0
             i += nt + 1
             if name == "null":
                 break
-            table[name] = Reaction(st, logK, molar_vol_cm3=vm)
+            table[name] = Reaction(st, logK, molar_vol_cm3=vm, molar_weight=mw)
     return db
+
+
+# unit factors to m, m^3 and kg
+_AREA_LEN = {"m": 1.0, "dm": 1.0e-1, "cm": 1.0e-2, "mm": 1.0e-3}
+_BULK_VOL = {"m^3": 1.0, "dm^3": 1.0e-3, "L": 1.0e-3, "cm^3": 1.0e-6, "mm^3": 1.0e-9}
+_MASS = {"kg": 1.0, "g": 1.0e-3, "mg": 1.0e-6}
+
+
+def mineral_surface_area(value, units: str, mineral: Reaction, volfrac, name: str = "mineral"):
+    """Specific surface area of a kinetic mineral given in a constraint, in
+    the engine's units (m^2 mineral per m^3 bulk, PfCellState.mnrl_area),
+    following MineralProcessConstraint (reaction_mineral.F90:590-640).
+
+    units is "<area>/<bulk volume>" (e.g. "cm^2/cm^3", "m^2/m^3") or, when it
+    ends in "g", "<area>/<mass of mineral>" (e.g. "cm^2/g", "m^2/kg"): the
+    mass-based area becomes m^2 mineral / m^3 mineral through the molar
+    weight (g/mol) and molar volume of the database, then m^2 / m^3 bulk
+    through the mineral's volume fraction.  value and volfrac may be arrays
+    (a per-cell dataset).  The reference's errors are raised as ValueError: a
+    molar weight or volume that is zero or the database's 500 marker, or a
+    zero volume fraction, with a mass-based area."""
+    num, _, den = units.replace(" ", "").partition("/")
+    if not num.endswith("^2") or num[:-2] not in _AREA_LEN or not den:
+        raise ValueError("%s: unsupported specific surface area units %r" % (name, units))
+    area = _AREA_LEN[num[:-2]] ** 2
+    per_unit_mass = den.endswith("g")
+    if per_unit_mass:
+        if den not in _MASS:
+            raise ValueError("%s: unsupported specific surface area units %r" % (name, units))
+        conv = area / _MASS[den]  # m^2 / kg mineral
+        mw, vm = mineral.molar_weight, mineral.molar_vol_cm3 * 1.0e-6
+        eps = 1.0e-40
+        if mw < eps or mw == MISSING_LOGK:
+            raise ValueError("Zero or undefined molar weight for mineral %r prevents specifying its "
+                             "specific surface area per mass" % name)
+        if vm < eps or mineral.molar_vol_cm3 == MISSING_LOGK:
+            raise ValueError("Zero or undefined molar volume for mineral %r prevents specifying its "
+                             "specific surface area per mass" % name)
+        # m^2/kg * 1e-3 kg/g * g/mol / (m^3/mol) = m^2 mineral / m^3 mineral
+        conv = conv * 1.0e-3 * mw / vm
+        vf = np.asarray(volfrac, np.float64)
+        out = conv * vf
+        if np.any(out < 1.0e-40):
+            raise ValueError("The zero volume fraction assigned to mineral %r prevents the use of a "
+                             "mass-based surface area" % name)
+        out = out * np.asarray(value, np.float64)
+    else:
+        if den not in _BULK_VOL:
+            raise ValueError("%s: unsupported specific surface area units %r" % (name, units))
+        out = area / _BULK_VOL[den] * np.asarray(value, np.float64)
+    return float(out) if np.ndim(out) == 0 else out
 
 
 def _crout_solve(a, b):

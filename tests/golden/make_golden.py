@@ -26,7 +26,7 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 
 DECKS = ["carbonate-unit-activity", "carbonate-debye-huckel-activity",
          "ca-carbonate-unit-activity", "ca-carbonate-debye-huckel-activity",
-         "calcite-kinetics", "calcite-kinetics-volume-fractions"]
+         "calcite-kinetics", "calcite-kinetics-volume-fractions", "calcite-area-per-mass"]
 
 TIME_UNITS = {"s": 1.0, "sec": 1.0, "min": 60.0, "h": 3600.0, "hr": 3600.0,
               "d": 86400.0, "day": 86400.0, "w": 7 * 86400.0,
@@ -60,7 +60,7 @@ def block(lines, start):
 
 
 def read_deck(path):
-    raw = [ln.split("#")[0].rstrip() for ln in open(path)]
+    raw = [ln.split("#")[0].split("!")[0].rstrip() for ln in open(path)]
     lines = [ln for ln in raw]
     up = [ln.strip().upper() for ln in lines]
     deck = {}
@@ -105,6 +105,9 @@ def read_deck(path):
             unit = p[3] if len(p) > 3 else "m^2/m^3"
             if unit == "cm^2/cm^3":
                 area *= 100.0
+            elif unit != "m^2/m^3":
+                # converted in main() with the database's molar weight/volume
+                deck.setdefault("area_units", {})[p[0]] = unit
             deck["mineral_init"][p[0]] = (fnum(p[1]), area)
     deck["porosity"] = fnum(re.search(r"POROSITY\s+(\S+)", " ".join(lines)).group(1))
     for key in ("FINAL_TIME", "INITIAL_TIMESTEP_SIZE", "MAXIMUM_TIMESTEP_SIZE"):
@@ -159,6 +162,16 @@ def main():
             gold=read_gold(os.path.join(BATCH, name + ".regression.gold")),
             tolerance_abs=1.0e-12,
         )
+        if deck.get("area_units"):
+            # specific surface area per mass of mineral (MineralProcessConstraint,
+            # reaction_mineral.F90:590-640) through the package's conversion
+            from pfgpu.database import mineral_surface_area, read_database
+            db = read_database(os.path.join(BATCH, deck["database"].lstrip("./")))
+            fx["mineral_area_input"] = {}
+            for m, unit in deck["area_units"].items():
+                vf, raw = deck["mineral_init"][m]
+                fx["mineral_area_input"][m] = [raw, unit]
+                fx["mineral_init"][m] = (vf, mineral_surface_area(raw, unit, db.minerals[m], vf, m))
         fixtures[name] = fx
     # IFC67 pin: src/pflotran/unittests/test_eos_water.pf
     pf = open(os.path.join(ROOT, "src", "pflotran", "unittests", "test_eos_water.pf")).read()

@@ -147,6 +147,44 @@ def test_reference_databases_build_the_fixture_networks():
             assert net.mnrl_logK[m] == mx["logK"] and net.mnrl_molar_vol[m] == mx["molar_vol"]
 
 
+def test_mineral_surface_area_units():
+    """MineralProcessConstraint (reaction_mineral.F90:590-640): bulk-volume
+    units scale directly; per-mass units go through molar weight / molar
+    volume and the volume fraction; the reference's refusals are errors."""
+    calcite = dbm.Reaction([], [], molar_vol_cm3=36.934, molar_weight=100.0872)
+    assert dbm.mineral_surface_area(1.0, "cm^2/cm^3", calcite, 0.2) == pytest.approx(100.0, rel=1e-15)
+    assert dbm.mineral_surface_area(3.0, "m^2/m^3", calcite, 0.2) == 3.0
+    assert dbm.mineral_surface_area(2.0, "m^2/L", calcite, 0.2) == pytest.approx(2000.0, rel=1e-15)
+    # 1.8450910805777365 cm^2/g of calcite at 20 % is 1 cm^2/cm^3 of bulk
+    # (the comment of regression_tests/ascem/batch/calcite-area-per-mass.in)
+    a = dbm.mineral_surface_area(1.8450910805777365, "cm^2/g", calcite, 0.2, "Calcite")
+    assert a == pytest.approx(100.0, rel=1e-14)
+    # m^2/kg and cm^2/g differ by 10; m^2/g and cm^2/g by 1e4
+    assert dbm.mineral_surface_area(1.0, "m^2/kg", calcite, 0.2) == pytest.approx(
+        10.0 * dbm.mineral_surface_area(1.0, "cm^2/g", calcite, 0.2), rel=1e-15)
+    assert dbm.mineral_surface_area(1.0, "m^2/g", calcite, 0.2) == pytest.approx(
+        1.0e4 * dbm.mineral_surface_area(1.0, "cm^2/g", calcite, 0.2), rel=1e-15)
+    # per-cell datasets: arrays of areas and volume fractions
+    vf = np.array([0.1, 0.2, 0.4])
+    arr = dbm.mineral_surface_area(np.array([1.0, 1.0, 2.0]), "cm^2/g", calcite, vf)
+    assert arr.shape == (3,) and arr[1] == pytest.approx(2.0 * arr[0]) and arr[2] == pytest.approx(8.0 * arr[0])
+    with pytest.raises(ValueError, match="volume fraction"):
+        dbm.mineral_surface_area(1.0, "cm^2/g", calcite, 0.0)
+    with pytest.raises(ValueError, match="molar weight"):
+        dbm.mineral_surface_area(1.0, "cm^2/g", dbm.Reaction([], [], molar_vol_cm3=36.9, molar_weight=500.0), 0.2)
+    with pytest.raises(ValueError, match="molar volume"):
+        dbm.mineral_surface_area(1.0, "cm^2/g", dbm.Reaction([], [], molar_vol_cm3=0.0, molar_weight=100.0), 0.2)
+    for bad in ("cm/cm^3", "cm^2", "cm^2/ft^3", "cm^2/lb"):
+        with pytest.raises(ValueError):
+            dbm.mineral_surface_area(1.0, bad, calcite, 0.2)
+
+
+def test_reader_keeps_mineral_molar_weight():
+    db = dbm.read_database(_carbonate_like())
+    assert db.minerals["Calcite"].molar_weight == 100.0
+    assert db.minerals["Dolomite"].molar_weight == 184.0 and db.minerals["Dolomite"].molar_vol_cm3 == 64.3
+
+
 def _carbonate_like():
     """A small carbonate-system database in the .dat format: logK near
     typical 25 C values, varying linearly with temperature (values chosen
