@@ -21,14 +21,26 @@ MUTABLE = ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "m
            "mnrl_rate", "status", "newton_its", "num_substeps", "total_sorb", "ionx_ref_sorbed", "ln_act_h2o")
 
 
-def network_key(eng) -> str:
-    import torch
+def network_key(eng, device_name: str | None = None) -> str:
     net = eng.net
+    if device_name is None:
+        import torch
+        device_name = torch.cuda.get_device_name()
     h = hashlib.sha1()
     for a in (net.sec_nspec, net.sec_spec, net.mnrl_nspec, net.mnrl_spec):
         h.update(a.tobytes())
-    return "%s|n%d|s%d|m%d|%s" % (torch.cuda.get_device_name(), net.ncomp, net.nsec, net.nmnrl,
-                                  h.hexdigest()[:12])
+    return "%s|n%d|s%d|m%d|%s" % (device_name, net.ncomp, net.nsec, net.nmnrl, h.hexdigest()[:12])
+
+
+def event_timer(fn) -> float:
+    """Milliseconds of fn() between two CUDA events on the current stream."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
 
 
 def candidates(quick: bool = False):
@@ -48,17 +60,22 @@ def candidates(quick: bool = False):
 
 
 def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2, use_cache: bool = True,
-         verbose: bool = False, quick: bool = False, cost_order: bool = False):
+         verbose: bool = False, quick: bool = False, cost_order: bool = False, timer=event_timer,
+         device_name: str | None = None, cache_path: str | None = None):
     """cost_order: time every configuration with the work queue ordered by a
     first step's Newton counts (longest cells first), as a time loop that
     orders by the previous step runs; without it the sample's tail of slow
-    cells favours configurations that are only better on unordered queues."""
+    cells favours configurations that are only better on unordered queues.
+    timer(fn) returns the milliseconds of one launch (CUDA events by
+    default); device_name and cache_path default to the current GPU's name
+    and the cache file next to this module."""
     import torch
-    key = network_key(eng)
+    key = network_key(eng, device_name)
+    cache_path = cache_path or CACHE
     cache = {}
-    if use_cache and os.path.exists(CACHE):
+    if use_cache and os.path.exists(cache_path):
         try:
-            cache = json.load(open(CACHE))
+            cache = json.load(open(cache_path))
         except Exception:
             cache = {}
     if use_cache and key in cache:
@@ -80,16 +97,13 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
         for _ in range(reps + 1):
             for k, v in pristine.items():
                 sample.a[k].copy_(v)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            eng.rstep(sample, dt, stats=False, order=order)
-            e1.record()
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1)
+            ms = timer(lambda: eng.rstep(sample, dt, stats=False, order=order))
             best = ms if best is None else min(best, ms)
         table.append(dict(cfg, ms=best))
         if verbose:
             print(cfg, "%.3f ms" % best)
+    if not table:
+        raise RuntimeError("pf_network_set_launch accepted no candidate configuration for this network")
     table.sort(key=lambda r: r["ms"])
     keys = ("threads_per_block", "blocks_per_sm", "jac_in_shared", "lanes_per_cell")
     top = {k: table[0][k] for k in keys}
@@ -103,7 +117,7 @@ def tune(eng, state: CellState, dt: float, max_cells: int = 65536, reps: int = 2
         sample.a[k].copy_(v)
     cache[key] = {"best": top, "table": table[:12], "cells": n, "cost_order": bool(cost_order)}
     try:
-        json.dump(cache, open(CACHE, "w"), indent=1)
+        json.dump(cache, open(cache_path, "w"), indent=1)
     except OSError:
         pass
     return top, table
