@@ -80,7 +80,7 @@ class ReactionEngine:
               stats: bool = True, order=None):
         """order: optional int64 CUDA tensor, a permutation of the cells giving
         the work-queue order of the batched kernel (results are unchanged)."""
-        s = state.struct()
+        s = state.struct("device", self.net)
         if order is not None:
             assert order.dtype.is_floating_point is False and order.numel() == state.ncells
             s.cell_order = C.cast(order.data_ptr(), C.POINTER(C.c_int64))
@@ -94,7 +94,7 @@ class ReactionEngine:
 
     def rstep_host(self, state: CellState, dt: float, kernel: int = abi.PF_KERNEL_BATCHED, order=None):
         """order: optional int64 numpy array (host), the work-queue order."""
-        s = state.struct()
+        s = state.struct("host", self.net)
         if order is not None:
             self._host_order = np.ascontiguousarray(order, np.int64)
             s.cell_order = C.cast(self._host_order.ctypes.data, C.POINTER(C.c_int64))
@@ -104,7 +104,7 @@ class ReactionEngine:
         return {k: getattr(st, k) for k, _ in abi.PfStepStats._fields_}
 
     def update_auxvars(self, state: CellState, update_activity_coefs: bool = False, stream=None):
-        s = state.struct()
+        s = state.struct("device", self.net)
         abi.check("pf_update_auxvars",
                   self.lib.pf_update_auxvars(self.handle, C.byref(s), int(update_activity_coefs),
                                              _stream_ptr(stream)), allow_cell_failures=False)
@@ -117,7 +117,7 @@ class ReactionEngine:
         import torch
         ct = np.ascontiguousarray(ctype, np.int32)
         its = torch.empty(state.ncells, dtype=torch.int32, device=cconc.device)
-        s = state.struct()
+        s = state.struct("device", self.net)
         cr = abi.constraint_reactions(len(ct), reactions)
         abi.check("pf_equilibrate_constraint_ex",
                   self.lib.pf_equilibrate_constraint_ex(
@@ -168,7 +168,7 @@ class ReactionEngine:
         a.dL_dlogK_sec, a.dL_dlogK_mnrl = ptr(out["dL_dlogK_sec"]), ptr(out["dL_dlogK_mnrl"])
         a.dL_dlnk, a.loss = ptr(out["dL_dlnk"]), ptr(out["loss"])
         a.adj_status = ptr(out["adj_status"], C.c_int32)
-        s = state.struct()
+        s = state.struct("device", self.net)
         if order is not None:
             s.cell_order = C.cast(order.data_ptr(), C.POINTER(C.c_int64))
         abi.check("pf_adjoint", self.lib.pf_adjoint(self.handle, C.byref(s), float(dt), C.byref(a),
@@ -182,7 +182,7 @@ class ReactionEngine:
         return out
 
     def update_activity_coefs(self, state: CellState, stream=None):
-        s = state.struct()
+        s = state.struct("device", self.net)
         abi.check("pf_update_activity_coefs",
                   self.lib.pf_update_activity_coefs(self.handle, C.byref(s), _stream_ptr(stream)),
                   allow_cell_failures=False)

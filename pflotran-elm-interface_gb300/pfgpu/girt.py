@@ -115,7 +115,7 @@ class GirtAssembler:
         if total_sorb_k is not None:
             total_sorb_k = total_sorb_k.contiguous()
         a = self.args(total_k, dt, total_sorb_k, numerical_derivatives)
-        s = state.struct()
+        s = state.struct("device", self.engine.net)
         abi.check("pf_girt_assemble",
                   self.engine.lib.pf_girt_assemble(self.engine.handle, C.byref(s), C.byref(a), _stream_ptr(stream)),
                   allow_cell_failures=False)

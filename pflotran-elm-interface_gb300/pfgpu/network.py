@@ -439,20 +439,48 @@ class CellState:
                 out[k] = v[..., idx].contiguous()
         return CellState(self.net, out)
 
-    def struct(self) -> abi.PfCellState:
+    def struct(self, where: str | None = None, net: ReactionNetwork | None = None) -> abi.PfCellState:
+        """The PfCellState of these arrays, after checking each one against
+        the field table: its dtype, rows x ncells elements (rows of `net`,
+        default this state's network) and C-contiguous storage.  where =
+        "device": every array a CUDA tensor, all on one device; "host": every
+        array a numpy array; None: either.  A buffer of the wrong type or
+        length would be read past its end by the kernels, so a mismatch is a
+        ValueError naming the field.  Missing fields stay NULL pointers, which
+        the library refuses where the network needs them."""
+        net = net or self.net
         s = abi.PfCellState()
         s.ncells = self.ncells
+        device = None
         for k, (r, dt) in STATE_FIELDS.items():
             v = self.a.get(k)
             ct = C.c_int32 if dt == np.int32 else C.c_double
             if v is None:
                 setattr(s, k, C.cast(None, C.POINTER(ct)))
                 continue
+            want = _rows(net, r) * self.ncells
             if isinstance(v, np.ndarray):
-                assert v.flags.c_contiguous and v.dtype == dt, k
+                if where == "device":
+                    raise ValueError("state field %r is a host array; this call needs CUDA tensors" % k)
+                if v.dtype != dt or not v.flags.c_contiguous or v.size != want:
+                    raise ValueError("state field %r: need a C-contiguous %s array of %d values, got %s %s%s"
+                                     % (k, np.dtype(dt).name, want, v.dtype, v.shape,
+                                        "" if v.flags.c_contiguous else " (not contiguous)"))
                 addr = v.ctypes.data
             else:
-                assert v.is_contiguous(), k
+                tname = "torch." + np.dtype(dt).name
+                if str(v.dtype) != tname or not v.is_contiguous() or v.numel() != want:
+                    raise ValueError("state field %r: need a contiguous %s tensor of %d values, got %s %s%s"
+                                     % (k, tname, want, v.dtype, tuple(v.shape),
+                                        "" if v.is_contiguous() else " (not contiguous)"))
+                if where == "host":
+                    raise ValueError("state field %r is a tensor; this call needs host numpy arrays" % k)
+                if where == "device":
+                    if not v.is_cuda:
+                        raise ValueError("state field %r is on %s; this call needs CUDA tensors" % (k, v.device))
+                    if device is not None and v.device != device:
+                        raise ValueError("state field %r is on %s, others on %s" % (k, v.device, device))
+                    device = v.device
                 addr = v.data_ptr()
             setattr(s, k, C.cast(addr, C.POINTER(ct)))
         return s
