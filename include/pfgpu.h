@@ -340,9 +340,8 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
  * not allocate device memory during the step.  No counterpart in the
  * reference (PFLOTRAN's Fortran loop has no device memory to allocate).
  * Callers that cannot let a library call cudaMalloc -- a host model whose GPU
- * memory belongs to another framework's pool, a coupled run with a fixed
- * device footprint, code recording the step into a CUDA graph -- use this
- * instead of pf_rstep: the per-cell scratch lives in a fixed 32 MiB device
+ * memory belongs to another framework's pool, or a coupled run with a fixed
+ * device footprint -- use this instead of pf_rstep: the per-cell scratch lives in a fixed 32 MiB device
  * array inside the library (held on every device that loads it until exit),
  * and the call allocates nothing.  Limit: (ncomp + nsec + nmnrl) * ncells
  * <= 4,194,304; larger states return PF_ERR_TOO_LARGE (split them across

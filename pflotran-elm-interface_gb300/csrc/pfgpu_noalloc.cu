@@ -4,8 +4,8 @@
 // pf_rstep normally keeps its per-cell scratch (the setup pre-pass output,
 // (ncomp + nsec + nmnrl) doubles per cell) in a buffer it grows with
 // cudaMalloc.  Some callers cannot allow that: a host model whose GPU memory
-// is owned by another framework's pool, a coupled run that fixes its device
-// footprint up front, or a caller recording the step into a CUDA graph.
+// is owned by another framework's pool, or a coupled run that fixes its
+// device footprint up front.
 // pf_rstep_noalloc runs the same kernels with the scratch in a fixed,
 // file-scope device array instead, so the call itself never allocates.
 #include <mutex>

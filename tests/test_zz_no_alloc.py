@@ -1,7 +1,6 @@
 """pf_rstep_noalloc: the batched step for callers that may not allocate device
 memory during the call (their GPU memory belongs to another framework's pool,
-their footprint is fixed up front, or they record the step into a CUDA
-graph).  Its scratch is a fixed array inside the library, shared by every
+or their footprint is fixed up front).  Its scratch is a fixed array inside the library, shared by every
 call, so this test checks that two calls in a row -- the second reusing
 whatever the first left in that array -- give the same results as the
 allocating entry point pf_rstep, to the parity tolerance of the other tests
