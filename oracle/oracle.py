@@ -8,6 +8,7 @@ routines it follows).
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 import sys
@@ -187,3 +188,78 @@ class Oracle:
 
     def density(self, t, p):
         return self.lib.oracle_ifc67_density(t, p)
+
+
+LOG_TO_LN = 2.30258509299  # pflotran_constants.F90:84
+
+
+def surface_complexation_eq(pri_molal, pri_act_coef, complexes, site_density, free_site_guess=1.0e-9,
+                            ln_act_h2o=0.0):
+    """Equilibrium surface complexation of one site (one reaction), a
+    pure-Python restatement of RTotalSorbEqSurfCplx1
+    (reaction_surf_complex.F90:641-900) for a single cell.
+
+    complexes: list of dicts with spec (primary indices), stoich, free_site_stoich,
+    logK (log10 at the cell's temperature) and optionally h2o_stoich.
+    site_density: mol sites / m^3 bulk (the NULL_SURFACE case, :720-722).
+    Returns (free_site_conc, cplx_conc[ncplx], total_sorb[ncomp],
+    dtotal_sorb[ncomp][ncomp]) in mol/m^3 bulk and kg water/m^3 bulk."""
+    n = len(pri_molal)
+    ln_act = [math.log(pri_molal[i]) + math.log(pri_act_coef[i]) for i in range(n)]  # :686-687
+    ncplx = len(complexes)
+    total_sorb = [0.0] * n
+    dtotal = [[0.0] * n for _ in range(n)]
+    if site_density < 1.0e-40:  # :728-737
+        return 0.0, [0.0] * ncplx, total_sorb, dtotal
+    stoich_flag = any(c["free_site_stoich"] > 1.0 for c in complexes)  # reaction_database.F90:2801-2803
+    free = max(free_site_guess, 1.0e-40)  # :691
+    conc = [0.0] * ncplx
+    one_more, its, damping = False, 0, 1.0
+    while True:  # :743-799
+        its += 1
+        total = free
+        ln_free = math.log(free)
+        for j, c in enumerate(complexes):
+            lnQK = -c["logK"] * LOG_TO_LN
+            if c.get("h2o_stoich", 0.0):
+                lnQK += c["h2o_stoich"] * ln_act_h2o
+            lnQK += c["free_site_stoich"] * ln_free
+            for i, nu in zip(c["spec"], c["stoich"]):
+                lnQK += nu * ln_act[i]
+            conc[j] = math.exp(lnQK)
+            total += c["free_site_stoich"] * conc[j]
+        if one_more:
+            break
+        if stoich_flag:  # Newton on the site balance (:770-790)
+            res = site_density - total
+            dres = 1.0
+            for j, c in enumerate(complexes):
+                dres += c["free_site_stoich"] * conc[j] / free
+            dfree = res / dres
+            if its > 1000:
+                damping = 0.5
+            free = free + damping * dfree
+            if abs(dfree / free) < 1.0e-12:
+                one_more = True
+        else:  # every complex holds one site: closed form (:792-797)
+            total = total / free
+            free = site_density / total
+            one_more = True
+    # derivatives (:803-824, 846-893)
+    dSx = [0.0] * n
+    tempreal = 0.0
+    for j, c in enumerate(complexes):
+        for i, nu in zip(c["spec"], c["stoich"]):
+            dSx[i] += nu * c["free_site_stoich"] * conc[j]
+        tempreal += c["free_site_stoich"] * c["free_site_stoich"] * conc[j]
+    tempreal = tempreal / free + 1.0
+    dSx = [-v / tempreal / pri_molal[i] for i, v in enumerate(dSx)]
+    for j, c in enumerate(complexes):
+        for i, nu in zip(c["spec"], c["stoich"]):
+            total_sorb[i] += nu * conc[j]
+        nui_Si_over_Sx = c["free_site_stoich"] * conc[j] / free
+        for jc, nuj in zip(c["spec"], c["stoich"]):
+            t = nuj * conc[j] / pri_molal[jc] + nui_Si_over_Sx * dSx[jc]
+            for ic, nui in zip(c["spec"], c["stoich"]):
+                dtotal[ic][jc] += nui * t
+    return free, conc, total_sorb, dtotal

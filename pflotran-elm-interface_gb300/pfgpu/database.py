@@ -9,9 +9,12 @@ Database format (DatabaseRead, src/pflotran/reaction_database.F90:26-811):
     'name' Vm k (nu 'species')*k logK*n MW       gases, until 'null'
     'name' Vm k (nu 'species')*k logK*n MW       minerals (Vm in cm^3/mol), until 'null'
 
+    'name' k (nu 'species')*k logK*n Z MW     surface complexes, until 'null'
+                                          (one species is the site, '>...')
+
 (tokens are whitespace-separated, names quoted; Fortran 'd' exponents
-accepted; a logK of 500 marks a temperature with no data).  Surface
-complexes and later sections are not read.
+accepted; a logK of 500 marks a temperature with no data).  Later sections
+are not read.
 
 Basis set-up (the subset of BasisInit, reaction_database.F90:812-4040, that
 this engine needs): the primary species must be basis species of the
@@ -68,6 +71,7 @@ class Database:
     secondary: dict = field(default_factory=dict)   # name -> Reaction
     gases: dict = field(default_factory=dict)       # name -> Reaction
     minerals: dict = field(default_factory=dict)    # name -> Reaction
+    surface_complexes: dict = field(default_factory=dict)  # name -> Reaction (site included in stoich)
 
 
 def read_database(source: str) -> Database:
@@ -118,7 +122,32 @@ def read_database(source: str) -> Database:
             if name == "null":
                 break
             table[name] = Reaction(st, logK, molar_vol_cm3=vm, molar_weight=mw)
+    # surface complexes: name k pairs logK*nt Z MW (the site is one of the
+    # species, its name starting with '>')
+    while i + 1 < len(toks):
+        name = toks[i]
+        k = int(_num(toks[i + 1]))
+        st, i = pairs(i + 2, k)
+        logK = [_num(t) for t in toks[i:i + nt]]
+        i += nt
+        Z = _num(toks[i]) if i < len(toks) else 0.0
+        i += 2
+        # an optional trailing source note ('llnl-99'): a string followed by
+        # a string (the next record's name) rather than by a count
+        if i + 1 < len(toks) and not _is_num(toks[i]) and not _is_num(toks[i + 1]):
+            i += 1
+        if name == "null":
+            break
+        db.surface_complexes[name] = Reaction(st, logK, Z=Z)
     return db
+
+
+def _is_num(tok: str) -> bool:
+    try:
+        _num(tok)
+        return True
+    except ValueError:
+        return False
 
 
 # unit factors to m, m^3 and kg

@@ -26,7 +26,8 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 
 DECKS = ["carbonate-unit-activity", "carbonate-debye-huckel-activity",
          "ca-carbonate-unit-activity", "ca-carbonate-debye-huckel-activity",
-         "calcite-kinetics", "calcite-kinetics-volume-fractions", "calcite-area-per-mass"]
+         "calcite-kinetics", "calcite-kinetics-volume-fractions", "calcite-area-per-mass",
+         "surface-complexation-1"]
 
 TIME_UNITS = {"s": 1.0, "sec": 1.0, "min": 60.0, "h": 3600.0, "hr": 3600.0,
               "d": 86400.0, "day": 86400.0, "w": 7 * 86400.0,
@@ -109,6 +110,11 @@ def read_deck(path):
                 # converted in main() with the database's molar weight/volume
                 deck.setdefault("area_units", {})[p[0]] = unit
             deck["mineral_init"][p[0]] = (fnum(p[1]), area)
+    if "SURFACE_COMPLEXATION_RXN" in up:
+        j = up.index("SURFACE_COMPLEXATION_RXN")
+        site = [lines[k].split() for k in range(j, len(up)) if up[k].startswith("SITE ")][0]
+        deck["surface"] = dict(site=site[1], site_density=fnum(site[2]),
+                               complexes=block(lines, up.index("COMPLEXES", j)))
     deck["porosity"] = fnum(re.search(r"POROSITY\s+(\S+)", " ".join(lines)).group(1))
     for key in ("FINAL_TIME", "INITIAL_TIMESTEP_SIZE", "MAXIMUM_TIMESTEP_SIZE"):
         m = re.search(key + r"\s+(\S+)\s+(\S+)", " ".join(lines))
@@ -162,6 +168,19 @@ def main():
             gold=read_gold(os.path.join(BATCH, name + ".regression.gold")),
             tolerance_abs=1.0e-12,
         )
+        if deck.get("surface"):
+            # equilibrium surface complexation on a fixed site density
+            # (SURFACE_COMPLEXATION_RXN ... SITE name density, NULL_SURFACE)
+            from pfgpu.database import read_database
+            db = read_database(os.path.join(BATCH, deck["database"].lstrip("./")))
+            sf = deck["surface"]
+            cplx = []
+            for cname in sf["complexes"]:
+                r = db.surface_complexes[cname]
+                cplx.append(dict(name=cname, logK=r.logK[tref_index], Z=r.Z,
+                                 free_site_stoich=sum(nu for sp, nu in r.stoich if sp == sf["site"]),
+                                 stoich={sp: nu for sp, nu in r.stoich if sp != sf["site"] and sp != "H2O"}))
+            fx["surface_complexation"] = dict(site=sf["site"], site_density=sf["site_density"], complexes=cplx)
         if deck.get("area_units"):
             # specific surface area per mass of mineral (MineralProcessConstraint,
             # reaction_mineral.F90:590-640) through the package's conversion

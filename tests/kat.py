@@ -24,11 +24,14 @@ from pfgpu.network import CellState, ReactionNetwork, default_options, tight_opt
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 KAT = json.load(open(os.path.join(HERE, "golden", "kat_batch.json")))
-CON = {"T": 1, "F": 2, "PH": 3, "Z": 4, "CHG": 4, "L": 5}
+CON = {"T": 1, "F": 2, "PH": 3, "P": 3, "Z": 4, "CHG": 4, "L": 5}
 
 
 def kat_names(kind=None):
     names = [k for k in KAT if not k.startswith("_")]
+    if kind == "surface":
+        return [k for k in names if "surface_complexation" in KAT[k]]
+    names = [k for k in names if "surface_complexation" not in KAT[k]]
     if kind == "speciation":
         return [k for k in names if KAT[k]["gold"].get("Time Steps", 0) == 0]
     if kind == "kinetics":

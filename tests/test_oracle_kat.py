@@ -64,3 +64,80 @@ def test_kinetics_kat(oracle, name):
         if key.startswith("Total"):
             tol = LOOSE_TOTAL.get(name, TOL)
         assert out[key] == pytest.approx(gold, abs=tol), (key, out[key], gold)
+
+
+def _surface(fx, net, st, oracle_mod):
+    sc = fx["surface_complexation"]
+    cplx = [dict(spec=[net.primary.index(s) for s in c["stoich"]], stoich=list(c["stoich"].values()),
+                 free_site_stoich=c["free_site_stoich"], logK=c["logK"]) for c in sc["complexes"]]
+    return sc, cplx, oracle_mod.surface_complexation_eq(
+        list(st.a["pri_molal"][:, 0]), list(st.a["pri_act_coef"][:, 0]), cplx, sc["site_density"])
+
+
+# The sorbed concentrations reach 7.6e4 mol/m^3, where batch.cfg's 1e-12
+# absolute is below one ulp; they are checked to 1e-12 relative instead.
+SURF_REL = 1.0e-12
+
+
+@pytest.mark.parametrize("name", kat.kat_names("surface"))
+def test_surface_complexation_kat(oracle, name):
+    """Equilibrium surface complexation (RTotalSorbEqSurfCplx1) on the
+    constraint's speciation: free sites, each complex and the sorbed totals
+    against the reference's gold."""
+    from oracle import oracle as om
+    fx = kat.KAT[name]
+    net = kat.network(fx)
+    st = kat.initial_state(fx, net, oracle, _density(oracle))
+    out = kat.outputs(fx, net, st)
+    sc, cplx, (free, conc, tsorb, _) = _surface(fx, net, st, om)
+    out["Free " + sc["site"]] = free
+    out[sc["site"] + " Site Density"] = sc["site_density"]
+    for c, v in zip(sc["complexes"], conc):
+        out[c["name"]] = v
+    for k, s in enumerate(net.primary):
+        out["Total Sorbed " + s] = tsorb[k]
+    checked = 0
+    for key, gold in fx["gold"].items():
+        if key in ("Time Steps", "Newton Iterations"):
+            continue
+        tol = max(TOL, SURF_REL * abs(gold))
+        assert out[key] == pytest.approx(gold, abs=tol), (key, out[key], gold)
+        checked += 1
+    assert checked >= 12
+
+
+def test_surface_complexation_restatement_properties(oracle):
+    """Site balance, mass action, and the sorbed-total derivative against
+    central differences in ln m (with a multidentate complex, which takes the
+    Newton branch of the free-site solve).  The reference's derivative
+    (reaction_surf_complex.F90:874-893) loops over each complex's own
+    species only, leaving out the free-site coupling to components the
+    complex does not hold; the difference check therefore uses complexes
+    that all hold the same two components."""
+    import math
+
+    from oracle import oracle as om
+    m = [1.0e-5, 2.0e-3, 1.0e-7]
+    g = [0.9, 0.8, 0.6]
+    cplx = [dict(spec=[0, 1], stoich=[1.0, 1.0], free_site_stoich=1.0, logK=-7.0),
+            dict(spec=[0, 1], stoich=[-1.0, 2.0], free_site_stoich=1.0, logK=2.0),
+            dict(spec=[0, 1], stoich=[-2.0, 1.0], free_site_stoich=2.0, logK=5.0)]
+    S = 500.0
+    free, conc, ts, dts = om.surface_complexation_eq(m, g, cplx, S)
+    assert free + sum(c["free_site_stoich"] * x for c, x in zip(cplx, conc)) == pytest.approx(S, rel=1e-12)
+    for c, x in zip(cplx, conc):
+        lnq = -c["logK"] * om.LOG_TO_LN + c["free_site_stoich"] * math.log(free) + sum(
+            nu * math.log(m[i] * g[i]) for i, nu in zip(c["spec"], c["stoich"]))
+        assert math.log(x) == pytest.approx(lnq, abs=1e-10)
+    for j in range(2):
+        h = 1.0e-6
+        up, dn = list(m), list(m)
+        up[j] *= math.exp(h)
+        dn[j] *= math.exp(-h)
+        tu = om.surface_complexation_eq(up, g, cplx, S, free)[2]
+        td = om.surface_complexation_eq(dn, g, cplx, S, free)[2]
+        for i in range(2):
+            fd = (tu[i] - td[i]) / (2 * h) / m[j]
+            assert dts[i][j] == pytest.approx(fd, rel=1e-5, abs=1e-6 * max(1.0, abs(fd))), (i, j)
+    # no sites: nothing sorbs
+    assert om.surface_complexation_eq(m, g, cplx, 0.0)[2] == [0.0, 0.0, 0.0]
