@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and reference legs use
 this module; the product path never imports it.  The C++ restatement it
 wraps is oracle/rxn_oracle.hpp (see the file header for the reference
 routines it follows).

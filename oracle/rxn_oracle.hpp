@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY.  This is the oracle the GPU engine is checked
 // against; nothing in the product links or calls it.  Only tests/,
-// __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+// __graft_entry__.smoke() and bench.py's CPU-baseline and reference legs use it.
 //
 // Every routine restates one reference subroutine, in the same loop order and
 // with the same left-to-right evaluation of each Fortran expression, so that
