@@ -131,13 +131,14 @@ class Clocks:
     """nvidia-smi sampling during the timed region."""
 
     def __init__(self, index=0):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        fd, self.path = tempfile.mkstemp(prefix="pfgpu_clocks_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index),
@@ -160,6 +161,10 @@ class Clocks:
             rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
         except Exception:
             return None
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         rows = [r for r in rows if len(r) >= 8]
         if not rows:
             return None
@@ -191,6 +196,20 @@ def fp64_peak(lib, device_sms):
         torch.cuda.synchronize()
         best = max(best, blocks * threads * iters * 16.0 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
     return best
+
+
+STEP = ("the second operator-split step from the equilibrated state; the first step (untimed) gives the "
+        "Newton counts that order the second step's work queue")
+
+
+def c2_config(cfg, ncells, dt, state_bytes):
+    """The workload description both arms print (ours and --impl reference)."""
+    if state_bytes > 129e6:
+        l2 = "state %.2f GB > L2 (129 MB); state reset to the step's input before each timed step" % (state_bytes / 1e9)
+    else:
+        l2 = ("state %.1f MB fits in L2, not flushed: this small case is launch-bound; state reset before each "
+              "timed step" % (state_bytes / 1e6))
+    return {"workload": cfg["workload"], "cells": ncells, "dt_s": dt, "step": STEP, "l2": l2}
 
 
 def time_steps(eng, dev, pristine, dt, kernel, steps, warmup, order=None):
@@ -421,23 +440,23 @@ def c3_transport(members, seed=4000):
     return stages, info
 
 
-def run_c3(args):
-    """Heterogeneous batching: 8 networks, per-cell dt, 50 operator-split
+def c3_measure(args, per=500_000, nsteps=50, replays=1, plain=True, eager_steps=5):
+    """Heterogeneous batching: 8 networks, per-cell dt, `nsteps` operator-split
     steps (RTUpdateAuxVars + TIMESTEP activities + RStep per network) in one
-    CUDA graph; value = cells x steps / graph time."""
+    CUDA graph; value = cells x steps / graph time.  The first step from the
+    equilibrated state is also timed eagerly per network, batched against
+    the plain one-thread-per-cell form."""
     import numpy as np
     import torch
 
     from pfgpu import abi, autotune
     from pfgpu.timeloop import OperatorSplitLoop
-    per = args.cells or 500_000
-    nsteps = args.graph_steps
     t0 = time.perf_counter()
     members = build_c3(per, "cuda")
     log("c3 state built: %d x %d cells in %.1f s" % (len(members), per, time.perf_counter() - t0))
     stages = [None] * len(members)
     transport_info = None
-    if args.transport:
+    if getattr(args, "transport", False):
         stages, transport_info = c3_transport(members)
         log("c3 transport:", json.dumps(transport_info))
     tuned = {}
@@ -471,18 +490,20 @@ def run_c3(args):
         reset(start)
         b_ms = timed(lambda: eng.rstep(dev, 86400.0, stats=False))
         its = dev.a["newton_its"].to(torch.float64)
-        reset(start)
-        p_ms = timed(lambda: eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_PLAIN, stats=False))
+        p_ms = None
+        if plain:
+            reset(start)
+            p_ms = timed(lambda: eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_PLAIN, stats=False))
         per_net.append(dict(ncomp=eng.net.ncomp, nsec=eng.net.nsec, nmnrl=eng.net.nmnrl, cells=dev.ncells,
                             batched_ms=b_ms, plain_ms=p_ms, its_mean=float(its.mean()),
                             its_p50=float(its.median()), its_max=int(its.max()),
                             its_min=int(its.min())))
     batched_first = sum(r["batched_ms"] for r in per_net)
-    plain_first = sum(r["plain_ms"] for r in per_net)
+    plain_first = sum(r["plain_ms"] for r in per_net) if plain else None
     # one eager warm step of the loop (its Newton counts order the first graph step)
     reset(start)
     loop = OperatorSplitLoop([(eng, dev, tr) for (eng, dev), tr in zip(members, stages)], dt=86400.0,
-                             concurrent=args.concurrent)
+                             concurrent=getattr(args, "concurrent", False))
     loop.step()
     torch.cuda.synchronize()
     s0 = [{k: dev.a[k].clone() for k in fields if k in dev.a} for _, dev in members]
@@ -490,35 +511,50 @@ def run_c3(args):
     torch.cuda.synchronize()
     graph_ms = []
     with Clocks(0) as clk:
-        for _ in range(max(1, args.steps)):
+        for _ in range(max(1, replays)):
             reset(s0)
             graph_ms.append(timed(loop.replay))
     summary = loop.summary()
-    # the same steps eagerly (launch overhead comparison), a few steps only
-    k_e = min(nsteps, 5)
-    reset(s0)
-    eager_ms = timed(lambda: [loop.step() for _ in range(k_e)])
+    eager_ms = None
+    if eager_steps:
+        k_e = min(nsteps, eager_steps)
+        reset(s0)
+        eager_ms = timed(lambda: [loop.step() for _ in range(k_e)]) / k_e
     total_cells = sum(dev.ncells for _, dev in members)
     g = float(np.min(graph_ms))
     value = total_cells * nsteps / (g * 1e-3)
-    line = {"metric": "heterogeneous batched cell-solves/s, 8 networks, %d operator-split steps in one CUDA graph"
-            % nsteps, "value": value, "unit": UNIT, "n_gpus": 1, "steps": len(graph_ms), "warmup": 1,
-            "ms_per_step": g / nsteps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "8 synthetic networks ncomp %s, 3*ncomp complexes, ncomp/2 kinetic minerals, "
-                                   "%d cells each, %s, T U[5,60] C" % (
-                                       C3_NCOMP, per, "structured grid per network, transport solve + reaction "
-                                       "each step, dt 1 d" if args.transport else "per-cell dt log-U[1 h, 30 d]"),
-                       "graph_steps": nsteps, "concurrent_streams": bool(args.concurrent),
-                       "l2": "state > L2; reset D2D before each replay, outside the timed region"},
-            "graph_ms": g, "eager_ms_per_step": eager_ms / k_e,
-            "first_step": {"batched_ms": batched_first, "plain_ms": plain_first,
-                           "speedup_vs_plain_gpu": plain_first / batched_first, "per_network": per_net},
-            "last_step": summary, "autotune": tuned, "clocks": clk.summary(), "transport": transport_info,
-            # per network per step: auxvars, activities, setup pre-pass, persistent kernel
-            # (+ the transport schedule's launches)
-            "gpu_launches": len(graph_ms) * nsteps * (4 * len(members) + sum(
-                transport_launches(tr) for tr in stages if tr is not None))}
+    out = {"metric": "heterogeneous batched cell-solves/s, 8 networks, %d operator-split steps in one CUDA graph"
+           % nsteps, "value": value, "unit": UNIT, "replays": len(graph_ms),
+           "ms_per_step": g / nsteps,
+           "config": {"workload": "8 synthetic networks ncomp %s, 3*ncomp complexes, ncomp/2 kinetic minerals, "
+                                  "%d cells each, %s, T U[5,60] C" % (
+                                      C3_NCOMP, per, "structured grid per network, transport solve + reaction "
+                                      "each step, dt 1 d" if getattr(args, "transport", False)
+                                      else "per-cell dt log-U[1 h, 30 d]"),
+                      "graph_steps": nsteps, "concurrent_streams": bool(getattr(args, "concurrent", False)),
+                      "l2": "state > L2; reset D2D before each replay, outside the timed region"},
+           "graph_ms": g, "eager_ms_per_step": eager_ms,
+           "first_step": {"batched_ms": batched_first, "plain_ms": plain_first,
+                          "speedup_vs_plain_gpu": (plain_first / batched_first) if plain else None,
+                          "per_network": per_net},
+           "last_step": summary, "autotune": tuned, "clocks": clk.summary(), "transport": transport_info,
+           # per network per step: auxvars, activities, setup pre-pass, persistent kernel
+           # (+ the transport schedule's launches)
+           "gpu_launches": len(graph_ms) * nsteps * (4 * len(members) + sum(
+               transport_launches(tr) for tr in stages if tr is not None))}
+    del members, loop, start, s0
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_c3(args):
+    out = c3_measure(args, per=args.cells or 500_000, nsteps=args.graph_steps, replays=max(1, args.steps),
+                     plain=True, eager_steps=5)
+    line = {"metric": out.pop("metric"), "value": out.pop("value"), "unit": UNIT, "n_gpus": 1,
+            "steps": out["replays"], "warmup": 1, "ms_per_step": out.pop("ms_per_step"), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": out.pop("config"), "gpu_launches": out.pop("gpu_launches")}
+    line.update(out)
     print(json.dumps(line), flush=True)
 
 
@@ -668,20 +704,28 @@ def build_state_host(cfg_name, pool, nsample, seed=2026, nthreads=1):
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the C++ restatement of the reference's
+    RStep; the Fortran reference needs PETSc and a Fortran compiler, neither
+    present) on the host cores, on the same workload as our arm: the same
+    generator and cells, prepared by the oracle itself, the first step
+    untimed, then the second step timed over every cell."""
     import numpy as np  # noqa: F401
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     cfg = workload(args.config)
     cores = os.cpu_count() or 1
-    n = min(cfg["cells"], 20000 if args.config != "c1" else 1000)
-    # inputs: the same generator and cells as our arm, equilibrated by the
-    # CPU restatement itself; that restatement is then timed on the host cores
-    net, host, o = build_state_host("c2" if args.config == "c5" else args.config,
-                                    min(cfg["cells"], 200_000), n, nthreads=cores)
+    n = args.cells or cfg["cells"]
+    name = "c2" if args.config == "c5" else args.config
+    t0 = time.perf_counter()
+    net, host, o = build_state_host(name, n, n, nthreads=cores)
+    s1 = host.copy()
+    o.rstep(net, s1, cfg["dt"], nthreads=cores)  # the first (untimed) step
+    log("reference arm: %d cells prepared in %.1f s" % (n, time.perf_counter() - t0))
+    state_bytes = sum(v.nbytes for v in s1.a.values())
     vals = []
     for k in range(args.warmup + args.steps):
-        sub = host.subset(range(n))
+        sub = s1.copy()
         t = time.perf_counter()
         o.rstep(net, sub, cfg["dt"], nthreads=cores)
         el = time.perf_counter() - t
@@ -691,13 +735,12 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v if v else None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": cfg["workload"], "cells_per_step_sample": n},
+            "data": "synthetic", "config": c2_config(cfg, n, cfg["dt"], state_bytes),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d cells per step (bounded sample of the %d-cell workload)" % (
-                                 n, cfg["cells"])},
+                             "sample": "every cell of the %d-cell workload, each step (median of %d steps)" % (
+                                 n, len(vals))},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "reference is Fortran+PETSc (no Fortran compiler here); timed its C++ restatement"}
+            "note": "the reference is Fortran on PETSc (no Fortran compiler here); its C++ restatement timed"}
     print(json.dumps(line), flush=True)
 
 
@@ -720,6 +763,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-girt", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="c2: leave out the heterogeneous-mix measurement")
+    ap.add_argument("--c3-cells", type=int, default=0, help="c2: cells per network of the heterogeneous mix")
     ap.add_argument("--grid", default="128x128x64", help="global-implicit grid NXxNYxNZ")
     ap.add_argument("--launch", default="",
                     help="threads_per_block,blocks_per_sm,jac_in_shared[,lanes_per_cell] (skips tuning)")
@@ -768,7 +813,7 @@ def main():
                               "osrt_transport": tm,
                               "gpu_launches": 2 * args.steps}), flush=True)
         return
-    pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}
+    s0 = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}
     dt = cfg["dt"]
     tuned = None
     if args.launch:
@@ -784,12 +829,18 @@ def main():
         tuned = {"best": best, "top": table[:6]}
         log("autotune:", json.dumps(tuned))
 
-    # one instrumented step: iteration statistics for the flop count
-    stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
-    its_mean = stats["newton_iterations"] / ncells
-    # work-queue order for the timed steps: descending Newton count of the
-    # previous step (here the instrumented one), longest cells first
+    # The timed step is the second operator-split step of a time loop: the
+    # first step (untimed) takes the equilibrated state S0 to S1, and its
+    # per-cell Newton counts order the second step's work queue (descending,
+    # stiffest cells first) -- the only cost information a time loop has.
+    for k in s0:
+        dev.a[k].copy_(s0[k])
+    stats1 = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
     order = torch.argsort(dev.a["newton_its"].to(torch.int64), descending=True)
+    pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}  # S1, the timed step's input
+    # one instrumented run of the timed step: iteration statistics for the flop count
+    stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True, order=order)
+    its_mean = stats["newton_iterations"] / ncells
     for k in pristine:
         dev.a[k].copy_(pristine[k])
 
@@ -838,12 +889,22 @@ def main():
     p_total, p_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_PLAIN, max(1, min(args.steps, 3)), 1)
     plain_value = ncells * len(p_kern) / (p_total * 1e-3)
 
-    # roofline: FP64 pipe (algorithmic flops of the reference iteration)
+    # roofline: FP64 pipe.  achieved = the reference algorithm's flops per
+    # Newton iteration (flops.per_iteration) x the step's Newton iterations /
+    # kernel time; also on the kernel's own algorithm (flops.kernel_per_
+    # iteration: LDL^T, no scaling) and against the DFMA issue rate ncu states
+    # for this part (2 DFMA per SM per clock) at the clock sampled during the
+    # timed region
     f_it, tr_it = flops.per_iteration(net)
+    k_it, _ = flops.kernel_per_iteration(net)
     flops_per_launch = f_it * its_mean * ncells
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     peak = fp64_peak(abi.load(), sms)
     achieved = flops_per_launch / (kern_avg * 1e-3) / 1e12
+    achieved_own = k_it * its_mean * ncells / (kern_avg * 1e-3) / 1e12
+    clocks = clk.summary()
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    dfma_peak = 2 * 2 * sms * sm_mhz * 1e6 / 1e12
     state_bytes = sum(v.numel() * v.element_size() for v in dev.a.values())
     # DRAM bytes per cell-solve of the launched kernel measured by ncu on the
     # same workload at 200,000 cells, scaled to this launch:
@@ -857,6 +918,11 @@ def main():
                 "traffic_unit": "bytes per launch (ncu, scaled by cells)",
                 "peak_source": "FP64 DFMA probe (pf_bench_fp64_fma) measured in this run",
                 "flops_per_cell_solve": f_it * its_mean, "transcendentals_per_cell_solve": tr_it * its_mean,
+                "own_algorithm": {"flops_per_cell_solve": k_it * its_mean, "achieved": achieved_own,
+                                  "frac": achieved_own / peak if peak else None},
+                "dfma_issue_peak": {"tflops": dfma_peak, "sm_mhz": sm_mhz,
+                                    "frac": achieved / dfma_peak, "frac_own_algorithm": achieved_own / dfma_peak,
+                                    "probe_frac": peak / dfma_peak},
                 "hbm_gbs": state_bytes * 2 / (kern_avg * 1e-3) / 1e9}
 
     e2e = None
@@ -914,29 +980,37 @@ def main():
             host.a[k] = pristine[k].cpu().numpy()
         cpu = cpu_baseline(net, host, dt)
 
+    hetero = None
+    if args.config == "c2" and not args.no_c3:
+        host = None
+        for k in list(dev.a):
+            dev.a[k] = None
+        dev = None
+        torch.cuda.empty_cache()
+        hetero = c3_measure(args, per=args.c3_cells or 500_000, nsteps=args.graph_steps, replays=1,
+                            plain=True, eager_steps=0)
+        hetero.pop("clocks", None)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": cfg["workload"], "cells": ncells, "dt_s": dt,
-                           "parallelism": "replicas" if world > 1 else "single-gpu",
-                           "l2": ("state %.2f GB > L2 (129 MB); state reset D2D each step" % (state_bytes / 1e9))
-                           if state_bytes > 129e6 else
-                           ("state %.1f MB fits in L2, not flushed: this small case is launch-bound; reset D2D "
-                            "each step" % (state_bytes / 1e6)),
-                           "kernel": "batched persistent (PF_KERNEL_BATCHED)",
-                           "cell_order": "descending Newton count of the previous step",
-                           "launch": eng.launch_config(), "autotune": tuned},
+                "config": c2_config(cfg, ncells, dt, state_bytes),
+                "launch": {"kernel": "batched persistent (PF_KERNEL_BATCHED)", "config": eng.launch_config(),
+                           "autotune": tuned,
+                           "cell_order": "descending Newton count of the previous (untimed) step"},
                 "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
                 "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
+                "first_step": {"newton_its_per_cell": stats1["newton_iterations"] / ncells,
+                               "failed_cells": stats1["failed_cells"]},
                 "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},
                 "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),
                                   "kernel_ms": float(np.mean(nat_kern))},
                 "speedup_vs_plain_gpu": value / plain_value,
                 "adjoint": adjoint, "girt_assembly": girt, "constraint_equilibration": constraint,
-                "osrt_transport": transport,
+                "osrt_transport": transport, "heterogeneous": hetero,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk.summary(),
+                "clocks": clocks,
                 # per step: the setup pre-pass and the persistent kernel
                 "gpu_launches": 2 * args.steps}
         print(json.dumps(line), flush=True)

@@ -47,7 +47,9 @@ typedef enum PfStatus {
 enum {
   PF_CELL_OK = 0,
   PF_CELL_TOO_MANY_CUTS = 1, /* RStep: num_cuts > maximum_reaction_cuts      */
-  PF_CELL_NAN = 2            /* non-finite residual or activity coefficient  */
+  PF_CELL_NAN = 2,           /* non-finite residual or activity coefficient  */
+  PF_CELL_NOT_RUN = -1       /* pf_rstep_noalloc: the launch ended before it
+                                reached the cell (a launch-level wait ran out) */
 };
 
 /* reaction%act_coef_update_frequency, src/pflotran/reaction_aux.F90:392 */
@@ -341,17 +343,23 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
  * reference (PFLOTRAN's Fortran loop has no device memory to allocate).
  * Callers that cannot let a library call cudaMalloc -- a host model whose GPU
  * memory belongs to another framework's pool, or a coupled run with a fixed
- * device footprint -- use this instead of pf_rstep: the per-cell scratch lives in a fixed 32 MiB device
- * array inside the library (held on every device that loads it until exit),
- * and the call allocates nothing.  Limit: (ncomp + nsec + nmnrl) * ncells
- * <= 4,194,304; larger states return PF_ERR_TOO_LARGE (split them across
- * calls).  The first call on a device resolves the array's device address;
- * make that first call before any stream capture.  All calls share the one
- * array, so calls that overlap on the GPU (other streams, other threads)
- * race; serialise them.  No statistics are reduced (use the per-cell
- * status/newton_its arrays).
+ * device footprint -- use this instead of pf_rstep: the per-cell scratch
+ * lives in a fixed 32 MiB device array inside the library (held on every
+ * device that loads it until exit), and the call allocates nothing.  Limit:
+ * (ncomp + nsec + nmnrl) * ncells <= 4,194,304; larger states return
+ * PF_ERR_TOO_LARGE (split them across calls).  The first call on a device
+ * resolves the array's device address; make that first call before any
+ * stream capture.  All calls share the one array, so calls that overlap on
+ * the GPU (other streams, other threads) race; serialise them.  The launch
+ * configuration and option checks are pf_rstep's.  Before the launch every
+ * status entry is set to PF_CELL_NOT_RUN; the kernel overwrites it for each
+ * cell it finishes.  stats: optional, as for pf_rstep (the call then
+ * synchronises the stream and returns PF_ERR_TIMEOUT or PF_CELL_FAILURES as
+ * pf_rstep does; the counters are read through the network's own pinned
+ * buffer, nothing is allocated).
  */
-int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream);
+int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream,
+                         PfStepStats* stats);
 
 /* ----------------------------------------------------------------- adjoint */
 /* Largest number of RStep substeps (dt cuts) whose converged states the

@@ -493,9 +493,8 @@ int32_t pf_internal_network_view(PfNetwork* net, DevNet* dev, PfLaunchConfig* cf
   return PF_OK;
 }
 
-int32_t pf_internal_validate_state(PfNetwork* net, const PfCellState* state) {
-  return validate_state(net, state);
-}
+int32_t pf_internal_check_rstep(PfNetwork* net, const PfCellState* state, double dt);
+int32_t pf_internal_read_step_stats(PfNetwork* net, int64_t ncells, void* stream, PfStepStats* stats);
 
 int32_t pf_network_destroy(PfNetwork* net) {
   if (!net) return PF_ERR_INVALID;
@@ -530,6 +529,16 @@ int32_t pf_network_set_options(PfNetwork* net, const PfOptions* opts) {
                             (net->dev.nm > 0 && !(net->dev.flags & NETF_MNRL_LOGKCOEF))))
     return PF_ERR_INVALID;
   net->dev.o = *opts;
+  // the launch configuration was chosen for the old options: a group of
+  // lanes per cell that the new ones rule out (e.g. the linear formulation)
+  // goes back to one lane per cell, or to the default for the new options
+  const PfLaunchConfig& c = net->launch;
+  const bool ok = c.lanes_per_cell > 1 ? group_supported(net->dev, c.lanes_per_cell) : lane_supported(net->dev);
+  if (!ok) {
+    const bool lane_cfg = net->launch_lane.lanes_per_cell <= 1 && lane_supported(net->dev) &&
+                          batched_smem_bytes(net->dev, net->launch_lane) <= 227u * 1024u;
+    net->launch = lane_cfg ? net->launch_lane : default_launch(net->dev);
+  }
   return PF_OK;
 }
 
@@ -587,6 +596,10 @@ static int check_rstep(PfNetwork* net, const PfCellState* state, double dt, int3
   return PF_OK;
 }
 
+int32_t pf_internal_check_rstep(PfNetwork* net, const PfCellState* state, double dt) {
+  return check_rstep(net, state, dt, PF_KERNEL_BATCHED);
+}
+
 // zero counters[0..8) and launch the step on stream s ([0] is the work queue;
 // scratch: the batched kernel's per-cell set-up values for these cells)
 static int enqueue_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel,
@@ -599,6 +612,24 @@ static int enqueue_rstep(PfNetwork* net, const PfCellState* state, double dt, in
     lr = launch_rstep_batched(net->dev, *state, dt, net->launch, net->num_sms, scratch, counters, counters + 1,
                               s);
   return lr != 0 ? PF_ERR_CUDA : PF_OK;
+}
+
+// Synchronises s, copies the counters of the last step into the pinned mirror
+// and fills stats: PF_ERR_TIMEOUT when a launch-level wait ran out,
+// PF_CELL_FAILURES when cells failed, else PF_OK.
+static int read_step_stats(PfNetwork* net, int64_t ncells, cudaStream_t s, PfStepStats* stats) {
+  cudaError_t e = cudaMemcpyAsync(net->h_counters, net->d_counters, 8 * sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return PF_ERR_CUDA;
+  const unsigned long long* h = net->h_counters;
+  stats->cells = ncells;
+  stats->newton_iterations = (int64_t)h[1];
+  stats->failed_cells = (int64_t)h[2];
+  stats->max_newton_iterations = (int32_t)h[4];
+  stats->max_substeps = (int32_t)h[5];
+  if (h[3]) return PF_ERR_TIMEOUT;
+  return stats->failed_cells ? PF_CELL_FAILURES : PF_OK;
 }
 
 int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t kernel, void* stream,
@@ -617,19 +648,11 @@ int32_t pf_rstep(PfNetwork* net, const PfCellState* state, double dt, int32_t ke
   rc = enqueue_rstep(net, state, dt, kernel, net->d_counters, net->d_scratch, s);
   if (rc) return rc;
   if (!stats) return PF_OK;
-  cudaError_t e;
-  e = cudaMemcpyAsync(net->h_counters, net->d_counters, 8 * sizeof(unsigned long long),
-                      cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return PF_ERR_CUDA;
-  const unsigned long long* h = net->h_counters;
-  stats->cells = state->ncells;
-  stats->newton_iterations = (int64_t)h[1];
-  stats->failed_cells = (int64_t)h[2];
-  stats->max_newton_iterations = (int32_t)h[4];
-  stats->max_substeps = (int32_t)h[5];
-  if (h[3]) return PF_ERR_TIMEOUT;
-  return stats->failed_cells ? PF_CELL_FAILURES : PF_OK;
+  return read_step_stats(net, state->ncells, s, stats);
+}
+
+int32_t pf_internal_read_step_stats(PfNetwork* net, int64_t ncells, void* stream, PfStepStats* stats) {
+  return read_step_stats(net, ncells, (cudaStream_t)stream, stats);
 }
 
 int32_t pf_update_auxvars(PfNetwork* net, const PfCellState* state, int32_t update_activity_coefs,

@@ -112,6 +112,10 @@ size_t batched_scratch_doubles(const DevNet& net, int64_t ncells) {
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
                          int num_sms, double* scratch, unsigned long long* queue, unsigned long long* counters,
                          cudaStream_t stream, const PfAdjointArgs* adj, double* adj_store) {
+  const bool grp = cfg.lanes_per_cell > 1 && (!adj || adj_store);
+  // a group configuration the network's current options rule out (the group
+  // kernel reads neither the linear formulation nor the other refused modes)
+  if (grp && !group_supported(net, cfg.lanes_per_cell)) return (int)cudaErrorInvalidConfiguration;
   {
     const int tpb = 128;
     const int64_t blocks = (st.ncells + tpb - 1) / tpb;
@@ -119,7 +123,7 @@ int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, co
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
   }
-  if (cfg.lanes_per_cell > 1 && (!adj || adj_store))
+  if (grp)
     return launch_rstep_group(net, net.grp, st, dt, cfg, num_sms, scratch, queue, counters, stream, adj,
                               adj_store);
   switch (net.n) {

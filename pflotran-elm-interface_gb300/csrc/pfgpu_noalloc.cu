@@ -42,32 +42,44 @@ int scratch_for_current_device(double** out) {
 }
 }  // namespace
 
-// Helpers from pfgpu_api.cu (the network's resident launch state).
+// Helpers from pfgpu_api.cu (the network's resident launch state, the
+// argument checks of pf_rstep and its read-back of the step counters into the
+// network's pinned mirror).
 extern "C" int32_t pf_internal_network_view(PfNetwork* net, pfgpu::DevNet* dev, PfLaunchConfig* cfg,
                                             int* num_sms, unsigned long long** counters);
-extern "C" int32_t pf_internal_validate_state(PfNetwork* net, const PfCellState* state);
+extern "C" int32_t pf_internal_check_rstep(PfNetwork* net, const PfCellState* state, double dt);
+extern "C" int32_t pf_internal_read_step_stats(PfNetwork* net, int64_t ncells, void* stream, PfStepStats* stats);
 
-extern "C" int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream) {
+extern "C" int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream,
+                                    PfStepStats* stats) {
   using namespace pfgpu;
-  int rc = pf_internal_validate_state(net, state);
+  int rc = pf_internal_check_rstep(net, state, dt);
   if (rc) return rc;
-  if (!(dt > 0.0) && !state->dt_cell) return PF_ERR_INVALID;
   DevNet dev;
   PfLaunchConfig cfg;
   int sms = 0;
   unsigned long long* counters = nullptr;
   rc = pf_internal_network_view(net, &dev, &cfg, &sms, &counters);
   if (rc) return rc;
-  if (!batched_supported(dev)) return PF_ERR_UNSUPPORTED;
-  if (state->ncells == 0) return PF_OK;
+  if (state->ncells == 0) {
+    if (stats) *stats = PfStepStats{};
+    return PF_OK;
+  }
   if (batched_scratch_doubles(dev, state->ncells) > (size_t)PF_NOALLOC_SCRATCH_DOUBLES) return PF_ERR_TOO_LARGE;
   double* scratch = nullptr;
   rc = scratch_for_current_device(&scratch);
   if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   // the work-queue counter and reduction slots must start at zero; the
-  // scratch needs no clearing (the setup pre-pass writes every value it reads)
+  // scratch needs no clearing (the setup pre-pass writes every value it reads
+  // before the step kernel reads it)
   if (cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess) return PF_ERR_CUDA;
+  // every byte 0xFF: status PF_CELL_NOT_RUN (-1) until the kernel finishes the
+  // cell, so a launch that gave up early (a table-staging wait that ran out)
+  // shows in the status array even without stats
+  if (state->status && cudaMemsetAsync(state->status, 0xFF, (size_t)state->ncells * sizeof(int32_t), s) != cudaSuccess)
+    return PF_ERR_CUDA;
   if (launch_rstep_batched(dev, *state, dt, cfg, sms, scratch, counters, counters + 1, s) != 0) return PF_ERR_CUDA;
-  return PF_OK;
+  if (!stats) return PF_OK;
+  return pf_internal_read_step_stats(net, state->ncells, stream, stats);
 }

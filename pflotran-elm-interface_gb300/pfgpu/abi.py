@@ -20,6 +20,7 @@ PF_ERR_TIMEOUT = -5
 PF_CELL_OK = 0
 PF_CELL_TOO_MANY_CUTS = 1
 PF_CELL_NAN = 2
+PF_CELL_NOT_RUN = -1
 
 PF_ACT_COEF_OFF = 0
 PF_ACT_COEF_TIMESTEP = 1
@@ -238,7 +239,7 @@ SIGNATURES = {
     "pf_transport_enqueue": (C.c_int32, [_P, C.POINTER(PfTransportArgs), C.c_int32, C.c_int32, _P]),
     "pf_transport_read_stats": (C.c_int32, [_P, C.c_double, _P, C.POINTER(PfTransportStats)]),
     "pf_girt_assemble": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(PfGirtArgs), _P]),
-    "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P]),
+    "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P, C.POINTER(PfStepStats)]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
                                   C.POINTER(PfStepStats)]),
     "pf_equilibrate_constraint": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(C.c_int32),

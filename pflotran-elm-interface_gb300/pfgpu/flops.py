@@ -61,6 +61,47 @@ def per_iteration(net, mineral_active=None):
     return f, tr
 
 
+def kernel_per_iteration(net):
+    """(flops, transcendentals) of one Newton iteration of the batched step
+    kernels as they run (log formulation, LDL^T, csrc/pfgpu_group.cuh and
+    pfgpu_batched.cuh), counted from their loops with the same units:
+    power table (a, a^2, and 1/a, 1/a^2 for species with a negative
+    coefficient), product-form complexes (one multiply per species, no
+    exp), the minerals' Q/K and rate law, the residual rows, the lower
+    triangle of the symmetric Jacobian entry by entry, LDL^T with the
+    forward solve alongside, D^-1, the backward solve, and the update (one
+    exp per species).  No row or column scaling and no pivot search: the
+    kernel's own algorithm is about half the reference's factorisation
+    work, so a roofline on these counts is lower than one on
+    per_iteration's."""
+    n = net.ncomp
+    s = [int(net.sec_nspec[i]) for i in range(net.nsec)]
+    t = [int(net.mnrl_nspec[m]) for m in range(net.nmnrl)]
+    neg = set()
+    for i in range(net.nsec):
+        for k in range(s[i]):
+            if net.sec_stoich[i, k] < 0:
+                neg.add(int(net.sec_spec[i, k]))
+    for m in range(net.nmnrl):
+        for k in range(t[m]):
+            if net.mnrl_stoich[m, k] < 0:
+                neg.add(int(net.mnrl_spec[m, k]))
+    f = 3                                   # a_acc, b_tot
+    f += 2 * n + 2 * len(neg)               # power table
+    f += sum(s)                             # complexes: K' prod a^nu
+    f += sum(ti + 12 for ti in t)           # minerals: Q/K, affinity, rate, dIm/dlnQ
+    f += 2 * sum(s) + n + 3 * n + 4 * n     # rows: sum nu s, a_acc *, totals, residual
+    f += 2 * sum(t) + 2 * n                 # mineral residual terms, |r|^2
+    f += sum(si * (si + 1) for si in s)     # entries: complexes' nu_i nu_j s
+    f += sum(ti * (ti + 1) for ti in t)     # entries: minerals' nu_i nu_j f
+    f += n + n * (n + 1) // 2               # diagonal m_i, a_acc * entry
+    f += 1 + n                              # norm
+    f += n + 3 * n * (n - 1) // 2 + (n - 1) * n * (n + 1) // 3  # LDL^T + forward solve
+    f += n + n * (n - 1)                    # D^-1, backward solve
+    f += 4 * n                              # update and relative-change test
+    return f, n
+
+
 def girt_per_cell(net, offdiag_blocks: float):
     """FP64 flops (FMA = 2) and transcendental calls per cell of one
     global-implicit assembly (pf_girt_assemble): RTotal (secondary

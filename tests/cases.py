@@ -61,6 +61,12 @@ def case(oracle, name, tight=False):
     return net, st.copy()
 
 
+# converged tolerances: every Newton solve runs to rounding level (relative
+# change below 1e-12, residual tests off, up to 100 iterations), so the result
+# does not depend on where a loose stopping test happened to fire
+CONVERGED = dict(max_relative_change_tolerance=1e-12, max_residual_tolerance=1e-300,
+                 max_rel_residual_tolerance=1e-300, maximum_reaction_iterations=100)
+
 CASE_DT = {"calcite": 3600.0, "random12": 86400.0, "random12raw": 86400.0}
 CASE_DT.update({"hetero%d" % n: 86400.0 for n in (4, 6, 8, 10, 12, 16, 20, 24)})
 HETERO = (4, 6, 8, 10, 12, 16, 20, 24)

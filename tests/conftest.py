@@ -18,3 +18,13 @@ def pytest_configure(config):
 def oracle():
     from oracle.oracle import Oracle
     return Oracle()
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    """Prints the per-case parity report (tests/parity.py) collected by the
+    GPU parity tests, so that it is part of the session's output."""
+    mod = sys.modules.get("parity")
+    if mod is None or not getattr(mod, "REPORT", None):
+        return
+    for line in mod.format_report():
+        terminalreporter.write_line(line)

@@ -1,8 +1,8 @@
 """Generate the known-answer fixtures in tests/golden/ from the reference's own
 regression decks, thermodynamic databases and gold files.
 
-Runs only where the reference tree is mounted (default /root/reference; pass
-another root as argv[1]).  The tests read the JSON this writes and never the
+Runs only where the reference tree is mounted: pass its root as argv[1] or in
+PFGPU_REFERENCE_ROOT.  The tests read the JSON this writes and never the
 reference tree itself.
 
 Sources (paths within fmyuan/pflotran-elm-interface):
@@ -18,7 +18,7 @@ import re
 import shlex
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = os.environ.get("PFGPU_REFERENCE_ROOT", "")
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
                                 "pflotran-elm-interface_gb300"))
 BATCH = os.path.join(ROOT, "regression_tests", "ascem", "batch")
@@ -203,4 +203,9 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 1:
+        ROOT = sys.argv[1]
+        BATCH = os.path.join(ROOT, "regression_tests", "ascem", "batch")
+    if not ROOT:
+        sys.exit("usage: make_golden.py <root of the reference tree>  (or set PFGPU_REFERENCE_ROOT)")
     main()

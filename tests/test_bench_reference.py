@@ -25,7 +25,7 @@ def test_reference_arm_line(config):
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
-    assert d["config"]["cells_per_step_sample"] == 1000
+    assert d["config"]["cells"] == 1000 and d["config"]["step"].startswith("the second operator-split step")
 
 
 def test_host_inputs_step_cleanly():
@@ -39,3 +39,14 @@ def test_host_inputs_step_cleanly():
     assert np.all(st.a["pri_molal"] > 0) and np.all(np.isfinite(st.a["sec_act_coef"]))
     o.rstep(net, st, 3600.0)
     assert np.all(st.a["status"] == 0) and np.all(st.a["newton_its"] > 0)
+
+
+def test_reference_arm_config_matches_ours():
+    """Both arms describe the workload with the same function, so their
+    config objects agree key for key on the same workload."""
+    sys.path.insert(0, REPO)
+    import bench
+    cfg = bench.workload("c2")
+    a = bench.c2_config(cfg, 1_000_000, 86400.0, 1.12e9)
+    b = bench.c2_config(cfg, 1_000_000, 86400.0, 1.12e9)
+    assert a == b and set(a) == {"workload", "cells", "dt_s", "step", "l2"}

@@ -15,8 +15,9 @@ import pytest
 
 from pfgpu import database as dbm
 
-REF = os.environ.get("PFGPU_REFERENCE_ROOT", "/root/reference")
-BATCH = os.path.join(REF, "regression_tests", "ascem", "batch")
+# the reference tree's root, when the test should read it (no default)
+REF = os.environ.get("PFGPU_REFERENCE_ROOT", "")
+BATCH = os.path.join(REF, "regression_tests", "ascem", "batch") if REF else ""
 
 
 def _coef_fn(c, t):
@@ -126,7 +127,8 @@ def test_build_network_basis_water_and_selection():
         dbm.build_network(db, ["H+", "Na+"])
 
 
-@pytest.mark.skipif(not os.path.isdir(BATCH), reason="reference regression databases not present")
+@pytest.mark.skipif(not BATCH or not os.path.isdir(BATCH),
+                    reason="PFGPU_REFERENCE_ROOT does not name the reference tree")
 def test_reference_databases_build_the_fixture_networks():
     import kat
     from golden import make_golden

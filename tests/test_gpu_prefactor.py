@@ -8,7 +8,7 @@ import pytest
 
 import cases
 from pfgpu import abi
-from test_gpu_parity import compare
+import parity
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -34,15 +34,10 @@ def test_plain_rstep_with_prefactors_matches_oracle(oracle, logf):
     dev = st.to("cuda")
     eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_PLAIN)
     got = dev.numpy()
-    errs, flips, same, outliers, self_flips, self_out = compare(
-        net, ref, got, "prefactors/plain/%s" % ("log" if logf else "linear"), perts)
-    slack = max(2, 0.01 * (int(same.sum()) + flips))
-    assert same.sum() > 0.9 * st.ncells, same.sum()
-    assert flips <= 2 * self_flips + slack, (flips, self_flips)
-    assert outliers <= 2 * self_out + slack, (outliers, self_out)
-    for k, v in errs.items():
-        assert v < REL, (k, v, errs)
-    r = ref.a["mnrl_rate"][:, same]
+    label = "prefactors/plain/%s" % ("log" if logf else "linear")
+    entry, ok = parity.compare(net, ref, got, 3600.0, label, perts)
+    parity.check(entry, label, min_compared=int(0.9 * st.ncells))
+    r = ref.a["mnrl_rate"][:, ok]
     assert all((r[m] > 0).any() and (r[m] < 0).any() for m in range(net.nmnrl))
 
 

@@ -9,7 +9,7 @@ import pytest
 
 import cases
 from pfgpu import abi
-from test_gpu_parity import compare
+import parity
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -52,15 +52,11 @@ def test_rstep_with_water_activity(oracle, kernel, freq):
     dev = st.to("cuda")
     eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED)
     got = dev.numpy()
-    errs, flips, same, outliers, self_flips, self_out = compare(net, ref, got, "water/%s/%d" % (kernel, freq), perts)
-    slack = max(2, 0.01 * (int(same.sum()) + flips))
-    assert same.sum() > 0.9 * st.ncells, same.sum()
-    assert flips <= 2 * self_flips + slack, (flips, self_flips)
-    assert outliers <= 2 * self_out + slack, (outliers, self_out)
-    for k, v in errs.items():
-        assert v < REL, (k, v, errs)
+    label = "water/%s/%d" % (kernel, freq)
+    entry, ok = parity.compare(net, ref, got, 3600.0, label, perts)
+    parity.check(entry, label, min_compared=int(0.9 * st.ncells))
     if freq == abi.PF_ACT_COEF_NEWTON_ITER:
-        np.testing.assert_allclose(got.a["ln_act_h2o"][same], ref.a["ln_act_h2o"][same], rtol=1e-10, atol=0)
+        np.testing.assert_allclose(got.a["ln_act_h2o"][ok], ref.a["ln_act_h2o"][ok], rtol=1e-10, atol=0)
 
 
 def test_water_activity_each_iteration_refused_by_the_fast_kernels(oracle):
