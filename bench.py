@@ -240,6 +240,35 @@ def time_steps(eng, dev, pristine, dt, kernel, steps, warmup, order=None):
     return total_ms, kern_ms
 
 
+def adjoint_measure(eng, dev, start, dt, order, reps, forward_ms):
+    """pf_adjoint of one step from `start` (loss sum w*(T_final - target)^2,
+    w ~ U[0,1], target = the forward output with 5 % lognormal noise): its
+    time, which includes the recomputed forward solve, over forward_ms."""
+    import numpy as np
+    import torch
+    for k in start:
+        dev.a[k].copy_(start[k])
+    eng.rstep(dev, dt, stats=False, order=order)
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    w = torch.rand(dev.a["total"].shape, dtype=torch.float64, device="cuda", generator=gen)
+    tgt = dev.a["total"] * torch.exp(0.05 * torch.randn(dev.a["total"].shape, dtype=torch.float64,
+                                                         device="cuda", generator=gen))
+    adj_ms = []
+    for k_ in range(1 + reps):
+        for k in start:
+            dev.a[k].copy_(start[k])
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        gout = eng.adjoint(dev, dt, weight=w, target=tgt, order=order)
+        a1.record()
+        torch.cuda.synchronize()
+        if k_:
+            adj_ms.append(a0.elapsed_time(a1))
+    return {"ms": float(np.mean(adj_ms)), "forward_ms": forward_ms,
+            "ratio_to_forward": float(np.mean(adj_ms)) / forward_ms,
+            "cells_with_gradient": int((gout["adj_status"] == 0).sum()), "loss": float(gout["loss"][0])}
+
+
 def cpu_baseline(net, host_state, dt, budget_s=15.0):
     """The oracle (C++ restatement of the reference, OpenMP over cells) on a
     bounded sample of the same cells, all host cores."""
@@ -833,6 +862,12 @@ def main():
     # first step (untimed) takes the equilibrated state S0 to S1, and its
     # per-cell Newton counts order the second step's work queue (descending,
     # stiffest cells first) -- the only cost information a time loop has.
+    # the first step itself, from the equilibrated state, in natural order (no
+    # cost information exists yet), batched and plain
+    nrep = max(1, min(args.steps, 3))
+    f1_total, f1_kern = time_steps(eng, dev, s0, dt, abi.PF_KERNEL_BATCHED, nrep, 1)
+    p1_total, p1_kern = time_steps(eng, dev, s0, dt, abi.PF_KERNEL_PLAIN, 1, 1)
+    adjoint1 = adjoint_measure(eng, dev, s0, dt, None, nrep, float(np.mean(f1_kern)))
     for k in s0:
         dev.a[k].copy_(s0[k])
     stats1 = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
@@ -860,30 +895,9 @@ def main():
     value = world * ncells * args.steps / (total_ms * 1e-3)
     kern_avg = float(np.mean(kern_ms))
 
-    # adjoint of the step (loss sum w*(T_final - target)^2, w ~ U[0,1], target
-    # = forward output with 5 % lognormal noise): time of pf_adjoint, which
-    # recomputes the forward solve, over the forward step
-    for k in pristine:
-        dev.a[k].copy_(pristine[k])
-    eng.rstep(dev, dt, stats=False, order=order)
-    gen = torch.Generator(device="cuda").manual_seed(4)
-    w = torch.rand(dev.a["total"].shape, dtype=torch.float64, device="cuda", generator=gen)
-    tgt = dev.a["total"] * torch.exp(0.05 * torch.randn(dev.a["total"].shape, dtype=torch.float64,
-                                                         device="cuda", generator=gen))
-    adj_ms = []
-    for k_ in range(1 + max(1, min(args.steps, 3))):
-        for k in pristine:
-            dev.a[k].copy_(pristine[k])
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record()
-        gout = eng.adjoint(dev, dt, weight=w, target=tgt, order=order)
-        a1.record()
-        torch.cuda.synchronize()
-        if k_:
-            adj_ms.append(a0.elapsed_time(a1))
-    adjoint = {"ms": float(np.mean(adj_ms)), "ratio_to_forward": float(np.mean(adj_ms)) / kern_avg,
-               "cells_with_gradient": int((gout["adj_status"] == 0).sum()),
-               "loss": float(gout["loss"][0])}
+    # adjoint of the timed step
+    adjoint = adjoint_measure(eng, dev, pristine, dt, order, nrep, kern_avg)
+    adjoint["first_step"] = adjoint1
 
     # plain one-thread-per-cell form, same inputs
     p_total, p_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_PLAIN, max(1, min(args.steps, 3)), 1)
@@ -1001,7 +1015,14 @@ def main():
                            "cell_order": "descending Newton count of the previous (untimed) step"},
                 "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
                 "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
-                "first_step": {"newton_its_per_cell": stats1["newton_iterations"] / ncells,
+                "first_step": {"what": "the first step from the equilibrated state, natural queue order",
+                               "value": ncells * len(f1_kern) / (f1_total * 1e-3),
+                               "kernel_ms": float(np.mean(f1_kern)),
+                               "plain_gpu": {"value": ncells * len(p1_kern) / (p1_total * 1e-3),
+                                             "kernel_ms": float(np.mean(p1_kern))},
+                               "speedup_vs_plain_gpu": float(np.mean(p1_kern)) / float(np.mean(f1_kern)),
+                               "newton_its_per_cell": stats1["newton_iterations"] / ncells,
+                               "max_newton_its": stats1["max_newton_iterations"],
                                "failed_cells": stats1["failed_cells"]},
                 "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},
                 "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),

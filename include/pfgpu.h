@@ -473,19 +473,45 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
 /* ------------------------------------------------- operator-split transport */
 /*
  * The transport half of an operator-split step on a structured grid
- * nx*ny*nz (cell index i + nx*(j + ny*k)), zero-flux outer boundaries, no
- * sources: replaces the transport solve of PMCSubsurfaceOSRTStepDT
- * (src/pflotran/pmc_subsurface_osrt.F90:259-330) -- the fixed accumulation
- * psv*T_k, the matrix of RTCalculateTransportMatrix
+ * nx*ny*nz (cell index i + nx*(j + ny*k)): replaces the transport solve of
+ * PMCSubsurfaceOSRTStepDT (src/pflotran/pmc_subsurface_osrt.F90:259-330) --
+ * the fixed accumulation psv*T_k, the matrix of RTCalculateTransportMatrix
  * (reactive_transport.F90:1469-1703) with TFluxCoef (transport.F90:495-565)
  * and the harmonic-mean dispersion of TDispersion, the right-hand side
- * psv*T_k/dt of RTCalculateRHS_t1, and one linear solve per component
- * (all components share the matrix).  Solved on the device, all components
- * at once, by mixed-precision iterative refinement (FP64 residual and
- * update, FP32 Jacobi-preconditioned BiCGStab corrections) from T_k to
+ * psv*T_k/dt of RTCalculateRHS_t1 (:1239-1465), and one linear solve per
+ * component (all components share the matrix).  Boundary conditions on the
+ * six outer faces and sources/sinks follow the boundary and source loops
+ * of both routines (TDispersionBC transport.F90:236-374, TFluxCoefBC
+ * :569-609, TSrcSinkCoef :613-673); a face without a condition is closed
+ * (zero flux).  Solved on the device, all components at once, by
+ * mixed-precision iterative refinement (FP64 residual and update, FP32
+ * Jacobi-preconditioned BiCGStab corrections) from T_k to
  * ||b - A x|| <= rtol ||b|| in FP64.  No counterpart in the reference for
  * the solver choice (PETSc KSP there).
  */
+/* the outer faces, in this order; a face's cells are indexed j + ny*k on
+ * the x faces, i + nx*k on the y faces, i + nx*j on the z faces */
+enum { PF_FACE_XM = 0, PF_FACE_XP = 1, PF_FACE_YM = 2, PF_FACE_YP = 3, PF_FACE_ZM = 4, PF_FACE_ZP = 5 };
+/* transport boundary condition types (tran_condition%itype as TDispersionBC
+ * and TFluxCoefBC treat them); the boundary connection's distance is half
+ * the cell's width, its area the face's */
+enum {
+  PF_BC_ZERO_FLUX = 0,              /* no boundary connection (closed face)       */
+  PF_BC_DIRICHLET = 1,              /* DIRICHLET_BC: advection in from, and
+                                       dispersion against, the boundary totals    */
+  PF_BC_DIRICHLET_ZERO_GRADIENT = 2, /* DIRICHLET_ZERO_GRADIENT_BC: as Dirichlet
+                                       where the flux enters, advection only where
+                                       it leaves                                  */
+  PF_BC_ZERO_GRADIENT = 3           /* ZERO_GRADIENT_BC (also NEUMANN_BC and
+                                       CONCENTRATION_SS): advection only          */
+};
+/* source/sink types (tran_src_sink_type of TSrcSinkCoef) */
+enum {
+  PF_SRC_VOLUMETRIC = 0,  /* q m^3/s: injection carries src_total in, extraction
+                             removes the cell's water                              */
+  PF_SRC_EQUILIBRIUM = 1, /* EQUILIBRIUM_SS: relaxation at 1e-3 L/s toward src_total */
+  PF_SRC_MASS_RATE = 2    /* MASS_RATE_SS: src_total is a rate, mol/s               */
+};
 typedef struct PfTransportArgs {
   int32_t nx, ny, nz, ncomp;
   double dx, dy, dz;                 /* m */
@@ -502,6 +528,20 @@ typedef struct PfTransportArgs {
   double* total;                     /* [ncomp][ncells] mol/L: in T_k, out T_k+1 */
   double rtol;                       /* relative residual tolerance */
   int32_t max_iterations;
+  /* boundary conditions, per face (all PF_BC_ZERO_FLUX: a closed box) */
+  int32_t bc_type[6];                /* PF_BC_*                                      */
+  const double* bc_q[6];             /* [face cells] Darcy flux through the face, m/s,
+                                        positive into the domain; NULL = no flow      */
+  const double* bc_total[6];         /* [ncomp][face cells] totals of the boundary
+                                        water, mol/L (rt_auxvars_bc%total)           */
+  double bc_saturation[6];           /* saturation at the boundary
+                                        (global_auxvars_bc%sat)                      */
+  /* sources and sinks (source_sink_list), applied in array order */
+  int32_t nsrc;
+  const int32_t* src_cell;           /* [nsrc] cell index                            */
+  const int32_t* src_type;           /* [nsrc] PF_SRC_*                              */
+  const double* src_q;               /* [nsrc] m^3/s, positive: injection            */
+  const double* src_total;           /* [ncomp][nsrc] mol/L (mol/s: PF_SRC_MASS_RATE) */
 } PfTransportArgs;
 
 typedef struct PfTransportStats {

@@ -164,6 +164,51 @@ class Oracle:
             raise RuntimeError("oracle_transport_matrix: %d" % rc)
         return vals
 
+    def transport_bc_terms(self, grid, porosity, saturation, volume, ncomp, bc=None, sources=None):
+        """Boundary and source terms of the operator-split transport system
+        (the boundary and source/sink loops of RTCalculateTransportMatrix
+        and RTCalculateRHS_t1): returns (diag_add [N], rhs_add [ncomp, N]).
+        bc: dict(type=[6 ints], q=[6 arrays or None], total=[6 arrays
+        (ncomp, face cells) or None], sat=[6 floats]), faces x-, x+, y-, y+,
+        z-, z+; sources: dict(cell, type, q, total (ncomp, nsrc)) or None."""
+        f = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+        gi = np.array([grid["nx"], grid["ny"], grid["nz"]], np.int32)
+        gd = f([grid["dx"], grid["dy"], grid["dz"], grid["diffusion"], grid["tortuosity"], grid["dispersivity"]])
+        N = int(gi.prod())
+        por, sat, vol = f(porosity), f(saturation), f(volume)
+        bc = bc or dict(type=[0] * 6, q=[None] * 6, total=[None] * 6, sat=[1.0] * 6)
+        keep = []
+        dp = C.POINTER(C.c_double)
+        qptr = (dp * 6)()
+        tptr = (dp * 6)()
+        for k in range(6):
+            for arr, dst in ((bc["q"][k], qptr), (bc["total"][k], tptr)):
+                if arr is not None:
+                    a = f(arr)
+                    keep.append(a)
+                    dst[k] = a.ctypes.data_as(dp)
+        btype = np.ascontiguousarray(bc["type"], np.int32)
+        bsat = f(bc["sat"])
+        src = sources or dict(cell=np.zeros(0), type=np.zeros(0), q=np.zeros(0), total=np.zeros((ncomp, 0)))
+        scell = np.ascontiguousarray(src["cell"], np.int32)
+        stype = np.ascontiguousarray(src["type"], np.int32)
+        sq = f(src["q"])
+        stot = f(src["total"])
+        diag = np.zeros(N)
+        rhs = np.zeros((ncomp, N))
+        ip = C.POINTER(C.c_int32)
+        P = lambda a: a.ctypes.data_as(dp)  # noqa: E731
+        fn = self.lib.oracle_transport_bc_terms
+        fn.argtypes = [ip, dp, dp, dp, dp, C.c_int32, ip, C.POINTER(dp), C.POINTER(dp), dp, C.c_int32, ip, ip, dp,
+                       dp, dp, dp]
+        fn.restype = C.c_int
+        rc = fn(gi.ctypes.data_as(ip), P(gd), P(por), P(sat), P(vol), int(ncomp), btype.ctypes.data_as(ip),
+                qptr, tptr, P(bsat), int(scell.size), scell.ctypes.data_as(ip), stype.ctypes.data_as(ip), P(sq),
+                P(stot), P(diag), P(rhs))
+        if rc:
+            raise RuntimeError("oracle_transport_bc_terms: %d" % rc)
+        return diag, rhs
+
     def count_rstep(self, net, state, dt):
         """RStep of every cell with counted arithmetic (single thread; the
         state is advanced).  Returns per-cell (flops, transcendental calls,

@@ -318,4 +318,37 @@ int oracle_transport_matrix(const int32_t* grid_i, const double* grid_d, const d
   return PF_OK;
 }
 
+// Boundary and source terms of the operator-split transport system (see
+// transport_bc_terms): bc_type[6], bc_q / bc_total as 6 pointers each (NULL
+// where a face has none), bc_sat[6]; sources as arrays of nsrc; outputs
+// diag_add[N] and rhs_add[ncomp][N].
+int oracle_transport_bc_terms(const int32_t* grid_i, const double* grid_d, const double* porosity,
+                              const double* saturation, const double* volume, int32_t ncomp, const int32_t* bc_type,
+                              const double* const* bc_q, const double* const* bc_total, const double* bc_sat,
+                              int32_t nsrc, const int32_t* src_cell, const int32_t* src_type, const double* src_q,
+                              const double* src_total, double* diag_add, double* rhs_add) {
+  GirtGrid g{grid_i[0], grid_i[1], grid_i[2], grid_d[0], grid_d[1], grid_d[2], nullptr, nullptr, nullptr,
+             grid_d[3], grid_d[4], grid_d[5]};
+  const int64_t N = (int64_t)g.nx * g.ny * g.nz;
+  std::vector<Cell> cells(N);
+  for (int64_t i = 0; i < N; ++i) {
+    cells[i].porosity = porosity[i];
+    cells[i].sat = saturation[i];
+    cells[i].volume = volume[i];
+  }
+  TransportBC bc{};
+  for (int f = 0; f < 6; ++f) {
+    bc.type[f] = bc_type[f];
+    bc.q[f] = bc_q[f];
+    bc.total[f] = bc_total[f];
+    bc.sat[f] = bc_sat[f];
+    if (bc.type[f] != 0 && !bc.total[f]) return PF_ERR_INVALID;
+  }
+  TransportSrc src{nsrc, src_cell, src_type, src_q, src_total};
+  for (int s = 0; s < nsrc; ++s)
+    if (src_cell[s] < 0 || src_cell[s] >= N) return PF_ERR_INVALID;
+  transport_bc_terms(cells.data(), g, ncomp, bc, src, diag_add, rhs_add);
+  return PF_OK;
+}
+
 }  // extern "C"

@@ -1402,4 +1402,111 @@ inline void transport_matrix(const Cell* cells, const GirtGrid& g, double dt, co
   }
 }
 
+// Boundary connections and sources of the operator-split transport system
+// on the structured grid.  Faces in the order x-, x+, y-, y+, z-, z+; a face's
+// cells are indexed (j + ny k) on x faces, (i + nx k) on y faces, (i + nx j)
+// on z faces.  q: Darcy flux through the face, positive into the domain (the
+// boundary is the upstream end of its connection); total: [ncomp][face cells].
+struct TransportBC {
+  int type[6];  // PF_BC_* of pfgpu.h (0: no boundary connection)
+  const double* q[6];
+  const double* total[6];
+  double sat[6];  // global_auxvars_bc(:)%sat
+};
+struct TransportSrc {
+  int n;
+  const int* cell;
+  const int* type;      // PF_SRC_*
+  const double* q;      // m^3/s, + injection
+  const double* total;  // [ncomp][n]
+};
+
+// TDispersionBC (transport.F90:236-374) for one boundary connection of a
+// structured grid (no transverse dispersion, no Millington-Quirk, no
+// secondary continuum: epsilon 1): the hydrodynamic dispersion over
+// dist(0) = half the cell's width, with the boundary's saturation.
+inline double transport_dispersion_bc(int type, double sat_bc, const Cell& dn, double q, double dist0,
+                                      const GirtGrid& g) {
+  if (sat_bc < rt_min_saturation || dn.sat < rt_min_saturation) return 0.0;
+  const double mechanical = g.dispersivity * std::fabs(q);
+  if (type == 1 || type == 2) {  // DIRICHLET_BC, DIRICHLET_ZERO_GRADIENT_BC
+    if (type == 2 && q < 0.0) return 0.0;  // outflow: skip
+    const double hd = std::max(mechanical + 1.0 * sat_bc * dn.porosity * g.tortuosity * g.diffusion, 1.0e-40);
+    return hd / dist0;
+  }
+  return 0.0;  // ZERO_GRADIENT_BC, NEUMANN_BC, CONCENTRATION_SS
+}
+
+// The terms boundary conditions and sources add to the scalar transport
+// system: the boundary loop of RTCalculateTransportMatrix
+// (reactive_transport.F90:1596-1627: -T_dn on the cell's diagonal) and of
+// RTCalculateRHS_t1 (:1337-1370: T_up times the boundary totals on the
+// right-hand side), both with TFluxCoefBC (transport.F90:569-609, i.e.
+// TFluxCoef without the upwind saturation check); the source/sink loops of
+// both (RHS :1372-1418, injection only; matrix :1651-1690, extraction only,
+// coefficient > 0) with TSrcSinkCoef (transport.F90:613-673).
+// diag_add[N] adds to the diagonal, rhs_add[ncomp][N] to the right-hand side.
+inline void transport_bc_terms(const Cell* cells, const GirtGrid& g, int ncomp, const TransportBC& bc,
+                               const TransportSrc& src, double* diag_add, double* rhs_add) {
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const long long N = (long long)nx * ny * nz;
+  for (long long c = 0; c < N; ++c) diag_add[c] = 0.0;
+  for (long long e = 0; e < N * ncomp; ++e) rhs_add[e] = 0.0;
+  for (int f = 0; f < 6; ++f) {
+    if (bc.type[f] == 0) continue;
+    const int axis = f / 2, plus = f % 2;
+    const int na = axis == 0 ? ny : nx, nb = axis == 2 ? ny : nz;  // face cells: a + na*b
+    const double area = axis == 0 ? g.dy * g.dz : (axis == 1 ? g.dx * g.dz : g.dx * g.dy);
+    const double dist0 = 0.5 * (axis == 0 ? g.dx : (axis == 1 ? g.dy : g.dz));
+    for (int b = 0; b < nb; ++b)
+      for (int a = 0; a < na; ++a) {
+        int i, j, k;
+        if (axis == 0) { i = plus ? nx - 1 : 0; j = a; k = b; }
+        else if (axis == 1) { i = a; j = plus ? ny - 1 : 0; k = b; }
+        else { i = a; j = b; k = plus ? nz - 1 : 0; }
+        const long long cell = (long long)i + (long long)nx * (j + (long long)ny * k);
+        const long long fi = (long long)a + (long long)na * b, nf = (long long)na * nb;
+        const Cell& dn = cells[cell];
+        const double q = bc.q[f] ? bc.q[f][fi] : 0.0;
+        const double tran = transport_dispersion_bc(bc.type[f], bc.sat[f], dn, q, dist0, g);
+        double T_up = 0.0, T_dn = 0.0;
+        if (!(dn.sat < rt_min_saturation)) {  // TFluxCoef, check_upwind_saturation false
+          double coef_up, coef_dn;
+          if (q > 0.0) { coef_up = tran + q; coef_dn = -tran; }
+          else { coef_up = tran; coef_dn = -tran + q; }
+          T_up = coef_up * area * 1000.0;
+          T_dn = coef_dn * area * 1000.0;
+        }
+        diag_add[cell] = diag_add[cell] + (-T_dn);
+        for (int c = 0; c < ncomp; ++c)
+          rhs_add[(long long)c * N + cell] = rhs_add[(long long)c * N + cell] + T_up * bc.total[f][c * nf + fi];
+      }
+  }
+  for (int s = 0; s < src.n; ++s) {
+    const long long cell = src.cell[s];
+    const Cell& cl = cells[cell];
+    const double qsrc = src.q[s];
+    double T_in = 0.0, T_out = 0.0;
+    if (!(cl.sat < rt_min_saturation)) {
+      if (src.type[s] == 1) {         // EQUILIBRIUM_SS
+        T_in = 1.0e-3;
+        T_out = -1.0 * T_in;
+      } else if (src.type[s] == 2) {  // MASS_RATE_SS: the "total" is a rate, mol/s
+        T_in = 0.0;
+        T_out = -1.0;
+      } else if (qsrc > 0.0) {        // injection
+        T_in = 0.0;
+        T_out = -1.0 * qsrc * 1000.0;
+      } else {
+        T_out = 0.0;
+        T_in = -1.0 * qsrc * 1000.0;
+      }
+    }
+    if (!(qsrc > 0.0) && T_in > 0.0) diag_add[cell] = diag_add[cell] + T_in;
+    if (!(qsrc < 0.0))
+      for (int c = 0; c < ncomp; ++c)
+        rhs_add[(long long)c * N + cell] = rhs_add[(long long)c * N + cell] - T_out * src.total[(long long)c * src.n + s];
+  }
+}
+
 }  // namespace oracle

@@ -1,15 +1,22 @@
 // pfgpu_transport.cu -- the transport half of the operator-split step.
 //
-// Replaces, for a structured grid with zero-flux outer boundaries and no
-// sources, the transport solve of PMCSubsurfaceOSRTStepDT
-// (src/pflotran/pmc_subsurface_osrt.F90:259-330): the fixed accumulation
-// psv*T_k (psv = porosity*saturation*1000*volume), the scalar transport matrix
-// of RTCalculateTransportMatrix (reactive_transport.F90:1469-1703: per
-// internal connection TFluxCoef's T_up / T_dn, transport.F90:495-565, added at
-// (up,up), (up,dn) and negated at (dn,dn), (dn,up); psv/dt on the diagonal),
-// the right-hand side psv*T_k/dt (RTCalculateRHS_t1 without boundary or
-// source terms), and one linear solve per component (the reference's
-// KSPSolve loop over idof), all components sharing the matrix.
+// Replaces, for a structured grid, the transport solve of
+// PMCSubsurfaceOSRTStepDT (src/pflotran/pmc_subsurface_osrt.F90:259-330):
+// the fixed accumulation psv*T_k (psv = porosity*saturation*1000*volume), the
+// scalar transport matrix of RTCalculateTransportMatrix
+// (reactive_transport.F90:1469-1703: per internal connection TFluxCoef's
+// T_up / T_dn, transport.F90:495-565, added at (up,up), (up,dn) and negated at
+// (dn,dn), (dn,up); per boundary connection -T_dn on the cell's diagonal;
+// psv/dt on the diagonal; extraction sources' coefficient on the diagonal),
+// the right-hand side psv*T_k/dt plus the inflowing boundary and injection
+// terms of RTCalculateRHS_t1 (:1239-1465), and one linear solve per
+// component (the reference's KSPSolve loop over idof), all components
+// sharing the matrix.  Boundary faces carry a condition type, the face Darcy
+// fluxes and the boundary totals; TDispersionBC (transport.F90:236-374) gives
+// the boundary dispersion over half the cell width with the boundary's
+// saturation.  The right-hand side's boundary and source part is one FP64
+// vector [ncomp][N] written by the coefficient pass and the (sequential,
+// deterministic) source pass; without boundaries or sources it is not used.
 //
 // GPU form.  The matrix is never assembled: a coefficient pass stores per
 // cell the diagonal and the six face coefficients (the same harmonic-mean
@@ -28,6 +35,7 @@
 // partials, then a fixed-order sum in FP64), so results do not depend on
 // scheduling.
 #include <cmath>
+#include <cstring>
 #include <new>
 
 #include "pfgpu_common.cuh"
@@ -68,11 +76,21 @@ __device__ __forceinline__ void cell_ijk(const Grid& g, long long X, int& i, int
 // A[8][N] FP64: 0 diag, 1 x-, 2 x+, 3 y-, 4 y+, 5 z-, 6 z+ (the coefficient of
 // the neighbour's value in this row; 0 where there is none), 7 the right-hand
 // side's scale (b = A[7] T_k)
+// boundary conditions as the coefficient pass reads them
+struct BcDev {
+  int type[6];
+  const double* q[6];
+  const double* total[6];
+  double sat[6];
+  int ncomp;
+  double* bb;  // [ncomp][N] right-hand side additions, nullptr: no boundary or source terms
+};
+
 __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const double* __restrict__ qx,
                             const double* __restrict__ qy, const double* __restrict__ qz, double diffusion,
                             double tortuosity, double dispersivity, const double* __restrict__ por,
                             const double* __restrict__ sat, const double* __restrict__ vol, double dt,
-                            double* __restrict__ A, double* __restrict__ inv_diag) {
+                            double* __restrict__ A, double* __restrict__ inv_diag, BcDev bc) {
   const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (X >= g.N) return;
   int i, j, k;
@@ -126,6 +144,47 @@ __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const doubl
       off[q] = -cup;
     }
   }
+  // boundary connections (RTCalculateTransportMatrix :1596-1627 and
+  // RTCalculateRHS_t1 :1337-1370): the boundary is the upstream end, q > 0
+  // flows into the domain
+  if (bc.bb) {
+    for (int c = 0; c < bc.ncomp; ++c) bc.bb[(size_t)c * g.N + X] = 0.0;
+#pragma unroll 1
+    for (int f = 0; f < 6; ++f) {
+      if (bc.type[f] == PF_BC_ZERO_FLUX) continue;
+      const int axis = f >> 1, plus = f & 1;
+      const int pos = axis == 0 ? i : (axis == 1 ? j : k);
+      const int lim = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+      if (plus ? pos != lim - 1 : pos != 0) continue;
+      const long long na = axis == 0 ? g.ny : g.nx;
+      const long long nf = na * (axis == 2 ? g.ny : g.nz);
+      const long long fi = axis == 0 ? (j + na * k) : (axis == 1 ? (i + na * k) : (i + na * j));
+      const double area = axis == 0 ? dy * dz : (axis == 1 ? dx * dz : dx * dy);
+      const double dist0 = 0.5 * (axis == 0 ? dx : (axis == 1 ? dy : dz));
+      const double qb = bc.q[f] ? bc.q[f][fi] : 0.0;
+      const double sdn = sat[X];
+      // TDispersionBC: Dirichlet (and Dirichlet-zero-gradient where the flux
+      // enters) disperses against the boundary water over dist0
+      double tr = 0.0;
+      if (!(bc.sat[f] < RT_MIN_SATURATION) && !(sdn < RT_MIN_SATURATION) &&
+          (bc.type[f] == PF_BC_DIRICHLET || (bc.type[f] == PF_BC_DIRICHLET_ZERO_GRADIENT && !(qb < 0.0)))) {
+        const double hd = fmax(dispersivity * fabs(qb) + 1.0 * bc.sat[f] * por[X] * tortuosity * diffusion, 1.0e-40);
+        tr = hd / dist0;
+      }
+      // TFluxCoefBC -> TFluxCoef without the upwind saturation check
+      double tup = 0.0, tdn = 0.0;
+      if (!(sdn < RT_MIN_SATURATION)) {
+        if (qb > 0.0) { tup = tr + qb; tdn = -tr; }
+        else { tup = tr; tdn = -tr + qb; }
+        tup = tup * area * 1000.0;
+        tdn = tdn * area * 1000.0;
+      }
+      diag = diag + (-tdn);
+      if (tup != 0.0)
+        for (int c = 0; c < bc.ncomp; ++c)
+          bc.bb[(size_t)c * g.N + X] = fma(tup, bc.total[f][(size_t)c * nf + fi], bc.bb[(size_t)c * g.N + X]);
+    }
+  }
   const double storage = psv / dt;
   diag = diag + storage;
   // a cell with neither storage nor connections (dry: saturation below
@@ -141,6 +200,47 @@ __global__ void coef_kernel(Grid g, double dx, double dy, double dz, const doubl
   for (int q = 0; q < 6; ++q) A[(size_t)(q + 1) * g.N + X] = off[q];
   A[(size_t)7 * g.N + X] = bscale;
   inv_diag[X] = 1.0 / diag;
+}
+
+// Sources and sinks, in array order (one block; thread c owns component c
+// of the right-hand side, thread 0 also the diagonal): the source loops of
+// RTCalculateTransportMatrix (:1651-1690, extraction: T_in on the diagonal
+// when positive) and RTCalculateRHS_t1 (:1372-1418, injection: -T_out times
+// the source totals) with TSrcSinkCoef (transport.F90:613-673).  An entry
+// whose cell lies outside the grid is skipped and counted in *bad.
+__global__ void source_kernel(long long N, int ncomp, int nsrc, const int32_t* __restrict__ cell,
+                              const int32_t* __restrict__ type, const double* __restrict__ qs,
+                              const double* __restrict__ total, const double* __restrict__ sat,
+                              double* __restrict__ A, double* __restrict__ inv_diag, double* __restrict__ bb,
+                              unsigned* __restrict__ bad) {
+  const int c = threadIdx.x;
+  for (int e = 0; e < nsrc; ++e) {
+    const long long X = cell[e];
+    if (X < 0 || X >= N) {
+      if (c == 0) atomicAdd(bad, 1u);
+      continue;
+    }
+    const double q = qs[e];
+    double tin = 0.0, tout = 0.0;
+    if (!(sat[X] < RT_MIN_SATURATION)) {
+      if (type[e] == PF_SRC_EQUILIBRIUM) {
+        tin = 1.0e-3;
+        tout = -1.0 * tin;
+      } else if (type[e] == PF_SRC_MASS_RATE) {
+        tin = 0.0;
+        tout = -1.0;
+      } else if (q > 0.0) {
+        tout = -1.0 * q * 1000.0;
+      } else {
+        tin = -1.0 * q * 1000.0;
+      }
+    }
+    if (c == 0 && !(q > 0.0) && tin > 0.0) {
+      A[X] = A[X] + tin;
+      inv_diag[X] = 1.0 / A[X];
+    }
+    if (c < ncomp && !(q < 0.0)) bb[(size_t)c * N + X] = bb[(size_t)c * N + X] - tout * total[(size_t)c * nsrc + e];
+  }
 }
 
 // Ah[6][N] FP32: the off-diagonals of A D^-1 (column q scaled by the
@@ -320,14 +420,15 @@ __device__ __forceinline__ bool chunk_active(const double* __restrict__ S, int n
 // ||r||^2 (w = 0) and, on the first call, ||b||^2 (w = 1)
 template <int NC>
 __device__ __forceinline__ void residual_body(const Grid& g, const double* __restrict__ A,
-                                              const double* __restrict__ total_k, const double* __restrict__ x,
-                                              double* __restrict__ r64, bool first, double (&acc)[2][CH]) {
+                                              const double* __restrict__ total_k, const double* __restrict__ bb,
+                                              const double* __restrict__ x, double* __restrict__ r64, bool first,
+                                              double (&acc)[2][CH]) {
   const size_t o0 = (size_t)blockIdx.y * CH * (size_t)g.Np;  // x, r64
   const size_t t0 = (size_t)blockIdx.y * CH * (size_t)g.N;   // the caller's totals
   for (unsigned X = blockIdx.x * blockDim.x + threadIdx.x; X < (unsigned)g.N; X += gridDim.x * blockDim.x) {
     unsigned idx[7];
     nbr_index(g, X, idx);
-    double w[7], xv[NC][7], tk[NC];
+    double w[7], xv[NC][7], tk[NC], ba[NC];
     // all loads before the first store (see spmv_body)
 #pragma unroll
     for (int q = 0; q < 7; ++q) w[q] = A[(size_t)q * g.N + X];
@@ -338,10 +439,11 @@ __device__ __forceinline__ void residual_body(const Grid& g, const double* __res
 #pragma unroll
       for (int q = 0; q < 7; ++q) xv[cc][q] = xc[idx[q]];
       tk[cc] = total_k[t0 + (size_t)cc * g.N + X];
+      ba[cc] = bb ? bb[t0 + (size_t)cc * g.N + X] : 0.0;  // boundary and source terms
     }
 #pragma unroll
     for (int cc = 0; cc < NC; ++cc) {
-      const double b = bs * tk[cc];
+      const double b = fma(bs, tk[cc], ba[cc]);
       double ax = w[0] * xv[cc][0];
 #pragma unroll
       for (int q = 1; q < 7; ++q) ax = fma(w[q], xv[cc][q], ax);
@@ -355,6 +457,7 @@ __device__ __forceinline__ void residual_body(const Grid& g, const double* __res
 
 __global__ void __launch_bounds__(TPB) residual_kernel(Grid g, const double* __restrict__ A,
                                                        const double* __restrict__ total_k,
+                                                       const double* __restrict__ bb,
                                                        const double* __restrict__ x, double* __restrict__ r64,
                                                        int ncomp, double* __restrict__ partials,
                                                        double* __restrict__ S, Stage st) {
@@ -362,10 +465,10 @@ __global__ void __launch_bounds__(TPB) residual_kernel(Grid g, const double* __r
   const bool first = st.first != 0;
   double acc[2][CH] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   switch (nc) {
-    case 4: residual_body<4>(g, A, total_k, x, r64, first, acc); break;
-    case 3: residual_body<3>(g, A, total_k, x, r64, first, acc); break;
-    case 2: residual_body<2>(g, A, total_k, x, r64, first, acc); break;
-    default: residual_body<1>(g, A, total_k, x, r64, first, acc); break;
+    case 4: residual_body<4>(g, A, total_k, bb, x, r64, first, acc); break;
+    case 3: residual_body<3>(g, A, total_k, bb, x, r64, first, acc); break;
+    case 2: residual_body<2>(g, A, total_k, bb, x, r64, first, acc); break;
+    default: residual_body<1>(g, A, total_k, bb, x, r64, first, acc); break;
   }
   block_partials_chunk<2, double>(acc, partials, c0, ncomp);
   finish_stage(st, partials, S, ncomp);
@@ -594,14 +697,16 @@ struct PfTransport {
 
 namespace {
 struct Layout {
-  double *A, *invD, *x, *r64, *partials, *S;
+  double *A, *invD, *x, *r64, *partials, *S, *bb;
   float *Ah, *r, *r0, *p, *v, *s, *t, *y;
-  unsigned* counter;
+  unsigned *counter, *bad_src;
 };
 
 // Work space, every array on a 256-byte boundary: FP64 A[8][N], invD[N],
-// x and r64 [ncomp][Np], partials, S; the stage counter; FP32 Ah[6][N] and the inner solver's
-// r, r0, p, v, s, t, y [ncomp][Np].  With base == nullptr only the size.
+// x and r64 [ncomp][Np], partials, S, the right-hand side's boundary and
+// source terms bb [ncomp][N]; the stage counter and the count of source
+// entries outside the grid; FP32 Ah[6][N] and the inner solver's r, r0, p, v,
+// s, t, y [ncomp][Np].  With base == nullptr only the size.
 size_t transport_layout(char* base, long long N, long long Np, int n, Layout* L) {
   size_t cur = 0;
   auto take = [&](size_t bytes) {
@@ -617,7 +722,9 @@ size_t transport_layout(char* base, long long N, long long Np, int n, Layout* L)
   l.r64 = (double*)take(vec * 8);
   l.partials = (double*)take(2 * (size_t)tr::RED_BLOCKS * n * 8);
   l.S = (double*)take((size_t)tr::NSCALAR * n * 8);
+  l.bb = (double*)take((size_t)n * (size_t)N * 8);
   l.counter = (unsigned*)take(4);
+  l.bad_src = (unsigned*)take(4);
   l.Ah = (float*)take(6 * (size_t)N * 4);
   l.r = (float*)take(vec * 4);
   l.r0 = (float*)take(vec * 4);
@@ -660,7 +767,7 @@ extern "C" int32_t pf_transport_create(int32_t nx, int32_t ny, int32_t nz, int32
   if (t->gx_res < 0 || t->gx_sp1 < 0 || t->gx_sp2 < 0 || t->gx_vec < 0 ||
       cudaMalloc(&t->buf, t->bytes) != cudaSuccess ||
       cudaMemset(t->buf, 0, t->bytes) != cudaSuccess ||  // the vectors' padding stays 0
-      cudaMallocHost(&t->h_scalars, tr::NSCALAR * ncomp * sizeof(double)) != cudaSuccess) {
+      cudaMallocHost(&t->h_scalars, (tr::NSCALAR * ncomp + 1) * sizeof(double)) != cudaSuccess) {
     if (t->buf) cudaFree(t->buf);
     delete t;
     return PF_ERR_CUDA;
@@ -685,8 +792,13 @@ int32_t read_stats(PfTransport* t, cudaStream_t s, double rtol, PfTransportStats
   Layout L;
   transport_layout(static_cast<char*>(t->buf), t->N, t->Np, n, &L);
   if (cudaMemcpyAsync(t->h_scalars, L.S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(t->h_scalars + NSCALAR * n, L.bad_src, sizeof(unsigned), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return PF_ERR_CUDA;
+  unsigned bad = 0;
+  memcpy(&bad, t->h_scalars + NSCALAR * n, sizeof(unsigned));
+  if (bad) return PF_ERR_INVALID;  // a source entry named a cell outside the grid
   const double* h = t->h_scalars;
   double worst = 0.0, its = 0.0, refs = 0.0, cyc = 0.0;
   bool conv = true;
@@ -717,6 +829,12 @@ int32_t check_args(const PfTransport* t, const PfTransportArgs* a) {
       !a->saturation || !a->volume || a->max_iterations < 1 || !(a->rtol > 0.0))
     return PF_ERR_INVALID;
   if ((t->nx > 1 && !a->qx) || (t->ny > 1 && !a->qy) || (t->nz > 1 && !a->qz)) return PF_ERR_INVALID;
+  for (int f = 0; f < 6; ++f) {
+    if (a->bc_type[f] < PF_BC_ZERO_FLUX || a->bc_type[f] > PF_BC_ZERO_GRADIENT) return PF_ERR_INVALID;
+    if (a->bc_type[f] != PF_BC_ZERO_FLUX && (!a->bc_total[f] || !(a->bc_saturation[f] >= 0.0))) return PF_ERR_INVALID;
+  }
+  if (a->nsrc < 0 || (a->nsrc > 0 && (!a->src_cell || !a->src_type || !a->src_q || !a->src_total)))
+    return PF_ERR_INVALID;
   return PF_OK;
 }
 
@@ -733,9 +851,24 @@ int32_t transport_run(PfTransport* t, const PfTransportArgs* a, cudaStream_t s, 
   transport_layout(static_cast<char*>(t->buf), N, Np, n, &L);
   Grid g{t->nx, t->ny, t->nz, N, (long long)t->nx * t->ny, Np};
   const unsigned cblocks = (unsigned)((N + TPB - 1) / TPB);
+  BcDev bc{};
+  bool open = a->nsrc > 0;
+  for (int f = 0; f < 6; ++f) {
+    bc.type[f] = a->bc_type[f];
+    bc.q[f] = a->bc_q[f];
+    bc.total[f] = a->bc_total[f];
+    bc.sat[f] = a->bc_saturation[f];
+    open = open || a->bc_type[f] != PF_BC_ZERO_FLUX;
+  }
+  bc.ncomp = n;
+  bc.bb = open ? L.bb : nullptr;
+  if (cudaMemsetAsync(L.bad_src, 0, sizeof(unsigned), s) != cudaSuccess) return PF_ERR_CUDA;
   coef_kernel<<<cblocks, TPB, 0, s>>>(g, a->dx, a->dy, a->dz, a->qx, a->qy, a->qz, a->diffusion_coefficient,
                                       a->tortuosity, a->dispersivity, a->porosity, a->saturation, a->volume, a->dt,
-                                      L.A, L.invD);
+                                      L.A, L.invD, bc);
+  if (a->nsrc > 0)
+    source_kernel<<<1, 32, 0, s>>>(N, n, a->nsrc, a->src_cell, a->src_type, a->src_q, a->src_total, a->saturation,
+                                   L.A, L.invD, L.bb, L.bad_src);
   scale_kernel<<<cblocks, TPB, 0, s>>>(g, L.A, L.invD, L.Ah);
   // blocks: one wave, but no more than the cells need
   auto cap = [&](int gx) { return (unsigned)((long long)gx < (long long)cblocks ? gx : (int)cblocks); };
@@ -747,7 +880,8 @@ int32_t transport_run(PfTransport* t, const PfTransportArgs* a, cudaStream_t s, 
   if (cudaMemsetAsync(L.counter, 0, sizeof(unsigned), s) != cudaSuccess) return PF_ERR_CUDA;
   copy_kernel<<<g_vec, TPB, 0, s>>>(N, N, Np, a->total, L.x);  // x0 = T_k
   auto outer_residual = [&](int first) {
-    residual_kernel<<<g_res, TPB, 0, s>>>(g, L.A, a->total, L.x, L.r64, n, L.partials, L.S, stage(0, first));
+    residual_kernel<<<g_res, TPB, 0, s>>>(g, L.A, a->total, bc.bb, L.x, L.r64, n, L.partials, L.S,
+                                          stage(0, first));
   };
   auto fetch = [&]() {
     return cudaMemcpyAsync(t->h_scalars, L.S, NSCALAR * n * sizeof(double), cudaMemcpyDeviceToHost, s) ==

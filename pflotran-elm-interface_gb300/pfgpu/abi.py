@@ -31,6 +31,14 @@ PF_ACT_COEF_ALGO_NEWTON = 1
 PF_KERNEL_PLAIN = 0
 PF_KERNEL_BATCHED = 1
 
+PF_BC_ZERO_FLUX = 0
+PF_BC_DIRICHLET = 1
+PF_BC_DIRICHLET_ZERO_GRADIENT = 2
+PF_BC_ZERO_GRADIENT = 3
+PF_SRC_VOLUMETRIC = 0
+PF_SRC_EQUILIBRIUM = 1
+PF_SRC_MASS_RATE = 2
+
 PF_CONSTRAINT_TOTAL = 1
 PF_CONSTRAINT_FREE = 2
 PF_CONSTRAINT_PH = 3
@@ -169,6 +177,9 @@ class PfTransportArgs(C.Structure):
         ("diffusion_coefficient", C.c_double), ("tortuosity", C.c_double), ("dispersivity", C.c_double),
         ("porosity", _dp), ("saturation", _dp), ("volume", _dp),
         ("dt", C.c_double), ("total", _dp), ("rtol", C.c_double), ("max_iterations", C.c_int32),
+        ("bc_type", C.c_int32 * 6), ("bc_q", _dp * 6), ("bc_total", _dp * 6), ("bc_saturation", C.c_double * 6),
+        ("nsrc", C.c_int32), ("src_cell", C.POINTER(C.c_int32)), ("src_type", C.POINTER(C.c_int32)),
+        ("src_q", _dp), ("src_total", _dp),
     ]
 
 

@@ -1,10 +1,13 @@
 """The transport half of the operator-split step (pf_transport_step).
 
 `OSTransport` owns the device work space of one structured grid and solves,
-per step, (psv/dt + A) T_k+1 = psv T_k / dt for every component at once
-(A: advection by the face Darcy fluxes, upwinded, plus dispersion-
-diffusion, zero-flux outer boundaries), as the reference's operator-split
-time step does before its reaction step (pmc_subsurface_osrt.F90:259-330).
+per step, (psv/dt + A) T_k+1 = psv T_k / dt + b_bc for every component at
+once (A: advection by the face Darcy fluxes, upwinded, plus dispersion-
+diffusion; boundary conditions on the outer faces and sources/sinks add to
+the diagonal and to b_bc), as the reference's operator-split time step does
+before its reaction step (pmc_subsurface_osrt.F90:259-330,
+RTCalculateTransportMatrix and RTCalculateRHS_t1).  Faces without a
+boundary condition are closed (zero flux).
 """
 from __future__ import annotations
 
@@ -29,8 +32,59 @@ class OSTransport:
                   allow_cell_failures=False)
         self.handle = h
         f64 = dict(dtype=torch.float64, device=device)
+        self.device = device
         self._q = [torch.as_tensor(np.ascontiguousarray(q), dtype=torch.float64).reshape(-1).to(device)
                    if np.size(q) else torch.zeros(1, **f64) for q in (grid.qx, grid.qy, grid.qz)]
+        self._bc = [None] * 6   # per face: (type, q tensor or None, total tensor, saturation)
+        self._src = None        # (cell, type, q, total) tensors
+
+    FACES = {"x-": 0, "x+": 1, "y-": 2, "y+": 3, "z-": 4, "z+": 5}
+
+    def face_cells(self, face: int) -> int:
+        g = self.grid
+        return (g.ny * g.nz, g.ny * g.nz, g.nx * g.nz, g.nx * g.nz, g.nx * g.ny, g.nx * g.ny)[face]
+
+    def set_boundary(self, face, bc_type, total, q=None, saturation=1.0):
+        """A boundary condition on one outer face (0..5 or "x-", "x+", "y-",
+        "y+", "z-", "z+"): bc_type PF_BC_*; total (ncomp, face cells) or
+        (ncomp,) totals of the boundary water, mol/L; q (face cells,) or a
+        scalar Darcy flux through the face, m/s, positive into the domain;
+        saturation at the boundary.  Face cells are indexed j + ny*k (x
+        faces), i + nx*k (y faces), i + nx*j (z faces).  bc_type
+        PF_BC_ZERO_FLUX closes the face again."""
+        import torch
+        f = self.FACES[face] if isinstance(face, str) else int(face)
+        if bc_type == abi.PF_BC_ZERO_FLUX:
+            self._bc[f] = None
+            return
+        nf = self.face_cells(f)
+        tot = np.asarray(total, np.float64)
+        if tot.ndim == 1:
+            tot = np.repeat(tot[:, None], nf, axis=1)
+        if tot.shape != (self.ncomp, nf):
+            raise ValueError("boundary totals must be (ncomp, %d) or (ncomp,)" % nf)
+        qt = None
+        if q is not None:
+            qa = np.broadcast_to(np.asarray(q, np.float64), (nf,))
+            qt = torch.from_numpy(np.ascontiguousarray(qa)).to(self.device)
+        self._bc[f] = (int(bc_type), qt, torch.from_numpy(np.ascontiguousarray(tot)).to(self.device),
+                       float(saturation))
+
+    def set_sources(self, cell=None, src_type=None, q=None, total=None):
+        """Sources and sinks, applied in the given order: cell indices, types
+        PF_SRC_*, q in m^3/s (positive: injection), total (ncomp, nsrc) in
+        mol/L (mol/s for PF_SRC_MASS_RATE).  No arguments: none."""
+        import torch
+        if cell is None or len(cell) == 0:
+            self._src = None
+            return
+        n = len(cell)
+        tot = np.asarray(total, np.float64).reshape(self.ncomp, n)
+        dev = self.device
+        self._src = (torch.from_numpy(np.ascontiguousarray(cell, np.int32)).to(dev),
+                     torch.from_numpy(np.ascontiguousarray(np.broadcast_to(src_type, (n,)), np.int32)).to(dev),
+                     torch.from_numpy(np.ascontiguousarray(np.broadcast_to(q, (n,)), np.float64)).to(dev),
+                     torch.from_numpy(np.ascontiguousarray(tot)).to(dev))
 
     def close(self):
         if getattr(self, "handle", None):
@@ -64,6 +118,20 @@ class OSTransport:
         a.total = C.cast(state.a["total"].data_ptr(), dp)
         a.rtol = float(rtol)
         a.max_iterations = int(max_iterations)
+        for f, b in enumerate(self._bc):
+            if b is None:
+                continue
+            a.bc_type[f] = b[0]
+            a.bc_q[f] = C.cast(b[1].data_ptr(), dp) if b[1] is not None else None
+            a.bc_total[f] = C.cast(b[2].data_ptr(), dp)
+            a.bc_saturation[f] = b[3]
+        if self._src is not None:
+            ip = C.POINTER(C.c_int32)
+            a.nsrc = int(self._src[0].numel())
+            a.src_cell = C.cast(self._src[0].data_ptr(), ip)
+            a.src_type = C.cast(self._src[1].data_ptr(), ip)
+            a.src_q = C.cast(self._src[2].data_ptr(), dp)
+            a.src_total = C.cast(self._src[3].data_ptr(), dp)
         return a
 
     @staticmethod

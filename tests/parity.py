@@ -13,6 +13,13 @@ Quantities and their scales (FP64 throughout; REL = 1e-10):
   mnrl_volfrac           relative to |volfrac| + gross rate * V_m * dt
   status, num_substeps   exact (they define the path)
 
+A cell that failed (status != 0: dt cut maximum_reaction_cuts times) is
+compared on its status, path and totals only: RStep restores its totals, and
+its molalities and rates are whatever the last non-converged Newton iterate
+held -- the reference's time loop discards them (the whole step is cut and
+repeated, pmc_subsurface_osrt.F90:381-396), and two factorisations of the
+same non-converging iteration drift apart by rounding.
+
 Cells are classified by their Newton path against the oracle's:
   path-identical   same Newton iteration count, substep count and status
                    (single-RReact cells, cells with dt cuts, failed cells)
@@ -102,6 +109,11 @@ def cell_errors(net, ref, got, dt):
         e["mnrl_rate"] = r(got.a["mnrl_rate"], ref.a["mnrl_rate"], gr)
         vs = np.abs(ref.a["mnrl_volfrac"]) + gr * net.mnrl_molar_vol[:, None] * _dt_cells(ref, dt)[None, :]
         e["mnrl_volfrac"] = r(got.a["mnrl_volfrac"], ref.a["mnrl_volfrac"], np.maximum(vs, 1e-30))
+    # failed in both: status, path and the restored totals only
+    failed = (ref.a["status"] != 0) & (got.a["status"] != 0)
+    for k in e:
+        if k != "total":
+            e[k] = np.where(failed, 0.0, e[k])
     return e
 
 
@@ -153,6 +165,10 @@ def compare(net, ref, got, dt, label, self_runs=(), its=True):
     cls = {"single": (sub == 1) & (stt == 0), "cut": (sub > 1) & (stt == 0), "failed": stt != 0}
     entry = dict(
         cells=int(ref.ncells), compared=int(p.sum()), flips=int(flips.sum()), outliers=int(outl.sum()),
+        outliers_by_class={k: int((outl & v).sum()) for k, v in
+                           {"single": (ref.a["num_substeps"] == 1) & (ref.a["status"] == 0),
+                            "cut": (ref.a["num_substeps"] > 1) & (ref.a["status"] == 0),
+                            "failed": ref.a["status"] != 0}.items()},
         oracle_self_flips=s_flips, oracle_self_outliers=s_out,
         compared_by_class={k: int((p & v).sum()) for k, v in cls.items()},
         cells_by_class={k: int(v.sum()) for k, v in cls.items()},
@@ -186,11 +202,13 @@ def format_report():
     for k in sorted(REPORT):
         r = REPORT[k]
         errs = " ".join("%s %.1e" % (q, v) for q, v in r["max_rel_err"].items())
+        ob = r["outliers_by_class"]
         lines.append("  %-34s cells %6d compared %6d (single %d, cut %d, failed %d) flips %d|%s outliers %d|%s "
-                     "its mean %.1f max %d | %s | flip err gpu %s oracle %s" % (
+                     "(%d/%d/%d) its mean %.1f max %d | %s | flip err gpu %s oracle %s" % (
                          k, r["cells"], r["compared"], r["compared_by_class"]["single"],
                          r["compared_by_class"]["cut"], r["compared_by_class"]["failed"], r["flips"],
-                         r["oracle_self_flips"], r["outliers"], r["oracle_self_outliers"], r["its_mean"],
+                         r["oracle_self_flips"], r["outliers"], r["oracle_self_outliers"], ob["single"], ob["cut"],
+                         ob["failed"], r["its_mean"],
                          r["its_max"], errs,
                          "%.1e" % r["flip_max_err_gpu"] if r["flip_max_err_gpu"] is not None else "-",
                          "%.1e" % r["flip_max_err_oracle_self"] if r["flip_max_err_oracle_self"] else "-"))
