@@ -529,10 +529,23 @@ def c3_measure(args, per=500_000, nsteps=50, replays=1, plain=True, eager_steps=
                             its_min=int(its.min())))
     batched_first = sum(r["batched_ms"] for r in per_net)
     plain_first = sum(r["plain_ms"] for r in per_net) if plain else None
+    # the same first step as one persistent launch over every network's
+    # cells (pf_rstep_multi), networks in descending ncomp
+    from pfgpu.engine import rstep_multi
+    by_cost = sorted(range(len(members)), key=lambda i: -members[i][0].net.ncomp)
+    multi_ms = None
+    if not getattr(args, "concurrent", False) and not getattr(args, "transport", False):
+        reset(start)
+        rstep_multi([members[i] for i in by_cost], 86400.0, stats=False)  # warm
+        reset(start)
+        multi_ms = timed(lambda: rstep_multi([members[i] for i in by_cost], 86400.0, stats=False))
+    use_multi = multi_ms is not None and not getattr(args, "per_network", False)
     # one eager warm step of the loop (its Newton counts order the first graph step)
     reset(start)
-    loop = OperatorSplitLoop([(eng, dev, tr) for (eng, dev), tr in zip(members, stages)], dt=86400.0,
-                             concurrent=getattr(args, "concurrent", False))
+    ordered = [members[i] for i in by_cost] if use_multi else members
+    ordered_stages = [stages[i] for i in by_cost] if use_multi else stages
+    loop = OperatorSplitLoop([(eng, dev, tr) for (eng, dev), tr in zip(ordered, ordered_stages)], dt=86400.0,
+                             concurrent=getattr(args, "concurrent", False), multi=use_multi)
     loop.step()
     torch.cuda.synchronize()
     s0 = [{k: dev.a[k].clone() for k in fields if k in dev.a} for _, dev in members]
@@ -565,12 +578,17 @@ def c3_measure(args, per=500_000, nsteps=50, replays=1, plain=True, eager_steps=
            "graph_ms": g, "eager_ms_per_step": eager_ms,
            "first_step": {"batched_ms": batched_first, "plain_ms": plain_first,
                           "speedup_vs_plain_gpu": (plain_first / batched_first) if plain else None,
+                          "one_launch_ms": multi_ms,
+                          "one_launch_speedup_vs_plain_gpu": (plain_first / multi_ms) if (plain and multi_ms)
+                          else None,
                           "per_network": per_net},
+           "graph_reaction_step": "one persistent launch over all networks (pf_rstep_multi)" if use_multi
+           else "one persistent launch per network",
            "last_step": summary, "autotune": tuned, "clocks": clk.summary(), "transport": transport_info,
            # per network per step: auxvars, activities, setup pre-pass, persistent kernel
-           # (+ the transport schedule's launches)
-           "gpu_launches": len(graph_ms) * nsteps * (4 * len(members) + sum(
-               transport_launches(tr) for tr in stages if tr is not None))}
+           # (one persistent kernel for all with pf_rstep_multi; + the transport schedule's launches)
+           "gpu_launches": len(graph_ms) * nsteps * ((3 * len(members) + 1) if use_multi else 4 * len(members)) +
+           len(graph_ms) * nsteps * sum(transport_launches(tr) for tr in stages if tr is not None)}
     del members, loop, start, s0
     torch.cuda.empty_cache()
     return out
@@ -784,6 +802,8 @@ def main():
                          "c5: only the global-implicit assembly on 128x128x64 cells")
     ap.add_argument("--graph-steps", type=int, default=50, help="c3: operator-split steps in the graph")
     ap.add_argument("--concurrent", action="store_true", help="c3: one stream per network inside the graph")
+    ap.add_argument("--per-network", action="store_true",
+                    help="c3: one persistent launch per network in the graph (default: one launch for all)")
     ap.add_argument("--transport", action="store_true",
                     help="c3: each network on a structured grid, transport solve before every reaction step "
                          "(uniform dt = 1 day)")

@@ -361,6 +361,33 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
 int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, double dt, void* stream,
                          PfStepStats* stats);
 
+/*
+ * pf_rstep_multi -- one operator-split step for the cells of several
+ * networks (a heterogeneous domain: regions whose chemistry has different
+ * reaction networks, ncomp up to 24) in one persistent launch.  No
+ * counterpart in the reference, whose cell loop calls RStep cell by cell
+ * whatever the cell's chemistry (pmc_subsurface_osrt.F90:346-378); each cell's
+ * step is exactly pf_rstep's with the batched kernel and a group of lanes per
+ * cell.  nets[k] and states[k] (device arrays, each state's cell_order
+ * honoured) for k < nnets <= PF_MULTI_MAX_NETS, every network on the current
+ * device; the launch works through the networks in array order (list the
+ * costliest first), every block staging a network's tables and pulling its
+ * cells until its queue is empty, then moving to the next, so the SMs idle
+ * only at the end of the launch.  Each network runs with 4 or 8 lanes per
+ * cell: its own launch configuration's group size when that is one of
+ * those, else the first of 4, 8 it supports.  A network the group kernel does
+ * not support (sorption, rate prefactors, the linear formulation, activity by
+ * the NEWTON algorithm or water activity at every Newton iteration) makes the
+ * call return PF_ERR_UNSUPPORTED.  stats: NULL, or an array of nnets
+ * (the call then synchronises the stream; PF_CELL_FAILURES when any network
+ * had failed cells, PF_ERR_TIMEOUT when a table-staging wait ran out).
+ * Per-network scratch grows as pf_rstep's does (pf_network_reserve first,
+ * before capturing the call into a CUDA graph).
+ */
+#define PF_MULTI_MAX_NETS 16
+int32_t pf_rstep_multi(PfNetwork* const* nets, const PfCellState* states, int32_t nnets, double dt, void* stream,
+                       PfStepStats* stats);
+
 /* ----------------------------------------------------------------- adjoint */
 /* Largest number of RStep substeps (dt cuts) whose converged states the
  * adjoint keeps per cell; cells with more report adj_status 2. */

@@ -36,7 +36,7 @@ module pfgpu_mod
   integer(c_int32_t), parameter, public :: PF_MAX_NCOMP = 24, PF_MAX_NSEC = 96, &
       PF_MAX_NMNRL = 16, PF_MAX_SPEC_PER_RXN = 24, PF_MAX_NKD = 8, PF_MAX_NIONX = 4, &
       PF_MAX_IONX_CATIONS = 8, PF_MAX_PREFACTORS = 4, PF_MAX_PREFACTOR_SPECIES = 4, &
-      PF_ADJ_MAX_SUBSTEPS = 16
+      PF_ADJ_MAX_SUBSTEPS = 16, PF_MULTI_MAX_NETS = 16
   integer(c_int32_t), parameter, public :: PF_SORPTION_LINEAR = 1, PF_SORPTION_LANGMUIR = 2, &
       PF_SORPTION_FREUNDLICH = 3, PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1
   integer(c_int32_t), parameter, public :: PF_BC_ZERO_FLUX = 0, PF_BC_DIRICHLET = 1, &
@@ -156,7 +156,7 @@ module pfgpu_mod
 
   ! ---------------------------------------------------------- entry points
   public :: pf_network_create, pf_network_destroy, pf_network_set_options, pf_network_reserve, &
-            pf_rstep, pf_update_auxvars, pf_update_activity_coefs, pf_rstep_host, pf_rstep_noalloc, &
+            pf_rstep, pf_update_auxvars, pf_update_activity_coefs, pf_rstep_host, pf_rstep_noalloc, pf_rstep_multi, &
             pf_adjoint, pf_network_shift_parameters, pf_girt_pattern, pf_girt_assemble, &
             pf_transport_create, pf_transport_destroy, pf_transport_step, pf_transport_enqueue, &
             pf_transport_read_stats, pf_equilibrate_constraint, pf_equilibrate_constraint_ex, &
@@ -218,6 +218,15 @@ module pfgpu_mod
       type(c_ptr), value :: net, stream, stats
       type(pf_cell_state_t), intent(in) :: state
       real(c_double), value :: dt
+    end function
+    ! one persistent launch over several networks' cells; stats: c_null_ptr or c_loc of pf_step_stats_t(nnets)
+    integer(c_int32_t) function pf_rstep_multi(nets, states, nnets, dt, stream, stats) bind(C, name="pf_rstep_multi")
+      import :: c_int32_t, c_ptr, c_double, pf_cell_state_t
+      type(c_ptr), intent(in) :: nets(*)
+      type(pf_cell_state_t), intent(in) :: states(*)
+      integer(c_int32_t), value :: nnets
+      real(c_double), value :: dt
+      type(c_ptr), value :: stream, stats
     end function
     integer(c_int32_t) function pf_adjoint(net, state, dt, args, stream) bind(C, name="pf_adjoint")
       import :: c_int32_t, c_ptr, c_double, pf_cell_state_t, pf_adjoint_args_t

@@ -655,6 +655,71 @@ int32_t pf_internal_read_step_stats(PfNetwork* net, int64_t ncells, void* stream
   return read_step_stats(net, ncells, (cudaStream_t)stream, stats);
 }
 
+int32_t pf_rstep_multi(PfNetwork* const* nets, const PfCellState* states, int32_t nnets, double dt, void* stream,
+                       PfStepStats* stats) {
+  if (!nets || !states || nnets < 1 || nnets > PF_MULTI_MAX_NETS) return PF_ERR_INVALID;
+  MultiNetLaunch L[PF_MULTI_MAX_NETS];
+  int nl = 0, device = -1, sms = 0;
+  for (int k = 0; k < nnets; ++k) {
+    PfNetwork* net = nets[k];
+    if (!net) return PF_ERR_INVALID;
+    int rc = check_rstep(net, &states[k], dt, PF_KERNEL_BATCHED);
+    if (rc) return rc;
+    if (device < 0) {
+      device = net->device;
+      sms = net->num_sms;
+    } else if (net->device != device) {
+      return PF_ERR_INVALID;
+    }
+    const int G = multi_lanes_for(net->dev, net->launch.lanes_per_cell);
+    if (!G) return PF_ERR_UNSUPPORTED;
+    if (states[k].ncells == 0) continue;
+    rc = ensure_scratch(net, states[k].ncells);
+    if (rc) return rc;
+    L[nl].net = net->dev;
+    L[nl].st = states[k];
+    L[nl].scratch = net->d_scratch;
+    L[nl].queue = net->d_counters;
+    L[nl].counters = net->d_counters + 1;
+    L[nl].lanes_per_cell = G;
+    ++nl;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int k = 0; k < nnets; ++k)
+    if (cudaMemsetAsync(nets[k]->d_counters, 0, 8 * sizeof(unsigned long long), s) != cudaSuccess)
+      return PF_ERR_CUDA;
+  if (nl > 0) {
+    // one block of 256 threads per SM (the group kernels' registers allow
+    // one), 128 threads when some network's workspace does not fit
+    int tpb = 256;
+    for (int k = 0; k < nl && tpb == 256; ++k) {
+      PfLaunchConfig c{256, 1, 0, L[k].lanes_per_cell};
+      if (group_smem_bytes(L[k].net, c, false) > 227u * 1024u) tpb = 128;
+    }
+    if (launch_rstep_multi(L, nl, dt, tpb, 1, sms, s) != 0) return PF_ERR_CUDA;
+  }
+  if (!stats) return PF_OK;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nnets && e == cudaSuccess; ++k)
+    e = cudaMemcpyAsync(nets[k]->h_counters, nets[k]->d_counters, 8 * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return PF_ERR_CUDA;
+  bool timeout = false, failures = false;
+  for (int k = 0; k < nnets; ++k) {
+    const unsigned long long* h = nets[k]->h_counters;
+    stats[k].cells = states[k].ncells;
+    stats[k].newton_iterations = (int64_t)h[1];
+    stats[k].failed_cells = (int64_t)h[2];
+    stats[k].max_newton_iterations = (int32_t)h[4];
+    stats[k].max_substeps = (int32_t)h[5];
+    timeout = timeout || h[3];
+    failures = failures || h[2];
+  }
+  if (timeout) return PF_ERR_TIMEOUT;
+  return failures ? PF_CELL_FAILURES : PF_OK;
+}
+
 int32_t pf_update_auxvars(PfNetwork* net, const PfCellState* state, int32_t update_activity_coefs,
                           void* stream) {
   int rc = validate_state(net, state);

@@ -109,6 +109,13 @@ size_t batched_scratch_doubles(const DevNet& net, int64_t ncells) {
   return (size_t)(net.ns + net.nm + net.n) * (size_t)ncells;
 }
 
+int launch_cell_setup(const DevNet& net, const PfCellState& st, double* scratch, cudaStream_t stream) {
+  const int tpb = 128;
+  const int64_t blocks = (st.ncells + tpb - 1) / tpb;
+  if (blocks) cell_setup_kernel<<<blocks, tpb, 0, stream>>>(net, st, scratch);
+  return (int)cudaGetLastError();
+}
+
 int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, const PfLaunchConfig& cfg,
                          int num_sms, double* scratch, unsigned long long* queue, unsigned long long* counters,
                          cudaStream_t stream, const PfAdjointArgs* adj, double* adj_store) {
@@ -117,11 +124,8 @@ int launch_rstep_batched(const DevNet& net, const PfCellState& st, double dt, co
   // kernel reads neither the linear formulation nor the other refused modes)
   if (grp && !group_supported(net, cfg.lanes_per_cell)) return (int)cudaErrorInvalidConfiguration;
   {
-    const int tpb = 128;
-    const int64_t blocks = (st.ncells + tpb - 1) / tpb;
-    if (blocks) cell_setup_kernel<<<blocks, tpb, 0, stream>>>(net, st, scratch);
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return (int)e;
+    const int e = launch_cell_setup(net, st, scratch, stream);
+    if (e) return e;
   }
   if (grp)
     return launch_rstep_group(net, net.grp, st, dt, cfg, num_sms, scratch, queue, counters, stream, adj,

@@ -73,7 +73,7 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
 
 // the per-entry assembly tables are staged in shared memory when they fit
 // beside the block's cells, else read through L1
-static bool group_entries_staged(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
+bool group_entries_staged(const DevNet& net, const PfLaunchConfig& cfg, bool adj) {
   const int G = cfg.lanes_per_cell > 0 ? cfg.lanes_per_cell : 1;
   const size_t cells = (size_t)cfg.threads_per_block / (size_t)G;
   const size_t ws = cells * ((size_t)group::ws_doubles(net, adj, G) * 8 + (size_t)net.n * 8);

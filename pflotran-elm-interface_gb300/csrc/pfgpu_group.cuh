@@ -52,56 +52,75 @@ __device__ __forceinline__ unsigned long long gmax(unsigned long long v, unsigne
   return v;
 }
 
-template <int G, int R, bool ADJ>
-__global__ void __launch_bounds__(256)
-rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
-                   unsigned long long* queue, unsigned long long* counters, PfAdjointArgs adj,
-                   double* __restrict__ adj_store) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(8) uint64_t tma_bar;
+// Staging of a network's tables into the block's shared memory: one bulk
+// TMA copy of each packed block (the prefixes the group kernel reads), on an
+// mbarrier whose phase `parity` completes the copy; a bounded wait (never a
+// hang): on a timeout the launch-level error flag is set and every thread of
+// the block returns false together.  `init` initialises the barrier (the
+// first staging of a launch); a later staging into the same memory must
+// follow a __syncthreads() after the last reads of the previous tables.
+__device__ __forceinline__ bool stage_tables(const DevNet& net, unsigned char* smem, uint64_t* bar, uint32_t parity,
+                                             bool init, unsigned long long* counters) {
   const int tid = threadIdx.x;
-  const int lane_id = tid & 31;
-  // the prefixes this kernel reads, with or without the per-entry tables
   const uint32_t ibytes = (uint32_t)(net.ent_staged ? net.int_words_grp : net.int_words_core) * 4u;
   const uint32_t dbytes = (uint32_t)(net.ent_staged ? net.dbl_words_grp : net.dbl_words_core) * 8u;
   int32_t* sI = reinterpret_cast<int32_t*>(smem);
   double* sD = reinterpret_cast<double*>(smem + ibytes);
-
-  // ---- stage the network tables: one bulk TMA copy per block -------------
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&tma_bar)), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (init) {
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(1));
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
   }
-  __syncthreads();
   if (tid == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&tma_bar)),
+    // the block's earlier generic-proxy accesses to this memory come before
+    // the async-proxy writes of the copy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                  "r"(ibytes + dbytes)
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(sI)),
-                 "l"(net.ints), "r"(ibytes), "r"(smem_u32(&tma_bar))
+                 "l"(net.ints), "r"(ibytes), "r"(smem_u32(bar))
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(sD)),
-                 "l"(net.dbls), "r"(dbytes), "r"(smem_u32(&tma_bar))
+                 "l"(net.dbls), "r"(dbytes), "r"(smem_u32(bar))
                  : "memory");
   }
-  {
-    uint32_t done = 0;
-    long long spins = 0;
-    while (!done && spins < TMA_WAIT_LIMIT) {
-      asm volatile(
-          "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-          : "=r"(done)
-          : "r"(smem_u32(&tma_bar)), "r"(0)
-          : "memory");
-      ++spins;
-    }
-    if (__syncthreads_or(!done)) {
-      if (tid == 0) atomicOr(&counters[2], 1ull);
-      return;
-    }
+  uint32_t done = 0;
+  long long spins = 0;
+  while (!done && spins < TMA_WAIT_LIMIT) {
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    ++spins;
   }
+  if (__syncthreads_or(!done)) {
+    if (tid == 0) atomicOr(&counters[2], 1ull);
+    return false;
+  }
+  return true;
+}
+
+// The step for the cells of one network's work queue, by the block's warps,
+// with the network's tables already staged at the start of smem.  A warp
+// returns when the queue is empty and its cells are done.
+template <int G, int R, bool ADJ>
+__device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& gt, const PfCellState& st,
+                                           double dt_uniform, const double* __restrict__ scratch,
+                                           unsigned long long* queue, unsigned long long* counters,
+                                           const PfAdjointArgs& adj, double* __restrict__ adj_store,
+                                           unsigned char* smem) {
+  const int tid = threadIdx.x;
+  const int lane_id = tid & 31;
+  const uint32_t ibytes = (uint32_t)(net.ent_staged ? net.int_words_grp : net.int_words_core) * 4u;
+  const uint32_t dbytes = (uint32_t)(net.ent_staged ? net.dbl_words_grp : net.dbl_words_core) * 8u;
+  const int32_t* sI = reinterpret_cast<const int32_t*>(smem);
+  const double* sD = reinterpret_cast<const double*>(smem + ibytes);
   const Tables T{sI, sD, &net};
 
   const int n = net.n, ns = net.ns, nm = net.nm;
@@ -855,6 +874,17 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
       atomicMax(&counters[4], my_maxsub);
     }
   }
+}
+
+template <int G, int R, bool ADJ>
+__global__ void __launch_bounds__(256)
+rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
+                   unsigned long long* queue, unsigned long long* counters, PfAdjointArgs adj,
+                   double* __restrict__ adj_store) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(8) uint64_t tma_bar;
+  if (!stage_tables(net, smem, &tma_bar, 0u, true, counters)) return;
+  group_body<G, R, ADJ>(net, gt, st, dt_uniform, scratch, queue, counters, adj, adj_store, smem);
 }
 
 template <int G, int R>

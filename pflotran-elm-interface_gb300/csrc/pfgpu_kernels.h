@@ -30,6 +30,26 @@ int launch_rstep_group(const DevNet& net, const GroupTabs& gt, const PfCellState
                        const PfLaunchConfig& cfg, int num_sms, const double* scratch, unsigned long long* queue,
                        unsigned long long* counters, cudaStream_t stream, const PfAdjointArgs* adj = nullptr,
                        double* adj_store = nullptr);
+// whether a group launch of this configuration stages the per-entry tables
+bool group_entries_staged(const DevNet& net, const PfLaunchConfig& cfg, bool adj);
+// the batched kernels' per-cell set-up pre-pass (pfgpu_batched.cu)
+int launch_cell_setup(const DevNet& net, const PfCellState& st, double* scratch, cudaStream_t stream);
+// one persistent launch over several networks' cells (pfgpu_multi.cu): per
+// network its tables, state, set-up scratch, work-queue counter and
+// reductions (both zeroed by the caller), and the group size
+struct MultiNetLaunch {
+  DevNet net;
+  PfCellState st;
+  double* scratch;
+  unsigned long long* queue;
+  unsigned long long* counters;
+  int lanes_per_cell;
+};
+// the group size the multi-network kernel runs a network with (the preferred
+// one when it carries it), 0 when it carries none for this network
+int multi_lanes_for(const DevNet& net, int preferred);
+int launch_rstep_multi(const MultiNetLaunch* nets, int nnets, double dt, int threads_per_block, int blocks_per_sm,
+                       int num_sms, cudaStream_t stream);
 // host: the group kernel's lookup tables from the host copies of the packed
 // network blocks
 int group_build_tables(const DevNet& net, const int32_t* h_ints, const double* h_dbls, void** d_buf,

@@ -53,6 +53,7 @@ PF_MAX_NMNRL = 16
 PF_MAX_SPEC_PER_RXN = 24
 PF_MAX_NKD = 8
 PF_MAX_NIONX = 4
+PF_MULTI_MAX_NETS = 16
 PF_MAX_IONX_CATIONS = 8
 PF_SORPTION_LINEAR = 1
 PF_SORPTION_LANGMUIR = 2
@@ -251,6 +252,8 @@ SIGNATURES = {
     "pf_transport_read_stats": (C.c_int32, [_P, C.c_double, _P, C.POINTER(PfTransportStats)]),
     "pf_girt_assemble": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(PfGirtArgs), _P]),
     "pf_rstep_noalloc": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, _P, C.POINTER(PfStepStats)]),
+    "pf_rstep_multi": (C.c_int32, [C.POINTER(C.c_void_p), C.POINTER(PfCellState), C.c_int32, C.c_double, _P,
+                                   C.POINTER(PfStepStats)]),
     "pf_rstep_host": (C.c_int32, [_P, C.POINTER(PfCellState), C.c_double, C.c_int32,
                                   C.POINTER(PfStepStats)]),
     "pf_equilibrate_constraint": (C.c_int32, [_P, C.POINTER(PfCellState), C.POINTER(C.c_int32),

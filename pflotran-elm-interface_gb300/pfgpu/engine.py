@@ -186,3 +186,26 @@ class ReactionEngine:
         abi.check("pf_update_activity_coefs",
                   self.lib.pf_update_activity_coefs(self.handle, C.byref(s), _stream_ptr(stream)),
                   allow_cell_failures=False)
+
+
+def rstep_multi(members, dt: float, stream=None, stats: bool = True, orders=None):
+    """One operator-split step for the cells of several networks in one
+    persistent launch (pf_rstep_multi): members is a sequence of
+    (ReactionEngine, CellState of CUDA tensors), processed in that order
+    (costliest first); orders: optional per-member work-queue permutations.
+    Returns a list of per-member statistics dicts (stats=True)."""
+    lib = members[0][0].lib
+    n = len(members)
+    handles = (C.c_void_p * n)(*[eng.handle.value for eng, _ in members])
+    structs = (abi.PfCellState * n)()
+    for k, (eng, st) in enumerate(members):
+        s = st.struct("device", eng.net)
+        if orders is not None and orders[k] is not None:
+            s.cell_order = C.cast(orders[k].data_ptr(), C.POINTER(C.c_int64))
+        structs[k] = s
+    out = (abi.PfStepStats * n)() if stats else None
+    rc = lib.pf_rstep_multi(handles, structs, n, float(dt), _stream_ptr(stream), out)
+    abi.check("pf_rstep_multi", rc)
+    if not stats:
+        return None
+    return [{k: getattr(o, k) for k, _ in abi.PfStepStats._fields_} for o in out]

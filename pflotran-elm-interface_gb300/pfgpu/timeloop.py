@@ -39,14 +39,17 @@ class TransportStage:
 
 class OperatorSplitLoop:
     def __init__(self, members, dt: float = 0.0, kernel: int = abi.PF_KERNEL_BATCHED, cost_order: bool = True,
-                 concurrent: bool = False):
+                 concurrent: bool = False, multi: bool = False):
         """members: sequence of (ReactionEngine, CellState on the device) or
         (ReactionEngine, CellState, TransportStage).
         dt: uniform step [s]; ignored by the reaction step of states that
         carry a per-cell dt; a member with transport needs dt > 0.
         concurrent: run each member's step on its own stream (forked from
         and joined back into the calling stream every step), so that one
-        network's queue tail overlaps the next network's work."""
+        network's queue tail overlaps the next network's work.
+        multi: the reaction steps of all members in one persistent launch
+        (pf_rstep_multi, members in the given order: list the costliest
+        first), after every member's auxvar update and transport."""
         self.members = [tuple(m) if len(m) == 3 else (m[0], m[1], None) for m in members]
         self.dt = float(dt)
         for _, st, tr in self.members:
@@ -57,6 +60,9 @@ class OperatorSplitLoop:
         self.graph = None
         self.nsteps = 0
         self.concurrent = concurrent
+        self.multi = multi
+        if multi and (concurrent or kernel != abi.PF_KERNEL_BATCHED):
+            raise ValueError("multi runs the batched kernel on the calling stream")
         self._streams = None
 
     def _order(self, st):
@@ -65,21 +71,30 @@ class OperatorSplitLoop:
             return None
         return torch.argsort(st.a["newton_its"].to(torch.int64), descending=True)
 
-    def _member_step(self, eng, st, tr):
+    def _member_step(self, eng, st, tr, react=True):
         eng.update_auxvars(st, False)
         if eng.net.options["act_coef_update_frequency"] == abi.PF_ACT_COEF_TIMESTEP:
             eng.update_activity_coefs(st)
         if tr is not None:
             tr.solver.enqueue(st, self.dt, tr.inner_iterations, tr.refinements, tr.rtol)
-        # a state's per-cell dt array, when present, overrides dt
-        dt = self.dt if self.dt > 0.0 else 1.0
-        eng.rstep(st, dt, kernel=self.kernel, stats=False, order=self._order(st))
+        if react:
+            # a state's per-cell dt array, when present, overrides dt
+            dt = self.dt if self.dt > 0.0 else 1.0
+            eng.rstep(st, dt, kernel=self.kernel, stats=False, order=self._order(st))
 
     def step(self):
         """One operator-split reaction step of every member, enqueued on the
         current stream (and, when concurrent, on per-member streams joined
         back into it); no host synchronisation."""
         import torch
+        if self.multi:
+            from .engine import rstep_multi
+            orders = [self._order(st) for _, st, _ in self.members]
+            for eng, st, tr in self.members:
+                self._member_step(eng, st, tr, react=False)
+            rstep_multi([(eng, st) for eng, st, _ in self.members], self.dt if self.dt > 0.0 else 1.0,
+                        stats=False, orders=orders)
+            return
         if not self.concurrent:
             for eng, st, tr in self.members:
                 self._member_step(eng, st, tr)
