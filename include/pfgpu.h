@@ -72,24 +72,38 @@ enum {
 #define PF_MAX_NKD 8            /* isotherm (K_D) reactions            */
 #define PF_MAX_NIONX 4          /* ion-exchange reactions              */
 #define PF_MAX_IONX_CATIONS 8   /* cations per ion-exchange reaction   */
+#define PF_MAX_NSRFCPLX_RXN 4   /* surface complexation reactions (sites) */
+#define PF_MAX_NSRFCPLX 16      /* surface complexes over all reactions  */
 
 /* isotherm types (reaction_isotherm_aux.F90 SORPTION_*) */
 enum { PF_SORPTION_LINEAR = 1, PF_SORPTION_LANGMUIR = 2, PF_SORPTION_FREUNDLICH = 3 };
 /* K_D units (isotherm%ikd_units) */
 enum { PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1 };
+/* surface types of a surface complexation reaction (srfcplxrxn_surf_type):
+ * the site density is mol/m^3 bulk (NULL), per unit volume fraction of a
+ * kinetic mineral (MINERAL), or per kg of solid, times the soil particle
+ * density and (1 - porosity) (ROCK) */
+enum { PF_SURF_NULL = 0, PF_SURF_MINERAL = 1, PF_SURF_ROCK = 2 };
 
 /*
- * Equilibrium sorption (RTotalSorb, reaction.F90:4783-4832): K_D isotherms
- * (RTotalSorbKD, reaction_isotherm.F90:273-359) and equilibrium ion
- * exchange (RTotalSorbEqIonx, reaction.F90:4906-5140), added to the
- * accumulation as total_sorb * volume (RAccumulationSorb[Derivative],
- * reaction.F90:5144-5210).  Surface complexation and dynamic K_D are not
+ * Equilibrium sorption (RTotalSorb, reaction.F90:4783-4832): equilibrium
+ * surface complexation (RTotalSorbEqSurfCplx1,
+ * reaction_surf_complex.F90:641-900), equilibrium ion exchange
+ * (RTotalSorbEqIonx, reaction.F90:4906-5140) and K_D isotherms
+ * (RTotalSorbKD, reaction_isotherm.F90:273-359), in that order, added to
+ * the accumulation as total_sorb * volume (RAccumulationSorb[Derivative],
+ * reaction.F90:5144-5210).  Dynamic K_D and multirate sorption are not
  * built.  Supported by pf_update_auxvars, pf_equilibrate_constraint[_ex]
  * and pf_rstep (the plain kernel and the one-lane batched kernel; a launch
  * configuration with several lanes per cell is refused) and
  * pf_girt_assemble (sorbed accumulation S*V/dt and its derivative
  * dS/dm*V/dt on the diagonal block, reactive_transport.F90:2412, 3183);
  * pf_adjoint returns PF_ERR_UNSUPPORTED for a network with sorption.
+ * Surface complex k of reaction r (k from srfcplx_rxn_ptr[r] to
+ * srfcplx_rxn_ptr[r+1]-1): S_k = exp(-logK_k ln10 + nu_fk ln S_x
+ * + sum_j nu_jk ln a_j (+ h2o_k ln a_H2O)), S_x the reaction's free-site
+ * concentration from its site balance (a Newton iteration when some nu_fk
+ * > 1, else closed form), warm-started from PfCellState.srfcplx_free_site.
  */
 typedef struct PfSorptionDesc {
   int32_t nkd;                    /* isotherm reactions, <= PF_MAX_NKD             */
@@ -112,6 +126,23 @@ typedef struct PfSorptionDesc {
   const int32_t* ionx_mineral;    /* [nionx] kinetic mineral whose volume fraction
                                      scales the CEC (eqionx_rxn_to_surf - 1), -1
                                      none; or NULL                                 */
+  /* equilibrium surface complexation (surface_complexation_type,
+   * reaction_surface_complexation_aux.F90) */
+  int32_t nsrfcplx_rxn;           /* reactions (sites), <= PF_MAX_NSRFCPLX_RXN      */
+  int32_t nsrfcplx;               /* complexes of all reactions, <= PF_MAX_NSRFCPLX */
+  const int32_t* srfcplx_rxn_ptr; /* [nsrfcplx_rxn + 1] (srfcplxrxn_to_complex)     */
+  const int32_t* srfcplx_surf_type;   /* [nsrfcplx_rxn] PF_SURF_*                   */
+  const int32_t* srfcplx_mineral;     /* [nsrfcplx_rxn] kinetic mineral of a MINERAL
+                                         surface (srfcplxrxn_to_surf - 1), or NULL */
+  const double* srfcplx_site_density; /* [nsrfcplx_rxn] srfcplxrxn_site_density     */
+  int32_t srfcplx_stride;             /* row stride of srfcplx_spec / _stoich       */
+  const int32_t* srfcplx_nspec;       /* [nsrfcplx] srfcplxspecid(0,:)              */
+  const int32_t* srfcplx_spec;        /* [nsrfcplx*stride] primary index            */
+  const double* srfcplx_stoich;       /* [nsrfcplx*stride]                          */
+  const double* srfcplx_free_site_stoich; /* [nsrfcplx]                             */
+  const double* srfcplx_logK;         /* [nsrfcplx] at the reference temperature    */
+  const double* srfcplx_logKcoef;     /* [nsrfcplx*5] or NULL (isothermal)          */
+  const double* srfcplx_h2o_stoich;   /* [nsrfcplx] srfcplxh2ostoich, or NULL       */
 } PfSorptionDesc;
 
 /*
@@ -269,6 +300,12 @@ typedef struct PfCellState {
   double* ln_act_h2o;      /* [1] rt_auxvar%ln_act_h2o (in; out where activity
                               coefficients are updated); NULL reads as 0.
                               Required when use_activity_h2o                   */
+  /* networks with surface complexation only (NULL otherwise): */
+  double* srfcplx_free_site; /* [nsrfcplx_rxn] srfcplxrxn_free_site_conc, mol/m^3
+                                bulk: the site balance's warm start, updated in
+                                place as the reference updates rt_auxvar         */
+  double* srfcplx_conc;      /* [nsrfcplx] eqsrfcplx_conc (out, mol/m^3 bulk) of
+                                the last evaluation, or NULL                    */
 } PfCellState;
 
 typedef struct PfStepStats {

@@ -38,7 +38,8 @@ module pfgpu_mod
       PF_MAX_IONX_CATIONS = 8, PF_MAX_PREFACTORS = 4, PF_MAX_PREFACTOR_SPECIES = 4, &
       PF_ADJ_MAX_SUBSTEPS = 16, PF_MULTI_MAX_NETS = 16
   integer(c_int32_t), parameter, public :: PF_SORPTION_LINEAR = 1, PF_SORPTION_LANGMUIR = 2, &
-      PF_SORPTION_FREUNDLICH = 3, PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1
+      PF_SORPTION_FREUNDLICH = 3, PF_KD_UNIT_KG_M3_BULK = 0, PF_KD_UNIT_MLW_GSOIL = 1, &
+      PF_SURF_NULL = 0, PF_SURF_MINERAL = 1, PF_SURF_ROCK = 2, PF_MAX_NSRFCPLX_RXN = 4, PF_MAX_NSRFCPLX = 16
   integer(c_int32_t), parameter, public :: PF_BC_ZERO_FLUX = 0, PF_BC_DIRICHLET = 1, &
       PF_BC_DIRICHLET_ZERO_GRADIENT = 2, PF_BC_ZERO_GRADIENT = 3, PF_SRC_VOLUMETRIC = 0, &
       PF_SRC_EQUILIBRIUM = 1, PF_SRC_MASS_RATE = 2
@@ -54,6 +55,11 @@ module pfgpu_mod
     real(c_double) :: soil_particle_density
     integer(c_int32_t) :: nionx, ionx_stride
     type(c_ptr) :: ionx_ncation, ionx_cation, ionx_k, ionx_cec, ionx_mineral
+    integer(c_int32_t) :: nsrfcplx_rxn, nsrfcplx
+    type(c_ptr) :: srfcplx_rxn_ptr, srfcplx_surf_type, srfcplx_mineral, srfcplx_site_density
+    integer(c_int32_t) :: srfcplx_stride
+    type(c_ptr) :: srfcplx_nspec, srfcplx_spec, srfcplx_stoich, srfcplx_free_site_stoich, srfcplx_logK, &
+                   srfcplx_logKcoef, srfcplx_h2o_stoich
   end type
 
   ! kinetic-mineral rate prefactors (kinmnrl_pref_*)
@@ -94,7 +100,8 @@ module pfgpu_mod
     type(c_ptr) :: total, pri_molal, pri_act_coef, sec_act_coef, sec_molal, &
                    mnrl_volfrac, mnrl_area, mnrl_rate, porosity, saturation, &
                    den_kg, volume, temperature, dt_cell, status, newton_its, &
-                   num_substeps, cell_order, total_sorb, ionx_ref_sorbed, ln_act_h2o
+                   num_substeps, cell_order, total_sorb, ionx_ref_sorbed, ln_act_h2o, &
+                   srfcplx_free_site, srfcplx_conc
   end type
 
   type, bind(C), public :: pf_step_stats_t
@@ -365,6 +372,8 @@ contains
     state%total_sorb = c_null_ptr               ! networks without sorption
     state%ionx_ref_sorbed = c_null_ptr
     state%ln_act_h2o = c_null_ptr
+    state%srfcplx_free_site = c_null_ptr        ! networks without surface complexation
+    state%srfcplx_conc = c_null_ptr
     if (nsec == 0) then
       state%sec_act_coef = c_null_ptr
       state%sec_molal = c_null_ptr

@@ -43,6 +43,9 @@ inline void gather(const Net& net, const PfCellState* s, int64_t i, Cell& c) {
   for (int k = 0; k < net.n; ++k) c.total_sorb[k] = s->total_sorb ? s->total_sorb[k * N + i] : 0.0;
   const int nionx = net.sorb ? net.sorb->nionx : 0;
   for (int k = 0; k < nionx; ++k) c.ionx_ref[k] = s->ionx_ref_sorbed ? s->ionx_ref_sorbed[k * N + i] : 1.0e-9;
+  const int nsrx = net.sorb ? net.sorb->nsrfcplx_rxn : 0, nsc = net.sorb ? net.sorb->nsrfcplx : 0;
+  for (int k = 0; k < nsrx; ++k) c.srf_free[k] = s->srfcplx_free_site ? s->srfcplx_free_site[k * N + i] : 1.0e-9;
+  for (int k = 0; k < nsc; ++k) c.srf_conc[k] = s->srfcplx_conc ? s->srfcplx_conc[k * N + i] : 0.0;
   set_logK(net, c);
 }
 
@@ -67,6 +70,10 @@ inline void scatter(const Net& net, const PfCellState* s, int64_t i, const Cell&
   if (s->ionx_ref_sorbed && net.sorb)
     for (int k = 0; k < net.sorb->nionx; ++k) s->ionx_ref_sorbed[k * N + i] = c.ionx_ref[k];
   if (s->ln_act_h2o) s->ln_act_h2o[i] = c.ln_act_h2o;
+  if (s->srfcplx_free_site && net.sorb)
+    for (int k = 0; k < net.sorb->nsrfcplx_rxn; ++k) s->srfcplx_free_site[k * N + i] = c.srf_free[k];
+  if (s->srfcplx_conc && net.sorb)
+    for (int k = 0; k < net.sorb->nsrfcplx; ++k) s->srfcplx_conc[k * N + i] = c.srf_conc[k];
 }
 
 // Rate prefactors: counts and ids in range; a primary prefactor species that

@@ -65,6 +65,9 @@ struct Cell {
   double total_sorb[MAXN];
   double dtotal_sorb[MAXN * MAXN];
   double ionx_ref[PF_MAX_NIONX];
+  // surface complexation: srfcplxrxn_free_site_conc, eqsrfcplx_conc
+  double srf_free[PF_MAX_NSRFCPLX_RXN];
+  double srf_conc[PF_MAX_NSRFCPLX];
 };
 
 struct Net {
@@ -79,7 +82,7 @@ struct Net {
   const PfPrefactorDesc* pref;  // null: no rate prefactors
   explicit Net(const PfNetworkDesc* desc) : d(desc), o(desc->opts), n(desc->ncomp),
       ns(desc->nsec), nm(desc->nmnrl),
-      sorb(desc->sorption && (desc->sorption->nkd > 0 || desc->sorption->nionx > 0) ? desc->sorption
+      sorb(desc->sorption && (desc->sorption->nkd > 0 || desc->sorption->nionx > 0 || desc->sorption->nsrfcplx_rxn > 0) ? desc->sorption
                                                                                       : nullptr),
       pref(desc->prefactors) {}
   // kinmnrl_num_prefactors, kinmnrl_prefactor_id(0,p,m) and the per-prefactor
@@ -417,11 +420,117 @@ inline void total_sorb_kd(const Net& net, Cell& c) {
 // RTotalSorb, reaction.F90:4783-4832 (RZeroSorb :4763-4779, then ion
 // exchange, then K_D; no surface complexation, no dynamic K_D).  Returns the
 // ion exchange's ierror.
+// RTotalSorbEqSurfCplx1 (reaction_surf_complex.F90:641-900), every
+// equilibrium surface complexation reaction in turn (RTotalSorbEqSurfCplx,
+// :446-491): the free-site concentration from the site balance (Newton when
+// a complex holds more than one site, tolerance 1e-12 on the relative change,
+// damping 0.5 after 1000 iterations; otherwise the closed form), the
+// complexes' concentrations, the sorbed totals and their derivative with
+// respect to the free-ion molalities (the free site's response included).
+// The complexes' logK follow the cell temperature like the others
+// (RUpdateTempDependentCoefs, reaction.F90:6025-6030).
+inline void total_sorb_eq_srfcplx(const Net& net, Cell& c) {
+  const PfSorptionDesc* sd = net.sorb;
+  const int n = net.n;
+  double ln_act[MAXN];
+  for (int i = 0; i < n; ++i) ln_act[i] = std::log(c.pri_molal[i]) + std::log(c.pri_act_coef[i]);  // :686-687
+  double logK[PF_MAX_NSRFCPLX];
+  for (int k = 0; k < sd->nsrfcplx; ++k) logK[k] = sd->srfcplx_logK[k];
+  if (!net.o.isothermal && sd->srfcplx_logKcoef) interpolate_logK(sd->srfcplx_logKcoef, logK, c.temp, sd->nsrfcplx);
+  for (int irxn = 0; irxn < sd->nsrfcplx_rxn; ++irxn) {
+    const int k0 = sd->srfcplx_rxn_ptr[irxn], k1 = sd->srfcplx_rxn_ptr[irxn + 1];
+    bool stoich_flag = false;  // srfcplxrxn_stoich_flag, reaction_database.F90:2801-2803
+    for (int k = k0; k < k1; ++k) stoich_flag = stoich_flag || sd->srfcplx_free_site_stoich[k] > 1.0;
+    double free_site_conc = std::max(c.srf_free[irxn], 1.0e-40);  // :691
+    for (int k = k0; k < k1; ++k) c.srf_conc[k] = 0.0;
+    double site_density;
+    switch (sd->srfcplx_surf_type[irxn]) {
+      case PF_SURF_MINERAL:
+        site_density = sd->srfcplx_site_density[irxn] * c.mnrl_volfrac[sd->srfcplx_mineral[irxn]];
+        break;
+      case PF_SURF_ROCK:
+        site_density = sd->srfcplx_site_density[irxn] * sd->soil_particle_density * (1.0 - c.porosity);
+        break;
+      default:
+        site_density = sd->srfcplx_site_density[irxn];
+    }
+    if (site_density < 1.0e-40) {  // :728-737
+      c.srf_free[irxn] = 0.0;
+      continue;
+    }
+    bool one_more = false;
+    int num_iterations = 0;
+    double damping_factor = 1.0;
+    for (;;) {  // :743-799
+      num_iterations = num_iterations + 1;
+      double total = free_site_conc;
+      const double ln_free_site = std::log(free_site_conc);
+      for (int k = k0; k < k1; ++k) {
+        double lnQK = -logK[k] * LOG_TO_LN;
+        if (sd->srfcplx_h2o_stoich && sd->srfcplx_h2o_stoich[k] != 0.0)
+          lnQK = lnQK + sd->srfcplx_h2o_stoich[k] * c.ln_act_h2o;
+        lnQK = lnQK + sd->srfcplx_free_site_stoich[k] * ln_free_site;
+        for (int p = 0; p < sd->srfcplx_nspec[k]; ++p)
+          lnQK = lnQK + sd->srfcplx_stoich[k * sd->srfcplx_stride + p] * ln_act[sd->srfcplx_spec[k * sd->srfcplx_stride + p]];
+        c.srf_conc[k] = std::exp(lnQK);
+        total = total + sd->srfcplx_free_site_stoich[k] * c.srf_conc[k];
+      }
+      if (one_more) break;
+      if (stoich_flag) {
+        const double res = site_density - total;
+        double dres_dfree_site = 1.0;
+        for (int k = k0; k < k1; ++k)
+          dres_dfree_site = dres_dfree_site + sd->srfcplx_free_site_stoich[k] * c.srf_conc[k] / free_site_conc;
+        const double dfree_site_conc = res / dres_dfree_site;
+        if (num_iterations > 1000) damping_factor = 0.5;
+        free_site_conc = free_site_conc + damping_factor * dfree_site_conc;
+        if (std::fabs(dfree_site_conc / free_site_conc) < 1.0e-12) one_more = true;
+      } else {
+        total = total / free_site_conc;
+        free_site_conc = site_density / total;
+        one_more = true;
+      }
+    }
+    c.srf_free[irxn] = free_site_conc;
+    // derivative of the free site (:803-824)
+    double dSx_dmi[MAXN];
+    for (int i = 0; i < n; ++i) dSx_dmi[i] = 0.0;
+    double tempreal = 0.0;
+    for (int k = k0; k < k1; ++k) {
+      for (int p = 0; p < sd->srfcplx_nspec[k]; ++p) {
+        const int icomp = sd->srfcplx_spec[k * sd->srfcplx_stride + p];
+        dSx_dmi[icomp] = dSx_dmi[icomp] +
+                         sd->srfcplx_stoich[k * sd->srfcplx_stride + p] * sd->srfcplx_free_site_stoich[k] * c.srf_conc[k];
+      }
+      tempreal = tempreal + sd->srfcplx_free_site_stoich[k] * sd->srfcplx_free_site_stoich[k] * c.srf_conc[k];
+    }
+    tempreal = tempreal / free_site_conc;
+    tempreal = tempreal + 1.0;
+    for (int i = 0; i < n; ++i) dSx_dmi[i] = -dSx_dmi[i] / tempreal;
+    for (int i = 0; i < n; ++i) dSx_dmi[i] = dSx_dmi[i] / c.pri_molal[i];
+    // sorbed totals and their derivative (:846-893)
+    for (int k = k0; k < k1; ++k) {
+      const int nc = sd->srfcplx_nspec[k];
+      const int* ids = sd->srfcplx_spec + k * sd->srfcplx_stride;
+      auto nu = [&](int p) { return sd->srfcplx_stoich[k * sd->srfcplx_stride + p]; };
+      for (int p = 0; p < nc; ++p) c.total_sorb[ids[p]] = c.total_sorb[ids[p]] + nu(p) * c.srf_conc[k];
+      const double nui_Si_over_Sx = sd->srfcplx_free_site_stoich[k] * c.srf_conc[k] / free_site_conc;
+      for (int q = 0; q < nc; ++q) {
+        const int jcomp = ids[q];
+        const double t = nu(q) * c.srf_conc[k] / c.pri_molal[jcomp] + nui_Si_over_Sx * dSx_dmi[jcomp];
+        for (int p = 0; p < nc; ++p)
+          c.dtotal_sorb[ids[p] * MAXN + jcomp] = c.dtotal_sorb[ids[p] * MAXN + jcomp] + nu(p) * t;
+      }
+    }
+  }
+}
+
 inline int total_sorb(const Net& net, Cell& c) {
   for (int i = 0; i < net.n; ++i) {
     c.total_sorb[i] = 0.0;
     for (int j = 0; j < net.n; ++j) c.dtotal_sorb[i * MAXN + j] = 0.0;
   }
+  if (net.sorb->nsrfcplx_rxn > 0) total_sorb_eq_srfcplx(net, c);
   if (net.sorb->nionx > 0 && total_sorb_eq_ionx(net, c) != 0) return 1;
   if (net.sorb->nkd > 0) total_sorb_kd(net, c);
   return 0;

@@ -110,6 +110,32 @@ int validate_desc(const PfNetworkDesc* d) {
       }
       if (sd->ionx_mineral && (sd->ionx_mineral[r] < -1 || sd->ionx_mineral[r] >= d->nmnrl)) return PF_ERR_INVALID;
     }
+    if (sd->nsrfcplx_rxn < 0 || sd->nsrfcplx < 0) return PF_ERR_INVALID;
+    if (sd->nsrfcplx_rxn > PF_MAX_NSRFCPLX_RXN || sd->nsrfcplx > PF_MAX_NSRFCPLX) return PF_ERR_TOO_LARGE;
+    if (sd->nsrfcplx_rxn > 0) {
+      if (!sd->srfcplx_rxn_ptr || !sd->srfcplx_surf_type || !sd->srfcplx_site_density || !sd->srfcplx_nspec ||
+          !sd->srfcplx_spec || !sd->srfcplx_stoich || !sd->srfcplx_free_site_stoich || !sd->srfcplx_logK ||
+          sd->srfcplx_stride < 1)
+        return PF_ERR_INVALID;
+      if (sd->srfcplx_rxn_ptr[0] != 0 || sd->srfcplx_rxn_ptr[sd->nsrfcplx_rxn] != sd->nsrfcplx) return PF_ERR_INVALID;
+      for (int r = 0; r < sd->nsrfcplx_rxn; ++r) {
+        if (sd->srfcplx_rxn_ptr[r + 1] <= sd->srfcplx_rxn_ptr[r]) return PF_ERR_INVALID;  // a site has complexes
+        const int t = sd->srfcplx_surf_type[r];
+        if (t != PF_SURF_NULL && t != PF_SURF_MINERAL && t != PF_SURF_ROCK) return PF_ERR_INVALID;
+        if (t == PF_SURF_MINERAL &&
+            (!sd->srfcplx_mineral || sd->srfcplx_mineral[r] < 0 || sd->srfcplx_mineral[r] >= d->nmnrl))
+          return PF_ERR_INVALID;
+      }
+      for (int k = 0; k < sd->nsrfcplx; ++k) {
+        const int ns = sd->srfcplx_nspec[k];
+        if (ns < 0 || ns > sd->srfcplx_stride || ns > PF_MAX_SPEC_PER_RXN) return PF_ERR_INVALID;
+        for (int p = 0; p < ns; ++p) {
+          const int j = sd->srfcplx_spec[k * sd->srfcplx_stride + p];
+          if (j < 0 || j >= d->ncomp) return PF_ERR_INVALID;
+        }
+        if (!(sd->srfcplx_free_site_stoich[k] > 0.0)) return PF_ERR_INVALID;
+      }
+    }
   }
   if (const PfPrefactorDesc* pf = d->prefactors) {
     if (!pf->num_prefactors || !pf->rate || !pf->activation_energy || !pf->nspec || !pf->spec || !pf->alpha ||
@@ -149,7 +175,8 @@ int validate_state(const PfNetwork* net, const PfCellState* s) {
   if (net->dev.ns > 0 && (!s->sec_act_coef || !s->sec_molal)) return PF_ERR_INVALID;
   if (net->dev.nm > 0 && (!s->mnrl_volfrac || !s->mnrl_area || !s->mnrl_rate)) return PF_ERR_INVALID;
   if (!net->dev.o.isothermal && !s->temperature) return PF_ERR_INVALID;
-  if (net->dev.nkd + net->dev.nionx > 0 && !s->total_sorb) return PF_ERR_INVALID;
+  if (has_sorption(net->dev) && !s->total_sorb) return PF_ERR_INVALID;
+  if (net->dev.nsrx > 0 && !s->srfcplx_free_site) return PF_ERR_INVALID;
   if (net->dev.nionx > 0 && !s->ionx_ref_sorbed) return PF_ERR_INVALID;
   if (net->dev.o.use_activity_h2o && !s->ln_act_h2o) return PF_ERR_INVALID;
   return PF_OK;
@@ -345,6 +372,33 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
         }
     ints.push_back(zf ? 1 : 0);
   }
+  // surface complexation: reactions' complex ranges, types, minerals,
+  // stoichiometry flags; the complexes' species CSR
+  const int nsx = sd ? sd->nsrfcplx_rxn : 0, nsc = nsx ? sd->nsrfcplx : 0;
+  dev.nsrx = nsx;
+  dev.nsrc = nsc;
+  dev.o_sx_ptr = (int)ints.size();
+  for (int r = 0; r <= nsx && nsx; ++r) ints.push_back(sd->srfcplx_rxn_ptr[r]);
+  dev.o_sx_type = (int)ints.size();
+  for (int r = 0; r < nsx; ++r) ints.push_back(sd->srfcplx_surf_type[r]);
+  dev.o_sx_min = (int)ints.size();
+  for (int r = 0; r < nsx; ++r) ints.push_back(sd->srfcplx_mineral ? sd->srfcplx_mineral[r] : -1);
+  dev.o_sx_flag = (int)ints.size();
+  for (int r = 0; r < nsx; ++r) {  // srfcplxrxn_stoich_flag (reaction_database.F90:2801-2803)
+    int f = 0;
+    for (int k = sd->srfcplx_rxn_ptr[r]; k < sd->srfcplx_rxn_ptr[r + 1]; ++k)
+      f = f || sd->srfcplx_free_site_stoich[k] > 1.0;
+    ints.push_back(f);
+  }
+  dev.o_sx_cptr = (int)ints.size();
+  {
+    int cnt = 0;
+    for (int k = 0; k < nsc; ++k) { ints.push_back(cnt); cnt += sd->srfcplx_nspec[k]; }
+    if (nsc) ints.push_back(cnt);
+  }
+  dev.o_sx_spec = (int)ints.size();
+  for (int k = 0; k < nsc; ++k)
+    for (int p = 0; p < sd->srfcplx_nspec[k]; ++p) ints.push_back(sd->srfcplx_spec[k * sd->srfcplx_stride + p]);
   // staged prefixes of the group kernel: [core] without, [grp] with the
   // per-entry tables (staged when they fit beside a block's cells)
   while (ints.size() % 4) ints.push_back(0);
@@ -414,6 +468,14 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   for (int r = 0; r < nix; ++r)
     for (int j = 0; j < sd->ionx_ncation[r]; ++j) dbls.push_back(sd->ionx_k[r * sd->ionx_stride + j]);
   dev.o_ix_cec = put(nix ? sd->ionx_cec : nullptr, nix, 0.0);
+  dev.o_sx_dens = put(nsx ? sd->srfcplx_site_density : nullptr, nsx, 0.0);
+  dev.o_sx_nu = (int)dbls.size();
+  for (int k = 0; k < nsc; ++k)
+    for (int p = 0; p < sd->srfcplx_nspec[k]; ++p) dbls.push_back(sd->srfcplx_stoich[k * sd->srfcplx_stride + p]);
+  dev.o_sx_nuf = put(nsc ? sd->srfcplx_free_site_stoich : nullptr, nsc, 1.0);
+  dev.o_sx_logK = put(nsc ? sd->srfcplx_logK : nullptr, nsc, 0.0);
+  dev.o_sx_logKcoef = put(nsc ? sd->srfcplx_logKcoef : nullptr, 5 * nsc, 0.0);
+  dev.o_sx_h2o = put(nsc ? sd->srfcplx_h2o_stoich : nullptr, nsc, 0.0);
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.dbl_words_core = (int)dbls.size();
   dev.o_ent_cf = put(ent_cf.data(), (int)ent_cf.size(), 0.0);
@@ -432,11 +494,12 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
   bool any_h2o = false;
   for (int i = 0; d->sec_h2o_stoich && i < ns; ++i) any_h2o = any_h2o || d->sec_h2o_stoich[i] != 0.0;
   for (int m = 0; d->mnrl_h2o_stoich && m < nm; ++m) any_h2o = any_h2o || d->mnrl_h2o_stoich[m] != 0.0;
+  for (int k = 0; nsc && sd->srfcplx_h2o_stoich && k < nsc; ++k) any_h2o = any_h2o || sd->srfcplx_h2o_stoich[k] != 0.0;
   while (dbls.size() % 2) dbls.push_back(0.0);
   dev.flags = (d->sec_logKcoef ? NETF_SEC_LOGKCOEF : 0) | (d->mnrl_logKcoef ? NETF_MNRL_LOGKCOEF : 0) |
               (d->mnrl_min_scale_factor ? NETF_MSF : 0) | (d->mnrl_Temkin_const ? NETF_TEMKIN : 0) |
               (d->mnrl_affinity_power ? NETF_POWER : 0) | (any_pref ? NETF_PREFACTOR : 0) |
-              (any_h2o ? NETF_H2O : 0);
+              (any_h2o ? NETF_H2O : 0) | ((nsc && sd->srfcplx_logKcoef) ? NETF_SX_LOGKCOEF : 0);
   dev.int_words = (int)ints.size();
   dev.dbl_words = (int)dbls.size();
   dev.A = d->debyeA;
@@ -690,13 +753,9 @@ int32_t pf_rstep_multi(PfNetwork* const* nets, const PfCellState* states, int32_
       return PF_ERR_CUDA;
   if (nl > 0) {
     // one block of 256 threads per SM (the group kernels' registers allow
-    // one), 128 threads when some network's workspace does not fit
-    int tpb = 256;
-    for (int k = 0; k < nl && tpb == 256; ++k) {
-      PfLaunchConfig c{256, 1, 0, L[k].lanes_per_cell};
-      if (group_smem_bytes(L[k].net, c, false) > 227u * 1024u) tpb = 128;
-    }
-    if (launch_rstep_multi(L, nl, dt, tpb, 1, sms, s) != 0) return PF_ERR_CUDA;
+    // one); a network whose workspace does not fit 256 threads' cells runs
+    // on fewer of the block's warps
+    if (launch_rstep_multi(L, nl, dt, 256, 1, sms, s) != 0) return PF_ERR_CUDA;
   }
   if (!stats) return PF_OK;
   cudaError_t e = cudaSuccess;
@@ -763,7 +822,7 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
   const DevNet& d = net->dev;
   if (!batched_supported(d)) return PF_ERR_UNSUPPORTED;
   if (d.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) return PF_ERR_UNSUPPORTED;
-  if (d.nkd + d.nionx > 0) return PF_ERR_UNSUPPORTED;  // no adjoint of the sorption terms
+  if (has_sorption(d)) return PF_ERR_UNSUPPORTED;  // no adjoint of the sorption terms
   if (!a->dL_dtotal0 || (d.nm > 0 && (!a->dL_dlnarea || !a->dL_dlogK_mnrl || !a->dL_dlnk)) ||
       (d.ns > 0 && !a->dL_dlogK_sec) || (!a->weight && !a->dL_dtotal) || (a->weight && !a->target))
     return PF_ERR_INVALID;
@@ -797,7 +856,7 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
       !a->colidx || !a->residual || !a->values || !(a->dx > 0) || !(a->dy > 0) || !(a->dz > 0))
     return PF_ERR_INVALID;
   if ((int64_t)a->nx * a->ny * a->nz != state->ncells) return PF_ERR_INVALID;
-  if (net->dev.nkd + net->dev.nionx > 0 && !a->total_sorb_k) return PF_ERR_INVALID;
+  if (has_sorption(net->dev) && !a->total_sorb_k) return PF_ERR_INVALID;
   if ((a->nx > 1 && !a->qx) || (a->ny > 1 && !a->qy) || (a->nz > 1 && !a->qz)) return PF_ERR_INVALID;
   if (!state->sec_molal && net->dev.ns) return PF_ERR_INVALID;
   if (girt_smem_bytes(net->dev, nullptr) > 227u * 1024u) return PF_ERR_TOO_LARGE;
@@ -884,6 +943,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
       {(void*)h->cell_order, 1, (int)sizeof(int64_t), false, false},  // remapped per chunk below
       {h->total_sorb, n, d8, true, true},      {h->ionx_ref_sorbed, nx, d8, true, true},
       {h->ln_act_h2o, 1, d8, true, true},
+      {h->srfcplx_free_site, net->dev.nsrx, d8, true, true}, {h->srfcplx_conc, net->dev.nsrc, d8, false, true},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
   // chunks of about 2^18 cells (at most 16); of 1, 2 and 4 chunks at 10^6
@@ -993,6 +1053,8 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     d.total_sorb = (double*)dev_field(c, 18);
     d.ionx_ref_sorbed = (double*)dev_field(c, 19);
     d.ln_act_h2o = (double*)dev_field(c, 20);
+    d.srfcplx_free_site = (double*)dev_field(c, 21);
+    d.srfcplx_conc = (double*)dev_field(c, 22);
     cudaStream_t sc = net->s_comp;
     e = cudaStreamWaitEvent(sc, net->ev_in[c], 0);
     if (e == cudaSuccess && h->cell_order)

@@ -150,7 +150,7 @@ __device__ void total(const DevNet& net, const Tables& T, const PfCellState& st,
   }
   const double den_L = st.den_kg[cell] * 1.0e-3;
   for (int j = 0; j < n; ++j) st.total[soa.at(j, cell)] = tot[j] * den_L;
-  if (net.nkd + net.nionx > 0) {
+  if (has_sorption(net)) {
     for (int j = 0; j < n; ++j) st.total_sorb[soa.at(j, cell)] = 0.0;
     // RTotal without ierror (RTUpdateAuxVars): a failed ion-exchange solve
     // leaves the last iterate, as the reference's message-and-continue does
@@ -159,7 +159,8 @@ __device__ void total(const DevNet& net, const Tables& T, const PfCellState& st,
         [&](int j) { return st.pri_act_coef[soa.at(j, cell)]; },
         [&](int m) { return st.mnrl_volfrac[soa.at(m, cell)]; }, st.porosity[cell], st.den_kg[cell],
         st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr, st.ncells,
-        [&](int j, double v) { st.total_sorb[soa.at(j, cell)] += v; }, [](int, int, double) {});
+        [&](int j, double v) { st.total_sorb[soa.at(j, cell)] += v; }, [](int, int, double) {},
+        surf_cell(net, st, cell));
   }
 }
 

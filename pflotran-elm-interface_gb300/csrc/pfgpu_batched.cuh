@@ -256,7 +256,7 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
   const bool logf = o.use_log_formulation != 0;
   const bool newton_iter_act = o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER;
   const unsigned neg_mask = (unsigned)net.neg_mask;
-  const bool has_sorb = !ADJ && net.nkd + net.nionx > 0;  // the adjoint refuses sorption
+  const bool has_sorb = !ADJ && has_sorption(net);  // the adjoint refuses sorption
   const int64_t ncells = st.ncells;
   const double* sc_sec = scratch;                                  // [ns][ncells]
   const double* sc_min = scratch + (size_t)ns * ncells;            // [nm][ncells]
@@ -589,7 +589,8 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
               st.total_sorb[soa.at(j, cell)] += v;
               L.rhs(j) = fma(v_t, v, L.rhs(j));
             },
-            [&](int i, int j, double v) { L.J(i, j) = fma(v_t * v, logf ? L.P(N + j) : 1.0, L.J(i, j)); });
+            [&](int i, int j, double v) { L.J(i, j) = fma(v_t * v, logf ? L.P(N + j) : 1.0, L.J(i, j)); },
+            surf_cell(net, st, cell));
       }
       // ---- convergence tests on the residual (reaction.F90:3946-3953) -----
       double dot = 0.0;

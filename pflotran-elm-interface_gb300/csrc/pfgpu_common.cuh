@@ -26,6 +26,7 @@ enum : int32_t {
   NETF_POWER = 16,
   NETF_PREFACTOR = 32,  // some mineral has rate prefactors
   NETF_H2O = 64,        // some complex or mineral has water in its reaction
+  NETF_SX_LOGKCOEF = 128,  // surface complexes carry logK temperature fits
 };
 
 // Device view of a network.  All pointers index one packed allocation whose
@@ -82,6 +83,14 @@ struct DevNet {
   int32_t nkd, nionx, kd_units;
   int32_t o_kd_spec, o_kd_type, o_kd_min, o_ix_ptr, o_ix_cat, o_ix_min, o_ix_zflag;
   int32_t o_kd_coeff, o_kd_b, o_kd_n, o_ix_k, o_ix_cec;
+  // equilibrium surface complexation: reactions (sites) and their complexes;
+  // ints: complexes of reaction r [sx_ptr(r), sx_ptr(r+1)), surface type,
+  // mineral, stoichiometry flag (a complex holds more than one site), the
+  // complexes' species CSR; doubles: site density, stoichiometry, free-site
+  // stoichiometry, logK, logK fits, water coefficient
+  int32_t nsrx, nsrc;
+  int32_t o_sx_ptr, o_sx_type, o_sx_min, o_sx_flag, o_sx_cptr, o_sx_spec;
+  int32_t o_sx_dens, o_sx_nu, o_sx_nuf, o_sx_logK, o_sx_logKcoef, o_sx_h2o;
   double soil_density;
   // kinetic-mineral rate prefactors (PfPrefactorDesc), dense [nm][MP] and
   // [nm][MP][MS]: counts, species ids (primary j, secondary i as -(i+1));
@@ -94,6 +103,12 @@ struct DevNet {
   PfOptions o;
   GroupTabs grp;
 };
+
+// the network has equilibrium sorption of any kind (the sorbed state
+// arrays are required, the sorbed accumulation enters the step)
+__host__ __device__ __forceinline__ bool has_sorption(const DevNet& net) {
+  return net.nkd + net.nionx + net.nsrx > 0;
+}
 
 // Table accessor over either global or shared copies of the packed blocks.
 // Water activity in ln Q/K: some reaction has water and the option is on
@@ -179,6 +194,20 @@ struct Tables {
   __device__ __forceinline__ double ix_cec(int r) const { return D[net->o_ix_cec + r]; }
   __device__ __forceinline__ int ix_min(int r) const { return I[net->o_ix_min + r]; }
   __device__ __forceinline__ int ix_zflag(int r) const { return I[net->o_ix_zflag + r]; }
+  __device__ __forceinline__ int sx_begin(int r) const { return I[net->o_sx_ptr + r]; }
+  __device__ __forceinline__ int sx_end(int r) const { return I[net->o_sx_ptr + r + 1]; }
+  __device__ __forceinline__ int sx_type(int r) const { return I[net->o_sx_type + r]; }
+  __device__ __forceinline__ int sx_min(int r) const { return I[net->o_sx_min + r]; }
+  __device__ __forceinline__ int sx_flag(int r) const { return I[net->o_sx_flag + r]; }
+  __device__ __forceinline__ int sx_cbegin(int k) const { return I[net->o_sx_cptr + k]; }
+  __device__ __forceinline__ int sx_cend(int k) const { return I[net->o_sx_cptr + k + 1]; }
+  __device__ __forceinline__ int sx_spec(int p) const { return I[net->o_sx_spec + p]; }
+  __device__ __forceinline__ double sx_dens(int r) const { return D[net->o_sx_dens + r]; }
+  __device__ __forceinline__ double sx_nu(int p) const { return D[net->o_sx_nu + p]; }
+  __device__ __forceinline__ double sx_nuf(int k) const { return D[net->o_sx_nuf + k]; }
+  __device__ __forceinline__ double sx_logK(int k) const { return D[net->o_sx_logK + k]; }
+  __device__ __forceinline__ const double* sx_logKcoef(int k) const { return D + net->o_sx_logKcoef + 5 * k; }
+  __device__ __forceinline__ double sx_h2o(int k) const { return D[net->o_sx_h2o + k]; }
   __device__ __forceinline__ int pf_cnt(int m) const { return I[net->o_pf_cnt + m]; }
   __device__ __forceinline__ double sec_h2o(int i) const { return D[net->o_sec_h2o + i]; }
   __device__ __forceinline__ double mnrl_h2o(int m) const { return D[net->o_mnrl_h2o + m]; }

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
       tot[j] *= den_L;
       for (int k = 0; k < n; ++k) J[j * NM + k] *= den_L;
     }
-    if (net.nkd + net.nionx > 0) {
+    if (has_sorption(net)) {
       // the rest of RTotal (:1594, no ierror): sorbed totals follow the
       // iterate; no constraint row here reads them
       for (int j = 0; j < n; ++j) st.total_sorb[soa.at(j, cell)] = 0.0;
@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
           net, T, [&](int j) { return c[j]; }, [&](int j) { return gam[j]; },
           [&](int m) { return st.mnrl_volfrac[soa.at(m, cell)]; }, st.porosity[cell], den,
           st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr, st.ncells,
-          [&](int j, double v) { st.total_sorb[soa.at(j, cell)] += v; }, [](int, int, double) {});
+          [&](int j, double v) { st.total_sorb[soa.at(j, cell)] += v; }, [](int, int, double) {},
+          surf_cell(net, st, cell));
     }
     // constraint rows (dtotal is J until a row is replaced; charge balance
     // reads dtotal rows of other components, so build it first)

@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   // ---- equilibrium sorption (RTotalSorb in RTUpdateAuxVars; a failed
   // ion-exchange solve leaves the last iterate, the reference's
   // message-and-continue).  Only this thread writes its diagonal block.
-  if (net.nkd + net.nionx > 0 && dblk >= 0) {
+  if (has_sorption(net) && dblk >= 0) {
     for (int jj = 0; jj < n; ++jj) st.total_sorb[soa.at(jj, X)] = 0.0;
     double* D = values + (size_t)dblk * nn;
     const double v_t = volume / dt;
@@ -450,7 +450,8 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
         [&](int m) { return st.mnrl_volfrac[soa.at(m, X)]; }, por, den_k,
         st.ionx_ref_sorbed ? st.ionx_ref_sorbed + X : nullptr, st.ncells,
         [&](int j, double v) { st.total_sorb[soa.at(j, X)] += v; },
-        [&](int i, int j, double v) { D[j * n + i] = fma(v * v_t, logf ? P[j * bd] : 1.0, D[j * n + i]); });
+        [&](int i, int j, double v) { D[j * n + i] = fma(v * v_t, logf ? P[j * bd] : 1.0, D[j * n + i]); },
+        surf_cell(net, st, X));
   }
 }
 
@@ -469,7 +470,7 @@ __global__ void __launch_bounds__(128) girt_residual_kernel(DevNet net, PfCellSt
   const double sat = st.saturation[X];
   const bool dry = sat < RT_MIN_SATURATION;
   const double psv = st.porosity[X] * sat * 1000.0 * st.volume[X];
-  const bool sorb = net.nkd + net.nionx > 0;
+  const bool sorb = has_sorption(net);
   for (int row = 0; row < n; ++row) {
     const double tx = st.total[(size_t)row * N + X];
     double v = 0.0;

@@ -114,7 +114,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
                                            double dt_uniform, const double* __restrict__ scratch,
                                            unsigned long long* queue, unsigned long long* counters,
                                            const PfAdjointArgs& adj, double* __restrict__ adj_store,
-                                           unsigned char* smem) {
+                                           unsigned char* smem, int threads) {
   const int tid = threadIdx.x;
   const int lane_id = tid & 31;
   const uint32_t ibytes = (uint32_t)(net.ent_staged ? net.int_words_grp : net.int_words_core) * 4u;
@@ -126,7 +126,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
   const int n = net.n, ns = net.ns, nm = net.nm;
   const int gi = lane_id / G, r = lane_id % G;
   const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << (gi * G));
-  const int cells_per_block = (int)(blockDim.x / G);
+  const int cells_per_block = threads / G;  // the threads taking part (whole warps)
   const int slot = tid / G;
   const int WS = ws_doubles(net, ADJ, G);
   double* wsbase = reinterpret_cast<double*>(smem + ibytes + dbytes);
@@ -884,7 +884,7 @@ rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, 
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) uint64_t tma_bar;
   if (!stage_tables(net, smem, &tma_bar, 0u, true, counters)) return;
-  group_body<G, R, ADJ>(net, gt, st, dt_uniform, scratch, queue, counters, adj, adj_store, smem);
+  group_body<G, R, ADJ>(net, gt, st, dt_uniform, scratch, queue, counters, adj, adj_store, smem, (int)blockDim.x);
 }
 
 template <int G, int R>

@@ -31,6 +31,7 @@ struct Net {
   unsigned long long* queue;     // the network's work-queue counter (zeroed)
   unsigned long long* counters;  // its reductions (zeroed)
   int variant;
+  int threads;  // threads of the block that work on this network (whole warps)
 };
 
 struct Args {
@@ -41,8 +42,10 @@ struct Args {
 
 template <int G, int R>
 __device__ __forceinline__ void run(const Net& m, double dt, unsigned char* smem) {
-  group::group_body<G, R, false>(m.net, m.net.grp, m.st, dt, m.scratch, m.queue, m.counters, PfAdjointArgs{},
-                                 nullptr, smem);
+  // warps beyond the network's workspace wait at the next barrier
+  if ((int)threadIdx.x < m.threads)
+    group::group_body<G, R, false>(m.net, m.net.grp, m.st, dt, m.scratch, m.queue, m.counters, PfAdjointArgs{},
+                                   nullptr, smem, m.threads);
 }
 
 __global__ void __launch_bounds__(256) rstep_multi_kernel(const __grid_constant__ Args args) {
@@ -89,7 +92,15 @@ int launch_rstep_multi(const MultiNetLaunch* nets, int nnets, double dt, int thr
     const int G = in.lanes_per_cell, R = (in.net.n + G - 1) / G;
     const int v = multi::variant_of(G, R);
     if (v < 0 || !group_supported(in.net, G)) return -1;
-    PfLaunchConfig cfg{threads_per_block, blocks_per_sm, 0, G};
+    // as many whole warps of the block as the network's per-cell workspace
+    // lets fit in shared memory
+    int threads = threads_per_block;
+    PfLaunchConfig cfg{threads, blocks_per_sm, 0, G};
+    while (threads > 32 && group_smem_bytes(in.net, cfg, false) > 227u * 1024u) {
+      threads -= 32;
+      cfg.threads_per_block = threads;
+    }
+    if (group_smem_bytes(in.net, cfg, false) > 227u * 1024u) return -1;
     multi::Net& m = args.nets[k];
     m.net = in.net;
     m.net.ent_staged = group_entries_staged(in.net, cfg, false) ? 1 : 0;
@@ -98,10 +109,10 @@ int launch_rstep_multi(const MultiNetLaunch* nets, int nnets, double dt, int thr
     m.queue = in.queue;
     m.counters = in.counters;
     m.variant = v;
+    m.threads = threads;
     const size_t b = group_smem_bytes(in.net, cfg, false);
     smem = b > smem ? b : smem;
   }
-  if (smem > 227u * 1024u) return -1;
   // the per-network set-up pre-pass (logK(T), K' and ln guess per cell)
   for (int k = 0; k < nnets; ++k) {
     const int rc = launch_cell_setup(nets[k].net, nets[k].st, const_cast<double*>(nets[k].scratch), stream);

@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
   int num_cuts = 0, n_const = 0, nsub = 0, its_total = 0, ierror_step = 0;
   const double psv_t = cs.porosity * cs.sat * 1000.0 * cs.volume;
   const bool dry = cs.sat < RT_MIN_SATURATION;
-  const bool has_sorb = net.nkd + net.nionx > 0;
+  const bool has_sorb = has_sorption(net);
   double* ionx_ref = st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr;
   // RTotalSorb (RZeroSorb first) at the current iterate into w.sorb,
   // w.dsorb and the state
@@ -293,7 +293,8 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
         net, T, [&](int j) { return w.c[j]; }, [&](int j) { return w.gamma[j]; },
         [&](int m) { return st.mnrl_volfrac[soa.at(m, cell)]; }, cs.porosity, cs.den_kg, ionx_ref, st.ncells,
         [&](int j, double v) { w.sorb[j] = w.sorb[j] + v; },
-        [&](int i, int j, double v) { w.dsorb[i * NMAX + j] = w.dsorb[i * NMAX + j] + v; });
+        [&](int i, int j, double v) { w.dsorb[i * NMAX + j] = w.dsorb[i * NMAX + j] + v; },
+        surf_cell(net, st, cell));
     for (int j = 0; j < n; ++j) st.total_sorb[soa.at(j, cell)] = w.sorb[j];
     return ok;
   };

@@ -1,7 +1,7 @@
 // pfgpu_sorb.cuh -- equilibrium sorption of one cell, shared by the kernels.
 //
-// RTotalSorb (src/pflotran/reaction.F90:4783-4832) without surface
-// complexation or dynamic K_D: ion exchange (RTotalSorbEqIonx, :4906-5140,
+// RTotalSorb (src/pflotran/reaction.F90:4783-4832) without dynamic K_D:
+// surface complexation (RTotalSorbEqSurfCplx1), ion exchange (RTotalSorbEqIonx, :4906-5140,
 // the "#if 1" Newton on the reference cation's K_D when the cations' charges
 // differ, the closed form when they are all equal) and then the K_D
 // isotherms (RTotalSorbKD, reaction_isotherm.F90:273-359).
@@ -10,6 +10,117 @@
 #include "pfgpu_common.cuh"
 
 namespace pfgpu {
+
+// The per-cell surface-complexation state a kernel passes to total_sorb:
+// the free-site warm start and the complexes' output (one value per
+// reaction / complex, `stride` apart; conc may be null), the cell's
+// temperature (logK of the complexes in non-isothermal runs) and ln a_H2O.
+struct SurfCell {
+  double* free_site;
+  double* conc;
+  int64_t stride;
+  double temp;
+  double lnaw;
+};
+
+__device__ __forceinline__ SurfCell surf_cell(const DevNet& net, const PfCellState& st, int64_t cell) {
+  SurfCell s;
+  s.free_site = (net.nsrx > 0 && st.srfcplx_free_site) ? st.srfcplx_free_site + cell : nullptr;
+  s.conc = (net.nsrx > 0 && st.srfcplx_conc) ? st.srfcplx_conc + cell : nullptr;
+  s.stride = st.ncells;
+  s.temp = st.temperature ? st.temperature[cell] : 25.0;
+  s.lnaw = cell_lnaw(net, st, cell);
+  return s;
+}
+
+// RTotalSorbEqSurfCplx1 (reaction_surf_complex.F90:641-900) for every
+// surface complexation reaction: the free-site concentration S_x from the
+// site balance (Newton on S_x when a complex holds more than one site,
+// relative change 1e-12, damping 0.5 after 1000 iterations, :743-799;
+// otherwise the closed form), the complexes S_k, the sorbed totals and
+// their derivative with the free site's response dS_x/dm (:803-893).
+template <class Mol, class Gam, class VF, class AddS, class AddDS>
+__device__ void total_sorb_srfcplx(const DevNet& net, const Tables& T, Mol mol, Gam gam, VF volfrac,
+                                   double porosity, const SurfCell& sc, AddS add_S, AddDS add_dS) {
+  const bool tdep = !net.o.isothermal && (net.flags & NETF_SX_LOGKCOEF);
+  const bool h2o = water_on(net);
+  double la[PF_MAX_NCOMP];  // ln a of the primaries (:686-687)
+  for (int j = 0; j < net.n; ++j) la[j] = log(mol(j)) + log(gam(j));
+  for (int r = 0; r < net.nsrx; ++r) {
+    const int k0 = T.sx_begin(r), k1 = T.sx_end(r);
+    double site;
+    if (T.sx_type(r) == PF_SURF_MINERAL) site = T.sx_dens(r) * volfrac(T.sx_min(r));
+    else if (T.sx_type(r) == PF_SURF_ROCK) site = T.sx_dens(r) * net.soil_density * (1.0 - porosity);
+    else site = T.sx_dens(r);
+    if (sc.conc)
+      for (int k = k0; k < k1; ++k) sc.conc[k * sc.stride] = 0.0;
+    if (site < 1.0e-40) {  // :728-737
+      if (sc.free_site) sc.free_site[r * sc.stride] = 0.0;
+      continue;
+    }
+    double S[PF_MAX_NSRFCPLX];
+    double free_site = fmax(sc.free_site ? sc.free_site[r * sc.stride] : 1.0e-9, 1.0e-40);
+    bool one_more = false;
+    int its = 0;
+    double damping = 1.0;
+    for (;;) {
+      its = its + 1;
+      double total = free_site;
+      const double ln_free = log(free_site);
+      for (int k = k0; k < k1; ++k) {
+        double lnQK = -(tdep ? interp_logK(T.sx_logKcoef(k), sc.temp) : T.sx_logK(k)) * LOG_TO_LN;
+        if (h2o) lnQK = add_h2o(lnQK, T.sx_h2o(k), sc.lnaw);
+        lnQK = lnQK + T.sx_nuf(k) * ln_free;
+        for (int p = T.sx_cbegin(k); p < T.sx_cend(k); ++p) {
+          const int j = T.sx_spec(p);
+          lnQK = lnQK + T.sx_nu(p) * la[j];
+        }
+        S[k - k0] = exp(lnQK);
+        total = total + T.sx_nuf(k) * S[k - k0];
+      }
+      if (one_more) break;
+      if (T.sx_flag(r)) {
+        const double res = site - total;
+        double dres = 1.0;
+        for (int k = k0; k < k1; ++k) dres = dres + T.sx_nuf(k) * S[k - k0] / free_site;
+        const double dfree = res / dres;
+        if (its > 1000) damping = 0.5;
+        free_site = free_site + damping * dfree;
+        if (fabs(dfree / free_site) < 1.0e-12) one_more = true;
+      } else {
+        total = total / free_site;
+        free_site = site / total;
+        one_more = true;
+      }
+    }
+    if (sc.free_site) sc.free_site[r * sc.stride] = free_site;
+    if (sc.conc)
+      for (int k = k0; k < k1; ++k) sc.conc[k * sc.stride] = S[k - k0];
+    // dS_x/dm_j (:803-824), in registers
+    double dSx[PF_MAX_NCOMP];
+    for (int j = 0; j < net.n; ++j) dSx[j] = 0.0;
+    double den = 0.0;
+    for (int k = k0; k < k1; ++k) {
+      for (int p = T.sx_cbegin(k); p < T.sx_cend(k); ++p)
+        dSx[T.sx_spec(p)] = dSx[T.sx_spec(p)] + T.sx_nu(p) * T.sx_nuf(k) * S[k - k0];
+      den = den + T.sx_nuf(k) * T.sx_nuf(k) * S[k - k0];
+    }
+    den = den / free_site;
+    den = den + 1.0;
+    for (int j = 0; j < net.n; ++j) dSx[j] = (-dSx[j] / den) / mol(j);
+    // sorbed totals and derivative (:846-893)
+    for (int k = k0; k < k1; ++k) {
+      const int p0 = T.sx_cbegin(k), p1 = T.sx_cend(k);
+      for (int p = p0; p < p1; ++p) add_S(T.sx_spec(p), T.sx_nu(p) * S[k - k0]);
+      const double nui_Si_over_Sx = T.sx_nuf(k) * S[k - k0] / free_site;
+      for (int q = p0; q < p1; ++q) {
+        const int jc = T.sx_spec(q);
+        const double t = T.sx_nu(q) * S[k - k0] / mol(jc) + nui_Si_over_Sx * dSx[jc];
+        for (int p = p0; p < p1; ++p) add_dS(T.sx_spec(p), jc, T.sx_nu(p) * t);
+      }
+    }
+  }
+}
 
 // Inputs come through callables so that each kernel keeps its own storage:
 // mol(j) and gam(j) (molality and activity coefficient of primary j),
@@ -22,7 +133,9 @@ namespace pfgpu {
 // iterations (the reference's ierror, :4981-4986).
 template <class Mol, class Gam, class VF, class AddS, class AddDS>
 __device__ bool total_sorb(const DevNet& net, const Tables& T, Mol mol, Gam gam, VF volfrac, double porosity,
-                           double den_kg, double* ionx_ref, int64_t ref_stride, AddS add_S, AddDS add_dS) {
+                           double den_kg, double* ionx_ref, int64_t ref_stride, AddS add_S, AddDS add_dS,
+                           const SurfCell& sc) {
+  if (net.nsrx > 0) total_sorb_srfcplx(net, T, mol, gam, volfrac, porosity, sc, add_S, add_dS);
   for (int r = 0; r < net.nionx; ++r) {
     const int b = T.ix_begin(r), nc = T.ix_end(r) - b;
     const int mi = T.ix_min(r);

@@ -53,6 +53,11 @@ PF_MAX_NMNRL = 16
 PF_MAX_SPEC_PER_RXN = 24
 PF_MAX_NKD = 8
 PF_MAX_NIONX = 4
+PF_MAX_NSRFCPLX_RXN = 4
+PF_MAX_NSRFCPLX = 16
+PF_SURF_NULL = 0
+PF_SURF_MINERAL = 1
+PF_SURF_ROCK = 2
 PF_MULTI_MAX_NETS = 16
 PF_MAX_IONX_CATIONS = 8
 PF_SORPTION_LINEAR = 1
@@ -90,6 +95,10 @@ class PfSorptionDesc(C.Structure):
         ("kd_freundlich_n", _dp), ("kd_mineral", _ip), ("soil_particle_density", C.c_double),
         ("nionx", C.c_int32), ("ionx_stride", C.c_int32),
         ("ionx_ncation", _ip), ("ionx_cation", _ip), ("ionx_k", _dp), ("ionx_cec", _dp), ("ionx_mineral", _ip),
+        ("nsrfcplx_rxn", C.c_int32), ("nsrfcplx", C.c_int32), ("srfcplx_rxn_ptr", _ip), ("srfcplx_surf_type", _ip),
+        ("srfcplx_mineral", _ip), ("srfcplx_site_density", _dp), ("srfcplx_stride", C.c_int32),
+        ("srfcplx_nspec", _ip), ("srfcplx_spec", _ip), ("srfcplx_stoich", _dp), ("srfcplx_free_site_stoich", _dp),
+        ("srfcplx_logK", _dp), ("srfcplx_logKcoef", _dp), ("srfcplx_h2o_stoich", _dp),
     ]
 
 
@@ -137,6 +146,7 @@ class PfCellState(C.Structure):
         ("status", _ip), ("newton_its", _ip), ("num_substeps", _ip),
         ("cell_order", C.POINTER(C.c_int64)),
         ("total_sorb", _dp), ("ionx_ref_sorbed", _dp), ("ln_act_h2o", _dp),
+        ("srfcplx_free_site", _dp), ("srfcplx_conc", _dp),
     ]
 
 

@@ -100,7 +100,10 @@ class ReactionNetwork:
     debyeB: float = 0.3288
     debyeBdot: float = 0.0410
     options: dict = field(default_factory=default_options)
-    # equilibrium sorption (None: none): dict(kd=[dict(species, type ('linear',
+    # equilibrium sorption (None: none): dict(surface=[dict(site_density,
+    # [surface ('null', 'mineral', 'rock')], [mineral], complexes=[dict(name,
+    # stoich={primary: nu}, free_site_stoich, logK, [logKcoef], [h2o_stoich])])]
+    # (equilibrium surface complexation, one entry per site), kd=[dict(species, type ('linear',
     # 'langmuir', 'freundlich'), coeff, [b], [n], [mineral])], kd_units
     # ('kg/m3 bulk' or 'mL/g soil'), soil_particle_density, ionx=[dict(
     # cations=[(name, k), ...] (the first is the reference cation), cec,
@@ -124,8 +127,16 @@ class ReactionNetwork:
         return len((self.sorption or {}).get("ionx", ()))
 
     @property
+    def nsrfcplx_rxn(self):
+        return len((self.sorption or {}).get("surface", ()))
+
+    @property
+    def nsrfcplx(self):
+        return sum(len(r["complexes"]) for r in (self.sorption or {}).get("surface", ()))
+
+    @property
     def has_sorption(self):
-        return self.nkd + self.nionx > 0
+        return self.nkd + self.nionx + self.nsrfcplx_rxn > 0
 
     @property
     def ncomp(self):
@@ -346,6 +357,34 @@ class ReactionNetwork:
             sd.ionx_cec = _ptr(arr([r["cec"] for r in ix], f64), C.c_double)
             sd.ionx_mineral = _ptr(arr([mins[r["mineral"]] if r.get("mineral") else -1 for r in ix], i32),
                                    C.c_int32)
+        sx = list(sp.get("surface", ()))
+        sd.nsrfcplx_rxn = len(sx)
+        if sx:
+            cplx = [c for r in sx for c in r["complexes"]]
+            sd.nsrfcplx = len(cplx)
+            stride = max(1, max(len(c["stoich"]) for c in cplx))
+            spec = np.zeros((len(cplx), stride), i32)
+            nu = np.zeros((len(cplx), stride), f64)
+            for k, c in enumerate(cplx):
+                for p, (name, v) in enumerate(c["stoich"].items()):
+                    spec[k, p], nu[k, p] = idx[name], v
+            ptr = np.cumsum([0] + [len(r["complexes"]) for r in sx])
+            stype = {"null": abi.PF_SURF_NULL, "mineral": abi.PF_SURF_MINERAL, "rock": abi.PF_SURF_ROCK}
+            sd.srfcplx_rxn_ptr = _ptr(arr(ptr, i32), C.c_int32)
+            sd.srfcplx_surf_type = _ptr(arr([stype[r.get("surface", "null")] for r in sx], i32), C.c_int32)
+            sd.srfcplx_mineral = _ptr(arr([mins[r["mineral"]] if r.get("mineral") else -1 for r in sx], i32),
+                                      C.c_int32)
+            sd.srfcplx_site_density = _ptr(arr([r["site_density"] for r in sx], f64), C.c_double)
+            sd.srfcplx_stride = stride
+            sd.srfcplx_nspec = _ptr(arr([len(c["stoich"]) for c in cplx], i32), C.c_int32)
+            sd.srfcplx_spec = _ptr(arr(spec, i32), C.c_int32)
+            sd.srfcplx_stoich = _ptr(arr(nu, f64), C.c_double)
+            sd.srfcplx_free_site_stoich = _ptr(arr([c.get("free_site_stoich", 1.0) for c in cplx], f64), C.c_double)
+            sd.srfcplx_logK = _ptr(arr([c["logK"] for c in cplx], f64), C.c_double)
+            if all(c.get("logKcoef") is not None for c in cplx):
+                sd.srfcplx_logKcoef = _ptr(arr([c["logKcoef"] for c in cplx], f64), C.c_double)
+            if any(c.get("h2o_stoich", 0.0) for c in cplx):
+                sd.srfcplx_h2o_stoich = _ptr(arr([c.get("h2o_stoich", 0.0) for c in cplx], f64), C.c_double)
         return sd
 
     def options_struct(self) -> abi.PfOptions:
@@ -370,14 +409,18 @@ STATE_FIELDS = {
     "total_sorb": ("n", np.float64), "ionx_ref_sorbed": ("x", np.float64),
     # networks with the water activity option only
     "ln_act_h2o": (1, np.float64),
+    # networks with surface complexation only
+    "srfcplx_free_site": ("r", np.float64), "srfcplx_conc": ("c", np.float64),
 }
 OPTIONAL_FIELDS = ("dt_cell",)
 SORPTION_FIELDS = ("total_sorb", "ionx_ref_sorbed")
+SURFACE_FIELDS = ("srfcplx_free_site", "srfcplx_conc")
 H2O_FIELDS = ("ln_act_h2o",)
 
 
 def _rows(net, r):
-    return {"n": net.ncomp, "s": net.nsec, "m": net.nmnrl, "x": net.nionx}.get(r, r)
+    return {"n": net.ncomp, "s": net.nsec, "m": net.nmnrl, "x": net.nionx, "r": net.nsrfcplx_rxn,
+            "c": net.nsrfcplx}.get(r, r)
 
 
 class CellState:
@@ -397,12 +440,16 @@ class CellState:
                 continue
             if k in SORPTION_FIELDS and not net.has_sorption:
                 continue
+            if k in SURFACE_FIELDS and not net.nsrfcplx_rxn:
+                continue
             if k in H2O_FIELDS and not net.options.get("use_activity_h2o"):
                 continue
             rows = _rows(net, r)
             a[k] = np.zeros((rows, ncells), dt) if r != 1 else np.zeros(ncells, dt)
         if net.has_sorption:
             a["ionx_ref_sorbed"][:] = 1.0e-9  # reactive_transport_aux.F90:282
+        if net.nsrfcplx_rxn:
+            a["srfcplx_free_site"][:] = 1.0e-9  # srfcplxrxn_free_site_conc's initial value
         a["pri_act_coef"][:] = 1.0
         a["sec_act_coef"][:] = 1.0
         a["saturation"][:] = 1.0

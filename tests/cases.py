@@ -102,7 +102,41 @@ SORB_A0 = [4.0, 6.0, 3.0, 3.0, 3.0, 8.0]
 SORB_SECS = [dict(name="NaCl(aq)", stoich={"Na+": 1.0, "Cl-": 1.0}, logK=0.5, Z=0.0, a0=3.0),
              dict(name="CaCl+", stoich={"Ca++": 1.0, "Cl-": 1.0}, logK=-0.4, Z=1.0, a0=4.0)]
 SORB_MINS = [dict(name="Sylvite-like", stoich={"K+": 1.0, "Cl-": 1.0}, logK=-2.0, rate=1e-8, molar_vol=3.7e-5)]
+# equilibrium surface complexation on three sites: a fixed site density with
+# one-site complexes (closed form), sites on the kinetic mineral with a
+# bidentate complex (the free-site Newton), and sites per kg of solid
+SURFACE_SITES = [
+    dict(site_density=500.0, complexes=[
+        dict(name=">A-Na", stoich={"Na+": 1.0}, free_site_stoich=1.0, logK=-1.0),
+        dict(name=">A-Ca+", stoich={"Ca++": 1.0}, free_site_stoich=1.0, logK=-2.0),
+        dict(name=">A-Tr", stoich={"Tr": 1.0}, free_site_stoich=1.0, logK=-1.5)]),
+    dict(site_density=2.0e4, surface="mineral", mineral="Sylvite-like", complexes=[
+        dict(name=">B2-Mg", stoich={"Mg++": 1.0}, free_site_stoich=2.0, logK=-3.0),
+        dict(name=">B-K", stoich={"K+": 1.0}, free_site_stoich=1.0, logK=-1.2),
+        dict(name=">B-CaCl", stoich={"Ca++": 1.0, "Cl-": 1.0}, free_site_stoich=1.0, logK=-2.5)]),
+    dict(site_density=0.05, surface="rock", complexes=[
+        dict(name=">C-NaCl", stoich={"Na+": 1.0, "Cl-": 1.0}, free_site_stoich=1.0, logK=-0.5)]),
+]
+
+# sites whose complexes all hold the same components: there the reference's
+# sorbed-total derivative (which spreads the free site's response over each
+# complex's own species only, reaction_surf_complex.F90:874-893) is the exact
+# derivative, so the oracle's Jacobian can be checked against differences
+SURFACE_SITES_SAME = [
+    dict(site_density=500.0, complexes=[
+        dict(name=">A-Na", stoich={"Na+": 1.0}, free_site_stoich=1.0, logK=-1.0),
+        dict(name=">A-Na2", stoich={"Na+": 2.0}, free_site_stoich=1.0, logK=-2.5)]),
+    dict(site_density=2.0e4, surface="mineral", mineral="Sylvite-like", complexes=[
+        dict(name=">B2-Mg", stoich={"Mg++": 1.0}, free_site_stoich=2.0, logK=-3.0),
+        dict(name=">B-Mg", stoich={"Mg++": 1.0}, free_site_stoich=1.0, logK=-1.2)]),
+]
+
 SORPTIONS = {
+    "surface-same": dict(surface=SURFACE_SITES_SAME, soil_particle_density=2650.0),
+    "surface": dict(surface=SURFACE_SITES, soil_particle_density=2650.0),
+    "surface+ionx+kd": dict(surface=SURFACE_SITES[:2], soil_particle_density=2650.0,
+                            kd=[dict(species="Tr", type="linear", coeff=5.0)],
+                            ionx=[dict(cations=[("Na+", 1.0), ("K+", 3.0)], cec=100.0)]),
     "ionx+langmuir": dict(kd=[dict(species="Tr", type="langmuir", coeff=80.0, b=3.0)],
                           ionx=[dict(cations=[("Na+", 1.0), ("Ca++", 0.3), ("K+", 5.0), ("Mg++", 0.4)],
                                      cec=250.0)]),

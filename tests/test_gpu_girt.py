@@ -127,7 +127,7 @@ def test_girt_parity(oracle, name, dims, logf):
 
 
 @pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
-@pytest.mark.parametrize("sorb", ["ionx+langmuir", "mineral-scaled"])
+@pytest.mark.parametrize("sorb", ["ionx+langmuir", "mineral-scaled", "surface", "surface+ionx+kd"])
 def test_girt_parity_with_sorption(oracle, sorb, logf):
     """Sorbed accumulation (S - S_k) V/dt in the residual and dS/dm V/dt on
     the diagonal blocks, dry cells included, against the oracle."""
