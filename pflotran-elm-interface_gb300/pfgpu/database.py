@@ -17,8 +17,13 @@ accepted; a logK of 500 marks a temperature with no data).  Later sections
 are not read.
 
 Basis set-up (the subset of BasisInit, reaction_database.F90:812-4040, that
-this engine needs): the primary species must be basis species of the
-database (no basis swapping); water leaves the species list of every
+this engine needs): primary species that are not basis species of the
+database are swapped in (the change of basis of BasisInit, :1063-1450: the
+reactions of the swapped-in primaries and of the secondaries form a linear
+system whose inverse writes every secondary -- the swapped-out basis species
+included -- in the new basis, logK at every database temperature; mineral
+reactions then have each secondary substituted, BasisSubSpeciesInMineralRxn,
+reaction_database_aux.F90:494-586); water leaves the species list of every
 reaction and its coefficient is kept apart (eqcplxh2ostoich,
 kinmnrlh2ostoich), entering ln Q times ln a_H2O, which is 0 unless the
 ACTIVITY_H2O option (use_activity_h2o) computes it; logK at the reference temperature
@@ -84,10 +89,18 @@ def read_database(source: str) -> Database:
     temps = [_num(t) for t in toks[2:2 + nt]]
     i = 2 + nt
     db = Database(temperatures=temps)
+    def skip_note(i):
+        # an optional trailing source note ('pcl-goethite colloid'): a string
+        # followed by a string (the next record's name) where a record starts
+        # with a name and a number
+        if i + 1 < len(toks) and not _is_num(toks[i]) and not _is_num(toks[i + 1]):
+            return i + 1
+        return i
+
     # primary species: name a0 Z MW
     while toks[i] != "null":
         db.primary[toks[i]] = (_num(toks[i + 1]), _num(toks[i + 2]), _num(toks[i + 3]))
-        i += 4
+        i = skip_note(i + 4)
     i += 4  # the 'null' record has the same four fields
 
     def pairs(i, k):
@@ -105,7 +118,7 @@ def read_database(source: str) -> Database:
         logK = [_num(t) for t in toks[i:i + nt]]
         i += nt
         a0, Z = _num(toks[i]), _num(toks[i + 1])
-        i += 3
+        i = skip_note(i + 3)
         if name == "null":
             break
         db.secondary[name] = Reaction(st, logK, a0=a0, Z=Z)
@@ -118,7 +131,7 @@ def read_database(source: str) -> Database:
             st, i = pairs(i + 3, k)
             logK = [_num(t) for t in toks[i:i + nt]]
             mw = _num(toks[i + nt]) if i + nt < len(toks) else 0.0
-            i += nt + 1
+            i = skip_note(i + nt + 1)
             if name == "null":
                 break
             table[name] = Reaction(st, logK, molar_vol_cm3=vm, molar_weight=mw)
@@ -318,6 +331,116 @@ def _water(stoich):
     return sum(nu for sp, nu in stoich if sp == "H2O")
 
 
+def _lu_inverse(a):
+    """Inverse by LUDecomposition and one LUBackSubstitution per unit vector
+    (the reference's sec_matrix_inverse, reaction_database.F90:1316-1326),
+    through the same Crout restatement as the logK fit."""
+    n = len(a)
+    inv = np.zeros((n, n))
+    for k in range(n):
+        e = [0.0] * n
+        e[k] = 1.0
+        inv[:, k] = _crout_solve(a, e)
+    return inv
+
+
+def swap_basis(db: Database, primary, secondary):
+    """The change of basis of BasisInit (reaction_database.F90:1063-1450).
+    primary: the new basis (database basis species and/or complexes);
+    secondary: the complexes of the network, which must include every basis
+    species of the database that the new basis leaves out and that some
+    kept reaction uses.  Returns (reactions, minerals_fn): reactions maps each
+    secondary to a Reaction in [H2O] + primary (stoichiometry with
+    |nu| > 1e-40, logK per database temperature); minerals_fn(Reaction)
+    rewrites a mineral's reaction in the new basis."""
+    new_basis = ["H2O"] + list(primary)
+    bidx = {sp: k for k, sp in enumerate(new_basis)}
+    sidx = {sp: k for k, sp in enumerate(secondary)}
+    rows = []  # the species with a database reaction: swapped-in primaries, then secondaries
+    for p in primary:
+        if p in db.secondary:
+            rows.append(db.secondary[p])
+        elif p not in db.primary:
+            raise KeyError("%s is neither a basis species nor a complex of the database" % p)
+    for sp in secondary:
+        if sp in db.secondary:
+            rows.append(db.secondary[sp])
+        elif sp not in db.primary:
+            raise KeyError("%s is neither a basis species nor a complex of the database" % sp)
+    nsec = len(secondary)
+    if len(rows) != nsec:
+        raise ValueError("the new basis leaves %d reactions for %d secondary species (a swapped-out basis "
+                         "species must be listed as a secondary)" % (len(rows), nsec))
+    names = [p for p in primary if p in db.secondary] + [sp for sp in secondary if sp in db.secondary]
+    nt = len(db.temperatures)
+    P = np.zeros((nsec, len(new_basis)))
+    S = np.zeros((nsec, nsec))
+    L = np.zeros((nsec, nt))
+    for r, (name, rxn) in enumerate(zip(names, rows)):
+        L[r] = rxn.logK
+        if name in bidx:
+            P[r, bidx[name]] = -1.0
+        else:
+            S[r, sidx[name]] = -1.0
+        for sp, nu in rxn.stoich:
+            if sp in bidx:
+                P[r, bidx[sp]] = nu
+            elif sp in sidx:
+                S[r, sidx[sp]] = nu
+            else:
+                raise KeyError("%s (in the reaction of %s) is neither in the new basis nor a secondary" % (sp, name))
+    Sinv = _lu_inverse(S)
+    stoich = -(Sinv @ P)
+    logK = np.zeros((nsec, nt))
+    missing = np.abs(L - MISSING_LOGK) < 1.0e-10
+    for j in range(nsec):
+        for t in range(nt):
+            logK[j, t] = logK[j, t] - float(np.dot(Sinv[j], L[:, t]))
+            # a combination that takes in a temperature without data has
+            # none either (the literal combination would carry 500 into the
+            # fit as if it were data)
+            if np.any(missing[np.abs(Sinv[j]) > 0.0, t]):
+                logK[j, t] = MISSING_LOGK
+    out = {}
+    for j, sp in enumerate(secondary):
+        st = [(new_basis[c], float(stoich[j, c])) for c in range(len(new_basis)) if abs(stoich[j, c]) > 1.0e-40]
+        if sp in db.secondary:
+            a0, Z = db.secondary[sp].a0, db.secondary[sp].Z
+        else:
+            a0, Z = db.primary[sp][0], db.primary[sp][1]
+        out[sp] = Reaction(st, list(logK[j]), a0=a0, Z=Z)
+
+    def mineral(rxn: Reaction) -> Reaction:
+        """Each secondary of the mineral's reaction replaced by its reaction
+        in the new basis, logK += coefficient * the secondary's logK
+        (BasisSubSpeciesInMineralRxn; coefficients below 1e-10 dropped)."""
+        st = list(rxn.stoich)
+        lk = list(rxn.logK)
+        for sp in secondary:
+            scale = None
+            keep = []
+            for name, nu in st:
+                if name == sp:
+                    scale = nu
+                else:
+                    keep.append([name, nu])
+            if scale is None:
+                continue
+            for name, nu in out[sp].stoich:
+                for item in keep:
+                    if item[0] == name:
+                        item[1] = item[1] + scale * nu
+                        break
+                else:
+                    keep.append([name, scale * nu])
+            st = [(name, nu) for name, nu in keep if abs(nu) > 1.0e-10]
+            lk = [MISSING_LOGK if (abs(a - MISSING_LOGK) < 1.0e-10 or abs(b - MISSING_LOGK) < 1.0e-10)
+                  else a + scale * b for a, b in zip(lk, out[sp].logK)]
+        return Reaction(st, lk, a0=rxn.a0, Z=rxn.Z, molar_vol_cm3=rxn.molar_vol_cm3, molar_weight=rxn.molar_weight)
+
+    return out, mineral
+
+
 def build_network(db: Database, primary, secondary=None, minerals=None, options=None,
                   reference_temperature: float = 25.0) -> ReactionNetwork:
     """ReactionNetwork of `primary` (basis species of the database), the
@@ -330,23 +453,30 @@ def build_network(db: Database, primary, secondary=None, minerals=None, options=
     temperature, others the temperature fits."""
     options = dict(options) if options is not None else default_options()
     isothermal = bool(options.get("isothermal", 1))
-    for p in primary:
-        if p not in db.primary:
-            raise KeyError("%s is not a basis species of the database" % p)
     pset = set(primary)
-    if secondary is None:
-        secondary = [name for name, r in db.secondary.items()
-                     if all(sp in pset or sp == "H2O" for sp, _ in r.stoich)]
+    for p in primary:
+        if p not in db.primary and p not in db.secondary:
+            raise KeyError("%s is neither a basis species nor a complex of the database" % p)
+    swap = any(p not in db.primary for p in primary)
+    if swap:
+        if secondary is None:
+            raise ValueError("a swapped basis needs its secondary species listed")
+        swapped, swap_mineral = swap_basis(db, primary, secondary)
+        sec_rxns = [(name, swapped[name]) for name in secondary]
+    else:
+        if secondary is None:
+            secondary = [name for name, r in db.secondary.items()
+                         if all(sp in pset or sp == "H2O" for sp, _ in r.stoich)]
+        sec_rxns = [(name, db.secondary[name]) for name in secondary]
     secs = []
-    for name in secondary:
-        r = db.secondary[name]
+    for name, r in sec_rxns:
         coefs = fit_logK_coefs(db.temperatures, r.logK)
         secs.append(dict(name=name, stoich=_drop_water(r.stoich, pset), h2o=_water(r.stoich),
                          logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
                          logKcoef=coefs, Z=r.Z, a0=r.a0))
     mins = []
     for name, par in (minerals or {}).items():
-        r = db.minerals[name]
+        r = swap_mineral(db.minerals[name]) if swap else db.minerals[name]
         coefs = fit_logK_coefs(db.temperatures, r.logK)
         m = dict(name=name, stoich=_drop_water(r.stoich, pset), h2o=_water(r.stoich),
                  logK=_reference_logK(db, r, coefs, reference_temperature, isothermal),
@@ -355,9 +485,10 @@ def build_network(db: Database, primary, secondary=None, minerals=None, options=
         if "rate" not in m:
             raise KeyError("mineral %s: a rate constant is required" % name)
         mins.append(m)
-    return ReactionNetwork.build(list(primary), [db.primary[p][1] for p in primary],
-                                 [db.primary[p][0] for p in primary], secs, mins,
-                                 debye=debye_huckel(reference_temperature), options=options)
+    def z_a0(p):  # a swapped-in primary keeps its complex's charge and size
+        return (db.primary[p][1], db.primary[p][0]) if p in db.primary else (db.secondary[p].Z, db.secondary[p].a0)
+    return ReactionNetwork.build(list(primary), [z_a0(p)[0] for p in primary], [z_a0(p)[1] for p in primary], secs,
+                                 mins, debye=debye_huckel(reference_temperature), options=options)
 
 
 def constraint_reaction(db: Database, primary, name: str, kind: str = "mineral",

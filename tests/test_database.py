@@ -120,7 +120,7 @@ def test_build_network_basis_water_and_selection():
     hot = dbm.build_network(db, ["H+", "Ca++", "HCO3-"], options=dict(isothermal=0), reference_temperature=30.0)
     assert hot.sec_logKcoef.shape == (3, 5)
     assert hot.sec_logK[2] == pytest.approx(_coef_fn(coefs["CaHCO3+"], 30.0), abs=1e-7)
-    # no basis swapping: a complex of a non-primary species is refused
+    # a complex of a species that is not primary (and not swapped in) is refused
     with pytest.raises(KeyError):
         dbm.build_network(db, ["H+", "Ca++", "HCO3-"], secondary=["MgCO3(aq)"])
     with pytest.raises(KeyError):
@@ -241,3 +241,90 @@ def test_database_network_runs_on_the_gpu(oracle):
     assert same.mean() > 0.9
     err = np.max(np.abs(got.a["pri_molal"][:, same] - ref.a["pri_molal"][:, same]) / ref.a["pri_molal"][:, same])
     assert err < 1e-10, err
+
+
+# ------------------------------------------------------------ basis swapping
+def _speciate(oracle, net, free, gamma1=True):
+    """Secondary molalities of `net` at the free-ion molalities `free`
+    (ncomp, ncells), activity coefficients one (OFF), through the oracle's
+    RTotal."""
+    from pfgpu.network import CellState
+    st = CellState.empty(net, free.shape[1])
+    st.a["pri_molal"][:] = free
+    st.a["den_kg"][:] = 1000.0
+    oracle.update_auxvars(net, st, False)
+    return st
+
+
+def _swap_case(db, prim0, sec0, prim1, sec1, mins, t_c, oracle, isothermal):
+    from pfgpu.network import default_options
+    from pfgpu import abi
+    opts = default_options(isothermal=int(isothermal), act_coef_update_frequency=abi.PF_ACT_COEF_OFF)
+    net0 = dbm.build_network(db, prim0, sec0, minerals=mins, options=opts)
+    net1 = dbm.build_network(db, prim1, sec1, minerals=mins, options=opts)
+    rng = np.random.default_rng(7)
+    N = 50
+    free0 = 10.0 ** rng.uniform(-6.0, -2.0, (len(prim0), N))
+    st0 = _speciate(oracle, net0, free0)
+    if not isothermal:
+        st0.a["temperature"][:] = t_c
+        oracle.update_auxvars(net0, st0, False)
+    # every species' molality in the unswapped network
+    conc = {p: st0.a["pri_molal"][k] for k, p in enumerate(prim0)}
+    conc.update({s: st0.a["sec_molal"][k] for k, s in enumerate(net0.secondary)})
+    from pfgpu.network import CellState
+    st1 = CellState.empty(net1, N)
+    st1.a["pri_molal"][:] = np.stack([conc[p] for p in prim1])
+    st1.a["den_kg"][:] = 1000.0
+    st1.a["temperature"][:] = t_c
+    oracle.update_auxvars(net1, st1, False)
+    for k, s in enumerate(net1.secondary):
+        np.testing.assert_allclose(st1.a["sec_molal"][k], conc[s], rtol=1e-11 if isothermal else 1e-9, err_msg=s)
+    # minerals: the same ln Q/K written in either basis
+    for m, name in enumerate(net0.minerals):
+        def lnqk(net, st, mi):
+            lq = np.zeros(N)
+            for j in range(net.mnrl_nspec[mi]):
+                lq += net.mnrl_stoich[mi, j] * np.log(st.a["pri_molal"][net.mnrl_spec[mi, j]])
+            logK = net.mnrl_logK[mi] if isothermal else dbm.eval_logK(net.mnrl_logKcoef[mi], t_c)
+            return lq - logK * 2.30258509299
+        np.testing.assert_allclose(lnqk(net1, st1, net1.minerals.index(name)), lnqk(net0, st0, m),
+                                   rtol=0, atol=1e-9 if isothermal else 1e-7, err_msg=name)
+    return net0, net1
+
+
+@pytest.mark.parametrize("isothermal,t_c", [(True, 25.0), (False, 40.0)], ids=["25C", "40C-fit"])
+def test_basis_swap_reproduces_the_unswapped_speciation(oracle, isothermal, t_c):
+    """CO3-- in place of HCO3- as a primary species of the synthetic
+    database: every complex, the swapped-out HCO3- and each mineral's Q/K
+    come out as in the database's own basis."""
+    db = dbm.read_database(_synthetic()[0])
+    net0, net1 = _swap_case(db, ["H+", "Ca++", "HCO3-", "Mg++"], ["OH-", "CO3--", "CaHCO3+", "MgCO3(aq)"],
+                            ["H+", "Ca++", "CO3--", "Mg++"], ["OH-", "HCO3-", "CaHCO3+", "MgCO3(aq)"],
+                            {"Calcite": dict(rate=1e-8), "Dolomite": dict(rate=1e-9)}, t_c, oracle, isothermal)
+    # the swapped-out species' reaction: HCO3- = CO3-- + H+ (water-free)
+    k = net1.secondary.index("HCO3-")
+    st = {net1.primary[net1.sec_spec[k, j]]: net1.sec_stoich[k, j] for j in range(net1.sec_nspec[k])}
+    assert st == {"CO3--": 1.0, "H+": 1.0}
+    # the charge and size of the swapped-in primary are the complex's
+    assert net1.pri_Z[net1.primary.index("CO3--")] == -2.0
+
+
+def test_basis_swap_needs_the_swapped_out_species():
+    db = dbm.read_database(_synthetic()[0])
+    with pytest.raises(ValueError):
+        dbm.build_network(db, ["H+", "Ca++", "CO3--", "Mg++"], ["OH-", "CaHCO3+", "MgCO3(aq)"])
+    with pytest.raises(ValueError):
+        dbm.build_network(db, ["H+", "Ca++", "CO3--", "Mg++"])
+
+
+@pytest.mark.skipif(not BATCH or not os.path.isdir(BATCH),
+                    reason="PFGPU_REFERENCE_ROOT does not name the reference tree")
+@pytest.mark.parametrize("isothermal,t_c", [(True, 25.0), (False, 45.0)], ids=["25C", "45C-fit"])
+def test_basis_swap_hanford_co2(oracle, isothermal, t_c):
+    """CO2(aq) in place of HCO3- with the reference's hanford.dat, where
+    CO2(aq) is a complex (database/hanford.dat:429)."""
+    db = dbm.read_database(os.path.join(REF, "database", "hanford.dat"))
+    _swap_case(db, ["H+", "HCO3-", "Ca++"], ["OH-", "CO3--", "CO2(aq)", "CaHCO3+", "CaCO3(aq)"],
+               ["H+", "CO2(aq)", "Ca++"], ["OH-", "CO3--", "HCO3-", "CaHCO3+", "CaCO3(aq)"],
+               {"Calcite": dict(rate=1e-6)}, t_c, oracle, isothermal)
