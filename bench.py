@@ -322,6 +322,16 @@ def girt_measure(net, eng, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, c
         b.record()
     torch.cuda.synchronize()
     ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    # the later Newton iterations of a time step: each cell's K of every
+    # reaction from the per-cell cache the step's first assembly filled
+    asm.assemble(st, tk, dt, k_cache="fill")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        a.record()
+        asm.assemble(st, tk, dt, k_cache="read")
+        b.record()
+    torch.cuda.synchronize()
+    ms_read = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     n, ns, nm = net.ncomp, net.nsec, net.nmnrl
     nnzb = asm.nnzb
     # reads: pri_molal, pri/sec act coefs, volfrac, area, porosity, saturation,
@@ -366,7 +376,10 @@ def girt_measure(net, eng, dev, steps, warmup, nx=128, ny=128, nz=64, seed=11, c
             "cells_per_s": N / (ms * 1e-3), "algorithmic_bytes": alg, "achieved_gbs": gbs, "peak_gbs": peak,
             "hbm_frac": gbs / peak if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
             "flops_per_cell": fl, "transcendentals_per_cell": tr, "achieved_tflops": tf, "fp64_peak_tflops": fp64,
-            "fp64_frac": tf / fp64 if fp64 else None, "kernels_per_assembly": 2}
+            "fp64_frac": tf / fp64 if fp64 else None, "kernels_per_assembly": 2,
+            "k_cache_read": {"ms": ms_read, "cells_per_s": N / (ms_read * 1e-3),
+                             "note": "later Newton iterations of a step: per-cell K (K/gamma of the complexes, "
+                                     "K of the minerals) read from the cache the step's first assembly filled"}}
 
 
 C3_NCOMP = (4, 6, 8, 10, 12, 16, 20, 24)

@@ -524,6 +524,21 @@ typedef struct PfGirtArgs {
                                         instead of analytically.  pf_rstep has no such
                                         mode: the reference stops there for OSRT
                                         (reaction.F90:3918-3920) */
+  double* k_cache;                   /* optional (NULL: none), [nsec + nmnrl][ncells]:
+                                        each cell's K_i / gamma_i of every complex, then
+                                        K_m of every kinetic mineral, at the cell's
+                                        temperature (ReactionInterpolateLogK,
+                                        reaction_aux.F90:1285-1312).  The Newton
+                                        iterations of one time step assemble at the
+                                        same temperatures and activity coefficients
+                                        (activity updated per time step), so the first
+                                        computes these and the others read them.
+                                        Not with the water activity on
+                                        (PF_ERR_UNSUPPORTED) */
+  int32_t k_cache_valid;             /* 0: compute the K and store them in k_cache;
+                                        1: read them from k_cache (what a call with 0
+                                        stored, temperatures, logK and the complexes'
+                                        activity coefficients unchanged since) */
 } PfGirtArgs;
 
 /* Host: block-row pattern of the 7-point structured-grid matrix (block

@@ -123,6 +123,8 @@ module pfgpu_mod
     real(c_double) :: dt
     type(c_ptr) :: rowptr, colidx, residual, values, total_sorb_k
     integer(c_int32_t) :: numerical_derivatives
+    type(c_ptr) :: k_cache                      ! optional per-cell K cache, (ncells, nsec + nmnrl)
+    integer(c_int32_t) :: k_cache_valid         ! 0: fill it, 1: read it
   end type
 
   type, bind(C), public :: pf_transport_args_t

@@ -859,11 +859,16 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
   if (has_sorption(net->dev) && !a->total_sorb_k) return PF_ERR_INVALID;
   if ((a->nx > 1 && !a->qx) || (a->ny > 1 && !a->qy) || (a->nz > 1 && !a->qz)) return PF_ERR_INVALID;
   if (!state->sec_molal && net->dev.ns) return PF_ERR_INVALID;
-  if (girt_smem_bytes(net->dev, nullptr) > 227u * 1024u) return PF_ERR_TOO_LARGE;
+  // the per-cell K cache: not with the water activity on (ln a_H2O follows
+  // the molalities, so K a_H2O^nu changes from one Newton iteration to the next)
+  if (a->k_cache && water_on(net->dev)) return PF_ERR_UNSUPPORTED;
   if (!net->d_girt) {
     rc = girt_build_tables(net->dev, net->ints_base.data(), net->dbls_base.data(), &net->d_girt, &net->girt);
     if (rc) return rc;
   }
+  if (girt_smem_bytes(net->dev, net->girt, (net->dev.flags & NETF_PREFACTOR) || a->numerical_derivatives, nullptr,
+                      nullptr) > 227u * 1024u)
+    return PF_ERR_TOO_LARGE;
   return launch_girt_assemble(net->dev, net->girt, *state, *a, net->num_sms, (cudaStream_t)stream);
 }
 

@@ -232,6 +232,29 @@ __device__ __forceinline__ double interp_logK(const double* c, double temp) {
   return c[0] * log(tk) + c[1] + c[2] * tk + c[3] / tk + c[4] / (tk * tk);
 }
 
+// interp_logK for many reactions at one temperature: ln T_K, 1/T_K and
+// 1/T_K^2 once per cell.  Each quotient c/t is the product q = c (1/t) plus
+// one residual correction q + (c - q t)(1/t) (Markstein's correction step,
+// one fused multiply-add for the exact residual), which gives the rounded
+// quotient but for rare ties -- four FP64 operations instead of a division.
+struct LogKAtT {
+  double ltk, tk, itk, tk2, itk2;
+  __device__ __forceinline__ explicit LogKAtT(double temp) {
+    tk = temp + 273.15;
+    ltk = log(tk);
+    itk = 1.0 / tk;
+    tk2 = tk * tk;
+    itk2 = 1.0 / tk2;
+  }
+  __device__ __forceinline__ static double quot(double c, double t, double it) {
+    const double q = c * it;
+    return fma(fma(-q, t, c), it, q);
+  }
+  __device__ __forceinline__ double operator()(const double* c) const {
+    return c[0] * ltk + c[1] + c[2] * tk + quot(c[3], tk, itk) + quot(c[4], tk2, itk2);
+  }
+};
+
 // Per-cell SoA accessor
 struct SoA {
   int64_t N;

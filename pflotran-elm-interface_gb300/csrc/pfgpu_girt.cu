@@ -18,14 +18,28 @@
 // computes dtot_X once and writes the diagonal block and the (Y, X) block of
 // every neighbour row Y; nothing is accumulated in memory.
 //
-// GB300 runs FP64 at ~1.7 lane-operations per clock per SM and a warp
+// GB300 runs FP64 at ~2 lane-operations per clock per SM and a warp
 // instruction costs the same pipe time with idle lanes, so all FP64 work is
-// one cell per lane:
+// one cell per lane, and the count of FP64 operations per cell sets the
+// speed:
 //   girt_cell_kernel      RTotal (totals, sec_molal), kinetic minerals and
-//                         their derivative, dtotal entry by entry, the block
-//                         column, and the cell's reaction residual
+//                         their derivative, dtotal, the block column, and the
+//                         cell's reaction residual
 //   girt_residual_kernel  flux + accumulation terms of the residual row
 //                         (needs the neighbours' totals of the first launch)
+// The cell kernel's arithmetic:
+//   * speciation in product form: s_i = K_i prod_j a_j^nu_ij / gamma_i with
+//     K_i = exp(-logK_i ln 10) computed once per block (isothermal, no water
+//     term) and every factor one multiply from a power table of a, a^2, 1/a,
+//     1/a^2 -- no transcendental per complex or per species;
+//   * d total/d m_c = den (delta_rc + sum_i nu_ri nu_ci s_i / m_c); the log
+//     formulation scales column c by m_c, which cancels the division:
+//     den (delta_rc m_c + sum_i nu_ri nu_ci s_i) is symmetric, so the sum is
+//     accumulated once per complex on the packed lower triangle, and so is
+//     the kinetic minerals' part sum_m nu_rm nu_cm dIm/dQK QK den 1e-3;
+//   * the blocks are written as whole 32-byte sectors (four doubles per
+//     store; BAIJ blocks of n*n % 4 == 0 doubles start on 32-byte
+//     boundaries).
 // With equilibrium sorption the cell kernel also runs RTotalSorb (total_sorb,
 // the ion-exchange warm start) and adds dtotal_sorb * V/dt to its diagonal
 // block (RAccumulationSorbDerivative, reactive_transport.F90:3183); the
@@ -33,8 +47,6 @@
 // Both are unconditional in the reference, dry cells included.  Minerals with
 // rate prefactors take their rate from prefactor_rate, and the cell kernel
 // adds the prefactor derivative to its diagonal block the same way.
-// Per-thread scratch (molalities, secondary molalities, mineral terms) lives
-// in shared memory, interleaved by thread so that accesses are conflict-free.
 // The diagonal flux term sums the connection coefficients first
 // ((sum_q c_q) dtot rather than sum_q (c_q dtot)); every c_q there is >= 0
 // (upwinding), so the two orders differ by rounding only.
@@ -57,11 +69,47 @@ struct Geo {
   const double* qz;
 };
 
-// doubles of per-thread shared memory: m, 1/m, ln a, totals (n each), the
-// secondary molalities (ns), the mineral column terms u (one per mineral CSR
-// slot) and the mineral derivative factors (nm)
-__host__ __device__ inline int thread_doubles(const DevNet& net) {
-  return 4 * net.n + net.ns + net.nnz_m + net.nm;
+// Shared memory of a block of the cell kernel:
+//   block part   K (ns + nm doubles, isothermal networks without water:
+//                exp(-logK ln 10) of every complex and kinetic mineral), then,
+//                when they fit, copies of the network's tables and of the
+//                assembly tables (read there instead of global memory)
+//   thread part  per-thread scratch, interleaved by thread (element e of a
+//                thread at P[e * bd], bd = threads per block, so that a warp's
+//                accesses to one element fall in distinct banks):
+//     pa  [2n]        a = m gamma and 1/a of the species that need it (their
+//                     squares are one more multiply); 1/m afterwards (linear
+//                     formulation)
+//     E   [n(n+1)/2]  packed lower triangle of sum_i nu_ri nu_ci s_i, turned
+//                     into d total/d m times the column scaling (log form)
+//     T   [n]         totals (mol/kg water); then GQ [nm] = dIm/dQK * QK *
+//                     den_kg * 1e-3 of each kinetic mineral
+//     lna [n]         ln a (rate prefactors and numerical derivatives only)
+struct Layout {
+  int pa, E, T, GQ, lna, per_thread;
+};
+__host__ __device__ inline Layout layout(const DevNet& net, bool with_lna) {
+  const int n = net.n;
+  Layout L;
+  L.pa = 0;
+  L.E = 2 * n;
+  L.T = L.E + n * (n + 1) / 2;
+  L.GQ = L.T;
+  L.lna = L.T + (n > net.nm ? n : net.nm);
+  L.per_thread = L.lna + (with_lna ? n : 0);
+  return L;
+}
+// bytes of the block part: K, then the staged tables (each 16-byte padded)
+__host__ __device__ inline size_t pad16(size_t b) { return (b + 15) & ~size_t(15); }
+__host__ __device__ inline size_t block_k_bytes(const DevNet& net) { return pad16((size_t)(net.ns + net.nm) * 8); }
+__host__ __device__ inline size_t block_table_bytes(const DevNet& net, const GirtTabs& gt) {
+  return pad16((size_t)net.int_words * 4) + pad16((size_t)net.dbl_words * 8) + (size_t)gt.ibytes + (size_t)gt.dbytes;
+}
+
+// packed index of the symmetric entry (r, c)
+__device__ __forceinline__ int sym_index(int r, int c) {
+  const int hi = r > c ? r : c, lo = r > c ? c : r;
+  return hi * (hi + 1) / 2 + lo;
 }
 
 // harmonic_tran_coefs_over_dist (transport.F90:199-225) for a connection at
@@ -135,47 +183,59 @@ __device__ __forceinline__ int find_block(const int32_t* __restrict__ rowptr, co
   return -1;
 }
 
-// Rate prefactors (the girt_cell_kernel<true> instantiation only).  P: the thread's scratch (m at P[j*bd], ln a at
-// P[o_lna + j*bd], complexes at P[o_s + i*bd]).
-__device__ __noinline__ double pref_rate(const Tables& T, const PfCellState& st, long long X, const double* P,
-                                         int bd, int o_lna, int o_s, double temp, int m) {
-  const SoA soa{st.ncells};
+// What the rate-prefactor and forward-difference helpers read of one cell:
+// m and the activity coefficients from the state, ln a from the thread's
+// scratch, the complexes' molalities as written by this launch.
+struct CellView {
+  const PfCellState* st;
+  long long X;
+  const double* lna;  // the thread's ln a, element j at lna[j * bd]
+  int bd;
+  __device__ __forceinline__ int64_t at(int k) const { return (int64_t)k * st->ncells + X; }
+  __device__ __forceinline__ double m(int j) const { return st->pri_molal[at(j)]; }
+  __device__ __forceinline__ double ln_act(int j) const { return lna[j * bd]; }
+  __device__ __forceinline__ double ln_sec_act(int i) const {
+    return log(st->sec_molal[at(i)]) + log(st->sec_act_coef[at(i)]);
+  }
+};
+
+// Rate prefactors (instantiations with HAS_LNA only)
+__device__ __noinline__ double pref_rate(const Tables& T, const CellView& cv, double temp, int m) {
   double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
   return prefactor_rate(
-      T, m, [&](int j) { return P[o_lna + j * bd]; },
-      [&](int i) { return log(P[o_s + i * bd]) + log(st.sec_act_coef[soa.at(i, X)]); }, temp, pref, lnps);
+      T, m, [&](int j) { return cv.ln_act(j); }, [&](int i) { return cv.ln_sec_act(i); }, temp, pref, lnps);
 }
 
 // adds the prefactor part of the reaction Jacobian of the minerals in mask
 // to the diagonal block D (column-major, columns scaled by m when logf)
-__device__ __noinline__ void pref_jacobian(const DevNet& net, const Tables& T, const PfCellState& st, long long X,
-                                           const double* P, int bd, int o_lna, int o_s, double temp,
+__device__ __noinline__ void pref_jacobian(const DevNet& net, const Tables& T, const CellView& cv, double temp,
                                            double volume, bool logf, bool tsec, unsigned mask, double* D) {
-  const SoA soa{st.ncells};
+  const PfCellState& st = *cv.st;
   const int n = net.n;
-  auto ln_act = [&](int j) { return P[o_lna + j * bd]; };
-  auto ln_sec_act = [&](int i) { return log(P[o_s + i * bd]) + log(st.sec_act_coef[soa.at(i, X)]); };
+  auto ln_act = [&](int j) { return cv.ln_act(j); };
+  auto ln_sec_act = [&](int i) { return cv.ln_sec_act(i); };
   for (int m = 0; m < net.nm; ++m) {
     if (!((mask >> m) & 1u)) continue;
     double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
     const double sum = prefactor_rate(T, m, ln_act, ln_sec_act, temp, pref, lnps);
     prefactor_derivative(
-        T, m, st.mnrl_rate[soa.at(m, X)] * volume, sum, pref, lnps, ln_act, ln_sec_act,
-        [&](int j) { return st.pri_act_coef[soa.at(j, X)]; }, [&](int i) { return st.sec_act_coef[soa.at(i, X)]; },
-        [&](int j) { return log(P[j * bd]); },
+        T, m, st.mnrl_rate[cv.at(m)] * volume, sum, pref, lnps, ln_act, ln_sec_act,
+        [&](int j) { return st.pri_act_coef[cv.at(j)]; }, [&](int i) { return st.sec_act_coef[cv.at(i)]; },
+        [&](int j) { return log(cv.m(j)); },
         [&](int i) {
           return add_h2o(-(tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i)) * LOG_TO_LN, T.sec_h2o(i),
-                         cell_lnaw(net, st, X));
+                         cell_lnaw(net, st, cv.X));
         },
         temp,
-        [&](int r, int c, double v) { D[c * n + r] = fma(v, logf ? P[c * bd] : 1.0, D[c * n + r]); });
+        [&](int r, int c, double v) { D[c * n + r] = fma(v, logf ? cv.m(c) : 1.0, D[c * n + r]); });
   }
 }
 
 // The mineral part of RReaction's residual for one cell (RKineticMineral
 // without the derivative, reaction_mineral.F90:647-913), at primary ln
 // activities lna[] and complexes' ln activities ln_sec_act(i): the same
-// arithmetic as the cell kernel's mineral loop.
+// arithmetic as the cell kernel's mineral loop, with ln Q/K summed as the
+// reference sums it.
 template <class LnSecAct>
 __device__ void mineral_residual(const DevNet& net, const Tables& T, const PfCellState& st, long long X,
                                  const double* lna, LnSecAct ln_sec_act, double temp, double volume, double* Res) {
@@ -222,33 +282,34 @@ __device__ void mineral_residual(const DevNet& net, const Tables& T, const PfCel
 // primary molality raised by 1e-5 of itself, RTotal's complexes at the
 // raised value, the mineral residual again; columns below 1e-40 in magnitude
 // zeroed, then added to D in the column scaling.
-__device__ __noinline__ void numerical_reaction_jacobian(const DevNet& net, const Tables& T, const PfCellState& st,
-                                                         long long X, const double* P, int bd, int o_lna, int o_s,
+__device__ __noinline__ void numerical_reaction_jacobian(const DevNet& net, const Tables& T, const CellView& cv,
                                                          double temp, double volume, bool logf, bool tsec,
                                                          double* D) {
-  const SoA soa{st.ncells};
+  const PfCellState& st = *cv.st;
+  const long long X = cv.X;
   const int n = net.n;
   double lna[PF_MAX_NCOMP], res0[PF_MAX_NCOMP], res1[PF_MAX_NCOMP];
   for (int j = 0; j < n; ++j) {
-    lna[j] = P[o_lna + j * bd];
+    lna[j] = cv.ln_act(j);
     res0[j] = 0.0;
   }
-  mineral_residual(
-      net, T, st, X, lna, [&](int i) { return log(P[o_s + i * bd]) + log(st.sec_act_coef[soa.at(i, X)]); }, temp,
-      volume, res0);
+  // RTotal of the copy at lna[], complex i, as the reference's RTotal forms
+  // it (both residuals from the same formula, so that their difference is
+  // the perturbation's alone)
+  auto ln_sec_act = [&](int i) {
+    double lnQK = -(tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i)) * LOG_TO_LN;
+    if (water_on(net)) lnQK = add_h2o(lnQK, T.sec_h2o(i), cell_lnaw(net, st, X));
+    for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
+    const double g = st.sec_act_coef[cv.at(i)];
+    return log(exp(lnQK) / g) + log(g);
+  };
+  mineral_residual(net, T, st, X, lna, ln_sec_act, temp, volume, res0);
   for (int jc = 0; jc < n; ++jc) {
-    const double m0 = P[jc * bd];
+    const double m0 = cv.m(jc);
     const double pert = m0 * 1.0e-5;  // perturbation_tolerance, reaction.F90:41
     const double saved = lna[jc];
-    lna[jc] = log(m0 + pert) + log(st.pri_act_coef[soa.at(jc, X)]);
+    lna[jc] = log(m0 + pert) + log(st.pri_act_coef[cv.at(jc)]);
     for (int i = 0; i < n; ++i) res1[i] = 0.0;
-    auto ln_sec_act = [&](int i) {  // RTotal of the perturbed copy, complex i
-      double lnQK = -(tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i)) * LOG_TO_LN;
-      if (water_on(net)) lnQK = add_h2o(lnQK, T.sec_h2o(i), cell_lnaw(net, st, X));
-      for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
-      const double g = st.sec_act_coef[soa.at(i, X)];
-      return log(exp(lnQK) / g) + log(g);
-    };
     mineral_residual(net, T, st, X, lna, ln_sec_act, temp, volume, res1);
     lna[jc] = saved;
     const double mc = logf ? m0 : 1.0;
@@ -260,90 +321,177 @@ __device__ __noinline__ void numerical_reaction_jacobian(const DevNet& net, cons
   }
 }
 
-// HAS_PF: rate prefactors; NUMJAC: the reaction Jacobian by forward
-// differences (instantiated with HAS_PF, whose rate code it needs)
+// 32-byte store of four doubles (dst 32-byte aligned): one whole sector
+__device__ __forceinline__ void st_sector(double* dst, double a, double b, double c, double d) {
+  asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(dst), "d"(a), "d"(b), "d"(c), "d"(d) : "memory");
+}
+
+// Kernel of one cell per thread.  HAS_PF: rate prefactors; NUMJAC: the
+// reaction Jacobian by forward differences (instantiated with HAS_PF, whose
+// rate code it needs).  vec: doubles per store of the block writes (4: every
+// block starts on a 32-byte boundary and n*n % 4 == 0; 2: 16 bytes; 1).
+// staged: the tables are copied into the block's shared memory.  kmode: 0
+// without a K cache, 1 computing the per-cell K of the reactions into kcache,
+// 2 reading them from it.
 template <bool HAS_PF, bool NUMJAC>
 __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt,
                                                         const int32_t* __restrict__ rowptr,
                                                         const int32_t* __restrict__ colidx, double* __restrict__ r,
-                                                        double* __restrict__ values, int vec2) {
-  extern __shared__ double smem[];
-  const long long X = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (X >= st.ncells) return;
+                                                        double* __restrict__ values, int vec, int staged,
+                                                        double* __restrict__ kcache, int kmode) {
+  constexpr bool HAS_LNA = HAS_PF || NUMJAC;
+  extern __shared__ __align__(16) unsigned char sraw[];
   const int bd = blockDim.x;
-  double* P = smem + threadIdx.x;  // this thread's scratch: P[k * bd]
+  const Layout Lo = layout(net, HAS_LNA);
+  double* const Kc = reinterpret_cast<double*>(sraw);
+  size_t off = block_k_bytes(net);
+  const int32_t* sI = net.ints;
+  const double* sD = net.dbls;
+  const unsigned char* gbase = reinterpret_cast<const unsigned char*>(gt.buf);
+  if (staged) {
+    int32_t* dI = reinterpret_cast<int32_t*>(sraw + off);
+    for (int k = threadIdx.x; k < net.int_words; k += bd) dI[k] = net.ints[k];
+    off += pad16((size_t)net.int_words * 4);
+    double* dD = reinterpret_cast<double*>(sraw + off);
+    for (int k = threadIdx.x; k < net.dbl_words; k += bd) dD[k] = net.dbls[k];
+    off += pad16((size_t)net.dbl_words * 8);
+    const int gw = (gt.ibytes + gt.dbytes) / 8;  // both parts are 8-byte multiples
+    double* dG = reinterpret_cast<double*>(sraw + off);
+    for (int k = threadIdx.x; k < gw; k += bd) dG[k] = reinterpret_cast<const double*>(gt.buf)[k];
+    sI = dI;
+    sD = dD;
+    gbase = sraw + off;
+    off += (size_t)gt.ibytes + gt.dbytes;
+  }
+  const int32_t* gI = reinterpret_cast<const int32_t*>(gbase);
+  const double* gD = reinterpret_cast<const double*>(gbase + gt.ibytes);
+  const int32_t* __restrict__ s_pair_ptr = gI + gt.o_spp;
+  const int32_t* __restrict__ s_pair_k = gI + gt.o_spk;
+  const double* __restrict__ s_pair_c = gD + gt.d_spc;
+  const int32_t* __restrict__ m_ent_ptr = gI + gt.o_mep;
+  const int32_t* __restrict__ m_ent_m = gI + gt.o_mem;
+  const double* __restrict__ m_ent_c = gD + gt.d_mec;
+  const Tables T{sI, sD, &net};
   const int n = net.n, nn = n * n, ns = net.ns, nm = net.nm;
-  const int o_ic = n * bd, o_lna = 2 * n * bd, o_t = 3 * n * bd, o_s = 4 * n * bd, o_u = (4 * n + ns) * bd,
-            o_G = (4 * n + ns + net.nnz_m) * bd;
-  const Tables T{net.ints, net.dbls, &net};
-  const SoA soa{st.ncells};
-  const bool logf = net.o.use_log_formulation != 0;
+  const bool has_h2o = water_on(net);
   const bool tsec = !net.o.isothermal && (net.flags & NETF_SEC_LOGKCOEF);
   const bool tmin = !net.o.isothermal && (net.flags & NETF_MNRL_LOGKCOEF);
+  const bool kc_sec = !tsec && !has_h2o, kc_mn = !tmin && !has_h2o;
+  if (kmode != 2)
+    for (int k = threadIdx.x; k < ns + nm; k += bd) {
+      if (k < ns ? kc_sec : kc_mn)
+        Kc[k] = exp(-(k < ns ? net.dbls[net.o_sec_logK + k] : net.dbls[net.o_mnrl_logK + k - ns]) * LOG_TO_LN);
+    }
+  __syncthreads();
+  const long long X = (long long)blockIdx.x * bd + threadIdx.x;
+  if (X >= st.ncells) return;
+  double* P = reinterpret_cast<double*>(sraw + off) + threadIdx.x;  // element e at P[e * bd]
+  const SoA soa{st.ncells};
+  const bool logf = net.o.use_log_formulation != 0;
   const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
-  constexpr bool has_pf = HAS_PF;  // rate prefactors: a separate instantiation
   unsigned pf_active = 0;  // minerals whose prefactor derivative is due
   const double temp = st.temperature ? st.temperature[X] : 25.0;
-  const bool has_h2o = water_on(net);
   const double lnaw = cell_lnaw(net, st, X);
   const double den_k = st.den_kg[X], den_L = den_k * 1.0e-3;
   const double por = st.porosity[X], sat = st.saturation[X], volume = st.volume[X];
   const bool dry = sat < RT_MIN_SATURATION;
-  // ---- RTotalAqueous (reaction.F90:4665-4759)
-  for (int jj = 0; jj < n; ++jj) {
-    const double m = st.pri_molal[soa.at(jj, X)];
-    P[jj * bd] = m;
-    P[o_ic + jj * bd] = 1.0 / m;
-    P[o_lna + jj * bd] = log(m) + log(st.pri_act_coef[soa.at(jj, X)]);
+  const unsigned neg = (unsigned)net.neg_mask;
+  // K of complex i (divided by its activity coefficient) and of mineral m:
+  // the block's table, or logK at the cell's temperature (ln T and 1/T once
+  // per cell) with the water term; cached per cell when kmode != 0
+  const LogKAtT logk_t(temp);
+  auto k_sec = [&](int i) {
+    if (kmode == 2) return kcache[soa.at(i, X)];
+    double K;
+    if (kc_sec) {
+      K = Kc[i];
+    } else {
+      const double logK = tsec ? logk_t(T.sec_logKcoef(i)) : T.sec_logK(i);
+      K = exp(add_h2o(-logK * LOG_TO_LN, T.sec_h2o(i), lnaw));
+    }
+    K = K / st.sec_act_coef[soa.at(i, X)];
+    if (kmode == 1) kcache[soa.at(i, X)] = K;
+    return K;
+  };
+  auto k_mn = [&](int m) {
+    if (kmode == 2) return kcache[soa.at(ns + m, X)];
+    double K;
+    if (kc_mn) {
+      K = Kc[ns + m];
+    } else {
+      const double logK = tmin ? logk_t(T.mnrl_logKcoef(m)) : T.mnrl_logK(m);
+      K = exp(add_h2o(-logK * LOG_TO_LN, T.mnrl_h2o(m), lnaw));
+    }
+    if (kmode == 1) kcache[soa.at(ns + m, X)] = K;
+    return K;
+  };
+  // ---- RTotalAqueous (reaction.F90:4665-4759) in product form: s_i =
+  // (K_i / gamma_i) prod_j a_j^nu_ij, each factor one or two multiplies from
+  // a and 1/a for nu in {+-1, +-2} (exp(nu ln a) otherwise); the reference's
+  // exp(ln K + sum nu ln a) / gamma_i to rounding
+  for (int j = 0; j < n; ++j) {
+    const double m = st.pri_molal[soa.at(j, X)], gam = st.pri_act_coef[soa.at(j, X)];
+    const double a = m * gam;
+    P[(Lo.pa + j) * bd] = a;
+    if ((neg >> j) & 1u) P[(Lo.pa + n + j) * bd] = 1.0 / a;
+    P[(Lo.T + j) * bd] = m;  // total = m, then += nu s
+    if constexpr (HAS_LNA) P[(Lo.lna + j) * bd] = log(m) + log(gam);
   }
-  for (int jj = 0; jj < n; ++jj) P[o_t + jj * bd] = P[jj * bd];  // total = m, then += nu s
+  const int nsym = n * (n + 1) / 2;
+  for (int k = 0; k < nsym; ++k) P[(Lo.E + k) * bd] = 0.0;
+  // factor a_j^nu from its power-table code (0: a, 1: a^2, 2: 1/a, 3: 1/a^2)
+  auto factor = [&](int pe, double nu, int j) {
+    if (pe >= 0) {
+      const int code = pe / n;
+      const double b = P[(Lo.pa + (code >= 2 ? n : 0) + j) * bd];
+      return (code & 1) ? b * b : b;
+    }
+    const double la = HAS_LNA ? P[(Lo.lna + j) * bd] : log(P[(Lo.pa + j) * bd]);
+    return exp(nu * la);
+  };
   for (int i = 0; i < ns; ++i) {
-    const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-    double lnQK = -logK * LOG_TO_LN;
-    if (has_h2o) lnQK = add_h2o(lnQK, T.sec_h2o(i), lnaw);
+    double s = k_sec(i);
     const int b = T.sec_begin(i), e = T.sec_end(i);
-    for (int p = b; p < e; ++p) lnQK = lnQK + T.sec_nu(p) * P[o_lna + T.sec_idx(p) * bd];
-    const double sv = exp(lnQK) / st.sec_act_coef[soa.at(i, X)];
-    P[o_s + i * bd] = sv;
-    st.sec_molal[soa.at(i, X)] = sv;
-  }
-  // totals in the reference's order: per component, the secondaries ascending
-  for (int i = 0; i < ns; ++i) {
-    const double sv = P[o_s + i * bd];
-    for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) {
-      const int a = o_t + T.sec_idx(p) * bd;
-      P[a] = P[a] + T.sec_nu(p) * sv;
+    for (int p = b; p < e; ++p) s *= factor(T.sec_pidx(p), T.sec_nu(p), T.sec_idx(p));
+    st.sec_molal[soa.at(i, X)] = s;
+    // totals in the reference's order: per component, the complexes ascending
+    for (int p = b; p < e; ++p) {
+      const int a = (Lo.T + T.sec_idx(p)) * bd;
+      P[a] = P[a] + T.sec_nu(p) * s;
+    }
+    // sum_i nu_ri nu_ci s_i, complexes ascending as the reference's entries
+    for (int q = s_pair_ptr[i]; q < s_pair_ptr[i + 1]; ++q) {
+      const int a = (Lo.E + s_pair_k[q]) * bd;
+      P[a] = fma(s_pair_c[q], s, P[a]);
     }
   }
-  for (int jj = 0; jj < n; ++jj) st.total[soa.at(jj, X)] = P[o_t + jj * bd] * den_L;
+  for (int j = 0; j < n; ++j) st.total[soa.at(j, X)] = P[(Lo.T + j) * bd] * den_L;
   // ---- RKineticMineral (reaction_mineral.F90:647-1078): rates, reaction
   // residual (into r, finished by girt_residual_kernel), derivative factors
-  for (int jj = 0; jj < n; ++jj) r[X * n + jj] = 0.0;
+  // (GQ takes the place of the totals)
+  for (int j = 0; j < n; ++j) r[X * n + j] = 0.0;
+  const CellView cv{&st, X, P + Lo.lna * bd, bd};
   for (int m = 0; m < nm; ++m) {
     const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
-    double Gm = 0.0, QK = 0.0;
-    bool active = false;
+    double GQ = 0.0;
     if (!dry) {
-      const double logK = tmin ? interp_logK(T.mnrl_logKcoef(m), temp) : T.mnrl_logK(m);
-      double lnQK = -logK * LOG_TO_LN;
-      if (has_h2o) lnQK = add_h2o(lnQK, T.mnrl_h2o(m), lnaw);
-      for (int p = b; p < e; ++p) lnQK = lnQK + T.mnrl_nu(p) * P[o_lna + T.mnrl_idx(p) * bd];
-      QK = exp(lnQK);
+      double QK = k_mn(m);
+      for (int p = b; p < e; ++p) QK *= factor(T.mnrl_pidx(p), T.mnrl_nu(p), T.mnrl_idx(p));
       double aff;
       if (has_tk) aff = 1.0 - pow(QK, 1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m)));
       else if (has_msf) aff = 1.0 - pow(QK, 1.0 / T.msf(m));
       else aff = 1.0 - QK;
       const double sign_ = fsign1(aff);
       const double vf = st.mnrl_volfrac[soa.at(m, X)];
-      active = (vf > 0 || sign_ < 0.0) && !(T.irreversible(m) == 1 && sign_ < 0.0) &&
-               !(T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m));
+      const bool active = (vf > 0 || sign_ < 0.0) && !(T.irreversible(m) == 1 && sign_ < 0.0) &&
+                          !(T.thresh(m) > 0.0 && sign_ < 0.0 && QK < T.thresh(m));
       double rate_out = 0.0;
       if (active) {
         const double rl = T.limiter(m);
         if (rl > 0.0) aff = aff / (1.0 + (1.0 - aff) / rl);
         double kr;
-        if (has_pf && T.pf_cnt(m) > 0) {
-          kr = pref_rate(T, st, X, P, bd, o_lna, o_s, temp, m);
+        if (HAS_PF && T.pf_cnt(m) > 0) {
+          kr = pref_rate(T, cv, temp, m);
           pf_active |= 1u << m;
         } else {
           double arr = 1.0;
@@ -363,19 +511,33 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
           dIm_dQK = dIm_dQK * (1.0 / (has_msf ? T.msf(m) * T.temkin(m) : T.temkin(m))) / QK * (1.0 - aff);
         else if (has_msf)
           dIm_dQK = dIm_dQK * (1.0 / T.msf(m)) / QK * (1.0 - aff);
+        double Gm;
         if (rl > 0.0) {
           const double den = 1.0 + (1.0 - aff) / rl;
           Gm = dIm_dQK * (1.0 + QK / rl / den) / den;
         } else {
           Gm = dIm_dQK;
         }
+        // d rate_r/d m_c = nu_r Gm nu_c QK / m_c den_kg 1e-3 (:944-947, :1062-1071)
+        GQ = Gm * QK * den_k * 1.0e-3;
       }
       st.mnrl_rate[soa.at(m, X)] = rate_out;
+    } else if (kmode == 1) {
+      k_mn(m);  // the cache holds every cell's K
     }
-    P[o_G + m * bd] = Gm;
-    // dQK/dm_j (the reference's den*1e-3 factor included, :944-947)
-    for (int p = b; p < e; ++p)
-      P[o_u + p * bd] = active ? T.mnrl_nu(p) * QK * P[o_ic + T.mnrl_idx(p) * bd] * den_k * 1.0e-3 : 0.0;
+    P[(Lo.GQ + m) * bd] = GQ;
+  }
+  // ---- d total/d m in the column scaling: log formulation
+  // den (delta_rc m_c + sum_i nu_ri nu_ci s_i), symmetric; the linear one
+  // divides the sum by m_c per column at the write, from 1/m in pa
+  if (logf) {
+    for (int hi = 0, k = 0; hi < n; ++hi)
+      for (int lo = 0; lo <= hi; ++lo, ++k) {
+        const int a = (Lo.E + k) * bd;
+        P[a] = (lo == hi ? P[a] + st.pri_molal[soa.at(hi, X)] : P[a]) * den_L;
+      }
+  } else {
+    for (int j = 0; j < n; ++j) P[(Lo.pa + j) * bd] = 1.0 / st.pri_molal[soa.at(j, X)];
   }
   // ---- block column X
   Conns c;
@@ -392,24 +554,47 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   const int dblk = find_block(rowptr, colidx, X, X);
   const double psvd_t = por * sat * 1000.0 * volume / dt;
   const double cdiag = csum + psvd_t;
-  auto entry = [&](int fe, double& vdiag, double& e) {
+  // entry fe of the column-major block: e = d total/d m in the column scaling,
+  // v = the diagonal block's value
+  auto entry = [&](int fe, double& v, double& e) {
     const int col = fe / n, row = fe - col * n;
-    const int f = row * n + col;
-    double acc = 0.0;
-    for (int q = gt.e_sec_ptr[f]; q < gt.e_sec_ptr[f + 1]; ++q)
-      acc = fma(gt.e_sec_nr[q], P[o_s + gt.e_sec_p[q] * bd], acc);
-    const double d = ((row == col ? 1.0 : 0.0) + acc * P[o_ic + col * bd]) * den_L;
-    double jr = 0.0;
-    if (!NUMJAC)
-      for (int q = gt.e_mn_ptr[f]; q < gt.e_mn_ptr[f + 1]; ++q)
-        jr = fma(gt.e_mn_nr[q] * P[o_G + gt.e_mn_m[q] * bd], P[o_u + gt.e_mn_p[q] * bd], jr);
-    if (fabs(jr) < 1.0e-40) jr = 0.0;  // reaction.F90:4232-4237
-    const double mc = logf ? P[col * bd] : 1.0;
-    const double v = dry ? fma(d, csum, (row == col) ? 1.0 : 0.0) : fma(d, cdiag, jr);
-    vdiag = v * mc;
-    e = d * mc;
+    const double E = P[(Lo.E + sym_index(row, col)) * bd];
+    const double im = logf ? 0.0 : P[(Lo.pa + col) * bd];
+    e = logf ? E : den_L * fma(E, im, row == col ? 1.0 : 0.0);
+    if (dry) {
+      v = fma(csum, e, row == col ? (logf ? st.pri_molal[soa.at(col, X)] : 1.0) : 0.0);
+      return;
+    }
+    double jl = 0.0;
+    if (!NUMJAC) {
+      const int f = row * n + col;
+      const int qb = m_ent_ptr[f], qe = m_ent_ptr[f + 1];
+      if (qb < qe) {
+        for (int q = qb; q < qe; ++q) jl = fma(m_ent_c[q], P[(Lo.GQ + m_ent_m[q]) * bd], jl);
+        // the reference zeroes |d R/d m| < 1e-40 before the column scaling
+        // (reaction.F90:4232-4237)
+        if (logf) {
+          if (fabs(jl) < 1.0e-40 * st.pri_molal[soa.at(col, X)]) jl = 0.0;
+        } else {
+          jl = jl * im;
+          if (fabs(jl) < 1.0e-40) jl = 0.0;
+        }
+      }
+    }
+    v = fma(cdiag, e, jl);
   };
-  if (vec2) {
+  if (vec == 4) {
+    for (int fe = 0; fe < nn; fe += 4) {
+      double v[4], e[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) entry(fe + u, v[u], e[u]);
+      if (dblk >= 0) st_sector(values + (size_t)dblk * nn + fe, v[0], v[1], v[2], v[3]);
+#pragma unroll
+      for (int q = 0; q < 6; ++q)
+        if (blk[q] >= 0)
+          st_sector(values + (size_t)blk[q] * nn + fe, sc[q] * e[0], sc[q] * e[1], sc[q] * e[2], sc[q] * e[3]);
+    }
+  } else if (vec == 2) {
     for (int fe = 0; fe < nn; fe += 2) {
       double v0, e0, v1, e1;
       entry(fe, v0, e0);
@@ -432,12 +617,12 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
   }
   // ---- rate-prefactor part of the reaction Jacobian (its residual part is in
   // the rates above), added to the diagonal block in the column scaling
-  if (NUMJAC && !dry && dblk >= 0)
-    numerical_reaction_jacobian(net, T, st, X, P, bd, o_lna, o_s, temp, volume, logf, tsec,
-                                values + (size_t)dblk * nn);
-  else if (has_pf && pf_active && dblk >= 0)
-    pref_jacobian(net, T, st, X, P, bd, o_lna, o_s, temp, volume, logf, tsec, pf_active,
-                  values + (size_t)dblk * nn);
+  if constexpr (HAS_LNA) {
+    if (NUMJAC && !dry && dblk >= 0)
+      numerical_reaction_jacobian(net, T, cv, temp, volume, logf, tsec, values + (size_t)dblk * nn);
+    else if (HAS_PF && pf_active && dblk >= 0)
+      pref_jacobian(net, T, cv, temp, volume, logf, tsec, pf_active, values + (size_t)dblk * nn);
+  }
   // ---- equilibrium sorption (RTotalSorb in RTUpdateAuxVars; a failed
   // ion-exchange solve leaves the last iterate, the reference's
   // message-and-continue).  Only this thread writes its diagonal block.
@@ -446,11 +631,13 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
     double* D = values + (size_t)dblk * nn;
     const double v_t = volume / dt;
     total_sorb(
-        net, T, [&](int j) { return P[j * bd]; }, [&](int j) { return st.pri_act_coef[soa.at(j, X)]; },
+        net, T, [&](int j) { return st.pri_molal[soa.at(j, X)]; }, [&](int j) { return st.pri_act_coef[soa.at(j, X)]; },
         [&](int m) { return st.mnrl_volfrac[soa.at(m, X)]; }, por, den_k,
         st.ionx_ref_sorbed ? st.ionx_ref_sorbed + X : nullptr, st.ncells,
         [&](int j, double v) { st.total_sorb[soa.at(j, X)] += v; },
-        [&](int i, int j, double v) { D[j * n + i] = fma(v * v_t, logf ? P[j * bd] : 1.0, D[j * n + i]); },
+        [&](int i, int j, double v) {
+          D[j * n + i] = fma(v * v_t, logf ? st.pri_molal[soa.at(j, X)] : 1.0, D[j * n + i]);
+        },
         surf_cell(net, st, X));
   }
 }
@@ -499,81 +686,93 @@ __global__ void __launch_bounds__(128) girt_residual_kernel(DevNet net, PfCellSt
 
 int girt_build_tables(const DevNet& net, const int32_t* I, const double* D, void** d_buf, GirtTabs* out) {
   const int n = net.n, nn = n * n;
-  std::vector<std::vector<int32_t>> sp(nn), mp(nn), mm(nn);
-  std::vector<std::vector<double>> snr(nn), mnr(nn);
+  // per complex: its reaction's species pairs (p <= q in the reaction's list)
+  std::vector<int32_t> sp_ptr{0}, sp_k;
+  std::vector<double> sp_c;
   for (int i = 0; i < net.ns; ++i) {
     const int b = I[net.o_sec_ptr + i], e = I[net.o_sec_ptr + i + 1];
-    for (int pc = b; pc < e; ++pc)
-      for (int pr = b; pr < e; ++pr) {
-        const int f = I[net.o_sec_idx + pr] * n + I[net.o_sec_idx + pc];
-        sp[f].push_back(i);
-        snr[f].push_back(D[net.o_sec_nu + pr] * D[net.o_sec_nu + pc]);
+    for (int p = b; p < e; ++p)
+      for (int q = p; q < e; ++q) {
+        const int r = I[net.o_sec_idx + p], c = I[net.o_sec_idx + q];
+        const int hi = r > c ? r : c, lo = r > c ? c : r;
+        sp_k.push_back(hi * (hi + 1) / 2 + lo);
+        sp_c.push_back(D[net.o_sec_nu + p] * D[net.o_sec_nu + q]);
       }
+    sp_ptr.push_back((int32_t)sp_k.size());
   }
+  // per flat entry row*n+col: the minerals whose reaction holds both species
+  std::vector<std::vector<int32_t>> em(nn);
+  std::vector<std::vector<double>> ec(nn);
   for (int m = 0; m < net.nm; ++m) {
     const int b = I[net.o_mnrl_ptr + m], e = I[net.o_mnrl_ptr + m + 1];
-    for (int pc = b; pc < e; ++pc)
-      for (int pr = b; pr < e; ++pr) {
+    for (int pr = b; pr < e; ++pr)
+      for (int pc = b; pc < e; ++pc) {
         const int f = I[net.o_mnrl_idx + pr] * n + I[net.o_mnrl_idx + pc];
-        mp[f].push_back(pc);
-        mm[f].push_back(m);
-        mnr[f].push_back(D[net.o_mnrl_nu + pr]);
+        em[f].push_back(m);
+        ec[f].push_back(D[net.o_mnrl_nu + pr] * D[net.o_mnrl_nu + pc]);
       }
   }
   std::vector<int32_t> ints;
   std::vector<double> dbls;
-  auto csr = [&](const std::vector<std::vector<int32_t>>& rows, int* o_ptr, int* o_idx) {
-    *o_ptr = (int)ints.size();
-    int c = 0;
-    for (auto& rw : rows) { ints.push_back(c); c += (int)rw.size(); }
-    ints.push_back(c);
-    *o_idx = (int)ints.size();
-    for (auto& rw : rows) ints.insert(ints.end(), rw.begin(), rw.end());
-  };
-  auto flat = [&](const std::vector<std::vector<int32_t>>& rows) {
-    const int o = (int)ints.size();
-    for (auto& rw : rows) ints.insert(ints.end(), rw.begin(), rw.end());
-    return o;
-  };
-  auto flatd = [&](const std::vector<std::vector<double>>& rows) {
-    const int o = (int)dbls.size();
-    for (auto& rw : rows) dbls.insert(dbls.end(), rw.begin(), rw.end());
-    return o;
-  };
-  int o_esp, o_esi, o_emp, o_emi;
-  csr(sp, &o_esp, &o_esi);
-  csr(mp, &o_emp, &o_emi);
-  const int o_emm = flat(mm);
-  const int d_esnr = flatd(snr), d_emnr = flatd(mnr);
+  out->o_spp = (int)ints.size();
+  ints.insert(ints.end(), sp_ptr.begin(), sp_ptr.end());
+  out->o_spk = (int)ints.size();
+  ints.insert(ints.end(), sp_k.begin(), sp_k.end());
+  out->o_mep = (int)ints.size();
+  int cnt = 0;
+  for (auto& rw : em) { ints.push_back(cnt); cnt += (int)rw.size(); }
+  ints.push_back(cnt);
+  out->o_mem = (int)ints.size();
+  for (auto& rw : em) ints.insert(ints.end(), rw.begin(), rw.end());
+  out->d_spc = (int)dbls.size();
+  dbls.insert(dbls.end(), sp_c.begin(), sp_c.end());
+  out->d_mec = (int)dbls.size();
+  for (auto& rw : ec) dbls.insert(dbls.end(), rw.begin(), rw.end());
   if (dbls.empty()) dbls.push_back(0.0);
-  const size_t ib = (ints.size() * 4 + 15) & ~size_t(15);
+  while (ints.size() % 4) ints.push_back(0);  // the doubles start on a 16-byte boundary
+  const size_t ib = ints.size() * 4;
   void* buf = nullptr;
   if (cudaMalloc(&buf, ib + dbls.size() * 8) != cudaSuccess) return PF_ERR_CUDA;
-  if (cudaMemcpy(buf, ints.data(), ints.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+  if (cudaMemcpy(buf, ints.data(), ib, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy((char*)buf + ib, dbls.data(), dbls.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
     cudaFree(buf);
     return PF_ERR_CUDA;
   }
-  const int32_t* di = (const int32_t*)buf;
-  const double* dd = (const double*)((char*)buf + ib);
-  out->e_sec_ptr = di + o_esp;
-  out->e_sec_p = di + o_esi;
-  out->e_sec_nr = dd + d_esnr;
-  out->e_mn_ptr = di + o_emp;
-  out->e_mn_p = di + o_emi;
-  out->e_mn_m = di + o_emm;
-  out->e_mn_nr = dd + d_emnr;
+  out->buf = buf;
+  out->ibytes = (int)ib;
+  out->dbytes = (int)(dbls.size() * 8);
   *d_buf = buf;
   return PF_OK;
 }
 
-// threads per block of the cell kernel and its shared memory
-size_t girt_smem_bytes(const DevNet& net, int* threads_per_block) {
-  const size_t tbytes = (size_t)girt::thread_doubles(net) * sizeof(double);
-  int tpb = 128;
-  while (tpb > 32 && tpb * tbytes > 72u * 1024u) tpb -= 32;
-  if (threads_per_block) *threads_per_block = tpb;
-  return tpb * tbytes;
+// threads per block of the cell kernel, whether the tables are staged in
+// shared memory, and the dynamic shared memory: the block size (a multiple
+// of 32, at most 128) that keeps the most warps resident, staging the tables
+// when that costs no warps
+size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, int* threads_per_block,
+                       int* staged) {
+  const size_t tbytes = (size_t)girt::layout(net, with_lna).per_thread * sizeof(double);
+  const size_t kbytes = girt::block_k_bytes(net), tab = girt::block_table_bytes(net, gt);
+  const size_t sm_bytes = 228u * 1024u, per_block_reserved = 1024u;
+  int best = 0, best_warps = -1, best_staged = 0;
+  for (int st = 1; st >= 0; --st) {
+    for (int tpb = 32; tpb <= 128; tpb += 32) {
+      const size_t b = tpb * tbytes + kbytes + (st ? tab : 0);
+      if (b > 227u * 1024u) break;
+      int blocks = (int)(sm_bytes / (b + per_block_reserved));
+      if (blocks > 32) blocks = 32;
+      const int warps = blocks * tpb / 32 > 48 ? 48 : blocks * tpb / 32;
+      if (warps > best_warps || (warps == best_warps && st == best_staged)) {
+        best_warps = warps;
+        best = tpb;
+        best_staged = st;
+      }
+    }
+  }
+  if (best == 0) return (size_t)-1;
+  if (threads_per_block) *threads_per_block = best;
+  if (staged) *staged = best_staged;
+  return best * tbytes + kbytes + (best_staged ? tab : 0);
 }
 
 int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const PfGirtArgs& a,
@@ -582,19 +781,25 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   if (st.ncells == 0) return PF_OK;
   girt::Geo g{a.nx, a.ny, a.nz, a.dx, a.dy, a.dz, a.diffusion_coefficient, a.tortuosity, a.dispersivity,
               a.qx, a.qy, a.qz};
-  int tpb = 32;
-  const size_t smem = girt_smem_bytes(net, &tpb);
+  const bool pf = (net.flags & NETF_PREFACTOR) != 0;
+  const bool with_lna = pf || a.numerical_derivatives;
+  int tpb = 32, staged = 0;
+  const size_t smem = girt_smem_bytes(net, gt, with_lna, &tpb, &staged);
   if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
   auto k = a.numerical_derivatives ? girt::girt_cell_kernel<true, true>
-           : (net.flags & NETF_PREFACTOR) ? girt::girt_cell_kernel<true, false>
-                                          : girt::girt_cell_kernel<false, false>;
+           : pf                    ? girt::girt_cell_kernel<true, false>
+                                   : girt::girt_cell_kernel<false, false>;
   if (smem > 48u * 1024u &&
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PF_ERR_CUDA;
-  // 16-byte stores when every block starts on a 16-byte boundary
-  const int vec2 = ((net.n * net.n) % 2 == 0) && (((uintptr_t)a.values & 15) == 0);
+  // whole-sector stores when every block starts on a 32-byte boundary
+  const int nn = net.n * net.n;
+  const uintptr_t va = (uintptr_t)a.values;
+  const int vec = (nn % 4 == 0 && (va & 31) == 0) ? 4 : ((nn % 2 == 0 && (va & 15) == 0) ? 2 : 1);
+  const int kmode = a.k_cache ? (a.k_cache_valid ? 2 : 1) : 0;
   const long long blocks = (st.ncells + tpb - 1) / tpb;
-  k<<<(unsigned)blocks, tpb, smem, s>>>(net, gt, st, g, a.dt, a.rowptr, a.colidx, a.residual, a.values, vec2);
+  k<<<(unsigned)blocks, tpb, smem, s>>>(net, gt, st, g, a.dt, a.rowptr, a.colidx, a.residual, a.values, vec, staged,
+                                        a.k_cache, kmode);
   if (cudaGetLastError() != cudaSuccess) return PF_ERR_CUDA;
   const long long rblocks = (st.ncells + 127) / 128;
   girt::girt_residual_kernel<<<(unsigned)rblocks, 128, 0, s>>>(net, st, g, a.total_k, a.total_sorb_k, a.dt,

@@ -75,19 +75,23 @@ int launch_update_activity_coefs(const DevNet& net, const PfCellState& st, cudaS
 //   e_mn_*   the kinetic-mineral derivative terms: CSR slot of the column
 //            species in the mineral's reaction, mineral index, nu_row
 struct GirtTabs {
-  const int32_t* e_sec_ptr;
-  const int32_t* e_sec_p;
-  const double* e_sec_nr;
-  const int32_t* e_mn_ptr;
-  const int32_t* e_mn_p;
-  const int32_t* e_mn_m;
-  const double* e_mn_nr;
+  // one device buffer [int32 part (ibytes, 16-byte padded) | double part]:
+  //   per complex i, the species pairs (p <= q) of its reaction: CSR s_pair
+  //   (ptr at o_spp, packed symmetric index at o_spk, nu_p nu_q at d_spc);
+  //   per flat entry row*n+col, the kinetic minerals whose reaction holds
+  //   both species: CSR m_ent (ptr at o_mep, mineral at o_mem, nu_row nu_col
+  //   at d_mec)
+  const void* buf;
+  int32_t ibytes, dbytes;
+  int32_t o_spp, o_spk, o_mep, o_mem;  // offsets in int32 words
+  int32_t d_spc, d_mec;                // offsets in doubles
 };
 // host: build the tables from the host copies of the packed network blocks
 // and upload them (*d_buf: the one device allocation)
 int girt_build_tables(const DevNet& net, const int32_t* h_ints, const double* h_dbls, void** d_buf,
                       GirtTabs* out);
-size_t girt_smem_bytes(const DevNet& net, int* threads_per_block);
+size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, int* threads_per_block,
+                       int* staged);
 // RTUpdateAuxVars then the column kernel; a PfStatus
 int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const PfGirtArgs& a,
                          int num_sms, cudaStream_t stream);

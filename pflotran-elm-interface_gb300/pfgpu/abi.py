@@ -177,6 +177,7 @@ class PfGirtArgs(C.Structure):
         ("diffusion_coefficient", C.c_double), ("tortuosity", C.c_double), ("dispersivity", C.c_double),
         ("total_k", _dp), ("dt", C.c_double), ("rowptr", _ip), ("colidx", _ip),
         ("residual", _dp), ("values", _dp), ("total_sorb_k", _dp), ("numerical_derivatives", C.c_int32),
+        ("k_cache", _dp), ("k_cache_valid", C.c_int32),
     ]
 
 

@@ -104,25 +104,35 @@ def kernel_per_iteration(net):
 
 def girt_per_cell(net, offdiag_blocks: float):
     """FP64 flops (FMA = 2) and transcendental calls per cell of one
-    global-implicit assembly (pf_girt_assemble): RTotal (secondary
-    molalities and totals), dtotal by entry lists, the kinetic minerals and
-    their derivative, the residual row, and the block column (diagonal block
-    plus `offdiag_blocks` scaled copies of dtotal diag(m))."""
+    global-implicit assembly (pf_girt_assemble) as its cell kernel computes
+    it: the power table, speciation in product form, totals, the packed
+    symmetric accumulation of sum_i nu nu s, the kinetic minerals and their
+    derivative factors, the diagonal block and `offdiag_blocks` scaled copies
+    of d total/d m, and the residual row.  logK(T) of a temperature-dependent
+    reaction is 4 terms and two corrected quotients per reaction with ln T
+    once per cell, then one exp per reaction; an isothermal network takes K
+    from the block's table (no transcendental per cell)."""
     n, ns, nm = net.ncomp, net.nsec, net.nmnrl
     k_s = [int(c) for c in net.sec_nspec]
     k_m = [int(c) for c in net.mnrl_nspec] if nm else []
-    nn = n * n
+    neg = set()
+    for i, k in enumerate(k_s):
+        neg.update(int(net.sec_spec[i, j]) for j in range(k) if net.sec_stoich[i, j] < 0)
+    for m, k in enumerate(k_m):
+        neg.update(int(net.mnrl_spec[m, j]) for j in range(k) if net.mnrl_stoich[m, j] < 0)
+    nn, nsym = n * n, n * (n + 1) // 2
     f = 0
-    f += sum(2 * k + 2 for k in k_s)        # ln Q, s = exp()/gamma, totals += nu s
-    f += 2 * n                              # den scaling of totals
-    f += sum(2 * k for k in k_s)            # t_p = nu (s / m)
-    f += sum(2 * k * k for k in k_s)        # dtotal entries (FMA)
-    f += nn                                 # den scaling of dtotal
-    f += sum(2 * k + 12 for k in k_m)       # ln QK, affinity, rate, dIm/dQK
-    f += sum(4 * k for k in k_m)            # u_p = nu QK / m den 1e-3
-    f += sum(3 * k * k for k in k_m)        # mineral derivative entries
+    f += 2 * n + 2 * len(neg)               # a = m gamma, a^2; 1/a, 1/a^2
+    f += sum(k + 1 for k in k_s)            # s = K prod a^nu / gamma
+    f += sum(2 * k for k in k_s) + n        # totals += nu s, den scaling
+    f += sum(k * (k + 1) for k in k_s)      # packed sum_i nu_r nu_c s_i (FMA)
+    f += sum(3 * k + 15 for k in k_m)       # QK product, affinity, rate, residual, dIm/dQK QK den
+    f += 2 * nsym + n                       # den (E + delta m)
+    f += 2 * nn + sum(2 * k * k for k in k_m)  # diagonal block: cdiag e + mineral part
+    f += nn * offdiag_blocks                # the scaled copies
     f += n * (3 * 7 + 6)                    # residual row
-    f += nn * 5                             # diagonal block
-    f += nn * (1 + offdiag_blocks)          # E = d m and the scaled copies
-    tr = ns + 2 * n + nm                    # exp per secondary, ln m and ln gamma, exp per mineral
+    temp_dep = not net.options.get("isothermal", 1) and net.sec_logKcoef is not None
+    tr = 1 + ns + nm if temp_dep else 0     # ln T, exp per reaction
+    if temp_dep:
+        f += 12 * (ns + nm)                 # logK(T): 4 terms, two corrected quotients, ln 10 scaling
     return float(f), float(tr)

@@ -76,6 +76,7 @@ class GirtAssembler:
         f64 = dict(dtype=torch.float64, device=device)
         self.residual = torch.zeros(grid.ncells * n, **f64)
         self.values = torch.zeros(len(ci) * n * n, **f64)
+        self._k_cache = None  # per-cell K of the reactions (k_cache="fill" / "read")
         self._q = [torch.as_tensor(np.ascontiguousarray(q), dtype=torch.float64).reshape(-1).to(device)
                    if np.size(q) else torch.zeros(1, **f64) for q in (grid.qx, grid.qy, grid.qz)]
 
@@ -83,7 +84,8 @@ class GirtAssembler:
     def nnzb(self) -> int:
         return len(self.colidx_host)
 
-    def args(self, total_k, dt: float, total_sorb_k=None, numerical_derivatives=False) -> abi.PfGirtArgs:
+    def args(self, total_k, dt: float, total_sorb_k=None, numerical_derivatives=False, k_cache="off",
+             ) -> abi.PfGirtArgs:
         g = self.grid
         a = abi.PfGirtArgs()
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
@@ -98,23 +100,39 @@ class GirtAssembler:
         if total_sorb_k is not None:
             a.total_sorb_k = C.cast(total_sorb_k.data_ptr(), dp)
         a.numerical_derivatives = int(bool(numerical_derivatives))
+        if k_cache not in ("off", "fill", "read"):
+            raise ValueError("k_cache: 'off', 'fill' or 'read'")
+        if k_cache != "off":
+            import torch
+            net = self.engine.net
+            shape = (net.nsec + net.nmnrl, self.grid.ncells)
+            if k_cache == "fill" and (self._k_cache is None or tuple(self._k_cache.shape) != shape):
+                self._k_cache = torch.empty(shape, dtype=torch.float64, device=self.values.device)
+            if self._k_cache is None:
+                raise ValueError("k_cache='read' before a k_cache='fill' assembly")
+            a.k_cache = C.cast(self._k_cache.data_ptr(), dp)
+            a.k_cache_valid = int(k_cache == "read")
         return a
 
     def assemble(self, state: CellState, total_k, dt: float, stream=None, total_sorb_k=None,
-                 numerical_derivatives=False):
+                 numerical_derivatives=False, k_cache="off"):
         """Residual and Jacobian values at the iterate in `state` (CUDA
         tensors); total_k: totals at the start of the step [ncomp][ncells];
         total_sorb_k: the sorbed totals at the start of the step (required
         when the network has sorption); numerical_derivatives: the reaction
         part of the Jacobian by forward differences (the reference's
-        NUMERICAL_JACOBIAN transport option).  Returns (residual, values),
-        views of this assembler's buffers."""
+        NUMERICAL_JACOBIAN transport option); k_cache: "off", or "fill" (the
+        first assembly of a time step: each cell's K of every reaction is
+        computed and kept in this assembler) then "read" (the step's later
+        Newton iterations, temperatures and activity coefficients unchanged:
+        the kept K are used).  Returns (residual, values), views of this
+        assembler's buffers."""
         total_k = total_k.contiguous()
         if self.engine.net.has_sorption and total_sorb_k is None:
             raise ValueError("a network with sorption needs total_sorb_k")
         if total_sorb_k is not None:
             total_sorb_k = total_sorb_k.contiguous()
-        a = self.args(total_k, dt, total_sorb_k, numerical_derivatives)
+        a = self.args(total_k, dt, total_sorb_k, numerical_derivatives, k_cache)
         s = state.struct("device", self.engine.net)
         abi.check("pf_girt_assemble",
                   self.engine.lib.pf_girt_assemble(self.engine.handle, C.byref(s), C.byref(a), _stream_ptr(stream)),

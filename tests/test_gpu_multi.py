@@ -21,6 +21,14 @@ FIELDS = ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mn
           "newton_its", "status", "num_substeps")
 
 
+def same(x, y):
+    """Equal element for element, a NaN equal to a NaN: a cell that failed
+    keeps its last non-converged iterate, and the next step's auxvar update
+    can turn that into NaN in both runs alike (torch.equal calls two NaN
+    different)."""
+    return x.shape == y.shape and bool(((x == y) | (torch.isnan(x) & torch.isnan(y))).all())
+
+
 def _members(oracle, names=None):
     from pfgpu.engine import ReactionEngine
     names = names or ["hetero%d" % n for n in reversed(cases.HETERO)]  # costliest first
@@ -52,7 +60,7 @@ def test_multi_equals_single_launches_and_oracle(oracle):
         ref_dev = st0.to("cuda")
         s1 = one.rstep(ref_dev, 86400.0)
         for k in FIELDS:
-            assert torch.equal(d.a[k], ref_dev.a[k]), (name, k)
+            assert same(d.a[k], ref_dev.a[k]), (name, k)
         assert sm == s1, (name, sm, s1)
         got = d.numpy()
         ref = st0.copy()
@@ -73,7 +81,7 @@ def test_multi_order_of_networks_and_cells_does_not_change_results(oracle):
     rstep_multi([(mem[k][1], b[k]) for k in rev], 86400.0, orders=[orders[k] for k in rev])
     for (name, _, _, _), x, y in zip(mem, a, b):
         for k in FIELDS:
-            assert torch.equal(x.a[k], y.a[k]), (name, k)
+            assert same(x.a[k], y.a[k]), (name, k)
 
 
 def test_multi_time_loop_graph_equals_eager(oracle):
@@ -95,7 +103,7 @@ def test_multi_time_loop_graph_equals_eager(oracle):
     torch.cuda.synchronize()
     for (name, _, _, _), x, y in zip(mem, eager, graphed):
         for k in FIELDS:
-            assert torch.equal(x.a[k], y.a[k]), (name, k)
+            assert same(x.a[k], y.a[k]), (name, k)
 
 
 def test_multi_refuses_networks_without_a_group_kernel(oracle):

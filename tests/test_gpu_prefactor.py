@@ -82,4 +82,10 @@ def test_girt_with_prefactors_matches_oracle(oracle, logf, numjac):
     noise = fd_noise(oracle, net, st, grid, tk, dt, asm.rowptr_host, asm.colidx_host) if numjac else None
     _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, dt,
            noise=noise)
-    np.testing.assert_allclose(dev.numpy().a["mnrl_rate"], ref_st.a["mnrl_rate"], rtol=1e-12, atol=1e-300)
+    # rates relative to their gross size |rate| (1 + Q/K / |1 - Q/K|): next to
+    # equilibrium 1 - Q/K cancels, and the rounding of Q/K (a product of
+    # powers on the device, exp of a sum on the host) is what remains
+    import parity
+    got_rate = dev.numpy().a["mnrl_rate"]
+    err = np.abs(got_rate - ref_st.a["mnrl_rate"]) / np.maximum(parity.gross_rate(net, ref_st), 1e-300)
+    assert np.all(np.where(got_rate == ref_st.a["mnrl_rate"], 0.0, err) < 1e-12), float(err.max())

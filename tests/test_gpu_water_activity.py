@@ -96,6 +96,10 @@ def test_girt_with_water_activity(oracle):
     ref_st = st.copy()
     r_ref, v_ref = oracle.girt_assemble(net, ref_st, grid, tk, 86400.0, asm.rowptr_host, asm.colidx_host)
     _check(net, st, ref_st, dev.numpy(), asm, r.cpu().numpy(), v.cpu().numpy(), r_ref, v_ref, tk, 86400.0)
+    # ln a_H2O follows the molalities: no K cache across Newton iterates
+    with pytest.raises(abi.PfError) as e:
+        asm.assemble(st.to("cuda"), torch.from_numpy(tk).cuda(), 86400.0, k_cache="fill")
+    assert e.value.code == abi.PF_ERR_UNSUPPORTED
 
 
 def test_constraint_with_water_activity(oracle):

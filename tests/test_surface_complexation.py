@@ -111,8 +111,14 @@ def test_gpu_auxvars_with_surface_complexation(oracle, sorb):
     dev = st.to("cuda")
     ReactionEngine(net).update_auxvars(dev, True)
     got = dev.numpy()
-    for k in ("total", "total_sorb", "srfcplx_free_site", "srfcplx_conc", "sec_molal", "pri_act_coef"):
+    for k in ("total", "sec_molal", "pri_act_coef"):
         np.testing.assert_allclose(got.a[k], ref.a[k], rtol=1e-12, atol=0, err_msg=k)
+    # the free-site Newton stops once its relative change is below 1e-12
+    # (reaction_surf_complex.F90:677, :793): the two sides may stop one
+    # iteration apart, so the free site and what is sorbed agree to a few
+    # 1e-12 -- up to the complexes' site stoichiometry times that
+    for k in ("srfcplx_free_site", "srfcplx_conc", "total_sorb"):
+        np.testing.assert_allclose(got.a[k], ref.a[k], rtol=1e-10, atol=0, err_msg=k)
 
 
 @pytest.mark.gpu
