@@ -393,7 +393,11 @@ rstep_batched_kernel(DevNet net, PfCellState st, double dt_uniform, const double
       const bool back = ADJ && phase == BACK;
       if (!back && !redo) its += 1;
       redo = false;
-      const bool ldl = (logf || back || dry) && !use_lu && !newton_iter_act;
+      // LDL^T needs the symmetric log-form Jacobian; the reference's surface
+      // complexation derivative is not symmetric (its free-site term takes
+      // nu_f for nu_f^2 and only the complex's own species), so networks
+      // with surface complexes keep the pivoted LU
+      const bool ldl = (logf || back || dry) && !use_lu && !newton_iter_act && !(net.nsrx > 0 && !back);
       if (newton_iter_act) {
         // RActivityCoefficients LAG (reaction.F90:4553-4612) from this
         // iterate and the previous evaluation's sec_molal

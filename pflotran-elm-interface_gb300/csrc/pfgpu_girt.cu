@@ -334,11 +334,11 @@ __device__ __forceinline__ void st_sector(double* dst, double a, double b, doubl
 // without a K cache, 1 computing the per-cell K of the reactions into kcache,
 // 2 reading them from it.
 template <bool HAS_PF, bool NUMJAC>
-__global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt,
-                                                        const int32_t* __restrict__ rowptr,
-                                                        const int32_t* __restrict__ colidx, double* __restrict__ r,
-                                                        double* __restrict__ values, int vec, int staged,
-                                                        double* __restrict__ kcache, int kmode) {
+__device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const Geo& g,
+                                          double dt, const int32_t* __restrict__ rowptr,
+                                          const int32_t* __restrict__ colidx, double* __restrict__ r,
+                                          double* __restrict__ values, int vec, int staged,
+                                          double* __restrict__ kcache, int kmode) {
   constexpr bool HAS_LNA = HAS_PF || NUMJAC;
   extern __shared__ __align__(16) unsigned char sraw[];
   const int bd = blockDim.x;
@@ -537,7 +537,11 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
         P[a] = (lo == hi ? P[a] + st.pri_molal[soa.at(hi, X)] : P[a]) * den_L;
       }
   } else {
-    for (int j = 0; j < n; ++j) P[(Lo.pa + j) * bd] = 1.0 / st.pri_molal[soa.at(j, X)];
+    for (int j = 0; j < n; ++j) {
+      const double im = 1.0 / st.pri_molal[soa.at(j, X)];
+      P[(Lo.pa + j) * bd] = im;
+      P[(Lo.pa + n + j) * bd] = den_L * im;
+    }
   }
   // ---- block column X
   Conns c;
@@ -560,7 +564,7 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
     const int col = fe / n, row = fe - col * n;
     const double E = P[(Lo.E + sym_index(row, col)) * bd];
     const double im = logf ? 0.0 : P[(Lo.pa + col) * bd];
-    e = logf ? E : den_L * fma(E, im, row == col ? 1.0 : 0.0);
+    e = logf ? E : fma(E, P[(Lo.pa + n + col) * bd], row == col ? den_L : 0.0);
     if (dry) {
       v = fma(csum, e, row == col ? (logf ? st.pri_molal[soa.at(col, X)] : 1.0) : 0.0);
       return;
@@ -641,6 +645,16 @@ __global__ void __launch_bounds__(128) girt_cell_kernel(DevNet net, GirtTabs gt,
         surf_cell(net, st, X));
   }
 }
+
+#define PF_GIRT_CELL_ARGS                                                                                           \
+  DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt, const int32_t* __restrict__ rowptr,                   \
+      const int32_t* __restrict__ colidx, double* __restrict__ r, double* __restrict__ values, int vec, int staged, \
+      double* __restrict__ kcache, int kmode
+template <bool HAS_PF, bool NUMJAC>
+__global__ void __launch_bounds__(128) girt_cell_kernel(PF_GIRT_CELL_ARGS) {
+  girt_cell<HAS_PF, NUMJAC>(net, gt, st, g, dt, rowptr, colidx, r, values, vec, staged, kcache, kmode);
+}
+#undef PF_GIRT_CELL_ARGS
 
 // residual row of cell X: connections (reference order), fixed and current
 // accumulation, then the reaction part the cell kernel left in r
@@ -786,6 +800,8 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   int tpb = 32, staged = 0;
   const size_t smem = girt_smem_bytes(net, gt, with_lna, &tpb, &staged);
   if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
+  const int nn = net.n * net.n;
+  const uintptr_t va = (uintptr_t)a.values;
   auto k = a.numerical_derivatives ? girt::girt_cell_kernel<true, true>
            : pf                    ? girt::girt_cell_kernel<true, false>
                                    : girt::girt_cell_kernel<false, false>;
@@ -793,8 +809,6 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return PF_ERR_CUDA;
   // whole-sector stores when every block starts on a 32-byte boundary
-  const int nn = net.n * net.n;
-  const uintptr_t va = (uintptr_t)a.values;
   const int vec = (nn % 4 == 0 && (va & 31) == 0) ? 4 : ((nn % 2 == 0 && (va & 15) == 0) ? 2 : 1);
   const int kmode = a.k_cache ? (a.k_cache_valid ? 2 : 1) : 0;
   const long long blocks = (st.ncells + tpb - 1) / tpb;

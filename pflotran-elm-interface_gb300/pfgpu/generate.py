@@ -103,7 +103,11 @@ def water_density(t_c: float, p_pa: float = 101325.0) -> float:
 
 
 def random_network(ncomp: int, nsec: int, nmnrl: int, seed: int, temperature_dependent: bool = True,
-                   options=None) -> ReactionNetwork:
+                   options=None, signed: bool = False) -> ReactionNetwork:
+    """signed: the non-H coefficients drawn from {-2, -1, 1, 2} (each row
+    keeps at least one positive one); some TOTAL constraints of such a
+    network have no solution, and the cells whose equilibration fails are
+    dropped by the callers (resampled from a larger draw)."""
     rng = np.random.default_rng(seed)
     primary = ["H+"] + ["P%d" % k for k in range(1, ncomp)]
     pri_Z = np.concatenate([[1.0], rng.integers(-2, 3, ncomp - 1).astype(float)])
@@ -113,9 +117,9 @@ def random_network(ncomp: int, nsec: int, nmnrl: int, seed: int, temperature_dep
     def rxn_row():
         while True:
             mask = rng.random(ncomp) < 0.3
-            nu = rng.choice([1.0, 2.0], ncomp) * mask
+            nu = rng.choice([-2.0, -1.0, 1.0, 2.0] if signed else [1.0, 2.0], ncomp) * mask
             nu[0] = rng.choice([-2.0, -1.0, 1.0, 2.0]) * mask[0]
-            if not nu[1:].any():
+            if not (nu[1:] > 0).any():
                 continue
             z = float(nu @ pri_Z)
             if abs(z) <= 2.0:
@@ -151,11 +155,13 @@ def random_network(ncomp: int, nsec: int, nmnrl: int, seed: int, temperature_dep
     return ReactionNetwork.build(primary, pri_Z, pri_a0, secs, mins, options=opts)
 
 
-def random_cells(net: ReactionNetwork, ncells: int, seed: int, dt_range=None):
+def random_cells(net: ReactionNetwork, ncells: int, seed: int, dt_range=None, free: bool = False):
     """Cells for a random network.  Returns (state, ctype, cconc); the
     constraint is TOTAL for every component but H+, which carries the charge
     balance (initial guess 1e-7).  dt_range=(lo, hi) adds a per-cell dt drawn
-    log-uniformly."""
+    log-uniformly.  free: FREE constraints instead (free molalities log10
+    U[-8, -4], H+ 10^-U[5, 9]), for networks with signed stoichiometry whose
+    TOTAL constraints mostly have no solution."""
     rng = np.random.default_rng(seed)
     st = CellState.empty(net, ncells, with_dt=dt_range is not None)
     n = net.ncomp
@@ -165,6 +171,12 @@ def random_cells(net: ReactionNetwork, ncells: int, seed: int, dt_range=None):
     cconc[h] = 1.0e-7
     ctype = [abi.PF_CONSTRAINT_TOTAL] * n
     ctype[h] = abi.PF_CONSTRAINT_CHARGE_BAL
+    if free:
+        # free-ion constraints: any molalities are an equilibrium state,
+        # whatever the signs of the stoichiometry
+        cconc = 10.0 ** rng.uniform(-8.0, -4.0, (n, ncells))
+        cconc[h] = 10.0 ** -rng.uniform(5.0, 9.0, ncells)
+        ctype = [abi.PF_CONSTRAINT_FREE] * n
     if net.nmnrl:
         st.a["mnrl_volfrac"][:] = rng.uniform(0.0, 0.1, (net.nmnrl, ncells))
         st.a["mnrl_area"][:] = rng.uniform(1.0, 100.0, (net.nmnrl, ncells))

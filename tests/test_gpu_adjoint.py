@@ -32,8 +32,8 @@ DT = None    # set per case by the fixture
 CASE = None
 
 
-def _setup(oracle, name, lanes=1, ncells=240):
-    net, st0 = cases.case(oracle, name, tight=True)
+def _setup(oracle, name, lanes=1, ncells=240, tight=True):
+    net, st0 = cases.case(oracle, name, tight=tight)
     st0 = st0.subset(np.arange(ncells))
     from pfgpu.engine import ReactionEngine
     eng = ReactionEngine(net)
@@ -149,7 +149,7 @@ def test_adjoint_status_and_loss(adjoint_case):
     assert g["loss"][0] == pytest.approx(base.sum(), rel=1e-12)
 
 
-def _check_global(net, st0, eng, w, tgt, g, lossfn):
+def _check_global(net, st0, eng, w, tgt, g, lossfn, rel=1e-4):
     fd, stable = _fd_global(lossfn, net.nsec, net.nmnrl)
     ok = stable & (g["adj_status"] == 0)
     assert ok.mean() > 0.9, ok.mean()
@@ -164,7 +164,7 @@ def _check_global(net, st0, eng, w, tgt, g, lossfn):
         ref = v[:, ok].sum(axis=1)
         got = gs[k].cpu().numpy()
         err = np.abs(got - ref)
-        assert np.all(err <= 1e-4 * np.abs(ref).max() + floor), (k, got, ref, floor)
+        assert np.all(err <= rel * np.abs(ref).max() + floor), (k, got, ref, floor)
         resolved[k] = int((np.abs(ref) > 30 * floor).sum())
     # the calcite case resolves every parameter group
     if CASE == "calcite":
@@ -275,3 +275,47 @@ def test_group_adjoint_matches_one_lane(oracle, lanes):
         a, b = g1[k][:, same], g2[k][:, same]
         assert np.max(np.abs(a - b)) <= 1e-8 * max(np.max(np.abs(a)), 1e-300), k
     assert g2["loss"][0] == pytest.approx(g1["loss"][0], rel=1e-9)
+
+
+@pytest.mark.parametrize("lanes", [1, 4], ids=["lane", "group4"])
+def test_adjoint_default_tolerances_vs_fd(oracle, lanes):
+    """The adjoint at the solver's default tolerances, the ones the
+    differentiation bench runs at (relative change 1e-6, residual 1e-12 and
+    relative residual 1e-8, 20 iterations), on the 12-component network at
+    dt = 1 day.  It differentiates the iterate where RReact stopped, which is
+    within about the last Newton update (1e-6 relative in the molalities) of
+    the root; the quantity it stands for is the gradient of the converged
+    step.  So the reference here is central differences of the converged
+    forward map (the same network and cells at the tight tolerances), and the
+    bar is 1e-3 of the largest gradient of a group on the gradients summed
+    over cells (logK of every complex and mineral, ln rate constants) and on
+    the per-cell area gradients.  (Differences of the default-tolerance map
+    itself measure where the stopping tests fire: a complex's logK moves the
+    stopping point, and with it the totals by up to the stopped update, while
+    the converged totals do not depend on it.)"""
+    global DT, CASE
+    DT, CASE = DTS["random12"], "random12"
+    net, st0, eng, w, tgt = _setup(oracle, "random12", lanes, tight=False)
+    net_t, st_t = cases.case(oracle, "random12", tight=True)
+    st_t = st_t.subset(np.arange(st0.ncells))
+    assert np.array_equal(st_t.a["total"], st0.a["total"])
+    from pfgpu.engine import ReactionEngine
+    eng_t = ReactionEngine(net_t)
+    dev = st0.to("cuda")
+    g = eng.adjoint(dev, DT, weight=torch.from_numpy(w).cuda(), target=torch.from_numpy(tgt).cuda())
+    g = {k: v.cpu().numpy() for k, v in g.items()}
+    lossfn = lambda **kw: _gpu_loss(eng_t, st0, w, tgt, **kw)  # noqa: E731
+    _check_global(net, st0, eng, w, tgt, g, lossfn, rel=1e-3)
+    ok = g["adj_status"] == 0
+    base_l, base_its = lossfn()
+    for m in range(net.nmnrl):
+        sp = np.ones_like(st0.a["mnrl_area"])
+        sp[m] = np.exp(H)
+        sm = np.ones_like(st0.a["mnrl_area"])
+        sm[m] = np.exp(-H)
+        lp, ip = lossfn(area_scale=sp)
+        lm, im = lossfn(area_scale=sm)
+        fd = (lp - lm) / (2 * H)
+        mask = ok & (ip == base_its) & (im == base_its)
+        sc = max(np.abs(fd[mask]).max(), 1e-300)
+        assert np.max(np.abs(g["dL_dlnarea"][m, mask] - fd[mask])) / sc < 1e-3, m
