@@ -63,7 +63,6 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
       net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON)
     return false;
   if (net.ns > PF_MAX_NSEC || net.nm > PF_MAX_NMNRL) return false;
-  if (has_sorption(net)) return false;  // sorption: one lane per cell
   if (net.flags & NETF_PREFACTOR) return false;  // rate prefactors: the plain kernel
   if (net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER && net.o.use_activity_h2o)
     return false;  // water activity moving each Newton iteration: the plain kernel

@@ -4,6 +4,7 @@
 #pragma once
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
 namespace group {
@@ -106,6 +107,30 @@ __device__ __forceinline__ bool stage_tables(const DevNet& net, unsigned char* s
   return true;
 }
 
+// Equilibrium sorption of one cell inside a group's evaluation (RTotalSorb
+// in RTAuxVarCompute with RAccumulationSorb[Derivative], reaction.F90:
+// 3861-3865, 3904-3909), run by one lane of the group: the sorbed totals to
+// the state and, times V/dt, to the residual rhs[] and the full rows of the
+// log-form Jacobian J (column j scaled by m_j).  m[], gam[]: molalities and
+// activity coefficients by species; vf[]: mineral volume fractions.  Out of
+// line so that networks without sorption keep the kernel's registers.
+// Returns false when the ion-exchange Newton fails (the reference's ierror).
+__device__ __forceinline__ bool group_sorb(const DevNet& net, const Tables& T, const PfCellState& st, long long cell,
+                                        const double* m, const double* gam, const double* vf, double den_k,
+                                        double v_t, double* J, double* rhs) {
+  const SoA soa{st.ncells};
+  const int n = net.n;
+  for (int j = 0; j < n; ++j) st.total_sorb[soa.at(j, cell)] = 0.0;
+  return total_sorb(
+      net, T, [&](int j) { return m[j]; }, [&](int j) { return gam[j]; }, [&](int k) { return vf[k]; },
+      st.porosity[cell], den_k, st.ionx_ref_sorbed ? st.ionx_ref_sorbed + cell : nullptr, st.ncells,
+      [&](int j, double v) {
+        st.total_sorb[soa.at(j, cell)] += v;
+        rhs[j] = fma(v_t, v, rhs[j]);
+      },
+      [&](int i, int j, double v) { J[i * n + j] = fma(v_t * v, m[j], J[i * n + j]); }, surf_cell(net, st, cell));
+}
+
 // The step for the cells of one network's work queue, by the block's warps,
 // with the network's tables already staged at the start of smem.  A warp
 // returns when the queue is empty and its cells are done.
@@ -153,6 +178,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
   const PfOptions o = net.o;
   const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
   const bool newton_iter_act = o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER;
+  const bool has_sorb = !ADJ && has_sorption(net);  // the adjoint refuses sorption
   const unsigned neg_mask = (unsigned)net.neg_mask;
   const int64_t ncells = st.ncells;
   const double* sc_sec = scratch;
@@ -271,6 +297,10 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
         init_tot[t] = tot[t];
         c[t] = guess[t];
         lnc[t] = lnguess[t];
+        // RAccumulationSorb into the fixed accumulation (reaction.F90:
+        // 3836-3839): the sorbed total of the last evaluation
+        const int i = r + G * t;
+        if (has_sorb && i < n) fixed[t] = fma(st.total_sorb[soa.at(i, cell)], volume, fixed[t]);
       }
       its = 0;
       r0 = 0.0;
@@ -284,7 +314,10 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
       const bool back = ADJ && phase == BACK;
       if (!back && !redo) its += 1;
       redo = false;
-      const bool ldl = !use_lu && !newton_iter_act;
+      // LDL^T needs the symmetric log-form Jacobian: the sorption derivative
+      // (the reference's surface complexation term is not symmetric) goes
+      // into the full rows of the pivoted LU
+      const bool ldl = !use_lu && !newton_iter_act && !has_sorb;
       if (newton_iter_act) {
         // RActivityCoefficients LAG from this iterate and the previous
         // evaluation's sec_molal (reaction.F90:4553-4612)
@@ -316,6 +349,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           pw[i] = a;
           pw[n + i] = a * a;
           xs[i] = c[t];  // molality by species for the entry assembly (xs is free until the solve)
+          if (has_sorb) vvs[i] = g[t];  // activity coefficient by species (vvs is free until the solve)
           if (neg_mask & (1u << i)) {
             const double ia = 1.0 / a;
             pw[2 * n + i] = ia;
@@ -469,6 +503,26 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           J[f] = v;
         }
       }
+      // ---- equilibrium sorption: one lane of the group, into the full rows
+      // and the residual; the residual norms are taken again
+      bool sorb_fail = false;
+      if (has_sorb && !back) {
+        __syncwarp(gmask);
+        int bad = 0;
+        if (r == 0) bad = !group_sorb(net, T, st, cell, xs, vvs, vfm, den_k, volume * inv_dt, J, rhsv);
+        sorb_fail = __shfl_sync(gmask, bad, gi * G) != 0;
+        __syncwarp(gmask);
+        dot_p = 0.0;
+        mx_p = 0;
+#pragma unroll
+        for (int t = 0; t < R; ++t) {
+          const int i = r + G * t;
+          if (i >= n) continue;
+          const double rr = rhsv[i];
+          dot_p = fma(rr, rr, dot_p);
+          mx_p = max(mx_p, absbits(rr));
+        }
+      }
       // ---- convergence tests on the residual (reaction.F90:3946-3953)
       const double two_norm = sqrt(gsum<G>(dot_p, gmask));
       const unsigned long long mxb = gmax<G>(mx_p, gmask);
@@ -476,6 +530,8 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
       int react_end = -1;
       if (back) {
         // falls through to the factorisation below
+      } else if (sorb_fail) {
+        react_end = 1;  // RTAuxVarCompute's ierror: no total restore (reaction.F90:3861-3865)
       } else if (its > o.maximum_reaction_iterations) {
 #pragma unroll
         for (int t = 0; t < R; ++t) tot[t] = init_tot[t];
@@ -877,7 +933,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
 }
 
 template <int G, int R, bool ADJ>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 1)
 rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
                    unsigned long long* queue, unsigned long long* counters, PfAdjointArgs adj,
                    double* __restrict__ adj_store) {

@@ -48,7 +48,7 @@ __device__ __forceinline__ void run(const Net& m, double dt, unsigned char* smem
                                    nullptr, smem, m.threads);
 }
 
-__global__ void __launch_bounds__(256) rstep_multi_kernel(const __grid_constant__ Args args) {
+__global__ void __launch_bounds__(256, 1) rstep_multi_kernel(const __grid_constant__ Args args) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) uint64_t tma_bar;
   for (int k = 0; k < args.nnets; ++k) {

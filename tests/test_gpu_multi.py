@@ -107,10 +107,28 @@ def test_multi_time_loop_graph_equals_eager(oracle):
 
 
 def test_multi_refuses_networks_without_a_group_kernel(oracle):
+    """The linear formulation has no group kernel (its Jacobian is not the
+    symmetric log-form one the group kernel assembles)."""
     from pfgpu.engine import ReactionEngine, rstep_multi
-    net, st, grid, total_k, sorb_k = cases.girt_sorption_case(oracle, "ionx+langmuir", 4, 3, 2)
-    eng = ReactionEngine(net)
-    (_, e2, _, s2), = _members(oracle, ["hetero8"])
+    (_, e2, net, s2), = _members(oracle, ["hetero8"])
+    eng = ReactionEngine(net.with_options(use_log_formulation=0))
     with pytest.raises(abi.PfError) as e:
-        rstep_multi([(e2, s2.to("cuda")), (eng, st.to("cuda"))], 3600.0)
+        rstep_multi([(e2, s2.to("cuda")), (eng, s2.to("cuda"))], 3600.0)
     assert e.value.code == abi.PF_ERR_UNSUPPORTED
+
+
+def test_multi_with_sorption_equals_single_launch(oracle):
+    """A network with equilibrium sorption (ion exchange and a Langmuir K_D)
+    among others in one launch: bit for bit its own group launch."""
+    from pfgpu.engine import ReactionEngine, rstep_multi
+    net, st, grid, total_k, sorb_k = cases.girt_sorption_case(oracle, "ionx+langmuir", 8, 6, 5)
+    eng = ReactionEngine(net)
+    (_, e2, _, s2), = _members(oracle, ["hetero12"])
+    a, b = st.to("cuda"), s2.to("cuda")
+    rstep_multi([(e2, b), (eng, a)], 86400.0)
+    one = ReactionEngine(net)
+    assert one.set_launch_config(128, 2, 0, _lanes(eng)) == abi.PF_OK
+    ref = st.to("cuda")
+    one.rstep(ref, 86400.0)
+    for k in FIELDS + ("total_sorb", "ionx_ref_sorbed"):
+        assert same(a.a[k], ref.a[k]), k

@@ -65,7 +65,7 @@ def test_auxvars_with_sorption_match_oracle(oracle, sorb):
         np.testing.assert_allclose(got.a[k], ref.a[k], rtol=1e-12, atol=0, err_msg=k)
 
 
-@pytest.mark.parametrize("kernel", ["batched", "plain"])
+@pytest.mark.parametrize("kernel", ["batched", "group2", "group4", "plain"])
 @pytest.mark.parametrize("sorb", ["ionx+langmuir", "mineral-scaled"])
 def test_rstep_with_sorption_matches_oracle(oracle, sorb, kernel):
     from pfgpu.engine import ReactionEngine
@@ -74,8 +74,12 @@ def test_rstep_with_sorption_matches_oracle(oracle, sorb, kernel):
     ref = st.copy()
     oracle.rstep(net, ref, 86400.0, nthreads=8)
     eng = ReactionEngine(net)
+    if kernel.startswith("group"):
+        # a group of lanes per cell: one lane runs the sorption routine into
+        # the rows of the pivoted LU
+        assert eng.set_launch_config(128, 2, 0, int(kernel[5:])) == abi.PF_OK
     dev = st.to("cuda")
-    eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_BATCHED if kernel == "batched" else abi.PF_KERNEL_PLAIN)
+    eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED)
     got = dev.numpy()
     ok = (got.a["newton_its"] == ref.a["newton_its"]) & (ref.a["status"] == 0) & (got.a["status"] == 0)
     assert ok.mean() > 0.9, (ok.mean(), (ref.a["status"] != 0).sum())
@@ -150,14 +154,18 @@ def test_five_components_run_on_the_plain_kernel(oracle):
         assert np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)) < 1e-10, k
 
 
-def test_entry_points_without_sorption_refuse_it(oracle):
+def test_sorption_launches_and_refusals(oracle):
     from pfgpu.engine import ReactionEngine
     net = _net(SORB)
     st = _cells(oracle, net, 16, 5)
     eng = ReactionEngine(net)
     dev = st.to("cuda")
-    assert eng.set_launch_config(128, 1, 0, 4) == abi.PF_ERR_UNSUPPORTED
+    assert eng.set_launch_config(128, 1, 0, 4) == abi.PF_OK  # the group kernel carries sorption
     assert eng.set_launch_config(128, 1, 1, 1) == abi.PF_OK
+    # the adjoint has no sorption terms
+    with pytest.raises(abi.PfError) as e:
+        eng.adjoint(dev, 3600.0, dL_dtotal=torch.ones_like(dev.a["total"]))
+    assert e.value.code == abi.PF_ERR_UNSUPPORTED
     # a state without the sorption arrays is an invalid argument
     bare = CellState(net, {k: v for k, v in dev.a.items() if k not in ("total_sorb", "ionx_ref_sorbed")})
     with pytest.raises(abi.PfError):

@@ -122,7 +122,7 @@ def test_gpu_auxvars_with_surface_complexation(oracle, sorb):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernel", ["batched", "plain"])
+@pytest.mark.parametrize("kernel", ["batched", "group4", "plain"])
 @pytest.mark.parametrize("sorb", ["surface", "surface+ionx+kd"])
 def test_gpu_rstep_with_surface_complexation(oracle, sorb, kernel):
     pytest.importorskip("torch")
@@ -140,8 +140,10 @@ def test_gpu_rstep_with_surface_complexation(oracle, sorb, kernel):
         oracle.rstep(net, p, 86400.0, nthreads=8)
         perts.append(p)
     eng = ReactionEngine(net)
+    if kernel.startswith("group"):
+        assert eng.set_launch_config(128, 2, 0, int(kernel[5:])) == abi.PF_OK
     dev = st.to("cuda")
-    eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_BATCHED if kernel == "batched" else abi.PF_KERNEL_PLAIN)
+    eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED)
     got = dev.numpy()
     label = "surface/%s/%s" % (sorb, kernel)
     entry, ok = parity.compare(net, ref, got, 86400.0, label, perts)
