@@ -139,7 +139,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
                                            double dt_uniform, const double* __restrict__ scratch,
                                            unsigned long long* queue, unsigned long long* counters,
                                            const PfAdjointArgs& adj, double* __restrict__ adj_store,
-                                           unsigned char* smem, int threads) {
+                                           unsigned char* smem, int threads, int adj_pass = 0) {
   const int tid = threadIdx.x;
   const int lane_id = tid & 31;
   const uint32_t ibytes = (uint32_t)(net.ent_staged ? net.int_words_grp : net.int_words_core) * 4u;
@@ -278,6 +278,43 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           num_cuts = 0;
           n_const = 0;
           zero_step = !(cum < target);
+          if constexpr (ADJ) {
+            if (adj_pass == 2) {
+              // backward pass of a two-pass adjoint: the forward pass left the
+              // cell's dL/dT(final) in dL_dtotal0 and, in adj_status, its
+              // substep count and floored species (bit 30 set), or the final
+              // status of a cell without a backward pass
+              zero_step = false;
+              const int seed = adj.adj_status[cell];
+              if (!(seed & (1 << 30))) {
+                phase = NEED;
+              } else {
+                const unsigned fmask = (unsigned)seed & 0xffffffu;
+                nsub = (seed >> 24) & 31;
+                small_mask = 0;
+#pragma unroll
+                for (int t = 0; t < R; ++t) {
+                  const int i = r + G * t;
+                  if (i >= n) continue;
+                  const double gj = adj.dL_dtotal0[soa.at(i, cell)];
+                  const bool fl = (fmask >> i) & 1u;
+                  if (fl) small_mask |= 1u << t;
+                  gdir[t] = fl ? gj : 0.0;
+                  Tbar[t] = fl ? 0.0 : gj;
+                  tb[i] = Tbar[t];
+                }
+                for (int m = r; m < nm; m += G) garea[m] = 0.0;
+                sb = nsub - 1;
+#pragma unroll
+                for (int t = 0; t < R; ++t) {
+                  const int i = r + G * t;
+                  if (i < n) c[t] = adj_store[((size_t)sb * (n + 1) + i) * ncells + cell];
+                }
+                inv_dt = 1.0 / adj_store[((size_t)sb * (n + 1) + n) * ncells + cell];
+                phase = BACK;
+              }
+            }
+          }
         }
       }
     }
@@ -770,7 +807,8 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
             const double v = vfm[m] + ratem[m] * T.molar_vol(m) * dt;
             vfm[m] = v < 0.0 ? 0.0 : v;
           }
-          if constexpr (ADJ) {
+          if (ADJ || adj_pass == 1) {
+            // the adjoint's substep store: the converged iterate and dt
             if (nsub < PF_ADJ_MAX_SUBSTEPS) {
 #pragma unroll
               for (int t = 0; t < R; ++t) {
@@ -845,8 +883,9 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
         my_maxsub = max(my_maxsub, (unsigned long long)nsub);
       }
       phase = NEED;
-      if constexpr (ADJ) {
-        // loss contribution and dL/dT(final); start the backward pass
+      if (ADJ || adj_pass == 1) {
+        // loss contribution and dL/dT(final); start the backward pass (or,
+        // in the forward pass of a two-pass adjoint, leave its seed)
 #pragma unroll
         for (int t = 0; t < R; ++t) {
           const int i = r + G * t;
@@ -865,9 +904,10 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           const bool fl = small_mask & (1u << t);
           gdir[t] = fl ? gj : 0.0;
           Tbar[t] = fl ? 0.0 : gj;
-          tb[i] = Tbar[t];
+          if constexpr (ADJ) tb[i] = Tbar[t];  // (the forward kernel's workspace has no tb)
         }
-        for (int m = r; m < nm; m += G) garea[m] = 0.0;
+        if constexpr (ADJ)
+          for (int m = r; m < nm; m += G) garea[m] = 0.0;
         const int astat = cell_failed ? 1 : (nsub > PF_ADJ_MAX_SUBSTEPS ? 2 : 0);
         if (astat != 0 || dry || nsub == 0) {
 #pragma unroll
@@ -877,7 +917,21 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           }
           for (int m = r; m < nm; m += G) adj.dL_dlnarea[soa.at(m, cell)] = 0.0;
           if (r == 0 && adj.adj_status) adj.adj_status[cell] = astat;
-        } else {
+        } else if (adj_pass == 1) {
+          // forward pass of a two-pass adjoint: dL/dT(final) and the seed of
+          // the backward pass (substeps, floored species of the group)
+          unsigned fm = 0;
+#pragma unroll
+          for (int t = 0; t < R; ++t) {
+            const int i = r + G * t;
+            if (i >= n) continue;
+            adj.dL_dtotal0[soa.at(i, cell)] = gdir[t] + Tbar[t];  // one of the two is zero
+            if (small_mask & (1u << t)) fm |= 1u << i;
+          }
+#pragma unroll
+          for (int off = 1; off < G; off <<= 1) fm |= __shfl_xor_sync(gmask, fm, off);
+          if (r == 0) adj.adj_status[cell] = (1 << 30) | (nsub << 24) | (int)fm;
+        } else if constexpr (ADJ) {
           sb = nsub - 1;
 #pragma unroll
           for (int t = 0; t < R; ++t) {
@@ -915,6 +969,10 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
     double l = loss_acc;
     for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(FULL, l, off);
     if (lane_id == 0 && adj.loss && l != 0.0) atomicAdd(adj.loss, l);
+  } else if (adj_pass == 1) {
+    double l = loss_acc;
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(FULL, l, off);
+    if (lane_id == 0 && adj.loss && l != 0.0) atomicAdd(adj.loss, l);
   }
   if (counters) {
     for (int off = 16; off > 0; off >>= 1) {
@@ -936,13 +994,21 @@ template <int G, int R, bool ADJ>
 __global__ void __launch_bounds__(256, 1)
 rstep_group_kernel(DevNet net, GroupTabs gt, PfCellState st, double dt_uniform, const double* __restrict__ scratch,
                    unsigned long long* queue, unsigned long long* counters, PfAdjointArgs adj,
-                   double* __restrict__ adj_store) {
+                   double* __restrict__ adj_store, int adj_pass) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ __align__(8) uint64_t tma_bar;
   if (!stage_tables(net, smem, &tma_bar, 0u, true, counters)) return;
-  group_body<G, R, ADJ>(net, gt, st, dt_uniform, scratch, queue, counters, adj, adj_store, smem, (int)blockDim.x);
+  group_body<G, R, ADJ>(net, gt, st, dt_uniform, scratch, queue, counters, adj, adj_store, smem, (int)blockDim.x,
+                        adj_pass);
 }
 
+// The adjoint runs in two passes when it has a status array to carry the
+// seeds: every cell's forward solve first, by the forward kernel with the
+// substep store, the loss and the seeds switched on (adj_pass 1), then every
+// cell's backward pass by the adjoint kernel (adj_pass 2, the queue
+// restarted).  The forward Newton trips in the adjoint instantiation ran at
+// 13 of 32 lanes per instruction against 22 in the forward kernel (ncu), in
+// one pass or two; its backward trips alone run at 24.
 template <int G, int R>
 int launch_k(const DevNet& net, const GroupTabs& gt, const PfCellState& st, double dt, size_t smem, int grid,
              int tpb, const double* scratch, unsigned long long* queue, unsigned long long* counters,
@@ -951,12 +1017,22 @@ int launch_k(const DevNet& net, const GroupTabs& gt, const PfCellState& st, doub
     auto k = rstep_group_kernel<G, R, true>;
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
-    k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, *adj, adj_store);
+    if (!adj->adj_status) {
+      k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, *adj, adj_store, 0);
+    } else {
+      auto kf = rstep_group_kernel<G, R, false>;
+      err = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (err != cudaSuccess) return (int)err;
+      kf<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, *adj, adj_store, 1);
+      err = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), stream);
+      if (err != cudaSuccess) return (int)err;
+      k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, *adj, adj_store, 2);
+    }
   } else {
     auto k = rstep_group_kernel<G, R, false>;
     cudaError_t err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return (int)err;
-    k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, PfAdjointArgs{}, nullptr);
+    k<<<grid, tpb, smem, stream>>>(net, gt, st, dt, scratch, queue, counters, PfAdjointArgs{}, nullptr, 0);
   }
   return (int)cudaGetLastError();
 }
