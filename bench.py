@@ -179,22 +179,36 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def fp64_peak(lib, device_sms):
-    """Measured FP64 FMA throughput (TFLOP/s) with the library's probe."""
+def fp64_peak(lib, device_sms, clocks=None):
+    """Measured FP64 FMA throughput (TFLOP/s) with the library's probe.
+    clocks: a dict that receives the SM clock nvidia-smi saw while the probe
+    ran (a second of back-to-back launches), which the probe's fraction of
+    the DFMA issue rate is read against."""
     import ctypes as C
 
     import torch
     blocks, threads, iters = device_sms * 8, 256, 5000
     out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
     s = torch.cuda.current_stream()
+
+    def launch():
+        lib.pf_bench_fp64_fma(C.c_void_p(out.data_ptr()), iters, blocks, threads, C.c_void_p(s.cuda_stream))
     best = 0.0
     for _ in range(4):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        lib.pf_bench_fp64_fma(C.c_void_p(out.data_ptr()), iters, blocks, threads, C.c_void_p(s.cuda_stream))
+        launch()
         e1.record()
         torch.cuda.synchronize()
         best = max(best, blocks * threads * iters * 16.0 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    if clocks is not None:
+        with Clocks(torch.cuda.current_device()) as clk:
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 1.2:
+                for _ in range(8):
+                    launch()
+                torch.cuda.synchronize()
+        clocks.update(clk.summary() or {})
     return best
 
 
@@ -946,7 +960,8 @@ def main():
     k_it, _ = flops.kernel_per_iteration(net)
     flops_per_launch = f_it * its_mean * ncells
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    peak = fp64_peak(abi.load(), sms)
+    probe_clocks = {}
+    peak = fp64_peak(abi.load(), sms, probe_clocks)
     achieved = flops_per_launch / (kern_avg * 1e-3) / 1e12
     achieved_own = k_it * its_mean * ncells / (kern_avg * 1e-3) / 1e12
     clocks = clk.summary()
@@ -969,7 +984,12 @@ def main():
                                   "frac": achieved_own / peak if peak else None},
                 "dfma_issue_peak": {"tflops": dfma_peak, "sm_mhz": sm_mhz,
                                     "frac": achieved / dfma_peak, "frac_own_algorithm": achieved_own / dfma_peak,
-                                    "probe_frac": peak / dfma_peak},
+                                    "probe_frac": peak / dfma_peak,
+                                    # the probe against the issue rate at the clock it ran at
+                                    "probe_clocks": probe_clocks or None,
+                                    "probe_frac_at_its_clock": (
+                                        peak / (2 * 2 * sms * probe_clocks["sm_mhz"] * 1e6 / 1e12)
+                                        if probe_clocks.get("sm_mhz") else None)},
                 "hbm_gbs": state_bytes * 2 / (kern_avg * 1e-3) / 1e9}
 
     e2e = None
