@@ -191,17 +191,25 @@ def fp64_peak(lib, device_sms, clocks=None):
     out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
     s = torch.cuda.current_stream()
 
-    def launch():
-        lib.pf_bench_fp64_fma(C.c_void_p(out.data_ptr()), iters, blocks, threads, C.c_void_p(s.cuda_stream))
-    best = 0.0
-    for _ in range(4):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        launch()
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, blocks * threads * iters * 16.0 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    def launch(b=blocks, t=threads):
+        lib.pf_bench_fp64_fma(C.c_void_p(out.data_ptr()), iters, b, t, C.c_void_p(s.cuda_stream))
+
+    def rate(b, t):
+        r = 0.0
+        for _ in range(4):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            launch(b, t)
+            e1.record()
+            torch.cuda.synchronize()
+            r = max(r, b * t * iters * 16.0 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+        return r
+    best = rate(blocks, threads)
     if clocks is not None:
+        # the same rate at a quarter and a sixteenth of the warps per SM: the
+        # probe is not short of independent work
+        clocks["shapes"] = {"64 warps/SM": best, "16 warps/SM": rate(device_sms * 2, threads),
+                            "4 warps/SM": rate(device_sms, 128)}
         with Clocks(torch.cuda.current_device()) as clk:
             t0 = time.perf_counter()
             while time.perf_counter() - t0 < 1.2:

@@ -315,22 +315,36 @@ int32_t pf_network_create(const PfNetworkDesc* d, PfNetwork** out) {
           em[i * (i + 1) / 2 + j].push_back(
               {m, d->mnrl_stoich[m * d->mnrl_stride + a] * d->mnrl_stoich[m * d->mnrl_stride + b]});
         }
+    // the group kernel deals the entries round-robin to the lanes of a
+    // group: listed longest first, the lanes of one round sum lists of about
+    // the same length (a diagonal entry collects every complex of its
+    // species, an off-diagonal one a few), so fewer lanes wait in each round;
+    // every entry is summed the same way in any order
+    const int ne = n * (n + 1) / 2;
+    std::vector<int> eord(ne), eflat(ne);
+    for (int i = 0, e = 0; i < n; ++i)
+      for (int j = 0; j <= i; ++j, ++e) {
+        eord[e] = e;
+        eflat[e] = i * n + j;
+      }
+    std::stable_sort(eord.begin(), eord.end(), [&](int a, int b) {
+      return es[a].size() + em[a].size() > es[b].size() + em[b].size();
+    });
     // into ent_ints (offsets relative to it, fixed up where it is appended)
     dev.o_ent_ij = (int)ent_ints.size();
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j <= i; ++j) ent_ints.push_back(i * n + j);
+    for (int e : eord) ent_ints.push_back(eflat[e]);
     dev.o_ent_ptr = (int)ent_ints.size();
-    for (auto& v : es) {
+    for (int e : eord) {
       ent_ints.push_back((int32_t)ent_sc.size());
-      for (auto& pr : v) { ent_sc.push_back(pr.first); ent_cf.push_back(pr.second); }
+      for (auto& pr : es[e]) { ent_sc.push_back(pr.first); ent_cf.push_back(pr.second); }
     }
     ent_ints.push_back((int32_t)ent_sc.size());
     dev.o_ent_sc = (int)ent_ints.size();
     ent_ints.insert(ent_ints.end(), ent_sc.begin(), ent_sc.end());
     dev.o_ent_mptr = (int)ent_ints.size();
-    for (auto& v : em) {
+    for (int e : eord) {
       ent_ints.push_back((int32_t)ent_mm.size());
-      for (auto& pr : v) { ent_mm.push_back(pr.first); ent_mcf.push_back(pr.second); }
+      for (auto& pr : em[e]) { ent_mm.push_back(pr.first); ent_mcf.push_back(pr.second); }
     }
     ent_ints.push_back((int32_t)ent_mm.size());
     dev.o_ent_mm = (int)ent_ints.size();

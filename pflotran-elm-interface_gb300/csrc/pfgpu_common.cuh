@@ -48,6 +48,9 @@ struct GroupTabs {
   const int32_t* mp_p;
   const double* sp_nu;  // nu of species i in complex sp_s[q] / mineral mp_m[q]
   const double* mp_nu;
+  // the complexes in the order a group's lanes take them in the evaluation,
+  // longest species list first (the lanes of one round loop alike)
+  const int32_t* s_perm;
 };
 
 struct DevNet {

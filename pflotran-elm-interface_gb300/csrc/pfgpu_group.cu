@@ -36,6 +36,7 @@
 // and accumulating theta_bar += (dT/dtheta)^T u - (dR/dtheta)^T lambda.
 // Gradients of the network parameters collect per lane over its own
 // complexes and minerals and are reduced over the warp at the end.
+#include <algorithm>
 #include <vector>
 
 #include "pfgpu_group.cuh"
@@ -138,6 +139,15 @@ int group_build_tables(const DevNet& net, const int32_t* I, const double* D, voi
   int o1, o2, o3, o4, o5, o6;
   csr(ss, sp, &o1, &o2, &o3);
   csr(mm, mp, &o4, &o5, &o6);
+  const int o7 = (int)ints.size();
+  {
+    std::vector<int> perm(net.ns);
+    for (int k = 0; k < net.ns; ++k) perm[k] = k;
+    auto len = [&](int k) { return I[net.o_sec_ptr + k + 1] - I[net.o_sec_ptr + k]; };
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return len(a) > len(b); });
+    ints.insert(ints.end(), perm.begin(), perm.end());
+    if (net.ns == 0) ints.push_back(0);
+  }
   // the stoichiometric coefficients along the same lists, after the ints
   std::vector<double> nus;
   for (auto& rw : sp)
@@ -164,6 +174,7 @@ int group_build_tables(const DevNet& net, const int32_t* I, const double* D, voi
   out->mp_ptr = d + o4;
   out->mp_m = d + o5;
   out->mp_p = d + o6;
+  out->s_perm = d + o7;
   *d_buf = buf;
   return PF_OK;
 }

@@ -396,8 +396,10 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
       }
       __syncwarp(gmask);
       const double a_acc = dry ? 1.0 : psv * inv_dt * den_L;
-      // ---- secondaries s = r, r+G, ... (RTotalAqueous in product form)
-      for (int s = r; s < ns; s += G) {
+      // ---- the complexes dealt to the lanes longest list first (RTotalAqueous
+      // in product form)
+      for (int k = r; k < ns; k += G) {
+        const int s = gt.s_perm[k];
         double v = newton_iter_act ? exp(Ks[s] - dh_ln_gamma(T.sec_Z(s), T.sec_a0(s), sqI, lgI, net)) : Ks[s];
         for (int p = T.sec_begin(s); p < T.sec_end(s); ++p) {
           const int pe = T.sec_pidx(p);
