@@ -837,6 +837,7 @@ int32_t pf_adjoint(PfNetwork* net, const PfCellState* state, double dt, const Pf
   if (!batched_supported(d)) return PF_ERR_UNSUPPORTED;
   if (d.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) return PF_ERR_UNSUPPORTED;
   if (has_sorption(d)) return PF_ERR_UNSUPPORTED;  // no adjoint of the sorption terms
+  if (d.flags & NETF_PREFACTOR) return PF_ERR_UNSUPPORTED;  // nor of the rate prefactors
   if (!a->dL_dtotal0 || (d.nm > 0 && (!a->dL_dlnarea || !a->dL_dlogK_mnrl || !a->dL_dlnk)) ||
       (d.ns > 0 && !a->dL_dlogK_sec) || (!a->weight && !a->dL_dtotal) || (a->weight && !a->target))
     return PF_ERR_INVALID;

@@ -64,7 +64,9 @@ bool group_supported(const DevNet& net, int lanes_per_cell) {
       net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON)
     return false;
   if (net.ns > PF_MAX_NSEC || net.nm > PF_MAX_NMNRL) return false;
-  if (net.flags & NETF_PREFACTOR) return false;  // rate prefactors: the plain kernel
+  // rate prefactors with activity coefficients moving each Newton iteration:
+  // the plain kernel (the prefactor's complexes' activities would follow them)
+  if ((net.flags & NETF_PREFACTOR) && net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) return false;
   if (net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER && net.o.use_activity_h2o)
     return false;  // water activity moving each Newton iteration: the plain kernel
   const int R = (net.n + lanes_per_cell - 1) / lanes_per_cell;

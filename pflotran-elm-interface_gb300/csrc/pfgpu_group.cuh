@@ -4,6 +4,7 @@
 #pragma once
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
+#include "pfgpu_prefactor.cuh"
 #include "pfgpu_sorb.cuh"
 
 namespace pfgpu {
@@ -131,6 +132,45 @@ __device__ __forceinline__ bool group_sorb(const DevNet& net, const Tables& T, c
       [&](int i, int j, double v) { J[i * n + j] = fma(v_t * v, m[j], J[i * n + j]); }, surf_cell(net, st, cell));
 }
 
+// Kinetic-mineral rate prefactors (RKineticMineral, reaction_mineral.F90:
+// 820-858, derivative 976-1070) inside a group's evaluation, out of line so
+// that networks without them keep the kernel's registers.  TG: the network's
+// tables in global memory (the prefactor tables are not among the staged
+// ones); a[], sv[]: activities and complexes' molalities by species.
+static __device__ __noinline__ double group_pref_rate(const Tables& TG, const PfCellState& st, long long cell, int m,
+                                               const double* a, const double* sv, double temp) {
+  const SoA soa{st.ncells};
+  double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
+  return prefactor_rate(
+      TG, m, [&](int j) { return log(a[j]); },
+      [&](int i) { return log(sv[i]) + log(st.sec_act_coef[soa.at(i, cell)]); }, temp, pref, lnps);
+}
+
+// The prefactor part of the log-form Jacobian of every active mineral with
+// prefactors, added to the full rows J (column j scaled by m_j), by one lane
+// of the group.  m[], gam[]: molalities and activity coefficients by
+// species; Ks[]: the complexes' K/gamma of the set-up pre-pass; Im[]: the
+// minerals' volume-scaled rates of this evaluation (0: inactive).
+static __device__ __noinline__ void group_pref_jacobian(const DevNet& net, const Tables& TG, const PfCellState& st,
+                                                 long long cell, const double* a, const double* sv,
+                                                 const double* m, const double* gam, const double* Ks,
+                                                 const double* Im, double temp, double* J) {
+  const SoA soa{st.ncells};
+  const int n = net.n;
+  auto ln_act = [&](int j) { return log(a[j]); };
+  auto ln_sec_act = [&](int i) { return log(sv[i]) + log(st.sec_act_coef[soa.at(i, cell)]); };
+  for (int k = 0; k < net.nm; ++k) {
+    if (TG.pf_cnt(k) == 0 || Im[k] == 0.0) continue;
+    double pref[PF_MAX_PREFACTORS], lnps[PF_MAX_PREFACTORS][PF_MAX_PREFACTOR_SPECIES];
+    const double sum = prefactor_rate(TG, k, ln_act, ln_sec_act, temp, pref, lnps);
+    prefactor_derivative(
+        TG, k, Im[k], sum, pref, lnps, ln_act, ln_sec_act, [&](int j) { return gam[j]; },
+        [&](int i) { return st.sec_act_coef[soa.at(i, cell)]; }, [&](int j) { return log(m[j]); },
+        [&](int i) { return log(Ks[i]) + log(st.sec_act_coef[soa.at(i, cell)]); }, temp,
+        [&](int r, int c, double v) { J[r * n + c] = fma(v, m[c], J[r * n + c]); });
+  }
+}
+
 // The step for the cells of one network's work queue, by the block's warps,
 // with the network's tables already staged at the start of smem.  A warp
 // returns when the queue is empty and its cells are done.
@@ -179,6 +219,8 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
   const bool has_msf = net.flags & NETF_MSF, has_tk = net.flags & NETF_TEMKIN, has_pw = net.flags & NETF_POWER;
   const bool newton_iter_act = o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER;
   const bool has_sorb = !ADJ && has_sorption(net);  // the adjoint refuses sorption
+  const bool has_pf = !ADJ && (net.flags & NETF_PREFACTOR);  // and rate prefactors
+  const Tables TG{net.ints, net.dbls, &net};
   const unsigned neg_mask = (unsigned)net.neg_mask;
   const int64_t ncells = st.ncells;
   const double* sc_sec = scratch;
@@ -354,7 +396,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
       // LDL^T needs the symmetric log-form Jacobian: the sorption derivative
       // (the reference's surface complexation term is not symmetric) goes
       // into the full rows of the pivoted LU
-      const bool ldl = !use_lu && !newton_iter_act && !has_sorb;
+      const bool ldl = !use_lu && !newton_iter_act && !has_sorb && !has_pf;
       if (newton_iter_act) {
         // RActivityCoefficients LAG from this iterate and the previous
         // evaluation's sec_molal (reaction.F90:4553-4612)
@@ -386,7 +428,7 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           pw[i] = a;
           pw[n + i] = a * a;
           xs[i] = c[t];  // molality by species for the entry assembly (xs is free until the solve)
-          if (has_sorb) vvs[i] = g[t];  // activity coefficient by species (vvs is free until the solve)
+          if (has_sorb || has_pf) vvs[i] = g[t];  // activity coefficient by species (free until the solve)
           if (neg_mask & (1u << i)) {
             const double ia = 1.0 / a;
             pw[2 * n + i] = ia;
@@ -408,6 +450,8 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
         sv[s] = v;
       }
       // ---- kinetic minerals m = r, r+G, ... (reaction_mineral.F90:647-1078)
+      const double temp_c = st.temperature ? st.temperature[cell] : 25.0;
+      if (has_pf) __syncwarp(gmask);  // the prefactors read other lanes' complexes
       for (int m = r; m < nm; m += G) {
         const int b = T.mnrl_begin(m), e = T.mnrl_end(m);
         double Imv = 0.0, fv = 0.0, rv = 0.0;
@@ -426,12 +470,15 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
         if (active) {
           const double rl = T.limiter(m);
           if (rl > 0.0) aff = aff / (1.0 + (1.0 - aff) / rl);
-          double arr = 1.0;
-          if (T.ea(m) > 0.0) {
-            const double temp = st.temperature ? st.temperature[cell] : 25.0;
-            arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp + 273.15)));
+          double k;
+          if (has_pf && TG.pf_cnt(m) > 0) {
+            k = group_pref_rate(TG, st, cell, m, pw, sv, temp_c);
+          } else {
+            double arr = 1.0;
+            if (T.ea(m) > 0.0)
+              arr = exp(T.ea(m) / IDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (temp_c + 273.15)));
+            k = T.rate(m) * arr;
           }
-          const double k = T.rate(m) * arr;
           double Im_const = -st.mnrl_area[soa.at(m, cell)];
           if (has_msf) Im_const = Im_const / T.msf(m);
           double Im = has_pw ? Im_const * sign_ * pow(fabs(aff), T.power(m)) * k : Im_const * sign_ * fabs(aff) * k;
@@ -541,6 +588,13 @@ __device__ __forceinline__ void group_body(const DevNet& net, const GroupTabs& g
           if (dry) v = (i == j) ? xs[i] : 0.0;
           J[f] = v;
         }
+      }
+      // ---- rate prefactors: their part of the Jacobian, one lane of the
+      // group, into the full rows (the rates above already carry them)
+      if (has_pf && !back && !dry) {
+        __syncwarp(gmask);
+        if (r == 0) group_pref_jacobian(net, TG, st, cell, pw, sv, xs, vvs, Ks, mIm, temp_c, J);
+        __syncwarp(gmask);
       }
       // ---- equilibrium sorption: one lane of the group, into the full rows
       // and the residual; the residual norms are taken again

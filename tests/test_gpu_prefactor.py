@@ -1,8 +1,8 @@
 """Kinetic-mineral rate prefactors on the GPU against the oracle: the plain
 step kernel (RStep with the prefactor rate and derivative of
 RKineticMineral, reaction_mineral.F90:820-858, 976-1070) in the log and
-linear formulations, the global-implicit assembly, and the entry points that
-refuse such a network."""
+linear formulations, the group-per-cell kernel, the global-implicit
+assembly, and the entry points that refuse such a network."""
 import numpy as np
 import pytest
 
@@ -16,8 +16,12 @@ pytestmark = pytest.mark.gpu
 REL = 1e-10
 
 
-@pytest.mark.parametrize("logf", [True, False], ids=["log", "linear"])
-def test_plain_rstep_with_prefactors_matches_oracle(oracle, logf):
+@pytest.mark.parametrize("kernel,logf", [("plain", True), ("plain", False), ("group4", True), ("group8", True),
+                                         ("group2", True)])
+def test_rstep_with_prefactors_matches_oracle(oracle, kernel, logf):
+    """The plain kernel (log and linear formulations) and the group-per-cell
+    kernel (log formulation: its pivoted LU takes the prefactor derivative,
+    which is not symmetric, into full rows)."""
     from pfgpu.engine import ReactionEngine
     net, st = cases.prefactor_case(oracle, ncells=1000, log_formulation=logf)
     ref = st.copy()
@@ -31,10 +35,12 @@ def test_plain_rstep_with_prefactors_matches_oracle(oracle, logf):
         oracle.rstep(net, p, 3600.0, nthreads=8)
         perts.append(p)
     eng = ReactionEngine(net)
+    if kernel.startswith("group"):
+        assert eng.set_launch_config(128, 2, 0, int(kernel[5:])) == abi.PF_OK
     dev = st.to("cuda")
-    eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_PLAIN)
+    eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED)
     got = dev.numpy()
-    label = "prefactors/plain/%s" % ("log" if logf else "linear")
+    label = "prefactors/%s/%s" % (kernel, "log" if logf else "linear")
     entry, ok = parity.compare(net, ref, got, 3600.0, label, perts)
     parity.check(entry, label, min_compared=int(0.9 * st.ncells))
     r = ref.a["mnrl_rate"][:, ok]
@@ -42,15 +48,22 @@ def test_plain_rstep_with_prefactors_matches_oracle(oracle, logf):
 
 
 def test_kernels_without_prefactors_refuse_them(oracle):
+    """The one-lane kernel (LDL^T of a symmetric Jacobian) and the adjoint
+    have no prefactor terms; the group kernel carries them, but not with
+    activity coefficients moving each Newton iteration."""
     from pfgpu.engine import ReactionEngine
     net, st = cases.prefactor_case(oracle, ncells=64)
     eng = ReactionEngine(net)
     dev = st.to("cuda")
+    assert eng.set_launch_config(128, 1, 0, 1) == abi.PF_ERR_UNSUPPORTED
+    for lanes in (2, 4, 8):
+        assert eng.set_launch_config(128, 1, 0, lanes) == abi.PF_OK
     with pytest.raises(abi.PfError) as e:
-        eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_BATCHED)
+        eng.adjoint(dev, 3600.0, dL_dtotal=torch.ones_like(dev.a["total"]))
     assert e.value.code == abi.PF_ERR_UNSUPPORTED
+    ni = ReactionEngine(net.with_options(act_coef_update_frequency=abi.PF_ACT_COEF_NEWTON_ITER))
     for lanes in (1, 2, 4, 8):
-        assert eng.set_launch_config(128, 1, 0, lanes) == abi.PF_ERR_UNSUPPORTED
+        assert ni.set_launch_config(128, 1, 0, lanes) == abi.PF_ERR_UNSUPPORTED
 
 
 @pytest.mark.parametrize("numjac", [False, True], ids=["analytical", "numerical"])
