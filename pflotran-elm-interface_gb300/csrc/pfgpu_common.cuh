@@ -253,8 +253,15 @@ struct LogKAtT {
     const double q = c * it;
     return fma(fma(-q, t, c), it, q);
   }
+  // A zero coefficient contributes an exact zero, so its term is skipped (a
+  // branch on the reaction's coefficient, the same in every lane): a fit
+  // linear in T costs one multiply-add.
   __device__ __forceinline__ double operator()(const double* c) const {
-    return c[0] * ltk + c[1] + c[2] * tk + quot(c[3], tk, itk) + quot(c[4], tk2, itk2);
+    double v = c[0] != 0.0 ? c[0] * ltk + c[1] : c[1];
+    if (c[2] != 0.0) v = v + c[2] * tk;
+    if (c[3] != 0.0) v = v + quot(c[3], tk, itk);
+    if (c[4] != 0.0) v = v + quot(c[4], tk2, itk2);
+    return v;
   }
 };
 
