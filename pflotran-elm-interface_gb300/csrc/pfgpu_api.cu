@@ -881,10 +881,17 @@ int32_t pf_girt_assemble(PfNetwork* net, const PfCellState* state, const PfGirtA
     rc = girt_build_tables(net->dev, net->ints_base.data(), net->dbls_base.data(), &net->d_girt, &net->girt);
     if (rc) return rc;
   }
-  if (girt_smem_bytes(net->dev, net->girt, (net->dev.flags & NETF_PREFACTOR) || a->numerical_derivatives, nullptr,
-                      nullptr) > 227u * 1024u)
+  // the packed sum of d total/d m in global memory ([entry][cell], the
+  // network's grow-only scratch): the shared-memory scratch per cell would
+  // cap the resident warps
+  const size_t nsym = (size_t)net->dev.n * (net->dev.n + 1) / 2;
+  rc = ensure_scratch_doubles(net, nsym * (size_t)state->ncells);
+  if (rc) return rc;
+  if (girt_smem_bytes(net->dev, net->girt, (net->dev.flags & NETF_PREFACTOR) || a->numerical_derivatives, false,
+                      nullptr, nullptr) > 227u * 1024u)
     return PF_ERR_TOO_LARGE;
-  return launch_girt_assemble(net->dev, net->girt, *state, *a, net->num_sms, (cudaStream_t)stream);
+  return launch_girt_assemble(net->dev, net->girt, *state, *a, net->num_sms, (cudaStream_t)stream,
+                              net->d_scratch);
 }
 
 int32_t pf_equilibrate_constraint_ex(PfNetwork* net, const PfCellState* state, const int32_t* ctype,

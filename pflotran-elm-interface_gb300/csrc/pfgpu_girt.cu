@@ -88,12 +88,12 @@ struct Geo {
 struct Layout {
   int pa, E, T, GQ, lna, per_thread;
 };
-__host__ __device__ inline Layout layout(const DevNet& net, bool with_lna) {
+__host__ __device__ inline Layout layout(const DevNet& net, bool with_lna, bool e_in_smem = true) {
   const int n = net.n;
   Layout L;
   L.pa = 0;
   L.E = 2 * n;
-  L.T = L.E + n * (n + 1) / 2;
+  L.T = L.E + (e_in_smem ? n * (n + 1) / 2 : 0);
   L.GQ = L.T;
   L.lna = L.T + (n > net.nm ? n : net.nm);
   L.per_thread = L.lna + (with_lna ? n : 0);
@@ -338,11 +338,11 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
                                           double dt, const int32_t* __restrict__ rowptr,
                                           const int32_t* __restrict__ colidx, double* __restrict__ r,
                                           double* __restrict__ values, int vec, int staged,
-                                          double* __restrict__ kcache, int kmode) {
+                                          double* __restrict__ kcache, int kmode, double* __restrict__ Eg) {
   constexpr bool HAS_LNA = HAS_PF || NUMJAC;
   extern __shared__ __align__(16) unsigned char sraw[];
   const int bd = blockDim.x;
-  const Layout Lo = layout(net, HAS_LNA);
+  const Layout Lo = layout(net, HAS_LNA, Eg == nullptr);
   double* const Kc = reinterpret_cast<double*>(sraw);
   size_t off = block_k_bytes(net);
   const int32_t* sI = net.ints;
@@ -438,7 +438,10 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
     if constexpr (HAS_LNA) P[(Lo.lna + j) * bd] = log(m) + log(gam);
   }
   const int nsym = n * (n + 1) / 2;
-  for (int k = 0; k < nsym; ++k) P[(Lo.E + k) * bd] = 0.0;
+  // the packed sum: in the thread's shared scratch, or (Eg) in global memory,
+  // [entry][cell], when the shared scratch would cap the resident warps
+  auto Eref = [&](int k) -> double& { return Eg ? Eg[(size_t)k * st.ncells + X] : P[(Lo.E + k) * bd]; };
+  for (int k = 0; k < nsym; ++k) Eref(k) = 0.0;
   // factor a_j^nu from its power-table code (0: a, 1: a^2, 2: 1/a, 3: 1/a^2)
   auto factor = [&](int pe, double nu, int j) {
     if (pe >= 0) {
@@ -461,8 +464,8 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
     }
     // sum_i nu_ri nu_ci s_i, complexes ascending as the reference's entries
     for (int q = s_pair_ptr[i]; q < s_pair_ptr[i + 1]; ++q) {
-      const int a = (Lo.E + s_pair_k[q]) * bd;
-      P[a] = fma(s_pair_c[q], s, P[a]);
+      double& a = Eref(s_pair_k[q]);
+      a = fma(s_pair_c[q], s, a);
     }
   }
   for (int j = 0; j < n; ++j) st.total[soa.at(j, X)] = P[(Lo.T + j) * bd] * den_L;
@@ -533,8 +536,8 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
   if (logf) {
     for (int hi = 0, k = 0; hi < n; ++hi)
       for (int lo = 0; lo <= hi; ++lo, ++k) {
-        const int a = (Lo.E + k) * bd;
-        P[a] = (lo == hi ? P[a] + st.pri_molal[soa.at(hi, X)] : P[a]) * den_L;
+        double& a = Eref(k);
+        a = (lo == hi ? a + st.pri_molal[soa.at(hi, X)] : a) * den_L;
       }
   } else {
     for (int j = 0; j < n; ++j) {
@@ -562,7 +565,7 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
   // v = the diagonal block's value
   auto entry = [&](int fe, double& v, double& e) {
     const int col = fe / n, row = fe - col * n;
-    const double E = P[(Lo.E + sym_index(row, col)) * bd];
+    const double E = Eref(sym_index(row, col));
     const double im = logf ? 0.0 : P[(Lo.pa + col) * bd];
     e = logf ? E : fma(E, P[(Lo.pa + n + col) * bd], row == col ? den_L : 0.0);
     if (dry) {
@@ -649,10 +652,10 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
 #define PF_GIRT_CELL_ARGS                                                                                           \
   DevNet net, GirtTabs gt, PfCellState st, Geo g, double dt, const int32_t* __restrict__ rowptr,                   \
       const int32_t* __restrict__ colidx, double* __restrict__ r, double* __restrict__ values, int vec, int staged, \
-      double* __restrict__ kcache, int kmode
+      double* __restrict__ kcache, int kmode, double* __restrict__ Eg
 template <bool HAS_PF, bool NUMJAC>
 __global__ void __launch_bounds__(128) girt_cell_kernel(PF_GIRT_CELL_ARGS) {
-  girt_cell<HAS_PF, NUMJAC>(net, gt, st, g, dt, rowptr, colidx, r, values, vec, staged, kcache, kmode);
+  girt_cell<HAS_PF, NUMJAC>(net, gt, st, g, dt, rowptr, colidx, r, values, vec, staged, kcache, kmode, Eg);
 }
 #undef PF_GIRT_CELL_ARGS
 
@@ -763,9 +766,9 @@ int girt_build_tables(const DevNet& net, const int32_t* I, const double* D, void
 // shared memory, and the dynamic shared memory: the block size (a multiple
 // of 32, at most 128) that keeps the most warps resident, staging the tables
 // when that costs no warps
-size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, int* threads_per_block,
+size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, bool e_in_smem, int* threads_per_block,
                        int* staged) {
-  const size_t tbytes = (size_t)girt::layout(net, with_lna).per_thread * sizeof(double);
+  const size_t tbytes = (size_t)girt::layout(net, with_lna, e_in_smem).per_thread * sizeof(double);
   const size_t kbytes = girt::block_k_bytes(net), tab = girt::block_table_bytes(net, gt);
   const size_t sm_bytes = 228u * 1024u, per_block_reserved = 1024u;
   int best = 0, best_warps = -1, best_staged = 0;
@@ -790,7 +793,7 @@ size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, int
 }
 
 int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const PfGirtArgs& a,
-                         int num_sms, cudaStream_t s) {
+                         int num_sms, cudaStream_t s, double* e_scratch) {
   (void)num_sms;
   if (st.ncells == 0) return PF_OK;
   girt::Geo g{a.nx, a.ny, a.nz, a.dx, a.dy, a.dz, a.diffusion_coefficient, a.tortuosity, a.dispersivity,
@@ -798,7 +801,7 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   const bool pf = (net.flags & NETF_PREFACTOR) != 0;
   const bool with_lna = pf || a.numerical_derivatives;
   int tpb = 32, staged = 0;
-  const size_t smem = girt_smem_bytes(net, gt, with_lna, &tpb, &staged);
+  const size_t smem = girt_smem_bytes(net, gt, with_lna, e_scratch == nullptr, &tpb, &staged);
   if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
   const int nn = net.n * net.n;
   const uintptr_t va = (uintptr_t)a.values;
@@ -813,7 +816,7 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
   const int kmode = a.k_cache ? (a.k_cache_valid ? 2 : 1) : 0;
   const long long blocks = (st.ncells + tpb - 1) / tpb;
   k<<<(unsigned)blocks, tpb, smem, s>>>(net, gt, st, g, a.dt, a.rowptr, a.colidx, a.residual, a.values, vec, staged,
-                                        a.k_cache, kmode);
+                                        a.k_cache, kmode, e_scratch);
   if (cudaGetLastError() != cudaSuccess) return PF_ERR_CUDA;
   const long long rblocks = (st.ncells + 127) / 128;
   girt::girt_residual_kernel<<<(unsigned)rblocks, 128, 0, s>>>(net, st, g, a.total_k, a.total_sorb_k, a.dt,

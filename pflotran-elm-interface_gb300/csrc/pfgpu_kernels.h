@@ -90,10 +90,12 @@ struct GirtTabs {
 // and upload them (*d_buf: the one device allocation)
 int girt_build_tables(const DevNet& net, const int32_t* h_ints, const double* h_dbls, void** d_buf,
                       GirtTabs* out);
-size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, int* threads_per_block,
+size_t girt_smem_bytes(const DevNet& net, const GirtTabs& gt, bool with_lna, bool e_in_smem, int* threads_per_block,
                        int* staged);
 // RTUpdateAuxVars then the column kernel; a PfStatus
+// e_scratch: nsym x ncells doubles of global memory for the packed sum of
+// d total/d m (NULL: in shared memory)
 int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellState& st, const PfGirtArgs& a,
-                         int num_sms, cudaStream_t stream);
+                         int num_sms, cudaStream_t stream, double* e_scratch);
 
 }  // namespace pfgpu
