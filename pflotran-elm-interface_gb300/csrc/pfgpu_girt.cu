@@ -800,17 +800,34 @@ int launch_girt_assemble(const DevNet& net, const GirtTabs& gt, const PfCellStat
               a.qx, a.qy, a.qz};
   const bool pf = (net.flags & NETF_PREFACTOR) != 0;
   const bool with_lna = pf || a.numerical_derivatives;
-  int tpb = 32, staged = 0;
-  const size_t smem = girt_smem_bytes(net, gt, with_lna, e_scratch == nullptr, &tpb, &staged);
-  if (smem > 227u * 1024u) return PF_ERR_TOO_LARGE;
   const int nn = net.n * net.n;
   const uintptr_t va = (uintptr_t)a.values;
   auto k = a.numerical_derivatives ? girt::girt_cell_kernel<true, true>
            : pf                    ? girt::girt_cell_kernel<true, false>
                                    : girt::girt_cell_kernel<false, false>;
-  if (smem > 48u * 1024u &&
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
     return PF_ERR_CUDA;
+  // the block size and table staging that keep the most warps resident, the
+  // kernel's registers included (occupancy calculator); staging on a tie
+  const bool e_smem = e_scratch == nullptr;
+  const size_t tbytes = (size_t)girt::layout(net, with_lna, e_smem).per_thread * sizeof(double);
+  const size_t kbytes = girt::block_k_bytes(net), tab = girt::block_table_bytes(net, gt);
+  int tpb = 0, staged = 0, best_warps = 0;
+  size_t smem = 0;
+  for (int stg = 1; stg >= 0; --stg)
+    for (int t = 32; t <= 128; t += 32) {
+      const size_t b = t * tbytes + kbytes + (stg ? tab : 0);
+      if (b > 227u * 1024u) continue;
+      int nb = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, t, b) != cudaSuccess) return PF_ERR_CUDA;
+      if (nb * t / 32 > best_warps) {
+        best_warps = nb * t / 32;
+        tpb = t;
+        staged = stg;
+        smem = b;
+      }
+    }
+  if (tpb == 0) return PF_ERR_TOO_LARGE;
   // whole-sector stores when every block starts on a 32-byte boundary
   const int vec = (nn % 4 == 0 && (va & 31) == 0) ? 4 : ((nn % 2 == 0 && (va & 15) == 0) ? 2 : 1);
   const int kmode = a.k_cache ? (a.k_cache_valid ? 2 : 1) : 0;
