@@ -654,7 +654,7 @@ __device__ __forceinline__ void girt_cell(const DevNet& net, const GirtTabs& gt,
       const int32_t* __restrict__ colidx, double* __restrict__ r, double* __restrict__ values, int vec, int staged, \
       double* __restrict__ kcache, int kmode, double* __restrict__ Eg
 template <bool HAS_PF, bool NUMJAC>
-__global__ void __launch_bounds__(128) girt_cell_kernel(PF_GIRT_CELL_ARGS) {
+__global__ void __launch_bounds__(128, 5) girt_cell_kernel(PF_GIRT_CELL_ARGS) {
   girt_cell<HAS_PF, NUMJAC>(net, gt, st, g, dt, rowptr, colidx, r, values, vec, staged, kcache, kmode, Eg);
 }
 #undef PF_GIRT_CELL_ARGS
