@@ -234,6 +234,21 @@ def c2_config(cfg, ncells, dt, state_bytes):
     return {"workload": cfg["workload"], "cells": ncells, "dt_s": dt, "step": STEP, "l2": l2}
 
 
+ITS_EDGES = (1, 2, 4, 8, 16, 32, 64, 128, 256, 512)
+
+
+def its_histogram(its):
+    """Cells per Newton-count bin [edge_k, edge_k+1) of a step's per-cell
+    Newton iterations (a device int32 tensor); the last bin is open."""
+    import torch
+    edges = torch.tensor(ITS_EDGES, dtype=torch.int64, device=its.device)
+    b = torch.bucketize(its.to(torch.int64), edges, right=True)
+    counts = torch.bincount(b, minlength=len(ITS_EDGES) + 1).cpu().tolist()
+    return {"bins": ["<1"] + ["%d-%d" % (lo, hi - 1) for lo, hi in zip(ITS_EDGES, ITS_EDGES[1:])] +
+                    [">=%d" % ITS_EDGES[-1]],
+            "cells": counts}
+
+
 def time_steps(eng, dev, pristine, dt, kernel, steps, warmup, order=None):
     import torch
     from pfgpu import abi  # noqa: F401
@@ -926,11 +941,13 @@ def main():
     for k in s0:
         dev.a[k].copy_(s0[k])
     stats1 = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
+    hist1 = its_histogram(dev.a["newton_its"])
     order = torch.argsort(dev.a["newton_its"].to(torch.int64), descending=True)
     pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}  # S1, the timed step's input
     # one instrumented run of the timed step: iteration statistics for the flop count
     stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True, order=order)
     its_mean = stats["newton_iterations"] / ncells
+    hist = its_histogram(dev.a["newton_its"])
     for k in pristine:
         dev.a[k].copy_(pristine[k])
 
@@ -1076,6 +1093,7 @@ def main():
                            "cell_order": "descending Newton count of the previous (untimed) step"},
                 "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
                 "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
+                "newton_its_histogram": hist,
                 "first_step": {"what": "the first step from the equilibrated state, natural queue order",
                                "value": ncells * len(f1_kern) / (f1_total * 1e-3),
                                "kernel_ms": float(np.mean(f1_kern)),
@@ -1084,7 +1102,8 @@ def main():
                                "speedup_vs_plain_gpu": float(np.mean(p1_kern)) / float(np.mean(f1_kern)),
                                "newton_its_per_cell": stats1["newton_iterations"] / ncells,
                                "max_newton_its": stats1["max_newton_iterations"],
-                               "failed_cells": stats1["failed_cells"]},
+                               "failed_cells": stats1["failed_cells"],
+                               "newton_its_histogram": hist1},
                 "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},
                 "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),
                                   "kernel_ms": float(np.mean(nat_kern))},

@@ -664,12 +664,9 @@ static int check_rstep(PfNetwork* net, const PfCellState* state, double dt, int3
   if (rc) return rc;
   if (!(dt > 0.0) && !state->dt_cell) return PF_ERR_INVALID;
   if (kernel != PF_KERNEL_PLAIN && kernel != PF_KERNEL_BATCHED) return PF_ERR_INVALID;
+  // activity coefficients by the NEWTON algorithm at every Newton iteration:
+  // the plain kernel (batched_supported refuses the combination)
   if (kernel == PF_KERNEL_BATCHED && !batched_supported(net->dev)) return PF_ERR_UNSUPPORTED;
-  // activity coefficients by the NEWTON algorithm at every Newton iteration
-  // are not built in the step kernels (LAG is)
-  if (net->dev.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
-      net->dev.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON)
-    return PF_ERR_UNSUPPORTED;
   return PF_OK;
 }
 

@@ -10,7 +10,8 @@
 // With equilibrium sorption RTAuxVarCompute adds RTotalSorb and the
 // accumulation RAccumulationSorb[Derivative] (reaction.F90:3836-3839,
 // 3861-3865, 3904-3909), any ncomp; kinetic-mineral rate prefactors
-// (reaction_mineral.F90:820-858, 976-1070) run here only.
+// (reaction_mineral.F90:820-858, 976-1070) and the NEWTON activity
+// algorithm at every Newton iteration (:3857-3860, 4403-4551) run here only.
 #include "pfgpu_common.cuh"
 #include "pfgpu_kernels.h"
 #include "pfgpu_prefactor.cuh"
@@ -239,6 +240,94 @@ __device__ int rsolve(int n, double* J, const double* conc, const double* Res, d
   return 0;
 }
 
+// RActivityCoefficients by the NEWTON algorithm (reaction.F90:4403-4551) at
+// the Newton iterate w.c: a Newton iteration on the ionic strength, the
+// primaries' activities held at the iterate and the coefficients of the
+// last evaluation; each pass rewrites both sets of coefficients, the
+// complexes' molalities and (water activity on) ln a_H2O.  Returns false
+// where the reference gives up -- more than 50 passes (:4420-4431) or a
+// negative ionic strength (:4476-4485) -- after setting the iterate and the
+// coefficients to NaN as it does; its option%ierror then fails RReact after
+// the residual (:3929-3943).
+template <int NMAX>
+__device__ bool activity_newton(const Tables& T, const DevNet& net, int n, int ns, const double* sec_logK,
+                                int64_t cell, const SoA& soa, const PfCellState& st, CellScalars& cs,
+                                Work<NMAX>& w) {
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  auto give_up = [&]() {
+    for (int j = 0; j < n; ++j) {
+      w.c[j] = nan;
+      w.gamma[j] = nan;
+    }
+    for (int i = 0; i < ns; ++i) st.sec_act_coef[soa.at(i, cell)] = nan;
+    return false;
+  };
+  double sum_pri_molal = 0.0, fpri = 0.0;
+  for (int j = 0; j < n; ++j) {
+    w.lna[j] = log(w.c[j]) + log(w.gamma[j]);
+    sum_pri_molal = sum_pri_molal + w.c[j];
+    fpri = fpri + w.c[j] * T.pri_Z(j) * T.pri_Z(j);
+  }
+  double II = 0.0;
+  for (int it = 1;; ++it) {
+    if (it > 50) return give_up();
+    double I = fpri;
+    for (int i = 0; i < ns; ++i) I = I + st.sec_molal[soa.at(i, cell)] * T.sec_Z(i) * T.sec_Z(i);
+    I = 0.5 * I;
+    const double f = I;
+    if (fabs(I - II) < 1.0e-6 * I) return true;
+    if (ns > 0) {
+      double didi = 0.0;
+      const double sqrt_I = sqrt(I);
+      for (int i = 0; i < ns; ++i) {
+        const double zi = T.sec_Z(i);
+        if (fabs(zi) > 0.0) {
+          const double t = 1.0 + net.B * T.sec_a0(i) * sqrt_I;
+          double sum = 0.5 * net.A * zi * zi / (sqrt_I * (t * t)) - net.Bdot;
+          for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) {
+            const double zj = T.pri_Z(T.sec_idx(p));
+            if (fabs(zj) > 0.0) {
+              const double tj = 1.0 + net.B * T.pri_a0(T.sec_idx(p)) * sqrt_I;
+              sum = sum + T.sec_nu(p) * (-0.5 * net.A * (zj * zj) / (sqrt_I * (tj * tj)) + net.Bdot);
+            }
+          }
+          didi = didi + 0.5 * zi * zi * (st.sec_molal[soa.at(i, cell)] * LOG_TO_LN * sum);
+        }
+      }
+      const double den = 1.0 - didi;
+      II = fabs(den) > 0.0 ? (f - I * didi) / den : f;
+    } else {
+      II = f;
+    }
+    if (II < 0.0) return give_up();
+    I = II;
+    const double sqrt_I = sqrt(I);
+    for (int j = 0; j < n; ++j) {
+      const double z = T.pri_Z(j);
+      w.gamma[j] = fabs(z) > 0.0
+                       ? exp((-z * z * sqrt_I * net.A / (1.0 + T.pri_a0(j) * net.B * sqrt_I) + net.Bdot * I) *
+                             LOG_TO_LN)
+                       : 1.0;
+    }
+    double sum_sec_molal = 0.0;
+    for (int i = 0; i < ns; ++i) {
+      const double z = T.sec_Z(i);
+      const double g =
+          fabs(z) > 0.0
+              ? exp((-z * z * sqrt_I * net.A / (1.0 + T.sec_a0(i) * net.B * sqrt_I) + net.Bdot * I) * LOG_TO_LN)
+              : 1.0;
+      st.sec_act_coef[soa.at(i, cell)] = g;
+      double lnQK = -sec_logK[i] * LOG_TO_LN;
+      if (water_on(net)) lnQK = add_h2o(lnQK, T.sec_h2o(i), cs.lnaw);
+      for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * w.lna[T.sec_idx(p)];
+      const double sm = exp(lnQK) / g;
+      st.sec_molal[soa.at(i, cell)] = sm;
+      sum_sec_molal = sum_sec_molal + sm;
+    }
+    if (net.o.use_activity_h2o) cs.lnaw = water_activity(sum_pri_molal, sum_sec_molal);
+  }
+}
+
 template <int NMAX, bool PF>
 __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellState st, double dt_uniform,
                                                           unsigned long long* counters) {
@@ -313,7 +402,11 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
     }
     for (;;) {
       its = its + 1;
-      if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) {
+      bool act_failed = false;
+      if (PF && o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
+          o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON) {
+        act_failed = !activity_newton<NMAX>(T, net, n, ns, sec_logK, cell, soa, st, cs, w);
+      } else if (o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER) {
         // RActivityCoefficients, LAG (reaction.F90:3857-3860, 4553-4612):
         // ionic strength from this iterate and the previous evaluation's
         // complexes
@@ -377,6 +470,10 @@ __global__ void __launch_bounds__(128) rstep_plain_kernel(DevNet net, PfCellStat
           w.res[j] = w.res[j] + w.sorb[j] * cs.volume / dt;
           for (int k = 0; k < n; ++k) w.J[j * NMAX + k] = w.J[j * NMAX + k] + w.dsorb[j * NMAX + k] * v_t;
         }
+      }
+      if (PF && act_failed) {  // option%ierror of the activity pass: no total restore (:3929-3943)
+        ierror = 1;
+        break;
       }
       double dot = 0.0, mx = 0.0;
       for (int j = 0; j < n; ++j) {
@@ -480,8 +577,11 @@ int launch_rstep_plain(const DevNet& net, const PfCellState& st, double dt,
   const int tpb = 128;
   const int64_t blocks = (st.ncells + tpb - 1) / tpb;
   if (blocks == 0) return 0;
-  if ((net.flags & NETF_PREFACTOR) || net.o.use_activity_h2o) {
-    // rate prefactors or water activity: the extended instantiation, three size buckets
+  if ((net.flags & NETF_PREFACTOR) || net.o.use_activity_h2o ||
+      (net.o.act_coef_update_frequency == PF_ACT_COEF_NEWTON_ITER &&
+       net.o.act_coef_update_algorithm == PF_ACT_COEF_ALGO_NEWTON)) {
+    // rate prefactors, water activity or the NEWTON activity algorithm at
+    // every Newton iteration: the extended instantiation, three size buckets
     if (net.n <= 8) plain::rstep_plain_kernel<8, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
     else if (net.n <= 12) plain::rstep_plain_kernel<12, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);
     else plain::rstep_plain_kernel<24, true><<<blocks, tpb, 0, stream>>>(net, st, dt, counters);

@@ -98,7 +98,10 @@ def cell_errors(net, ref, got, dt):
     def r(a, b, scale):
         with np.errstate(divide="ignore", invalid="ignore"):
             e = np.abs(a - b) / scale
-        e = np.where(a == b, 0.0, e)  # equal values (including equal infinities) agree
+        # equal values (including equal infinities) agree, and so do NaNs in
+        # the same place (a cell the reference leaves NaN, e.g. a failed
+        # activity iteration, reaction.F90:4420-4431)
+        e = np.where((a == b) | (np.isnan(a) & np.isnan(b)), 0.0, e)
         return np.nan_to_num(e, nan=np.inf).reshape(-1, ref.ncells).max(axis=0)
     e = {"pri_molal": r(got.a["pri_molal"], ref.a["pri_molal"], np.abs(ref.a["pri_molal"]))}
     if net.nsec:

@@ -288,11 +288,13 @@ def test_component_counts_without_one_lane_kernel(oracle, ncomp):
     parity.check(entry, "odd%d" % ncomp, min_compared=50)
 
 
-def _newton_iter_case(oracle):
+def _newton_iter_case(oracle, algo=None):
     from pfgpu import abi, generate
     from pfgpu.network import default_options
     opts = default_options(isothermal=0)
     opts["act_coef_update_frequency"] = abi.PF_ACT_COEF_NEWTON_ITER
+    if algo is not None:
+        opts["act_coef_update_algorithm"] = algo
     net = generate.random_network(12, 40, 6, seed=12, options=opts)
     st, ct, cc = generate.random_cells(net, 600, seed=4242)
     st, _ = cases.prepare(oracle, net, st, ct, cc)
@@ -327,6 +329,37 @@ def test_activity_each_newton_iteration(oracle, kernel):
     entry, ok = parity.compare(net, ref, got, 86400.0, "newton_iter/" + kernel, perts)
     parity.check(entry, "newton_iter/" + kernel, min_compared=100)
     np.testing.assert_allclose(got.a["pri_act_coef"][:, ok], ref.a["pri_act_coef"][:, ok], rtol=1e-10)
+
+
+@pytest.mark.gpu
+def test_newton_activity_each_newton_iteration(oracle):
+    """act_coef_update_frequency = NEWTON_ITERATION with the NEWTON
+    algorithm (reaction.F90:3857-3860, 4403-4551): the ionic-strength
+    iteration at every Newton iterate runs in the plain kernel, against the
+    oracle with the flip-aware comparison; the batched kernels refuse it."""
+    from pfgpu import abi
+    from pfgpu.engine import ReactionEngine
+    net, st = _newton_iter_case(oracle, abi.PF_ACT_COEF_ALGO_NEWTON)
+    ref = st.copy()
+    oracle.rstep(net, ref, 86400.0, nthreads=8)
+    perts = []
+    for key, to in (("total", np.inf), ("total", -np.inf), ("pri_molal", np.inf)):
+        p = st.copy()
+        p.a[key][:] = np.nextafter(p.a[key], to)
+        oracle.rstep(net, p, 86400.0, nthreads=8)
+        perts.append(p)
+    eng = ReactionEngine(net)
+    dev = st.to("cuda")
+    with pytest.raises(abi.PfError) as e:
+        eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_BATCHED)
+    assert e.value.code == abi.PF_ERR_UNSUPPORTED
+    assert eng.set_launch_config(128, 2, 0, 4) == abi.PF_ERR_UNSUPPORTED
+    eng.rstep(dev, 86400.0, kernel=abi.PF_KERNEL_PLAIN)
+    got = dev.numpy()
+    entry, ok = parity.compare(net, ref, got, 86400.0, "newton_algo_iter/plain", perts)
+    parity.check(entry, "newton_algo_iter/plain", min_compared=100)
+    for key in ("pri_act_coef", "sec_act_coef"):
+        np.testing.assert_allclose(got.a[key][:, ok], ref.a[key][:, ok], rtol=1e-10)
 
 
 @pytest.mark.gpu
