@@ -220,8 +220,8 @@ def fp64_peak(lib, device_sms, clocks=None):
     return best
 
 
-STEP = ("the second operator-split step from the equilibrated state; the first step (untimed) gives the "
-        "Newton counts that order the second step's work queue")
+STEP = ("the second operator-split step from the equilibrated state, its work queue in cell order (the first "
+        "step, untimed, gives the state it starts from)")
 
 
 def c2_config(cfg, ncells, dt, state_bytes):
@@ -921,17 +921,20 @@ def main():
             raise SystemExit("launch config %s rejected" % args.launch)
     elif not args.no_tune:
         from pfgpu import autotune
-        # the timed steps run with the cost-ordered queue: tune that way, on a
-        # quarter of the cells
-        best, table = autotune.tune(eng, dev, dt, use_cache=False, cost_order=True,
+        # the timed steps run with the queue in cell order: tune that way, on
+        # a quarter of the cells
+        best, table = autotune.tune(eng, dev, dt, use_cache=False, cost_order=False,
                                     max_cells=max(65536, ncells // 4), reps=1)
         tuned = {"best": best, "top": table[:6]}
         log("autotune:", json.dumps(tuned))
 
     # The timed step is the second operator-split step of a time loop: the
-    # first step (untimed) takes the equilibrated state S0 to S1, and its
-    # per-cell Newton counts order the second step's work queue (descending,
-    # stiffest cells first) -- the only cost information a time loop has.
+    # first step (untimed) takes the equilibrated state S0 to S1.  Its work
+    # queue is in cell order: ordered by the first step's Newton counts
+    # (descending, the only cost information a time loop has) it measured 2 %
+    # slower -- the first step's stiff cells are not the second step's, and a
+    # block's cells then come from all over the state, one 32-byte sector per
+    # cell -- so that order is measured beside it (cost_order).
     # the first step itself, from the equilibrated state, in natural order (no
     # cost information exists yet), batched and plain
     nrep = max(1, min(args.steps, 3))
@@ -945,7 +948,7 @@ def main():
     order = torch.argsort(dev.a["newton_its"].to(torch.int64), descending=True)
     pristine = {k: dev.a[k].clone() for k in MUTABLE if k in dev.a}  # S1, the timed step's input
     # one instrumented run of the timed step: iteration statistics for the flop count
-    stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True, order=order)
+    stats = eng.rstep(dev, dt, kernel=abi.PF_KERNEL_BATCHED, stats=True)
     its_mean = stats["newton_iterations"] / ncells
     hist = its_histogram(dev.a["newton_its"])
     for k in pristine:
@@ -955,9 +958,9 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with Clocks(local) as clk:
-        total_ms, kern_ms = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, args.steps, args.warmup,
-                                       order=order)
-    nat_total, nat_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, max(1, min(args.steps, 3)), 1)
+        total_ms, kern_ms = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, args.steps, args.warmup)
+    ord_total, ord_kern = time_steps(eng, dev, pristine, dt, abi.PF_KERNEL_BATCHED, max(1, min(args.steps, 3)), 1,
+                                     order=order)
     if dist:
         # replicas: the slowest rank's time, and the reference loop's
         # rstep_error MAX / iteration sums over the ranks
@@ -968,7 +971,7 @@ def main():
     kern_avg = float(np.mean(kern_ms))
 
     # adjoint of the timed step
-    adjoint = adjoint_measure(eng, dev, pristine, dt, order, nrep, kern_avg)
+    adjoint = adjoint_measure(eng, dev, pristine, dt, None, nrep, kern_avg)
     adjoint["first_step"] = adjoint1
 
     # plain one-thread-per-cell form, same inputs
@@ -996,9 +999,10 @@ def main():
     # DRAM bytes per cell-solve of the launched kernel measured by ncu on the
     # same workload at 200,000 cells, scaled to this launch:
     #   one lane per cell  profiles/rstep_batched_kernel_n12_200k.txt   6.431 + 4.639 GB
-    #   group of lanes     profiles/rstep_group_kernel_g4_n12_200k.txt  2.303 + 0.433 GB
+    #   group of lanes     profiles/rstep_group_kernel_g4_n12_200k.txt  0.2232 + 0.1005 GB
+    #                      (the second step, queue in cell order)
     grp = eng.launch_config()["lanes_per_cell"] > 1
-    per_launch_200k = (2.303e9 + 0.433e9) if grp else (6.431e9 + 4.639e9)
+    per_launch_200k = (0.2232e9 + 0.1005e9) if grp else (6.431e9 + 4.639e9)
     traffic = per_launch_200k / 200_000 * ncells if args.config == "c2" else None
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic,
@@ -1027,18 +1031,16 @@ def main():
         hs = CellState(net, {k: pin[k].numpy() for k in pin})
         h2d = sum(pin[k].numel() * pin[k].element_size() for k in pin if k not in ("mnrl_rate", "status",
                                                                                   "newton_its", "num_substeps"))
-        h2d += ncells * 8  # the work-queue order
         d2h = sum(pin[k].numel() * pin[k].element_size() for k in pin
                   if k in ("total", "pri_molal", "pri_act_coef", "sec_act_coef", "sec_molal", "mnrl_volfrac",
                            "mnrl_rate", "status", "newton_its", "num_substeps"))
         src = {k: pristine[k].cpu().numpy() if k in pristine else host.a[k] for k in pin}
-        horder = order.cpu().numpy()
         times = []
         for k in range(args.warmup + args.steps):
             for f in pin:
                 np.copyto(hs.a[f], src[f])
             t = time.perf_counter()
-            eng.rstep_host(hs, dt, order=horder)
+            eng.rstep_host(hs, dt)
             el = time.perf_counter() - t
             if k >= args.warmup:
                 times.append(el)
@@ -1090,7 +1092,7 @@ def main():
                 "config": c2_config(cfg, ncells, dt, state_bytes),
                 "launch": {"kernel": "batched persistent (PF_KERNEL_BATCHED)", "config": eng.launch_config(),
                            "autotune": tuned,
-                           "cell_order": "descending Newton count of the previous (untimed) step"},
+                           "cell_order": "cell index (natural)"},
                 "kernel_ms": kern_avg, "newton_its_per_cell": its_mean,
                 "max_newton_its": stats["max_newton_iterations"], "failed_cells": stats["failed_cells"],
                 "newton_its_histogram": hist,
@@ -1105,8 +1107,9 @@ def main():
                                "failed_cells": stats1["failed_cells"],
                                "newton_its_histogram": hist1},
                 "plain_gpu": {"value": plain_value, "kernel_ms": float(np.mean(p_kern))},
-                "natural_order": {"value": ncells * len(nat_kern) / (nat_total * 1e-3),
-                                  "kernel_ms": float(np.mean(nat_kern))},
+                "cost_order": {"what": "the same step, its queue in descending Newton count of the first step",
+                               "value": ncells * len(ord_kern) / (ord_total * 1e-3),
+                               "kernel_ms": float(np.mean(ord_kern))},
                 "speedup_vs_plain_gpu": value / plain_value,
                 "adjoint": adjoint, "girt_assembly": girt, "constraint_equilibration": constraint,
                 "osrt_transport": transport, "heterogeneous": hetero,

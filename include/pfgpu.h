@@ -370,6 +370,10 @@ int32_t pf_update_activity_coefs(PfNetwork* net, const PfCellState* state,
  * the device, runs pf_rstep (kernel form as given), copies results back.
  * Host arrays use the same SoA layout.  This is the entry point a Fortran
  * caller binds through iso_c_binding (contiguous temporaries via c_loc).
+ * Large states go in chunks whose copies in and out overlap the compute;
+ * host_state->cell_order (host memory) is restricted to each chunk, and an
+ * order that is not a permutation of 0..ncells-1 returns PF_ERR_INVALID
+ * with the caller's arrays untouched.
  */
 int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
                       double dt, int32_t kernel, PfStepStats* stats);

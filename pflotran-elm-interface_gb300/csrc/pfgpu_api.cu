@@ -1035,32 +1035,77 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     return to_dev ? cudaMemcpy2DAsync(dp, w, hp, (size_t)N * es, w, f[k].rows, cudaMemcpyHostToDevice, st)
                   : cudaMemcpy2DAsync(hp, (size_t)N * es, dp, w, w, f[k].rows, cudaMemcpyDeviceToHost, st);
   };
-  for (int c = 0; c < K && e == cudaSuccess; ++c) {
+  const int kord = 17;  // the order's slot in f[]
+  auto copy_in = [&](int c) {
     for (int k = 0; k < nf && e == cudaSuccess; ++k)
       if (f[k].host && f[k].in && f[k].rows > 0) e = copy(c, k, true, net->s_in);
-    if (e == cudaSuccess) e = cudaEventRecord(net->ev_in[c], net->s_in);
-  }
+  };
+  // the chunk's local order to the device, on the input stream (a copy on
+  // another stream can still queue behind the inputs on the same copy engine)
+  auto copy_order = [&](int c) {
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dev_field(c, kord), net->h_order + c * chunk, (size_t)cells_of(c) * sizeof(int64_t),
+                          cudaMemcpyHostToDevice, net->s_in);
+  };
+  // chunk-local orders.  Chunk 0 (cells [0, n0)) gets its order in a first
+  // pass while its inputs are in flight, and the copy of that order follows
+  // them, ahead of the other chunks' inputs: chunk 0's compute waits for it.
+  // Its local order is the order's entries below n0 in sequence, written
+  // branch-free (a slot past the end takes the writes once chunk 0 is
+  // complete).  The other chunks' orders, and the check that the order is a
+  // permutation (a bitmap of the cells seen), come after chunk 0's compute is
+  // enqueued, while it runs, and before any result is copied back, so that a
+  // refused order leaves the caller's buffers untouched.
+  const int64_t n0 = cells_of(0);
+  copy_in(0);
   if (e != cudaSuccess) return fail(PF_ERR_CUDA);
-  // chunk-local orders, built while the inputs are in flight
-  const int kord = 17;
+  // h_order: the chunk-local orders, the slot past them, then the bitmap
+  const size_t order_words = (size_t)N + 1 + (size_t)(N + 63) / 64;
   if (h->cell_order) {
-    if (net->h_order_cap < (size_t)N) {
+    if (net->h_order_cap < order_words) {
       if (net->h_order) cudaFreeHost(net->h_order);
       net->h_order = nullptr;
       net->h_order_cap = 0;
-      if (cudaMallocHost(&net->h_order, (size_t)N * sizeof(int64_t)) != cudaSuccess) return fail(PF_ERR_CUDA);
-      net->h_order_cap = (size_t)N;
+      if (cudaMallocHost(&net->h_order, order_words * sizeof(int64_t)) != cudaSuccess) return fail(PF_ERR_CUDA);
+      net->h_order_cap = order_words;
     }
-    int64_t pos[16];
-    for (int c = 0; c < K; ++c) pos[c] = c * chunk;
+    int64_t* ho = net->h_order;
+    int64_t p = 0;
     for (int64_t i = 0; i < N; ++i) {
       const int64_t o = h->cell_order[i];
       if (o < 0 || o >= N) return fail(PF_ERR_INVALID);
+      ho[p < n0 ? p : N] = o;
+      p += o < n0;
+    }
+    if (p != n0) return fail(PF_ERR_INVALID);  // not a permutation
+    copy_order(0);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(net->ev_in[0], net->s_in);
+  for (int c = 1; c < K && e == cudaSuccess; ++c) {
+    copy_in(c);
+    // with an order, chunk c's inputs are complete once its order is copied
+    if (e == cudaSuccess && !h->cell_order) e = cudaEventRecord(net->ev_in[c], net->s_in);
+  }
+  if (e != cudaSuccess) return fail(PF_ERR_CUDA);
+  // the rest of the chunks' orders (entries in range: checked above) and
+  // the permutation check
+  auto remap_rest = [&]() {
+    uint64_t* seen = (uint64_t*)(net->h_order + N + 1);
+    std::memset(seen, 0, (size_t)(N + 63) / 64 * sizeof(uint64_t));
+    int64_t pos[16];
+    for (int c = 1; c < K; ++c) pos[c] = c * chunk;
+    for (int64_t i = 0; i < N; ++i) {
+      const int64_t o = h->cell_order[i];
+      const uint64_t bit = 1ull << (o & 63);
+      if (seen[o >> 6] & bit) return false;  // a cell twice
+      seen[o >> 6] |= bit;
+      if (o < n0) continue;  // chunk 0's, placed in the first pass
       const int c = (int)(o / chunk);
-      if (pos[c] >= c * chunk + cells_of(c)) return fail(PF_ERR_INVALID);  // not a permutation
+      if (pos[c] >= c * chunk + cells_of(c)) return false;
       net->h_order[pos[c]++] = o - c * chunk;
     }
-  }
+    return true;
+  };
   for (int c = 0; c < K && e == cudaSuccess; ++c) {
     const int64_t nc = cells_of(c);
     PfCellState d = *h;
@@ -1081,13 +1126,18 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     d.srfcplx_conc = (double*)dev_field(c, 22);
     cudaStream_t sc = net->s_comp;
     e = cudaStreamWaitEvent(sc, net->ev_in[c], 0);
-    if (e == cudaSuccess && h->cell_order)
-      e = cudaMemcpyAsync(dev_field(c, kord), net->h_order + c * chunk, (size_t)nc * sizeof(int64_t),
-                          cudaMemcpyHostToDevice, sc);
     if (e != cudaSuccess) break;
     rc = enqueue_rstep(net, &d, dt, kernel, net->d_ccounters + 8 * c,
                        net->d_scratch ? net->d_scratch + scratch_chunk * c : nullptr, sc);
     if (rc) return fail(rc);
+    if (c == 0 && h->cell_order) {
+      if (!remap_rest()) return fail(PF_ERR_INVALID);
+      for (int q = 1; q < K && e == cudaSuccess; ++q) {
+        copy_order(q);
+        if (e == cudaSuccess) e = cudaEventRecord(net->ev_in[q], net->s_in);
+      }
+      if (e != cudaSuccess) break;
+    }
     e = cudaEventRecord(net->ev_comp[c], sc);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(net->s_out, net->ev_comp[c], 0);
     for (int k = 0; k < nf && e == cudaSuccess; ++k)

@@ -2,8 +2,9 @@
 
 The throughput figures of bench.py come from two workloads: the 12/40/6
 network over 1,000,000 cells (network seed 12, cells seed 2026, dt = 1 day),
-whose timed step is the second operator-split step (the first step's Newton
-counts order the second step's work queue), and the eight heterogeneous
+whose timed step is the second operator-split step (its work queue in cell
+order; the first step's Newton order is measured beside it and gives the
+same results), and the eight heterogeneous
 networks (ncomp 4 ... 24, network seeds 3000 + ncomp, per-cell dt
 log-uniform in [1 h, 30 d]).  These tests build those states exactly as
 bench.py does (bench.build_state, bench.build_c3: the same generator calls,
@@ -86,13 +87,19 @@ def test_c2_bench_steps(oracle, c2, lanes):
         fe, _, _ = _oracle_parity(oracle, net, s0, got1, fail, 86400.0, "bench-c2/step1-failed/lanes%d" % lanes)
         assert fe["failed_ref"] >= fe["failed_gpu"] - 2 * fe["oracle_self_flips"] - 2, fe
     assert stats1["failed_cells"] == fail.size
-    # second step: from the GPU's own state after the first, cells in the
-    # order of the first step's Newton counts (what the bench times)
+    # second step: from the GPU's own state after the first, the queue in
+    # cell order (what the bench times); the first step's Newton order gives
+    # the same bits
     order = torch.argsort(dev.a["newton_its"].to(torch.int64), descending=True)
     s1 = got1
     dev2 = s1.to("cuda")
-    eng.rstep(dev2, 86400.0, order=order)
+    eng.rstep(dev2, 86400.0)
     got2 = dev2.numpy()
+    dev3 = s1.to("cuda")
+    eng.rstep(dev3, 86400.0, order=order)
+    got3 = dev3.numpy()
+    for k in ("total", "pri_molal", "sec_molal", "mnrl_rate", "mnrl_volfrac", "newton_its", "status"):
+        np.testing.assert_array_equal(got3.a[k], got2.a[k], err_msg=k)
     idx2, _ = _sample(got2, 20000, seed=2)
     entry2, _, _ = _oracle_parity(oracle, net, s1, got2, idx2, 86400.0, "bench-c2/step2/lanes%d" % lanes)
     parity.check(entry2, "c2 step 2", min_compared=int(0.95 * idx2.size))

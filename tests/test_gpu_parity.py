@@ -158,11 +158,23 @@ def test_rstep_host_pipeline_over_chunks_matches_device(oracle, with_order):
         np.testing.assert_array_equal(host.a[k], d.a[k], err_msg=k)
     assert s_host == s_dev
     if with_order:
-        bad = order_host.copy()
-        bad[7] = bad[8]
-        with pytest.raises(abi.PfError) as e:
-            eng.rstep_host(big.copy(), 86400.0, order=bad)
-        assert e.value.code == abi.PF_ERR_INVALID
+        # a cell twice and another missing: across chunks, inside chunk 0,
+        # inside the last chunk; an entry out of range.  Each is refused and
+        # leaves the caller's state as it was.
+        first = np.flatnonzero(order_host < 2 ** 18)[:2]
+        last = np.flatnonzero(order_host >= 2 * 2 ** 18)[:2]
+        cross = np.array([np.flatnonzero(order_host < 2 ** 18)[0], np.flatnonzero(order_host >= 2 ** 18)[0]])
+        for i, j, v in ((cross[0], cross[1], None), (first[0], first[1], None), (last[0], last[1], None),
+                        (5, None, 600000)):
+            bad = order_host.copy()
+            bad[i] = bad[j] if v is None else v
+            before = big.copy()
+            arg = big.copy()
+            with pytest.raises(abi.PfError) as e:
+                eng.rstep_host(arg, 86400.0, order=bad)
+            assert e.value.code == abi.PF_ERR_INVALID
+            for k in ("total", "pri_molal", "status"):
+                np.testing.assert_array_equal(arg.a[k], before.a[k], err_msg=k)
 
 
 def test_cell_order_does_not_change_results(oracle):
