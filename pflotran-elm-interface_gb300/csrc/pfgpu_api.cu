@@ -970,15 +970,38 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
       {h->srfcplx_free_site, net->dev.nsrx, d8, true, true}, {h->srfcplx_conc, net->dev.nsrc, d8, false, true},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
-  // chunks of about 2^18 cells (at most 16); of 1, 2 and 4 chunks at 10^6
-  // cells, 4 hid the most copy time behind the compute
+  // The chunk plan: cells [0, N) in chunks starting on whole 64-cell groups
+  // (aligned slices); up to 2^18 cells one chunk, else three: N/10 cells,
+  // the rest, N/10 cells.  Nothing hides the first chunk's copy in or the
+  // last one's copy out, and each launch costs about half a millisecond of
+  // ramp-up and tail (the persistent kernel's last cells); at the bench's
+  // chemistry a chunk's copies take about an eighth of its compute, so the
+  // first chunk's compute covers the middle one's copy in and the last one's
+  // covers its copy out.  Measured at 10^6 cells, device-resident: one launch
+  // 43.4 ms, these three 44.7 ms, four equal chunks 45.4 ms, six (N/32 at
+  // either end) 47.9 ms.
   const int64_t target = 262144;
-  const int K = (int)std::min<int64_t>(16, (N + target - 1) / target);
-  const int64_t chunk = ((N + K - 1) / K + 63) / 64 * 64;  // whole 64-cell groups: aligned slices
-  size_t per_chunk = 0;
-  for (int k = 0; k < nf; ++k)
-    if (f[k].host) per_chunk += pad16((size_t)f[k].rows * chunk * f[k].esize);
-  const size_t need = per_chunk * K;
+  auto r64 = [](int64_t x) { return (x + 63) / 64 * 64; };
+  int64_t cstart[4];
+  int K = 1;
+  cstart[0] = 0;
+  if (N > target) {
+    const int64_t edge = r64((N + 9) / 10);
+    cstart[K++] = edge;
+    cstart[K++] = (N - edge) / 64 * 64;  // the last chunk takes the ragged end
+  }
+  cstart[K] = N;
+  auto cells_of = [&](int c) { return cstart[c + 1] - cstart[c]; };
+  auto chunk_bytes = [&](int64_t nc) {
+    size_t b = 0;
+    for (int k = 0; k < nf; ++k)
+      if (f[k].host) b += pad16((size_t)f[k].rows * nc * f[k].esize);
+    return b;
+  };
+  size_t arena_off[4];
+  arena_off[0] = 0;
+  for (int c = 0; c < K; ++c) arena_off[c + 1] = arena_off[c] + chunk_bytes(cells_of(c));
+  const size_t need = arena_off[K];
   if (need > net->arena_bytes) {
     if (net->d_arena) cudaFree(net->d_arena);
     net->d_arena = nullptr;
@@ -1000,22 +1023,20 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     if (e != cudaSuccess) return PF_ERR_CUDA;
   }
   if (kernel == PF_KERNEL_BATCHED) {
-    rc = ensure_scratch(net, chunk * K);
+    rc = ensure_scratch(net, N);
     if (rc) return rc;
   }
-  const size_t scratch_chunk = batched_scratch_doubles(net->dev, chunk);
   // the step's device buffers may still be in use by work on the legacy stream
   e = cudaEventRecord(net->ev_start, 0);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(net->s_in, net->ev_start, 0);
   if (e == cudaSuccess) e = cudaStreamWaitEvent(net->s_comp, net->ev_start, 0);
   if (e != cudaSuccess) return PF_ERR_CUDA;
-  auto cells_of = [&](int c) { return std::min(chunk, N - c * chunk); };
   // chunk c's block of field k (nullptr for a field the caller did not pass)
   auto dev_field = [&](int c, int k) -> char* {
     if (!f[k].host) return nullptr;
-    size_t off = per_chunk * c;
+    size_t off = arena_off[c];
     for (int q = 0; q < k; ++q)
-      if (f[q].host) off += pad16((size_t)f[q].rows * chunk * f[q].esize);
+      if (f[q].host) off += pad16((size_t)f[q].rows * cells_of(c) * f[q].esize);
     return (char*)net->d_arena + off;
   };
   // an error after copies were enqueued: let them finish before returning,
@@ -1030,7 +1051,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
   auto copy = [&](int c, int k, bool to_dev, cudaStream_t st) {
     const int64_t nc = cells_of(c);
     const size_t es = f[k].esize, w = (size_t)nc * es;
-    char* hp = (char*)f[k].host + (size_t)c * chunk * es;
+    char* hp = (char*)f[k].host + (size_t)cstart[c] * es;
     char* dp = dev_field(c, k);
     return to_dev ? cudaMemcpy2DAsync(dp, w, hp, (size_t)N * es, w, f[k].rows, cudaMemcpyHostToDevice, st)
                   : cudaMemcpy2DAsync(hp, (size_t)N * es, dp, w, w, f[k].rows, cudaMemcpyDeviceToHost, st);
@@ -1044,7 +1065,7 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
   // another stream can still queue behind the inputs on the same copy engine)
   auto copy_order = [&](int c) {
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(dev_field(c, kord), net->h_order + c * chunk, (size_t)cells_of(c) * sizeof(int64_t),
+      e = cudaMemcpyAsync(dev_field(c, kord), net->h_order + cstart[c], (size_t)cells_of(c) * sizeof(int64_t),
                           cudaMemcpyHostToDevice, net->s_in);
   };
   // chunk-local orders.  Chunk 0 (cells [0, n0)) gets its order in a first
@@ -1092,17 +1113,18 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
   auto remap_rest = [&]() {
     uint64_t* seen = (uint64_t*)(net->h_order + N + 1);
     std::memset(seen, 0, (size_t)(N + 63) / 64 * sizeof(uint64_t));
-    int64_t pos[16];
-    for (int c = 1; c < K; ++c) pos[c] = c * chunk;
+    int64_t pos[4];
+    for (int c = 1; c < K; ++c) pos[c] = cstart[c];
     for (int64_t i = 0; i < N; ++i) {
       const int64_t o = h->cell_order[i];
       const uint64_t bit = 1ull << (o & 63);
       if (seen[o >> 6] & bit) return false;  // a cell twice
       seen[o >> 6] |= bit;
       if (o < n0) continue;  // chunk 0's, placed in the first pass
-      const int c = (int)(o / chunk);
-      if (pos[c] >= c * chunk + cells_of(c)) return false;
-      net->h_order[pos[c]++] = o - c * chunk;
+      int c = 1;
+      while (o >= cstart[c + 1]) ++c;  // o < N = cstart[K]
+      if (pos[c] >= cstart[c + 1]) return false;
+      net->h_order[pos[c]++] = o - cstart[c];
     }
     return true;
   };
@@ -1128,7 +1150,8 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
     e = cudaStreamWaitEvent(sc, net->ev_in[c], 0);
     if (e != cudaSuccess) break;
     rc = enqueue_rstep(net, &d, dt, kernel, net->d_ccounters + 8 * c,
-                       net->d_scratch ? net->d_scratch + scratch_chunk * c : nullptr, sc);
+                       net->d_scratch ? net->d_scratch + batched_scratch_doubles(net->dev, cstart[c]) : nullptr,
+                       sc);
     if (rc) return fail(rc);
     if (c == 0 && h->cell_order) {
       if (!remap_rest()) return fail(PF_ERR_INVALID);

@@ -133,11 +133,12 @@ def test_rstep_host_path_matches_device(oracle):
 
 @pytest.mark.parametrize("with_order", [False, True], ids=["natural", "permuted"])
 def test_rstep_host_pipeline_over_chunks_matches_device(oracle, with_order):
-    """pf_rstep_host cuts a large state into chunks of 2^18 cells (copy-in,
-    compute and copy-out overlapped on three streams, the work-queue order
-    restricted to each chunk): 600,000 cells (three chunks, the last one
-    short) give the device path's results bit for bit, with the same
-    statistics; an order that is not a permutation is refused."""
+    """pf_rstep_host cuts a large state into chunks (copy-in, compute and
+    copy-out overlapped on three streams): a tenth of the cells, the rest,
+    a tenth (the last chunk takes the ragged end), the order restricted to
+    each chunk.  600,000 cells give the device path's results
+    bit for bit, with the same statistics; an order that is not a
+    permutation is refused."""
     net, st0 = cases.case(oracle, "random12")
     reps = -(-600000 // st0.ncells)
     big = CellState(net, {k: (np.tile(v, reps)[..., :600000] if v.ndim == 1 else np.tile(v, (1, reps))[:, :600000])
@@ -161,9 +162,11 @@ def test_rstep_host_pipeline_over_chunks_matches_device(oracle, with_order):
         # a cell twice and another missing: across chunks, inside chunk 0,
         # inside the last chunk; an entry out of range.  Each is refused and
         # leaves the caller's state as it was.
-        first = np.flatnonzero(order_host < 2 ** 18)[:2]
-        last = np.flatnonzero(order_host >= 2 * 2 ** 18)[:2]
-        cross = np.array([np.flatnonzero(order_host < 2 ** 18)[0], np.flatnonzero(order_host >= 2 ** 18)[0]])
+        edge = ((600000 + 9) // 10 + 63) // 64 * 64
+        tail = (600000 - edge) // 64 * 64
+        first = np.flatnonzero(order_host < edge)[:2]
+        last = np.flatnonzero(order_host >= tail)[:2]
+        cross = np.array([np.flatnonzero(order_host < edge)[0], np.flatnonzero(order_host >= edge)[0]])
         for i, j, v in ((cross[0], cross[1], None), (first[0], first[1], None), (last[0], last[1], None),
                         (5, None, 600000)):
             bad = order_host.copy()
