@@ -388,9 +388,10 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* host_state,
  * lives in a fixed 32 MiB device array inside the library (held on every
  * device that loads it until exit), and the call allocates nothing.  Limit:
  * (ncomp + nsec + nmnrl) * ncells <= 4,194,304; larger states return
- * PF_ERR_TOO_LARGE (split them across calls).  The first call on a device
- * resolves the array's device address; make that first call before any
- * stream capture.  All calls share the one array, so calls that overlap on
+ * PF_ERR_TOO_LARGE (split them across calls).  Each call outside a stream
+ * capture resolves the array's device address (after a cudaDeviceReset it
+ * may move); a call inside a capture uses the last one, so make one call on
+ * the device before capturing.  All calls share the one array, so calls that overlap on
  * the GPU (other streams, other threads) race; serialise them.  The launch
  * configuration and option checks are pf_rstep's.  Before the launch every
  * status entry is set to PF_CELL_NOT_RUN; the kernel overwrites it for each

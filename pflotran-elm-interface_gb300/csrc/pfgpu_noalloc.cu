@@ -25,18 +25,23 @@ std::mutex g_mutex;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 // Device address of the static array on the current device.  The host-side
-// symbol is only a stand-in; the address must come from the runtime, once per
-// device, with that device current (the first call on a device does this; it
-// must therefore happen before any stream capture that includes the call).
-int scratch_for_current_device(double** out) {
+// symbol is only a stand-in; the address must come from the runtime with that
+// device current.  It is looked up afresh on every call outside a stream
+// capture (a cudaDeviceReset reloads the module, and the array may move), and
+// the last address is used inside one (so a captured call needs one earlier
+// call on the device outside the capture).
+int scratch_for_current_device(cudaStream_t stream, double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PF_ERR_CUDA;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return PF_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, pf_noalloc_scratch) != cudaSuccess || !p) return PF_ERR_CUDA;
     g_scratch_ptr[dev] = static_cast<double*>(p);
   }
+  if (!g_scratch_ptr[dev]) return PF_ERR_CUDA;
   *out = g_scratch_ptr[dev];
   return PF_OK;
 }
@@ -66,10 +71,10 @@ extern "C" int32_t pf_rstep_noalloc(PfNetwork* net, const PfCellState* state, do
     return PF_OK;
   }
   if (batched_scratch_doubles(dev, state->ncells) > (size_t)PF_NOALLOC_SCRATCH_DOUBLES) return PF_ERR_TOO_LARGE;
-  double* scratch = nullptr;
-  rc = scratch_for_current_device(&scratch);
-  if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  double* scratch = nullptr;
+  rc = scratch_for_current_device(s, &scratch);
+  if (rc) return rc;
   // the work-queue counter and reduction slots must start at zero; the
   // scratch needs no clearing (the setup pre-pass writes every value it reads
   // before the step kernel reads it)

@@ -92,3 +92,26 @@ def test_noalloc_rejects_oversized_state():
     rc = eng.lib.pf_rstep_noalloc(eng.handle, C.byref(s), 3600.0,
                                   C.c_void_p(torch.cuda.current_stream().cuda_stream), None)
     assert rc == abi.PF_ERR_TOO_LARGE
+
+
+def test_noalloc_in_a_cuda_graph():
+    """A call outside any capture resolves the scratch array's address; a call
+    captured into a CUDA graph then uses that address, and the replayed graph
+    gives pf_rstep's results bit for bit."""
+    net = _net(12)
+    eng, base = _state(net, 20000, seed=4242)
+    ref = base.copy()
+    eng.rstep(ref, 86400.0)
+    warm = base.copy()
+    _noalloc(eng, warm, 86400.0)
+    got = base.copy()
+    s = got.struct()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = eng.lib.pf_rstep_noalloc(eng.handle, C.byref(s), 86400.0,
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream), None)
+    assert rc == abi.PF_OK
+    g.replay()
+    torch.cuda.synchronize()
+    for k in FIELDS:
+        assert torch.equal(got.a[k], ref.a[k]), k
