@@ -50,3 +50,17 @@ def test_reference_arm_config_matches_ours():
     a = bench.c2_config(cfg, 1_000_000, 86400.0, 1.12e9)
     b = bench.c2_config(cfg, 1_000_000, 86400.0, 1.12e9)
     assert a == b and set(a) == {"workload", "cells", "dt_s", "step", "l2"}
+
+
+def test_newton_count_histogram_bins():
+    """The bench line's Newton-count histogram: cells per bin [2^k, 2^(k+1)),
+    a bin below 1 and an open last bin, every cell counted once."""
+    import torch
+    sys.path.insert(0, REPO)
+    import bench
+    its = torch.tensor([0, 1, 1, 2, 3, 4, 7, 8, 15, 16, 300, 511, 512, 1000], dtype=torch.int32)
+    h = bench.its_histogram(its)
+    assert h["bins"] == ["<1", "1-1", "2-3", "4-7", "8-15", "16-31", "32-63", "64-127", "128-255", "256-511",
+                         ">=512"]
+    assert h["cells"] == [1, 2, 2, 2, 2, 1, 0, 0, 0, 2, 2]
+    assert sum(h["cells"]) == its.numel()
