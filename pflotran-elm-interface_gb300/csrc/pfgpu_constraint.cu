@@ -94,10 +94,14 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
       if (ctype[j] == 2 || ctype[j] == 5) c[j] = free_conc[j];
     if (net.o.act_coef_update_frequency != PF_ACT_COEF_OFF && act)
       activity_lag<NM>(net, T, c, st, soa, cell, gam, lnaw);
-    // RTotalAqueous
+    // RTotalAqueous; d s_i / d m_j = nu_ij s_i / m_j (the reference forms
+    // exp(lnQK - ln m_j) / gamma_i, an exp per species of every complex:
+    // the same quantity, and the product with 1/m_j rounds within an ulp of it)
+    double inv_c[NM];
     for (int j = 0; j < n; ++j) {
       lnc[j] = log(c[j]);
       lna[j] = lnc[j] + log(gam[j]);
+      inv_c[j] = 1.0 / c[j];
       tot[j] = c[j];
       for (int k = 0; k < n; ++k) J[j * NM + k] = (j == k) ? 1.0 : 0.0;
     }
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
       for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) tot[T.sec_idx(p)] += T.sec_nu(p) * s;
       for (int pj = T.sec_begin(i); pj < T.sec_end(i); ++pj) {
         const int jc = T.sec_idx(pj);
-        const double t = T.sec_nu(pj) * exp(lnQK - lnc[jc]) / g;
+        const double t = T.sec_nu(pj) * s * inv_c[jc];
         for (int pi = T.sec_begin(i); pi < T.sec_end(i); ++pi) J[T.sec_idx(pi) * NM + jc] += T.sec_nu(pi) * t;
       }
     }
