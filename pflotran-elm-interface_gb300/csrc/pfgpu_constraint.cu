@@ -86,6 +86,10 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
     }
     c[j] = free_conc[j];
   }
+  // the complexes' logK at the cell's temperature, once (the same values the
+  // reference recomputes in every RTotal)
+  double logK_sec[PF_MAX_NSEC];
+  for (int i = 0; i < ns; ++i) logK_sec[i] = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
   int its = 0, on_it = 0;
   bool act = use_prev != 0, warned = false;
   int result = -1;
@@ -106,8 +110,7 @@ __global__ void __launch_bounds__(128) equilibrate_kernel(DevNet net, PfCellStat
       for (int k = 0; k < n; ++k) J[j * NM + k] = (j == k) ? 1.0 : 0.0;
     }
     for (int i = 0; i < ns; ++i) {
-      const double logK = tsec ? interp_logK(T.sec_logKcoef(i), temp) : T.sec_logK(i);
-      double lnQK = add_h2o(-logK * LOG_TO_LN, T.sec_h2o(i), lnaw);
+      double lnQK = add_h2o(-logK_sec[i] * LOG_TO_LN, T.sec_h2o(i), lnaw);
       for (int p = T.sec_begin(i); p < T.sec_end(i); ++p) lnQK = lnQK + T.sec_nu(p) * lna[T.sec_idx(p)];
       const double g = st.sec_act_coef[soa.at(i, cell)];
       const double s = exp(lnQK) / g;
