@@ -932,6 +932,37 @@ int32_t pf_equilibrate_constraint(PfNetwork* net, const PfCellState* state, cons
   return pf_equilibrate_constraint_ex(net, state, ctype, nullptr, cconc, use_prev, iterations, stream);
 }
 
+// The host-buffer step's chunk plan: cells [0, N) in chunks starting on
+// whole 64-cell groups (aligned slices); up to 2^18 cells one chunk, else
+// three: N/10 cells, the rest, N/10 cells.  Nothing hides the first chunk's
+// copy in or the last one's copy out, and each launch costs about half a
+// millisecond of ramp-up and tail (the persistent kernel's last cells); at
+// the bench's chemistry a chunk's copies take about an eighth of its
+// compute, so the first chunk's compute covers the middle one's copy in and
+// the last one's covers its copy out.  Measured at 10^6 cells,
+// device-resident: one launch 43.4 ms, these three 44.7 ms, four equal
+// chunks 45.4 ms, six (N/32 at either end) 47.9 ms.  Writes the K + 1
+// boundaries (cstart[0] = 0, cstart[K] = N) and returns K.
+static int host_chunk_plan(int64_t N, int64_t cstart[4]) {
+  const int64_t target = 262144;
+  auto r64 = [](int64_t x) { return (x + 63) / 64 * 64; };
+  int K = 1;
+  cstart[0] = 0;
+  if (N > target) {
+    const int64_t edge = r64((N + 9) / 10);
+    cstart[K++] = edge;
+    cstart[K++] = (N - edge) / 64 * 64;  // the last chunk takes the ragged end
+  }
+  cstart[K] = N;
+  return K;
+}
+
+// The chunk plan for tests of the host logic (no device work).
+int32_t pf_internal_host_chunk_plan(int64_t ncells, int64_t* starts) {
+  if (ncells < 0 || !starts) return -1;
+  return host_chunk_plan(ncells, starts);
+}
+
 // Host-buffer step, pipelined over chunks of cells: chunk c's inputs go in on
 // one stream while earlier chunks compute on a second and finished chunks'
 // results come back on a third.  Each chunk has its own counters and set-up
@@ -970,27 +1001,8 @@ int32_t pf_rstep_host(PfNetwork* net, const PfCellState* h, double dt, int32_t k
       {h->srfcplx_free_site, net->dev.nsrx, d8, true, true}, {h->srfcplx_conc, net->dev.nsrc, d8, false, true},
   };
   const int nf = sizeof(f) / sizeof(f[0]);
-  // The chunk plan: cells [0, N) in chunks starting on whole 64-cell groups
-  // (aligned slices); up to 2^18 cells one chunk, else three: N/10 cells,
-  // the rest, N/10 cells.  Nothing hides the first chunk's copy in or the
-  // last one's copy out, and each launch costs about half a millisecond of
-  // ramp-up and tail (the persistent kernel's last cells); at the bench's
-  // chemistry a chunk's copies take about an eighth of its compute, so the
-  // first chunk's compute covers the middle one's copy in and the last one's
-  // covers its copy out.  Measured at 10^6 cells, device-resident: one launch
-  // 43.4 ms, these three 44.7 ms, four equal chunks 45.4 ms, six (N/32 at
-  // either end) 47.9 ms.
-  const int64_t target = 262144;
-  auto r64 = [](int64_t x) { return (x + 63) / 64 * 64; };
   int64_t cstart[4];
-  int K = 1;
-  cstart[0] = 0;
-  if (N > target) {
-    const int64_t edge = r64((N + 9) / 10);
-    cstart[K++] = edge;
-    cstart[K++] = (N - edge) / 64 * 64;  // the last chunk takes the ragged end
-  }
-  cstart[K] = N;
+  const int K = host_chunk_plan(N, cstart);
   auto cells_of = [&](int c) { return cstart[c + 1] - cstart[c]; };
   auto chunk_bytes = [&](int64_t nc) {
     size_t b = 0;
