@@ -32,12 +32,16 @@ def test_auxvars_with_water_activity(oracle, algo):
         np.testing.assert_allclose(got.a[k][..., ok], ref.a[k][..., ok], rtol=1e-12, atol=0, err_msg=k)
 
 
-@pytest.mark.parametrize("kernel,freq", [("batched", abi.PF_ACT_COEF_TIMESTEP), ("group4", abi.PF_ACT_COEF_TIMESTEP),
-                                         ("plain", abi.PF_ACT_COEF_TIMESTEP),
-                                         ("plain", abi.PF_ACT_COEF_NEWTON_ITER)])
-def test_rstep_with_water_activity(oracle, kernel, freq):
+@pytest.mark.parametrize("kernel,freq,algo", [("batched", abi.PF_ACT_COEF_TIMESTEP, abi.PF_ACT_COEF_ALGO_LAG),
+                                              ("group4", abi.PF_ACT_COEF_TIMESTEP, abi.PF_ACT_COEF_ALGO_LAG),
+                                              ("plain", abi.PF_ACT_COEF_TIMESTEP, abi.PF_ACT_COEF_ALGO_LAG),
+                                              ("plain", abi.PF_ACT_COEF_NEWTON_ITER, abi.PF_ACT_COEF_ALGO_LAG),
+                                              ("plain", abi.PF_ACT_COEF_NEWTON_ITER, abi.PF_ACT_COEF_ALGO_NEWTON)],
+                         ids=["batched", "group4", "plain", "plain-lag-each-iteration",
+                              "plain-newton-each-iteration"])
+def test_rstep_with_water_activity(oracle, kernel, freq, algo):
     from pfgpu.engine import ReactionEngine
-    net, st = cases.water_case(oracle, ncells=800, act_coef_update_frequency=freq)
+    net, st = cases.water_case(oracle, ncells=800, act_coef_update_frequency=freq, act_coef_update_algorithm=algo)
     ref = st.copy()
     assert oracle.rstep(net, ref, 3600.0, nthreads=8) == 0
     perts = []
@@ -52,7 +56,7 @@ def test_rstep_with_water_activity(oracle, kernel, freq):
     dev = st.to("cuda")
     eng.rstep(dev, 3600.0, kernel=abi.PF_KERNEL_PLAIN if kernel == "plain" else abi.PF_KERNEL_BATCHED)
     got = dev.numpy()
-    label = "water/%s/%d" % (kernel, freq)
+    label = "water/%s/%d%s" % (kernel, freq, "/newton" if algo == abi.PF_ACT_COEF_ALGO_NEWTON else "")
     entry, ok = parity.compare(net, ref, got, 3600.0, label, perts)
     parity.check(entry, label, min_compared=int(0.9 * st.ncells))
     if freq == abi.PF_ACT_COEF_NEWTON_ITER:
