@@ -44,6 +44,12 @@ class OperatorSplitLoop:
         (ReactionEngine, CellState, TransportStage).
         dt: uniform step [s]; ignored by the reaction step of states that
         carry a per-cell dt; a member with transport needs dt > 0.
+        cost_order: each step's work queue takes the cells in descending
+        Newton count of the previous step (stiffest first).  It pays where
+        the counts have a long tail (a heterogeneous mix with counts in the
+        hundreds: 22.2 s against 25.7 s for 50 steps of eight networks);
+        where every cell takes a few iterations, cell order is about 2 %
+        faster (neighbouring cells share memory sectors), so pass False.
         concurrent: run each member's step on its own stream (forked from
         and joined back into the calling stream every step), so that one
         network's queue tail overlaps the next network's work.
